@@ -1,0 +1,275 @@
+"""Python access to the CPU checker.
+
+TEST INFRASTRUCTURE ONLY.  Imported by tests/, __graft_entry__.smoke() and
+bench.py's CPU-baseline leg; never by the product package.
+
+* ``Oracle``  -- ctypes binding of this project's C restatement
+  (hsr_oracle.c, built by ``make`` into oracle/_build/).
+* ``run_reference`` -- runs the reference's own force tree (oracle/_ref/rcb_ref,
+  built by ``make ref`` from the reference sources) in a subprocess with the
+  unlimited stack it needs.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import json
+import os
+import resource
+import struct
+import subprocess
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB = os.path.join(HERE, "_build", "libhsr_oracle.so")
+REF_EXE = os.path.join(HERE, "_ref", "rcb_ref")
+
+LAW_POLY6 = 0
+LAW_POLY5_STEP16 = 1
+ERRORS = {1: "bad argument", 2: "interaction list reached VMAX", 3: "out of memory"}
+
+
+def build(ref: bool = False) -> None:
+    """Compiles the restatement (and the reference build when asked and the
+    reference sources are present)."""
+    targets = ["all"] + (["ref"] if ref else [])
+    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+
+
+class OraParams(C.Structure):
+    _fields_ = [("min", C.c_float * 3), ("max", C.c_float * 3),
+                ("min_force", C.c_float * 3), ("max_force", C.c_float * 3),
+                ("avg_mass", C.c_float), ("fsrrmax", C.c_float), ("rsm", C.c_float),
+                ("open_angle", C.c_float), ("nd", C.c_int64), ("ds", C.c_int64),
+                ("tmin", C.c_int64), ("fcoeff", C.c_float), ("ppc", C.c_float),
+                ("tdpts", C.c_int32), ("law", C.c_int32), ("vmax", C.c_int32),
+                ("nthreads", C.c_int32)]
+
+
+class OraStats(C.Structure):
+    _fields_ = [("nodes", C.c_int64), ("leaves", C.c_int64), ("empty_leaves", C.c_int64),
+                ("max_ppn", C.c_int64), ("processed_leaves", C.c_int64),
+                ("list_entries", C.c_int64), ("pairs", C.c_int64), ("t_build", C.c_double),
+                ("t_walk", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def _ptr(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def params_struct(kp, nthreads: int = 0, vmax: int = 0) -> OraParams:
+    P = OraParams()
+    for k in ("min", "max", "min_force", "max_force"):
+        getattr(P, k)[:] = [float(v) for v in getattr(kp, k)]
+    P.avg_mass, P.fsrrmax, P.rsm, P.open_angle = kp.avg_mass, kp.fsrrmax, kp.rsm, kp.open_angle
+    P.nd, P.ds, P.tmin = kp.nd, kp.ds, kp.tmin
+    P.fcoeff, P.ppc, P.tdpts, P.law = kp.fcoeff, kp.ppc, kp.tdpts, kp.law
+    P.vmax, P.nthreads = vmax, nthreads
+    return P
+
+
+class OracleResult:
+    """Tree, lists and statistics of one restatement run."""
+
+    def __init__(self, lib, handle, particles):
+        self._lib, self._h, self._p = lib, handle, particles
+        st = OraStats()
+        lib.ora_result_stats(handle, C.byref(st))
+        self.stats = st.as_dict()
+
+    def __del__(self):
+        if getattr(self, "_h", None):
+            self._lib.ora_result_free(self._h)
+            self._h = None
+
+    def leaves(self):
+        nl = self._lib.ora_result_nleaves(self._h)
+        off = np.zeros(nl, np.int64)
+        cnt = np.zeros(nl, np.int64)
+        ptr = np.zeros(nl + 1, np.int64)
+        self._lib.ora_result_leaves(self._h, _ptr(off, C.c_int64), _ptr(cnt, C.c_int64),
+                                    _ptr(ptr, C.c_int64))
+        return off, cnt, ptr
+
+    def entries(self):
+        ne = self._lib.ora_result_nentries(self._h)
+        e = np.zeros((4, ne), np.float32)
+        self._lib.ora_result_entries(self._h, *[_ptr(e[i], C.c_float) for i in range(4)])
+        return e
+
+    def nodes(self, tdpts: int):
+        nn = self._lib.ora_result_nnodes(self._h)
+        cnt, off, cl, cr = (np.zeros(nn, np.int64) for _ in range(4))
+        tdr = np.zeros(nn, np.float32)
+        bbox = np.zeros((nn, 9), np.float32)
+        ppm = np.zeros((nn, tdpts), np.float32)
+        self._lib.ora_result_nodes(self._h, _ptr(cnt, C.c_int64), _ptr(off, C.c_int64),
+                                   _ptr(cl, C.c_int64), _ptr(cr, C.c_int64),
+                                   _ptr(tdr, C.c_float), _ptr(bbox, C.c_float),
+                                   _ptr(ppm, C.c_float))
+        return dict(count=cnt, offset=off, cl=cl, cr=cr, tdr=tdr, bbox=bbox, ppm=ppm)
+
+    def acc_fp64(self):
+        n = self._p.n
+        a = [np.full(n, np.nan) for _ in range(3)]
+        self._lib.ora_result_acc_fp64(self._h, *[_ptr(v, C.c_double) for v in a])
+        return np.stack(a, axis=1)
+
+
+class Oracle:
+    def __init__(self, path: str = LIB):
+        if not os.path.exists(path):
+            build()
+        lib = C.CDLL(path)
+        self.lib = lib
+        i64, f32, f64 = C.c_int64, C.c_float, C.c_double
+        pf, pd, pi64, pu16 = (C.POINTER(C.c_float), C.POINTER(C.c_double),
+                              C.POINTER(C.c_int64), C.POINTER(C.c_uint16))
+        lib.ora_rcb_run.restype = C.c_void_p
+        lib.ora_rcb_run.argtypes = [C.POINTER(OraParams), i64] + [pf] * 8 + [pi64, pu16, C.c_int,
+                                                                             C.c_int, C.POINTER(C.c_int)]
+        lib.ora_result_stats.argtypes = [C.c_void_p, C.POINTER(OraStats)]
+        lib.ora_result_nleaves.restype = i64
+        lib.ora_result_nleaves.argtypes = [C.c_void_p]
+        lib.ora_result_nentries.restype = i64
+        lib.ora_result_nentries.argtypes = [C.c_void_p]
+        lib.ora_result_leaves.argtypes = [C.c_void_p, pi64, pi64, pi64]
+        lib.ora_result_entries.argtypes = [C.c_void_p, pf, pf, pf, pf]
+        lib.ora_result_nnodes.restype = i64
+        lib.ora_result_nnodes.argtypes = [C.c_void_p]
+        lib.ora_result_nodes.argtypes = [C.c_void_p, pi64, pi64, pi64, pi64, pf, pf, pf]
+        lib.ora_result_acc_fp64.argtypes = [C.c_void_p, pd, pd, pd]
+        lib.ora_result_free.argtypes = [C.c_void_p]
+        lib.ora_law_f32.restype = f32
+        lib.ora_law_f32.argtypes = [C.c_int, f32, f32]
+        lib.ora_law_f64.restype = f64
+        lib.ora_law_f64.argtypes = [C.c_int, f64, f64]
+        lib.ora_law_dg_f64.restype = f64
+        lib.ora_law_dg_f64.argtypes = [C.c_int, f64, f64]
+        lib.ora_direct_fp64.argtypes = [i64, pf, pf, pf, pf, C.c_int, f32, f32, i64, pi64, pd, pd, pd]
+        lib.ora_vjp_fp64.argtypes = [i64, pf, pf, pf, pf, C.c_int, f32, f32, f64, i64, pi64, pi64,
+                                     pi64, pi64, pd, pd]
+        lib.ora_map1.argtypes = [i64, pf, pf, pf, pf, pf, pf, f32, f32, f32, f32]
+        lib.ora_resort.restype = i64
+        lib.ora_resort.argtypes = [i64, C.POINTER(C.c_int), pf, pf, pf, pf, pf, pf, pf, pf, pi64, pu16]
+
+    # -- the RCBForceTree constructor -------------------------------------
+    def rcb_run(self, p, kp, keep_lists: bool = False, do_kick: bool = True,
+                nthreads: int = 0, vmax: int = 0) -> OracleResult:
+        """Runs build + walk (+ kick) on `p` in place."""
+        P = params_struct(kp, nthreads, vmax)
+        err = C.c_int(0)
+        arrs = [_ptr(getattr(p, k), C.c_float) for k in ("x", "y", "z", "vx", "vy", "vz", "mass", "phi")]
+        h = self.lib.ora_rcb_run(C.byref(P), p.n, *arrs, _ptr(p.id, C.c_int64),
+                                 _ptr(p.mask, C.c_uint16), int(keep_lists), int(do_kick),
+                                 C.byref(err))
+        if not h:
+            raise RuntimeError(f"oracle failed: {ERRORS.get(err.value, err.value)}")
+        return OracleResult(self.lib, h, p)
+
+    def law_f32(self, law: int, rsm: float, r2: float) -> float:
+        return self.lib.ora_law_f32(law, rsm, r2)
+
+    def law_f64(self, law: int, rsm: float, r2: float) -> float:
+        return self.lib.ora_law_f64(law, rsm, r2)
+
+    def direct_fp64(self, p, targets, law=LAW_POLY6, rsm=0.1, fsrrmax=3.116326355):
+        t = np.ascontiguousarray(targets, dtype=np.int64)
+        a = [np.zeros(len(t)) for _ in range(3)]
+        self.lib.ora_direct_fp64(p.n, _ptr(p.x, C.c_float), _ptr(p.y, C.c_float),
+                                 _ptr(p.z, C.c_float), _ptr(p.mass, C.c_float), law, rsm,
+                                 fsrrmax, len(t), _ptr(t, C.c_int64),
+                                 *[_ptr(v, C.c_double) for v in a])
+        return np.stack(a, axis=1)
+
+    def vjp_fp64(self, p, c, leaf_offset, leaf_count, list_ptr, list_idx, u,
+                 law=LAW_POLY6, rsm=0.1, fsrrmax=3.116326355):
+        u = np.ascontiguousarray(u, dtype=np.float64)
+        xbar = np.zeros((p.n, 3))
+        lo, lc, lp, li = (np.ascontiguousarray(a, dtype=np.int64)
+                          for a in (leaf_offset, leaf_count, list_ptr, list_idx))
+        self.lib.ora_vjp_fp64(p.n, _ptr(p.x, C.c_float), _ptr(p.y, C.c_float),
+                              _ptr(p.z, C.c_float), _ptr(p.mass, C.c_float), law, rsm, fsrrmax,
+                              c, len(lo), _ptr(lo, C.c_int64), _ptr(lc, C.c_int64),
+                              _ptr(lp, C.c_int64), _ptr(li, C.c_int64),
+                              _ptr(u, C.c_double), _ptr(xbar, C.c_double))
+        return xbar
+
+    def map1(self, p, alpha, pp, tau, adot):
+        self.lib.ora_map1(p.n, *[_ptr(getattr(p, k), C.c_float) for k in ("x", "y", "z", "vx", "vy", "vz")],
+                          alpha, pp, tau, adot)
+
+    def resort(self, p) -> int:
+        ng = (C.c_int * 3)(*p.nglt)
+        return self.lib.ora_resort(p.n, ng, *[_ptr(getattr(p, k), C.c_float) for k in
+                                             ("x", "y", "z", "vx", "vy", "vz", "phi", "mass")],
+                                   _ptr(p.id, C.c_int64), _ptr(p.mask, C.c_uint16))
+
+
+# ---------------------------------------------------------------------------
+# Reference runs (case files for oracle/_ref/rcb_ref)
+# ---------------------------------------------------------------------------
+
+CASE_MAGIC = b"HSRCASE1"
+_PFMT = "<16f3q2f6i"
+
+
+def write_case(path: str, p, kp, nthreads: int = 0, reps: int = 1) -> None:
+    head = struct.pack(_PFMT, *kp.min, *kp.max, *kp.min_force, *kp.max_force, kp.avg_mass,
+                       kp.fsrrmax, kp.rsm, kp.open_angle, kp.nd, kp.ds, kp.tmin, kp.fcoeff,
+                       kp.ppc, kp.tdpts, kp.law, 0, nthreads, reps, 0)
+    with open(path, "wb") as f:
+        f.write(CASE_MAGIC)
+        f.write(struct.pack("<q", p.n))
+        f.write(head)
+        for k in ("x", "y", "z", "vx", "vy", "vz", "mass", "phi"):
+            f.write(np.ascontiguousarray(getattr(p, k), np.float32).tobytes())
+        f.write(np.ascontiguousarray(p.id, np.int64).tobytes())
+        f.write(np.ascontiguousarray(p.mask, np.uint16).tobytes())
+
+
+def read_case_arrays(path: str):
+    with open(path, "rb") as f:
+        buf = f.read()
+    assert buf[:8] == CASE_MAGIC
+    n = struct.unpack_from("<q", buf, 8)[0]
+    off = 16 + struct.calcsize(_PFMT)
+    out = {}
+    for k in ("x", "y", "z", "vx", "vy", "vz", "mass", "phi"):
+        out[k] = np.frombuffer(buf, np.float32, n, off).copy()
+        off += 4 * n
+    out["id"] = np.frombuffer(buf, np.int64, n, off).copy()
+    off += 8 * n
+    out["mask"] = np.frombuffer(buf, np.uint16, n, off).copy()
+    return out
+
+
+def _unlimited_stack():
+    resource.setrlimit(resource.RLIMIT_STACK, (resource.RLIM_INFINITY, resource.RLIM_INFINITY))
+
+
+def reference_available() -> bool:
+    return os.path.exists(REF_EXE)
+
+
+def run_reference(p, kp, nthreads: int = 0, reps: int = 1, timeout: float = 3600.0):
+    """Runs the reference force tree on a copy of `p`; returns (arrays after the
+    last repetition, list of wall times in seconds)."""
+    if not reference_available():
+        raise FileNotFoundError(REF_EXE)
+    with tempfile.TemporaryDirectory() as td:
+        cin, cout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        write_case(cin, p, kp, nthreads, reps)
+        env = dict(os.environ, OMP_STACKSIZE="256M")
+        if nthreads > 0:
+            env["OMP_NUM_THREADS"] = str(nthreads)
+        r = subprocess.run([REF_EXE, cin, cout], env=env, capture_output=True, text=True,
+                           preexec_fn=_unlimited_stack, timeout=timeout)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference run failed ({r.returncode}): {r.stderr[-2000:]}")
+        info = json.loads(r.stdout.strip().splitlines()[-1])
+        return read_case_arrays(cout), info["times"], info["threads"]
