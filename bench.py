@@ -1,0 +1,277 @@
+#!/usr/bin/env python
+"""Pair-interaction throughput of the RCB short-range kick on one GB300.
+
+Workload (one "step"): the short-range kick of a 128^3 Zel'dovich particle set
+at z = 50 (seeded Gaussian field, n = -2 power law, 2 Mpc/h cells) with
+periodic overload ghosts (2.57 M particles), RCB leaves of at most 128
+particles, opening angle 0.1, rsm = 0.1, 6th-order polynomial law, monopole
+pseudo-particles: every (leaf particle, list entry) pair of every leaf inside
+the force box, fused with the velocity kick.
+
+* value      -- pairs/s of the device step with its inputs resident in HBM
+                (pair kernel relaunched on the resident lists, L2 flushed
+                between launches), max over ranks.
+* e2e        -- pairs/s of hsr_rcb_kick through the C ABI with host arrays:
+                tree build, lists, host<->device copies and the kernels.
+* roofline   -- the pair kernel against the FP32 FMA peak measured by the
+                library's FFMA probe on this device (31 algorithmic flops per
+                pair).
+* cpu_baseline -- the CPU restatement of the reference force tree (oracle),
+                timed on this host's cores on a bounded slab of the workload.
+
+`--impl reference` times that CPU path alone as the reference arm.  Under
+torchrun each rank runs an independent replica on its own GPU (the path does
+not shard across GPUs); rank 0 prints one JSON line.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (os.path.join(ROOT, "hacc-coral_gb300"), os.path.join(ROOT, "oracle")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+
+import synth  # noqa: E402
+
+FLOPS_PER_PAIR = 31
+METRIC = "pair interactions/s"
+UNIT = "pairs/s"
+L2_NOTE = "L2 flushed (256 MB write) before every timed pair-kernel launch"
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--ng", type=int, default=128)
+    ap.add_argument("--nd", type=int, default=128)
+    ap.add_argument("--kernel", choices=["auto", "plain", "batched"], default="auto")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-slab", type=float, default=0.25,
+                    help="fraction of the force box (along x) in the CPU sample")
+    return ap.parse_args()
+
+
+def workload(ng: int, nd: int):
+    p = synth.zeldovich_box(ng, z=50.0)
+    kp = synth.kick_params(p, nd=nd)
+    cfg = {"workload": f"zeldovich{ng}_z50_nd{nd}_monopole", "n_side": ng, "n_particles": p.n,
+           "nd": nd, "open_angle": kp.open_angle, "rsm": kp.rsm, "fsrrmax": kp.fsrrmax,
+           "tdpts": kp.tdpts, "law": "poly6", "fcoeff": kp.fcoeff, "l2": L2_NOTE}
+    return p, kp, cfg
+
+
+def dist_init():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(world, x: float) -> float:
+    if world <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms during a timed region."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device: int):
+        self.device = device
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.device), f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except OSError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def __exit__(self, *a):
+        self.out = ""
+        if self.proc:
+            time.sleep(0.3)
+            self.proc.terminate()
+            try:
+                self.out, _ = self.proc.communicate(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+                self.out, _ = self.proc.communicate()
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for line in (self.out or "").strip().splitlines():
+            f = [v.strip() for v in line.split(",")]
+            if len(f) < 8:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[4:8]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(p, kp, slab: float, threads: int):
+    """Reference force tree (CPU restatement) on a slab of the force box."""
+    import oracle
+    oracle.build()
+    O = oracle.Oracle()
+    q = p.copy()
+    ks = synth.KickParams(**{**kp.__dict__})
+    lo, hi = kp.min_force[0], kp.max_force[0]
+    ks.max_force = (lo + slab * (hi - lo), kp.max_force[1], kp.max_force[2])
+    t0 = time.perf_counter()
+    r = O.rcb_run(q, ks, nthreads=threads)
+    dt = time.perf_counter() - t0
+    pairs = r.stats["pairs"]
+    return {"value": pairs / dt, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": (f"leaves of the force box with x in [{lo:.1f}, {ks.max_force[0]:.1f}] "
+                       f"({pairs:.3e} pairs, full tree built), {dt:.2f} s wall"),
+            "seconds": dt, "pairs": pairs}
+
+
+def run_reference_arm(args, world, rank):
+    if rank != 0:
+        return 0
+    p, kp, cfg = workload(args.ng, args.nd)
+    threads = os.cpu_count() or 1
+    for _ in range(args.warmup):
+        cpu_baseline(p, kp, args.cpu_slab / 4, threads)
+    runs = [cpu_baseline(p, kp, args.cpu_slab / 4, threads) for _ in range(args.steps)]
+    pairs = sum(r["pairs"] for r in runs)
+    secs = sum(r["seconds"] for r in runs)
+    value = pairs / secs
+    line = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * secs / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "impl": "reference",
+            "data": "synthetic (seeded Zel'dovich lattice with overload ghosts)", "config": cfg,
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": runs[0]["sample"]},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def main():
+    args = parse_args()
+    world, rank, local = dist_init()
+    if args.impl == "reference":
+        return run_reference_arm(args, world, rank)
+
+    import build_ext
+    build_ext.build()
+    import hsr
+
+    kernel = {"auto": hsr.KERNEL_AUTO, "plain": hsr.KERNEL_PLAIN, "batched": hsr.KERNEL_BATCHED}[args.kernel]
+    p0, kp, cfg = workload(args.ng, args.nd)
+    ctx = hsr.Context(local)
+
+    # ---- end to end through the C ABI (host arrays in, host arrays out) ----
+    for _ in range(max(args.warmup, 3)):
+        ctx.rcb_kick(p0.copy(), kp, kernel=kernel)
+    e2e_secs, st = [], None
+    barrier(world)
+    for _ in range(args.steps):
+        q = p0.copy()
+        t0 = time.perf_counter()
+        st = ctx.rcb_kick(q, kp, kernel=kernel)
+        e2e_secs.append(time.perf_counter() - t0)
+    e2e_t = max_over_ranks(world, sum(e2e_secs))
+    pairs = st["pairs"]
+    h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
+
+    # ---- device-resident step: pair kernel on the resident lists ----
+    ctx.bench_pairs(max(args.warmup, 3), kernel=kernel)
+    barrier(world)
+    with ClockSampler(local) as cs:
+        t0 = time.perf_counter()
+        ms = ctx.bench_pairs(args.steps, kernel=kernel)
+        wall = time.perf_counter() - t0
+    ms = max_over_ranks(world, ms)
+    value = world * pairs / (ms * 1e-3)
+
+    peak = ctx.fp32_peak_tflops()
+    achieved = pairs * FLOPS_PER_PAIR / (ms * 1e-3) / 1e12
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(p0, kp, args.cpu_slab, os.cpu_count() or 1)
+        cpu = {k: v for k, v in cpu.items() if k not in ("seconds", "pairs")}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Zel'dovich lattice with overload ghosts)",
+            "config": {**cfg, "pairs_per_step": pairs, "processed_leaves": st["processed_leaves"],
+                       "list_entries": st["list_entries"], "kernel": args.kernel,
+                       "parallelism": f"replicas{world}"},
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                         "frac": achieved / peak if peak else None, "traffic": None,
+                         "peak_source": "FFMA-chain probe on this device (hsr_probe_fp32_peak)",
+                         "flops_per_pair": FLOPS_PER_PAIR},
+            "cpu_baseline": cpu,
+            "e2e": {"value": world * pairs * args.steps / e2e_t, "unit": UNIT,
+                    "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
+                    "s_per_kick": e2e_t / args.steps,
+                    "host_build_ms": st["t_build_ms"], "host_walk_ms": st["t_walk_ms"]},
+            "gpu_launches": args.steps,
+            "clocks": cs.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    ctx.close()
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

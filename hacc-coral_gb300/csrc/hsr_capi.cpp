@@ -1,0 +1,575 @@
+// hsr_capi.cpp -- the C ABI (include/hacc_sr.h) over the host tree and the
+// sm_103a kernels.
+#include "hacc_sr.h"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <limits>
+#include <memory>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "rcb_host.hpp"
+#include "sr_kernels.cuh"
+
+namespace {
+
+using clk = std::chrono::steady_clock;
+double ms_since(clk::time_point t0) {
+  return std::chrono::duration<double, std::milli>(clk::now() - t0).count();
+}
+
+// Device buffer that only grows.
+struct DevBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(bytes + bytes / 4, 1 << 16);
+    cudaError_t e = cudaMalloc(&p, want);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFree(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <typename T> T *as() const { return static_cast<T *>(p); }
+};
+
+// Pinned host buffer that only grows.
+struct PinBuf {
+  void *p = nullptr;
+  size_t cap = 0;
+  cudaError_t ensure(size_t bytes) {
+    if (bytes <= cap) return cudaSuccess;
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+    size_t want = std::max<size_t>(bytes + bytes / 4, 1 << 16);
+    cudaError_t e = cudaHostAlloc(&p, want, cudaHostAllocDefault);
+    if (e == cudaSuccess) cap = want;
+    return e;
+  }
+  void release() {
+    if (p) cudaFreeHost(p);
+    p = nullptr;
+    cap = 0;
+  }
+  template <typename T> T *as() const { return static_cast<T *>(p); }
+};
+
+// Strict upper bound on r2 combining the pair kernel's `dist2 < fsrrmax2`
+// (RCBForceTree.cxx:612-613) with the law's own `r2 <= r2max`
+// (ForceLaw.cxx:140, 189), r2max = rmax^2 with FGrid's rmax (ForceLaw.cxx:32).
+float cut2(int law, float fsrrmax) {
+  const float fs2 = fsrrmax * fsrrmax;
+  if (law == HSR_LAW_POLY5_STEP16) return fs2;
+  const float rmax = 3.116326355f;
+  const float r2max = rmax * rmax;
+  return std::min(fs2, std::nextafter(r2max, std::numeric_limits<float>::infinity()));
+}
+
+}  // namespace
+
+struct hsr_ctx {
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  std::unique_ptr<hsr::RcbHost> host;
+  DevBuf d_pos, d_vel, d_leaves, d_segs, d_idx, d_law;
+  PinBuf h_pos, h_vel, h_leaves, h_segs;
+  hsr_stats stats{};
+  std::string err = "no error";
+  bool have_lists = false;
+  int64_t last_n = 0;
+  int last_tdpts = 1;
+  // launch arguments of the last kick's pair kernel (diagnostic replays)
+  int last_law = 0;
+  int64_t last_nleaves = 0;
+  float last_fcoeff = 0, last_rsm2 = 0, last_rc2 = 0;
+  DevBuf d_flush, d_probe;
+
+  hsr_status fail(hsr_status s, const std::string &msg) {
+    err = msg;
+    return s;
+  }
+  hsr_status cuda_fail(cudaError_t e, const char *what) {
+    err = std::string(what) + ": " + cudaGetErrorString(e);
+    return HSR_ERR_CUDA;
+  }
+};
+
+#define CU(call, what)                                   \
+  do {                                                   \
+    cudaError_t e_ = (call);                             \
+    if (e_ != cudaSuccess) return ctx->cuda_fail(e_, what); \
+  } while (0)
+
+extern "C" {
+
+const char *hsr_version(void) { return "hacc-sr-gb300 0.1 (sm_103a)"; }
+
+const char *hsr_last_error(const hsr_ctx *ctx) {
+  return ctx ? ctx->err.c_str() : "null context";
+}
+
+hsr_status hsr_create(hsr_ctx **out, int device) {
+  if (!out) return HSR_ERR_ARG;
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev <= 0) return HSR_ERR_NO_DEVICE;
+  if (device < 0 || device >= ndev) return HSR_ERR_ARG;
+  auto *ctx = new (std::nothrow) hsr_ctx();
+  if (!ctx) return HSR_ERR_NOMEM;
+  ctx->device = device;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+  if (e != cudaSuccess) {
+    delete ctx;
+    return HSR_ERR_CUDA;
+  }
+  int nth = int(std::thread::hardware_concurrency());
+  ctx->host.reset(new hsr::RcbHost(std::max(1, nth)));
+  *out = ctx;
+  return HSR_OK;
+}
+
+hsr_status hsr_destroy(hsr_ctx *ctx) {
+  if (!ctx) return HSR_ERR_ARG;
+  cudaSetDevice(ctx->device);
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (DevBuf *b : {&ctx->d_pos, &ctx->d_vel, &ctx->d_leaves, &ctx->d_segs, &ctx->d_idx, &ctx->d_law,
+                    &ctx->d_flush, &ctx->d_probe})
+    b->release();
+  for (PinBuf *b : {&ctx->h_pos, &ctx->h_vel, &ctx->h_leaves, &ctx->h_segs}) b->release();
+  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
+  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return HSR_OK;
+}
+
+hsr_status hsr_get_stats(const hsr_ctx *ctx, hsr_stats *st) {
+  if (!ctx || !st) return HSR_ERR_ARG;
+  *st = ctx->stats;
+  return HSR_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+hsr_status check_params(const hsr_params *p, int64_t n, const void *const *arrs, std::string &err) {
+  if (!p) return err = "null params", HSR_ERR_ARG;
+  if (n < 0) return err = "negative particle count", HSR_ERR_ARG;
+  if (n > 0)
+    for (int i = 0; i < 10; ++i)
+      if (!arrs[i]) return err = "null particle array", HSR_ERR_ARG;
+  if (p->tdpts != 1 && p->tdpts != 12) return err = "tdpts must be 1 or 12", HSR_ERR_ARG;
+  if (p->nd < 1) return err = "nd must be >= 1", HSR_ERR_ARG;
+  if (p->law != HSR_LAW_POLY6 && p->law != HSR_LAW_POLY5_STEP16)
+    return err = "unknown force law", HSR_ERR_ARG;
+  // int32 position-table indices: particles plus pseudo-particles of <= 2n+1 nodes
+  if (n > (int64_t(INT32_MAX) - 64) / (1 + 2 * int64_t(p->tdpts)))
+    return err = "too many particles for one call", HSR_ERR_ARG;
+  return HSR_OK;
+}
+
+hsr::TreeParams tree_params(const hsr_params *p) {
+  hsr::TreeParams tp{};
+  for (int i = 0; i < 3; ++i) {
+    tp.min[i] = p->min[i];
+    tp.max[i] = p->max[i];
+    tp.min_force[i] = p->min_force[i];
+    tp.max_force[i] = p->max_force[i];
+  }
+  tp.fsrrmax = p->fsrrmax;
+  tp.tan_oa = std::tan(p->open_angle);
+  tp.nd = p->nd;
+  tp.ppc = p->ppc;
+  tp.tdpts = p->tdpts;
+  return tp;
+}
+
+// Sizes of the work description produced by host_build.
+struct PlanSizes {
+  int64_t ntab, nleaves, nsegs, nidx;
+};
+
+// Tree build and lists on the host; fills the statistics.
+PlanSizes host_build(hsr::RcbHost &H, const hsr_params *p, int64_t n, const float *x,
+                     const float *y, const float *z, const float *mass, hsr_stats &st) {
+  auto t0 = clk::now();
+  H.build(tree_params(p), n, x, y, z, mass);
+  st.t_build_ms = ms_since(t0);
+  t0 = clk::now();
+  H.walk();
+  st.t_walk_ms = ms_since(t0);
+  st.n = n;
+  st.nodes = H.num_nodes();
+  st.leaves = H.nonempty_leaves();
+  st.processed_leaves = int64_t(H.leaves().size());
+  st.list_entries = H.list_entries();
+  st.pairs = H.pairs();
+  return PlanSizes{n + H.num_nodes() * p->tdpts, int64_t(H.leaves().size()),
+                   int64_t(H.segs().size()), H.list_entries()};
+}
+
+// Applies the tree's permutation to the caller's arrays (the reference
+// permutes all ten in place) and fills the position table (particles, then
+// pseudo-particles), the permuted velocities (3 x n, may be null; the
+// caller's velocities are then left for the caller to overwrite) and the
+// leaf/segment descriptors (may be null).
+void host_fill(hsr::RcbHost &H, int64_t n, float *x, float *y, float *z, float *vx, float *vy,
+               float *vz, float *mass, float *phi, int64_t *id, uint16_t *mask, float *tab,
+               float *vel, hsr::LeafDesc *ld, hsr::SegDesc *sd) {
+  const auto &el = H.elems();
+  hsr::Pool &pool = H.pool();
+  pool.parallel_for(n, 1 << 15, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      const hsr::Elem &q = el[i];
+      float *o = tab + 4 * i;
+      o[0] = q.x; o[1] = q.y; o[2] = q.z; o[3] = q.m;
+      if (vel) {
+        vel[i] = vx[q.idx];
+        vel[n + i] = vy[q.idx];
+        vel[2 * n + i] = vz[q.idx];
+      }
+    }
+  });
+  std::vector<float> tf(static_cast<size_t>(n));
+  auto gather_f = [&](float *a) {
+    pool.parallel_for(n, 1 << 15, [&](int64_t b, int64_t e) {
+      for (int64_t i = b; i < e; ++i) tf[i] = a[el[i].idx];
+    });
+    std::memcpy(a, tf.data(), size_t(n) * 4);
+  };
+  gather_f(phi);
+  if (!vel) {
+    gather_f(vx);
+    gather_f(vy);
+    gather_f(vz);
+  }
+  {
+    std::vector<int64_t> ti(static_cast<size_t>(n));
+    std::vector<uint16_t> tm(static_cast<size_t>(n));
+    pool.parallel_for(n, 1 << 15, [&](int64_t b, int64_t e) {
+      for (int64_t i = b; i < e; ++i) {
+        ti[i] = id[el[i].idx];
+        tm[i] = mask[el[i].idx];
+      }
+    });
+    if (n) {
+      std::memcpy(id, ti.data(), size_t(n) * 8);
+      std::memcpy(mask, tm.data(), size_t(n) * 2);
+    }
+  }
+  pool.parallel_for(n, 1 << 15, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      x[i] = el[i].x;
+      y[i] = el[i].y;
+      z[i] = el[i].z;
+      mass[i] = el[i].m;
+    }
+  });
+  H.pseudo_table(tab + 4 * n);
+  if (!ld) return;
+  const auto &leaves = H.leaves();
+  const auto &segs = H.segs();
+  const int64_t nl = int64_t(leaves.size());
+  std::vector<int64_t> lb(static_cast<size_t>(nl));
+  int64_t run = 0;
+  for (int64_t l = 0; l < nl; ++l) {
+    lb[l] = run;
+    run += leaves[l].list_len;
+  }
+  pool.parallel_for(nl, 64, [&](int64_t b, int64_t e) {
+    for (int64_t l = b; l < e; ++l) {
+      const auto &L = leaves[l];
+      hsr::LeafDesc d{};
+      d.offset = int32_t(L.offset);
+      d.count = int32_t(L.count);
+      d.list_len = int32_t(L.list_len);
+      d.list_begin = lb[l];
+      ld[l] = d;
+      int64_t dst = lb[l];
+      for (int64_t s = L.seg_begin; s < L.seg_end; ++s) {
+        sd[s] = hsr::SegDesc{segs[s].start, segs[s].count, dst};
+        dst += segs[s].count;
+      }
+    }
+  });
+}
+
+// Expands the segments of the lists into entries (x, y, z, m) and/or
+// position-table indices.
+void export_lists(const hsr::RcbHost &H, const float *tab, int64_t *leaf_offset,
+                  int64_t *leaf_count, int64_t *list_ptr, float *ex, float *ey, float *ez,
+                  float *em, int64_t *eidx) {
+  int64_t run = 0;
+  for (size_t l = 0; l < H.leaves().size(); ++l) {
+    const auto &L = H.leaves()[l];
+    if (leaf_offset) leaf_offset[l] = L.offset;
+    if (leaf_count) leaf_count[l] = L.count;
+    if (list_ptr) list_ptr[l] = run;
+    for (int64_t s = L.seg_begin; s < L.seg_end; ++s) {
+      const auto &sg = H.segs()[s];
+      for (int32_t q = 0; q < sg.count; ++q) {
+        const int64_t t = int64_t(sg.start) + q;
+        if (ex) {
+          const float *e = tab + 4 * t;
+          ex[run] = e[0];
+          ey[run] = e[1];
+          ez[run] = e[2];
+          em[run] = e[3];
+        }
+        if (eidx) eidx[run] = t;
+        ++run;
+      }
+    }
+  }
+  if (list_ptr) list_ptr[H.leaves().size()] = run;
+}
+
+}  // namespace
+
+struct hsr_lists {
+  std::unique_ptr<hsr::RcbHost> host;
+  std::vector<float> tab;
+  hsr_stats st{};
+};
+
+extern "C" {
+
+hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, float *y, float *z,
+                        float *vx, float *vy, float *vz, float *mass, float *phi, int64_t *id,
+                        uint16_t *mask, int32_t mem) {
+  if (!ctx) return HSR_ERR_ARG;
+  const auto t_start = clk::now();
+  const void *arrs[10] = {x, y, z, vx, vy, vz, mass, phi, id, mask};
+  if (hsr_status e = check_params(p, n, arrs, ctx->err)) return e;
+  if (mem != HSR_MEM_HOST) return ctx->fail(HSR_ERR_UNSUPPORTED, "hsr_rcb_kick takes host arrays");
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  ctx->have_lists = false;
+  hsr_stats st{};
+  hsr::RcbHost &H = *ctx->host;
+  const PlanSizes ps = host_build(H, p, n, x, y, z, mass, st);
+
+  CU(ctx->h_pos.ensure(size_t(std::max<int64_t>(ps.ntab, 1)) * 16), "cudaHostAlloc(pos)");
+  CU(ctx->h_vel.ensure(size_t(std::max<int64_t>(3 * n, 1)) * 4), "cudaHostAlloc(vel)");
+  CU(ctx->h_leaves.ensure(size_t(std::max<int64_t>(ps.nleaves, 1)) * sizeof(hsr::LeafDesc)),
+     "cudaHostAlloc(leaves)");
+  CU(ctx->h_segs.ensure(size_t(std::max<int64_t>(ps.nsegs, 1)) * sizeof(hsr::SegDesc)),
+     "cudaHostAlloc(segs)");
+  float *hp = ctx->h_pos.as<float>();
+  float *hv = ctx->h_vel.as<float>();
+  auto *hl = ctx->h_leaves.as<hsr::LeafDesc>();
+  auto *hs = ctx->h_segs.as<hsr::SegDesc>();
+  host_fill(H, n, x, y, z, vx, vy, vz, mass, phi, id, mask, hp, hv, hl, hs);
+
+  cudaStream_t s = ctx->stream;
+  CU(ctx->d_pos.ensure(size_t(std::max<int64_t>(ps.ntab, 1)) * 16), "cudaMalloc(pos)");
+  CU(ctx->d_vel.ensure(size_t(std::max<int64_t>(3 * n, 1)) * 4), "cudaMalloc(vel)");
+  CU(ctx->d_leaves.ensure(size_t(std::max<int64_t>(ps.nleaves, 1)) * sizeof(hsr::LeafDesc)),
+     "cudaMalloc(leaves)");
+  CU(ctx->d_segs.ensure(size_t(std::max<int64_t>(ps.nsegs, 1)) * sizeof(hsr::SegDesc)),
+     "cudaMalloc(segs)");
+  CU(ctx->d_idx.ensure(size_t(std::max<int64_t>(ps.nidx, 1)) * 4), "cudaMalloc(idx)");
+  CU(cudaMemcpyAsync(ctx->d_pos.p, hp, size_t(ps.ntab) * 16, cudaMemcpyHostToDevice, s), "H2D pos");
+  CU(cudaMemcpyAsync(ctx->d_vel.p, hv, size_t(3 * n) * 4, cudaMemcpyHostToDevice, s), "H2D vel");
+  CU(cudaMemcpyAsync(ctx->d_leaves.p, hl, size_t(ps.nleaves) * sizeof(hsr::LeafDesc),
+                     cudaMemcpyHostToDevice, s), "H2D leaves");
+  CU(cudaMemcpyAsync(ctx->d_segs.p, hs, size_t(ps.nsegs) * sizeof(hsr::SegDesc),
+                     cudaMemcpyHostToDevice, s), "H2D segs");
+  int64_t launches = 0;
+  CU(hsr::launch_expand_segments(ctx->d_segs.as<hsr::SegDesc>(), ps.nsegs, ctx->d_idx.as<int32_t>(), s),
+     "expand kernel");
+  launches += ps.nsegs > 0;
+  float *dv = ctx->d_vel.as<float>();
+  const float rsm2 = p->rsm * p->rsm;
+  const float rc2 = cut2(p->law, p->fsrrmax);
+  CU(cudaEventRecord(ctx->ev0, s), "event");
+  CU(hsr::launch_leaf_plain(p->law, ctx->d_pos.as<float4>(), ctx->d_leaves.as<hsr::LeafDesc>(),
+                            ps.nleaves, ctx->d_idx.as<int32_t>(), dv, dv + n, dv + 2 * n, p->fcoeff,
+                            rsm2, rc2, s),
+     "pair kernel");
+  launches += ps.nleaves > 0;
+  CU(cudaEventRecord(ctx->ev1, s), "event");
+  CU(cudaMemcpyAsync(hv, dv, size_t(3 * n) * 4, cudaMemcpyDeviceToHost, s), "D2H vel");
+  CU(cudaStreamSynchronize(s), "kernel execution");
+  float fms = 0;
+  CU(cudaEventElapsedTime(&fms, ctx->ev0, ctx->ev1), "event time");
+  st.t_force_ms = fms;
+  H.pool().parallel_for(n, 1 << 15, [&](int64_t b, int64_t e) {
+    for (int64_t i = b; i < e; ++i) {
+      vx[i] = hv[i];
+      vy[i] = hv[n + i];
+      vz[i] = hv[2 * n + i];
+    }
+  });
+  st.kernel_launches = launches;
+  st.h2d_bytes = ps.ntab * 16 + 3 * n * 4 + ps.nleaves * int64_t(sizeof(hsr::LeafDesc)) +
+                 ps.nsegs * int64_t(sizeof(hsr::SegDesc));
+  st.d2h_bytes = 3 * n * 4;
+  st.t_total_ms = ms_since(t_start);
+  ctx->stats = st;
+  ctx->have_lists = true;
+  ctx->last_n = n;
+  ctx->last_tdpts = p->tdpts;
+  ctx->last_law = p->law;
+  ctx->last_nleaves = ps.nleaves;
+  ctx->last_fcoeff = p->fcoeff;
+  ctx->last_rsm2 = rsm2;
+  ctx->last_rc2 = rc2;
+  return HSR_OK;
+}
+
+hsr_status hsr_lists_size(const hsr_ctx *ctx, int64_t *nleaves, int64_t *nentries) {
+  if (!ctx || !nleaves || !nentries) return HSR_ERR_ARG;
+  if (!ctx->have_lists) return HSR_ERR_STATE;
+  *nleaves = int64_t(ctx->host->leaves().size());
+  *nentries = ctx->host->list_entries();
+  return HSR_OK;
+}
+
+hsr_status hsr_lists_export(const hsr_ctx *ctx, int64_t *leaf_offset, int64_t *leaf_count,
+                            int64_t *list_ptr, float *ex, float *ey, float *ez, float *em) {
+  if (!ctx || !leaf_offset || !leaf_count || !list_ptr || !ex || !ey || !ez || !em) return HSR_ERR_ARG;
+  if (!ctx->have_lists) return HSR_ERR_STATE;
+  export_lists(*ctx->host, ctx->h_pos.as<float>(), leaf_offset, leaf_count, list_ptr, ex, ey, ez, em,
+               nullptr);
+  return HSR_OK;
+}
+
+hsr_status hsr_build_lists(const hsr_params *p, int64_t n, float *x, float *y, float *z, float *vx,
+                           float *vy, float *vz, float *mass, float *phi, int64_t *id, uint16_t *mask,
+                           hsr_lists **out) {
+  if (!out) return HSR_ERR_ARG;
+  *out = nullptr;
+  std::string err;
+  const void *arrs[10] = {x, y, z, vx, vy, vz, mass, phi, id, mask};
+  if (hsr_status e = check_params(p, n, arrs, err)) return e;
+  auto *L = new (std::nothrow) hsr_lists();
+  if (!L) return HSR_ERR_NOMEM;
+  int nth = int(std::thread::hardware_concurrency());
+  L->host.reset(new hsr::RcbHost(std::max(1, nth)));
+  const PlanSizes ps = host_build(*L->host, p, n, x, y, z, mass, L->st);
+  L->tab.resize(size_t(std::max<int64_t>(ps.ntab, 1)) * 4);
+  host_fill(*L->host, n, x, y, z, vx, vy, vz, mass, phi, id, mask, L->tab.data(), nullptr, nullptr,
+            nullptr);
+  *out = L;
+  return HSR_OK;
+}
+
+hsr_status hsr_lists_info(const hsr_lists *L, int64_t *nleaves, int64_t *nentries, hsr_stats *st) {
+  if (!L) return HSR_ERR_ARG;
+  if (nleaves) *nleaves = int64_t(L->host->leaves().size());
+  if (nentries) *nentries = L->host->list_entries();
+  if (st) *st = L->st;
+  return HSR_OK;
+}
+
+hsr_status hsr_lists_get(const hsr_lists *L, int64_t *leaf_offset, int64_t *leaf_count,
+                         int64_t *list_ptr, float *ex, float *ey, float *ez, float *em) {
+  if (!L || !leaf_offset || !leaf_count || !list_ptr || !ex || !ey || !ez || !em) return HSR_ERR_ARG;
+  export_lists(*L->host, L->tab.data(), leaf_offset, leaf_count, list_ptr, ex, ey, ez, em, nullptr);
+  return HSR_OK;
+}
+
+hsr_status hsr_lists_index(const hsr_lists *L, int64_t *entry_index) {
+  if (!L || !entry_index) return HSR_ERR_ARG;
+  export_lists(*L->host, L->tab.data(), nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+               entry_index);
+  return HSR_OK;
+}
+
+hsr_status hsr_lists_free(hsr_lists *L) {
+  if (!L) return HSR_ERR_ARG;
+  delete L;
+  return HSR_OK;
+}
+
+hsr_status hsr_force_law(hsr_ctx *ctx, int32_t law, float rsm, float fsrrmax, int64_t n,
+                         const float *r2, float *g) {
+  if (!ctx) return HSR_ERR_ARG;
+  if (n < 0 || (n > 0 && (!r2 || !g))) return ctx->fail(HSR_ERR_ARG, "bad arrays");
+  if (law != HSR_LAW_POLY6 && law != HSR_LAW_POLY5_STEP16) return ctx->fail(HSR_ERR_ARG, "unknown law");
+  if (n == 0) return HSR_OK;
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  CU(ctx->d_law.ensure(size_t(n) * 8), "cudaMalloc(law)");
+  float *d = ctx->d_law.as<float>();
+  cudaStream_t s = ctx->stream;
+  CU(cudaMemcpyAsync(d, r2, size_t(n) * 4, cudaMemcpyHostToDevice, s), "H2D r2");
+  CU(hsr::launch_force_law(law, d, d + n, n, rsm * rsm, cut2(law, fsrrmax), s), "law kernel");
+  CU(cudaMemcpyAsync(g, d + n, size_t(n) * 4, cudaMemcpyDeviceToHost, s), "D2H g");
+  CU(cudaStreamSynchronize(s), "law kernel execution");
+  return HSR_OK;
+}
+
+hsr_status hsr_bench_pairs(hsr_ctx *ctx, int32_t kernel, int32_t iters, int32_t flush_l2,
+                           double *ms_per_launch) {
+  if (!ctx || !ms_per_launch || iters < 1) return HSR_ERR_ARG;
+  if (!ctx->have_lists) return ctx->fail(HSR_ERR_STATE, "no kick to replay");
+  (void)kernel;
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  cudaStream_t s = ctx->stream;
+  const size_t flush_bytes = size_t(256) << 20;
+  if (flush_l2) CU(ctx->d_flush.ensure(flush_bytes), "cudaMalloc(flush)");
+  const int64_t n = ctx->last_n;
+  float *dv = ctx->d_vel.as<float>();
+  double total = 0;
+  for (int it = 0; it < iters; ++it) {
+    if (flush_l2) CU(cudaMemsetAsync(ctx->d_flush.p, it & 0xff, flush_bytes, s), "L2 flush");
+    CU(cudaEventRecord(ctx->ev0, s), "event");
+    CU(hsr::launch_leaf_plain(ctx->last_law, ctx->d_pos.as<float4>(), ctx->d_leaves.as<hsr::LeafDesc>(),
+                              ctx->last_nleaves, ctx->d_idx.as<int32_t>(), dv, dv + n, dv + 2 * n,
+                              ctx->last_fcoeff, ctx->last_rsm2, ctx->last_rc2, s),
+       "pair kernel");
+    CU(cudaEventRecord(ctx->ev1, s), "event");
+    CU(cudaEventSynchronize(ctx->ev1), "pair kernel execution");
+    float ms = 0;
+    CU(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "event time");
+    total += ms;
+  }
+  *ms_per_launch = total / iters;
+  return HSR_OK;
+}
+
+hsr_status hsr_probe_fp32_peak(hsr_ctx *ctx, double *tflops) {
+  if (!ctx || !tflops) return HSR_ERR_ARG;
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  int sms = 0;
+  CU(cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, ctx->device), "device attribute");
+  const int threads = 512, blocks = sms * 4, iters = 1 << 16;
+  CU(ctx->d_probe.ensure(size_t(blocks) * threads * 4), "cudaMalloc(probe)");
+  cudaStream_t s = ctx->stream;
+  CU(hsr::launch_ffma_probe(ctx->d_probe.as<float>(), blocks, threads, 256, s), "probe warm-up");
+  double best = 0;
+  for (int rep = 0; rep < 3; ++rep) {
+    CU(cudaEventRecord(ctx->ev0, s), "event");
+    CU(hsr::launch_ffma_probe(ctx->d_probe.as<float>(), blocks, threads, iters, s), "probe");
+    CU(cudaEventRecord(ctx->ev1, s), "event");
+    CU(cudaEventSynchronize(ctx->ev1), "probe execution");
+    float ms = 0;
+    CU(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "event time");
+    const double flops = 2.0 * 8.0 * double(iters) * double(blocks) * threads;
+    best = std::max(best, flops / (double(ms) * 1e-3) / 1e12);
+  }
+  *tflops = best;
+  return HSR_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,134 @@
+// sr_kernels.cu -- sm_103a kernels of the short-range pair interaction.
+#include "sr_kernels.cuh"
+
+namespace hsr {
+
+// ---------------------------------------------------------------------------
+// Segment expansion: each segment [start, start + count) of the position
+// table becomes `count` consecutive indices at idx[dst].  One warp per
+// segment, grid-stride over segments.
+// ---------------------------------------------------------------------------
+__global__ void k_expand_segments(const SegDesc *__restrict__ segs, int64_t nsegs,
+                                  int32_t *__restrict__ idx) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t w = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; w < nsegs; w += warps) {
+    const SegDesc s = segs[w];
+    for (int k = lane; k < s.count; k += 32) idx[s.dst + k] = s.start + k;
+  }
+}
+
+cudaError_t launch_expand_segments(const SegDesc *segs, int64_t nsegs, int32_t *idx,
+                                   cudaStream_t s) {
+  if (nsegs <= 0) return cudaSuccess;
+  int64_t blocks = (nsegs + 7) / 8;
+  if (blocks > 152 * 64) blocks = 152 * 64;
+  k_expand_segments<<<unsigned(blocks), 256, 0, s>>>(segs, nsegs, idx);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Plain per-leaf kernel: one CTA per processed leaf, one thread per leaf
+// particle, every list entry evaluated against every particle of the leaf,
+// exactly the pair set of the reference's nbody1.  The list streams through a
+// shared-memory tile of NT float4 entries (x, y, z, m) gathered from the
+// position table by index; all threads of a warp read the same entry, so the
+// shared-memory read is a broadcast.  Warps with no particle left skip the
+// arithmetic but keep loading tiles.
+// ---------------------------------------------------------------------------
+template <int LAW, int NT>
+__global__ void __launch_bounds__(NT)
+    k_leaf_plain(const float4 *__restrict__ pos, const LeafDesc *__restrict__ leaves,
+                 const int32_t *__restrict__ idx, float *__restrict__ vx, float *__restrict__ vy,
+                 float *__restrict__ vz, float fcoeff, float rsm2, float rcut2) {
+  __shared__ float4 tile[NT];
+  const LeafDesc L = leaves[blockIdx.x];
+  const int tid = threadIdx.x;
+  const int32_t *lst = idx + L.list_begin;
+  for (int i0 = 0; i0 < L.count; i0 += NT) {
+    const int i = i0 + tid;
+    const bool act = i < L.count;
+    const float4 pi = act ? pos[L.offset + i] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const bool warp_act = i0 + (tid & ~31) < L.count;
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    for (int t0 = 0; t0 < L.list_len; t0 += NT) {
+      const int tn = min(NT, L.list_len - t0);
+      __syncthreads();
+      if (tid < tn) tile[tid] = pos[lst[t0 + tid]];
+      __syncthreads();
+      if (warp_act) {
+#pragma unroll 4
+        for (int j = 0; j < tn; ++j)
+          pair_acc<LAW>(pi.x, pi.y, pi.z, tile[j], rsm2, rcut2, ax, ay, az);
+      }
+    }
+    if (act) {
+      const float c = (LAW == LAW_POLY5_STEP16) ? fcoeff : fcoeff * pi.w;
+      const int o = L.offset + i;
+      vx[o] += c * ax;
+      vy[o] += c * ay;
+      vz[o] += c * az;
+    }
+  }
+}
+
+cudaError_t launch_leaf_plain(int law, const float4 *pos, const LeafDesc *leaves, int64_t nleaves,
+                              const int32_t *idx, float *vx, float *vy, float *vz, float fcoeff,
+                              float rsm2, float rcut2, cudaStream_t s) {
+  if (nleaves <= 0) return cudaSuccess;
+  constexpr int NT = 128;
+  if (law == LAW_POLY5_STEP16)
+    k_leaf_plain<LAW_POLY5_STEP16, NT><<<unsigned(nleaves), NT, 0, s>>>(pos, leaves, idx, vx, vy, vz,
+                                                                        fcoeff, rsm2, rcut2);
+  else
+    k_leaf_plain<LAW_POLY6, NT><<<unsigned(nleaves), NT, 0, s>>>(pos, leaves, idx, vx, vy, vz,
+                                                                 fcoeff, rsm2, rcut2);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Force law on a batch of r2 values (law tests).
+// ---------------------------------------------------------------------------
+template <int LAW>
+__global__ void k_force_law(const float *__restrict__ r2, float *__restrict__ g, int64_t n,
+                            float rsm2, float rcut2) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const float r = r2[i];
+    g[i] = in_range<LAW>(r, rcut2) ? law_g<LAW>(r, rsm2) : 0.0f;
+  }
+}
+
+cudaError_t launch_force_law(int law, const float *r2, float *g, int64_t n, float rsm2, float rcut2,
+                             cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (law == LAW_POLY5_STEP16)
+    k_force_law<LAW_POLY5_STEP16><<<unsigned(blocks), 256, 0, s>>>(r2, g, n, rsm2, rcut2);
+  else
+    k_force_law<LAW_POLY6><<<unsigned(blocks), 256, 0, s>>>(r2, g, n, rsm2, rcut2);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// FP32 FMA throughput probe: 8 independent dependent chains per thread.
+// ---------------------------------------------------------------------------
+__global__ void k_ffma_probe(float *out, int iters) {
+  const float a = 0.99999f, b = 1.0e-6f;
+  float x0 = threadIdx.x * 1e-7f, x1 = x0 + 0.1f, x2 = x0 + 0.2f, x3 = x0 + 0.3f;
+  float x4 = x0 + 0.4f, x5 = x0 + 0.5f, x6 = x0 + 0.6f, x7 = x0 + 0.7f;
+#pragma unroll 4
+  for (int i = 0; i < iters; ++i) {
+    x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
+    x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);
+  }
+  out[blockIdx.x * blockDim.x + threadIdx.x] = ((x0 + x1) + (x2 + x3)) + ((x4 + x5) + (x6 + x7));
+}
+
+cudaError_t launch_ffma_probe(float *out, int blocks, int threads, int iters, cudaStream_t s) {
+  k_ffma_probe<<<blocks, threads, 0, s>>>(out, iters);
+  return cudaGetLastError();
+}
+
+}  // namespace hsr

@@ -1,0 +1,113 @@
+// sr_kernels.cuh -- device side of the short-range pair interaction.
+//
+// The pair term is the reference's nbody1 inner loop
+// (src/halo_finder/RCBForceTree.cxx:599-619) with ForceLawSR over
+// FGridEvalPoly (src/halo_finder/ForceLaw.cxx:137-141, 187-192):
+//   g(r2) = (r2 + rsm^2)^(-3/2) - sum_{k=0..6} a_k r2^k,
+//   a_i  += [r2 < fsrrmax^2] m_j g(r2) (x_j - x_i),   v_i += fcoeff m_i a_i.
+// FP32 on the CUDA cores: (r2 + rsm^2)^(-3/2) is y^3 with y = rsqrt(r2 +
+// rsm^2), and the polynomial is subtracted inside the final multiply-add
+// (g = y * y^2 + (-p)), which is 20 FMA-pipe operations and one MUFU per pair.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace hsr {
+
+enum { LAW_POLY6 = 0, LAW_POLY5_STEP16 = 1 };
+
+// Work description of one processed leaf on the device.
+struct alignas(16) LeafDesc {
+  int32_t offset;      // first particle of the leaf in the position table
+  int32_t count;       // particles in the leaf
+  int32_t list_len;    // entries in its interaction list (self included)
+  int32_t pad;
+  int64_t list_begin;  // first entry of the list in the index array
+  int64_t pad2;
+};
+
+// Segment of consecutive position-table entries, expanded into the index
+// array at `dst`.
+struct alignas(16) SegDesc {
+  int32_t start;
+  int32_t count;
+  int64_t dst;
+};
+
+#if defined(__CUDACC__)
+// -p(r2) for the law's polynomial, in Horner form on negated coefficients.
+// The coefficients are the reference's double literals rounded to float, as
+// FGridEvalPoly stores them in float m_a[7] (ForceLaw.cxx:98-104) and
+// Step16_int writes them (BGQStep16.c:167).
+template <int LAW>
+__device__ __forceinline__ float neg_poly(float r2);
+
+template <>
+__device__ __forceinline__ float neg_poly<LAW_POLY6>(float r2) {
+  float q = -static_cast<float>(0.000000147305);
+  q = fmaf(q, r2, -static_cast<float>(-0.00000663394));
+  q = fmaf(q, r2, -static_cast<float>(0.000132336));
+  q = fmaf(q, r2, -static_cast<float>(-0.00159485));
+  q = fmaf(q, r2, -static_cast<float>(0.0133122));
+  q = fmaf(q, r2, -static_cast<float>(-0.0783394));
+  q = fmaf(q, r2, -static_cast<float>(0.271431));
+  return q;
+}
+
+template <>
+__device__ __forceinline__ float neg_poly<LAW_POLY5_STEP16>(float r2) {
+  float q = -static_cast<float>(-0.00000147177);
+  q = fmaf(q, r2, -static_cast<float>(0.0000605491));
+  q = fmaf(q, r2, -static_cast<float>(-0.00109313));
+  q = fmaf(q, r2, -static_cast<float>(0.0114808));
+  q = fmaf(q, r2, -static_cast<float>(-0.0750978));
+  q = fmaf(q, r2, -static_cast<float>(0.269327));
+  return q;
+}
+
+// g(r2) without the cutoff mask.
+template <int LAW>
+__device__ __forceinline__ float law_g(float r2, float rsm2) {
+  const float y = rsqrtf(r2 + rsm2);
+  return fmaf(y, y * y, neg_poly<LAW>(r2));
+}
+
+// Whether a pair at squared distance r2 contributes (the reference's
+// updateq and the law's own range, folded into one strict threshold rcut2;
+// Step16_int also drops r2 == 0).
+template <int LAW>
+__device__ __forceinline__ bool in_range(float r2, float rcut2) {
+  if (LAW == LAW_POLY5_STEP16) return r2 < rcut2 && r2 > 0.0f;
+  return r2 < rcut2;
+}
+
+// One pair: accumulates m_j g(r2) d into (ax, ay, az).
+template <int LAW>
+__device__ __forceinline__ void pair_acc(float xi, float yi, float zi, const float4 pj, float rsm2,
+                                         float rcut2, float &ax, float &ay, float &az) {
+  const float dx = pj.x - xi;
+  const float dy = pj.y - yi;
+  const float dz = pj.z - zi;
+  const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+  const float g = law_g<LAW>(r2, rsm2);
+  const float w = in_range<LAW>(r2, rcut2) ? pj.w * g : 0.0f;
+  ax = fmaf(w, dx, ax);
+  ay = fmaf(w, dy, ay);
+  az = fmaf(w, dz, az);
+}
+
+#endif  // __CUDACC__
+
+// Launchers (sr_kernels.cu).  All take the stream to launch on and return
+// the launch status.
+cudaError_t launch_expand_segments(const SegDesc *segs, int64_t nsegs, int32_t *idx,
+                                   cudaStream_t s);
+cudaError_t launch_leaf_plain(int law, const float4 *pos, const LeafDesc *leaves, int64_t nleaves,
+                              const int32_t *idx, float *vx, float *vy, float *vz, float fcoeff,
+                              float rsm2, float rcut2, cudaStream_t s);
+cudaError_t launch_ffma_probe(float *out, int blocks, int threads, int iters, cudaStream_t s);
+cudaError_t launch_force_law(int law, const float *r2, float *g, int64_t n, float rsm2, float rcut2,
+                             cudaStream_t s);
+
+}  // namespace hsr

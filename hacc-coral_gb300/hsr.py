@@ -1,0 +1,307 @@
+"""Python binding of the GB300 short-range gravity library (libhacc_sr.so).
+
+Everything goes through the C ABI declared in include/hacc_sr.h.  There is no
+CPU fallback: if the library is missing or no CUDA device is present, the
+calls raise.
+
+``RCBForceTree`` mirrors the reference constructor
+(src/halo_finder/RCBForceTree.h:96-124): the same arguments in the same order,
+the same in-place effect on the ten particle arrays (tree permutation plus the
+short-range velocity kick).  ``ForceLawSR`` stands for the reference's
+ForceLawSR over FGridEvalPoly (src/halo_finder/ForceLaw.h:114-127).
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "lib", "libhacc_sr.so")
+
+HSR_OK = 0
+STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory",
+          4: "device wait timed out", 5: "unsupported", 6: "no CUDA device", 7: "bad call order"}
+MEM_HOST, MEM_DEVICE = 0, 1
+LAW_POLY6, LAW_POLY5_STEP16 = 0, 1
+KERNEL_AUTO, KERNEL_PLAIN, KERNEL_BATCHED = 0, 1, 2
+
+# Symbols the library exports (include/hacc_sr.h).
+EXPORTS = ("hsr_create", "hsr_destroy", "hsr_last_error", "hsr_version", "hsr_rcb_kick",
+           "hsr_get_stats", "hsr_lists_size", "hsr_lists_export", "hsr_build_lists",
+           "hsr_lists_info", "hsr_lists_get", "hsr_lists_index", "hsr_lists_free",
+           "hsr_force_law", "hsr_bench_pairs", "hsr_probe_fp32_peak")
+
+
+class HsrError(RuntimeError):
+    def __init__(self, status: int, msg: str = ""):
+        super().__init__(f"hsr status {status} ({STATUS.get(status, '?')}): {msg}")
+        self.status = status
+
+
+class HsrParams(C.Structure):
+    _fields_ = [("min", C.c_float * 3), ("max", C.c_float * 3),
+                ("min_force", C.c_float * 3), ("max_force", C.c_float * 3),
+                ("avg_mass", C.c_float), ("fsrrmax", C.c_float), ("rsm", C.c_float),
+                ("open_angle", C.c_float), ("nd", C.c_int64), ("ds", C.c_int64),
+                ("tmin", C.c_int64), ("fcoeff", C.c_float), ("ppc", C.c_float),
+                ("tdpts", C.c_int32), ("law", C.c_int32), ("kernel", C.c_int32),
+                ("reserved", C.c_int32)]
+
+
+class HsrStats(C.Structure):
+    _fields_ = [("n", C.c_int64), ("nodes", C.c_int64), ("leaves", C.c_int64),
+                ("processed_leaves", C.c_int64), ("list_entries", C.c_int64),
+                ("pairs", C.c_int64), ("kernel_launches", C.c_int64),
+                ("t_build_ms", C.c_double), ("t_walk_ms", C.c_double),
+                ("t_force_ms", C.c_double), ("t_total_ms", C.c_double),
+                ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+_lib = None
+
+
+def load(path: str = LIB_PATH):
+    """Loads libhacc_sr.so (built by build_ext.py); raises if it is absent."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise FileNotFoundError(
+            f"{path} is missing: build it with `python hacc-coral_gb300/build_ext.py` "
+            "(there is no CPU fallback)")
+    lib = C.CDLL(path)
+    vp, i32, i64, f32 = C.c_void_p, C.c_int32, C.c_int64, C.c_float
+    pf, pi64, pu16 = C.POINTER(C.c_float), C.POINTER(C.c_int64), C.POINTER(C.c_uint16)
+    lib.hsr_create.restype = i32
+    lib.hsr_create.argtypes = [C.POINTER(vp), C.c_int]
+    lib.hsr_destroy.restype = i32
+    lib.hsr_destroy.argtypes = [vp]
+    lib.hsr_last_error.restype = C.c_char_p
+    lib.hsr_last_error.argtypes = [vp]
+    lib.hsr_version.restype = C.c_char_p
+    lib.hsr_rcb_kick.restype = i32
+    lib.hsr_rcb_kick.argtypes = [vp, C.POINTER(HsrParams), i64] + [pf] * 8 + [pi64, pu16, i32]
+    lib.hsr_get_stats.restype = i32
+    lib.hsr_get_stats.argtypes = [vp, C.POINTER(HsrStats)]
+    lib.hsr_lists_size.restype = i32
+    lib.hsr_lists_size.argtypes = [vp, pi64, pi64]
+    lib.hsr_lists_export.restype = i32
+    lib.hsr_lists_export.argtypes = [vp, pi64, pi64, pi64, pf, pf, pf, pf]
+    lib.hsr_build_lists.restype = i32
+    lib.hsr_build_lists.argtypes = [C.POINTER(HsrParams), i64] + [pf] * 8 + [pi64, pu16, C.POINTER(vp)]
+    lib.hsr_lists_info.restype = i32
+    lib.hsr_lists_info.argtypes = [vp, pi64, pi64, C.POINTER(HsrStats)]
+    lib.hsr_lists_get.restype = i32
+    lib.hsr_lists_get.argtypes = [vp, pi64, pi64, pi64, pf, pf, pf, pf]
+    lib.hsr_lists_index.restype = i32
+    lib.hsr_lists_index.argtypes = [vp, pi64]
+    lib.hsr_lists_free.restype = i32
+    lib.hsr_lists_free.argtypes = [vp]
+    lib.hsr_force_law.restype = i32
+    lib.hsr_force_law.argtypes = [vp, i32, f32, f32, i64, pf, pf]
+    lib.hsr_bench_pairs.restype = i32
+    lib.hsr_bench_pairs.argtypes = [vp, i32, i32, i32, C.POINTER(C.c_double)]
+    lib.hsr_probe_fp32_peak.restype = i32
+    lib.hsr_probe_fp32_peak.argtypes = [vp, C.POINTER(C.c_double)]
+    _lib = lib
+    return lib
+
+
+def _p(a, ct):
+    return a.ctypes.data_as(C.POINTER(ct))
+
+
+def _check_host(a, dtype, n, name):
+    if not isinstance(a, np.ndarray) or a.dtype != dtype or not a.flags.c_contiguous \
+            or a.shape[0] < n or not a.flags.writeable:
+        raise TypeError(f"{name} must be a writable C-contiguous {np.dtype(dtype)} array of >= {n}")
+
+
+def make_params(kp, kernel: int = KERNEL_AUTO) -> HsrParams:
+    P = HsrParams()
+    for k in ("min", "max", "min_force", "max_force"):
+        getattr(P, k)[:] = [float(v) for v in getattr(kp, k)]
+    P.avg_mass, P.fsrrmax, P.rsm, P.open_angle = kp.avg_mass, kp.fsrrmax, kp.rsm, kp.open_angle
+    P.nd, P.ds, P.tmin = kp.nd, kp.ds, kp.tmin
+    P.fcoeff, P.ppc, P.tdpts, P.law = kp.fcoeff, kp.ppc, kp.tdpts, kp.law
+    P.kernel = kernel
+    return P
+
+
+class Context:
+    """One hsr_ctx: a CUDA device, its stream and buffers (one per host thread)."""
+
+    def __init__(self, device: int = 0):
+        self.lib = load()
+        h = C.c_void_p()
+        st = self.lib.hsr_create(C.byref(h), device)
+        if st != HSR_OK:
+            raise HsrError(st, f"hsr_create(device={device})")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.hsr_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        self.close()
+
+    def _check(self, st, what):
+        if st != HSR_OK:
+            raise HsrError(st, f"{what}: {self.lib.hsr_last_error(self.h).decode()}")
+
+    def stats(self) -> dict:
+        s = HsrStats()
+        self._check(self.lib.hsr_get_stats(self.h, C.byref(s)), "hsr_get_stats")
+        return s.as_dict()
+
+    def rcb_kick(self, p, kp, kernel: int = KERNEL_AUTO) -> dict:
+        """hsr_rcb_kick on the host arrays of `p` (modified in place)."""
+        P = make_params(kp, kernel)
+        st = self.lib.hsr_rcb_kick(self.h, C.byref(P), p.n, *_particle_args(p), MEM_HOST)
+        self._check(st, "hsr_rcb_kick")
+        return self.stats()
+
+    def lists(self):
+        nl, ne = C.c_int64(), C.c_int64()
+        self._check(self.lib.hsr_lists_size(self.h, C.byref(nl), C.byref(ne)), "hsr_lists_size")
+        off = np.zeros(nl.value, np.int64)
+        cnt = np.zeros(nl.value, np.int64)
+        ptr = np.zeros(nl.value + 1, np.int64)
+        e = np.zeros((4, ne.value), np.float32)
+        self._check(self.lib.hsr_lists_export(self.h, _p(off, C.c_int64), _p(cnt, C.c_int64),
+                                              _p(ptr, C.c_int64),
+                                              *[_p(e[i], C.c_float) for i in range(4)]),
+                    "hsr_lists_export")
+        return off, cnt, ptr, e
+
+    def bench_pairs(self, iters: int, kernel: int = KERNEL_AUTO, flush_l2: bool = True) -> float:
+        """Mean ms per relaunch of the last kick's pair kernel (hsr_bench_pairs)."""
+        ms = C.c_double()
+        self._check(self.lib.hsr_bench_pairs(self.h, kernel, iters, int(flush_l2), C.byref(ms)),
+                    "hsr_bench_pairs")
+        return ms.value
+
+    def fp32_peak_tflops(self) -> float:
+        t = C.c_double()
+        self._check(self.lib.hsr_probe_fp32_peak(self.h, C.byref(t)), "hsr_probe_fp32_peak")
+        return t.value
+
+    def force_law(self, r2, law: int = LAW_POLY6, rsm: float = 0.1,
+                  fsrrmax: float = 3.116326355) -> np.ndarray:
+        r2 = np.ascontiguousarray(r2, dtype=np.float32)
+        g = np.zeros_like(r2)
+        self._check(self.lib.hsr_force_law(self.h, law, rsm, fsrrmax, r2.size,
+                                           _p(r2, C.c_float), _p(g, C.c_float)), "hsr_force_law")
+        return g
+
+
+def _particle_args(p):
+    n = p.n
+    for k in ("x", "y", "z", "vx", "vy", "vz", "mass", "phi"):
+        _check_host(getattr(p, k), np.float32, n, k)
+    _check_host(p.id, np.int64, n, "id")
+    _check_host(p.mask, np.uint16, n, "mask")
+    return ([_p(getattr(p, k), C.c_float) for k in ("x", "y", "z", "vx", "vy", "vz", "mass", "phi")]
+            + [_p(p.id, C.c_int64), _p(p.mask, C.c_uint16)])
+
+
+class HostLists:
+    """hsr_build_lists: the tree and lists built on the host only (no GPU)."""
+
+    def __init__(self, p, kp):
+        self.lib = load()
+        P = make_params(kp)
+        h = C.c_void_p()
+        st = self.lib.hsr_build_lists(C.byref(P), p.n, *_particle_args(p), C.byref(h))
+        if st != HSR_OK:
+            raise HsrError(st, "hsr_build_lists")
+        self.h = h
+        self.n = p.n
+        nl, ne, s = C.c_int64(), C.c_int64(), HsrStats()
+        self.lib.hsr_lists_info(self.h, C.byref(nl), C.byref(ne), C.byref(s))
+        self.nleaves, self.nentries, self.stats = nl.value, ne.value, s.as_dict()
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            self.lib.hsr_lists_free(self.h)
+            self.h = None
+
+    def get(self):
+        off = np.zeros(self.nleaves, np.int64)
+        cnt = np.zeros(self.nleaves, np.int64)
+        ptr = np.zeros(self.nleaves + 1, np.int64)
+        e = np.zeros((4, self.nentries), np.float32)
+        st = self.lib.hsr_lists_get(self.h, _p(off, C.c_int64), _p(cnt, C.c_int64),
+                                    _p(ptr, C.c_int64), *[_p(e[i], C.c_float) for i in range(4)])
+        if st != HSR_OK:
+            raise HsrError(st, "hsr_lists_get")
+        return off, cnt, ptr, e
+
+    def index(self):
+        idx = np.zeros(self.nentries, np.int64)
+        st = self.lib.hsr_lists_index(self.h, _p(idx, C.c_int64))
+        if st != HSR_OK:
+            raise HsrError(st, "hsr_lists_index")
+        return idx
+
+
+# ---------------------------------------------------------------------------
+# Reference-shaped interface
+# ---------------------------------------------------------------------------
+
+class ForceLawSR:
+    """ForceLawSR(FGridEvalPoly, rsm): the short-range law the tree evaluates
+    (src/halo_finder/ForceLaw.h:114-127; POLY_ORDER 6)."""
+
+    def __init__(self, rsm: float, law: int = LAW_POLY6):
+        self.rsm = float(rsm)
+        self.law = law
+
+
+_default_ctx = None
+
+
+def default_context() -> Context:
+    global _default_ctx
+    if _default_ctx is None:
+        _default_ctx = Context(0)
+    return _default_ctx
+
+
+class _Args:
+    pass
+
+
+def RCBForceTree(minLoc, maxLoc, minForceLoc, maxForceLoc, count, xLoc, yLoc, zLoc, xVel, yVel,
+                 zVel, mass, phiLoc, idLoc, maskLoc, avgMass, fsm, r, oa, nd=1, ds=1, tmin=128,
+                 fl=None, fcoeff=0.0, ppc=0.9, tdpts=1, ctx: Context | None = None):
+    """The RCBForceTree<TDPTS> constructor: builds the tree over `count`
+    particles (permuting the ten arrays in place), walks it and kicks the
+    velocities.  `fl` must be a ForceLawSR: the reference's default
+    (fl = 0 -> ForceLawNewton, fcoeff = 1) is not part of the short-range
+    path and raises.  Returns the call's statistics."""
+    if fl is None:
+        raise HsrError(5, "fl=None selects ForceLawNewton in the reference; pass a ForceLawSR")
+    a = _Args()
+    a.min, a.max = tuple(minLoc), tuple(maxLoc)
+    a.min_force, a.max_force = tuple(minForceLoc), tuple(maxForceLoc)
+    a.avg_mass, a.fsrrmax, a.rsm, a.open_angle = avgMass, fsm, fl.rsm, oa
+    a.nd, a.ds, a.tmin, a.fcoeff, a.ppc, a.tdpts, a.law = nd, ds, tmin, fcoeff, ppc, tdpts, fl.law
+    p = _Args()
+    p.n = int(count)
+    p.x, p.y, p.z, p.vx, p.vy, p.vz = xLoc, yLoc, zLoc, xVel, yVel, zVel
+    p.mass, p.phi, p.id, p.mask = mass, phiLoc, idLoc, maskLoc
+    return (ctx or default_context()).rcb_kick(p, a)

@@ -1,0 +1,179 @@
+/*
+ * hacc_sr.h -- C ABI of the GB300 short-range gravity path (RCBForceTree).
+ *
+ * This library replaces HACC's RCB force tree hot path: the tree build over a
+ * rank's particles, the per-leaf interaction lists and the polynomial
+ * short-range force law evaluated over every (leaf particle, list entry)
+ * pair, fused with the sub-cycle velocity kick.  The pair evaluation runs as
+ * hand-written CUDA kernels for sm_103a in FP32 on the CUDA cores.
+ *
+ * Reference interfaces replaced (paths inside the reference project):
+ *   hsr_rcb_kick      <- template<int TDPTS> RCBForceTree::RCBForceTree(...)
+ *                        src/halo_finder/RCBForceTree.h:96-124,
+ *                        src/halo_finder/RCBForceTree.cxx:336-450
+ *                        (build + list walk + nbody1 kick in one call)
+ *   hsr_subcycle      <- Particles::subCycle / map1 / map2
+ *                        src/cpu/Particles.cxx:1176-1201, 732-758, 1205-1367
+ *   hsr_force_law     <- ForceLawSR::f_over_r over FGridEvalPoly
+ *                        src/halo_finder/ForceLaw.cxx:137-141, 187-192
+ *
+ * Conventions: plain pointers and sizes only.  Particle arrays are the
+ * reference's SoA layout (POSVEL_T = float, ID_T = int64_t, MASK_T = uint16_t,
+ * src/halo_finder/BasicDefinition.h:60-91).  Every call returns an hsr_status;
+ * where the reference calls exit(1) or assert()s (tree reallocation during a
+ * parallel build, interaction list overflow), this library has no such limit
+ * and returns HSR_OK.  One context per host thread; a context owns its CUDA
+ * stream, device buffers and pinned staging memory.
+ */
+#ifndef HACC_SR_H
+#define HACC_SR_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t hsr_status;
+enum {
+  HSR_OK = 0,
+  HSR_ERR_ARG = 1,          /* invalid argument (null pointer, bad size, ...)   */
+  HSR_ERR_CUDA = 2,         /* a CUDA runtime call failed (see hsr_last_error)  */
+  HSR_ERR_NOMEM = 3,        /* host or device allocation failed                 */
+  HSR_ERR_TIMEOUT = 4,      /* a bounded device-side wait gave up               */
+  HSR_ERR_UNSUPPORTED = 5,  /* option combination not implemented               */
+  HSR_ERR_NO_DEVICE = 6,    /* no CUDA device / the library's kernels cannot run */
+  HSR_ERR_STATE = 7         /* call out of order (e.g. VJP before forward)      */
+};
+
+/* Where the particle arrays live. */
+enum { HSR_MEM_HOST = 0, HSR_MEM_DEVICE = 1 };
+
+/* Force laws.  POLY6: ForceLawSR over FGridEvalPoly, POLY_ORDER 6
+ * (src/halo_finder/ForceLaw.cxx:93-141,187-192): g(r2) = (r2+rsm^2)^-3/2 -
+ * sum_k a_k r2^k, with the pair weight m_i m_j.  POLY5_STEP16: the BG/Q
+ * kernel Step16_int (src/halo_finder/BGQStep16.c:23-189): 5th-order
+ * polynomial, weight m_j only, pairs with r2 == 0 dropped. */
+enum { HSR_LAW_POLY6 = 0, HSR_LAW_POLY5_STEP16 = 1 };
+
+/* Kernel variants for the pair evaluation (same results up to FP32
+ * summation order). */
+enum {
+  HSR_KERNEL_AUTO = 0,      /* batched persistent kernel, autotuned shape      */
+  HSR_KERNEL_PLAIN = 1,     /* one CTA per leaf, every list entry evaluated    */
+  HSR_KERNEL_BATCHED = 2    /* persistent CTAs over a work queue of tiles       */
+};
+
+/* RCBForceTree constructor arguments (src/halo_finder/RCBForceTree.h:96-124).
+ * ForceLaw *fl is replaced by `law` + `rsm` (the law's softening). */
+typedef struct hsr_params {
+  float min[3], max[3];             /* minLoc, maxLoc: root bounding box        */
+  float min_force[3], max_force[3]; /* minForceLoc, maxForceLoc                 */
+  float avg_mass;                   /* avgMass (accepted, unused as in the ref) */
+  float fsrrmax;                    /* fsm: cutoff radius                       */
+  float rsm;                        /* softening of the force law               */
+  float open_angle;                 /* oa, radians                              */
+  int64_t nd;                       /* leaf size                                */
+  int64_t ds;                       /* depth safety (accepted, unused)          */
+  int64_t tmin;                     /* task size (accepted, unused)             */
+  float fcoeff;                     /* kick coefficient                         */
+  float ppc;                        /* pseudo-particle contraction factor       */
+  int32_t tdpts;                    /* 1 = monopole, 12 = quadrupole            */
+  int32_t law;                      /* HSR_LAW_*                                */
+  int32_t kernel;                   /* HSR_KERNEL_*                             */
+  int32_t reserved;
+} hsr_params;
+
+/* Statistics of the last call on a context. */
+typedef struct hsr_stats {
+  int64_t n;                 /* particles in the tree                           */
+  int64_t nodes;             /* tree nodes                                      */
+  int64_t leaves;            /* non-empty leaves                                */
+  int64_t processed_leaves;  /* leaves inside the force box                     */
+  int64_t list_entries;      /* sum of list lengths (self included)             */
+  int64_t pairs;             /* sum over processed leaves of count * list length */
+  int64_t kernel_launches;   /* CUDA kernels this call launched                 */
+  double t_build_ms;         /* host: tree build                                */
+  double t_walk_ms;          /* host: interaction lists                         */
+  double t_force_ms;         /* device: pair kernel, CUDA events                */
+  double t_total_ms;         /* wall time of the whole call                     */
+  int64_t h2d_bytes;         /* bytes copied host -> device by the call         */
+  int64_t d2h_bytes;         /* bytes copied device -> host by the call         */
+} hsr_stats;
+
+typedef struct hsr_ctx hsr_ctx;
+
+/* Creates a context on CUDA device `device` (its own stream and buffers). */
+hsr_status hsr_create(hsr_ctx **ctx, int device);
+hsr_status hsr_destroy(hsr_ctx *ctx);
+/* Message of the last error on this context (static storage, never NULL). */
+const char *hsr_last_error(const hsr_ctx *ctx);
+/* Library version string. */
+const char *hsr_version(void);
+
+/* The RCBForceTree constructor: builds the RCB tree over the n particles
+ * (permuting all ten arrays in place exactly as the reference does), builds
+ * the interaction list of every leaf inside the force box and adds
+ * fcoeff * sum_j m_i m_j g(r2_ij) (x_j - x_i) to v_i for r2_ij < fsrrmax^2.
+ * mem: HSR_MEM_HOST (any host memory).  Synchronous: the arrays hold the
+ * result when the call returns. */
+hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, float *y,
+                        float *z, float *vx, float *vy, float *vz, float *mass, float *phi,
+                        int64_t *id, uint16_t *mask, int32_t mem);
+
+hsr_status hsr_get_stats(const hsr_ctx *ctx, hsr_stats *st);
+
+/* Interaction lists of the last hsr_rcb_kick, for inspection and parity
+ * checks.  hsr_lists_size gives the number of processed leaves and of list
+ * entries; hsr_lists_export fills leaf_offset/leaf_count (per leaf, into the
+ * permuted arrays), list_ptr (nleaves+1) and the entries as the reference's
+ * nx/ny/nz/nm arrays would hold them (any order within a leaf). */
+hsr_status hsr_lists_size(const hsr_ctx *ctx, int64_t *nleaves, int64_t *nentries);
+hsr_status hsr_lists_export(const hsr_ctx *ctx, int64_t *leaf_offset, int64_t *leaf_count,
+                            int64_t *list_ptr, float *ex, float *ey, float *ez, float *em);
+
+/* Host-only tree build and interaction lists, no device work: the same tree,
+ * permutation and lists as hsr_rcb_kick (the ten arrays are permuted in
+ * place, velocities are not kicked), kept in a standalone handle.  Replaces
+ * the build and list halves of the RCBForceTree constructor
+ * (src/halo_finder/RCBForceTree.cxx:892-918, 923-1197) for callers that
+ * evaluate the pairs themselves; also what the CPU test suite uses to check
+ * the lists without a GPU. */
+typedef struct hsr_lists hsr_lists;
+hsr_status hsr_build_lists(const hsr_params *p, int64_t n, float *x, float *y, float *z,
+                           float *vx, float *vy, float *vz, float *mass, float *phi, int64_t *id,
+                           uint16_t *mask, hsr_lists **out);
+/* nleaves/nentries as hsr_lists_size; stats as hsr_get_stats (no timings of
+ * device work). */
+hsr_status hsr_lists_info(const hsr_lists *L, int64_t *nleaves, int64_t *nentries, hsr_stats *st);
+hsr_status hsr_lists_get(const hsr_lists *L, int64_t *leaf_offset, int64_t *leaf_count,
+                         int64_t *list_ptr, float *ex, float *ey, float *ez, float *em);
+/* Position-table index of every entry: < n is a particle (post-permutation
+ * index), >= n a pseudo-particle. */
+hsr_status hsr_lists_index(const hsr_lists *L, int64_t *entry_index);
+hsr_status hsr_lists_free(hsr_lists *L);
+
+/* ForceLawSR::f_over_r on the device for a batch of r2 values (host arrays),
+ * with the kernel's own FP32 arithmetic; for law tests. */
+hsr_status hsr_force_law(hsr_ctx *ctx, int32_t law, float rsm, float fsrrmax, int64_t n,
+                         const float *r2, float *g);
+
+/* ---- diagnostics ------------------------------------------------------- */
+
+/* Relaunches the pair kernel of the last hsr_rcb_kick `iters` times on the
+ * work still resident on the device (the velocities keep accumulating kicks),
+ * each launch timed with CUDA events on the context's stream.  flush_l2 != 0
+ * overwrites a 256 MB device buffer before every launch so no launch starts
+ * with the previous one's data in L2.  *ms_per_launch is the mean time. */
+hsr_status hsr_bench_pairs(hsr_ctx *ctx, int32_t kernel, int32_t iters, int32_t flush_l2,
+                           double *ms_per_launch);
+
+/* Measures this device's FP32 FMA throughput with a kernel of independent
+ * fused multiply-add chains (2 flops each) on every SM; the roofline
+ * denominator of the pair kernels. */
+hsr_status hsr_probe_fp32_peak(hsr_ctx *ctx, double *tflops);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* HACC_SR_H */

@@ -1,0 +1,122 @@
+"""The C-ABI library on a CPU-only machine: it loads, exports every function
+include/*.h declares, refuses to run without a device, and its host-side tree
+and interaction lists equal the oracle's exactly."""
+import ctypes as C
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+import hsr
+import synth
+from hsr_testutil import golden_names, load_golden, same_lists
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def header_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        text = open(h).read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        names |= set(re.findall(r"^\s*(?:hsr_status|const char \*|void)\s*\**\s*(hsr_\w+)\s*\(",
+                                text, flags=re.M))
+    return sorted(names)
+
+
+def test_header_declares_functions():
+    assert len(header_functions()) >= 10
+
+
+@pytest.mark.parametrize("name", header_functions())
+def test_library_exports(hsr_lib, name):
+    assert hasattr(hsr_lib, name), f"{name} declared in include/ but not exported"
+
+
+def test_python_binding_lists_every_export(hsr_lib):
+    assert set(header_functions()) == set(hsr.EXPORTS)
+
+
+def test_version(hsr_lib):
+    assert b"sm_103a" in hsr_lib.hsr_version()
+
+
+def _has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
+
+
+@pytest.mark.skipif(_has_gpu(), reason="a CUDA device is present")
+def test_create_without_device_fails_loudly(hsr_lib):
+    h = C.c_void_p()
+    assert hsr_lib.hsr_create(C.byref(h), 0) == 6  # HSR_ERR_NO_DEVICE
+    with pytest.raises(hsr.HsrError):
+        hsr.Context(0)
+
+
+@pytest.mark.parametrize("name", golden_names())
+def test_host_tree_permutation_matches_golden(hsr_lib, name):
+    p, kp, out = load_golden(name)
+    L = hsr.HostLists(p, kp)
+    for k in ("x", "y", "z", "mass", "phi", "id", "mask"):
+        assert np.array_equal(getattr(p, k).view(np.uint8), out[k].view(np.uint8)), f"{name}: {k}"
+    assert L.nleaves >= 1 or p.n == 0
+
+
+@pytest.mark.parametrize("case", ["zel16_nd32", "zel16_nd16_quad", "zel16_oa05_nd8", "random_nd1"])
+def test_host_lists_equal_oracle_lists(hsr_lib, oracle_lib, case):
+    if case.startswith("zel16"):
+        p = synth.zeldovich_box(16, z=10.0, seed=4)
+        nd = int(case.split("nd")[-1].split("_")[0])
+        kp = synth.kick_params(p, nd=nd, tdpts=12 if "quad" in case else 1,
+                               open_angle=0.5 if "oa05" in case else 0.1)
+    else:
+        p = synth.random_box(600, 8.0, 3)
+        kp = synth.kick_params(p, nd=1)
+        kp.min_force, kp.max_force = (0.5,) * 3, (7.5,) * 3
+    q = p.copy()
+    L = hsr.HostLists(p, kp)
+    r = oracle_lib.rcb_run(q, kp, keep_lists=True, do_kick=False, nthreads=2)
+    for k in ("x", "y", "z", "mass", "phi", "id", "mask", "vx"):
+        assert np.array_equal(getattr(p, k).view(np.uint8), getattr(q, k).view(np.uint8)), k
+    off, cnt, ptr, e = L.get()
+    ooff, ocnt, optr = r.leaves()
+    assert L.stats["pairs"] == r.stats["pairs"]
+    assert L.stats["list_entries"] == r.stats["list_entries"]
+    assert same_lists(off, cnt, ptr, e, ooff, ocnt, optr, r.entries())
+
+
+def test_host_lists_index_points_at_entries(hsr_lib):
+    p = synth.zeldovich_box(8, seed=2)
+    kp = synth.kick_params(p, nd=16)
+    L = hsr.HostLists(p, kp)
+    off, cnt, ptr, e = L.get()
+    idx = L.index()
+    real = idx < p.n
+    assert np.array_equal(e[0][real], p.x[idx[real]])
+    assert np.array_equal(e[3][real], p.mass[idx[real]])
+
+
+@pytest.mark.parametrize("bad", ["tdpts", "nd", "n", "null"])
+def test_bad_arguments_rejected(hsr_lib, bad):
+    p = synth.random_box(10, 4.0, 1)
+    kp = synth.kick_params(p, nd=4)
+    P = hsr.make_params(kp)
+    args = hsr._particle_args(p)
+    n = p.n
+    if bad == "tdpts":
+        P.tdpts = 3
+    elif bad == "nd":
+        P.nd = 0
+    elif bad == "n":
+        n = -1
+    else:
+        args[3] = C.cast(None, C.POINTER(C.c_float))
+    h = C.c_void_p()
+    assert hsr_lib.hsr_build_lists(C.byref(P), n, *args, C.byref(h)) == 1
+    assert not h.value

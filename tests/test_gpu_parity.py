@@ -1,0 +1,203 @@
+"""Parity of the GPU path (through the C ABI) with the reference and the oracle.
+
+Tolerances: FP32 forces within RMS_TOL = 1e-5 rms relative and MAX_TOL = 1e-3
+of the rms force (hsr_testutil.force_errors); every integer/index result (the
+tree permutation, positions, ids, masks, the list entries) bit-exact.
+"""
+import numpy as np
+import pytest
+
+import hsr
+import synth
+from hsr_testutil import (MAX_TOL, RMS_TOL, force_errors, golden_names, load_golden,
+                          same_lists, vel)
+
+pytestmark = pytest.mark.gpu
+
+EXACT = ("x", "y", "z", "mass", "phi", "id", "mask")
+
+
+@pytest.mark.parametrize("kernel", [hsr.KERNEL_PLAIN, hsr.KERNEL_AUTO])
+@pytest.mark.parametrize("name", golden_names())
+def test_golden_kick(ctx, name, kernel):
+    p, kp, out = load_golden(name)
+    v_in = p.copy()
+    hsr.HostLists(v_in, kp)  # the input velocities in the tree's order
+    st = ctx.rcb_kick(p, kp, kernel=kernel)
+    for k in EXACT:
+        assert np.array_equal(getattr(p, k).view(np.uint8), out[k].view(np.uint8)), f"{name}: {k}"
+    dv = vel(p) - vel(v_in)
+    dv_ref = np.stack([out["vx"], out["vy"], out["vz"]], 1).astype(np.float64) - vel(v_in)
+    rms, mx = force_errors(dv, dv_ref)
+    # The reference adds every pair term straight into v, so its kick carries
+    # FP32 rounding of |v| per term; allow for that where v_in is not zero.
+    vscale = np.abs(vel(v_in)).max(initial=0.0)
+    dscale = np.sqrt((dv_ref ** 2).sum(1).mean()) if p.n else 1.0
+    slack = 0.0 if vscale == 0 else 64 * 2.0 ** -24 * vscale / dscale
+    assert rms <= RMS_TOL + slack, (name, rms, slack)
+    assert mx <= MAX_TOL + slack, (name, mx, slack)
+    assert st["kernel_launches"] >= (1 if st["processed_leaves"] else 0)
+
+
+def _zero_v(p):
+    p.vx[:] = 0
+    p.vy[:] = 0
+    p.vz[:] = 0
+    return p
+
+
+@pytest.mark.parametrize("nd,tdpts", [(64, 1), (128, 1), (32, 12)])
+def test_zeldovich32_forces_vs_oracle(ctx, oracle_lib, nd, tdpts):
+    """32^3 lattice at z=50 with overload ghosts (the one-PM-step case): GPU
+    forces vs the oracle's (the reference's arithmetic) and vs FP64 over the
+    same lists; lists bit-exact."""
+    p = _zero_v(synth.zeldovich_box(32))
+    kp = synth.kick_params(p, nd=nd, tdpts=tdpts, fcoeff=1.0)
+    q = p.copy()
+    ctx.rcb_kick(p, kp, kernel=hsr.KERNEL_AUTO)
+    r = oracle_lib.rcb_run(q, kp, keep_lists=True, nthreads=0)
+    for k in EXACT:
+        assert np.array_equal(getattr(p, k).view(np.uint8), getattr(q, k).view(np.uint8)), k
+    off, cnt, ptr = r.leaves()
+    sel = np.concatenate([np.arange(o, o + c) for o, c in zip(off, cnt)])
+    rms, mx = force_errors(vel(p)[sel], vel(q)[sel])
+    assert rms <= RMS_TOL and mx <= MAX_TOL, (rms, mx)
+    a64 = r.acc_fp64()[sel]
+    rms64, mx64 = force_errors(vel(p)[sel], a64)
+    assert rms64 <= RMS_TOL and mx64 <= MAX_TOL, (rms64, mx64)
+    goff, gcnt, gptr, ge = ctx.lists()
+    assert same_lists(goff, gcnt, gptr, ge, off, cnt, ptr, r.entries())
+    assert ctx.stats()["pairs"] == r.stats["pairs"]
+
+
+def test_plain_and_batched_agree(ctx):
+    p = _zero_v(synth.zeldovich_box(32, z=10.0, seed=3))
+    kp = synth.kick_params(p, nd=128, fcoeff=1.0)
+    q = p.copy()
+    ctx.rcb_kick(p, kp, kernel=hsr.KERNEL_PLAIN)
+    ctx.rcb_kick(q, kp, kernel=hsr.KERNEL_BATCHED)
+    rms, mx = force_errors(vel(q), vel(p))
+    assert rms <= RMS_TOL and mx <= MAX_TOL
+
+
+def test_force_law_on_device(ctx, oracle_lib):
+    r2 = np.linspace(0.0, 10.0, 4001).astype(np.float32)
+    g = ctx.force_law(r2)
+    rmax2 = np.float32(3.116326355) ** 2
+    for x, gx in zip(r2, g):
+        if x < rmax2:
+            g64 = oracle_lib.law_f64(0, 0.1, float(x))
+            assert abs(gx - g64) <= 1e-6 * max(float(x + 0.01) ** -1.5, 0.3), (x, gx, g64)
+        else:
+            assert gx == 0.0
+    # the cutoff is strict at fsrrmax^2 and inclusive of the law's own r2max
+    g2 = ctx.force_law(np.array([np.nextafter(rmax2, 0, dtype=np.float32), rmax2], np.float32))
+    assert g2[0] != 0.0 and g2[1] == 0.0
+
+
+def test_linear_in_fcoeff(ctx):
+    """v_out = fcoeff * m * a: doubling fcoeff doubles the kick bit for bit."""
+    p = _zero_v(synth.zeldovich_box(24, z=10.0, seed=8))
+    kp = synth.kick_params(p, nd=64, fcoeff=0.375)
+    q = p.copy()
+    ctx.rcb_kick(p, kp)
+    kp.fcoeff = 0.75
+    ctx.rcb_kick(q, kp)
+    assert np.array_equal(2 * vel(p), vel(q))
+
+
+def test_momentum_conserved_with_symmetric_lists(ctx):
+    """Opening angle 0 opens every node, so every list holds whole leaves whose
+    boxes lie within fsrrmax of the target leaf: the pair set is symmetric and
+    the pair forces cancel, sum_i m_i a_i = 0 up to FP32 rounding."""
+    p = _zero_v(synth.random_box(6000, 14.0, 17))
+    kp = synth.kick_params(p, nd=32, open_angle=0.0, fcoeff=1.0)
+    kp.min_force, kp.max_force = (-1.0,) * 3, (15.0,) * 3
+    ctx.rcb_kick(p, kp)
+    a = vel(p)
+    total = np.abs((a * p.mass[:, None]).sum(0))
+    scale = np.abs(a).sum(0)
+    assert np.all(total <= 1e-5 * scale), (total, scale)
+
+
+@pytest.mark.parametrize("case", ["empty", "one", "coincident", "nd1", "outside"])
+def test_edge_cases(ctx, oracle_lib, case):
+    if case == "empty":
+        p = synth.random_box(0, 4.0, 1)
+    elif case == "one":
+        p = synth.random_box(1, 4.0, 1)
+    elif case == "coincident":  # one split fails: a leaf far above nd
+        p = synth.random_box(300, 4.0, 1)
+        p.x[:200] = 2.0
+        p.y[:200] = 2.0
+        p.z[:200] = 2.0
+    elif case == "nd1":
+        p = synth.random_box(400, 6.0, 2)
+    else:  # nothing inside the force box
+        p = synth.random_box(500, 6.0, 3)
+    p = _zero_v(p)
+    kp = synth.kick_params(p, nd=1 if case == "nd1" else 16, fcoeff=1.0)
+    if case == "outside":
+        kp.min_force, kp.max_force = (20.0,) * 3, (30.0,) * 3
+    else:
+        kp.min_force, kp.max_force = (-1.0,) * 3, (9.0,) * 3
+    q = p.copy()
+    st = ctx.rcb_kick(p, kp)
+    r = oracle_lib.rcb_run(q, kp, nthreads=2)
+    assert st["pairs"] == r.stats["pairs"]
+    for k in EXACT:
+        assert np.array_equal(getattr(p, k).view(np.uint8), getattr(q, k).view(np.uint8)), k
+    if p.n:
+        rms, mx = force_errors(vel(p), vel(q))
+        assert rms <= RMS_TOL and mx <= MAX_TOL, (rms, mx)
+
+
+def test_repeated_calls_reuse_buffers(ctx):
+    """Shrinking and growing inputs on one context give the same answers as
+    fresh calls."""
+    big = _zero_v(synth.zeldovich_box(20, seed=1))
+    small = _zero_v(synth.zeldovich_box(10, seed=2))
+    kb, ks = synth.kick_params(big, nd=64, fcoeff=1.0), synth.kick_params(small, nd=64, fcoeff=1.0)
+    outs = []
+    for p, kp in ((big, kb), (small, ks), (big, kb)):
+        q = p.copy()
+        ctx.rcb_kick(q, kp)
+        outs.append(vel(q))
+    assert np.array_equal(outs[0], outs[2])
+
+
+def test_full_size_128_sampled_leaves_vs_fp64(ctx):
+    """128^3 at z=50 (the plain-vs-batched workload) through the C ABI: the
+    permutation keeps every particle, and the forces of a sample of leaves
+    match an FP64 evaluation of the exported lists."""
+    p = _zero_v(synth.zeldovich_box(128))
+    ids_in = np.sort(p.id)
+    kp = synth.kick_params(p, nd=128, fcoeff=1.0)
+    st = ctx.rcb_kick(p, kp)
+    assert np.array_equal(np.sort(p.id), ids_in)
+    off, cnt, ptr, e = ctx.lists()
+    rng = np.random.default_rng(0)
+    a_gpu, a64 = [], []
+    for l in rng.choice(len(off), 40, replace=False):
+        o, c = off[l], cnt[l]
+        E = e[:, ptr[l]:ptr[l + 1]].astype(np.float64)
+        xi = np.stack([p.x[o:o + c], p.y[o:o + c], p.z[o:o + c]], 1).astype(np.float64)
+        d = E[:3].T[None, :, :] - xi[:, None, :]
+        r2 = (d ** 2).sum(-1)
+        g = _g64(r2)
+        w = g * E[3][None, :] * (r2 < float(np.float32(3.116326355) ** 2))
+        a64.append((w[:, :, None] * d).sum(1) * p.mass[o:o + c, None])
+        a_gpu.append(vel(p)[o:o + c])
+    rms, mx = force_errors(np.concatenate(a_gpu), np.concatenate(a64))
+    assert rms <= RMS_TOL and mx <= MAX_TOL, (rms, mx)
+    assert st["pairs"] > 1e9
+
+
+def _g64(r2, rsm=float(np.float32(0.1))):
+    a = [0.271431, -0.0783394, 0.0133122, -0.00159485, 0.000132336, -0.00000663394,
+         0.000000147305]
+    a = [float(np.float32(v)) for v in a]
+    p = np.zeros_like(r2)
+    for c in a[::-1]:
+        p = p * r2 + c
+    return (r2 + rsm * rsm) ** -1.5 - p
