@@ -80,6 +80,16 @@ float cut2(int law, float fsrrmax) {
   return std::min(fs2, std::nextafter(r2max, std::numeric_limits<float>::infinity()));
 }
 
+// Squared distance bound of the batched kernel's box test: entries farther
+// than this from a group's bounding box are skipped.  It sits 1e-4 (relative)
+// above the pair cutoff, far beyond the few-ulp error of an FP32 r2, so every
+// skipped pair would have failed the pair mask anyway.
+float cull2(float rc2) { return rc2 * 1.0001f + 1e-6f; }
+
+// Longest list range one batched item covers; longer lists are split over
+// several items that add into the velocities with atomics.
+constexpr int64_t kJSplit = 8192;
+
 }  // namespace
 
 struct hsr_ctx {
@@ -98,7 +108,31 @@ struct hsr_ctx {
   int last_law = 0;
   int64_t last_nleaves = 0;
   float last_fcoeff = 0, last_rsm2 = 0, last_rc2 = 0;
-  DevBuf d_flush, d_probe;
+  DevBuf d_flush, d_probe, d_items, d_gidx, d_queue;
+  PinBuf h_items, h_gidx;
+  int last_kernel = HSR_KERNEL_BATCHED;
+  int64_t last_nitems = 0;
+  float last_rcull2 = 0;
+  int batched_ctas = 0;
+
+  // Launches the last kick's pair kernel on the resident work (the
+  // batched kernel's queue counter is reset first).
+  cudaError_t launch_pairs(int kernel) {
+    float *dv = d_vel.as<float>();
+    const int64_t n = last_n;
+    if (kernel == HSR_KERNEL_PLAIN)
+      return hsr::launch_leaf_plain(last_law, d_pos.as<float4>(), d_leaves.as<hsr::LeafDesc>(),
+                                    last_nleaves, d_idx.as<int32_t>(), dv, dv + n, dv + 2 * n,
+                                    last_fcoeff, last_rsm2, last_rc2, stream);
+    if (batched_ctas == 0) batched_ctas = hsr::batched_resident_ctas(device);
+    cudaError_t e = cudaMemsetAsync(d_queue.p, 0, 2 * sizeof(unsigned long long), stream);
+    if (e != cudaSuccess) return e;
+    return hsr::launch_pairs_batched(last_law, d_pos.as<float4>(), d_items.as<hsr::PairItem>(),
+                                     last_nitems, d_gidx.as<int32_t>(), d_idx.as<int32_t>(), dv,
+                                     dv + n, dv + 2 * n, last_fcoeff, last_rsm2, last_rc2,
+                                     last_rcull2, d_queue.as<unsigned long long>(), batched_ctas,
+                                     stream);
+  }
 
   hsr_status fail(hsr_status s, const std::string &msg) {
     err = msg;
@@ -152,9 +186,10 @@ hsr_status hsr_destroy(hsr_ctx *ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf *b : {&ctx->d_pos, &ctx->d_vel, &ctx->d_leaves, &ctx->d_segs, &ctx->d_idx, &ctx->d_law,
-                    &ctx->d_flush, &ctx->d_probe})
+                    &ctx->d_flush, &ctx->d_probe, &ctx->d_items, &ctx->d_gidx, &ctx->d_queue})
     b->release();
-  for (PinBuf *b : {&ctx->h_pos, &ctx->h_vel, &ctx->h_leaves, &ctx->h_segs}) b->release();
+  for (PinBuf *b : {&ctx->h_pos, &ctx->h_vel, &ctx->h_leaves, &ctx->h_segs, &ctx->h_items, &ctx->h_gidx})
+    b->release();
   if (ctx->ev0) cudaEventDestroy(ctx->ev0);
   if (ctx->ev1) cudaEventDestroy(ctx->ev1);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -235,7 +270,8 @@ PlanSizes host_build(hsr::RcbHost &H, const hsr_params *p, int64_t n, const floa
 // leaf/segment descriptors (may be null).
 void host_fill(hsr::RcbHost &H, int64_t n, float *x, float *y, float *z, float *vx, float *vy,
                float *vz, float *mass, float *phi, int64_t *id, uint16_t *mask, float *tab,
-               float *vel, hsr::LeafDesc *ld, hsr::SegDesc *sd) {
+               float *vel, hsr::LeafDesc *ld, hsr::SegDesc *sd,
+               std::vector<int64_t> *list_begin = nullptr) {
   const auto &el = H.elems();
   hsr::Pool &pool = H.pool();
   pool.parallel_for(n, 1 << 15, [&](int64_t b, int64_t e) {
@@ -296,6 +332,7 @@ void host_fill(hsr::RcbHost &H, int64_t n, float *x, float *y, float *z, float *
     lb[l] = run;
     run += leaves[l].list_len;
   }
+  if (list_begin) *list_begin = lb;
   pool.parallel_for(nl, 64, [&](int64_t b, int64_t e) {
     for (int64_t l = b; l < e; ++l) {
       const auto &L = leaves[l];
@@ -344,6 +381,84 @@ void export_lists(const hsr::RcbHost &H, const float *tab, int64_t *leaf_offset,
   if (list_ptr) list_ptr[H.leaves().size()] = run;
 }
 
+// Splits each processed leaf into ceil(count/32) spatially compact groups
+// (recursive halving along the longest axis, left part a multiple of 32) and
+// emits one batched-kernel item per group and list chunk of at most `jsplit`
+// entries, sorted by list length, longest first.  gidx has n entries: each
+// leaf's range holds a permutation of its particles, grouped.
+void make_items(hsr::RcbHost &H, const std::vector<int64_t> &list_begin, int64_t jsplit,
+                std::vector<int32_t> &gidx, std::vector<hsr::PairItem> &items) {
+  const auto &leaves = H.leaves();
+  const auto &el = H.elems();
+  const int64_t nl = int64_t(leaves.size());
+  gidx.resize(size_t(H.n()));
+  std::vector<int64_t> item_base(size_t(nl) + 1, 0);
+  for (int64_t l = 0; l < nl; ++l) {
+    const int64_t ng = std::max<int64_t>(0, (leaves[l].count + 31) / 32);
+    const int64_t nch = std::max<int64_t>(1, (leaves[l].list_len + jsplit - 1) / jsplit);
+    item_base[l + 1] = item_base[l] + ng * nch;
+  }
+  items.resize(size_t(item_base[nl]));
+  H.pool().parallel_for(nl, 16, [&](int64_t b, int64_t e) {
+    std::vector<int32_t> tmp;
+    std::vector<std::pair<int32_t, int32_t>> stack, out;
+    for (int64_t l = b; l < e; ++l) {
+      const auto &L = leaves[l];
+      if (L.count <= 0) continue;  // an empty root leaf has no groups and no items
+      tmp.resize(size_t(L.count));
+      for (int64_t i = 0; i < L.count; ++i) tmp[i] = int32_t(L.offset + i);
+      out.clear();
+      stack.assign(1, {0, int32_t(L.count)});
+      while (!stack.empty()) {
+        auto [a, c] = stack.back();
+        stack.pop_back();
+        if (c <= 32) {
+          if (c > 0) out.push_back({a, c});
+          continue;
+        }
+        float lo[3] = {1e30f, 1e30f, 1e30f}, hi[3] = {-1e30f, -1e30f, -1e30f};
+        for (int32_t i = a; i < a + c; ++i) {
+          const hsr::Elem &q = el[tmp[i]];
+          const float v[3] = {q.x, q.y, q.z};
+          for (int d = 0; d < 3; ++d) {
+            lo[d] = std::min(lo[d], v[d]);
+            hi[d] = std::max(hi[d], v[d]);
+          }
+        }
+        int d = 0;
+        for (int k = 1; k < 3; ++k)
+          if (hi[k] - lo[k] > hi[d] - lo[d]) d = k;
+        const int32_t ng = (c + 31) / 32;
+        const int32_t left = 32 * ((ng + 1) / 2);
+        auto key = [&](int32_t i) {
+          const hsr::Elem &q = el[i];
+          return d == 0 ? q.x : d == 1 ? q.y : q.z;
+        };
+        std::nth_element(tmp.begin() + a, tmp.begin() + a + left, tmp.begin() + a + c,
+                         [&](int32_t u, int32_t v) { return key(u) < key(v); });
+        stack.push_back({a + left, c - left});
+        stack.push_back({a, left});
+      }
+      std::copy(tmp.begin(), tmp.end(), gidx.begin() + L.offset);
+      const int64_t nch = std::max<int64_t>(1, (L.list_len + jsplit - 1) / jsplit);
+      int64_t k = item_base[l];
+      for (const auto &g : out)
+        for (int64_t c = 0; c < nch; ++c) {
+          hsr::PairItem it{};
+          it.j_begin = list_begin[l] + c * jsplit;
+          it.j_len = int32_t(std::min<int64_t>(jsplit, L.list_len - c * jsplit));
+          it.g_begin = int32_t(L.offset + g.first);
+          it.g_count = g.second;
+          it.flags = nch > 1 ? 1 : 0;
+          items[k++] = it;
+        }
+    }
+  });
+  std::stable_sort(items.begin(), items.end(), [](const hsr::PairItem &a, const hsr::PairItem &b) {
+    return a.j_len > b.j_len;
+  });
+}
+
 }  // namespace
 
 struct hsr_lists {
@@ -378,7 +493,20 @@ hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, 
   float *hv = ctx->h_vel.as<float>();
   auto *hl = ctx->h_leaves.as<hsr::LeafDesc>();
   auto *hs = ctx->h_segs.as<hsr::SegDesc>();
-  host_fill(H, n, x, y, z, vx, vy, vz, mass, phi, id, mask, hp, hv, hl, hs);
+  std::vector<int64_t> list_begin;
+  host_fill(H, n, x, y, z, vx, vy, vz, mass, phi, id, mask, hp, hv, hl, hs, &list_begin);
+  const bool plain = p->kernel == HSR_KERNEL_PLAIN;
+  int64_t nitems = 0;
+  if (!plain) {
+    std::vector<int32_t> gidx;
+    std::vector<hsr::PairItem> items;
+    make_items(H, list_begin, kJSplit, gidx, items);
+    nitems = int64_t(items.size());
+    CU(ctx->h_items.ensure(std::max<size_t>(items.size(), 1) * sizeof(hsr::PairItem)), "cudaHostAlloc(items)");
+    CU(ctx->h_gidx.ensure(std::max<size_t>(gidx.size(), 1) * 4), "cudaHostAlloc(gidx)");
+    std::memcpy(ctx->h_items.p, items.data(), items.size() * sizeof(hsr::PairItem));
+    std::memcpy(ctx->h_gidx.p, gidx.data(), gidx.size() * 4);
+  }
 
   cudaStream_t s = ctx->stream;
   CU(ctx->d_pos.ensure(size_t(std::max<int64_t>(ps.ntab, 1)) * 16), "cudaMalloc(pos)");
@@ -388,28 +516,50 @@ hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, 
   CU(ctx->d_segs.ensure(size_t(std::max<int64_t>(ps.nsegs, 1)) * sizeof(hsr::SegDesc)),
      "cudaMalloc(segs)");
   CU(ctx->d_idx.ensure(size_t(std::max<int64_t>(ps.nidx, 1)) * 4), "cudaMalloc(idx)");
+  CU(ctx->d_queue.ensure(64), "cudaMalloc(queue)");
   CU(cudaMemcpyAsync(ctx->d_pos.p, hp, size_t(ps.ntab) * 16, cudaMemcpyHostToDevice, s), "H2D pos");
   CU(cudaMemcpyAsync(ctx->d_vel.p, hv, size_t(3 * n) * 4, cudaMemcpyHostToDevice, s), "H2D vel");
   CU(cudaMemcpyAsync(ctx->d_leaves.p, hl, size_t(ps.nleaves) * sizeof(hsr::LeafDesc),
                      cudaMemcpyHostToDevice, s), "H2D leaves");
   CU(cudaMemcpyAsync(ctx->d_segs.p, hs, size_t(ps.nsegs) * sizeof(hsr::SegDesc),
                      cudaMemcpyHostToDevice, s), "H2D segs");
+  int64_t h2d_items = 0;
+  if (!plain) {
+    CU(ctx->d_items.ensure(size_t(std::max<int64_t>(nitems, 1)) * sizeof(hsr::PairItem)), "cudaMalloc(items)");
+    CU(ctx->d_gidx.ensure(size_t(std::max<int64_t>(n, 1)) * 4), "cudaMalloc(gidx)");
+    CU(cudaMemcpyAsync(ctx->d_items.p, ctx->h_items.p, size_t(nitems) * sizeof(hsr::PairItem),
+                       cudaMemcpyHostToDevice, s), "H2D items");
+    CU(cudaMemcpyAsync(ctx->d_gidx.p, ctx->h_gidx.p, size_t(n) * 4, cudaMemcpyHostToDevice, s),
+       "H2D gidx");
+    h2d_items = nitems * int64_t(sizeof(hsr::PairItem)) + 4 * n;
+  }
   int64_t launches = 0;
   CU(hsr::launch_expand_segments(ctx->d_segs.as<hsr::SegDesc>(), ps.nsegs, ctx->d_idx.as<int32_t>(), s),
      "expand kernel");
   launches += ps.nsegs > 0;
-  float *dv = ctx->d_vel.as<float>();
   const float rsm2 = p->rsm * p->rsm;
   const float rc2 = cut2(p->law, p->fsrrmax);
+  ctx->last_n = n;
+  ctx->last_law = p->law;
+  ctx->last_nleaves = ps.nleaves;
+  ctx->last_fcoeff = p->fcoeff;
+  ctx->last_rsm2 = rsm2;
+  ctx->last_rc2 = rc2;
+  ctx->last_rcull2 = cull2(rc2);
+  ctx->last_kernel = plain ? HSR_KERNEL_PLAIN : HSR_KERNEL_BATCHED;
+  ctx->last_nitems = nitems;
   CU(cudaEventRecord(ctx->ev0, s), "event");
-  CU(hsr::launch_leaf_plain(p->law, ctx->d_pos.as<float4>(), ctx->d_leaves.as<hsr::LeafDesc>(),
-                            ps.nleaves, ctx->d_idx.as<int32_t>(), dv, dv + n, dv + 2 * n, p->fcoeff,
-                            rsm2, rc2, s),
-     "pair kernel");
-  launches += ps.nleaves > 0;
+  CU(ctx->launch_pairs(ctx->last_kernel), "pair kernel");
+  launches += plain ? ps.nleaves > 0 : nitems > 0;
   CU(cudaEventRecord(ctx->ev1, s), "event");
+  float *dv = ctx->d_vel.as<float>();
   CU(cudaMemcpyAsync(hv, dv, size_t(3 * n) * 4, cudaMemcpyDeviceToHost, s), "D2H vel");
+  unsigned long long counters[2] = {0, 0};
+  if (!plain) CU(cudaMemcpyAsync(counters, ctx->d_queue.p, sizeof(counters), cudaMemcpyDeviceToHost, s),
+                 "D2H counters");
   CU(cudaStreamSynchronize(s), "kernel execution");
+  // the plain kernel evaluates every listed pair for every lane of a warp
+  st.evaluated_pairs = plain ? H.padded_pairs() : int64_t(counters[1]);
   float fms = 0;
   CU(cudaEventElapsedTime(&fms, ctx->ev0, ctx->ev1), "event time");
   st.t_force_ms = fms;
@@ -421,19 +571,14 @@ hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, 
     }
   });
   st.kernel_launches = launches;
+  st.work_items = nitems;
   st.h2d_bytes = ps.ntab * 16 + 3 * n * 4 + ps.nleaves * int64_t(sizeof(hsr::LeafDesc)) +
-                 ps.nsegs * int64_t(sizeof(hsr::SegDesc));
-  st.d2h_bytes = 3 * n * 4;
+                 ps.nsegs * int64_t(sizeof(hsr::SegDesc)) + h2d_items;
+  st.d2h_bytes = 3 * n * 4 + (plain ? 0 : 16);
   st.t_total_ms = ms_since(t_start);
   ctx->stats = st;
   ctx->have_lists = true;
-  ctx->last_n = n;
   ctx->last_tdpts = p->tdpts;
-  ctx->last_law = p->law;
-  ctx->last_nleaves = ps.nleaves;
-  ctx->last_fcoeff = p->fcoeff;
-  ctx->last_rsm2 = rsm2;
-  ctx->last_rc2 = rc2;
   return HSR_OK;
 }
 
@@ -468,8 +613,15 @@ hsr_status hsr_build_lists(const hsr_params *p, int64_t n, float *x, float *y, f
   L->host.reset(new hsr::RcbHost(std::max(1, nth)));
   const PlanSizes ps = host_build(*L->host, p, n, x, y, z, mass, L->st);
   L->tab.resize(size_t(std::max<int64_t>(ps.ntab, 1)) * 4);
-  host_fill(*L->host, n, x, y, z, vx, vy, vz, mass, phi, id, mask, L->tab.data(), nullptr, nullptr,
-            nullptr);
+  std::vector<hsr::LeafDesc> ld(static_cast<size_t>(std::max<int64_t>(ps.nleaves, 1)));
+  std::vector<hsr::SegDesc> sd(static_cast<size_t>(std::max<int64_t>(ps.nsegs, 1)));
+  std::vector<int64_t> list_begin;
+  host_fill(*L->host, n, x, y, z, vx, vy, vz, mass, phi, id, mask, L->tab.data(), nullptr, ld.data(),
+            sd.data(), &list_begin);
+  std::vector<int32_t> gidx;
+  std::vector<hsr::PairItem> items;
+  make_items(*L->host, list_begin, kJSplit, gidx, items);
+  L->st.work_items = int64_t(items.size());
   *out = L;
   return HSR_OK;
 }
@@ -523,21 +675,19 @@ hsr_status hsr_bench_pairs(hsr_ctx *ctx, int32_t kernel, int32_t iters, int32_t 
                            double *ms_per_launch) {
   if (!ctx || !ms_per_launch || iters < 1) return HSR_ERR_ARG;
   if (!ctx->have_lists) return ctx->fail(HSR_ERR_STATE, "no kick to replay");
-  (void)kernel;
+  // replays run the kick's own kernel unless the plain one is asked for
+  const int kk = kernel == HSR_KERNEL_PLAIN ? HSR_KERNEL_PLAIN : ctx->last_kernel;
+  if (kk == HSR_KERNEL_BATCHED && ctx->last_nitems == 0 && ctx->last_nleaves > 0)
+    return ctx->fail(HSR_ERR_STATE, "last kick had no batched work to replay");
   CU(cudaSetDevice(ctx->device), "cudaSetDevice");
   cudaStream_t s = ctx->stream;
   const size_t flush_bytes = size_t(256) << 20;
   if (flush_l2) CU(ctx->d_flush.ensure(flush_bytes), "cudaMalloc(flush)");
-  const int64_t n = ctx->last_n;
-  float *dv = ctx->d_vel.as<float>();
   double total = 0;
   for (int it = 0; it < iters; ++it) {
     if (flush_l2) CU(cudaMemsetAsync(ctx->d_flush.p, it & 0xff, flush_bytes, s), "L2 flush");
     CU(cudaEventRecord(ctx->ev0, s), "event");
-    CU(hsr::launch_leaf_plain(ctx->last_law, ctx->d_pos.as<float4>(), ctx->d_leaves.as<hsr::LeafDesc>(),
-                              ctx->last_nleaves, ctx->d_idx.as<int32_t>(), dv, dv + n, dv + 2 * n,
-                              ctx->last_fcoeff, ctx->last_rsm2, ctx->last_rc2, s),
-       "pair kernel");
+    CU(ctx->launch_pairs(kk), "pair kernel");
     CU(cudaEventRecord(ctx->ev1, s), "event");
     CU(cudaEventSynchronize(ctx->ev1), "pair kernel execution");
     float ms = 0;

@@ -340,6 +340,12 @@ void RcbHost::pseudo_table(float *out) const {
   });
 }
 
+int64_t RcbHost::padded_pairs() const {
+  int64_t s = 0;
+  for (const auto &L : leaves_) s += ((L.count + 31) / 32) * 32 * L.list_len;
+  return s;
+}
+
 int64_t RcbHost::nonempty_leaves() const {
   int64_t c = 0;
   for (int64_t t = 1; t < num_nodes_; ++t)

@@ -108,6 +108,8 @@ class RcbHost {
   const std::vector<Seg> &segs() const { return segs_; }
   int64_t list_entries() const { return list_entries_; }
   int64_t pairs() const { return pairs_; }
+  // pairs with each leaf's count rounded up to whole warps of 32
+  int64_t padded_pairs() const;
   int64_t nonempty_leaves() const;
   Pool &pool() { return pool_; }
   const TreeParams &params() const { return p_; }

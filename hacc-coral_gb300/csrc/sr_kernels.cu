@@ -1,6 +1,8 @@
 // sr_kernels.cu -- sm_103a kernels of the short-range pair interaction.
 #include "sr_kernels.cuh"
 
+#include <algorithm>
+
 namespace hsr {
 
 // ---------------------------------------------------------------------------
@@ -83,6 +85,118 @@ cudaError_t launch_leaf_plain(int law, const float4 *pos, const LeafDesc *leaves
   else
     k_leaf_plain<LAW_POLY6, NT><<<unsigned(nleaves), NT, 0, s>>>(pos, leaves, idx, vx, vy, vz,
                                                                  fcoeff, rsm2, rcut2);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
+// Batched persistent kernel.  Every warp works alone: it takes the next item
+// from the queue (items are sorted by cost, largest first), loads its group's
+// particles (one per lane) and the group's bounding box, then streams the
+// item's list range 32 entries at a time.  Each lane gathers one entry and
+// tests it against the box; the warp ballots, and only entries within the
+// cutoff of the box are evaluated, broadcast from the warp's shared-memory
+// slot.  The skipped entries are farther than fsrrmax from every particle of
+// the group (the test uses a bound slightly above fsrrmax^2), so the
+// reference's mask gives them an exactly zero contribution: the result is the
+// full list's, up to FP32 summation order.
+// ---------------------------------------------------------------------------
+constexpr int kBatchedWarps = 8;
+
+template <int LAW>
+__global__ void __launch_bounds__(32 * kBatchedWarps)
+    k_pairs_batched(const float4 *__restrict__ pos, const PairItem *__restrict__ items,
+                    int64_t nitems, const int32_t *__restrict__ gidx,
+                    const int32_t *__restrict__ idx, float *__restrict__ vx,
+                    float *__restrict__ vy, float *__restrict__ vz, float fcoeff, float rsm2,
+                    float rcut2, float rcull2, unsigned long long *__restrict__ queue) {
+  __shared__ float4 slot[kBatchedWarps][32];
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const unsigned full = 0xffffffffu;
+  unsigned long long evaluated = 0;  // (particle, entry) pairs this warp evaluated
+  for (;;) {
+    unsigned long long it = 0;
+    if (lane == 0) it = atomicAdd(queue, 1ull);
+    it = __shfl_sync(full, it, 0);
+    if (it >= (unsigned long long)nitems) break;
+    const PairItem W = items[it];
+    const bool act = lane < W.g_count;
+    const int pi = gidx[W.g_begin + (act ? lane : 0)];
+    const float4 P = pos[pi];
+    // group bounding box (inactive lanes repeat lane 0's particle)
+    float lox = P.x, hix = P.x, loy = P.y, hiy = P.y, loz = P.z, hiz = P.z;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lox = fminf(lox, __shfl_xor_sync(full, lox, o));
+      hix = fmaxf(hix, __shfl_xor_sync(full, hix, o));
+      loy = fminf(loy, __shfl_xor_sync(full, loy, o));
+      hiy = fmaxf(hiy, __shfl_xor_sync(full, hiy, o));
+      loz = fminf(loz, __shfl_xor_sync(full, loz, o));
+      hiz = fmaxf(hiz, __shfl_xor_sync(full, hiz, o));
+    }
+    float ax = 0.f, ay = 0.f, az = 0.f;
+    const int32_t *lst = idx + W.j_begin;
+    for (int j0 = 0; j0 < W.j_len; j0 += 32) {
+      const int j = j0 + lane;
+      const bool ok = j < W.j_len;
+      const float4 J = pos[lst[ok ? j : 0]];
+      const float dx = fmaxf(fmaxf(lox - J.x, J.x - hix), 0.f);
+      const float dy = fmaxf(fmaxf(loy - J.y, J.y - hiy), 0.f);
+      const float dz = fmaxf(fmaxf(loz - J.z, J.z - hiz), 0.f);
+      unsigned keep = __ballot_sync(full, ok && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < rcull2);
+      if (!keep) continue;
+      evaluated += (unsigned long long)__popc(keep) * (unsigned long long)W.g_count;
+      slot[w][lane] = J;
+      __syncwarp();
+      while (keep) {
+        const int b = __ffs(keep) - 1;
+        keep &= keep - 1;
+        pair_acc<LAW>(P.x, P.y, P.z, slot[w][b], rsm2, rcut2, ax, ay, az);
+      }
+      __syncwarp();
+    }
+    if (act) {
+      const float c = (LAW == LAW_POLY5_STEP16) ? fcoeff : fcoeff * P.w;
+      if (W.flags & 1) {
+        atomicAdd(vx + pi, c * ax);
+        atomicAdd(vy + pi, c * ay);
+        atomicAdd(vz + pi, c * az);
+      } else {
+        vx[pi] += c * ax;
+        vy[pi] += c * ay;
+        vz[pi] += c * az;
+      }
+    }
+  }
+  if (lane == 0 && evaluated) atomicAdd(queue + 1, evaluated);
+}
+
+int batched_resident_ctas(int device) {
+  int sms = 0, per = 0;
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pairs_batched<LAW_POLY6>,
+                                                32 * kBatchedWarps, 0);
+  return std::max(1, sms) * std::max(1, per);
+}
+
+cudaError_t launch_pairs_batched(int law, const float4 *pos, const PairItem *items, int64_t nitems,
+                                 const int32_t *gidx, const int32_t *idx, float *vx, float *vy,
+                                 float *vz, float fcoeff, float rsm2, float rcut2, float rcull2,
+                                 unsigned long long *queue, int ctas, cudaStream_t s) {
+  if (nitems <= 0) return cudaSuccess;
+  if (ctas <= 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    ctas = batched_resident_ctas(dev);
+  }
+  const int64_t need = (nitems + kBatchedWarps - 1) / kBatchedWarps;
+  if (ctas > need) ctas = int(need);
+  if (law == LAW_POLY5_STEP16)
+    k_pairs_batched<LAW_POLY5_STEP16><<<ctas, 32 * kBatchedWarps, 0, s>>>(
+        pos, items, nitems, gidx, idx, vx, vy, vz, fcoeff, rsm2, rcut2, rcull2, queue);
+  else
+    k_pairs_batched<LAW_POLY6><<<ctas, 32 * kBatchedWarps, 0, s>>>(
+        pos, items, nitems, gidx, idx, vx, vy, vz, fcoeff, rsm2, rcut2, rcull2, queue);
   return cudaGetLastError();
 }
 

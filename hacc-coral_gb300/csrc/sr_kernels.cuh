@@ -35,6 +35,19 @@ struct alignas(16) SegDesc {
   int64_t dst;
 };
 
+// Work item of the batched kernel: one group of at most 32 particles of a
+// leaf (spatially compact, listed in the group index array at g_begin)
+// against a contiguous range of that leaf's list.  Items of a group whose list
+// is split over several items accumulate with atomics (flags & 1).
+struct alignas(16) PairItem {
+  int64_t j_begin;   // first entry in the index array
+  int32_t j_len;     // entries in this item
+  int32_t g_begin;   // first particle of the group in the group index array
+  int32_t g_count;   // particles in the group (1..32)
+  int32_t flags;     // bit 0: list split over several items
+  int64_t pad;
+};
+
 #if defined(__CUDACC__)
 // -p(r2) for the law's polynomial, in Horner form on negated coefficients.
 // The coefficients are the reference's double literals rounded to float, as
@@ -107,6 +120,15 @@ cudaError_t launch_leaf_plain(int law, const float4 *pos, const LeafDesc *leaves
                               const int32_t *idx, float *vx, float *vy, float *vz, float fcoeff,
                               float rsm2, float rcut2, cudaStream_t s);
 cudaError_t launch_ffma_probe(float *out, int blocks, int threads, int iters, cudaStream_t s);
+// Persistent batched kernel: `ctas` CTAs (0 = size from occupancy) pull
+// items through the counter queue[0] (zero at launch); queue[1] receives the
+// number of (particle, entry) pairs actually evaluated after the box test.
+cudaError_t launch_pairs_batched(int law, const float4 *pos, const PairItem *items, int64_t nitems,
+                                 const int32_t *gidx, const int32_t *idx, float *vx, float *vy,
+                                 float *vz, float fcoeff, float rsm2, float rcut2, float rcull2,
+                                 unsigned long long *queue, int ctas, cudaStream_t s);
+// CTAs of the batched kernel that fit on the device at once.
+int batched_resident_ctas(int device);
 cudaError_t launch_force_law(int law, const float *r2, float *g, int64_t n, float rsm2, float rcut2,
                              cudaStream_t s);
 

@@ -56,7 +56,8 @@ class HsrStats(C.Structure):
                 ("pairs", C.c_int64), ("kernel_launches", C.c_int64),
                 ("t_build_ms", C.c_double), ("t_walk_ms", C.c_double),
                 ("t_force_ms", C.c_double), ("t_total_ms", C.c_double),
-                ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64)]
+                ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64),
+                ("evaluated_pairs", C.c_int64), ("work_items", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

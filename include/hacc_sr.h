@@ -99,6 +99,11 @@ typedef struct hsr_stats {
   double t_total_ms;         /* wall time of the whole call                     */
   int64_t h2d_bytes;         /* bytes copied host -> device by the call         */
   int64_t d2h_bytes;         /* bytes copied device -> host by the call         */
+  int64_t evaluated_pairs;   /* (particle, entry) pairs the kernel evaluated:
+                                every listed pair for each lane of a warp for
+                                the plain kernel; after the box test for the
+                                batched kernel (the others contribute exactly 0) */
+  int64_t work_items;        /* batched-kernel work items (group x list chunk)  */
 } hsr_stats;
 
 typedef struct hsr_ctx hsr_ctx;

@@ -120,3 +120,29 @@ def test_bad_arguments_rejected(hsr_lib, bad):
     h = C.c_void_p()
     assert hsr_lib.hsr_build_lists(C.byref(P), n, *args, C.byref(h)) == 1
     assert not h.value
+
+
+@pytest.mark.parametrize("case", ["empty", "one", "coincident", "nd1", "big_leaf"])
+def test_host_work_items_cover_every_leaf_particle(hsr_lib, case):
+    """Batched work items: one per group of <= 32 particles of each processed
+    leaf (times list chunks); empty leaves get none."""
+    if case == "empty":
+        p = synth.random_box(0, 4.0, 1)
+    elif case == "one":
+        p = synth.random_box(1, 4.0, 1)
+    elif case == "coincident":
+        p = synth.random_box(300, 4.0, 1)
+        p.x[:200] = 2.0
+        p.y[:200] = 2.0
+        p.z[:200] = 2.0
+    elif case == "nd1":
+        p = synth.random_box(400, 6.0, 2)
+    else:
+        p = synth.random_box(3000, 6.0, 2)
+    kp = synth.kick_params(p, nd={"nd1": 1, "big_leaf": 5000}.get(case, 16), fcoeff=1.0)
+    kp.min_force, kp.max_force = (-1.0,) * 3, (9.0,) * 3
+    L = hsr.HostLists(p, kp)
+    off, cnt, ptr, e = L.get()
+    lens = np.diff(ptr)
+    chunks = np.maximum(1, (lens + 8191) // 8192)
+    assert L.stats["work_items"] == int((((cnt + 31) // 32) * chunks).sum())
