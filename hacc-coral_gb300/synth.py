@@ -146,7 +146,7 @@ def _displacement(ng: int, n_index: float, sigma: float, rng) -> np.ndarray:
     dk = dk * amp
     psi = np.empty((3, ng, ng, ng))
     for a, K in enumerate((KX, KY, KZ)):
-        psi[a] = np.fft.irfftn(1j * K / k2 * dk, s=(ng, ng, ng))
+        psi[a] = np.fft.irfftn(1j * K / k2 * dk, s=(ng, ng, ng), axes=(0, 1, 2))
     psi *= sigma / max(psi.std(), 1e-30)
     return psi
 
