@@ -6,6 +6,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <limits>
 #include <memory>
@@ -15,6 +16,7 @@
 
 #include <cuda_runtime.h>
 
+#include "rcb_device.cuh"
 #include "rcb_host.hpp"
 #include "sr_kernels.cuh"
 
@@ -92,46 +94,58 @@ constexpr int64_t kJSplit = 8192;
 
 }  // namespace
 
+// Device work of the last kick: what a pair-kernel launch reads.
+struct Work {
+  const float4 *table = nullptr;
+  const hsr::LeafDesc *leaves = nullptr;
+  const int32_t *idx = nullptr;
+  const hsr::PairItem *items = nullptr;
+  const int32_t *gidx = nullptr;
+  float *vel = nullptr;  // 3 x n
+  int64_t n = 0, nleaves = 0, nitems = 0;
+  int law = 0;
+  int kernel = HSR_KERNEL_BATCHED;
+  float fcoeff = 0, rsm2 = 0, rc2 = 0, rcull2 = 0;
+  bool device_built = false;
+};
+
 struct hsr_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
   std::unique_ptr<hsr::RcbHost> host;
-  DevBuf d_pos, d_vel, d_leaves, d_segs, d_idx, d_law;
-  PinBuf h_pos, h_vel, h_leaves, h_segs;
+  hsr::DeviceTree tree;
+  // host-build path
+  DevBuf d_pos, d_vel, d_leaves, d_segs, d_idx, d_items, d_gidx;
+  PinBuf h_pos, h_vel, h_leaves, h_segs, h_items, h_gidx;
+  // device-build path: staged inputs and outputs of the ten arrays
+  DevBuf d_in, d_out, d_pos4;
+  // misc
+  DevBuf d_law, d_flush, d_probe, d_queue;
   hsr_stats stats{};
   std::string err = "no error";
   bool have_lists = false;
-  int64_t last_n = 0;
   int last_tdpts = 1;
-  // launch arguments of the last kick's pair kernel (diagnostic replays)
-  int last_law = 0;
-  int64_t last_nleaves = 0;
-  float last_fcoeff = 0, last_rsm2 = 0, last_rc2 = 0;
-  DevBuf d_flush, d_probe, d_items, d_gidx, d_queue;
-  PinBuf h_items, h_gidx;
-  int last_kernel = HSR_KERNEL_BATCHED;
-  int64_t last_nitems = 0;
-  float last_rcull2 = 0;
+  Work work;
   int batched_ctas = 0;
 
-  // Launches the last kick's pair kernel on the resident work (the
-  // batched kernel's queue counter is reset first).
+  // Launches a pair kernel on the current work (the batched kernel's queue
+  // counter and evaluated-pair counter are reset first).
   cudaError_t launch_pairs(int kernel) {
-    float *dv = d_vel.as<float>();
-    const int64_t n = last_n;
+    const Work &w = work;
+    float *dv = w.vel;
+    const int64_t n = w.n;
     if (kernel == HSR_KERNEL_PLAIN)
-      return hsr::launch_leaf_plain(last_law, d_pos.as<float4>(), d_leaves.as<hsr::LeafDesc>(),
-                                    last_nleaves, d_idx.as<int32_t>(), dv, dv + n, dv + 2 * n,
-                                    last_fcoeff, last_rsm2, last_rc2, stream);
+      return hsr::launch_leaf_plain(w.law, w.table, w.leaves, w.nleaves, w.idx, dv, dv + n,
+                                    dv + 2 * n, w.fcoeff, w.rsm2, w.rc2, stream);
     if (batched_ctas == 0) batched_ctas = hsr::batched_resident_ctas(device);
-    cudaError_t e = cudaMemsetAsync(d_queue.p, 0, 2 * sizeof(unsigned long long), stream);
+    cudaError_t e = d_queue.ensure(64);
     if (e != cudaSuccess) return e;
-    return hsr::launch_pairs_batched(last_law, d_pos.as<float4>(), d_items.as<hsr::PairItem>(),
-                                     last_nitems, d_gidx.as<int32_t>(), d_idx.as<int32_t>(), dv,
-                                     dv + n, dv + 2 * n, last_fcoeff, last_rsm2, last_rc2,
-                                     last_rcull2, d_queue.as<unsigned long long>(), batched_ctas,
-                                     stream);
+    e = cudaMemsetAsync(d_queue.p, 0, 2 * sizeof(unsigned long long), stream);
+    if (e != cudaSuccess) return e;
+    return hsr::launch_pairs_batched(w.law, w.table, w.items, w.nitems, w.gidx, w.idx, dv, dv + n,
+                                     dv + 2 * n, w.fcoeff, w.rsm2, w.rc2, w.rcull2,
+                                     d_queue.as<unsigned long long>(), batched_ctas, stream);
   }
 
   hsr_status fail(hsr_status s, const std::string &msg) {
@@ -171,6 +185,8 @@ hsr_status hsr_create(hsr_ctx **out, int device) {
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev0);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev2);
+  if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev3);
   if (e != cudaSuccess) {
     delete ctx;
     return HSR_ERR_CUDA;
@@ -186,12 +202,13 @@ hsr_status hsr_destroy(hsr_ctx *ctx) {
   cudaSetDevice(ctx->device);
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf *b : {&ctx->d_pos, &ctx->d_vel, &ctx->d_leaves, &ctx->d_segs, &ctx->d_idx, &ctx->d_law,
-                    &ctx->d_flush, &ctx->d_probe, &ctx->d_items, &ctx->d_gidx, &ctx->d_queue})
+                    &ctx->d_flush, &ctx->d_probe, &ctx->d_items, &ctx->d_gidx, &ctx->d_queue,
+                    &ctx->d_in, &ctx->d_out, &ctx->d_pos4})
     b->release();
   for (PinBuf *b : {&ctx->h_pos, &ctx->h_vel, &ctx->h_leaves, &ctx->h_segs, &ctx->h_items, &ctx->h_gidx})
     b->release();
-  if (ctx->ev0) cudaEventDestroy(ctx->ev0);
-  if (ctx->ev1) cudaEventDestroy(ctx->ev1);
+  for (cudaEvent_t ev : {ctx->ev0, ctx->ev1, ctx->ev2, ctx->ev3})
+    if (ev) cudaEventDestroy(ev);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
   return HSR_OK;
@@ -467,22 +484,24 @@ struct hsr_lists {
   hsr_stats st{};
 };
 
-extern "C" {
+namespace {
 
-hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, float *y, float *z,
-                        float *vx, float *vy, float *vz, float *mass, float *phi, int64_t *id,
-                        uint16_t *mask, int32_t mem) {
-  if (!ctx) return HSR_ERR_ARG;
-  const auto t_start = clk::now();
-  const void *arrs[10] = {x, y, z, vx, vy, vz, mass, phi, id, mask};
-  if (hsr_status e = check_params(p, n, arrs, ctx->err)) return e;
-  if (mem != HSR_MEM_HOST) return ctx->fail(HSR_ERR_UNSUPPORTED, "hsr_rcb_kick takes host arrays");
-  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
-  ctx->have_lists = false;
-  hsr_stats st{};
+void set_work_params(Work &w, const hsr_params *p, int64_t n) {
+  w.n = n;
+  w.law = p->law;
+  w.fcoeff = p->fcoeff;
+  w.rsm2 = p->rsm * p->rsm;
+  w.rc2 = cut2(p->law, p->fsrrmax);
+  w.rcull2 = cull2(w.rc2);
+  w.kernel = p->kernel == HSR_KERNEL_PLAIN ? HSR_KERNEL_PLAIN : HSR_KERNEL_BATCHED;
+}
+
+// Tree and lists on the host (rcb_host.cpp), pair kernel on the device.
+hsr_status kick_host_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, float *y,
+                           float *z, float *vx, float *vy, float *vz, float *mass, float *phi,
+                           int64_t *id, uint16_t *mask, hsr_stats &st) {
   hsr::RcbHost &H = *ctx->host;
   const PlanSizes ps = host_build(H, p, n, x, y, z, mass, st);
-
   CU(ctx->h_pos.ensure(size_t(std::max<int64_t>(ps.ntab, 1)) * 16), "cudaHostAlloc(pos)");
   CU(ctx->h_vel.ensure(size_t(std::max<int64_t>(3 * n, 1)) * 4), "cudaHostAlloc(vel)");
   CU(ctx->h_leaves.ensure(size_t(std::max<int64_t>(ps.nleaves, 1)) * sizeof(hsr::LeafDesc)),
@@ -495,7 +514,9 @@ hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, 
   auto *hs = ctx->h_segs.as<hsr::SegDesc>();
   std::vector<int64_t> list_begin;
   host_fill(H, n, x, y, z, vx, vy, vz, mass, phi, id, mask, hp, hv, hl, hs, &list_begin);
-  const bool plain = p->kernel == HSR_KERNEL_PLAIN;
+  Work &w = ctx->work;
+  set_work_params(w, p, n);
+  const bool plain = w.kernel == HSR_KERNEL_PLAIN;
   int64_t nitems = 0;
   if (!plain) {
     std::vector<int32_t> gidx;
@@ -507,7 +528,6 @@ hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, 
     std::memcpy(ctx->h_items.p, items.data(), items.size() * sizeof(hsr::PairItem));
     std::memcpy(ctx->h_gidx.p, gidx.data(), gidx.size() * 4);
   }
-
   cudaStream_t s = ctx->stream;
   CU(ctx->d_pos.ensure(size_t(std::max<int64_t>(ps.ntab, 1)) * 16), "cudaMalloc(pos)");
   CU(ctx->d_vel.ensure(size_t(std::max<int64_t>(3 * n, 1)) * 4), "cudaMalloc(vel)");
@@ -516,7 +536,6 @@ hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, 
   CU(ctx->d_segs.ensure(size_t(std::max<int64_t>(ps.nsegs, 1)) * sizeof(hsr::SegDesc)),
      "cudaMalloc(segs)");
   CU(ctx->d_idx.ensure(size_t(std::max<int64_t>(ps.nidx, 1)) * 4), "cudaMalloc(idx)");
-  CU(ctx->d_queue.ensure(64), "cudaMalloc(queue)");
   CU(cudaMemcpyAsync(ctx->d_pos.p, hp, size_t(ps.ntab) * 16, cudaMemcpyHostToDevice, s), "H2D pos");
   CU(cudaMemcpyAsync(ctx->d_vel.p, hv, size_t(3 * n) * 4, cudaMemcpyHostToDevice, s), "H2D vel");
   CU(cudaMemcpyAsync(ctx->d_leaves.p, hl, size_t(ps.nleaves) * sizeof(hsr::LeafDesc),
@@ -537,28 +556,25 @@ hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, 
   CU(hsr::launch_expand_segments(ctx->d_segs.as<hsr::SegDesc>(), ps.nsegs, ctx->d_idx.as<int32_t>(), s),
      "expand kernel");
   launches += ps.nsegs > 0;
-  const float rsm2 = p->rsm * p->rsm;
-  const float rc2 = cut2(p->law, p->fsrrmax);
-  ctx->last_n = n;
-  ctx->last_law = p->law;
-  ctx->last_nleaves = ps.nleaves;
-  ctx->last_fcoeff = p->fcoeff;
-  ctx->last_rsm2 = rsm2;
-  ctx->last_rc2 = rc2;
-  ctx->last_rcull2 = cull2(rc2);
-  ctx->last_kernel = plain ? HSR_KERNEL_PLAIN : HSR_KERNEL_BATCHED;
-  ctx->last_nitems = nitems;
+  w.table = ctx->d_pos.as<float4>();
+  w.leaves = ctx->d_leaves.as<hsr::LeafDesc>();
+  w.idx = ctx->d_idx.as<int32_t>();
+  w.items = ctx->d_items.as<hsr::PairItem>();
+  w.gidx = ctx->d_gidx.as<int32_t>();
+  w.vel = ctx->d_vel.as<float>();
+  w.nleaves = ps.nleaves;
+  w.nitems = nitems;
+  w.device_built = false;
   CU(cudaEventRecord(ctx->ev0, s), "event");
-  CU(ctx->launch_pairs(ctx->last_kernel), "pair kernel");
+  CU(ctx->launch_pairs(w.kernel), "pair kernel");
   launches += plain ? ps.nleaves > 0 : nitems > 0;
   CU(cudaEventRecord(ctx->ev1, s), "event");
-  float *dv = ctx->d_vel.as<float>();
+  float *dv = w.vel;
   CU(cudaMemcpyAsync(hv, dv, size_t(3 * n) * 4, cudaMemcpyDeviceToHost, s), "D2H vel");
   unsigned long long counters[2] = {0, 0};
   if (!plain) CU(cudaMemcpyAsync(counters, ctx->d_queue.p, sizeof(counters), cudaMemcpyDeviceToHost, s),
                  "D2H counters");
   CU(cudaStreamSynchronize(s), "kernel execution");
-  // the plain kernel evaluates every listed pair for every lane of a warp
   st.evaluated_pairs = plain ? H.padded_pairs() : int64_t(counters[1]);
   float fms = 0;
   CU(cudaEventElapsedTime(&fms, ctx->ev0, ctx->ev1), "event time");
@@ -575,6 +591,177 @@ hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, 
   st.h2d_bytes = ps.ntab * 16 + 3 * n * 4 + ps.nleaves * int64_t(sizeof(hsr::LeafDesc)) +
                  ps.nsegs * int64_t(sizeof(hsr::SegDesc)) + h2d_items;
   st.d2h_bytes = 3 * n * 4 + (plain ? 0 : 16);
+  return HSR_OK;
+}
+
+// Offsets of the ten arrays inside one staging region (8 float arrays, the
+// int64 ids, the uint16 masks), each 256-byte aligned.
+struct ArrayLayout {
+  size_t f[8], id, mask, bytes;
+  explicit ArrayLayout(int64_t n) {
+    auto up = [](size_t v) { return (v + 255) & ~size_t(255); };
+    size_t o = 0;
+    for (int i = 0; i < 8; ++i) {
+      f[i] = o;
+      o = up(o + size_t(n) * 4);
+    }
+    id = o;
+    o = up(o + size_t(n) * 8);
+    mask = o;
+    o = up(o + size_t(n) * 2);
+    bytes = std::max<size_t>(o, 256);
+  }
+};
+
+// Tree, lists, work items and the kick all on the device (rcb_device.cu).
+hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, float *y,
+                             float *z, float *vx, float *vy, float *vz, float *mass, float *phi,
+                             int64_t *id, uint16_t *mask, int32_t mem, hsr_stats &st) {
+  cudaStream_t s = ctx->stream;
+  const ArrayLayout A(n);
+  float *arr[8] = {x, y, z, vx, vy, vz, mass, phi};
+  CU(ctx->d_out.ensure(A.bytes), "cudaMalloc(out)");
+  CU(ctx->d_pos4.ensure(size_t(std::max<int64_t>(n, 1)) * 16), "cudaMalloc(pos4)");
+  const float *in[8];
+  const int64_t *in_id;
+  const uint16_t *in_mask;
+  char *ob = ctx->d_out.as<char>();
+  CU(cudaEventRecord(ctx->ev2, s), "event");
+  if (mem == HSR_MEM_HOST) {
+    CU(ctx->d_in.ensure(A.bytes), "cudaMalloc(in)");
+    char *ib = ctx->d_in.as<char>();
+    for (int i = 0; i < 8; ++i) {
+      CU(cudaMemcpyAsync(ib + A.f[i], arr[i], size_t(n) * 4, cudaMemcpyHostToDevice, s), "H2D arrays");
+      in[i] = reinterpret_cast<const float *>(ib + A.f[i]);
+    }
+    CU(cudaMemcpyAsync(ib + A.id, id, size_t(n) * 8, cudaMemcpyHostToDevice, s), "H2D ids");
+    CU(cudaMemcpyAsync(ib + A.mask, mask, size_t(n) * 2, cudaMemcpyHostToDevice, s), "H2D masks");
+    in_id = reinterpret_cast<const int64_t *>(ib + A.id);
+    in_mask = reinterpret_cast<const uint16_t *>(ib + A.mask);
+    st.h2d_bytes = n * 42;
+  } else {
+    for (int i = 0; i < 8; ++i) in[i] = arr[i];
+    in_id = id;
+    in_mask = mask;
+  }
+  int64_t launches = 0;
+  float4 *pos4 = ctx->d_pos4.as<float4>();
+  CU(hsr::launch_pack4(in[0], in[1], in[2], in[6], pos4, n, s), "pack kernel");
+  ++launches;
+  hsr::TreeConfig cfg{};
+  for (int i = 0; i < 3; ++i) {
+    cfg.min[i] = p->min[i];
+    cfg.max[i] = p->max[i];
+    cfg.min_force[i] = p->min_force[i];
+    cfg.max_force[i] = p->max_force[i];
+  }
+  cfg.fsrrmax = p->fsrrmax;
+  cfg.tan_oa = std::tan(p->open_angle);  // host tanf, as the reference computes it
+  cfg.ppc = p->ppc;
+  cfg.nd = int32_t(std::min<int64_t>(p->nd, INT32_MAX));
+  cfg.tdpts = p->tdpts;
+  {
+    const char *f = std::getenv("HSR_FORCE_CM_FALLBACK");  // test hook
+    cfg.force_cm_fallback = (f && f[0] == '1') ? 1 : 0;
+  }
+  CU(cudaEventRecord(ctx->ev3, s), "event");
+  const auto tb = clk::now();
+  cudaError_t e = ctx->tree.build(cfg, n, pos4, kJSplit, s);
+  if (e != cudaSuccess) {
+    if (ctx->tree.error()) return ctx->fail(HSR_ERR_UNSUPPORTED, ctx->tree.error());
+    return ctx->cuda_fail(e, "device tree build");
+  }
+  st.t_build_ms = ms_since(tb);  // build, lists and items (synchronizes per level)
+  const hsr::DeviceTreeInfo &ti = ctx->tree.info();
+  launches += ti.levels * 16 + 24;
+  const int32_t *perm = ctx->tree.perm();
+  // outputs in tree order: velocities to the kick buffer, the rest to d_out
+  Work &w = ctx->work;
+  set_work_params(w, p, n);
+  float *ovx = reinterpret_cast<float *>(ob + A.f[3]), *ovy = reinterpret_cast<float *>(ob + A.f[4]),
+        *ovz = reinterpret_cast<float *>(ob + A.f[5]);
+  CU(ctx->d_vel.ensure(size_t(std::max<int64_t>(3 * n, 1)) * 4), "cudaMalloc(vel)");
+  float *dv = ctx->d_vel.as<float>();
+  CU(hsr::launch_gather_f32(in[3], perm, dv, n, s), "gather vx");
+  CU(hsr::launch_gather_f32(in[4], perm, dv + n, n, s), "gather vy");
+  CU(hsr::launch_gather_f32(in[5], perm, dv + 2 * n, n, s), "gather vz");
+  CU(hsr::launch_gather_f32(in[7], perm, reinterpret_cast<float *>(ob + A.f[7]), n, s), "gather phi");
+  CU(hsr::launch_gather_i64(in_id, perm, reinterpret_cast<int64_t *>(ob + A.id), n, s), "gather id");
+  CU(hsr::launch_gather_u16(in_mask, perm, reinterpret_cast<uint16_t *>(ob + A.mask), n, s),
+     "gather mask");
+  CU(hsr::launch_unpack4(ctx->tree.table(), reinterpret_cast<float *>(ob + A.f[0]),
+                         reinterpret_cast<float *>(ob + A.f[1]), reinterpret_cast<float *>(ob + A.f[2]),
+                         reinterpret_cast<float *>(ob + A.f[6]), n, s),
+     "unpack kernel");
+  launches += 7;
+  w.table = ctx->tree.table();
+  w.leaves = ctx->tree.leaves();
+  w.idx = ctx->tree.index();
+  w.items = ctx->tree.items();
+  w.gidx = ctx->tree.gidx();
+  w.vel = dv;
+  w.nleaves = ti.processed_leaves;
+  w.nitems = ti.items;
+  w.device_built = true;
+  const bool plain = w.kernel == HSR_KERNEL_PLAIN;
+  CU(cudaEventRecord(ctx->ev0, s), "event");
+  CU(ctx->launch_pairs(w.kernel), "pair kernel");
+  launches += plain ? w.nleaves > 0 : w.nitems > 0;
+  CU(cudaEventRecord(ctx->ev1, s), "event");
+  // kicked velocities into the output slots, then everything back
+  CU(cudaMemcpyAsync(ovx, dv, size_t(n) * 4, cudaMemcpyDeviceToDevice, s), "copy vx");
+  CU(cudaMemcpyAsync(ovy, dv + n, size_t(n) * 4, cudaMemcpyDeviceToDevice, s), "copy vy");
+  CU(cudaMemcpyAsync(ovz, dv + 2 * n, size_t(n) * 4, cudaMemcpyDeviceToDevice, s), "copy vz");
+  const cudaMemcpyKind back = mem == HSR_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  for (int i = 0; i < 8; ++i)
+    CU(cudaMemcpyAsync(arr[i], ob + A.f[i], size_t(n) * 4, back, s), "copy arrays back");
+  CU(cudaMemcpyAsync(id, ob + A.id, size_t(n) * 8, back, s), "copy ids back");
+  CU(cudaMemcpyAsync(mask, ob + A.mask, size_t(n) * 2, back, s), "copy masks back");
+  unsigned long long counters[2] = {0, 0};
+  if (!plain) CU(cudaMemcpyAsync(counters, ctx->d_queue.p, sizeof(counters), cudaMemcpyDeviceToHost, s),
+                 "D2H counters");
+  CU(cudaStreamSynchronize(s), "kernel execution");
+  float fms = 0;
+  CU(cudaEventElapsedTime(&fms, ctx->ev0, ctx->ev1), "event time");
+  st.t_force_ms = fms;
+  st.t_walk_ms = 0;
+  st.n = n;
+  st.nodes = ti.nodes;
+  st.leaves = 0;
+  st.processed_leaves = ti.processed_leaves;
+  st.list_entries = ti.list_entries;
+  st.pairs = ti.pairs;
+  st.evaluated_pairs = plain ? ctx->tree.padded_pairs() : int64_t(counters[1]);
+  st.work_items = ti.items;
+  st.cm_fallbacks = ti.cm_fallbacks;
+  st.kernel_launches = launches;
+  if (mem == HSR_MEM_HOST) st.d2h_bytes = n * 42 + (plain ? 0 : 16);
+  return HSR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, float *y, float *z,
+                        float *vx, float *vy, float *vz, float *mass, float *phi, int64_t *id,
+                        uint16_t *mask, int32_t mem) {
+  if (!ctx) return HSR_ERR_ARG;
+  const auto t_start = clk::now();
+  const void *arrs[10] = {x, y, z, vx, vy, vz, mass, phi, id, mask};
+  if (hsr_status e = check_params(p, n, arrs, ctx->err)) return e;
+  if (mem != HSR_MEM_HOST && mem != HSR_MEM_DEVICE) return ctx->fail(HSR_ERR_ARG, "bad memory kind");
+  if (p->build != HSR_BUILD_DEVICE && p->build != HSR_BUILD_HOST)
+    return ctx->fail(HSR_ERR_ARG, "bad build location");
+  if (p->build == HSR_BUILD_HOST && mem != HSR_MEM_HOST)
+    return ctx->fail(HSR_ERR_UNSUPPORTED, "the host build takes host arrays");
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  ctx->have_lists = false;
+  hsr_stats st{};
+  hsr_status r = p->build == HSR_BUILD_HOST
+                     ? kick_host_build(ctx, p, n, x, y, z, vx, vy, vz, mass, phi, id, mask, st)
+                     : kick_device_build(ctx, p, n, x, y, z, vx, vy, vz, mass, phi, id, mask, mem, st);
+  if (r != HSR_OK) return r;
   st.t_total_ms = ms_since(t_start);
   ctx->stats = st;
   ctx->have_lists = true;
@@ -585,17 +772,59 @@ hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, 
 hsr_status hsr_lists_size(const hsr_ctx *ctx, int64_t *nleaves, int64_t *nentries) {
   if (!ctx || !nleaves || !nentries) return HSR_ERR_ARG;
   if (!ctx->have_lists) return HSR_ERR_STATE;
-  *nleaves = int64_t(ctx->host->leaves().size());
-  *nentries = ctx->host->list_entries();
+  *nleaves = ctx->work.device_built ? ctx->tree.info().processed_leaves
+                                    : int64_t(ctx->host->leaves().size());
+  *nentries = ctx->work.device_built ? ctx->tree.info().list_entries : ctx->host->list_entries();
   return HSR_OK;
 }
 
-hsr_status hsr_lists_export(const hsr_ctx *ctx, int64_t *leaf_offset, int64_t *leaf_count,
+hsr_status hsr_lists_export(const hsr_ctx *ctx_c, int64_t *leaf_offset, int64_t *leaf_count,
                             int64_t *list_ptr, float *ex, float *ey, float *ez, float *em) {
+  hsr_ctx *ctx = const_cast<hsr_ctx *>(ctx_c);
   if (!ctx || !leaf_offset || !leaf_count || !list_ptr || !ex || !ey || !ez || !em) return HSR_ERR_ARG;
   if (!ctx->have_lists) return HSR_ERR_STATE;
-  export_lists(*ctx->host, ctx->h_pos.as<float>(), leaf_offset, leaf_count, list_ptr, ex, ey, ez, em,
-               nullptr);
+  if (!ctx->work.device_built) {
+    export_lists(*ctx->host, ctx->h_pos.as<float>(), leaf_offset, leaf_count, list_ptr, ex, ey, ez,
+                 em, nullptr);
+    return HSR_OK;
+  }
+  // device-built lists: copy the descriptors and the table, expand here
+  const auto &ti = ctx->tree.info();
+  const int64_t nl = ti.processed_leaves, ns = ti.segments;
+  const int64_t ntab = ctx->work.n + ti.nodes * ctx->last_tdpts;
+  std::vector<hsr::LeafDesc> ld(static_cast<size_t>(std::max<int64_t>(nl, 1)));
+  std::vector<hsr::SegDesc> sd(static_cast<size_t>(std::max<int64_t>(ns, 1)));
+  std::vector<float4> tab(static_cast<size_t>(std::max<int64_t>(ntab, 1)));
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  cudaStream_t s = ctx->stream;
+  CU(cudaMemcpyAsync(ld.data(), ctx->tree.leaves(), size_t(nl) * sizeof(hsr::LeafDesc),
+                     cudaMemcpyDeviceToHost, s), "D2H leaves");
+  CU(cudaMemcpyAsync(sd.data(), ctx->tree.segs(), size_t(ns) * sizeof(hsr::SegDesc),
+                     cudaMemcpyDeviceToHost, s), "D2H segments");
+  CU(cudaMemcpyAsync(tab.data(), ctx->tree.table(), size_t(ntab) * sizeof(float4),
+                     cudaMemcpyDeviceToHost, s), "D2H table");
+  CU(cudaStreamSynchronize(s), "list export");
+  // segments are stored leaf after leaf in list order
+  int64_t seg = 0;
+  for (int64_t l = 0; l < nl; ++l) {
+    leaf_offset[l] = ld[l].offset;
+    leaf_count[l] = ld[l].count;
+    list_ptr[l] = ld[l].list_begin;
+    int64_t run = ld[l].list_begin;
+    const int64_t end = ld[l].list_begin + ld[l].list_len;
+    while (run < end && seg < ns) {
+      const hsr::SegDesc &g = sd[seg++];
+      for (int32_t q = 0; q < g.count; ++q) {
+        const float4 e = tab[size_t(g.start) + q];
+        ex[run] = e.x;
+        ey[run] = e.y;
+        ez[run] = e.z;
+        em[run] = e.w;
+        ++run;
+      }
+    }
+  }
+  list_ptr[nl] = ti.list_entries;
   return HSR_OK;
 }
 
@@ -676,8 +905,8 @@ hsr_status hsr_bench_pairs(hsr_ctx *ctx, int32_t kernel, int32_t iters, int32_t 
   if (!ctx || !ms_per_launch || iters < 1) return HSR_ERR_ARG;
   if (!ctx->have_lists) return ctx->fail(HSR_ERR_STATE, "no kick to replay");
   // replays run the kick's own kernel unless the plain one is asked for
-  const int kk = kernel == HSR_KERNEL_PLAIN ? HSR_KERNEL_PLAIN : ctx->last_kernel;
-  if (kk == HSR_KERNEL_BATCHED && ctx->last_nitems == 0 && ctx->last_nleaves > 0)
+  const int kk = kernel == HSR_KERNEL_PLAIN ? HSR_KERNEL_PLAIN : ctx->work.kernel;
+  if (kk == HSR_KERNEL_BATCHED && ctx->work.nitems == 0 && ctx->work.nleaves > 0)
     return ctx->fail(HSR_ERR_STATE, "last kick had no batched work to replay");
   CU(cudaSetDevice(ctx->device), "cudaSetDevice");
   cudaStream_t s = ctx->stream;

@@ -1,0 +1,1246 @@
+// rcb_device.cu -- RCB tree, interaction lists and batched work items built on
+// the GPU (see rcb_device.cuh for the method).
+#include "rcb_device.cuh"
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <vector>
+
+namespace hsr {
+
+namespace {
+
+// ---- exactly rounded float helpers: never fused, as the reference rounds ----
+__device__ __forceinline__ float fmul_(float a, float b) { return __fmul_rn(a, b); }
+__device__ __forceinline__ float fadd_(float a, float b) { return __fadd_rn(a, b); }
+__device__ __forceinline__ float fsub_(float a, float b) { return __fsub_rn(a, b); }
+__device__ __forceinline__ float smin_(float a, float b) { return (b < a) ? b : a; }
+// ((a*a) + (b*b)) + (c*c)
+__device__ __forceinline__ float norm2_(float a, float b, float c) {
+  return fadd_(fadd_(fmul_(a, a), fmul_(b, b)), fmul_(c, c));
+}
+
+__host__ __device__ __forceinline__ int64_t max64(int64_t a, int64_t b) { return a > b ? a : b; }
+__host__ __device__ __forceinline__ int64_t min64(int64_t a, int64_t b) { return a < b ? a : b; }
+
+constexpr int kChunk = 4096;        // elements per statistics / partition chunk
+constexpr int kChunkThreads = 256;  // threads per chunk (16 elements each)
+constexpr int kPer = kChunk / kChunkThreads;
+constexpr int kPartDoubles = 16;    // per-chunk partial record
+constexpr int kWalkStack = 256;     // DFS stack of the list walk
+
+enum { C_NCHUNK = 0, C_NSPLIT = 1, C_NFALLBACK = 2, C_NLEAF = 3, C_NSEG = 4, C_NENT = 5,
+       C_PAIRS = 6, C_PADDED = 7, C_NITEMS = 8, C_MAXLEN = 9, C_BUCKET = 16, C_FILL = 48,
+       C_COUNT = 80 };
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float warp_min(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fminf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+__device__ __forceinline__ float warp_max(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  return v;
+}
+
+// ---------------------------------------------------------------------------
+// Scan
+// ---------------------------------------------------------------------------
+constexpr int kScanThreads = 1024;
+constexpr int kScanPer = 4;
+constexpr int64_t kScanBlock = kScanThreads * kScanPer;
+
+__global__ void __launch_bounds__(kScanThreads)
+    k_scan_block(const int64_t *in, int64_t *out, int64_t n, int64_t *bsum) {
+  __shared__ int64_t wsum[32];
+  const int64_t base = int64_t(blockIdx.x) * kScanBlock + int64_t(threadIdx.x) * kScanPer;
+  int64_t v[kScanPer];
+  int64_t t = 0;
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    v[k] = base + k < n ? in[base + k] : 0;
+    t += v[k];
+  }
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int64_t x = t;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int64_t w = wsum[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    wsum[lane] = w;
+  }
+  __syncthreads();
+  const int64_t excl = x - t + (warp > 0 ? wsum[warp - 1] : 0);
+  int64_t run = excl;
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    if (base + k < n) out[base + k] = run;
+    run += v[k];
+  }
+  if (threadIdx.x == kScanThreads - 1) bsum[blockIdx.x] = run;
+}
+
+__global__ void k_scan_add(int64_t *out, int64_t n, const int64_t *boff) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) out[i] += boff[i / kScanBlock];
+}
+
+__global__ void k_copy_total(const int64_t *src, int64_t *dst) { *dst = *src; }
+
+}  // namespace
+
+int64_t scan_tmp_size(int64_t n) {
+  const int64_t nb = (n + kScanBlock - 1) / kScanBlock;
+  return nb <= 1 ? 2 : nb + 1 + scan_tmp_size(nb);
+}
+
+cudaError_t exclusive_scan_i64(const int64_t *in, int64_t *out, int64_t n, int64_t *total,
+                               int64_t *tmp, cudaStream_t s) {
+  if (n <= 0) {
+    if (total) return cudaMemsetAsync(total, 0, sizeof(int64_t), s);
+    return cudaSuccess;
+  }
+  const int64_t nb = (n + kScanBlock - 1) / kScanBlock;
+  k_scan_block<<<unsigned(nb), kScanThreads, 0, s>>>(in, out, n, tmp);
+  if (nb == 1) {
+    if (total) k_copy_total<<<1, 1, 0, s>>>(tmp, total);
+    return cudaGetLastError();
+  }
+  // scan the block sums in place, then add them
+  cudaError_t e = exclusive_scan_i64(tmp, tmp, nb, total, tmp + nb + 1, s);
+  if (e != cudaSuccess) return e;
+  k_scan_add<<<unsigned((n + 255) / 256), 256, 0, s>>>(out, n, tmp);
+  return cudaGetLastError();
+}
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// Level kernels
+// ---------------------------------------------------------------------------
+
+// Number of chunks of each node of the level [nb, ne).
+__global__ void k_chunk_counts(const DNode *nodes, int32_t nb, int32_t ne, int64_t *cnt) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (nb + i < ne) cnt[i] = (int64_t(nodes[nb + i].count) + kChunk - 1) / kChunk;
+}
+
+__global__ void k_chunk_fill(const DNode *nodes, int32_t nb, int32_t ne, const int64_t *base,
+                             int32_t *chunk_node) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (nb + i >= ne) return;
+  const int64_t c = (int64_t(nodes[nb + i].count) + kChunk - 1) / kChunk;
+  for (int64_t k = 0; k < c; ++k) chunk_node[base[i] + k] = nb + i;
+}
+
+struct ChunkRange {
+  int32_t node, begin, len, local;  // local: first element's position inside the node
+};
+
+__device__ __forceinline__ ChunkRange chunk_range(const DNode *nodes, const int32_t *chunk_node,
+                                                  const int64_t *chunk_base, int32_t nb,
+                                                  int64_t chunk) {
+  ChunkRange r;
+  r.node = chunk_node[chunk];
+  const DNode &N = nodes[r.node];
+  const int64_t c = chunk - chunk_base[r.node - nb];
+  r.local = int32_t(c * kChunk);
+  r.begin = N.offset + r.local;
+  r.len = min(kChunk, N.count - r.local);
+  return r;
+}
+
+// Partial sums of one chunk: sum w*x, sum |w*x| (x, y, z), sum w, sum |w|,
+// and the bounding box.  Fixed thread-to-element map and reduction tree.
+__global__ void __launch_bounds__(kChunkThreads)
+    k_stats_partial(const float4 *__restrict__ pos, const DNode *nodes,
+                    const int32_t *chunk_node, const int64_t *chunk_base, int32_t nb,
+                    const int64_t *nchunk, double *part) {
+  const int64_t chunk = blockIdx.x;
+  if (chunk >= *nchunk) return;
+  const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
+  double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  bool any = false;
+  for (int k = threadIdx.x; k < R.len; k += kChunkThreads) {
+    const float4 p = pos[R.begin + k];
+    const float w = p.w;
+    const double wx = double(fmul_(w, p.x)), wy = double(fmul_(w, p.y)), wz = double(fmul_(w, p.z));
+    s[0] += wx; s[1] += wy; s[2] += wz; s[3] += double(w);
+    s[4] += fabs(wx); s[5] += fabs(wy); s[6] += fabs(wz); s[7] += fabs(double(w));
+    if (!any) {
+      lo[0] = hi[0] = p.x; lo[1] = hi[1] = p.y; lo[2] = hi[2] = p.z;
+      any = true;
+    } else {
+      lo[0] = fminf(lo[0], p.x); hi[0] = fmaxf(hi[0], p.x);
+      lo[1] = fminf(lo[1], p.y); hi[1] = fmaxf(hi[1], p.y);
+      lo[2] = fminf(lo[2], p.z); hi[2] = fmaxf(hi[2], p.z);
+    }
+  }
+  // fminf/fmaxf ignore the +-INFINITY identity only if a real value exists;
+  // lanes without elements hold the identities, which min/max absorb.
+#pragma unroll
+  for (int q = 0; q < 8; ++q) s[q] = warp_sum(s[q]);
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = warp_min(lo[d]);
+    hi[d] = warp_max(hi[d]);
+  }
+  __shared__ double sh[kChunkThreads / 32][14];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  if (lane == 0) {
+    for (int q = 0; q < 8; ++q) sh[warp][q] = s[q];
+    for (int d = 0; d < 3; ++d) {
+      sh[warp][8 + d] = lo[d];
+      sh[warp][11 + d] = hi[d];
+    }
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t[14];
+    for (int q = 0; q < 14; ++q) t[q] = sh[0][q];
+    for (int w = 1; w < kChunkThreads / 32; ++w) {
+      for (int q = 0; q < 8; ++q) t[q] += sh[w][q];
+      for (int d = 0; d < 3; ++d) {
+        t[8 + d] = fmin(t[8 + d], sh[w][8 + d]);
+        t[11 + d] = fmax(t[11 + d], sh[w][11 + d]);
+      }
+    }
+    double *o = part + chunk * kPartDoubles;
+    for (int q = 0; q < 14; ++q) o[q] = t[q];
+  }
+}
+
+// Float that the reference's (float)(sx / sm) gives, if the bounds decide it.
+// sx, sm: this build's sums; bx, bm: bounds on |reference sum - this sum|.
+__device__ bool certify(double sx, double bx, double sm, double bm, float *out) {
+  const double xl = sx - bx, xh = sx + bx, ml = sm - bm, mh = sm + bm;
+  if (!(ml > 0.0) || !isfinite(xl) || !isfinite(xh) || !isfinite(mh)) return false;
+  const double q0 = __ddiv_rd(xl, mh), q1 = __ddiv_rd(xl, ml), q2 = __ddiv_ru(xh, mh),
+               q3 = __ddiv_ru(xh, ml);
+  double lo = fmin(fmin(q0, q1), fmin(q2, q3));
+  double hi = fmax(fmax(q0, q1), fmax(q2, q3));
+  // the reference rounds its quotient to double once more
+  lo -= fabs(lo) * 0x1p-51;
+  hi += fabs(hi) * 0x1p-51;
+  const float fl = __double2float_rn(lo), fh = __double2float_rn(hi);
+  if (fl != fh) return false;
+  *out = fl;
+  return true;
+}
+
+// One warp per node of the level: reduce the node's chunk partials, set the
+// bounding box and, where certified, the centre of mass; list the others for
+// the sequential fallback.
+__global__ void k_stats_final(DNode *nodes, int32_t nb, int32_t ne, const int64_t *chunk_base,
+                              const double *part, int32_t *fallback, int64_t *counters,
+                              int32_t force_fallback) {
+  const int32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+  const int lane = threadIdx.x & 31;
+  const int32_t node = nb + wid;
+  if (node >= ne) return;
+  DNode &N = nodes[node];
+  if (N.count <= 0) return;
+  const int64_t cb = chunk_base[wid];
+  const int64_t nc = (int64_t(N.count) + kChunk - 1) / kChunk;
+  double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int64_t c = lane; c < nc; c += 32) {
+    const double *p = part + (cb + c) * kPartDoubles;
+    for (int q = 0; q < 8; ++q) s[q] += p[q];
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = fminf(lo[d], float(p[8 + d]));
+      hi[d] = fmaxf(hi[d], float(p[11 + d]));
+    }
+  }
+  for (int q = 0; q < 8; ++q) s[q] = warp_sum(s[q]);
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = warp_min(lo[d]);
+    hi[d] = warp_max(hi[d]);
+  }
+  if (lane != 0) return;
+  for (int d = 0; d < 3; ++d) {
+    N.xmin[d] = lo[d];
+    N.xmax[d] = hi[d];
+  }
+  // Both the reference's sequential sum and this tree sum are within
+  // (n - 1 + depth) u sum|terms| of the exact sum (depth < 64 + n); the factor
+  // 2 covers the higher-order terms.
+  const double g = 2.0 * (double(N.count) + 64.0) * 0x1p-53;
+  const double bm = g * s[7];
+  bool ok = !force_fallback;
+  for (int d = 0; d < 3 && ok; ++d) {
+    float v;
+    if (certify(s[d], g * s[4 + d], s[3], bm, &v)) N.xc[d] = v;
+    else ok = false;
+  }
+  if (!ok) {
+    const unsigned long long k = atomicAdd((unsigned long long *)&counters[C_NFALLBACK], 1ull);
+    fallback[k] = node;
+  }
+}
+
+// The reference's centre of mass for the listed nodes, summed sequentially
+// in array order in double (BGQCM.c:186-211).
+__global__ void k_cm_fallback(const float4 *__restrict__ pos, DNode *nodes, const int32_t *fallback,
+                              const int64_t *counters) {
+  const int64_t nf = counters[C_NFALLBACK];
+  for (int64_t f = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; f < nf;
+       f += int64_t(gridDim.x) * blockDim.x) {
+    DNode &N = nodes[fallback[f]];
+    double x = 0, y = 0, z = 0, m = 0;
+    for (int32_t i = 0; i < N.count; ++i) {
+      const float4 p = pos[N.offset + i];
+      x = __dadd_rn(x, double(fmul_(p.w, p.x)));
+      y = __dadd_rn(y, double(fmul_(p.w, p.y)));
+      z = __dadd_rn(z, double(fmul_(p.w, p.z)));
+      m = __dadd_rn(m, double(p.w));
+    }
+    N.xc[0] = __double2float_rn(__ddiv_rn(x, m));
+    N.xc[1] = __double2float_rn(__ddiv_rn(y, m));
+    N.xc[2] = __double2float_rn(__ddiv_rn(z, m));
+  }
+}
+
+// Leaf by size, or the split axis: the longest box edge, ties to the later
+// axis (RCBForceTree.cxx:837-852).
+__global__ void k_split_decide(DNode *nodes, int32_t nb, int32_t ne, int32_t nd) {
+  const int32_t i = nb + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= ne) return;
+  DNode &N = nodes[i];
+  N.nleft = 0;
+  if (N.count <= nd) {
+    N.split_dim = -1;
+    return;
+  }
+  const float l0 = fsub_(N.xmax[0], N.xmin[0]), l1 = fsub_(N.xmax[1], N.xmin[1]),
+              l2 = fsub_(N.xmax[2], N.xmin[2]);
+  N.split_dim = (l0 > l1 && l0 > l2) ? 0 : (l1 > l2 ? 1 : 2);
+}
+
+__device__ __forceinline__ float key_of(const float4 &p, int d) {
+  return d == 0 ? p.x : (d == 1 ? p.y : p.z);
+}
+
+// Block-wide exclusive scan of one int per thread.
+__device__ __forceinline__ int block_excl_scan(int v, int *sh_warp, int *total) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) sh_warp[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int w = lane < (int)(blockDim.x >> 5) ? sh_warp[lane] : 0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    sh_warp[lane] = w;
+  }
+  __syncthreads();
+  const int excl = x - v + (warp > 0 ? sh_warp[warp - 1] : 0);
+  *total = sh_warp[(blockDim.x >> 5) - 1];
+  __syncthreads();
+  return excl;
+}
+
+// Left counts of each chunk of a splitting node.
+__global__ void __launch_bounds__(kChunkThreads)
+    k_part_count(const float4 *__restrict__ pos, const DNode *nodes, const int32_t *chunk_node,
+                 const int64_t *chunk_base, int32_t nb, const int64_t *nchunk, int32_t *left_cnt) {
+  const int64_t chunk = blockIdx.x;
+  if (chunk >= *nchunk) return;
+  const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
+  const DNode &N = nodes[R.node];
+  if (N.split_dim < 0) {
+    if (threadIdx.x == 0) left_cnt[chunk] = 0;
+    return;
+  }
+  const int d = N.split_dim;
+  const float split = N.xc[d];
+  int c = 0;
+  for (int k = threadIdx.x; k < R.len; k += kChunkThreads) c += key_of(pos[R.begin + k], d) < split;
+  __shared__ int sw[32];
+  int tot;
+  block_excl_scan(c, sw, &tot);
+  if (threadIdx.x == 0) left_cnt[chunk] = tot;
+}
+
+// Per splitting node: exclusive scan of its chunks' left counts (in chunk
+// order) and the node's total.
+__global__ void k_part_node_scan(DNode *nodes, int32_t nb, int32_t ne, const int64_t *chunk_base,
+                                 const int32_t *left_cnt, int64_t *left_base) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (nb + i >= ne) return;
+  DNode &N = nodes[nb + i];
+  if (N.split_dim < 0) return;
+  const int64_t cb = chunk_base[i];
+  const int64_t nc = (int64_t(N.count) + kChunk - 1) / kChunk;
+  int64_t run = 0;
+  for (int64_t c = 0; c < nc; ++c) {
+    left_base[cb + c] = run;
+    run += left_cnt[cb + c];
+  }
+  N.nleft = int32_t(run);
+}
+
+// Left particles go to their rank; idx[rank] records where each came from.
+__global__ void __launch_bounds__(kChunkThreads)
+    k_part_left(const float4 *__restrict__ pos, const int32_t *__restrict__ oid, const DNode *nodes,
+                const int32_t *chunk_node, const int64_t *chunk_base, int32_t nb,
+                const int64_t *nchunk, const int64_t *left_base, float4 *tpos, int32_t *toid,
+                int32_t *idx) {
+  const int64_t chunk = blockIdx.x;
+  if (chunk >= *nchunk) return;
+  const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
+  const DNode &N = nodes[R.node];
+  if (N.split_dim < 0) return;
+  const int d = N.split_dim;
+  const float split = N.xc[d];
+  // thread t owns kPer consecutive elements so ranks follow array order
+  const int k0 = threadIdx.x * kPer;
+  unsigned flags = 0;
+  int c = 0;
+  for (int k = 0; k < kPer; ++k) {
+    const int e = k0 + k;
+    if (e < R.len && key_of(pos[R.begin + e], d) < split) {
+      flags |= 1u << k;
+      ++c;
+    }
+  }
+  __shared__ int sw[32];
+  int tot;
+  int r = block_excl_scan(c, sw, &tot) + int(left_base[chunk]);
+  for (int k = 0; k < kPer; ++k) {
+    if (!(flags & (1u << k))) continue;
+    const int e = k0 + k;
+    const int64_t src = R.begin + e;
+    tpos[N.offset + r] = pos[src];
+    toid[N.offset + r] = oid[src];
+    idx[N.offset + r] = R.local + e;
+    ++r;
+  }
+}
+
+// The other particles: those at or after position nleft stay; one at p <
+// nleft moves along p -> idx[p] -> ... until it lands at or after nleft (the
+// reference's swap sequence, RCBForceTree.cxx:647-669).  Positions increase
+// strictly along a chain, so it ends within count steps.
+__global__ void __launch_bounds__(kChunkThreads)
+    k_part_right(const float4 *__restrict__ pos, const int32_t *__restrict__ oid, const DNode *nodes,
+                 const int32_t *chunk_node, const int64_t *chunk_base, int32_t nb,
+                 const int64_t *nchunk, const int32_t *__restrict__ idx, float4 *tpos,
+                 int32_t *toid, int32_t *err) {
+  const int64_t chunk = blockIdx.x;
+  if (chunk >= *nchunk) return;
+  const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
+  const DNode &N = nodes[R.node];
+  if (N.split_dim < 0) return;
+  const int d = N.split_dim;
+  const float split = N.xc[d];
+  const int32_t is = N.nleft;
+  for (int k = threadIdx.x; k < R.len; k += kChunkThreads) {
+    const int64_t src = R.begin + k;
+    const float4 p = pos[src];
+    if (key_of(p, d) < split) continue;
+    int32_t q = R.local + k;
+    int32_t steps = 0;
+    while (q < is && steps++ <= N.count) {
+      const int32_t nq = idx[N.offset + q];
+      if (nq <= q || nq >= N.count) {  // cannot happen for a valid partition
+        atomicExch(err, 2);
+        break;
+      }
+      q = nq;
+    }
+    if (q < is) {
+      atomicExch(err, 2);
+      continue;
+    }
+    tpos[N.offset + q] = p;
+    toid[N.offset + q] = oid[src];
+  }
+}
+
+__global__ void __launch_bounds__(kChunkThreads)
+    k_part_copyback(float4 *pos, int32_t *oid, const DNode *nodes, const int32_t *chunk_node,
+                    const int64_t *chunk_base, int32_t nb, const int64_t *nchunk,
+                    const float4 *tpos, const int32_t *toid) {
+  const int64_t chunk = blockIdx.x;
+  if (chunk >= *nchunk) return;
+  const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
+  if (nodes[R.node].split_dim < 0) return;
+  for (int k = threadIdx.x; k < R.len; k += kChunkThreads) {
+    pos[R.begin + k] = tpos[R.begin + k];
+    oid[R.begin + k] = toid[R.begin + k];
+  }
+}
+
+// 1 for nodes whose split produced two non-empty children.
+__global__ void k_split_flags(const DNode *nodes, int32_t nb, int32_t ne, int64_t *flag) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (nb + i >= ne) return;
+  const DNode &N = nodes[nb + i];
+  flag[i] = (N.split_dim >= 0 && N.nleft > 0 && N.nleft < N.count) ? 1 : 0;
+}
+
+__global__ void k_children(DNode *nodes, int32_t nb, int32_t ne, const int64_t *rank) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (nb + i >= ne) return;
+  DNode &N = nodes[nb + i];
+  if (!(N.split_dim >= 0 && N.nleft > 0 && N.nleft < N.count)) {
+    N.cl = N.cr = 0;
+    return;
+  }
+  const int32_t cl = ne + 2 * int32_t(rank[i]), cr = cl + 1;
+  N.cl = cl;
+  N.cr = cr;
+  for (int s = 0; s < 2; ++s) {
+    DNode &C = nodes[s == 0 ? cl : cr];
+    C.count = s == 0 ? N.nleft : N.count - N.nleft;
+    C.offset = s == 0 ? N.offset : N.offset + N.nleft;
+    C.cl = C.cr = 0;
+    for (int d = 0; d < 3; ++d) {
+      C.xmin[d] = N.xmin[d];
+      C.xmax[d] = N.xmax[d];
+      C.xc[d] = 0.f;
+    }
+    C.tdr = 0.f;
+    C.split_dim = -1;
+    C.nleft = 0;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Pseudo-particles (RCBForceTree.cxx:519-569, 788-800, 856-889)
+// ---------------------------------------------------------------------------
+__constant__ float c_design[12][3];
+
+__device__ __forceinline__ float pptdr_(const DNode &t) {
+  return smin_(fsub_(t.xmax[0], t.xc[0]),
+               smin_(fsub_(t.xmax[1], t.xc[1]),
+                     smin_(fsub_(t.xmax[2], t.xc[2]),
+                           smin_(fsub_(t.xc[0], t.xmin[0]),
+                                 smin_(fsub_(t.xc[1], t.xmin[1]), fsub_(t.xc[2], t.xmin[2]))))));
+}
+
+__device__ __forceinline__ void pppts_(int k, float tdr, const float *xc, float *px, float *py,
+                                       float *pz) {
+  for (int i = 0; i < k; ++i) {
+    px[i] = fadd_(fmul_(tdr, c_design[i][0]), xc[0]);
+    py[i] = fadd_(fmul_(tdr, c_design[i][1]), xc[1]);
+    pz[i] = fadd_(fmul_(tdr, c_design[i][2]), xc[2]);
+  }
+}
+
+// Adds `count` sources (x, y, z, m from src(i)) to the pseudo-particle masses.
+template <typename Src>
+__device__ void pp_accum_(int k, int32_t count, Src src, const float *xc, const float *px,
+                          const float *py, const float *pz, float *ppm, float tdr) {
+  const float K = float(k);
+  const float odr0 = __fdiv_rn(1.0f, K);
+  for (int32_t i = 0; i < count; ++i) {
+    float sx, sy, sz, sm;
+    src(i, sx, sy, sz, sm);
+    const float xi = fsub_(sx, xc[0]), yi = fsub_(sy, xc[1]), zi = fsub_(sz, xc[2]);
+    const float ri = __fsqrt_rn(norm2_(xi, yi, zi));
+    for (int j = 0; j < k; ++j) {
+      const float xj = fsub_(px[j], xc[0]), yj = fsub_(py[j], xc[1]), zj = fsub_(pz[j], xc[2]);
+      const float rj2 = norm2_(xj, yj, zj);
+      float odr1 = 0.f, odr2 = 0.f;
+      if (rj2 != 0.f) {
+        const float rj = __fsqrt_rn(rj2);
+        const float aij = __fdiv_rn(fadd_(fadd_(fmul_(xi, xj), fmul_(yi, yj)), fmul_(zi, zj)),
+                                    fmul_(ri, rj));
+        const float rt = __fdiv_rn(ri, tdr);
+        odr1 = fmul_(fmul_(__fdiv_rn(3.0f, K), rt), aij);
+        const float a = fmul_(fmul_(__fdiv_rn(5.0f, K), rt), rt);
+        const float b = fsub_(fmul_(fmul_(3.0f, aij), aij), 1.0f);
+        odr2 = __double2float_rn(__dmul_rn(__dmul_rn(double(a), 0.5), double(b)));
+      }
+      ppm[j] = fadd_(ppm[j], fmul_(sm, fadd_(fadd_(odr0, odr1), odr2)));
+    }
+  }
+}
+
+// Pseudo-particles of the nodes [lb, le), children done first.
+__global__ void k_pseudo(DNode *nodes, int32_t lb, int32_t le, const float4 *__restrict__ pos,
+                         float *ppm_all, int k, float ppc, int32_t nd) {
+  const int32_t t = lb + blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= le) return;
+  DNode &T = nodes[t];
+  T.tdr = fmul_(ppc, pptdr_(T));
+  float ppm[12];
+  for (int j = 0; j < 12; ++j) ppm[j] = 0.f;
+  float px[12], py[12], pz[12];
+  if (T.cl == 0 && T.cr == 0) {
+    // leaf by size: masses from its particles when it has more than k;
+    // a leaf left by a failed split keeps zero masses (its children are empty)
+    if (T.count <= nd && T.count > k) {
+      pppts_(k, T.tdr, T.xc, px, py, pz);
+      const float4 *p = pos + T.offset;
+      pp_accum_(k, T.count, [&](int32_t i, float &x, float &y, float &z, float &m) {
+        const float4 q = p[i];
+        x = q.x; y = q.y; z = q.z; m = q.w;
+      }, T.xc, px, py, pz, ppm, T.tdr);
+    }
+  } else {
+    pppts_(k, T.tdr, T.xc, px, py, pz);
+    for (int s = 0; s < 2; ++s) {
+      const DNode &C = nodes[s == 0 ? T.cl : T.cr];
+      if (C.count <= 0) continue;
+      if (C.count <= k) {
+        const float4 *p = pos + C.offset;
+        pp_accum_(k, C.count, [&](int32_t i, float &x, float &y, float &z, float &m) {
+          const float4 q = p[i];
+          x = q.x; y = q.y; z = q.z; m = q.w;
+        }, T.xc, px, py, pz, ppm, T.tdr);
+      } else {
+        float cx[12], cy[12], cz[12];
+        pppts_(k, C.tdr, C.xc, cx, cy, cz);
+        const float *cm = ppm_all + int64_t(s == 0 ? T.cl : T.cr) * k;
+        pp_accum_(k, k, [&](int32_t i, float &x, float &y, float &z, float &m) {
+          x = cx[i]; y = cy[i]; z = cz[i]; m = cm[i];
+        }, T.xc, px, py, pz, ppm, T.tdr);
+      }
+    }
+  }
+  for (int j = 0; j < k; ++j) ppm_all[int64_t(t) * k + j] = ppm[j];
+}
+
+// Position table: particles, then every node's pseudo-particles.
+__global__ void k_table_pseudo(const DNode *nodes, int32_t nnodes, const float *ppm_all, int k,
+                               float4 *table, int64_t n) {
+  const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nnodes) return;
+  const DNode &T = nodes[t];
+  float px[12], py[12], pz[12];
+  pppts_(k, T.tdr, T.xc, px, py, pz);
+  for (int j = 0; j < k; ++j)
+    table[n + int64_t(t) * k + j] = make_float4(px[j], py[j], pz[j], ppm_all[int64_t(t) * k + j]);
+}
+
+// ---------------------------------------------------------------------------
+// Processed leaves (calcInternodeForces, RCBForceTree.cxx:1150-1197): leaves
+// inside the force box, in the reference's DFS order, which visits the right
+// child first, i.e. by decreasing particle offset.
+// ---------------------------------------------------------------------------
+__global__ void k_mark_leaves(const DNode *nodes, int32_t nnodes, TreeConfig cfg, int64_t n,
+                              int64_t *leaf_at) {
+  const int32_t t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= nnodes) return;
+  const DNode &T = nodes[t];
+  if (T.cl != 0 || T.cr != 0 || T.count <= 0) return;
+  bool inside = true;
+  for (int i = 0; i < 3; ++i)
+    inside &= (T.xmax[i] < cfg.max_force[i] && T.xmax[i] > cfg.min_force[i]) ||
+              (T.xmin[i] < cfg.max_force[i] && T.xmin[i] > cfg.min_force[i]);
+  if (inside) leaf_at[n - 1 - T.offset] = t;  // reversed: decreasing offset
+}
+
+__global__ void k_leaf_flags(const int64_t *leaf_at, int64_t n, int64_t *flag) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n) flag[i] = leaf_at[i] >= 0;
+}
+
+__global__ void k_leaf_compact(const int64_t *leaf_at, const int64_t *pos_of, int64_t n,
+                               int32_t *leaf_ids) {
+  const int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (i < n && leaf_at[i] >= 0) leaf_ids[pos_of[i]] = int32_t(leaf_at[i]);
+}
+
+// ---------------------------------------------------------------------------
+// Interaction lists (calcInternodeForce, RCBForceTree.cxx:923-1144), one
+// thread per processed leaf; a counting pass and a writing pass.
+// ---------------------------------------------------------------------------
+template <bool WRITE>
+__global__ void k_walk(const DNode *__restrict__ nodes, int32_t nnodes, const int32_t *leaf_ids,
+                       int64_t nleaves, TreeConfig cfg, int64_t n, int64_t *seg_cnt, int64_t *list_len,
+                       const int64_t *seg_base, const int64_t *list_base, SegDesc *segs,
+                       int32_t *err) {
+  const int64_t li = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (li >= nleaves) return;
+  const int32_t tl = leaf_ids[li];
+  const DNode T = nodes[tl];
+  const float fsr = cfg.fsrrmax;
+  const float fsr2 = fmul_(fsr, fsr);
+  const float tan_oa = cfg.tan_oa;
+  const int k = cfg.tdpts;
+  int32_t stack[kWalkStack];
+  int sp = 0;
+  int64_t nseg = 0, len = 0;
+  const int64_t sb = WRITE ? seg_base[li] : 0, lb = WRITE ? list_base[li] : 0;
+  auto emit = [&](int64_t start, int64_t count) {
+    if (count <= 0) return;
+    if (WRITE) segs[sb + nseg] = SegDesc{int32_t(start), int32_t(count), lb + len};
+    ++nseg;
+    len += count;
+  };
+  auto push = [&](int32_t v) {
+    if (sp < kWalkStack) stack[sp++] = v;
+    else atomicExch(err, 1);
+  };
+  auto close_to = [&](const DNode &C) {
+    for (int i = 0; i < 3; ++i) {
+      float dist = 0.f;
+      if (T.xmax[i] < C.xmin[i]) dist = fsub_(C.xmin[i], T.xmax[i]);
+      else if (T.xmin[i] > C.xmax[i]) dist = fsub_(T.xmin[i], C.xmax[i]);
+      if (dist > fsr) return false;
+    }
+    return true;
+  };
+  push(0);
+  int64_t pops = 0;
+  while (sp > 0) {
+    if (++pops > int64_t(nnodes) + 1) {  // a tree walk visits each node at most once
+      atomicExch(err, 3);
+      break;
+    }
+    const int32_t t = stack[--sp];
+    if (t < 0 || t >= nnodes) {
+      atomicExch(err, 3);
+      break;
+    }
+    const DNode Q = nodes[t];
+    if (Q.cl >= nnodes || Q.cr >= nnodes) {
+      atomicExch(err, 3);
+      break;
+    }
+    if (t != tl && Q.offset <= T.offset && T.offset + T.count <= Q.offset + Q.count) {
+      if (Q.cl != tl && Q.cl > 0 && nodes[Q.cl].count > 0) push(Q.cl);
+      if (Q.cr != tl && Q.cr > 0 && nodes[Q.cr].count > 0) push(Q.cr);
+      continue;
+    }
+    const float dx = fsub_(Q.xc[0], T.xc[0]), dy = fsub_(Q.xc[1], T.xc[1]),
+                dz = fsub_(Q.xc[2], T.xc[2]);
+    const float dist2 = norm2_(dx, dy, dz);
+    const float sx = fsub_(Q.xmax[0], Q.xmin[0]), sy = fsub_(Q.xmax[1], Q.xmin[1]),
+                sz = fsub_(Q.xmax[2], Q.xmin[2]);
+    const float l2 = smin_(fmul_(sx, sx), smin_(fmul_(sy, sy), fmul_(sz, sz)));
+    const float dtt2 = fmul_(fmul_(dist2, tan_oa), tan_oa);
+    bool big = l2 > dtt2;
+    for (int i = 0; i < 2 && !big; ++i)
+      for (int j = 0; j < 2 && !big; ++j) {
+        const float x1 = fsub_((i == 0 ? Q.xmin : Q.xmax)[0], T.xc[0]);
+        const float y1 = fsub_((j == 0 ? Q.xmin : Q.xmax)[1], T.xc[1]);
+        const float z1 = fsub_(Q.xmin[2], T.xc[2]);
+        const float x2 = fsub_((i == 0 ? Q.xmax : Q.xmin)[0], T.xc[0]);
+        const float y2 = fsub_((j == 0 ? Q.xmax : Q.xmin)[1], T.xc[1]);
+        const float z2 = fsub_(Q.xmax[2], T.xc[2]);
+        big = norm2_(fsub_(x1, x2), fsub_(y1, y2), fsub_(z1, z2)) > dtt2;
+      }
+    if (!big) {
+      if (dist2 > fsr2) continue;
+      if (Q.count <= k) emit(Q.offset, Q.count);
+      else emit(n + int64_t(t) * k, k);
+      continue;
+    }
+    if (Q.cr == 0 && Q.cl == 0) {
+      emit(Q.offset, Q.count);
+      continue;
+    }
+    if (Q.cl > 0 && nodes[Q.cl].count > 0 && close_to(nodes[Q.cl])) push(Q.cl);
+    if (Q.cr > 0 && nodes[Q.cr].count > 0 && close_to(nodes[Q.cr])) push(Q.cr);
+  }
+  emit(T.offset, T.count);
+  if (!WRITE) {
+    seg_cnt[li] = nseg;
+    list_len[li] = len;
+  }
+}
+
+__global__ void k_leaf_desc(const DNode *nodes, const int32_t *leaf_ids, int64_t nleaves,
+                            const int64_t *list_len, const int64_t *list_base, LeafDesc *ld,
+                            int64_t *counters) {
+  const int64_t li = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  long long pairs = 0, padded = 0, mx = 0;
+  if (li < nleaves) {
+    const DNode &T = nodes[leaf_ids[li]];
+    LeafDesc d{};
+    d.offset = T.offset;
+    d.count = T.count;
+    d.list_len = int32_t(list_len[li]);
+    d.list_begin = list_base[li];
+    ld[li] = d;
+    pairs = (long long)T.count * list_len[li];
+    padded = (long long)((T.count + 31) / 32) * 32 * list_len[li];
+    mx = list_len[li];
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
+    padded += __shfl_xor_sync(0xffffffffu, padded, o);
+    mx = max(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  }
+  if ((threadIdx.x & 31) == 0) {
+    atomicAdd((unsigned long long *)&counters[C_PAIRS], (unsigned long long)pairs);
+    atomicAdd((unsigned long long *)&counters[C_PADDED], (unsigned long long)padded);
+    atomicMax((long long *)&counters[C_MAXLEN], mx);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Groups of <= 32 spatially close particles per processed leaf (Morton order
+// inside the leaf's box) and the batched kernel's work items.
+// ---------------------------------------------------------------------------
+constexpr int kGroupSort = 1024;
+
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+  v &= 0x3ff;
+  v = (v | (v << 16)) & 0x030000ff;
+  v = (v | (v << 8)) & 0x0300f00f;
+  v = (v | (v << 4)) & 0x030c30c3;
+  v = (v | (v << 2)) & 0x09249249;
+  return v;
+}
+
+__global__ void __launch_bounds__(256)
+    k_groups(const DNode *nodes, const int32_t *leaf_ids, int64_t nleaves,
+             const float4 *__restrict__ pos, int32_t *gidx) {
+  __shared__ uint64_t key[kGroupSort];
+  const int64_t li = blockIdx.x;
+  if (li >= nleaves) return;
+  const DNode &T = nodes[leaf_ids[li]];
+  const int32_t c = T.count;
+  if (c > kGroupSort) {
+    for (int32_t i = threadIdx.x; i < c; i += blockDim.x) gidx[T.offset + i] = T.offset + i;
+    return;
+  }
+  int m = 1;
+  while (m < c) m <<= 1;
+  float sc[3];
+  for (int d = 0; d < 3; ++d) {
+    const float ext = T.xmax[d] - T.xmin[d];
+    sc[d] = ext > 0.f ? 1023.0f / ext : 0.f;
+  }
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    uint64_t kv = ~0ull;
+    if (i < c) {
+      const float4 p = pos[T.offset + i];
+      const uint32_t qx = uint32_t(fminf(fmaxf((p.x - T.xmin[0]) * sc[0], 0.f), 1023.f));
+      const uint32_t qy = uint32_t(fminf(fmaxf((p.y - T.xmin[1]) * sc[1], 0.f), 1023.f));
+      const uint32_t qz = uint32_t(fminf(fmaxf((p.z - T.xmin[2]) * sc[2], 0.f), 1023.f));
+      const uint32_t mort = (spread3(qx) << 2) | (spread3(qy) << 1) | spread3(qz);
+      kv = (uint64_t(mort) << 32) | uint32_t(i);
+    }
+    key[i] = kv;
+  }
+  __syncthreads();
+  for (int size = 2; size <= m; size <<= 1)
+    for (int stride = size >> 1; stride > 0; stride >>= 1) {
+      for (int i = threadIdx.x; i < m; i += blockDim.x) {
+        const int j = i ^ stride;
+        if (j > i) {
+          const bool up = (i & size) == 0;
+          const uint64_t a = key[i], b = key[j];
+          if ((a > b) == up) {
+            key[i] = b;
+            key[j] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  for (int i = threadIdx.x; i < c; i += blockDim.x)
+    gidx[T.offset + i] = T.offset + int32_t(key[i] & 0xffffffffu);
+}
+
+__device__ __forceinline__ int len_bucket(int64_t len) {
+  // 32 buckets, longest lists first
+  const int b = 63 - __clzll((unsigned long long)max64(len, 1));
+  return 31 - min(31, b);
+}
+
+__global__ void k_item_hist(const LeafDesc *ld, int64_t nleaves, int64_t jsplit,
+                            int64_t *counters) {
+  const int64_t li = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (li >= nleaves) return;
+  const LeafDesc &L = ld[li];
+  const int64_t nch = max64(1, (L.list_len + jsplit - 1) / jsplit);
+  const int64_t items = int64_t((L.count + 31) / 32) * nch;
+  atomicAdd((unsigned long long *)&counters[C_BUCKET + len_bucket(min64(L.list_len, jsplit))],
+            (unsigned long long)items);
+}
+
+__global__ void k_item_bases(int64_t *counters) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int64_t run = 0;
+  for (int b = 0; b < 32; ++b) {
+    counters[C_FILL + b] = run;
+    run += counters[C_BUCKET + b];
+  }
+  counters[C_NITEMS] = run;
+}
+
+__global__ void k_item_fill(const LeafDesc *ld, int64_t nleaves, int64_t jsplit, int64_t *counters,
+                            PairItem *items) {
+  const int64_t li = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
+  if (li >= nleaves) return;
+  const LeafDesc &L = ld[li];
+  const int64_t nch = max64(1, (L.list_len + jsplit - 1) / jsplit);
+  const int32_t ng = (L.count + 31) / 32;
+  const int64_t items_n = int64_t(ng) * nch;
+  if (items_n == 0) return;
+  const int b = len_bucket(min64(L.list_len, jsplit));
+  int64_t at = int64_t(atomicAdd((unsigned long long *)&counters[C_FILL + b],
+                                 (unsigned long long)items_n));
+  for (int32_t g = 0; g < ng; ++g)
+    for (int64_t c = 0; c < nch; ++c) {
+      PairItem it{};
+      it.j_begin = L.list_begin + c * jsplit;
+      it.j_len = int32_t(min64(jsplit, L.list_len - c * jsplit));
+      it.g_begin = L.offset + 32 * g;
+      it.g_count = min(32, L.count - 32 * g);
+      it.flags = nch > 1 ? 1 : 0;
+      items[at++] = it;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Gathers and packing
+// ---------------------------------------------------------------------------
+template <typename T>
+__global__ void k_gather(const T *__restrict__ in, const int32_t *__restrict__ perm, T *out,
+                         int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    out[i] = in[perm[i]];
+}
+
+__global__ void k_pack4(const float *x, const float *y, const float *z, const float *m, float4 *out,
+                        int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    out[i] = make_float4(x[i], y[i], z[i], m[i]);
+}
+
+__global__ void k_unpack4(const float4 *in, float *x, float *y, float *z, float *m, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const float4 p = in[i];
+    x[i] = p.x;
+    y[i] = p.y;
+    z[i] = p.z;
+    m[i] = p.w;
+  }
+}
+
+__global__ void k_iota(int32_t *p, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    p[i] = int32_t(i);
+}
+
+__global__ void k_fill_i64(int64_t *p, int64_t n, int64_t v) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    p[i] = v;
+}
+
+__global__ void k_root(DNode *nodes, int64_t n, TreeConfig cfg) {
+  DNode &R = nodes[0];
+  R.count = int32_t(n);
+  R.offset = 0;
+  R.cl = R.cr = 0;
+  for (int d = 0; d < 3; ++d) {
+    R.xmin[d] = cfg.min[d];
+    R.xmax[d] = cfg.max[d];
+    R.xc[d] = 0.f;
+  }
+  R.tdr = 0.f;
+  R.split_dim = -1;
+  R.nleft = 0;
+}
+
+inline unsigned grid_for(int64_t n, int threads, int64_t cap = 152 * 32) {
+  int64_t b = (n + threads - 1) / threads;
+  return unsigned(std::max<int64_t>(1, std::min(b, cap)));
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// Host orchestration
+// ---------------------------------------------------------------------------
+
+DeviceTree::~DeviceTree() {
+  void *ptrs[] = {epos_, tpos_, oid_, toid_, idx_, nodes_, ppm_, chunk_node_, chunk_base_, part_,
+                  left_cnt_, left_base_, scan_tmp_, node_tmp_, fallback_, counters_, leaf_ids_,
+                  leaf_tmp_, leafdesc_, segs_, idx_list_, table_, items_, items_tmp_, gidx_,
+                  walk_err_};
+  for (void *p : ptrs)
+    if (p) cudaFree(p);
+  if (h_counters_) cudaFreeHost(h_counters_);
+}
+
+template <typename T>
+cudaError_t DeviceTree::grow(T *&p, size_t &cap, size_t count, cudaStream_t s, bool keep) {
+  if (count <= cap && p) return cudaSuccess;
+  size_t want = std::max<size_t>(count + count / 4, 256);
+  T *q = nullptr;
+  cudaError_t e = cudaMalloc(&q, want * sizeof(T));
+  if (e != cudaSuccess) return e;
+  if (keep && p && cap) {
+    e = cudaMemcpyAsync(q, p, cap * sizeof(T), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return e;
+    e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return e;
+  }
+  if (p) cudaFree(p);
+  p = q;
+  cap = want;
+  return cudaSuccess;
+}
+
+#define DT_CHECK(x)                         \
+  do {                                      \
+    cudaError_t e_ = (x);                   \
+    if (e_ != cudaSuccess) return e_;       \
+  } while (0)
+
+cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *pos_in, int64_t jsplit,
+                              cudaStream_t s) {
+  info_ = DeviceTreeInfo{};
+  err_ = nullptr;
+  padded_pairs_ = 0;
+  const int k = cfg.tdpts;
+  {
+    float d[12][3];
+    static const float ia = 0.525731112119134f, ib = 0.85065080835204f;
+    const float ico[12][3] = {{0, ib, ia},   {0, ib, -ia},  {ia, 0, ib},   {-ia, 0, ib},
+                              {ib, ia, 0},   {-ib, ia, 0},  {0, -ib, -ia}, {0, -ib, ia},
+                              {-ia, 0, -ib}, {ia, 0, -ib},  {-ib, -ia, 0}, {ib, -ia, 0}};
+    std::memset(d, 0, sizeof(d));
+    if (k == 12) std::memcpy(d, ico, sizeof(d));
+    DT_CHECK(cudaMemcpyToSymbolAsync(c_design, d, sizeof(d), 0, cudaMemcpyHostToDevice, s));
+  }
+  const size_t nn = size_t(std::max<int64_t>(n, 1));
+  DT_CHECK(grow(epos_, cap_e_, nn, s));
+  DT_CHECK(grow(tpos_, cap_t_, nn, s));
+  DT_CHECK(grow(oid_, cap_o_, nn, s));
+  DT_CHECK(grow(toid_, cap_to_, nn, s));
+  DT_CHECK(grow(idx_, cap_i_, nn, s));
+  if (!counters_) {
+    DT_CHECK(cudaMalloc(&counters_, C_COUNT * sizeof(int64_t)));
+    DT_CHECK(cudaHostAlloc(&h_counters_, C_COUNT * sizeof(int64_t), cudaHostAllocDefault));
+    DT_CHECK(cudaMalloc(&walk_err_, sizeof(int32_t)));
+  }
+  DT_CHECK(cudaMemsetAsync(counters_, 0, C_COUNT * sizeof(int64_t), s));
+  DT_CHECK(cudaMemsetAsync(walk_err_, 0, sizeof(int32_t), s));
+  if (n > 0) {
+    DT_CHECK(cudaMemcpyAsync(epos_, pos_in, size_t(n) * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+    k_iota<<<grid_for(n, 256), 256, 0, s>>>(oid_, n);
+  }
+  size_t want_nodes = size_t(std::max<int64_t>(64, 4 * n / std::max(1, cfg.nd) + 64));
+  DT_CHECK(grow(nodes_, cap_nodes_, want_nodes, s));
+  k_root<<<1, 1, 0, s>>>(nodes_, n, cfg);
+  DT_CHECK(cudaGetLastError());
+
+  // ---- levels ----
+  std::vector<int32_t> level_begin{0};
+  int32_t nb = 0, ne = 1;
+  while (ne > nb) {
+    const int32_t L = ne - nb;
+    if (size_t(ne) + 2 * size_t(L) > cap_nodes_)
+      DT_CHECK(grow(nodes_, cap_nodes_, size_t(ne) + 2 * size_t(L), s, true));
+    DT_CHECK(grow(node_tmp_, cap_nt_, size_t(L) + 1, s));
+    DT_CHECK(grow(chunk_base_, cap_cb_, size_t(L) + 1, s));
+    DT_CHECK(grow(scan_tmp_, cap_scan_, size_t(scan_tmp_size(std::max<int64_t>(L, n + 1))), s));
+    DT_CHECK(grow(fallback_, cap_fb_, size_t(L), s));
+    const int64_t max_chunks = n / kChunk + L + 1;
+    DT_CHECK(grow(chunk_node_, cap_cn_, size_t(max_chunks), s));
+    DT_CHECK(grow(part_, cap_part_, size_t(max_chunks) * kPartDoubles, s));
+    DT_CHECK(grow(left_cnt_, cap_lc_, size_t(max_chunks), s));
+    DT_CHECK(grow(left_base_, cap_lb_, size_t(max_chunks), s));
+    DT_CHECK(cudaMemsetAsync(counters_ + C_NFALLBACK, 0, sizeof(int64_t), s));
+
+    const unsigned gL = unsigned((L + 127) / 128);
+    k_chunk_counts<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
+    DT_CHECK(exclusive_scan_i64(node_tmp_, chunk_base_, L, counters_ + C_NCHUNK, scan_tmp_, s));
+    k_chunk_fill<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, chunk_node_);
+    const unsigned gC = unsigned(max_chunks);
+    k_stats_partial<<<gC, kChunkThreads, 0, s>>>(epos_, nodes_, chunk_node_, chunk_base_, nb,
+                                                 counters_ + C_NCHUNK, part_);
+    k_stats_final<<<unsigned((int64_t(L) * 32 + 255) / 256), 256, 0, s>>>(
+        nodes_, nb, ne, chunk_base_, part_, fallback_, counters_, cfg.force_cm_fallback);
+    k_cm_fallback<<<unsigned(std::min<int64_t>((L + 127) / 128, 1024)), 128, 0, s>>>(
+        epos_, nodes_, fallback_, counters_);
+    k_split_decide<<<gL, 128, 0, s>>>(nodes_, nb, ne, cfg.nd);
+    k_part_count<<<gC, kChunkThreads, 0, s>>>(epos_, nodes_, chunk_node_, chunk_base_, nb,
+                                              counters_ + C_NCHUNK, left_cnt_);
+    k_part_node_scan<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, left_cnt_, left_base_);
+    k_part_left<<<gC, kChunkThreads, 0, s>>>(epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
+                                             counters_ + C_NCHUNK, left_base_, tpos_, toid_, idx_);
+    k_part_right<<<gC, kChunkThreads, 0, s>>>(epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
+                                              counters_ + C_NCHUNK, idx_, tpos_, toid_, walk_err_);
+    k_part_copyback<<<gC, kChunkThreads, 0, s>>>(epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
+                                                 counters_ + C_NCHUNK, tpos_, toid_);
+    k_split_flags<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
+    DT_CHECK(exclusive_scan_i64(node_tmp_, node_tmp_, L, counters_ + C_NSPLIT, scan_tmp_, s));
+    k_children<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
+    DT_CHECK(cudaGetLastError());
+    DT_CHECK(cudaMemcpyAsync(h_counters_, counters_, 4 * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    int32_t perr = 0;
+    DT_CHECK(cudaMemcpyAsync(&perr, walk_err_, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    DT_CHECK(cudaStreamSynchronize(s));
+    if (perr) {
+      err_ = "partition chain check failed";
+      return cudaErrorUnknown;
+    }
+    info_.cm_fallbacks += h_counters_[C_NFALLBACK];
+    const int64_t nsplit = h_counters_[C_NSPLIT];
+    nb = ne;
+    ne = int32_t(ne + 2 * nsplit);
+    level_begin.push_back(nb);
+  }
+  const int32_t nnodes = ne;
+  info_.nodes = nnodes;
+  info_.levels = int64_t(level_begin.size()) - 1;
+
+  // ---- pseudo-particles, deepest level first ----
+  DT_CHECK(grow(ppm_, cap_ppm_, size_t(nnodes) * k + 1, s));
+  for (int64_t l = int64_t(level_begin.size()) - 2; l >= 0; --l) {
+    const int32_t lb = level_begin[l], le = level_begin[l + 1];
+    if (le > lb)
+      k_pseudo<<<unsigned((le - lb + 127) / 128), 128, 0, s>>>(nodes_, lb, le, epos_, ppm_, k,
+                                                               cfg.ppc, cfg.nd);
+  }
+  const int64_t ntab = n + int64_t(nnodes) * k;
+  DT_CHECK(grow(table_, cap_tab_, size_t(std::max<int64_t>(ntab, 1)), s));
+  if (n > 0)
+    DT_CHECK(cudaMemcpyAsync(table_, epos_, size_t(n) * sizeof(float4), cudaMemcpyDeviceToDevice, s));
+  k_table_pseudo<<<unsigned((nnodes + 127) / 128), 128, 0, s>>>(nodes_, nnodes, ppm_, k, table_, n);
+  DT_CHECK(cudaGetLastError());
+
+  // ---- processed leaves in DFS order ----
+  const int64_t nl_cap = std::max<int64_t>(n, 1);
+  DT_CHECK(grow(leaf_tmp_, cap_lt_, size_t(2 * nl_cap), s));
+  DT_CHECK(grow(leaf_ids_, cap_leaf_, size_t(nl_cap), s));
+  DT_CHECK(grow(scan_tmp_, cap_scan_, size_t(scan_tmp_size(nl_cap)), s));
+  int64_t *leaf_at = leaf_tmp_, *lflag = leaf_tmp_ + nl_cap;
+  k_fill_i64<<<grid_for(nl_cap, 256), 256, 0, s>>>(leaf_at, nl_cap, -1);
+  k_mark_leaves<<<unsigned((nnodes + 127) / 128), 128, 0, s>>>(nodes_, nnodes, cfg, n, leaf_at);
+  k_leaf_flags<<<unsigned((nl_cap + 255) / 256), 256, 0, s>>>(leaf_at, nl_cap, lflag);
+  DT_CHECK(exclusive_scan_i64(lflag, lflag, nl_cap, counters_ + C_NLEAF, scan_tmp_, s));
+  k_leaf_compact<<<unsigned((nl_cap + 255) / 256), 256, 0, s>>>(leaf_at, lflag, nl_cap, leaf_ids_);
+  DT_CHECK(cudaGetLastError());
+  DT_CHECK(cudaMemcpyAsync(h_counters_ + C_NLEAF, counters_ + C_NLEAF, sizeof(int64_t),
+                           cudaMemcpyDeviceToHost, s));
+  DT_CHECK(cudaStreamSynchronize(s));
+  const int64_t nleaves = h_counters_[C_NLEAF];
+  info_.processed_leaves = nleaves;
+
+  // ---- lists: count, scan, write ----
+  const size_t nlw = size_t(std::max<int64_t>(nleaves, 1));
+  DT_CHECK(grow(node_tmp_, cap_nt_, 4 * nlw + 4, s));
+  int64_t *seg_cnt = node_tmp_, *list_len = node_tmp_ + nlw, *seg_base = node_tmp_ + 2 * nlw,
+          *list_base = node_tmp_ + 3 * nlw;
+  DT_CHECK(grow(scan_tmp_, cap_scan_, size_t(scan_tmp_size(int64_t(nlw))), s));
+  if (nleaves > 0) {
+    k_walk<false><<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(
+        nodes_, nnodes, leaf_ids_, nleaves, cfg, n, seg_cnt, list_len, nullptr, nullptr, nullptr, walk_err_);
+    DT_CHECK(exclusive_scan_i64(seg_cnt, seg_base, nleaves, counters_ + C_NSEG, scan_tmp_, s));
+    DT_CHECK(exclusive_scan_i64(list_len, list_base, nleaves, counters_ + C_NENT, scan_tmp_, s));
+  }
+  DT_CHECK(cudaGetLastError());
+  DT_CHECK(cudaMemcpyAsync(h_counters_ + C_NSEG, counters_ + C_NSEG, 2 * sizeof(int64_t),
+                           cudaMemcpyDeviceToHost, s));
+  int32_t h_err = 0;
+  DT_CHECK(cudaMemcpyAsync(&h_err, walk_err_, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  DT_CHECK(cudaStreamSynchronize(s));
+  if (h_err) {
+    err_ = h_err == 1 ? "interaction-list walk exceeded its stack"
+                      : "interaction-list walk visited more nodes than the tree has";
+    return cudaErrorUnknown;
+  }
+  const int64_t nseg = nleaves > 0 ? h_counters_[C_NSEG] : 0;
+  const int64_t nent = nleaves > 0 ? h_counters_[C_NENT] : 0;
+  info_.segments = nseg;
+  info_.list_entries = nent;
+  DT_CHECK(grow(segs_, cap_seg_, size_t(std::max<int64_t>(nseg, 1)), s));
+  DT_CHECK(grow(idx_list_, cap_idx_, size_t(std::max<int64_t>(nent, 1)), s));
+  DT_CHECK(grow(leafdesc_, cap_ld_, nlw, s));
+  if (nleaves > 0) {
+    k_walk<true><<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(
+        nodes_, nnodes, leaf_ids_, nleaves, cfg, n, nullptr, nullptr, seg_base, list_base, segs_, walk_err_);
+    DT_CHECK(launch_expand_segments(segs_, nseg, idx_list_, s));
+    k_leaf_desc<<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(nodes_, leaf_ids_, nleaves, list_len,
+                                                                list_base, leafdesc_, counters_);
+  }
+  DT_CHECK(cudaGetLastError());
+
+  // ---- groups and work items ----
+  DT_CHECK(grow(gidx_, cap_gidx_, nn, s));
+  if (nleaves > 0) {
+    k_groups<<<unsigned(nleaves), 256, 0, s>>>(nodes_, leaf_ids_, nleaves, epos_, gidx_);
+    k_item_hist<<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(leafdesc_, nleaves, jsplit, counters_);
+    k_item_bases<<<1, 32, 0, s>>>(counters_);
+  }
+  DT_CHECK(cudaGetLastError());
+  DT_CHECK(cudaMemcpyAsync(h_counters_, counters_, C_COUNT * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+  DT_CHECK(cudaStreamSynchronize(s));
+  const int64_t nitems = nleaves > 0 ? h_counters_[C_NITEMS] : 0;
+  info_.items = nitems;
+  info_.pairs = h_counters_[C_PAIRS];
+  padded_pairs_ = h_counters_[C_PADDED];
+  DT_CHECK(grow(items_, cap_items_, size_t(std::max<int64_t>(nitems, 1)), s));
+  if (nitems > 0)
+    k_item_fill<<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(leafdesc_, nleaves, jsplit, counters_,
+                                                               items_);
+  DT_CHECK(cudaGetLastError());
+  return cudaSuccess;
+}
+
+cudaError_t launch_gather_f32(const float *in, const int32_t *perm, float *out, int64_t n,
+                              cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_gather<float><<<grid_for(n, 256), 256, 0, s>>>(in, perm, out, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_gather_i64(const int64_t *in, const int32_t *perm, int64_t *out, int64_t n,
+                              cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_gather<int64_t><<<grid_for(n, 256), 256, 0, s>>>(in, perm, out, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_gather_u16(const uint16_t *in, const int32_t *perm, uint16_t *out, int64_t n,
+                              cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_gather<uint16_t><<<grid_for(n, 256), 256, 0, s>>>(in, perm, out, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_pack4(const float *x, const float *y, const float *z, const float *m,
+                         float4 *out, int64_t n, cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_pack4<<<grid_for(n, 256), 256, 0, s>>>(x, y, z, m, out, n);
+  return cudaGetLastError();
+}
+cudaError_t launch_unpack4(const float4 *in, float *x, float *y, float *z, float *m, int64_t n,
+                           cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_unpack4<<<grid_for(n, 256), 256, 0, s>>>(in, x, y, z, m, n);
+  return cudaGetLastError();
+}
+
+}  // namespace hsr

@@ -1,0 +1,156 @@
+// rcb_device.cuh -- the RCB tree build, the interaction lists and the
+// batched work description on the GPU.
+//
+// Reproduces the reference exactly (the same permutation of the particle
+// arrays, the same centres of mass, bounding boxes, pseudo-particles and
+// interaction lists) as the host implementation in rcb_host.cpp:
+//   build  : src/halo_finder/RCBForceTree.cxx:623-918, src/halo_finder/BGQCM.c:181-212
+//   lists  : src/halo_finder/RCBForceTree.cxx:923-1197
+// Level by level, all nodes of a level at once:
+//   * bounding box and centre of mass per node by a chunked segmented
+//     reduction.  The reference sums the centre of mass in double in array
+//     order; the parallel sum differs from it by at most a bound covering both
+//     summation orders.  When both ends of that bound round to the same float,
+//     that float is the reference's centre of mass; otherwise (rare, ~1e-2 of
+//     the root's coordinates) one thread repeats the reference's sequential
+//     sum for that node.
+//   * the partition at the centre of mass: ranks of the "left" particles by a
+//     scan; the reference's swap sequence moves each remaining particle along
+//     a chain of left positions (p -> idx[p] -> ...), which one thread per
+//     particle follows (chains average two steps).
+// Every float expression that decides the tree or a list uses explicitly
+// rounded intrinsics so no multiply-add is fused, as in the reference.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "sr_kernels.cuh"
+
+namespace hsr {
+
+// Tree node on the device (the reference's TreeNode, RCBForceTree.h:131-147).
+struct alignas(16) DNode {
+  int32_t count, offset, cl, cr;  // cl == cr == 0: leaf
+  float xmin[3], xmax[3], xc[3], tdr;
+  int32_t split_dim;              // -1: no split attempted (leaf by size)
+  int32_t nleft;                  // particles below the split (partition result)
+};
+
+struct TreeConfig {
+  float min[3], max[3], min_force[3], max_force[3];
+  float fsrrmax, tan_oa, ppc;
+  int32_t nd, tdpts;
+  int32_t force_cm_fallback;  // test hook: every node takes the sequential sum
+};
+
+// Result sizes of a device build.
+struct DeviceTreeInfo {
+  int64_t nodes = 0, levels = 0, leaves = 0, processed_leaves = 0;
+  int64_t segments = 0, list_entries = 0, pairs = 0, items = 0;
+  int64_t cm_fallbacks = 0;
+};
+
+// Owns the device buffers of one tree; reused across calls (grows only).
+class DeviceTree {
+ public:
+  DeviceTree() = default;
+  ~DeviceTree();
+  DeviceTree(const DeviceTree &) = delete;
+  DeviceTree &operator=(const DeviceTree &) = delete;
+
+  // Builds the tree over n particles whose (x, y, z, m) are in `pos_in`
+  // (float4, device).  Afterwards `perm()` maps each final position to its
+  // input index, `table()` holds the position table (particles in tree order,
+  // then tdpts pseudo-particles per node), and the processed leaves' lists,
+  // work items and group index are built.  `jsplit` bounds the list range of
+  // one work item.  Synchronizes `s` a few times per tree level.
+  cudaError_t build(const TreeConfig &cfg, int64_t n, const float4 *pos_in, int64_t jsplit,
+                    cudaStream_t s);
+
+  const DeviceTreeInfo &info() const { return info_; }
+  const int32_t *perm() const { return oid_; }
+  const float4 *table() const { return table_; }
+  const LeafDesc *leaves() const { return leafdesc_; }
+  const SegDesc *segs() const { return segs_; }
+  const int32_t *index() const { return idx_list_; }
+  const PairItem *items() const { return items_; }
+  const int32_t *gidx() const { return gidx_; }
+  const DNode *nodes() const { return nodes_; }
+  const int32_t *leaf_nodes() const { return leaf_ids_; }
+  int64_t padded_pairs() const { return padded_pairs_; }
+  // Whether a device-side bound was hit (walk stack); the build then failed.
+  const char *error() const { return err_; }
+
+ private:
+  template <typename T>
+  cudaError_t grow(T *&p, size_t &cap, size_t count, cudaStream_t s, bool keep = false);
+
+  DeviceTreeInfo info_{};
+  int64_t padded_pairs_ = 0;
+  const char *err_ = nullptr;
+  // elements: current and scratch (x, y, z, m) + input index
+  float4 *epos_ = nullptr, *tpos_ = nullptr;
+  int32_t *oid_ = nullptr, *toid_ = nullptr, *idx_ = nullptr;
+  size_t cap_e_ = 0, cap_t_ = 0, cap_o_ = 0, cap_to_ = 0, cap_i_ = 0;
+  DNode *nodes_ = nullptr;
+  size_t cap_nodes_ = 0;
+  float *ppm_ = nullptr;
+  size_t cap_ppm_ = 0;
+  // per-level work
+  int32_t *chunk_node_ = nullptr;
+  int64_t *chunk_base_ = nullptr;
+  size_t cap_cn_ = 0, cap_cb_ = 0;
+  double *part_ = nullptr;   // per-chunk partial sums
+  size_t cap_part_ = 0;
+  int32_t *left_cnt_ = nullptr;
+  int64_t *left_base_ = nullptr;
+  size_t cap_lc_ = 0, cap_lb_ = 0;
+  int64_t *scan_tmp_ = nullptr;
+  size_t cap_scan_ = 0;
+  int64_t *node_tmp_ = nullptr;
+  size_t cap_nt_ = 0;
+  int32_t *fallback_ = nullptr;
+  size_t cap_fb_ = 0;
+  int64_t *counters_ = nullptr;  // device scalars
+  int64_t *h_counters_ = nullptr;  // pinned mirror
+  // lists
+  int32_t *leaf_ids_ = nullptr;
+  size_t cap_leaf_ = 0;
+  int64_t *leaf_tmp_ = nullptr;
+  size_t cap_lt_ = 0;
+  LeafDesc *leafdesc_ = nullptr;
+  size_t cap_ld_ = 0;
+  SegDesc *segs_ = nullptr;
+  size_t cap_seg_ = 0;
+  int32_t *idx_list_ = nullptr;
+  size_t cap_idx_ = 0;
+  float4 *table_ = nullptr;
+  size_t cap_tab_ = 0;
+  PairItem *items_ = nullptr, *items_tmp_ = nullptr;
+  size_t cap_items_ = 0, cap_items_tmp_ = 0;
+  int32_t *gidx_ = nullptr;
+  size_t cap_gidx_ = 0;
+  int32_t *walk_err_ = nullptr;
+};
+
+// Gathers the caller's arrays into tree order: out[i] = in[perm[i]].
+cudaError_t launch_gather_f32(const float *in, const int32_t *perm, float *out, int64_t n,
+                              cudaStream_t s);
+cudaError_t launch_gather_i64(const int64_t *in, const int32_t *perm, int64_t *out, int64_t n,
+                              cudaStream_t s);
+cudaError_t launch_gather_u16(const uint16_t *in, const int32_t *perm, uint16_t *out, int64_t n,
+                              cudaStream_t s);
+// pos4[i] = (x[i], y[i], z[i], m[i]); and its inverse split.
+cudaError_t launch_pack4(const float *x, const float *y, const float *z, const float *m,
+                         float4 *out, int64_t n, cudaStream_t s);
+cudaError_t launch_unpack4(const float4 *in, float *x, float *y, float *z, float *m, int64_t n,
+                           cudaStream_t s);
+
+// Exclusive prefix sum of n int64 values (in may equal out); *total (device,
+// may be null) receives the sum.  tmp needs scan_tmp_size(n) elements.
+int64_t scan_tmp_size(int64_t n);
+cudaError_t exclusive_scan_i64(const int64_t *in, int64_t *out, int64_t n, int64_t *total,
+                               int64_t *tmp, cudaStream_t s);
+
+}  // namespace hsr

@@ -26,6 +26,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory",
 MEM_HOST, MEM_DEVICE = 0, 1
 LAW_POLY6, LAW_POLY5_STEP16 = 0, 1
 KERNEL_AUTO, KERNEL_PLAIN, KERNEL_BATCHED = 0, 1, 2
+BUILD_DEVICE, BUILD_HOST = 0, 1
 
 # Symbols the library exports (include/hacc_sr.h).
 EXPORTS = ("hsr_create", "hsr_destroy", "hsr_last_error", "hsr_version", "hsr_rcb_kick",
@@ -47,7 +48,7 @@ class HsrParams(C.Structure):
                 ("open_angle", C.c_float), ("nd", C.c_int64), ("ds", C.c_int64),
                 ("tmin", C.c_int64), ("fcoeff", C.c_float), ("ppc", C.c_float),
                 ("tdpts", C.c_int32), ("law", C.c_int32), ("kernel", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("build", C.c_int32)]
 
 
 class HsrStats(C.Structure):
@@ -57,7 +58,8 @@ class HsrStats(C.Structure):
                 ("t_build_ms", C.c_double), ("t_walk_ms", C.c_double),
                 ("t_force_ms", C.c_double), ("t_total_ms", C.c_double),
                 ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64),
-                ("evaluated_pairs", C.c_int64), ("work_items", C.c_int64)]
+                ("evaluated_pairs", C.c_int64), ("work_items", C.c_int64),
+                ("cm_fallbacks", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -123,7 +125,7 @@ def _check_host(a, dtype, n, name):
         raise TypeError(f"{name} must be a writable C-contiguous {np.dtype(dtype)} array of >= {n}")
 
 
-def make_params(kp, kernel: int = KERNEL_AUTO) -> HsrParams:
+def make_params(kp, kernel: int = KERNEL_AUTO, build: int = BUILD_DEVICE) -> HsrParams:
     P = HsrParams()
     for k in ("min", "max", "min_force", "max_force"):
         getattr(P, k)[:] = [float(v) for v in getattr(kp, k)]
@@ -131,6 +133,7 @@ def make_params(kp, kernel: int = KERNEL_AUTO) -> HsrParams:
     P.nd, P.ds, P.tmin = kp.nd, kp.ds, kp.tmin
     P.fcoeff, P.ppc, P.tdpts, P.law = kp.fcoeff, kp.ppc, kp.tdpts, kp.law
     P.kernel = kernel
+    P.build = build
     return P
 
 
@@ -168,11 +171,26 @@ class Context:
         self._check(self.lib.hsr_get_stats(self.h, C.byref(s)), "hsr_get_stats")
         return s.as_dict()
 
-    def rcb_kick(self, p, kp, kernel: int = KERNEL_AUTO) -> dict:
+    def rcb_kick(self, p, kp, kernel: int = KERNEL_AUTO, build: int = BUILD_DEVICE) -> dict:
         """hsr_rcb_kick on the host arrays of `p` (modified in place)."""
-        P = make_params(kp, kernel)
+        P = make_params(kp, kernel, build)
         st = self.lib.hsr_rcb_kick(self.h, C.byref(P), p.n, *_particle_args(p), MEM_HOST)
         self._check(st, "hsr_rcb_kick")
+        return self.stats()
+
+    def rcb_kick_device(self, t: dict, n: int, kp, kernel: int = KERNEL_AUTO) -> dict:
+        """hsr_rcb_kick on device arrays: `t` maps the ten field names to CUDA
+        tensors (float32 x..phi, int64 id, int16/uint16 mask) on this context's
+        device, modified in place.  The caller synchronizes its own streams
+        before the call; the call returns with the results in place."""
+        P = make_params(kp, kernel, BUILD_DEVICE)
+        ptr = [C.cast(C.c_void_p(t[k].data_ptr()), C.POINTER(C.c_float))
+               for k in ("x", "y", "z", "vx", "vy", "vz", "mass", "phi")]
+        st = self.lib.hsr_rcb_kick(self.h, C.byref(P), n, *ptr,
+                                   C.cast(C.c_void_p(t["id"].data_ptr()), C.POINTER(C.c_int64)),
+                                   C.cast(C.c_void_p(t["mask"].data_ptr()), C.POINTER(C.c_uint16)),
+                                   MEM_DEVICE)
+        self._check(st, "hsr_rcb_kick(device arrays)")
         return self.stats()
 
     def lists(self):

@@ -56,6 +56,10 @@ enum { HSR_MEM_HOST = 0, HSR_MEM_DEVICE = 1 };
  * polynomial, weight m_j only, pairs with r2 == 0 dropped. */
 enum { HSR_LAW_POLY6 = 0, HSR_LAW_POLY5_STEP16 = 1 };
 
+/* Where the tree and the interaction lists are built (same results, bit for
+ * bit).  DEVICE is the default. */
+enum { HSR_BUILD_DEVICE = 0, HSR_BUILD_HOST = 1 };
+
 /* Kernel variants for the pair evaluation (same results up to FP32
  * summation order). */
 enum {
@@ -81,7 +85,7 @@ typedef struct hsr_params {
   int32_t tdpts;                    /* 1 = monopole, 12 = quadrupole            */
   int32_t law;                      /* HSR_LAW_*                                */
   int32_t kernel;                   /* HSR_KERNEL_*                             */
-  int32_t reserved;
+  int32_t build;                    /* HSR_BUILD_*                              */
 } hsr_params;
 
 /* Statistics of the last call on a context. */
@@ -93,8 +97,8 @@ typedef struct hsr_stats {
   int64_t list_entries;      /* sum of list lengths (self included)             */
   int64_t pairs;             /* sum over processed leaves of count * list length */
   int64_t kernel_launches;   /* CUDA kernels this call launched                 */
-  double t_build_ms;         /* host: tree build                                */
-  double t_walk_ms;          /* host: interaction lists                         */
+  double t_build_ms;         /* tree build (host wall or device events)         */
+  double t_walk_ms;          /* interaction lists and work items                */
   double t_force_ms;         /* device: pair kernel, CUDA events                */
   double t_total_ms;         /* wall time of the whole call                     */
   int64_t h2d_bytes;         /* bytes copied host -> device by the call         */
@@ -104,6 +108,8 @@ typedef struct hsr_stats {
                                 the plain kernel; after the box test for the
                                 batched kernel (the others contribute exactly 0) */
   int64_t work_items;        /* batched-kernel work items (group x list chunk)  */
+  int64_t cm_fallbacks;      /* device build: nodes whose centre of mass needed
+                                the sequential sum (see rcb_device.cuh)         */
 } hsr_stats;
 
 typedef struct hsr_ctx hsr_ctx;
@@ -120,8 +126,9 @@ const char *hsr_version(void);
  * (permuting all ten arrays in place exactly as the reference does), builds
  * the interaction list of every leaf inside the force box and adds
  * fcoeff * sum_j m_i m_j g(r2_ij) (x_j - x_i) to v_i for r2_ij < fsrrmax^2.
- * mem: HSR_MEM_HOST (any host memory).  Synchronous: the arrays hold the
- * result when the call returns. */
+ * mem: HSR_MEM_HOST (any host memory) or HSR_MEM_DEVICE (device pointers on
+ * the context's device; HSR_BUILD_DEVICE only).  Synchronous: the arrays
+ * hold the result when the call returns. */
 hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, float *y,
                         float *z, float *vx, float *vy, float *vz, float *mass, float *phi,
                         int64_t *id, uint16_t *mask, int32_t mem);

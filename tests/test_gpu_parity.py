@@ -201,3 +201,70 @@ def _g64(r2, rsm=float(np.float32(0.1))):
     for c in a[::-1]:
         p = p * r2 + c
     return (r2 + rsm * rsm) ** -1.5 - p
+
+
+@pytest.mark.parametrize("case", ["zel32_nd64", "zel24_quad", "blob_oa05", "random_nd4"])
+def test_device_build_equals_host_build(ctx, case):
+    """The GPU tree/list build gives the host build's permutation and lists
+    bit for bit, and the same kick within the FP32 tolerance."""
+    if case == "zel32_nd64":
+        p = synth.zeldovich_box(32, seed=21)
+        kp = synth.kick_params(p, nd=64)
+    elif case == "zel24_quad":
+        p = synth.zeldovich_box(24, z=10.0, seed=22)
+        kp = synth.kick_params(p, nd=32, tdpts=12)
+    elif case == "blob_oa05":
+        p, kp, _ = load_golden("blob3000_nd8_oa05_mono")
+    else:
+        p = synth.random_box(5000, 10.0, 23)
+        kp = synth.kick_params(p, nd=4, fcoeff=1.0)
+        kp.min_force, kp.max_force = (0.5,) * 3, (9.5,) * 3
+    q = p.copy()
+    ctx.rcb_kick(p, kp, build=hsr.BUILD_HOST)
+    lh = ctx.lists()
+    st = ctx.rcb_kick(q, kp, build=hsr.BUILD_DEVICE)
+    ld = ctx.lists()
+    for k in EXACT:
+        assert np.array_equal(getattr(p, k).view(np.uint8), getattr(q, k).view(np.uint8)), k
+    assert same_lists(*lh, *ld)
+    rms, mx = force_errors(vel(q), vel(p))
+    assert rms <= RMS_TOL and mx <= MAX_TOL, (rms, mx)
+    assert st["pairs"] == ctx.stats()["pairs"]
+
+
+def test_cm_sequential_fallback_path(ctx, monkeypatch):
+    """Every node's centre of mass through the sequential fallback gives the
+    same tree as the certified parallel sum."""
+    p = synth.zeldovich_box(20, seed=31)
+    kp = synth.kick_params(p, nd=32)
+    q = p.copy()
+    ctx.rcb_kick(p, kp)
+    lp = ctx.lists()
+    monkeypatch.setenv("HSR_FORCE_CM_FALLBACK", "1")
+    st = ctx.rcb_kick(q, kp)
+    monkeypatch.delenv("HSR_FORCE_CM_FALLBACK")
+    assert st["cm_fallbacks"] == st["nodes"]
+    for k in EXACT:
+        assert np.array_equal(getattr(p, k).view(np.uint8), getattr(q, k).view(np.uint8)), k
+    assert same_lists(*lp, *ctx.lists())
+    assert np.array_equal(vel(p), vel(q))
+
+
+def test_device_memory_arrays(ctx):
+    """HSR_MEM_DEVICE: the same kick on arrays already in HBM."""
+    torch = pytest.importorskip("torch")
+    p = synth.zeldovich_box(24, seed=41)
+    kp = synth.kick_params(p, nd=64)
+    q = p.copy()
+    ctx.rcb_kick(p, kp)
+    t = {k: torch.from_numpy(getattr(q, k).view(np.int16) if k == "mask" else getattr(q, k)).cuda()
+         for k in synth.FIELDS}
+    torch.cuda.synchronize()
+    ctx.rcb_kick_device(t, q.n, kp)
+    for k in EXACT:
+        got = t[k].cpu().numpy()
+        if k == "mask":
+            got = got.view(np.uint16)
+        assert np.array_equal(got.view(np.uint8), getattr(p, k).view(np.uint8)), k
+    gv = np.stack([t["vx"].cpu().numpy(), t["vy"].cpu().numpy(), t["vz"].cpu().numpy()], 1)
+    assert np.array_equal(gv, np.stack([p.vx, p.vy, p.vz], 1))
