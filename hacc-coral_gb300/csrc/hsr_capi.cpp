@@ -626,7 +626,7 @@ hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float
   const int64_t *in_id;
   const uint16_t *in_mask;
   char *ob = ctx->d_out.as<char>();
-  CU(cudaEventRecord(ctx->ev2, s), "event");
+  const auto t_in = clk::now();
   if (mem == HSR_MEM_HOST) {
     CU(ctx->d_in.ensure(A.bytes), "cudaMalloc(in)");
     char *ib = ctx->d_in.as<char>();
@@ -646,6 +646,8 @@ hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float
   }
   int64_t launches = 0;
   float4 *pos4 = ctx->d_pos4.as<float4>();
+  CU(cudaStreamSynchronize(s), "host to device copies");
+  st.t_h2d_ms = ms_since(t_in);
   CU(hsr::launch_pack4(in[0], in[1], in[2], in[6], pos4, n, s), "pack kernel");
   ++launches;
   hsr::TreeConfig cfg{};
@@ -671,7 +673,9 @@ hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float
     if (ctx->tree.error()) return ctx->fail(HSR_ERR_UNSUPPORTED, ctx->tree.error());
     return ctx->cuda_fail(e, "device tree build");
   }
-  st.t_build_ms = ms_since(tb);  // build, lists and items (synchronizes per level)
+  st.t_build_ms = ctx->tree.build_ms();
+  st.t_walk_ms = ctx->tree.lists_ms();
+  (void)tb;
   const hsr::DeviceTreeInfo &ti = ctx->tree.info();
   launches += ti.levels * 16 + 24;
   const int32_t *perm = ctx->tree.perm();
@@ -720,11 +724,13 @@ hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float
   unsigned long long counters[2] = {0, 0};
   if (!plain) CU(cudaMemcpyAsync(counters, ctx->d_queue.p, sizeof(counters), cudaMemcpyDeviceToHost, s),
                  "D2H counters");
+  CU(cudaEventRecord(ctx->ev2, s), "event");
   CU(cudaStreamSynchronize(s), "kernel execution");
-  float fms = 0;
+  float fms = 0, oms = 0;
   CU(cudaEventElapsedTime(&fms, ctx->ev0, ctx->ev1), "event time");
+  CU(cudaEventElapsedTime(&oms, ctx->ev1, ctx->ev2), "event time");
   st.t_force_ms = fms;
-  st.t_walk_ms = 0;
+  st.t_d2h_ms = oms;
   st.n = n;
   st.nodes = ti.nodes;
   st.leaves = 0;

@@ -3,6 +3,8 @@
 #include "rcb_device.cuh"
 
 #include <algorithm>
+#include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <vector>
@@ -23,6 +25,20 @@ __device__ __forceinline__ float norm2_(float a, float b, float c) {
 
 __host__ __device__ __forceinline__ int64_t max64(int64_t a, int64_t b) { return a > b ? a : b; }
 __host__ __device__ __forceinline__ int64_t min64(int64_t a, int64_t b) { return a < b ? a : b; }
+
+// Exponent of the lowest set bit of a float (INT_MAX for zero, INT_MIN for
+// inf/NaN).  A sum of terms that are all multiples of 2^e is exact in double,
+// in any order, while the sum of magnitudes stays below 2^(53 + e).
+__device__ __forceinline__ int lsb_exp(float t) {
+  const uint32_t b = __float_as_uint(t) & 0x7fffffffu;
+  if (b == 0) return INT_MAX;
+  int e = int(b >> 23);
+  if (e == 255) return INT_MIN;
+  uint32_t m = b & 0x7fffffu;
+  if (e == 0) e = 1;
+  else m |= 0x800000u;
+  return e - 150 + (__ffs(int(m)) - 1);
+}
 
 constexpr int kChunk = 4096;        // elements per statistics / partition chunk
 constexpr int kChunkThreads = 256;  // threads per chunk (16 elements each)
@@ -178,11 +194,17 @@ __global__ void __launch_bounds__(kChunkThreads)
   const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
   double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  int emin[4] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX};
   bool any = false;
   for (int k = threadIdx.x; k < R.len; k += kChunkThreads) {
     const float4 p = pos[R.begin + k];
     const float w = p.w;
-    const double wx = double(fmul_(w, p.x)), wy = double(fmul_(w, p.y)), wz = double(fmul_(w, p.z));
+    const float fx = fmul_(w, p.x), fy = fmul_(w, p.y), fz = fmul_(w, p.z);
+    emin[0] = min(emin[0], lsb_exp(fx));
+    emin[1] = min(emin[1], lsb_exp(fy));
+    emin[2] = min(emin[2], lsb_exp(fz));
+    emin[3] = min(emin[3], lsb_exp(w));
+    const double wx = double(fx), wy = double(fy), wz = double(fz);
     s[0] += wx; s[1] += wy; s[2] += wz; s[3] += double(w);
     s[4] += fabs(wx); s[5] += fabs(wy); s[6] += fabs(wz); s[7] += fabs(double(w));
     if (!any) {
@@ -203,6 +225,10 @@ __global__ void __launch_bounds__(kChunkThreads)
     lo[d] = warp_min(lo[d]);
     hi[d] = warp_max(hi[d]);
   }
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+    for (int o = 16; o > 0; o >>= 1) emin[q] = min(emin[q], __shfl_xor_sync(0xffffffffu, emin[q], o));
+  __shared__ int she[kChunkThreads / 32][4];
   __shared__ double sh[kChunkThreads / 32][14];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0) {
@@ -211,20 +237,26 @@ __global__ void __launch_bounds__(kChunkThreads)
       sh[warp][8 + d] = lo[d];
       sh[warp][11 + d] = hi[d];
     }
+    for (int q = 0; q < 4; ++q) she[warp][q] = emin[q];
   }
   __syncthreads();
   if (threadIdx.x == 0) {
     double t[14];
+    int e[4];
     for (int q = 0; q < 14; ++q) t[q] = sh[0][q];
+    for (int q = 0; q < 4; ++q) e[q] = she[0][q];
     for (int w = 1; w < kChunkThreads / 32; ++w) {
       for (int q = 0; q < 8; ++q) t[q] += sh[w][q];
       for (int d = 0; d < 3; ++d) {
         t[8 + d] = fmin(t[8 + d], sh[w][8 + d]);
         t[11 + d] = fmax(t[11 + d], sh[w][11 + d]);
       }
+      for (int q = 0; q < 4; ++q) e[q] = min(e[q], she[w][q]);
     }
     double *o = part + chunk * kPartDoubles;
     for (int q = 0; q < 14; ++q) o[q] = t[q];
+    int *oe = reinterpret_cast<int *>(o + 14);
+    for (int q = 0; q < 4; ++q) oe[q] = e[q];
   }
 }
 
@@ -262,6 +294,7 @@ __global__ void k_stats_final(DNode *nodes, int32_t nb, int32_t ne, const int64_
   const int64_t nc = (int64_t(N.count) + kChunk - 1) / kChunk;
   double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  int emin[4] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX};
   for (int64_t c = lane; c < nc; c += 32) {
     const double *p = part + (cb + c) * kPartDoubles;
     for (int q = 0; q < 8; ++q) s[q] += p[q];
@@ -269,12 +302,16 @@ __global__ void k_stats_final(DNode *nodes, int32_t nb, int32_t ne, const int64_
       lo[d] = fminf(lo[d], float(p[8 + d]));
       hi[d] = fmaxf(hi[d], float(p[11 + d]));
     }
+    const int *pe = reinterpret_cast<const int *>(p + 14);
+    for (int q = 0; q < 4; ++q) emin[q] = min(emin[q], pe[q]);
   }
   for (int q = 0; q < 8; ++q) s[q] = warp_sum(s[q]);
   for (int d = 0; d < 3; ++d) {
     lo[d] = warp_min(lo[d]);
     hi[d] = warp_max(hi[d]);
   }
+  for (int q = 0; q < 4; ++q)
+    for (int o = 16; o > 0; o >>= 1) emin[q] = min(emin[q], __shfl_xor_sync(0xffffffffu, emin[q], o));
   if (lane != 0) return;
   for (int d = 0; d < 3; ++d) {
     N.xmin[d] = lo[d];
@@ -285,10 +322,20 @@ __global__ void k_stats_final(DNode *nodes, int32_t nb, int32_t ne, const int64_
   // 2 covers the higher-order terms.
   const double g = 2.0 * (double(N.count) + 64.0) * 0x1p-53;
   const double bm = g * s[7];
+  // Exact sums: every term a multiple of 2^emin and the magnitudes summing
+  // below 2^(53 + emin) -- then the reference's sequential sum and this one are
+  // the same exact value, and so is the quotient it rounds.
+  auto exact = [&](int q, double sabs) {
+    if (emin[q] == INT_MAX) return true;  // all terms zero
+    if (emin[q] == INT_MIN || emin[q] < -1000) return false;
+    return sabs < ldexp(1.0, 53 + emin[q]);
+  };
+  const bool mexact = exact(3, s[7]);
   bool ok = !force_fallback;
   for (int d = 0; d < 3 && ok; ++d) {
     float v;
-    if (certify(s[d], g * s[4 + d], s[3], bm, &v)) N.xc[d] = v;
+    if (mexact && exact(d, s[4 + d]) && s[3] != 0.0) N.xc[d] = __double2float_rn(__ddiv_rn(s[d], s[3]));
+    else if (certify(s[d], g * s[4 + d], s[3], bm, &v)) N.xc[d] = v;
     else ok = false;
   }
   if (!ok) {
@@ -1024,6 +1071,7 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   info_ = DeviceTreeInfo{};
   err_ = nullptr;
   padded_pairs_ = 0;
+  const auto t0 = std::chrono::steady_clock::now();
   const int k = cfg.tdpts;
   {
     float d[12][3];
@@ -1116,6 +1164,8 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   }
   const int32_t nnodes = ne;
   info_.nodes = nnodes;
+  const auto t1 = std::chrono::steady_clock::now();
+  build_ms_ = std::chrono::duration<double, std::milli>(t1 - t0).count();
   info_.levels = int64_t(level_begin.size()) - 1;
 
   // ---- pseudo-particles, deepest level first ----
@@ -1209,6 +1259,8 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     k_item_fill<<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(leafdesc_, nleaves, jsplit, counters_,
                                                                items_);
   DT_CHECK(cudaGetLastError());
+  DT_CHECK(cudaStreamSynchronize(s));
+  lists_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
   return cudaSuccess;
 }
 

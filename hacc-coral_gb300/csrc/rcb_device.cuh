@@ -79,6 +79,9 @@ class DeviceTree {
   const DNode *nodes() const { return nodes_; }
   const int32_t *leaf_nodes() const { return leaf_ids_; }
   int64_t padded_pairs() const { return padded_pairs_; }
+  // Device time of the last build's tree levels and of its lists + items.
+  double build_ms() const { return build_ms_; }
+  double lists_ms() const { return lists_ms_; }
   // Whether a device-side bound was hit (walk stack); the build then failed.
   const char *error() const { return err_; }
 
@@ -88,6 +91,7 @@ class DeviceTree {
 
   DeviceTreeInfo info_{};
   int64_t padded_pairs_ = 0;
+  double build_ms_ = 0, lists_ms_ = 0;
   const char *err_ = nullptr;
   // elements: current and scratch (x, y, z, m) + input index
   float4 *epos_ = nullptr, *tpos_ = nullptr;

@@ -59,7 +59,8 @@ class HsrStats(C.Structure):
                 ("t_force_ms", C.c_double), ("t_total_ms", C.c_double),
                 ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64),
                 ("evaluated_pairs", C.c_int64), ("work_items", C.c_int64),
-                ("cm_fallbacks", C.c_int64)]
+                ("cm_fallbacks", C.c_int64), ("t_h2d_ms", C.c_double),
+                ("t_d2h_ms", C.c_double)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -97,8 +97,8 @@ typedef struct hsr_stats {
   int64_t list_entries;      /* sum of list lengths (self included)             */
   int64_t pairs;             /* sum over processed leaves of count * list length */
   int64_t kernel_launches;   /* CUDA kernels this call launched                 */
-  double t_build_ms;         /* tree build (host wall or device events)         */
-  double t_walk_ms;          /* interaction lists and work items                */
+  double t_build_ms;         /* tree build (host: wall; device: events)         */
+  double t_walk_ms;          /* interaction lists and work items (same)         */
   double t_force_ms;         /* device: pair kernel, CUDA events                */
   double t_total_ms;         /* wall time of the whole call                     */
   int64_t h2d_bytes;         /* bytes copied host -> device by the call         */
@@ -110,6 +110,8 @@ typedef struct hsr_stats {
   int64_t work_items;        /* batched-kernel work items (group x list chunk)  */
   int64_t cm_fallbacks;      /* device build: nodes whose centre of mass needed
                                 the sequential sum (see rcb_device.cuh)         */
+  double t_h2d_ms;           /* device build: host -> device copies             */
+  double t_d2h_ms;           /* device build: results back to the caller        */
 } hsr_stats;
 
 typedef struct hsr_ctx hsr_ctx;
