@@ -32,7 +32,7 @@ BUILD_DEVICE, BUILD_HOST = 0, 1
 EXPORTS = ("hsr_create", "hsr_destroy", "hsr_last_error", "hsr_version", "hsr_rcb_kick",
            "hsr_get_stats", "hsr_lists_size", "hsr_lists_export", "hsr_build_lists",
            "hsr_lists_info", "hsr_lists_get", "hsr_lists_index", "hsr_lists_free",
-           "hsr_force_law", "hsr_bench_pairs", "hsr_probe_fp32_peak")
+           "hsr_force_law", "hsr_bench_pairs", "hsr_probe_fp32_peak", "hsr_kick_lists_noalloc")
 
 
 class HsrError(RuntimeError):
@@ -108,6 +108,9 @@ def load(path: str = LIB_PATH):
     lib.hsr_lists_free.argtypes = [vp]
     lib.hsr_force_law.restype = i32
     lib.hsr_force_law.argtypes = [vp, i32, f32, f32, i64, pf, pf]
+    lib.hsr_kick_lists_noalloc.restype = i32
+    lib.hsr_kick_lists_noalloc.argtypes = [vp, i64, i64, vp, vp, vp, vp, i64, vp, vp, vp, vp,
+                                           f32, f32, f32, i32, vp]
     lib.hsr_bench_pairs.restype = i32
     lib.hsr_bench_pairs.argtypes = [vp, i32, i32, i32, C.POINTER(C.c_double)]
     lib.hsr_probe_fp32_peak.restype = i32
@@ -276,6 +279,20 @@ class HostLists:
         if st != HSR_OK:
             raise HsrError(st, "hsr_lists_index")
         return idx
+
+
+def kick_lists_noalloc(table, n, leaf_offset, leaf_count, list_begin, list_len, list_index,
+                       vx, vy, vz, fcoeff, rsm=0.1, fsrrmax=3.116326355, law=LAW_POLY6):
+    """hsr_kick_lists_noalloc on CUDA tensors (the caller owns every buffer;
+    the library allocates nothing).  Raises HsrError on a non-zero status."""
+    lib = load()
+    ptr = lambda t: C.c_void_p(t.data_ptr())
+    st = lib.hsr_kick_lists_noalloc(ptr(table), table.shape[0], n, ptr(leaf_offset),
+                                    ptr(leaf_count), ptr(list_begin), ptr(list_len),
+                                    leaf_offset.shape[0], ptr(list_index), ptr(vx), ptr(vy),
+                                    ptr(vz), fcoeff, rsm, fsrrmax, law, None)
+    if st != HSR_OK:
+        raise HsrError(st, "hsr_kick_lists_noalloc")
 
 
 # ---------------------------------------------------------------------------

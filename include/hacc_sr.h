@@ -172,6 +172,34 @@ hsr_status hsr_lists_free(hsr_lists *L);
 hsr_status hsr_force_law(hsr_ctx *ctx, int32_t law, float rsm, float fsrrmax, int64_t n,
                          const float *r2, float *g);
 
+/* The short-range kick over interaction lists the caller already holds on the
+ * device, with no memory allocation of any kind.  No counterpart in the
+ * reference.
+ *
+ * For callers that cannot allocate device memory once running (a simulation
+ * that sizes all buffers at start-up and forbids allocation in its time loop,
+ * code whose memory pool or arena owns the device, an embedding that must not
+ * grow its footprint).  Everything is the caller's: the position table
+ * (ntab entries of 4 floats x, y, z, m, 16-byte aligned; entries >= n are
+ * pseudo-particles), the leaves (particle offset and count, list begin and
+ * length, as hsr_lists_export / hsr_build_lists describe them), the list
+ * entries as table indices, and vx, vy, vz (n floats, kicked in place, in
+ * table order) -- all device pointers on the current device.  The kernel's
+ * scratch (work items and counters) lives in a fixed 4 MiB device array that
+ * every device loading the library holds until the process exits; lists that
+ * need more than 131064 work items (one per group of up to 32 leaf particles
+ * per 8192 list entries) are rejected with HSR_ERR_ARG before any pair is
+ * evaluated.  The first call on a device looks up that array's device address
+ * (set-up); make that first call before any stream capture.  Calls share the
+ * array: calls that overlap on the GPU race and must not be issued
+ * concurrently.  The call waits for its stream (NULL: the default stream). */
+hsr_status hsr_kick_lists_noalloc(const float *table, int64_t ntab, int64_t n,
+                                  const int32_t *leaf_offset, const int32_t *leaf_count,
+                                  const int64_t *list_begin, const int32_t *list_len,
+                                  int64_t nleaves, const int32_t *list_index, float *vx, float *vy,
+                                  float *vz, float fcoeff, float rsm, float fsrrmax, int32_t law,
+                                  void *stream);
+
 /* ---- diagnostics ------------------------------------------------------- */
 
 /* Relaunches the pair kernel of the last hsr_rcb_kick `iters` times on the
