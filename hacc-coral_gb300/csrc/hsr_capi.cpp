@@ -121,7 +121,8 @@ struct hsr_ctx {
   // device-build path: staged inputs and outputs of the ten arrays
   DevBuf d_in, d_out, d_pos4;
   // misc
-  DevBuf d_law, d_flush, d_probe, d_queue;
+  DevBuf d_law, d_flush, d_probe, d_queue, d_adj;
+  bool tape = false;  // the last call was hsr_force_fwd
   hsr_stats stats{};
   std::string err = "no error";
   bool have_lists = false;
@@ -203,7 +204,7 @@ hsr_status hsr_destroy(hsr_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf *b : {&ctx->d_pos, &ctx->d_vel, &ctx->d_leaves, &ctx->d_segs, &ctx->d_idx, &ctx->d_law,
                     &ctx->d_flush, &ctx->d_probe, &ctx->d_items, &ctx->d_gidx, &ctx->d_queue,
-                    &ctx->d_in, &ctx->d_out, &ctx->d_pos4})
+                    &ctx->d_in, &ctx->d_out, &ctx->d_pos4, &ctx->d_adj})
     b->release();
   for (PinBuf *b : {&ctx->h_pos, &ctx->h_vel, &ctx->h_leaves, &ctx->h_segs, &ctx->h_items, &ctx->h_gidx})
     b->release();
@@ -763,6 +764,7 @@ hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, 
     return ctx->fail(HSR_ERR_UNSUPPORTED, "the host build takes host arrays");
   CU(cudaSetDevice(ctx->device), "cudaSetDevice");
   ctx->have_lists = false;
+  ctx->tape = false;
   hsr_stats st{};
   hsr_status r = p->build == HSR_BUILD_HOST
                      ? kick_host_build(ctx, p, n, x, y, z, vx, vy, vz, mass, phi, id, mask, st)
@@ -831,6 +833,249 @@ hsr_status hsr_lists_export(const hsr_ctx *ctx_c, int64_t *leaf_offset, int64_t 
     }
   }
   list_ptr[nl] = ti.list_entries;
+  return HSR_OK;
+}
+
+hsr_status hsr_force_fwd(hsr_ctx *ctx, const hsr_params *p, int64_t n, const float *x,
+                         const float *y, const float *z, const float *mass, float *dvx,
+                         float *dvy, float *dvz, int32_t mem) {
+  if (!ctx) return HSR_ERR_ARG;
+  const auto t_start = clk::now();
+  const void *arrs[10] = {x, y, z, dvx, dvy, dvz, mass, x, x, x};
+  if (hsr_status e = check_params(p, n, arrs, ctx->err)) return e;
+  if (mem != HSR_MEM_HOST && mem != HSR_MEM_DEVICE) return ctx->fail(HSR_ERR_ARG, "bad memory kind");
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  ctx->have_lists = false;
+  ctx->tape = false;
+  cudaStream_t s = ctx->stream;
+  const size_t nb = size_t(std::max<int64_t>(n, 1)) * 4;
+  CU(ctx->d_pos4.ensure(size_t(std::max<int64_t>(n, 1)) * 16), "cudaMalloc(pos4)");
+  const float *in[4] = {x, y, z, mass};
+  if (mem == HSR_MEM_HOST) {
+    CU(ctx->d_in.ensure(4 * nb + 1024), "cudaMalloc(in)");
+    for (int i = 0; i < 4; ++i) {
+      float *d = reinterpret_cast<float *>(ctx->d_in.as<char>() + i * ((nb + 255) & ~size_t(255)));
+      CU(cudaMemcpyAsync(d, in[i], size_t(n) * 4, cudaMemcpyHostToDevice, s), "H2D positions");
+      in[i] = d;
+    }
+  }
+  float4 *pos4 = ctx->d_pos4.as<float4>();
+  CU(hsr::launch_pack4(in[0], in[1], in[2], in[3], pos4, n, s), "pack kernel");
+  hsr::TreeConfig cfg{};
+  for (int i = 0; i < 3; ++i) {
+    cfg.min[i] = p->min[i];
+    cfg.max[i] = p->max[i];
+    cfg.min_force[i] = p->min_force[i];
+    cfg.max_force[i] = p->max_force[i];
+  }
+  cfg.fsrrmax = p->fsrrmax;
+  cfg.tan_oa = std::tan(p->open_angle);
+  cfg.ppc = p->ppc;
+  cfg.nd = int32_t(std::min<int64_t>(p->nd, INT32_MAX));
+  cfg.tdpts = p->tdpts;
+  cudaError_t e = ctx->tree.build(cfg, n, pos4, kJSplit, s);
+  if (e != cudaSuccess) {
+    if (ctx->tree.error()) return ctx->fail(HSR_ERR_UNSUPPORTED, ctx->tree.error());
+    return ctx->cuda_fail(e, "device tree build");
+  }
+  const hsr::DeviceTreeInfo &ti = ctx->tree.info();
+  Work &w = ctx->work;
+  set_work_params(w, p, n);
+  CU(ctx->d_vel.ensure(size_t(std::max<int64_t>(3 * n, 1)) * 4 + 256), "cudaMalloc(vel)");
+  float *dv = ctx->d_vel.as<float>();
+  CU(cudaMemsetAsync(dv, 0, size_t(3 * n) * 4, s), "zero dv");
+  w.table = ctx->tree.table();
+  w.leaves = ctx->tree.leaves();
+  w.idx = ctx->tree.index();
+  w.items = ctx->tree.items();
+  w.gidx = ctx->tree.gidx();
+  w.vel = dv;
+  w.nleaves = ti.processed_leaves;
+  w.nitems = ti.items;
+  w.device_built = true;
+  CU(cudaEventRecord(ctx->ev0, s), "event");
+  CU(ctx->launch_pairs(w.kernel), "pair kernel");
+  CU(cudaEventRecord(ctx->ev1, s), "event");
+  // back to the caller's order
+  CU(ctx->d_out.ensure(3 * nb + 1024), "cudaMalloc(out)");
+  float *ob = ctx->d_out.as<float>();
+  const size_t stride = ((nb + 255) & ~size_t(255)) / 4;
+  float *outs[3] = {dvx, dvy, dvz};
+  for (int d = 0; d < 3; ++d) {
+    float *o = mem == HSR_MEM_HOST ? ob + d * stride : outs[d];
+    CU(hsr::launch_scatter_f32(dv + d * n, ctx->tree.perm(), o, n, s), "scatter dv");
+    if (mem == HSR_MEM_HOST)
+      CU(cudaMemcpyAsync(outs[d], o, size_t(n) * 4, cudaMemcpyDeviceToHost, s), "D2H dv");
+  }
+  CU(cudaStreamSynchronize(s), "forward");
+  float fms = 0;
+  CU(cudaEventElapsedTime(&fms, ctx->ev0, ctx->ev1), "event time");
+  hsr_stats st{};
+  st.n = n;
+  st.nodes = ti.nodes;
+  st.processed_leaves = ti.processed_leaves;
+  st.list_entries = ti.list_entries;
+  st.pairs = ti.pairs;
+  st.work_items = ti.items;
+  st.cm_fallbacks = ti.cm_fallbacks;
+  st.t_build_ms = ctx->tree.build_ms();
+  st.t_walk_ms = ctx->tree.lists_ms();
+  st.t_force_ms = fms;
+  st.t_total_ms = ms_since(t_start);
+  ctx->stats = st;
+  ctx->have_lists = true;
+  ctx->last_tdpts = p->tdpts;
+  ctx->tape = true;
+  return HSR_OK;
+}
+
+hsr_status hsr_force_vjp(hsr_ctx *ctx, const float *dvbx, const float *dvby, const float *dvbz,
+                         float *xbx, float *xby, float *xbz, int32_t mem) {
+  if (!ctx) return HSR_ERR_ARG;
+  if (!ctx->tape) return ctx->fail(HSR_ERR_STATE, "hsr_force_vjp needs a preceding hsr_force_fwd");
+  if (ctx->last_tdpts != 1)
+    return ctx->fail(HSR_ERR_UNSUPPORTED, "the adjoint takes monopole pseudo-particles (tdpts = 1)");
+  if (mem != HSR_MEM_HOST && mem != HSR_MEM_DEVICE) return ctx->fail(HSR_ERR_ARG, "bad memory kind");
+  const Work &w = ctx->work;
+  const int64_t n = w.n;
+  if (n > 0 && (!dvbx || !dvby || !dvbz || !xbx || !xby || !xbz))
+    return ctx->fail(HSR_ERR_ARG, "null array");
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  cudaStream_t s = ctx->stream;
+  const hsr::DeviceTreeInfo &ti = ctx->tree.info();
+  const int64_t ntab = n + ti.nodes;
+  const size_t sn = size_t((std::max<int64_t>(n, 1) + 63) & ~int64_t(63));
+  const size_t st_ = size_t((std::max<int64_t>(ntab, 1) + 63) & ~int64_t(63));
+  const size_t sa = size_t(std::max<int64_t>(ti.nodes, 1)) * 3;
+  // cotangent (caller order) | cotangent (tree order) | xbar table (3 x ntab) | node acc
+  CU(ctx->d_adj.ensure((6 * sn + 3 * st_ + sa + 64) * 4), "cudaMalloc(adjoint)");
+  float *ub = ctx->d_adj.as<float>();
+  float *ut = ub + 3 * sn;
+  float *xb = ut + 3 * sn;
+  float *acc = xb + 3 * st_;
+  const float *uin[3] = {dvbx, dvby, dvbz};
+  const int32_t *perm = ctx->tree.perm();
+  for (int d = 0; d < 3; ++d) {
+    const float *src = uin[d];
+    if (mem == HSR_MEM_HOST) {
+      CU(cudaMemcpyAsync(ub + d * sn, uin[d], size_t(n) * 4, cudaMemcpyHostToDevice, s), "H2D cotangent");
+      src = ub + d * sn;
+    }
+    CU(hsr::launch_gather_f32(src, perm, ut + d * sn, n, s), "gather cotangent");
+  }
+  CU(cudaMemsetAsync(xb, 0, 3 * st_ * 4, s), "zero xbar");
+  CU(ctx->d_queue.ensure(64), "cudaMalloc(queue)");
+  CU(cudaMemsetAsync(ctx->d_queue.p, 0, 2 * sizeof(unsigned long long), s), "reset queue");
+  if (ctx->batched_ctas == 0) ctx->batched_ctas = hsr::batched_resident_ctas(ctx->device);
+  CU(cudaEventRecord(ctx->ev0, s), "event");
+  CU(hsr::launch_pairs_vjp(w.law, w.table, w.items, w.nitems, w.gidx, w.idx, ut, ut + sn, ut + 2 * sn,
+                           xb, xb + st_, xb + 2 * st_, w.fcoeff, w.rsm2, w.rc2, w.rcull2,
+                           ctx->d_queue.as<unsigned long long>(), ctx->batched_ctas, s),
+     "adjoint kernel");
+  CU(hsr::launch_pseudo_adjoint(ctx->tree.nodes(), ctx->tree.levels(), w.table, n, xb, xb + st_,
+                                xb + 2 * st_, acc, s),
+     "pseudo-particle adjoint");
+  CU(cudaEventRecord(ctx->ev1, s), "event");
+  float *outs[3] = {xbx, xby, xbz};
+  for (int d = 0; d < 3; ++d) {
+    float *o = mem == HSR_MEM_HOST ? ub + d * sn : outs[d];
+    CU(hsr::launch_scatter_f32(xb + d * st_, perm, o, n, s), "scatter xbar");
+    if (mem == HSR_MEM_HOST)
+      CU(cudaMemcpyAsync(outs[d], o, size_t(n) * 4, cudaMemcpyDeviceToHost, s), "D2H xbar");
+  }
+  CU(cudaStreamSynchronize(s), "adjoint");
+  float ms = 0;
+  CU(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "event time");
+  ctx->stats.t_force_ms = ms;
+  return HSR_OK;
+}
+
+hsr_status hsr_last_perm(const hsr_ctx *ctx_c, int64_t *perm) {
+  hsr_ctx *ctx = const_cast<hsr_ctx *>(ctx_c);
+  if (!ctx || !perm) return HSR_ERR_ARG;
+  if (!ctx->have_lists) return HSR_ERR_STATE;
+  const int64_t n = ctx->work.n;
+  if (!ctx->work.device_built) {
+    const auto &el = ctx->host->elems();
+    for (int64_t i = 0; i < n; ++i) perm[i] = el[i].idx;
+    return HSR_OK;
+  }
+  std::vector<int32_t> p32(static_cast<size_t>(std::max<int64_t>(n, 1)));
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  CU(cudaMemcpy(p32.data(), ctx->tree.perm(), size_t(n) * 4, cudaMemcpyDeviceToHost), "D2H perm");
+  for (int64_t i = 0; i < n; ++i) perm[i] = p32[i];
+  return HSR_OK;
+}
+
+hsr_status hsr_tree_size(const hsr_ctx *ctx, int64_t *nnodes) {
+  if (!ctx || !nnodes) return HSR_ERR_ARG;
+  if (!ctx->have_lists) return HSR_ERR_STATE;
+  *nnodes = ctx->work.device_built ? ctx->tree.info().nodes : ctx->host->num_nodes();
+  return HSR_OK;
+}
+
+hsr_status hsr_tree_export(const hsr_ctx *ctx_c, int64_t *count, int64_t *offset, int64_t *cl,
+                           int64_t *cr, float *tdr, float *bbox9, float *ppm) {
+  hsr_ctx *ctx = const_cast<hsr_ctx *>(ctx_c);
+  if (!ctx || !count || !offset || !cl || !cr || !tdr || !bbox9 || !ppm) return HSR_ERR_ARG;
+  if (!ctx->have_lists) return HSR_ERR_STATE;
+  const int k = ctx->last_tdpts;
+  if (!ctx->work.device_built) {
+    const auto &H = *ctx->host;
+    for (int64_t t = 0; t < H.num_nodes(); ++t) {
+      const hsr::Node &N = H.node(t);
+      count[t] = N.count;
+      offset[t] = N.offset;
+      cl[t] = N.cl;
+      cr[t] = N.cr;
+      tdr[t] = N.tdr;
+      for (int i = 0; i < 3; ++i) {
+        bbox9[9 * t + i] = N.xmin[i];
+        bbox9[9 * t + 3 + i] = N.xmax[i];
+        bbox9[9 * t + 6 + i] = N.xc[i];
+      }
+      for (int i = 0; i < k; ++i) ppm[k * t + i] = N.ppm[i];
+    }
+    return HSR_OK;
+  }
+  const int64_t nn = ctx->tree.info().nodes;
+  std::vector<hsr::DNode> nodes(static_cast<size_t>(std::max<int64_t>(nn, 1)));
+  std::vector<float> pm(static_cast<size_t>(std::max<int64_t>(nn * k, 1)));
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  CU(cudaMemcpy(nodes.data(), ctx->tree.nodes(), size_t(nn) * sizeof(hsr::DNode), cudaMemcpyDeviceToHost),
+     "D2H nodes");
+  CU(cudaMemcpy(pm.data(), ctx->tree.ppm(), size_t(nn * k) * 4, cudaMemcpyDeviceToHost), "D2H ppm");
+  for (int64_t t = 0; t < nn; ++t) {
+    const hsr::DNode &N = nodes[t];
+    count[t] = N.count;
+    offset[t] = N.offset;
+    cl[t] = N.cl;
+    cr[t] = N.cr;
+    tdr[t] = N.tdr;
+    for (int i = 0; i < 3; ++i) {
+      bbox9[9 * t + i] = N.xmin[i];
+      bbox9[9 * t + 3 + i] = N.xmax[i];
+      bbox9[9 * t + 6 + i] = N.xc[i];
+    }
+    for (int i = 0; i < k; ++i) ppm[k * t + i] = pm[k * t + i];
+  }
+  return HSR_OK;
+}
+
+hsr_status hsr_lists_export_index(const hsr_ctx *ctx_c, int64_t *entry_index) {
+  hsr_ctx *ctx = const_cast<hsr_ctx *>(ctx_c);
+  if (!ctx || !entry_index) return HSR_ERR_ARG;
+  if (!ctx->have_lists) return HSR_ERR_STATE;
+  if (!ctx->work.device_built) {
+    export_lists(*ctx->host, ctx->h_pos.as<float>(), nullptr, nullptr, nullptr, nullptr, nullptr,
+                 nullptr, nullptr, entry_index);
+    return HSR_OK;
+  }
+  const int64_t ne = ctx->tree.info().list_entries;
+  std::vector<int32_t> ix(static_cast<size_t>(std::max<int64_t>(ne, 1)));
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  CU(cudaMemcpy(ix.data(), ctx->tree.index(), size_t(ne) * 4, cudaMemcpyDeviceToHost), "D2H index");
+  for (int64_t i = 0; i < ne; ++i) entry_index[i] = ix[i];
   return HSR_OK;
 }
 

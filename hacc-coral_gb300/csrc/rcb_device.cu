@@ -993,6 +993,57 @@ __global__ void k_unpack4(const float4 *in, float *x, float *y, float *z, float 
   }
 }
 
+__global__ void k_scatter_f32(const float *__restrict__ in, const int32_t *__restrict__ perm,
+                              float *out, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    out[perm[i]] = in[i];
+}
+
+// acc holds, per node, sum over it and its ancestors of xbar_P / M_P.
+__global__ void k_adj_root(const float4 *table, int64_t n, const float *xbx, const float *xby,
+                           const float *xbz, float *acc) {
+  const float m = table[n].w;
+  const float s = m != 0.f ? 1.f / m : 0.f;
+  acc[0] = xbx[n] * s;
+  acc[1] = xby[n] * s;
+  acc[2] = xbz[n] * s;
+}
+
+__global__ void k_adj_down(const DNode *nodes, int32_t lb, int32_t le, const float4 *table,
+                           int64_t n, const float *xbx, const float *xby, const float *xbz,
+                           float *acc) {
+  const int32_t t = lb + blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= le) return;
+  const DNode &T = nodes[t];
+  for (int s = 0; s < 2; ++s) {
+    const int32_t c = s == 0 ? T.cl : T.cr;
+    if (c <= 0) continue;
+    const float m = table[n + c].w;
+    const float inv = m != 0.f ? 1.f / m : 0.f;
+    acc[3 * int64_t(c) + 0] = acc[3 * int64_t(t) + 0] + xbx[n + c] * inv;
+    acc[3 * int64_t(c) + 1] = acc[3 * int64_t(t) + 1] + xby[n + c] * inv;
+    acc[3 * int64_t(c) + 2] = acc[3 * int64_t(t) + 2] + xbz[n + c] * inv;
+  }
+}
+
+__global__ void k_adj_leaves(const DNode *nodes, int32_t nnodes, const float4 *table, float *xbx,
+                             float *xby, float *xbz, const float *acc) {
+  const int32_t t = blockIdx.x;
+  if (t >= nnodes) return;
+  const DNode &T = nodes[t];
+  if (T.cl != 0 || T.cr != 0) return;
+  const float a0 = acc[3 * int64_t(t)], a1 = acc[3 * int64_t(t) + 1], a2 = acc[3 * int64_t(t) + 2];
+  if (a0 == 0.f && a1 == 0.f && a2 == 0.f) return;
+  for (int32_t i = threadIdx.x; i < T.count; i += blockDim.x) {
+    const int32_t k = T.offset + i;
+    const float m = table[k].w;
+    xbx[k] += m * a0;
+    xby[k] += m * a1;
+    xbz[k] += m * a2;
+  }
+}
+
 __global__ void k_iota(int32_t *p, int64_t n) {
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * blockDim.x)
@@ -1162,6 +1213,7 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     ne = int32_t(ne + 2 * nsplit);
     level_begin.push_back(nb);
   }
+  levels_ = level_begin;
   const int32_t nnodes = ne;
   info_.nodes = nnodes;
   const auto t1 = std::chrono::steady_clock::now();
@@ -1282,6 +1334,30 @@ cudaError_t launch_gather_u16(const uint16_t *in, const int32_t *perm, uint16_t 
   k_gather<uint16_t><<<grid_for(n, 256), 256, 0, s>>>(in, perm, out, n);
   return cudaGetLastError();
 }
+cudaError_t launch_scatter_f32(const float *in, const int32_t *perm, float *out, int64_t n,
+                               cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_scatter_f32<<<grid_for(n, 256), 256, 0, s>>>(in, perm, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pseudo_adjoint(const DNode *nodes, const std::vector<int32_t> &levels,
+                                  const float4 *table, int64_t n, float *xbx, float *xby,
+                                  float *xbz, float *acc, cudaStream_t s) {
+  if (levels.size() < 2) return cudaSuccess;
+  const int32_t nnodes = levels.back();
+  if (nnodes <= 0) return cudaSuccess;
+  k_adj_root<<<1, 1, 0, s>>>(table, n, xbx, xby, xbz, acc);
+  for (size_t l = 0; l + 1 < levels.size(); ++l) {
+    const int32_t lb = levels[l], le = levels[l + 1];
+    if (le > lb)
+      k_adj_down<<<unsigned((le - lb + 127) / 128), 128, 0, s>>>(nodes, lb, le, table, n, xbx, xby,
+                                                                 xbz, acc);
+  }
+  k_adj_leaves<<<unsigned(nnodes), 128, 0, s>>>(nodes, nnodes, table, xbx, xby, xbz, acc);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_pack4(const float *x, const float *y, const float *z, const float *m,
                          float4 *out, int64_t n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;

@@ -23,6 +23,8 @@
 #pragma once
 
 #include <cstdint>
+#include <vector>
+
 #include <cuda_runtime.h>
 
 #include "sr_kernels.cuh"
@@ -77,6 +79,9 @@ class DeviceTree {
   const PairItem *items() const { return items_; }
   const int32_t *gidx() const { return gidx_; }
   const DNode *nodes() const { return nodes_; }
+  const float *ppm() const { return ppm_; }
+  // First node of each tree level (BFS order), plus the node count at the end.
+  const std::vector<int32_t> &levels() const { return levels_; }
   const int32_t *leaf_nodes() const { return leaf_ids_; }
   int64_t padded_pairs() const { return padded_pairs_; }
   // Device time of the last build's tree levels and of its lists + items.
@@ -92,6 +97,7 @@ class DeviceTree {
   DeviceTreeInfo info_{};
   int64_t padded_pairs_ = 0;
   double build_ms_ = 0, lists_ms_ = 0;
+  std::vector<int32_t> levels_;
   const char *err_ = nullptr;
   // elements: current and scratch (x, y, z, m) + input index
   float4 *epos_ = nullptr, *tpos_ = nullptr;
@@ -150,6 +156,15 @@ cudaError_t launch_pack4(const float *x, const float *y, const float *z, const f
                          float4 *out, int64_t n, cudaStream_t s);
 cudaError_t launch_unpack4(const float4 *in, float *x, float *y, float *z, float *m, int64_t n,
                            cudaStream_t s);
+// out[perm[i]] = in[i] (back to the caller's order).
+cudaError_t launch_scatter_f32(const float *in, const int32_t *perm, float *out, int64_t n,
+                               cudaStream_t s);
+// Monopole pseudo-particle gradients passed to the particles through the
+// nodes' centres of mass: xbar_k += m_k sum_{nodes P containing k} xbar_P / M_P,
+// where xbar_P sits at slot n + P of the 3 arrays and M_P is the pseudo mass.
+cudaError_t launch_pseudo_adjoint(const DNode *nodes, const std::vector<int32_t> &levels,
+                                  const float4 *table, int64_t n, float *xbx, float *xby,
+                                  float *xbz, float *acc, cudaStream_t s);
 
 // Exclusive prefix sum of n int64 values (in may equal out); *total (device,
 // may be null) receives the sum.  tmp needs scan_tmp_size(n) elements.

@@ -201,6 +201,131 @@ cudaError_t launch_pairs_batched(int law, const float4 *pos, const PairItem *ite
 }
 
 // ---------------------------------------------------------------------------
+// Adjoint of the batched kernel.  For a pair (i, j) with d = x_j - x_i,
+// r2 = |d|^2 and w = fcoeff m_i m_j:
+//   d dv_i / d x_j = w (g(r2) I + 2 g'(r2) d d^T) =: M,  d dv_i / d x_i = -M,
+// so the pair adds M u_i to xbar_j and subtracts it from xbar_i.  The i side
+// accumulates in registers; the j side is summed over the warp's lanes and
+// added with one atomic per kept entry.
+// ---------------------------------------------------------------------------
+template <int LAW>
+__global__ void __launch_bounds__(32 * kBatchedWarps)
+    k_pairs_vjp(const float4 *__restrict__ pos, const PairItem *__restrict__ items, int64_t nitems,
+                const int32_t *__restrict__ gidx, const int32_t *__restrict__ idx,
+                const float *__restrict__ ux, const float *__restrict__ uy,
+                const float *__restrict__ uz, float *__restrict__ xbx, float *__restrict__ xby,
+                float *__restrict__ xbz, float fcoeff, float rsm2, float rcut2, float rcull2,
+                unsigned long long *__restrict__ queue) {
+  __shared__ float4 slot[kBatchedWarps][32];
+  __shared__ int32_t sidx[kBatchedWarps][32];
+  const int lane = threadIdx.x & 31;
+  const int w = threadIdx.x >> 5;
+  const unsigned full = 0xffffffffu;
+  for (;;) {
+    unsigned long long it = 0;
+    if (lane == 0) it = atomicAdd(queue, 1ull);
+    it = __shfl_sync(full, it, 0);
+    if (it >= (unsigned long long)nitems) break;
+    const PairItem W = items[it];
+    const bool act = lane < W.g_count;
+    const int pi = gidx[W.g_begin + (act ? lane : 0)];
+    const float4 P = pos[pi];
+    // inactive lanes carry a zero cotangent, so they add nothing
+    const float u0 = act ? ux[pi] : 0.f, u1 = act ? uy[pi] : 0.f, u2 = act ? uz[pi] : 0.f;
+    const float wi = (LAW == LAW_POLY5_STEP16) ? fcoeff : fcoeff * P.w;
+    float lox = P.x, hix = P.x, loy = P.y, hiy = P.y, loz = P.z, hiz = P.z;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lox = fminf(lox, __shfl_xor_sync(full, lox, o));
+      hix = fmaxf(hix, __shfl_xor_sync(full, hix, o));
+      loy = fminf(loy, __shfl_xor_sync(full, loy, o));
+      hiy = fmaxf(hiy, __shfl_xor_sync(full, hiy, o));
+      loz = fminf(loz, __shfl_xor_sync(full, loz, o));
+      hiz = fmaxf(hiz, __shfl_xor_sync(full, hiz, o));
+    }
+    float bx = 0.f, by = 0.f, bz = 0.f;
+    const int32_t *lst = idx + W.j_begin;
+    for (int j0 = 0; j0 < W.j_len; j0 += 32) {
+      const int j = j0 + lane;
+      const bool ok = j < W.j_len;
+      const int32_t jt = lst[ok ? j : 0];
+      const float4 J = pos[jt];
+      const float dx = fmaxf(fmaxf(lox - J.x, J.x - hix), 0.f);
+      const float dy = fmaxf(fmaxf(loy - J.y, J.y - hiy), 0.f);
+      const float dz = fmaxf(fmaxf(loz - J.z, J.z - hiz), 0.f);
+      unsigned keep = __ballot_sync(full, ok && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < rcull2);
+      if (!keep) continue;
+      slot[w][lane] = J;
+      sidx[w][lane] = jt;
+      __syncwarp();
+      while (keep) {
+        const int b = __ffs(keep) - 1;
+        keep &= keep - 1;
+        const float4 Q = slot[w][b];
+        const int32_t qt = sidx[w][b];
+        const float ex = Q.x - P.x, ey = Q.y - P.y, ez = Q.z - P.z;
+        const float r2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
+        float vx = 0.f, vy = 0.f, vz = 0.f;
+        if (qt != pi && in_range<LAW>(r2, rcut2)) {
+          const float y = rsqrtf(r2 + rsm2);
+          const float y2 = y * y;
+          const float g = fmaf(y, y2, neg_poly<LAW>(r2));
+          const float gp = fmaf(-1.5f * y2, y2 * y, neg_dpoly<LAW>(r2));  // dg/dr2
+          const float wij = wi * Q.w;
+          const float du = fmaf(ex, u0, fmaf(ey, u1, ez * u2));
+          const float a = wij * g, bq = 2.f * wij * gp * du;
+          vx = fmaf(a, u0, bq * ex);
+          vy = fmaf(a, u1, bq * ey);
+          vz = fmaf(a, u2, bq * ez);
+        }
+        bx -= vx;
+        by -= vy;
+        bz -= vz;
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+          vx += __shfl_xor_sync(full, vx, o);
+          vy += __shfl_xor_sync(full, vy, o);
+          vz += __shfl_xor_sync(full, vz, o);
+        }
+        if (lane == 0 && (vx != 0.f || vy != 0.f || vz != 0.f)) {
+          atomicAdd(xbx + qt, vx);
+          atomicAdd(xby + qt, vy);
+          atomicAdd(xbz + qt, vz);
+        }
+      }
+      __syncwarp();
+    }
+    if (act) {
+      atomicAdd(xbx + pi, bx);
+      atomicAdd(xby + pi, by);
+      atomicAdd(xbz + pi, bz);
+    }
+  }
+}
+
+cudaError_t launch_pairs_vjp(int law, const float4 *pos, const PairItem *items, int64_t nitems,
+                             const int32_t *gidx, const int32_t *idx, const float *ux,
+                             const float *uy, const float *uz, float *xbx, float *xby, float *xbz,
+                             float fcoeff, float rsm2, float rcut2, float rcull2,
+                             unsigned long long *queue, int ctas, cudaStream_t s) {
+  if (nitems <= 0) return cudaSuccess;
+  if (ctas <= 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    ctas = batched_resident_ctas(dev);
+  }
+  const int64_t need = (nitems + kBatchedWarps - 1) / kBatchedWarps;
+  if (ctas > need) ctas = int(need);
+  if (law == LAW_POLY5_STEP16)
+    k_pairs_vjp<LAW_POLY5_STEP16><<<ctas, 32 * kBatchedWarps, 0, s>>>(
+        pos, items, nitems, gidx, idx, ux, uy, uz, xbx, xby, xbz, fcoeff, rsm2, rcut2, rcull2, queue);
+  else
+    k_pairs_vjp<LAW_POLY6><<<ctas, 32 * kBatchedWarps, 0, s>>>(
+        pos, items, nitems, gidx, idx, ux, uy, uz, xbx, xby, xbz, fcoeff, rsm2, rcut2, rcull2, queue);
+  return cudaGetLastError();
+}
+
+// ---------------------------------------------------------------------------
 // Force law on a batch of r2 values (law tests).
 // ---------------------------------------------------------------------------
 template <int LAW>

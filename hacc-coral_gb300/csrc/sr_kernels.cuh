@@ -86,6 +86,31 @@ __device__ __forceinline__ float law_g(float r2, float rsm2) {
   return fmaf(y, y * y, neg_poly<LAW>(r2));
 }
 
+// -p'(r2), the derivative of the law's polynomial, negated.
+template <int LAW>
+__device__ __forceinline__ float neg_dpoly(float r2);
+
+template <>
+__device__ __forceinline__ float neg_dpoly<LAW_POLY6>(float r2) {
+  float q = -6.0f * static_cast<float>(0.000000147305);
+  q = fmaf(q, r2, -5.0f * static_cast<float>(-0.00000663394));
+  q = fmaf(q, r2, -4.0f * static_cast<float>(0.000132336));
+  q = fmaf(q, r2, -3.0f * static_cast<float>(-0.00159485));
+  q = fmaf(q, r2, -2.0f * static_cast<float>(0.0133122));
+  q = fmaf(q, r2, -static_cast<float>(-0.0783394));
+  return q;
+}
+
+template <>
+__device__ __forceinline__ float neg_dpoly<LAW_POLY5_STEP16>(float r2) {
+  float q = -5.0f * static_cast<float>(-0.00000147177);
+  q = fmaf(q, r2, -4.0f * static_cast<float>(0.0000605491));
+  q = fmaf(q, r2, -3.0f * static_cast<float>(-0.00109313));
+  q = fmaf(q, r2, -2.0f * static_cast<float>(0.0114808));
+  q = fmaf(q, r2, -static_cast<float>(-0.0750978));
+  return q;
+}
+
 // Whether a pair at squared distance r2 contributes (the reference's
 // updateq and the law's own range, folded into one strict threshold rcut2;
 // Step16_int also drops r2 == 0).
@@ -129,6 +154,16 @@ cudaError_t launch_pairs_batched(int law, const float4 *pos, const PairItem *ite
                                  unsigned long long *queue, int ctas, cudaStream_t s);
 // CTAs of the batched kernel that fit on the device at once.
 int batched_resident_ctas(int device);
+
+// Vector-Jacobian product of the kick dv_i = fcoeff m_i sum_j m_j g(r2) d_ij
+// with respect to positions, over the same work items: for cotangent u (tree
+// order, 3 x n), adds (d dv / d x)^T u into xbar (3 arrays of ntab entries:
+// particles, then pseudo-particle slots).  Self entries are skipped.
+cudaError_t launch_pairs_vjp(int law, const float4 *pos, const PairItem *items, int64_t nitems,
+                             const int32_t *gidx, const int32_t *idx, const float *ux,
+                             const float *uy, const float *uz, float *xbx, float *xby, float *xbz,
+                             float fcoeff, float rsm2, float rcut2, float rcull2,
+                             unsigned long long *queue, int ctas, cudaStream_t s);
 cudaError_t launch_force_law(int law, const float *r2, float *g, int64_t n, float rsm2, float rcut2,
                              cudaStream_t s);
 

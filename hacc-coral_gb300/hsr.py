@@ -32,7 +32,9 @@ BUILD_DEVICE, BUILD_HOST = 0, 1
 EXPORTS = ("hsr_create", "hsr_destroy", "hsr_last_error", "hsr_version", "hsr_rcb_kick",
            "hsr_get_stats", "hsr_lists_size", "hsr_lists_export", "hsr_build_lists",
            "hsr_lists_info", "hsr_lists_get", "hsr_lists_index", "hsr_lists_free",
-           "hsr_force_law", "hsr_bench_pairs", "hsr_probe_fp32_peak", "hsr_kick_lists_noalloc")
+           "hsr_force_law", "hsr_bench_pairs", "hsr_probe_fp32_peak", "hsr_kick_lists_noalloc",
+           "hsr_force_fwd", "hsr_force_vjp", "hsr_last_perm", "hsr_tree_size", "hsr_tree_export",
+           "hsr_lists_export_index")
 
 
 class HsrError(RuntimeError):
@@ -108,6 +110,18 @@ def load(path: str = LIB_PATH):
     lib.hsr_lists_free.argtypes = [vp]
     lib.hsr_force_law.restype = i32
     lib.hsr_force_law.argtypes = [vp, i32, f32, f32, i64, pf, pf]
+    lib.hsr_force_fwd.restype = i32
+    lib.hsr_force_fwd.argtypes = [vp, C.POINTER(HsrParams), i64, vp, vp, vp, vp, vp, vp, vp, i32]
+    lib.hsr_force_vjp.restype = i32
+    lib.hsr_force_vjp.argtypes = [vp, vp, vp, vp, vp, vp, vp, i32]
+    lib.hsr_last_perm.restype = i32
+    lib.hsr_last_perm.argtypes = [vp, pi64]
+    lib.hsr_tree_size.restype = i32
+    lib.hsr_tree_size.argtypes = [vp, pi64]
+    lib.hsr_tree_export.restype = i32
+    lib.hsr_tree_export.argtypes = [vp, pi64, pi64, pi64, pi64, pf, pf, pf]
+    lib.hsr_lists_export_index.restype = i32
+    lib.hsr_lists_export_index.argtypes = [vp, pi64]
     lib.hsr_kick_lists_noalloc.restype = i32
     lib.hsr_kick_lists_noalloc.argtypes = [vp, i64, i64, vp, vp, vp, vp, i64, vp, vp, vp, vp,
                                            f32, f32, f32, i32, vp]
@@ -209,6 +223,53 @@ class Context:
                                               *[_p(e[i], C.c_float) for i in range(4)]),
                     "hsr_lists_export")
         return off, cnt, ptr, e
+
+    def force_fwd(self, x, y, z, mass, kp, kernel: int = KERNEL_AUTO):
+        """hsr_force_fwd on host arrays; returns dv (n x 3, caller order)."""
+        n = len(x)
+        arrs = [np.ascontiguousarray(a, np.float32) for a in (x, y, z, mass)]
+        dv = [np.zeros(n, np.float32) for _ in range(3)]
+        P = make_params(kp, kernel, BUILD_DEVICE)
+        vp = lambda a: a.ctypes.data_as(C.c_void_p)
+        self._check(self.lib.hsr_force_fwd(self.h, C.byref(P), n, *[vp(a) for a in arrs],
+                                           *[vp(a) for a in dv], MEM_HOST), "hsr_force_fwd")
+        return np.stack(dv, 1)
+
+    def force_vjp(self, dvbar):
+        """hsr_force_vjp: xbar (n x 3) for the cotangent dvbar (n x 3), caller order."""
+        u = [np.ascontiguousarray(dvbar[:, d], np.float32) for d in range(3)]
+        xb = [np.zeros(len(u[0]), np.float32) for _ in range(3)]
+        vp = lambda a: a.ctypes.data_as(C.c_void_p)
+        self._check(self.lib.hsr_force_vjp(self.h, *[vp(a) for a in u], *[vp(a) for a in xb],
+                                           MEM_HOST), "hsr_force_vjp")
+        return np.stack(xb, 1)
+
+    def last_perm(self, n: int):
+        perm = np.zeros(n, np.int64)
+        self._check(self.lib.hsr_last_perm(self.h, _p(perm, C.c_int64)), "hsr_last_perm")
+        return perm
+
+    def tree(self, tdpts: int = 1):
+        nn = C.c_int64()
+        self._check(self.lib.hsr_tree_size(self.h, C.byref(nn)), "hsr_tree_size")
+        nn = nn.value
+        cnt, off, cl, cr = (np.zeros(nn, np.int64) for _ in range(4))
+        tdr = np.zeros(nn, np.float32)
+        bbox = np.zeros((nn, 9), np.float32)
+        ppm = np.zeros((nn, tdpts), np.float32)
+        self._check(self.lib.hsr_tree_export(self.h, _p(cnt, C.c_int64), _p(off, C.c_int64),
+                                             _p(cl, C.c_int64), _p(cr, C.c_int64),
+                                             _p(tdr, C.c_float), _p(bbox, C.c_float),
+                                             _p(ppm, C.c_float)), "hsr_tree_export")
+        return dict(count=cnt, offset=off, cl=cl, cr=cr, tdr=tdr, bbox=bbox, ppm=ppm)
+
+    def lists_index(self):
+        nl, ne = C.c_int64(), C.c_int64()
+        self._check(self.lib.hsr_lists_size(self.h, C.byref(nl), C.byref(ne)), "hsr_lists_size")
+        idx = np.zeros(ne.value, np.int64)
+        self._check(self.lib.hsr_lists_export_index(self.h, _p(idx, C.c_int64)),
+                    "hsr_lists_export_index")
+        return idx
 
     def bench_pairs(self, iters: int, kernel: int = KERNEL_AUTO, flush_l2: bool = True) -> float:
         """Mean ms per relaunch of the last kick's pair kernel (hsr_bench_pairs)."""

@@ -167,6 +167,48 @@ hsr_status hsr_lists_get(const hsr_lists *L, int64_t *leaf_offset, int64_t *leaf
 hsr_status hsr_lists_index(const hsr_lists *L, int64_t *entry_index);
 hsr_status hsr_lists_free(hsr_lists *L);
 
+/* ---- adjoint (vector-Jacobian product) --------------------------------- */
+
+/* Forward half: the short-range velocity change the kick would apply,
+ *   dv_i = fcoeff m_i sum_{j in list(i), r2 < fsrrmax^2} m_j g(r2) (x_j - x_i)
+ * (zero for particles outside the processed leaves), for positions x, y, z and
+ * masses (read only, never permuted), written to dvx, dvy, dvz in the
+ * caller's order.  Keeps the tree, lists and positions on the context as the
+ * tape for hsr_force_vjp (any other kick or forward call replaces it).
+ * mem: HSR_MEM_HOST or HSR_MEM_DEVICE; the tree is built on the device.
+ * No counterpart in the reference (differentiation is new in this build). */
+hsr_status hsr_force_fwd(hsr_ctx *ctx, const hsr_params *p, int64_t n, const float *x,
+                         const float *y, const float *z, const float *mass, float *dvx,
+                         float *dvy, float *dvz, int32_t mem);
+
+/* Backward half: xbar = (d dv / d x)^T dvbar for the tape of the last
+ * hsr_force_fwd, caller's order, with the tree and the lists held fixed (they
+ * are piecewise constant in the positions).  A monopole pseudo-particle sits
+ * at its node's centre of mass, so its gradient passes on to the node's
+ * particles with weights m_k / M_node.  The cutoff is a step: its delta
+ * contribution is not included.  HSR_ERR_STATE without a forward;
+ * HSR_ERR_UNSUPPORTED for 12-point pseudo-particles (tdpts = 12). */
+hsr_status hsr_force_vjp(hsr_ctx *ctx, const float *dvbx, const float *dvby, const float *dvbz,
+                         float *xbx, float *xby, float *xbz, int32_t mem);
+
+/* The tree order of the last kick or forward: position k holds input
+ * particle perm[k] (n entries). */
+hsr_status hsr_last_perm(const hsr_ctx *ctx, int64_t *perm);
+
+/* The last tree's nodes (any numbering; children have larger indices than
+ * their parents): particle range, children (0 = none), pseudo-particle
+ * radius, box and centre of mass (xmin[3], xmax[3], xc[3] per node) and the
+ * tdpts pseudo-particle masses per node.  A node's pseudo-particles sit at
+ * position-table index n + node * tdpts. */
+hsr_status hsr_tree_size(const hsr_ctx *ctx, int64_t *nnodes);
+hsr_status hsr_tree_export(const hsr_ctx *ctx, int64_t *count, int64_t *offset, int64_t *cl,
+                           int64_t *cr, float *tdr, float *bbox9, float *ppm);
+
+/* Position-table index of every list entry of the last kick or forward, in
+ * the order of hsr_lists_export (< n: particle in tree order, >= n:
+ * pseudo-particle). */
+hsr_status hsr_lists_export_index(const hsr_ctx *ctx, int64_t *entry_index);
+
 /* ForceLawSR::f_over_r on the device for a batch of r2 values (host arrays),
  * with the kernel's own FP32 arithmetic; for law tests. */
 hsr_status hsr_force_law(hsr_ctx *ctx, int32_t law, float rsm, float fsrrmax, int64_t n,

@@ -1058,6 +1058,176 @@ void ora_vjp_fp64(int64_t n, const float *x, const float *y, const float *z,
   }
 }
 
+/* Pair term weight and its derivative pieces in FP64. */
+static int pair_terms(int law, double rsm, double rmax2, double mi, double mj, const double d[3],
+                      double *w_g, double *w_gp) {
+  double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+  if (!(r2 < rmax2)) return 0;
+  if (law == ORA_LAW_POLY5_STEP16 && !(r2 > 0)) return 0;
+  double mm = mj * (law == ORA_LAW_POLY5_STEP16 ? 1.0 : mi);
+  *w_g = mm * ora_law_f64(law, rsm, r2);
+  *w_gp = mm * ora_law_dg_f64(law, rsm, r2);
+  return 1;
+}
+
+void ora_vjp_fp64_tab(int64_t n, const float *tab, int64_t ntab, const int64_t *pnode_off,
+                      const int64_t *pnode_cnt, int law, float rsm, float fsrrmax, double c,
+                      int64_t nleaves, const int64_t *leaf_offset, const int64_t *leaf_count,
+                      const int64_t *list_ptr, const int64_t *list_idx, const double *u,
+                      double *xbar) {
+  double rmax2 = (double)(fsrrmax * fsrrmax);
+  double *xt = (double *)calloc((size_t)(3 * ntab), sizeof(double));
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 4)
+#endif
+  for (int64_t l = 0; l < nleaves; ++l) {
+    for (int64_t i = leaf_offset[l]; i < leaf_offset[l] + leaf_count[l]; ++i) {
+      const double *ui = u + 3 * i;
+      double xi[3] = {tab[4 * i], tab[4 * i + 1], tab[4 * i + 2]};
+      double mi = tab[4 * i + 3];
+      double acc[3] = {0, 0, 0};
+      for (int64_t k = list_ptr[l]; k < list_ptr[l + 1]; ++k) {
+        int64_t e = list_idx[k];
+        if (e == i) continue;
+        double d[3] = {tab[4 * e] - xi[0], tab[4 * e + 1] - xi[1], tab[4 * e + 2] - xi[2]};
+        double wg, wgp;
+        if (!pair_terms(law, rsm, rmax2, mi, tab[4 * e + 3], d, &wg, &wgp)) continue;
+        double du = d[0] * ui[0] + d[1] * ui[1] + d[2] * ui[2];
+        for (int a = 0; a < 3; ++a) {
+          double v = c * (wg * ui[a] + 2.0 * wgp * du * d[a]);
+          acc[a] -= v;
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+          xt[3 * e + a] += v;
+        }
+      }
+      for (int a = 0; a < 3; ++a) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+        xt[3 * i + a] += acc[a];
+      }
+    }
+  }
+  for (int64_t k = 0; k < n; ++k)
+    for (int a = 0; a < 3; ++a) xbar[3 * k + a] = xt[3 * k + a];
+  /* pseudo-particles: d xc / d x_k = m_k / M */
+  for (int64_t t = n; t < ntab; ++t) {
+    double g[3] = {xt[3 * t], xt[3 * t + 1], xt[3 * t + 2]};
+    if (g[0] == 0 && g[1] == 0 && g[2] == 0) continue;
+    double M = tab[4 * t + 3];
+    if (M == 0) continue;
+    for (int64_t k = pnode_off[t - n]; k < pnode_off[t - n] + pnode_cnt[t - n]; ++k)
+      for (int a = 0; a < 3; ++a) xbar[3 * k + a] += (double)tab[4 * k + 3] / M * g[a];
+  }
+  free(xt);
+}
+
+typedef struct occ_t { int64_t leaf, pos; } occ_t;
+
+void ora_fd_fp64_tab(int64_t n, const float *tab, int64_t ntab, const int64_t *pnode_off,
+                     const int64_t *pnode_cnt, int law, float rsm, float fsrrmax, double c,
+                     int64_t nleaves, const int64_t *leaf_offset, const int64_t *leaf_count,
+                     const int64_t *list_ptr, const int64_t *list_idx, const double *u,
+                     int64_t nsamples, const int64_t *samples, double h, double *fd, int32_t *near) {
+  double rmax2 = (double)(fsrrmax * fsrrmax), rmax = sqrt(rmax2);
+  /* occurrences of each sample as an entry, directly or through a pseudo-particle */
+  int64_t *sample_of = (int64_t *)malloc((size_t)(n > 0 ? n : 1) * sizeof(int64_t));
+  for (int64_t k = 0; k < n; ++k) sample_of[k] = -1;
+  for (int64_t s = 0; s < nsamples; ++s) sample_of[samples[s]] = s;
+  occ_t **occ = (occ_t **)calloc((size_t)nsamples, sizeof(occ_t *));
+  int64_t *nocc = (int64_t *)calloc((size_t)nsamples, sizeof(int64_t));
+  int64_t *cap = (int64_t *)calloc((size_t)nsamples, sizeof(int64_t));
+  int64_t *own = (int64_t *)malloc((size_t)(nsamples > 0 ? nsamples : 1) * sizeof(int64_t));
+  for (int64_t s = 0; s < nsamples; ++s) own[s] = -1;
+  for (int64_t l = 0; l < nleaves; ++l) {
+    for (int64_t i = leaf_offset[l]; i < leaf_offset[l] + leaf_count[l]; ++i)
+      if (sample_of[i] >= 0) own[sample_of[i]] = l;
+    for (int64_t pos = list_ptr[l]; pos < list_ptr[l + 1]; ++pos) {
+      int64_t e = list_idx[pos];
+      int64_t lo, hi;
+      if (e < n) { lo = e; hi = e + 1; }
+      else { lo = pnode_off[e - n]; hi = lo + pnode_cnt[e - n]; }
+      for (int64_t s = 0; s < nsamples; ++s) {
+        int64_t k = samples[s];
+        if (k < lo || k >= hi) continue;
+        if (nocc[s] == cap[s]) {
+          cap[s] = cap[s] ? 2 * cap[s] : 64;
+          occ[s] = (occ_t *)realloc(occ[s], (size_t)cap[s] * sizeof(occ_t));
+        }
+        occ[s][nocc[s]].leaf = l;
+        occ[s][nocc[s]].pos = pos;
+        nocc[s]++;
+      }
+    }
+  }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 1)
+#endif
+  for (int64_t s = 0; s < nsamples; ++s) {
+    int64_t k = samples[s];
+    double mk = tab[4 * k + 3];
+    near[s] = 0;
+    for (int dim = 0; dim < 3; ++dim) {
+      double Ls[2] = {0, 0};
+      for (int sg = 0; sg < 2; ++sg) {
+        double step = sg == 0 ? h : -h;
+        double L = 0;
+        /* position of table entry e with k displaced */
+#define ENTRY_POS(e, out)                                                            \
+  do {                                                                               \
+    (out)[0] = tab[4 * (e)]; (out)[1] = tab[4 * (e) + 1]; (out)[2] = tab[4 * (e) + 2]; \
+    if ((e) == k) (out)[dim] += step;                                                \
+    else if ((e) >= n && k >= pnode_off[(e) - n] &&                                  \
+             k < pnode_off[(e) - n] + pnode_cnt[(e) - n] && tab[4 * (e) + 3] != 0)   \
+      (out)[dim] += step * mk / (double)tab[4 * (e) + 3];                            \
+  } while (0)
+        if (own[s] >= 0) { /* terms with i = k */
+          int64_t l = own[s];
+          double xk[3] = {tab[4 * k], tab[4 * k + 1], tab[4 * k + 2]};
+          xk[dim] += step;
+          for (int64_t pos = list_ptr[l]; pos < list_ptr[l + 1]; ++pos) {
+            int64_t e = list_idx[pos];
+            if (e == k) continue;
+            double pe[3];
+            ENTRY_POS(e, pe);
+            double d[3] = {pe[0] - xk[0], pe[1] - xk[1], pe[2] - xk[2]};
+            double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            if (fabs(r - rmax) < 2 * h) near[s] = 1;
+            double wg, wgp;
+            if (!pair_terms(law, rsm, rmax2, mk, tab[4 * e + 3], d, &wg, &wgp)) continue;
+            L += c * wg * (u[3 * k] * d[0] + u[3 * k + 1] * d[1] + u[3 * k + 2] * d[2]);
+          }
+        }
+        for (int64_t q = 0; q < nocc[s]; ++q) { /* terms where k is (in) the entry */
+          int64_t l = occ[s][q].leaf, pos = occ[s][q].pos, e = list_idx[pos];
+          double pe[3];
+          ENTRY_POS(e, pe);
+          for (int64_t i = leaf_offset[l]; i < leaf_offset[l] + leaf_count[l]; ++i) {
+            if (i == k || i == e) continue;
+            double d[3] = {pe[0] - tab[4 * i], pe[1] - tab[4 * i + 1], pe[2] - tab[4 * i + 2]};
+            double r = sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+            if (fabs(r - rmax) < 2 * h) near[s] = 1;
+            double wg, wgp;
+            if (!pair_terms(law, rsm, rmax2, tab[4 * i + 3], tab[4 * e + 3], d, &wg, &wgp)) continue;
+            L += c * wg * (u[3 * i] * d[0] + u[3 * i + 1] * d[1] + u[3 * i + 2] * d[2]);
+          }
+        }
+#undef ENTRY_POS
+        Ls[sg] = L;
+      }
+      fd[3 * s + dim] = (Ls[0] - Ls[1]) / (2 * h);
+    }
+  }
+  for (int64_t s = 0; s < nsamples; ++s) free(occ[s]);
+  free(occ);
+  free(nocc);
+  free(cap);
+  free(own);
+  free(sample_of);
+}
+
 /* ------------------------------------------------------------------------- */
 /* Sub-cycle helpers (src/cpu/Particles.cxx)                                 */
 /* ------------------------------------------------------------------------- */

@@ -121,6 +121,25 @@ void ora_vjp_fp64(int64_t n, const float *x, const float *y, const float *z,
                   const int64_t *leaf_count, const int64_t *list_ptr,
                   const int64_t *list_idx, const double *u, double *xbar);
 
+/* The same VJP over lists of position-table indices (tab: ntab x 4 floats,
+ * x y z m; entries >= n are monopole pseudo-particles at their node's centre
+ * of mass, node particle range pnode_off/pnode_cnt per slot idx - n), with
+ * self entries skipped: xbar = (d dv / d x)^T u for dv_i = c m_i sum_j m_j g d.
+ * u, xbar: n x 3. */
+void ora_vjp_fp64_tab(int64_t n, const float *tab, int64_t ntab, const int64_t *pnode_off,
+                      const int64_t *pnode_cnt, int law, float rsm, float fsrrmax, double c,
+                      int64_t nleaves, const int64_t *leaf_offset, const int64_t *leaf_count,
+                      const int64_t *list_ptr, const int64_t *list_idx, const double *u,
+                      double *xbar);
+/* FP64 central differences of L = sum_i u_i . dv_i with the lists fixed, for
+ * each sampled particle k (tree order) and axis: fd[3s + d].  near[s] = 1 when
+ * a pair involving k lies within 2h of the cutoff (the law steps there). */
+void ora_fd_fp64_tab(int64_t n, const float *tab, int64_t ntab, const int64_t *pnode_off,
+                     const int64_t *pnode_cnt, int law, float rsm, float fsrrmax, double c,
+                     int64_t nleaves, const int64_t *leaf_offset, const int64_t *leaf_count,
+                     const int64_t *list_ptr, const int64_t *list_idx, const double *u,
+                     int64_t nsamples, const int64_t *samples, double h, double *fd, int32_t *near);
+
 /* Particles::map1 (src/cpu/Particles.cxx:732-758): x += prefactor*tau*v. */
 void ora_map1(int64_t n, float *x, float *y, float *z, const float *vx,
               const float *vy, const float *vz, float alpha, float pp,

@@ -153,6 +153,11 @@ class Oracle:
         lib.ora_direct_fp64.argtypes = [i64, pf, pf, pf, pf, C.c_int, f32, f32, i64, pi64, pd, pd, pd]
         lib.ora_vjp_fp64.argtypes = [i64, pf, pf, pf, pf, C.c_int, f32, f32, f64, i64, pi64, pi64,
                                      pi64, pi64, pd, pd]
+        lib.ora_vjp_fp64_tab.argtypes = [i64, pf, i64, pi64, pi64, C.c_int, f32, f32, f64, i64, pi64,
+                                         pi64, pi64, pi64, pd, pd]
+        lib.ora_fd_fp64_tab.argtypes = [i64, pf, i64, pi64, pi64, C.c_int, f32, f32, f64, i64, pi64,
+                                        pi64, pi64, pi64, pd, i64, pi64, f64, pd,
+                                        C.POINTER(C.c_int32)]
         lib.ora_map1.argtypes = [i64, pf, pf, pf, pf, pf, pf, f32, f32, f32, f32]
         lib.ora_resort.restype = i64
         lib.ora_resort.argtypes = [i64, C.POINTER(C.c_int), pf, pf, pf, pf, pf, pf, pf, pf, pi64, pu16]
@@ -198,6 +203,39 @@ class Oracle:
                               _ptr(lp, C.c_int64), _ptr(li, C.c_int64),
                               _ptr(u, C.c_double), _ptr(xbar, C.c_double))
         return xbar
+
+    def vjp_tab(self, n, tab, pnode_off, pnode_cnt, c, leaf_offset, leaf_count, list_ptr,
+                list_idx, u, law=LAW_POLY6, rsm=0.1, fsrrmax=3.116326355):
+        """FP64 VJP over table-index lists (monopole pseudo-particles through
+        their node's centre of mass); u, result: n x 3."""
+        tab = np.ascontiguousarray(tab, np.float32)
+        arrs = [np.ascontiguousarray(a, np.int64) for a in (pnode_off, pnode_cnt, leaf_offset,
+                                                             leaf_count, list_ptr, list_idx)]
+        u = np.ascontiguousarray(u, np.float64)
+        xbar = np.zeros((n, 3))
+        self.lib.ora_vjp_fp64_tab(n, _ptr(tab, C.c_float), tab.shape[0], _ptr(arrs[0], C.c_int64),
+                                  _ptr(arrs[1], C.c_int64), law, rsm, fsrrmax, c, len(arrs[2]),
+                                  *[_ptr(a, C.c_int64) for a in arrs[2:]], _ptr(u, C.c_double),
+                                  _ptr(xbar, C.c_double))
+        return xbar
+
+    def fd_tab(self, n, tab, pnode_off, pnode_cnt, c, leaf_offset, leaf_count, list_ptr,
+               list_idx, u, samples, h=1e-4, law=LAW_POLY6, rsm=0.1, fsrrmax=3.116326355):
+        """FP64 central differences of sum_i u_i . dv_i at the sampled
+        particles; returns (fd: s x 3, near_cutoff: s)."""
+        tab = np.ascontiguousarray(tab, np.float32)
+        arrs = [np.ascontiguousarray(a, np.int64) for a in (pnode_off, pnode_cnt, leaf_offset,
+                                                             leaf_count, list_ptr, list_idx)]
+        u = np.ascontiguousarray(u, np.float64)
+        smp = np.ascontiguousarray(samples, np.int64)
+        fd = np.zeros((len(smp), 3))
+        near = np.zeros(len(smp), np.int32)
+        self.lib.ora_fd_fp64_tab(n, _ptr(tab, C.c_float), tab.shape[0], _ptr(arrs[0], C.c_int64),
+                                 _ptr(arrs[1], C.c_int64), law, rsm, fsrrmax, c, len(arrs[2]),
+                                 *[_ptr(a, C.c_int64) for a in arrs[2:]], _ptr(u, C.c_double),
+                                 len(smp), _ptr(smp, C.c_int64), h, _ptr(fd, C.c_double),
+                                 near.ctypes.data_as(C.POINTER(C.c_int32)))
+        return fd, near.astype(bool)
 
     def map1(self, p, alpha, pp, tau, adot):
         self.lib.ora_map1(p.n, *[_ptr(getattr(p, k), C.c_float) for k in ("x", "y", "z", "vx", "vy", "vz")],
