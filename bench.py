@@ -61,6 +61,8 @@ def parse_args():
     ap.add_argument("--nd", type=int, default=128)
     ap.add_argument("--kernel", choices=["auto", "plain", "batched"], default="auto")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--multibox", type=int, default=8,
+                    help="boxes of 96^3 in the multi-box line (0: skip)")
     ap.add_argument("--cpu-slab", type=float, default=0.25,
                     help="fraction of the force box (along x) in the CPU sample")
     return ap.parse_args()
@@ -243,8 +245,36 @@ def main():
     ms_plain = ctx.bench_pairs(max(2, args.steps // 2), kernel=hsr.KERNEL_PLAIN) \
         if kernel != hsr.KERNEL_PLAIN else ms
 
+    ms_graph = ctx.bench_pairs_graph(max(2, args.steps // 2))
+
+    # ---- adjoint: forward + VJP of the same workload ----
+    ctx.force_fwd(p0.x, p0.y, p0.z, p0.mass, kp)
+    u = np.random.default_rng(1).standard_normal((p0.n, 3)).astype(np.float32)
+    ctx.force_vjp(u)
+    vjp_ms = []
+    for _ in range(3):
+        ctx.force_vjp(u)
+        vjp_ms.append(ctx.stats()["t_force_ms"])
+    vjp_ms = min(vjp_ms)
+
     peak = ctx.fp32_peak_tflops()
     achieved = evaluated * FLOPS_PER_PAIR / (ms * 1e-3) / 1e12
+
+    # ---- several boxes in one persistent launch (8 boxes of 96^3) ----
+    multibox = None
+    if args.multibox > 0:
+        boxes = [synth.zeldovich_box(96, z=50.0, seed=100 + b) for b in range(args.multibox)]
+        kpb = [synth.kick_params(b, nd=args.nd) for b in boxes]
+        ctx.rcb_kick_batch([b.copy() for b in boxes], kpb)
+        t0 = time.perf_counter()
+        stb = ctx.rcb_kick_batch([b.copy() for b in boxes], kpb)
+        wall_b = time.perf_counter() - t0
+        ms_b = ctx.bench_pairs(max(3, args.steps // 2))
+        ms_bg = ctx.bench_pairs_graph(max(3, args.steps // 2))
+        multibox = {"boxes": args.multibox, "n_side": 96, "pairs": stb["pairs"],
+                    "one_launch_ms": ms_b, "one_launch_graph_ms": ms_bg,
+                    "pairs_per_s": stb["pairs"] / (ms_b * 1e-3),
+                    "e2e_s": wall_b, "e2e_pairs_per_s": stb["pairs"] / wall_b}
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -263,7 +293,10 @@ def main():
                        "parallelism": f"replicas{world}"},
             "plain_vs_batched": {"plain_pairs_per_s": world * pairs / (ms_plain * 1e-3),
                                  "plain_ms": ms_plain, "selected_ms": ms,
+                                 "selected_graph_ms": ms_graph,
                                  "speedup": ms_plain / ms},
+            "adjoint": {"vjp_ms": vjp_ms, "vjp_pairs_per_s": pairs / (vjp_ms * 1e-3)},
+            "multibox": multibox,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak if peak else None, "traffic": None,
                          "peak_source": "FFMA-chain probe on this device (hsr_probe_fp32_peak)",

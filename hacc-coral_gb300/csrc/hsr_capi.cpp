@@ -94,6 +94,14 @@ constexpr int64_t kJSplit = 8192;
 
 }  // namespace
 
+// Device state of one box of a multi-box kick.
+struct BoxState {
+  hsr::DeviceTree tree;
+  DevBuf in, out, pos4, vel;
+  int64_t n = 0;
+  bool plain = false;
+};
+
 // Device work of the last kick: what a pair-kernel launch reads.
 struct Work {
   const float4 *table = nullptr;
@@ -129,6 +137,13 @@ struct hsr_ctx {
   int last_tdpts = 1;
   Work work;
   int batched_ctas = 0;
+  // multi-box kicks
+  std::vector<std::unique_ptr<BoxState>> boxes;
+  DevBuf d_box_desc, d_box_items;
+  bool last_was_batch = false;
+  int32_t batch_n = 0;        // boxes of the last multi-box kick (replays)
+  int64_t batch_items = 0;
+  int batch_law = 0;
 
   // Launches a pair kernel on the current work (the batched kernel's queue
   // counter and evaluated-pair counter are reset first).
@@ -147,6 +162,15 @@ struct hsr_ctx {
     return hsr::launch_pairs_batched(w.law, w.table, w.items, w.nitems, w.gidx, w.idx, dv, dv + n,
                                      dv + 2 * n, w.fcoeff, w.rsm2, w.rc2, w.rcull2,
                                      d_queue.as<unsigned long long>(), batched_ctas, stream);
+  }
+
+  // The last multi-box kick's one persistent launch, on its resident work.
+  cudaError_t launch_batch_pairs() {
+    cudaError_t e = cudaMemsetAsync(d_queue.p, 0, 2 * sizeof(unsigned long long), stream);
+    if (e != cudaSuccess) return e;
+    return hsr::launch_pairs_batched_multi(batch_law, d_box_desc.as<hsr::BoxDesc>(),
+                                           d_box_items.as<hsr::PairItem>(), batch_items,
+                                           d_queue.as<unsigned long long>(), batched_ctas, stream);
   }
 
   hsr_status fail(hsr_status s, const std::string &msg) {
@@ -204,10 +228,14 @@ hsr_status hsr_destroy(hsr_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (DevBuf *b : {&ctx->d_pos, &ctx->d_vel, &ctx->d_leaves, &ctx->d_segs, &ctx->d_idx, &ctx->d_law,
                     &ctx->d_flush, &ctx->d_probe, &ctx->d_items, &ctx->d_gidx, &ctx->d_queue,
-                    &ctx->d_in, &ctx->d_out, &ctx->d_pos4, &ctx->d_adj})
+                    &ctx->d_in, &ctx->d_out, &ctx->d_pos4, &ctx->d_adj, &ctx->d_box_desc,
+                    &ctx->d_box_items})
     b->release();
   for (PinBuf *b : {&ctx->h_pos, &ctx->h_vel, &ctx->h_leaves, &ctx->h_segs, &ctx->h_items, &ctx->h_gidx})
     b->release();
+  for (auto &b : ctx->boxes)
+    for (DevBuf *d : {&b->in, &b->out, &b->pos4, &b->vel}) d->release();
+  ctx->boxes.clear();
   for (cudaEvent_t ev : {ctx->ev0, ctx->ev1, ctx->ev2, ctx->ev3})
     if (ev) cudaEventDestroy(ev);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -765,6 +793,7 @@ hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, 
   CU(cudaSetDevice(ctx->device), "cudaSetDevice");
   ctx->have_lists = false;
   ctx->tape = false;
+  ctx->last_was_batch = false;
   hsr_stats st{};
   hsr_status r = p->build == HSR_BUILD_HOST
                      ? kick_host_build(ctx, p, n, x, y, z, vx, vy, vz, mass, phi, id, mask, st)
@@ -847,6 +876,7 @@ hsr_status hsr_force_fwd(hsr_ctx *ctx, const hsr_params *p, int64_t n, const flo
   CU(cudaSetDevice(ctx->device), "cudaSetDevice");
   ctx->have_lists = false;
   ctx->tape = false;
+  ctx->last_was_batch = false;
   cudaStream_t s = ctx->stream;
   const size_t nb = size_t(std::max<int64_t>(n, 1)) * 4;
   CU(ctx->d_pos4.ensure(size_t(std::max<int64_t>(n, 1)) * 16), "cudaMalloc(pos4)");
@@ -1079,6 +1109,176 @@ hsr_status hsr_lists_export_index(const hsr_ctx *ctx_c, int64_t *entry_index) {
   return HSR_OK;
 }
 
+hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *params,
+                              const int64_t *ns, float *const *x, float *const *y,
+                              float *const *z, float *const *vx, float *const *vy,
+                              float *const *vz, float *const *mass, float *const *phi,
+                              int64_t *const *id, uint16_t *const *mask, int32_t mem) {
+  if (!ctx) return HSR_ERR_ARG;
+  const auto t_start = clk::now();
+  if (nbox < 1 || nbox > (1 << 20) || !params || !ns || !x || !y || !z || !vx || !vy || !vz ||
+      !mass || !phi || !id || !mask)
+    return ctx->fail(HSR_ERR_ARG, "bad batch arguments");
+  if (mem != HSR_MEM_HOST && mem != HSR_MEM_DEVICE) return ctx->fail(HSR_ERR_ARG, "bad memory kind");
+  for (int32_t b = 0; b < nbox; ++b) {
+    const void *arrs[10] = {x[b], y[b], z[b], vx[b], vy[b], vz[b], mass[b], phi[b], id[b], mask[b]};
+    if (hsr_status e = check_params(&params[b], ns[b], arrs, ctx->err)) return e;
+    if (params[b].law != params[0].law)
+      return ctx->fail(HSR_ERR_UNSUPPORTED, "all boxes of a batch use one force law");
+  }
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  ctx->have_lists = false;
+  ctx->tape = false;
+  cudaStream_t s = ctx->stream;
+  while (int32_t(ctx->boxes.size()) < nbox) ctx->boxes.emplace_back(new BoxState());
+  hsr_stats st{};
+  std::vector<hsr::BoxDesc> desc(static_cast<size_t>(nbox));
+  int64_t total_items = 0;
+  double build_ms = 0, lists_ms = 0;
+  for (int32_t b = 0; b < nbox; ++b) {
+    BoxState &B = *ctx->boxes[b];
+    const hsr_params *p = &params[b];
+    const int64_t n = ns[b];
+    B.n = n;
+    const ArrayLayout A(n);
+    float *arr[8] = {x[b], y[b], z[b], vx[b], vy[b], vz[b], mass[b], phi[b]};
+    CU(B.out.ensure(A.bytes), "cudaMalloc(out)");
+    CU(B.pos4.ensure(size_t(std::max<int64_t>(n, 1)) * 16), "cudaMalloc(pos4)");
+    CU(B.vel.ensure(size_t(std::max<int64_t>(3 * n, 1)) * 4), "cudaMalloc(vel)");
+    const float *in[8];
+    const int64_t *in_id;
+    const uint16_t *in_mask;
+    if (mem == HSR_MEM_HOST) {
+      CU(B.in.ensure(A.bytes), "cudaMalloc(in)");
+      char *ib = B.in.as<char>();
+      for (int i = 0; i < 8; ++i) {
+        CU(cudaMemcpyAsync(ib + A.f[i], arr[i], size_t(n) * 4, cudaMemcpyHostToDevice, s), "H2D arrays");
+        in[i] = reinterpret_cast<const float *>(ib + A.f[i]);
+      }
+      CU(cudaMemcpyAsync(ib + A.id, id[b], size_t(n) * 8, cudaMemcpyHostToDevice, s), "H2D ids");
+      CU(cudaMemcpyAsync(ib + A.mask, mask[b], size_t(n) * 2, cudaMemcpyHostToDevice, s), "H2D masks");
+      in_id = reinterpret_cast<const int64_t *>(ib + A.id);
+      in_mask = reinterpret_cast<const uint16_t *>(ib + A.mask);
+      st.h2d_bytes += n * 42;
+    } else {
+      for (int i = 0; i < 8; ++i) in[i] = arr[i];
+      in_id = id[b];
+      in_mask = mask[b];
+    }
+    CU(hsr::launch_pack4(in[0], in[1], in[2], in[6], B.pos4.as<float4>(), n, s), "pack kernel");
+    hsr::TreeConfig cfg{};
+    for (int i = 0; i < 3; ++i) {
+      cfg.min[i] = p->min[i];
+      cfg.max[i] = p->max[i];
+      cfg.min_force[i] = p->min_force[i];
+      cfg.max_force[i] = p->max_force[i];
+    }
+    cfg.fsrrmax = p->fsrrmax;
+    cfg.tan_oa = std::tan(p->open_angle);
+    cfg.ppc = p->ppc;
+    cfg.nd = int32_t(std::min<int64_t>(p->nd, INT32_MAX));
+    cfg.tdpts = p->tdpts;
+    cudaError_t e = B.tree.build(cfg, n, B.pos4.as<float4>(), kJSplit, s);
+    if (e != cudaSuccess) {
+      if (B.tree.error()) return ctx->fail(HSR_ERR_UNSUPPORTED, B.tree.error());
+      return ctx->cuda_fail(e, "device tree build");
+    }
+    build_ms += B.tree.build_ms();
+    lists_ms += B.tree.lists_ms();
+    const hsr::DeviceTreeInfo &ti = B.tree.info();
+    const int32_t *perm = B.tree.perm();
+    char *ob = B.out.as<char>();
+    float *dv = B.vel.as<float>();
+    CU(hsr::launch_gather_f32(in[3], perm, dv, n, s), "gather vx");
+    CU(hsr::launch_gather_f32(in[4], perm, dv + n, n, s), "gather vy");
+    CU(hsr::launch_gather_f32(in[5], perm, dv + 2 * n, n, s), "gather vz");
+    CU(hsr::launch_gather_f32(in[7], perm, reinterpret_cast<float *>(ob + A.f[7]), n, s), "gather phi");
+    CU(hsr::launch_gather_i64(in_id, perm, reinterpret_cast<int64_t *>(ob + A.id), n, s), "gather id");
+    CU(hsr::launch_gather_u16(in_mask, perm, reinterpret_cast<uint16_t *>(ob + A.mask), n, s),
+       "gather mask");
+    CU(hsr::launch_unpack4(B.tree.table(), reinterpret_cast<float *>(ob + A.f[0]),
+                           reinterpret_cast<float *>(ob + A.f[1]), reinterpret_cast<float *>(ob + A.f[2]),
+                           reinterpret_cast<float *>(ob + A.f[6]), n, s),
+       "unpack kernel");
+    hsr::BoxDesc &D = desc[b];
+    D.table = B.tree.table();
+    D.idx = B.tree.index();
+    D.gidx = B.tree.gidx();
+    D.vx = dv;
+    D.vy = dv + n;
+    D.vz = dv + 2 * n;
+    D.fcoeff = p->fcoeff;
+    D.rsm2 = p->rsm * p->rsm;
+    D.rcut2 = cut2(p->law, p->fsrrmax);
+    D.rcull2 = cull2(D.rcut2);
+    total_items += ti.items;
+    st.n += n;
+    st.nodes += ti.nodes;
+    st.processed_leaves += ti.processed_leaves;
+    st.list_entries += ti.list_entries;
+    st.pairs += ti.pairs;
+    st.cm_fallbacks += ti.cm_fallbacks;
+  }
+  // all boxes' items, tagged with their box, in one persistent launch
+  CU(ctx->d_box_items.ensure(size_t(std::max<int64_t>(total_items, 1)) * sizeof(hsr::PairItem)),
+     "cudaMalloc(items)");
+  CU(ctx->d_box_desc.ensure(size_t(nbox) * sizeof(hsr::BoxDesc)), "cudaMalloc(boxes)");
+  auto *items = ctx->d_box_items.as<hsr::PairItem>();
+  int64_t at = 0;
+  for (int32_t b = 0; b < nbox; ++b) {
+    const int64_t ni = ctx->boxes[b]->tree.info().items;
+    CU(hsr::launch_tag_items(ctx->boxes[b]->tree.items(), items + at, ni, b, s), "tag items");
+    at += ni;
+  }
+  CU(cudaMemcpyAsync(ctx->d_box_desc.p, desc.data(), size_t(nbox) * sizeof(hsr::BoxDesc),
+                     cudaMemcpyHostToDevice, s), "H2D box descriptors");
+  CU(ctx->d_queue.ensure(64), "cudaMalloc(queue)");
+  CU(cudaMemsetAsync(ctx->d_queue.p, 0, 2 * sizeof(unsigned long long), s), "reset queue");
+  if (ctx->batched_ctas == 0) ctx->batched_ctas = hsr::batched_resident_ctas(ctx->device);
+  CU(cudaEventRecord(ctx->ev0, s), "event");
+  CU(hsr::launch_pairs_batched_multi(params[0].law, ctx->d_box_desc.as<hsr::BoxDesc>(), items,
+                                     total_items, ctx->d_queue.as<unsigned long long>(),
+                                     ctx->batched_ctas, s),
+     "multi-box pair kernel");
+  CU(cudaEventRecord(ctx->ev1, s), "event");
+  const cudaMemcpyKind back = mem == HSR_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
+  for (int32_t b = 0; b < nbox; ++b) {
+    BoxState &B = *ctx->boxes[b];
+    const int64_t n = B.n;
+    const ArrayLayout A(n);
+    char *ob = B.out.as<char>();
+    float *dv = B.vel.as<float>();
+    float *arr[8] = {x[b], y[b], z[b], vx[b], vy[b], vz[b], mass[b], phi[b]};
+    for (int d = 0; d < 3; ++d)
+      CU(cudaMemcpyAsync(ob + A.f[3 + d], dv + d * n, size_t(n) * 4, cudaMemcpyDeviceToDevice, s),
+         "copy velocities");
+    for (int i = 0; i < 8; ++i)
+      CU(cudaMemcpyAsync(arr[i], ob + A.f[i], size_t(n) * 4, back, s), "copy arrays back");
+    CU(cudaMemcpyAsync(id[b], ob + A.id, size_t(n) * 8, back, s), "copy ids back");
+    CU(cudaMemcpyAsync(mask[b], ob + A.mask, size_t(n) * 2, back, s), "copy masks back");
+    if (mem == HSR_MEM_HOST) st.d2h_bytes += n * 42;
+  }
+  unsigned long long counters[2] = {0, 0};
+  CU(cudaMemcpyAsync(counters, ctx->d_queue.p, sizeof(counters), cudaMemcpyDeviceToHost, s),
+     "D2H counters");
+  CU(cudaStreamSynchronize(s), "multi-box kick");
+  float fms = 0;
+  CU(cudaEventElapsedTime(&fms, ctx->ev0, ctx->ev1), "event time");
+  st.t_force_ms = fms;
+  st.t_build_ms = build_ms;
+  st.t_walk_ms = lists_ms;
+  st.evaluated_pairs = int64_t(counters[1]);
+  st.work_items = total_items;
+  st.kernel_launches = 1;
+  st.t_total_ms = ms_since(t_start);
+  ctx->stats = st;
+  ctx->last_was_batch = true;
+  ctx->batch_n = nbox;
+  ctx->batch_items = total_items;
+  ctx->batch_law = params[0].law;
+  return HSR_OK;
+}
+
 hsr_status hsr_build_lists(const hsr_params *p, int64_t n, float *x, float *y, float *z, float *vx,
                            float *vy, float *vz, float *mass, float *phi, int64_t *id, uint16_t *mask,
                            hsr_lists **out) {
@@ -1154,10 +1354,13 @@ hsr_status hsr_force_law(hsr_ctx *ctx, int32_t law, float rsm, float fsrrmax, in
 hsr_status hsr_bench_pairs(hsr_ctx *ctx, int32_t kernel, int32_t iters, int32_t flush_l2,
                            double *ms_per_launch) {
   if (!ctx || !ms_per_launch || iters < 1) return HSR_ERR_ARG;
-  if (!ctx->have_lists) return ctx->fail(HSR_ERR_STATE, "no kick to replay");
+  if (!ctx->have_lists && !ctx->last_was_batch) return ctx->fail(HSR_ERR_STATE, "no kick to replay");
   // replays run the kick's own kernel unless the plain one is asked for
+  const bool multi = ctx->last_was_batch;
+  if (multi && kernel == HSR_KERNEL_PLAIN)
+    return ctx->fail(HSR_ERR_STATE, "a multi-box kick replays its batched launch only");
   const int kk = kernel == HSR_KERNEL_PLAIN ? HSR_KERNEL_PLAIN : ctx->work.kernel;
-  if (kk == HSR_KERNEL_BATCHED && ctx->work.nitems == 0 && ctx->work.nleaves > 0)
+  if (!multi && kk == HSR_KERNEL_BATCHED && ctx->work.nitems == 0 && ctx->work.nleaves > 0)
     return ctx->fail(HSR_ERR_STATE, "last kick had no batched work to replay");
   CU(cudaSetDevice(ctx->device), "cudaSetDevice");
   cudaStream_t s = ctx->stream;
@@ -1167,13 +1370,58 @@ hsr_status hsr_bench_pairs(hsr_ctx *ctx, int32_t kernel, int32_t iters, int32_t 
   for (int it = 0; it < iters; ++it) {
     if (flush_l2) CU(cudaMemsetAsync(ctx->d_flush.p, it & 0xff, flush_bytes, s), "L2 flush");
     CU(cudaEventRecord(ctx->ev0, s), "event");
-    CU(ctx->launch_pairs(kk), "pair kernel");
+    CU(multi ? ctx->launch_batch_pairs() : ctx->launch_pairs(kk), "pair kernel");
     CU(cudaEventRecord(ctx->ev1, s), "event");
     CU(cudaEventSynchronize(ctx->ev1), "pair kernel execution");
     float ms = 0;
     CU(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "event time");
     total += ms;
   }
+  *ms_per_launch = total / iters;
+  return HSR_OK;
+}
+
+hsr_status hsr_bench_pairs_graph(hsr_ctx *ctx, int32_t iters, int32_t flush_l2,
+                                 double *ms_per_launch) {
+  if (!ctx || !ms_per_launch || iters < 1) return HSR_ERR_ARG;
+  if (!ctx->have_lists && !ctx->last_was_batch) return ctx->fail(HSR_ERR_STATE, "no kick to replay");
+  const bool multi = ctx->last_was_batch;
+  if (!multi && ctx->work.kernel != HSR_KERNEL_BATCHED)
+    return ctx->fail(HSR_ERR_STATE, "graph replays run the batched kernel");
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  cudaStream_t s = ctx->stream;
+  CU(ctx->d_queue.ensure(64), "cudaMalloc(queue)");
+  if (ctx->batched_ctas == 0) ctx->batched_ctas = hsr::batched_resident_ctas(ctx->device);
+  const size_t flush_bytes = size_t(256) << 20;
+  if (flush_l2) CU(ctx->d_flush.ensure(flush_bytes), "cudaMalloc(flush)");
+  // capture the launch sequence (queue reset + persistent kernel) once
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  CU(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal), "begin capture");
+  cudaError_t le = multi ? ctx->launch_batch_pairs() : ctx->launch_pairs(HSR_KERNEL_BATCHED);
+  cudaError_t ce = cudaStreamEndCapture(s, &graph);
+  if (le != cudaSuccess) {
+    if (graph) cudaGraphDestroy(graph);
+    return ctx->cuda_fail(le, "capture pair launch");
+  }
+  CU(ce, "end capture");
+  cudaError_t ie = cudaGraphInstantiate(&exec, graph, 0);
+  cudaGraphDestroy(graph);
+  CU(ie, "instantiate graph");
+  double total = 0;
+  cudaError_t e = cudaSuccess;
+  for (int it = 0; it < iters && e == cudaSuccess; ++it) {
+    if (flush_l2) e = cudaMemsetAsync(ctx->d_flush.p, it & 0xff, flush_bytes, s);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev0, s);
+    if (e == cudaSuccess) e = cudaGraphLaunch(exec, s);
+    if (e == cudaSuccess) e = cudaEventRecord(ctx->ev1, s);
+    if (e == cudaSuccess) e = cudaEventSynchronize(ctx->ev1);
+    float ms = 0;
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    total += ms;
+  }
+  cudaGraphExecDestroy(exec);
+  CU(e, "graph replay");
   *ms_per_launch = total / iters;
   return HSR_OK;
 }

@@ -102,13 +102,14 @@ cudaError_t launch_leaf_plain(int law, const float4 *pos, const LeafDesc *leaves
 // ---------------------------------------------------------------------------
 constexpr int kBatchedWarps = 8;
 
-template <int LAW>
+template <int LAW, bool MULTI>
 __global__ void __launch_bounds__(32 * kBatchedWarps)
-    k_pairs_batched(const float4 *__restrict__ pos, const PairItem *__restrict__ items,
-                    int64_t nitems, const int32_t *__restrict__ gidx,
-                    const int32_t *__restrict__ idx, float *__restrict__ vx,
-                    float *__restrict__ vy, float *__restrict__ vz, float fcoeff, float rsm2,
-                    float rcut2, float rcull2, unsigned long long *__restrict__ queue) {
+    k_pairs_batched(const float4 *__restrict__ pos_, const PairItem *__restrict__ items,
+                    int64_t nitems, const int32_t *__restrict__ gidx_,
+                    const int32_t *__restrict__ idx_, float *__restrict__ vx_,
+                    float *__restrict__ vy_, float *__restrict__ vz_, float fcoeff_, float rsm2_,
+                    float rcut2_, float rcull2_, unsigned long long *__restrict__ queue,
+                    const BoxDesc *__restrict__ boxes) {
   __shared__ float4 slot[kBatchedWarps][32];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
@@ -120,6 +121,23 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
     it = __shfl_sync(full, it, 0);
     if (it >= (unsigned long long)nitems) break;
     const PairItem W = items[it];
+    const float4 *pos = pos_;
+    const int32_t *gidx = gidx_, *idx = idx_;
+    float *vx = vx_, *vy = vy_, *vz = vz_;
+    float fcoeff = fcoeff_, rsm2 = rsm2_, rcut2 = rcut2_, rcull2 = rcull2_;
+    if (MULTI) {
+      const BoxDesc &B = boxes[W.flags >> 8];
+      pos = B.table;
+      gidx = B.gidx;
+      idx = B.idx;
+      vx = B.vx;
+      vy = B.vy;
+      vz = B.vz;
+      fcoeff = B.fcoeff;
+      rsm2 = B.rsm2;
+      rcut2 = B.rcut2;
+      rcull2 = B.rcull2;
+    }
     const bool act = lane < W.g_count;
     const int pi = gidx[W.g_begin + (act ? lane : 0)];
     const float4 P = pos[pi];
@@ -174,7 +192,7 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
 int batched_resident_ctas(int device) {
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pairs_batched<LAW_POLY6>,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pairs_batched<LAW_POLY6, false>,
                                                 32 * kBatchedWarps, 0);
   return std::max(1, sms) * std::max(1, per);
 }
@@ -192,11 +210,51 @@ cudaError_t launch_pairs_batched(int law, const float4 *pos, const PairItem *ite
   const int64_t need = (nitems + kBatchedWarps - 1) / kBatchedWarps;
   if (ctas > need) ctas = int(need);
   if (law == LAW_POLY5_STEP16)
-    k_pairs_batched<LAW_POLY5_STEP16><<<ctas, 32 * kBatchedWarps, 0, s>>>(
-        pos, items, nitems, gidx, idx, vx, vy, vz, fcoeff, rsm2, rcut2, rcull2, queue);
+    k_pairs_batched<LAW_POLY5_STEP16, false><<<ctas, 32 * kBatchedWarps, 0, s>>>(
+        pos, items, nitems, gidx, idx, vx, vy, vz, fcoeff, rsm2, rcut2, rcull2, queue, nullptr);
   else
-    k_pairs_batched<LAW_POLY6><<<ctas, 32 * kBatchedWarps, 0, s>>>(
-        pos, items, nitems, gidx, idx, vx, vy, vz, fcoeff, rsm2, rcut2, rcull2, queue);
+    k_pairs_batched<LAW_POLY6, false><<<ctas, 32 * kBatchedWarps, 0, s>>>(
+        pos, items, nitems, gidx, idx, vx, vy, vz, fcoeff, rsm2, rcut2, rcull2, queue, nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pairs_batched_multi(int law, const BoxDesc *boxes, const PairItem *items,
+                                       int64_t nitems, unsigned long long *queue, int ctas,
+                                       cudaStream_t s) {
+  if (nitems <= 0) return cudaSuccess;
+  if (ctas <= 0) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    ctas = batched_resident_ctas(dev);
+  }
+  const int64_t need = (nitems + kBatchedWarps - 1) / kBatchedWarps;
+  if (ctas > need) ctas = int(need);
+  if (law == LAW_POLY5_STEP16)
+    k_pairs_batched<LAW_POLY5_STEP16, true><<<ctas, 32 * kBatchedWarps, 0, s>>>(
+        nullptr, items, nitems, nullptr, nullptr, nullptr, nullptr, nullptr, 0.f, 0.f, 0.f, 0.f,
+        queue, boxes);
+  else
+    k_pairs_batched<LAW_POLY6, true><<<ctas, 32 * kBatchedWarps, 0, s>>>(
+        nullptr, items, nitems, nullptr, nullptr, nullptr, nullptr, nullptr, 0.f, 0.f, 0.f, 0.f,
+        queue, boxes);
+  return cudaGetLastError();
+}
+
+__global__ void k_tag_items(const PairItem *in, PairItem *out, int64_t n, int box) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    PairItem it = in[i];
+    it.flags = (it.flags & 0xff) | (box << 8);
+    out[i] = it;
+  }
+}
+
+cudaError_t launch_tag_items(const PairItem *in, PairItem *out, int64_t n, int box,
+                             cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  int64_t blocks = (n + 255) / 256;
+  if (blocks > 152 * 8) blocks = 152 * 8;
+  k_tag_items<<<unsigned(blocks), 256, 0, s>>>(in, out, n, box);
   return cudaGetLastError();
 }
 

@@ -48,6 +48,16 @@ struct alignas(16) PairItem {
   int64_t pad;
 };
 
+// One box of a multi-box launch: where its work lives and its kick
+// parameters.  Items carry their box in flags >> 8.
+struct alignas(16) BoxDesc {
+  const float4 *table;
+  const int32_t *idx;
+  const int32_t *gidx;
+  float *vx, *vy, *vz;
+  float fcoeff, rsm2, rcut2, rcull2;
+};
+
 #if defined(__CUDACC__)
 // -p(r2) for the law's polynomial, in Horner form on negated coefficients.
 // The coefficients are the reference's double literals rounded to float, as
@@ -152,6 +162,14 @@ cudaError_t launch_pairs_batched(int law, const float4 *pos, const PairItem *ite
                                  const int32_t *gidx, const int32_t *idx, float *vx, float *vy,
                                  float *vz, float fcoeff, float rsm2, float rcut2, float rcull2,
                                  unsigned long long *queue, int ctas, cudaStream_t s);
+// The batched kernel over the items of several boxes (items of box b carry
+// b << 8 in flags), one persistent launch; queue as above.
+cudaError_t launch_pairs_batched_multi(int law, const BoxDesc *boxes, const PairItem *items,
+                                       int64_t nitems, unsigned long long *queue, int ctas,
+                                       cudaStream_t s);
+// Copies n items, tagging them with box b.
+cudaError_t launch_tag_items(const PairItem *in, PairItem *out, int64_t n, int box,
+                             cudaStream_t s);
 // CTAs of the batched kernel that fit on the device at once.
 int batched_resident_ctas(int device);
 

@@ -34,7 +34,7 @@ EXPORTS = ("hsr_create", "hsr_destroy", "hsr_last_error", "hsr_version", "hsr_rc
            "hsr_lists_info", "hsr_lists_get", "hsr_lists_index", "hsr_lists_free",
            "hsr_force_law", "hsr_bench_pairs", "hsr_probe_fp32_peak", "hsr_kick_lists_noalloc",
            "hsr_force_fwd", "hsr_force_vjp", "hsr_last_perm", "hsr_tree_size", "hsr_tree_export",
-           "hsr_lists_export_index")
+           "hsr_lists_export_index", "hsr_rcb_kick_batch", "hsr_bench_pairs_graph")
 
 
 class HsrError(RuntimeError):
@@ -125,6 +125,10 @@ def load(path: str = LIB_PATH):
     lib.hsr_kick_lists_noalloc.restype = i32
     lib.hsr_kick_lists_noalloc.argtypes = [vp, i64, i64, vp, vp, vp, vp, i64, vp, vp, vp, vp,
                                            f32, f32, f32, i32, vp]
+    lib.hsr_rcb_kick_batch.restype = i32
+    lib.hsr_rcb_kick_batch.argtypes = [vp, i32, C.POINTER(HsrParams), pi64] + [vp] * 10 + [i32]
+    lib.hsr_bench_pairs_graph.restype = i32
+    lib.hsr_bench_pairs_graph.argtypes = [vp, i32, i32, C.POINTER(C.c_double)]
     lib.hsr_bench_pairs.restype = i32
     lib.hsr_bench_pairs.argtypes = [vp, i32, i32, i32, C.POINTER(C.c_double)]
     lib.hsr_probe_fp32_peak.restype = i32
@@ -277,6 +281,30 @@ class Context:
         self._check(self.lib.hsr_bench_pairs(self.h, kernel, iters, int(flush_l2), C.byref(ms)),
                     "hsr_bench_pairs")
         return ms.value
+
+    def bench_pairs_graph(self, iters: int, flush_l2: bool = True) -> float:
+        """Mean ms per replay of the batched launch captured as a CUDA graph."""
+        ms = C.c_double()
+        self._check(self.lib.hsr_bench_pairs_graph(self.h, iters, int(flush_l2), C.byref(ms)),
+                    "hsr_bench_pairs_graph")
+        return ms.value
+
+    def rcb_kick_batch(self, boxes, kps, kernel: int = KERNEL_AUTO) -> dict:
+        """hsr_rcb_kick_batch on a list of particle sets (host arrays, each
+        permuted and kicked in place) with one KickParams each."""
+        nb = len(boxes)
+        P = (HsrParams * nb)(*[make_params(k, kernel, BUILD_DEVICE) for k in kps])
+        ns = np.array([b.n for b in boxes], np.int64)
+        for b in boxes:
+            _particle_args(b)  # type and size checks
+        tables = []
+        for k in ("x", "y", "z", "vx", "vy", "vz", "mass", "phi", "id", "mask"):
+            arr = (C.c_void_p * nb)(*[getattr(b, k).ctypes.data for b in boxes])
+            tables.append(arr)
+        self._check(self.lib.hsr_rcb_kick_batch(self.h, nb, P, _p(ns, C.c_int64),
+                                                *[C.cast(t, C.c_void_p) for t in tables], MEM_HOST),
+                    "hsr_rcb_kick_batch")
+        return self.stats()
 
     def fp32_peak_tflops(self) -> float:
         t = C.c_double()

@@ -137,6 +137,20 @@ hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, 
 
 hsr_status hsr_get_stats(const hsr_ctx *ctx, hsr_stats *st);
 
+/* Several independent boxes in one call (BASELINE's multi-box batching; no
+ * counterpart in the reference, which kicks one rank's box per constructor):
+ * every box's tree and lists are built on the device, then ONE persistent
+ * launch of the batched kernel evaluates the work items of all boxes, each
+ * with its own parameters (fcoeff, rsm, cutoff; one force law for all).  The
+ * per-box arrays are given as arrays of nbox pointers; each box's arrays are
+ * permuted and kicked exactly as hsr_rcb_kick would.  Statistics sum over the
+ * boxes. */
+hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *params,
+                              const int64_t *n, float *const *x, float *const *y,
+                              float *const *z, float *const *vx, float *const *vy,
+                              float *const *vz, float *const *mass, float *const *phi,
+                              int64_t *const *id, uint16_t *const *mask, int32_t mem);
+
 /* Interaction lists of the last hsr_rcb_kick, for inspection and parity
  * checks.  hsr_lists_size gives the number of processed leaves and of list
  * entries; hsr_lists_export fills leaf_offset/leaf_count (per leaf, into the
@@ -248,9 +262,14 @@ hsr_status hsr_kick_lists_noalloc(const float *table, int64_t ntab, int64_t n,
  * work still resident on the device (the velocities keep accumulating kicks),
  * each launch timed with CUDA events on the context's stream.  flush_l2 != 0
  * overwrites a 256 MB device buffer before every launch so no launch starts
- * with the previous one's data in L2.  *ms_per_launch is the mean time. */
+ * with the previous one's data in L2.  *ms_per_launch is the mean time.
+ * kernel: HSR_KERNEL_PLAIN or the kick's own; HSR_KERNEL_BATCHED after
+ * hsr_rcb_kick_batch replays its one multi-box launch.  use_graph != 0 replays
+ * the launch sequence (queue reset + kernel) as a captured CUDA graph. */
 hsr_status hsr_bench_pairs(hsr_ctx *ctx, int32_t kernel, int32_t iters, int32_t flush_l2,
                            double *ms_per_launch);
+hsr_status hsr_bench_pairs_graph(hsr_ctx *ctx, int32_t iters, int32_t flush_l2,
+                                 double *ms_per_launch);
 
 /* Measures this device's FP32 FMA throughput with a kernel of independent
  * fused multiply-add chains (2 flops each) on every SM; the roofline
