@@ -17,6 +17,7 @@
 #include <cuda_runtime.h>
 
 #include "rcb_device.cuh"
+#include "subcycle.cuh"
 #include "rcb_host.hpp"
 #include "sr_kernels.cuh"
 
@@ -129,7 +130,7 @@ struct hsr_ctx {
   // device-build path: staged inputs and outputs of the ten arrays
   DevBuf d_in, d_out, d_pos4;
   // misc
-  DevBuf d_law, d_flush, d_probe, d_queue, d_adj;
+  DevBuf d_law, d_flush, d_probe, d_queue, d_adj, d_res, d_sort;
   bool tape = false;  // the last call was hsr_force_fwd
   hsr_stats stats{};
   std::string err = "no error";
@@ -229,7 +230,7 @@ hsr_status hsr_destroy(hsr_ctx *ctx) {
   for (DevBuf *b : {&ctx->d_pos, &ctx->d_vel, &ctx->d_leaves, &ctx->d_segs, &ctx->d_idx, &ctx->d_law,
                     &ctx->d_flush, &ctx->d_probe, &ctx->d_items, &ctx->d_gidx, &ctx->d_queue,
                     &ctx->d_in, &ctx->d_out, &ctx->d_pos4, &ctx->d_adj, &ctx->d_box_desc,
-                    &ctx->d_box_items})
+                    &ctx->d_box_items, &ctx->d_res, &ctx->d_sort})
     b->release();
   for (PinBuf *b : {&ctx->h_pos, &ctx->h_vel, &ctx->h_leaves, &ctx->h_segs, &ctx->h_items, &ctx->h_gidx})
     b->release();
@@ -862,6 +863,85 @@ hsr_status hsr_lists_export(const hsr_ctx *ctx_c, int64_t *leaf_offset, int64_t 
     }
   }
   list_ptr[nl] = ti.list_entries;
+  return HSR_OK;
+}
+
+hsr_status hsr_subcycle(hsr_ctx *ctx, const hsr_subcycle_params *sp, int64_t n, float *x,
+                        float *y, float *z, float *vx, float *vy, float *vz, float *mass,
+                        float *phi, int64_t *id, uint16_t *mask, int32_t mem, int64_t *n_inbox) {
+  if (!ctx) return HSR_ERR_ARG;
+  if (!sp) return ctx->fail(HSR_ERR_ARG, "null parameters");
+  const auto t_start = clk::now();
+  const void *arrs[10] = {x, y, z, vx, vy, vz, mass, phi, id, mask};
+  if (hsr_status e = check_params(&sp->kick, n, arrs, ctx->err)) return e;
+  if (mem != HSR_MEM_HOST && mem != HSR_MEM_DEVICE) return ctx->fail(HSR_ERR_ARG, "bad memory kind");
+  if (sp->nsub < 0 || sp->ng[0] < 1 || sp->ng[1] < 1 || sp->ng[2] < 1 ||
+      double(sp->ng[0]) * sp->ng[1] * sp->ng[2] >= 4294967295.0)
+    return ctx->fail(HSR_ERR_ARG, "bad sub-cycle count or grid");
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  ctx->tape = false;
+  ctx->last_was_batch = false;
+  cudaStream_t s = ctx->stream;
+  // resident arrays
+  const ArrayLayout A(n);
+  float *f[8] = {x, y, z, vx, vy, vz, mass, phi};
+  int64_t *ids = id;
+  uint16_t *msk = mask;
+  if (mem == HSR_MEM_HOST) {
+    CU(ctx->d_res.ensure(A.bytes), "cudaMalloc(resident)");
+    char *rb = ctx->d_res.as<char>();
+    for (int i = 0; i < 8; ++i) {
+      CU(cudaMemcpyAsync(rb + A.f[i], f[i], size_t(n) * 4, cudaMemcpyHostToDevice, s), "H2D arrays");
+      f[i] = reinterpret_cast<float *>(rb + A.f[i]);
+    }
+    CU(cudaMemcpyAsync(rb + A.id, id, size_t(n) * 8, cudaMemcpyHostToDevice, s), "H2D ids");
+    CU(cudaMemcpyAsync(rb + A.mask, mask, size_t(n) * 2, cudaMemcpyHostToDevice, s), "H2D masks");
+    ids = reinterpret_cast<int64_t *>(rb + A.id);
+    msk = reinterpret_cast<uint16_t *>(rb + A.mask);
+  }
+  CU(ctx->d_sort.ensure(hsr::resort_scratch_bytes(n)), "cudaMalloc(sort)");
+  // map1's prefactor in float, as the reference computes it
+  const float pf = std::pow(sp->pp, float(1.0 + 1.0 / sp->alpha));
+  const float prefactor = float(1.0 / (sp->alpha * sp->adot * pf));
+  const float pt = prefactor * sp->tau;
+  hsr_stats total{};
+  int64_t inbox = n;
+  for (int32_t step = 0; step < sp->nsub; ++step) {
+    if (!sp->skip_stream) CU(hsr::launch_stream(f[0], f[1], f[2], f[3], f[4], f[5], n, pt, s), "stream");
+    if (!sp->skip_kick) {
+      CU(hsr::resort_by_cell(n, sp->ng, f, ids, msk, ctx->d_sort.p, &inbox, s), "resort");
+      CU(hsr::launch_fill(f[6], n, 1.0f, s), "masses");
+      hsr_stats st{};
+      hsr_status r = kick_device_build(ctx, &sp->kick, inbox, f[0], f[1], f[2], f[3], f[4], f[5],
+                                       f[6], f[7], ids, msk, HSR_MEM_DEVICE, st);
+      if (r != HSR_OK) return r;
+      total.pairs += st.pairs;
+      total.evaluated_pairs += st.evaluated_pairs;
+      total.list_entries += st.list_entries;
+      total.processed_leaves += st.processed_leaves;
+      total.nodes += st.nodes;
+      total.t_build_ms += st.t_build_ms;
+      total.t_walk_ms += st.t_walk_ms;
+      total.t_force_ms += st.t_force_ms;
+      total.cm_fallbacks += st.cm_fallbacks;
+    }
+    if (!sp->skip_stream) CU(hsr::launch_stream(f[0], f[1], f[2], f[3], f[4], f[5], n, pt, s), "stream");
+  }
+  if (mem == HSR_MEM_HOST) {
+    float *out[8] = {x, y, z, vx, vy, vz, mass, phi};
+    for (int i = 0; i < 8; ++i)
+      CU(cudaMemcpyAsync(out[i], f[i], size_t(n) * 4, cudaMemcpyDeviceToHost, s), "D2H arrays");
+    CU(cudaMemcpyAsync(id, ids, size_t(n) * 8, cudaMemcpyDeviceToHost, s), "D2H ids");
+    CU(cudaMemcpyAsync(mask, msk, size_t(n) * 2, cudaMemcpyDeviceToHost, s), "D2H masks");
+    total.h2d_bytes = n * 42;
+    total.d2h_bytes = n * 42;
+  }
+  CU(cudaStreamSynchronize(s), "sub-cycle");
+  if (n_inbox) *n_inbox = inbox;
+  total.n = n;
+  total.t_total_ms = ms_since(t_start);
+  ctx->stats = total;
+  ctx->have_lists = !sp->skip_kick && sp->nsub > 0;
   return HSR_OK;
 }
 

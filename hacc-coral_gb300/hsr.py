@@ -34,7 +34,8 @@ EXPORTS = ("hsr_create", "hsr_destroy", "hsr_last_error", "hsr_version", "hsr_rc
            "hsr_lists_info", "hsr_lists_get", "hsr_lists_index", "hsr_lists_free",
            "hsr_force_law", "hsr_bench_pairs", "hsr_probe_fp32_peak", "hsr_kick_lists_noalloc",
            "hsr_force_fwd", "hsr_force_vjp", "hsr_last_perm", "hsr_tree_size", "hsr_tree_export",
-           "hsr_lists_export_index", "hsr_rcb_kick_batch", "hsr_bench_pairs_graph")
+           "hsr_lists_export_index", "hsr_rcb_kick_batch", "hsr_bench_pairs_graph",
+           "hsr_subcycle")
 
 
 class HsrError(RuntimeError):
@@ -51,6 +52,12 @@ class HsrParams(C.Structure):
                 ("tmin", C.c_int64), ("fcoeff", C.c_float), ("ppc", C.c_float),
                 ("tdpts", C.c_int32), ("law", C.c_int32), ("kernel", C.c_int32),
                 ("build", C.c_int32)]
+
+
+class HsrSubcycleParams(C.Structure):
+    _fields_ = [("kick", HsrParams), ("nsub", C.c_int32), ("ng", C.c_int32 * 3),
+                ("alpha", C.c_float), ("pp", C.c_float), ("tau", C.c_float), ("adot", C.c_float),
+                ("skip_stream", C.c_int32), ("skip_kick", C.c_int32)]
 
 
 class HsrStats(C.Structure):
@@ -125,6 +132,9 @@ def load(path: str = LIB_PATH):
     lib.hsr_kick_lists_noalloc.restype = i32
     lib.hsr_kick_lists_noalloc.argtypes = [vp, i64, i64, vp, vp, vp, vp, i64, vp, vp, vp, vp,
                                            f32, f32, f32, i32, vp]
+    lib.hsr_subcycle.restype = i32
+    lib.hsr_subcycle.argtypes = [vp, C.POINTER(HsrSubcycleParams), i64] + [pf] * 8 + [pi64, pu16, i32,
+                                                                                  pi64]
     lib.hsr_rcb_kick_batch.restype = i32
     lib.hsr_rcb_kick_batch.argtypes = [vp, i32, C.POINTER(HsrParams), pi64] + [vp] * 10 + [i32]
     lib.hsr_bench_pairs_graph.restype = i32
@@ -214,6 +224,21 @@ class Context:
                                    MEM_DEVICE)
         self._check(st, "hsr_rcb_kick(device arrays)")
         return self.stats()
+
+    def subcycle(self, p, kp, nsub, ng, alpha, pp, tau, adot, skip_stream=False,
+                 skip_kick=False, kernel: int = KERNEL_AUTO):
+        """hsr_subcycle on the host arrays of `p` (all n particles, modified in
+        place); returns (stats, in-box count of the last resort)."""
+        S = HsrSubcycleParams()
+        S.kick = make_params(kp, kernel, BUILD_DEVICE)
+        S.nsub = nsub
+        S.ng[:] = [int(v) for v in ng]
+        S.alpha, S.pp, S.tau, S.adot = alpha, pp, tau, adot
+        S.skip_stream, S.skip_kick = int(skip_stream), int(skip_kick)
+        nin = C.c_int64()
+        self._check(self.lib.hsr_subcycle(self.h, C.byref(S), p.n, *_particle_args(p), MEM_HOST,
+                                          C.byref(nin)), "hsr_subcycle")
+        return self.stats(), nin.value
 
     def lists(self):
         nl, ne = C.c_int64(), C.c_int64()

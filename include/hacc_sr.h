@@ -181,6 +181,32 @@ hsr_status hsr_lists_get(const hsr_lists *L, int64_t *leaf_offset, int64_t *leaf
 hsr_status hsr_lists_index(const hsr_lists *L, int64_t *entry_index);
 hsr_status hsr_lists_free(hsr_lists *L);
 
+/* ---- the sub-cycle around the kick ------------------------------------- */
+
+/* Particles::subCycle (src/cpu/Particles.cxx:1176-1201) with map1 (:732-758)
+ * and map2 (:1205-1367) on the device: nsub times
+ *   half-stream  x += prefactor * tau * v,
+ *   resort       stable sort by unit grid cell of the ng box, out-of-box last,
+ *   masses = 1,
+ *   kick         the RCB short-range kick (hsr_rcb_kick) of the in-box
+ *                particles with `kick` (fcoeff = map2's c),
+ *   half-stream.
+ * prefactor = 1 / (alpha * adot * pp^(1 + 1/alpha)) in float as map1 computes
+ * it; tau is map1's argument (stepFraction * tau2).  The arrays stay resident
+ * on the device for all sub-cycles.  *n_inbox receives the in-box count of the
+ * last resort. */
+typedef struct hsr_subcycle_params {
+  hsr_params kick;
+  int32_t nsub;
+  int32_t ng[3];
+  float alpha, pp, tau, adot;
+  int32_t skip_stream, skip_kick;
+} hsr_subcycle_params;
+
+hsr_status hsr_subcycle(hsr_ctx *ctx, const hsr_subcycle_params *sp, int64_t n, float *x,
+                        float *y, float *z, float *vx, float *vy, float *vz, float *mass,
+                        float *phi, int64_t *id, uint16_t *mask, int32_t mem, int64_t *n_inbox);
+
 /* ---- adjoint (vector-Jacobian product) --------------------------------- */
 
 /* Forward half: the short-range velocity change the kick would apply,
