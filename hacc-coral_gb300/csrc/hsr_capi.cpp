@@ -1291,6 +1291,7 @@ hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *para
     D.rsm2 = p->rsm * p->rsm;
     D.rcut2 = cut2(p->law, p->fsrrmax);
     D.rcull2 = cull2(D.rcut2);
+    D.law = hsr::make_law_s(p->law, D.rsm2, D.rcut2);
     total_items += ti.items;
     st.n += n;
     st.nodes += ti.nodes;

@@ -852,20 +852,30 @@ __global__ void k_leaf_desc(const DNode *nodes, const int32_t *leaf_ids, int64_t
 // inside the leaf's box) and the batched kernel's work items.
 // ---------------------------------------------------------------------------
 constexpr int kGroupSort = 1024;
+constexpr int kGroupThreads = 256;
 
-__device__ __forceinline__ uint32_t spread3(uint32_t v) {
-  v &= 0x3ff;
-  v = (v | (v << 16)) & 0x030000ff;
-  v = (v | (v << 8)) & 0x0300f00f;
-  v = (v | (v << 4)) & 0x030c30c3;
-  v = (v | (v << 2)) & 0x09249249;
-  return v;
+// Order-preserving map of a float to an unsigned integer.
+__device__ __forceinline__ uint32_t f2o(float v) {
+  const uint32_t b = __float_as_uint(v);
+  return (b & 0x80000000u) ? ~b : (b | 0x80000000u);
+}
+__device__ __forceinline__ float o2f(uint32_t o) {
+  return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
 }
 
-__global__ void __launch_bounds__(256)
+// Splits each processed leaf into groups of 32 (the last one shorter) by
+// recursive median splits along the longest axis, left parts a multiple of
+// 32: the particles of a group are close, so the batched kernel's box test
+// keeps few list entries.  Every level sorts all segments of the leaf at once
+// by (segment, coordinate along the segment's longest axis).
+__global__ void __launch_bounds__(kGroupThreads)
     k_groups(const DNode *nodes, const int32_t *leaf_ids, int64_t nleaves,
              const float4 *__restrict__ pos, int32_t *gidx) {
   __shared__ uint64_t key[kGroupSort];
+  __shared__ int32_t val[kGroupSort];
+  __shared__ int32_t seg_a[kGroupSort / 32 + 1], seg_c[kGroupSort / 32 + 1];
+  __shared__ uint32_t seg_lo[3][kGroupSort / 32 + 1], seg_hi[3][kGroupSort / 32 + 1];
+  __shared__ int nseg_s, more_s;
   const int64_t li = blockIdx.x;
   if (li >= nleaves) return;
   const DNode &T = nodes[leaf_ids[li]];
@@ -876,41 +886,104 @@ __global__ void __launch_bounds__(256)
   }
   int m = 1;
   while (m < c) m <<= 1;
-  float sc[3];
-  for (int d = 0; d < 3; ++d) {
-    const float ext = T.xmax[d] - T.xmin[d];
-    sc[d] = ext > 0.f ? 1023.0f / ext : 0.f;
-  }
-  for (int i = threadIdx.x; i < m; i += blockDim.x) {
-    uint64_t kv = ~0ull;
-    if (i < c) {
-      const float4 p = pos[T.offset + i];
-      const uint32_t qx = uint32_t(fminf(fmaxf((p.x - T.xmin[0]) * sc[0], 0.f), 1023.f));
-      const uint32_t qy = uint32_t(fminf(fmaxf((p.y - T.xmin[1]) * sc[1], 0.f), 1023.f));
-      const uint32_t qz = uint32_t(fminf(fmaxf((p.z - T.xmin[2]) * sc[2], 0.f), 1023.f));
-      const uint32_t mort = (spread3(qx) << 2) | (spread3(qy) << 1) | spread3(qz);
-      kv = (uint64_t(mort) << 32) | uint32_t(i);
-    }
-    key[i] = kv;
+  // padding slots sort last but pass through the upper half on the way
+  for (int i = threadIdx.x; i < m; i += blockDim.x) val[i] = i < c ? T.offset + i : -1;
+  if (threadIdx.x == 0) {
+    seg_a[0] = 0;
+    seg_c[0] = c;
+    nseg_s = 1;
   }
   __syncthreads();
-  for (int size = 2; size <= m; size <<= 1)
-    for (int stride = size >> 1; stride > 0; stride >>= 1) {
-      for (int i = threadIdx.x; i < m; i += blockDim.x) {
-        const int j = i ^ stride;
-        if (j > i) {
-          const bool up = (i & size) == 0;
-          const uint64_t a = key[i], b = key[j];
-          if ((a > b) == up) {
-            key[i] = b;
-            key[j] = a;
+  for (int level = 0; level < 16; ++level) {
+    const int nseg = nseg_s;
+    // boxes of the segments that still need a split
+    for (int q = threadIdx.x; q < nseg; q += blockDim.x)
+      for (int d = 0; d < 3; ++d) {
+        seg_lo[d][q] = 0xffffffffu;
+        seg_hi[d][q] = 0u;
+      }
+    __syncthreads();
+    for (int i = threadIdx.x; i < c; i += blockDim.x) {
+      int q = 0;
+      while (q + 1 < nseg && seg_a[q + 1] <= i) ++q;
+      if (seg_c[q] <= 32) continue;
+      const float4 p = pos[val[i]];
+      const uint32_t o[3] = {f2o(p.x), f2o(p.y), f2o(p.z)};
+      for (int d = 0; d < 3; ++d) {
+        atomicMin(&seg_lo[d][q], o[d]);
+        atomicMax(&seg_hi[d][q], o[d]);
+      }
+    }
+    __syncthreads();
+    // sort key: segment, then the coordinate on the segment's longest axis
+    for (int i = threadIdx.x; i < m; i += blockDim.x) {
+      uint64_t kv = ~0ull;
+      if (i < c) {
+        int q = 0;
+        while (q + 1 < nseg && seg_a[q + 1] <= i) ++q;
+        uint32_t ko = 0;
+        if (seg_c[q] > 32) {
+          float ext[3];
+          for (int d = 0; d < 3; ++d) ext[d] = o2f(seg_hi[d][q]) - o2f(seg_lo[d][q]);
+          const int ax = (ext[0] >= ext[1] && ext[0] >= ext[2]) ? 0 : (ext[1] >= ext[2] ? 1 : 2);
+          const float4 p = pos[val[i]];
+          ko = f2o(ax == 0 ? p.x : (ax == 1 ? p.y : p.z));
+        } else {
+          ko = uint32_t(i);  // settled segments keep their order
+        }
+        kv = (uint64_t(q) << 32) | ko;
+      }
+      key[i] = kv;
+    }
+    __syncthreads();
+    for (int size = 2; size <= m; size <<= 1)
+      for (int stride = size >> 1; stride > 0; stride >>= 1) {
+        for (int i = threadIdx.x; i < m; i += blockDim.x) {
+          const int j = i ^ stride;
+          if (j > i) {
+            const bool up = (i & size) == 0;
+            const uint64_t ka = key[i], kb = key[j];
+            if ((ka > kb) == up) {
+              key[i] = kb;
+              key[j] = ka;
+              const int32_t t = val[i];
+              val[i] = val[j];
+              val[j] = t;
+            }
           }
         }
+        __syncthreads();
       }
-      __syncthreads();
+    // split every segment above 32 at 32 * ceil(groups / 2)
+    if (threadIdx.x == 0) {
+      int n2 = 0;
+      int32_t na[kGroupSort / 32 + 1], nc[kGroupSort / 32 + 1];
+      int more = 0;
+      for (int q = 0; q < nseg; ++q) {
+        const int32_t a0 = seg_a[q], c0 = seg_c[q];
+        if (c0 <= 32) {
+          na[n2] = a0;
+          nc[n2++] = c0;
+          continue;
+        }
+        const int32_t ng = (c0 + 31) / 32, left = 32 * ((ng + 1) / 2);
+        na[n2] = a0;
+        nc[n2++] = left;
+        na[n2] = a0 + left;
+        nc[n2++] = c0 - left;
+        more |= left > 32 || c0 - left > 32;
+      }
+      for (int q = 0; q < n2; ++q) {
+        seg_a[q] = na[q];
+        seg_c[q] = nc[q];
+      }
+      nseg_s = n2;
+      more_s = more;
     }
-  for (int i = threadIdx.x; i < c; i += blockDim.x)
-    gidx[T.offset + i] = T.offset + int32_t(key[i] & 0xffffffffu);
+    __syncthreads();
+    if (!more_s) break;
+  }
+  for (int i = threadIdx.x; i < c; i += blockDim.x) gidx[T.offset + i] = val[i];
 }
 
 __device__ __forceinline__ int len_bucket(int64_t len) {
@@ -1295,7 +1368,7 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   // ---- groups and work items ----
   DT_CHECK(grow(gidx_, cap_gidx_, nn, s));
   if (nleaves > 0) {
-    k_groups<<<unsigned(nleaves), 256, 0, s>>>(nodes_, leaf_ids_, nleaves, epos_, gidx_);
+    k_groups<<<unsigned(nleaves), kGroupThreads, 0, s>>>(nodes_, leaf_ids_, nleaves, epos_, gidx_);
     k_item_hist<<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(leafdesc_, nleaves, jsplit, counters_);
     k_item_bases<<<1, 32, 0, s>>>(counters_);
   }

@@ -2,6 +2,7 @@
 #include "sr_kernels.cuh"
 
 #include <algorithm>
+#include <cmath>
 
 namespace hsr {
 
@@ -27,6 +28,38 @@ cudaError_t launch_expand_segments(const SegDesc *segs, int64_t nsegs, int32_t *
   if (blocks > 152 * 64) blocks = 152 * 64;
   k_expand_segments<<<unsigned(blocks), 256, 0, s>>>(segs, nsegs, idx);
   return cudaGetLastError();
+}
+
+LawS make_law_s(int law, float rsm2, float rcut2) {
+  // a_k of the law's polynomial in r2 (float values, as the reference stores them)
+  double a[7] = {0, 0, 0, 0, 0, 0, 0};
+  if (law == LAW_POLY5_STEP16) {
+    const float c[6] = {static_cast<float>(0.269327), static_cast<float>(-0.0750978),
+                        static_cast<float>(0.0114808), static_cast<float>(-0.00109313),
+                        static_cast<float>(0.0000605491), static_cast<float>(-0.00000147177)};
+    for (int k = 0; k < 6; ++k) a[k] = c[k];
+  } else {
+    const float c[7] = {static_cast<float>(0.271431), static_cast<float>(-0.0783394),
+                        static_cast<float>(0.0133122), static_cast<float>(-0.00159485),
+                        static_cast<float>(0.000132336), static_cast<float>(-0.00000663394),
+                        static_cast<float>(0.000000147305)};
+    for (int k = 0; k < 7; ++k) a[k] = c[k];
+  }
+  // p(r2) = p(s - t), t = rsm2: b_k = sum_{m >= k} a_m C(m, k) (-t)^(m - k)
+  const double t = rsm2;
+  LawS L{};
+  for (int k = 0; k < 7; ++k) {
+    double b = 0, binom = 1;  // C(m, k) for m = k
+    for (int m = k; m < 7; ++m) {
+      b += a[m] * binom * std::pow(-t, m - k);
+      binom = binom * double(m + 1) / double(m + 1 - k);
+    }
+    L.nb[k] = float(-b);
+  }
+  L.rsm2 = rsm2;
+  L.scut = rcut2 + rsm2;
+  L.drop_self = law == LAW_POLY5_STEP16 ? 1 : 0;
+  return L;
 }
 
 // ---------------------------------------------------------------------------
@@ -107,13 +140,16 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
     k_pairs_batched(const float4 *__restrict__ pos_, const PairItem *__restrict__ items,
                     int64_t nitems, const int32_t *__restrict__ gidx_,
                     const int32_t *__restrict__ idx_, float *__restrict__ vx_,
-                    float *__restrict__ vy_, float *__restrict__ vz_, float fcoeff_, float rsm2_,
-                    float rcut2_, float rcull2_, unsigned long long *__restrict__ queue,
+                    float *__restrict__ vy_, float *__restrict__ vz_, float fcoeff_, LawS law_,
+                    float rcull2_, unsigned long long *__restrict__ queue,
                     const BoxDesc *__restrict__ boxes) {
-  __shared__ float4 slot[kBatchedWarps][32];
+  // kept entries of the current item, compacted; full batches of 32 are
+  // evaluated in one unrolled loop
+  __shared__ float4 buf[kBatchedWarps][64];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
   const unsigned full = 0xffffffffu;
+  const unsigned below = (1u << lane) - 1u;
   unsigned long long evaluated = 0;  // (particle, entry) pairs this warp evaluated
   for (;;) {
     unsigned long long it = 0;
@@ -124,7 +160,8 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
     const float4 *pos = pos_;
     const int32_t *gidx = gidx_, *idx = idx_;
     float *vx = vx_, *vy = vy_, *vz = vz_;
-    float fcoeff = fcoeff_, rsm2 = rsm2_, rcut2 = rcut2_, rcull2 = rcull2_;
+    float fcoeff = fcoeff_, rcull2 = rcull2_;
+    LawS L = law_;
     if (MULTI) {
       const BoxDesc &B = boxes[W.flags >> 8];
       pos = B.table;
@@ -134,9 +171,8 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
       vy = B.vy;
       vz = B.vz;
       fcoeff = B.fcoeff;
-      rsm2 = B.rsm2;
-      rcut2 = B.rcut2;
       rcull2 = B.rcull2;
+      L = B.law;
     }
     const bool act = lane < W.g_count;
     const int pi = gidx[W.g_begin + (act ? lane : 0)];
@@ -154,6 +190,8 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
     }
     float ax = 0.f, ay = 0.f, az = 0.f;
     const int32_t *lst = idx + W.j_begin;
+    int nbuf = 0;  // warp-uniform
+    unsigned kept = 0;
     for (int j0 = 0; j0 < W.j_len; j0 += 32) {
       const int j = j0 + lane;
       const bool ok = j < W.j_len;
@@ -161,18 +199,25 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
       const float dx = fmaxf(fmaxf(lox - J.x, J.x - hix), 0.f);
       const float dy = fmaxf(fmaxf(loy - J.y, J.y - hiy), 0.f);
       const float dz = fmaxf(fmaxf(loz - J.z, J.z - hiz), 0.f);
-      unsigned keep = __ballot_sync(full, ok && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < rcull2);
-      if (!keep) continue;
-      evaluated += (unsigned long long)__popc(keep) * (unsigned long long)W.g_count;
-      slot[w][lane] = J;
-      __syncwarp();
-      while (keep) {
-        const int b = __ffs(keep) - 1;
-        keep &= keep - 1;
-        pair_acc<LAW>(P.x, P.y, P.z, slot[w][b], rsm2, rcut2, ax, ay, az);
+      const bool k = ok && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < rcull2;
+      const unsigned keep = __ballot_sync(full, k);
+      if (k) buf[w][nbuf + __popc(keep & below)] = J;
+      nbuf += __popc(keep);
+      kept += __popc(keep);
+      if (nbuf >= 32) {
+        __syncwarp();
+#pragma unroll 8
+        for (int q = 0; q < 32; ++q) pair_acc_s(P.x, P.y, P.z, buf[w][q], L, ax, ay, az);
+        __syncwarp();
+        if (lane < nbuf - 32) buf[w][lane] = buf[w][32 + lane];
+        nbuf -= 32;
+        __syncwarp();
       }
-      __syncwarp();
     }
+    __syncwarp();
+    for (int q = 0; q < nbuf; ++q) pair_acc_s(P.x, P.y, P.z, buf[w][q], L, ax, ay, az);
+    __syncwarp();
+    evaluated += (unsigned long long)kept * (unsigned long long)W.g_count;
     if (act) {
       const float c = (LAW == LAW_POLY5_STEP16) ? fcoeff : fcoeff * P.w;
       if (W.flags & 1) {
@@ -209,12 +254,13 @@ cudaError_t launch_pairs_batched(int law, const float4 *pos, const PairItem *ite
   }
   const int64_t need = (nitems + kBatchedWarps - 1) / kBatchedWarps;
   if (ctas > need) ctas = int(need);
+  const LawS L = make_law_s(law, rsm2, rcut2);
   if (law == LAW_POLY5_STEP16)
     k_pairs_batched<LAW_POLY5_STEP16, false><<<ctas, 32 * kBatchedWarps, 0, s>>>(
-        pos, items, nitems, gidx, idx, vx, vy, vz, fcoeff, rsm2, rcut2, rcull2, queue, nullptr);
+        pos, items, nitems, gidx, idx, vx, vy, vz, fcoeff, L, rcull2, queue, nullptr);
   else
     k_pairs_batched<LAW_POLY6, false><<<ctas, 32 * kBatchedWarps, 0, s>>>(
-        pos, items, nitems, gidx, idx, vx, vy, vz, fcoeff, rsm2, rcut2, rcull2, queue, nullptr);
+        pos, items, nitems, gidx, idx, vx, vy, vz, fcoeff, L, rcull2, queue, nullptr);
   return cudaGetLastError();
 }
 
@@ -229,14 +275,15 @@ cudaError_t launch_pairs_batched_multi(int law, const BoxDesc *boxes, const Pair
   }
   const int64_t need = (nitems + kBatchedWarps - 1) / kBatchedWarps;
   if (ctas > need) ctas = int(need);
+  const LawS L{};
   if (law == LAW_POLY5_STEP16)
     k_pairs_batched<LAW_POLY5_STEP16, true><<<ctas, 32 * kBatchedWarps, 0, s>>>(
-        nullptr, items, nitems, nullptr, nullptr, nullptr, nullptr, nullptr, 0.f, 0.f, 0.f, 0.f,
-        queue, boxes);
+        nullptr, items, nitems, nullptr, nullptr, nullptr, nullptr, nullptr, 0.f, L, 0.f, queue,
+        boxes);
   else
     k_pairs_batched<LAW_POLY6, true><<<ctas, 32 * kBatchedWarps, 0, s>>>(
-        nullptr, items, nitems, nullptr, nullptr, nullptr, nullptr, nullptr, 0.f, 0.f, 0.f, 0.f,
-        queue, boxes);
+        nullptr, items, nitems, nullptr, nullptr, nullptr, nullptr, nullptr, 0.f, L, 0.f, queue,
+        boxes);
   return cudaGetLastError();
 }
 

@@ -48,6 +48,16 @@ struct alignas(16) PairItem {
   int64_t pad;
 };
 
+// The law in terms of s = r2 + rsm^2, for the batched kernel: g = s^-3/2 +
+// q(s) with q(s) = -p(s - rsm^2) re-expanded in s (nb[k], computed in double
+// and rounded), and the cutoff as s < scut (scut = rcut2 + rsm^2 in float).
+// Step16 also drops s <= rsm^2, i.e. r2 == 0.
+struct LawS {
+  float nb[7];
+  float rsm2, scut;
+  int32_t drop_self;
+};
+
 // One box of a multi-box launch: where its work lives and its kick
 // parameters.  Items carry their box in flags >> 8.
 struct alignas(16) BoxDesc {
@@ -56,7 +66,11 @@ struct alignas(16) BoxDesc {
   const int32_t *gidx;
   float *vx, *vy, *vz;
   float fcoeff, rsm2, rcut2, rcull2;
+  LawS law;
 };
+
+// LawS of a law with softening rsm and strict cutoff rcut2 on r2.
+LawS make_law_s(int law, float rsm2, float rcut2);
 
 #if defined(__CUDACC__)
 // -p(r2) for the law's polynomial, in Horner form on negated coefficients.
@@ -128,6 +142,30 @@ template <int LAW>
 __device__ __forceinline__ bool in_range(float r2, float rcut2) {
   if (LAW == LAW_POLY5_STEP16) return r2 < rcut2 && r2 > 0.0f;
   return r2 < rcut2;
+}
+
+// One pair in the s form (batched kernel): FMA chain from rsm^2 straight to
+// s, polynomial in s, accumulation predicated on the cutoff.
+__device__ __forceinline__ void pair_acc_s(float xi, float yi, float zi, const float4 pj,
+                                           const LawS &L, float &ax, float &ay, float &az) {
+  const float dx = pj.x - xi;
+  const float dy = pj.y - yi;
+  const float dz = pj.z - zi;
+  const float s = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, L.rsm2)));
+  const float y = rsqrtf(s);
+  float q = L.nb[6];
+  q = fmaf(q, s, L.nb[5]);
+  q = fmaf(q, s, L.nb[4]);
+  q = fmaf(q, s, L.nb[3]);
+  q = fmaf(q, s, L.nb[2]);
+  q = fmaf(q, s, L.nb[1]);
+  q = fmaf(q, s, L.nb[0]);
+  const float w = pj.w * fmaf(y, y * y, q);
+  if (s < L.scut && (!L.drop_self || s > L.rsm2)) {
+    ax = fmaf(w, dx, ax);
+    ay = fmaf(w, dy, ay);
+    az = fmaf(w, dz, az);
+  }
 }
 
 // One pair: accumulates m_j g(r2) d into (ax, ay, az).
