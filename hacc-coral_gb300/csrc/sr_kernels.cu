@@ -136,7 +136,7 @@ cudaError_t launch_leaf_plain(int law, const float4 *pos, const LeafDesc *leaves
 constexpr int kBatchedWarps = 8;
 
 template <int LAW, bool MULTI>
-__global__ void __launch_bounds__(32 * kBatchedWarps)
+__global__ void __launch_bounds__(32 * kBatchedWarps, 5)
     k_pairs_batched(const float4 *__restrict__ pos_, const PairItem *__restrict__ items,
                     int64_t nitems, const int32_t *__restrict__ gidx_,
                     const int32_t *__restrict__ idx_, float *__restrict__ vx_,
@@ -207,7 +207,7 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
       if (nbuf >= 32) {
         __syncwarp();
 #pragma unroll 8
-        for (int q = 0; q < 32; ++q) pair_acc_s(P.x, P.y, P.z, buf[w][q], L, ax, ay, az);
+        for (int q = 0; q < 32; ++q) pair_acc_s<LAW == LAW_POLY5_STEP16>(P.x, P.y, P.z, buf[w][q], L, ax, ay, az);
         __syncwarp();
         if (lane < nbuf - 32) buf[w][lane] = buf[w][32 + lane];
         nbuf -= 32;
@@ -215,7 +215,7 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
       }
     }
     __syncwarp();
-    for (int q = 0; q < nbuf; ++q) pair_acc_s(P.x, P.y, P.z, buf[w][q], L, ax, ay, az);
+    for (int q = 0; q < nbuf; ++q) pair_acc_s<LAW == LAW_POLY5_STEP16>(P.x, P.y, P.z, buf[w][q], L, ax, ay, az);
     __syncwarp();
     evaluated += (unsigned long long)kept * (unsigned long long)W.g_count;
     if (act) {

@@ -144,15 +144,25 @@ __device__ __forceinline__ bool in_range(float r2, float rcut2) {
   return r2 < rcut2;
 }
 
+// 1/sqrt(s), approximate, subnormals flushed: s >= rsm^2 is a normal number
+// for every law with softening, and the flush saves the subnormal rescaling.
+__device__ __forceinline__ float rsqrt_ftz(float s) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(s));
+  return y;
+}
+
 // One pair in the s form (batched kernel): FMA chain from rsm^2 straight to
-// s, polynomial in s, accumulation predicated on the cutoff.
+// s, polynomial in s, weight zeroed outside the cutoff (and, for Step16, at
+// r2 == 0).
+template <bool DROP_SELF>
 __device__ __forceinline__ void pair_acc_s(float xi, float yi, float zi, const float4 pj,
                                            const LawS &L, float &ax, float &ay, float &az) {
   const float dx = pj.x - xi;
   const float dy = pj.y - yi;
   const float dz = pj.z - zi;
   const float s = fmaf(dx, dx, fmaf(dy, dy, fmaf(dz, dz, L.rsm2)));
-  const float y = rsqrtf(s);
+  const float y = rsqrt_ftz(s);
   float q = L.nb[6];
   q = fmaf(q, s, L.nb[5]);
   q = fmaf(q, s, L.nb[4]);
@@ -160,12 +170,12 @@ __device__ __forceinline__ void pair_acc_s(float xi, float yi, float zi, const f
   q = fmaf(q, s, L.nb[2]);
   q = fmaf(q, s, L.nb[1]);
   q = fmaf(q, s, L.nb[0]);
-  const float w = pj.w * fmaf(y, y * y, q);
-  if (s < L.scut && (!L.drop_self || s > L.rsm2)) {
-    ax = fmaf(w, dx, ax);
-    ay = fmaf(w, dy, ay);
-    az = fmaf(w, dz, az);
-  }
+  float w = pj.w * fmaf(y, y * y, q);
+  const bool in = DROP_SELF ? (s < L.scut && s > L.rsm2) : (s < L.scut);
+  w = in ? w : 0.f;
+  ax = fmaf(w, dx, ax);
+  ay = fmaf(w, dy, ay);
+  az = fmaf(w, dz, az);
 }
 
 // One pair: accumulates m_j g(r2) d into (ax, ay, az).
