@@ -77,6 +77,31 @@ def workload(ng: int, nd: int):
     return p, kp, cfg
 
 
+TRAFFIC_NOTE = ("dram__bytes_read.sum + dram__bytes_write.sum of one ncu capture of the pair "
+                "kernel on this workload and shape, bytes per launch (profiles/, line "
+                "'traffic <workload> <shape>: <bytes>')")
+
+
+def profiled_traffic(workload: str, shape: dict):
+    """DRAM bytes per launch of the pair kernel from the committed ncu
+    summaries, or None when no capture of this workload and shape exists."""
+    key = (f"traffic {workload} {shape['kernel']}-"
+           f"{shape['group'] if shape['kernel'] == 'batched' else shape['leaf_threads']}:")
+    pdir = os.path.join(ROOT, "profiles")
+    for name in sorted(os.listdir(pdir)) if os.path.isdir(pdir) else []:
+        if not name.endswith((".md", ".txt")):
+            continue
+        with open(os.path.join(pdir, name)) as f:
+            for line in f:
+                line = line.strip().strip("`")
+                if line.startswith(key):
+                    try:
+                        return int(line[len(key):].split()[0])
+                    except ValueError:
+                        return None
+    return None
+
+
 def dist_init():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -217,6 +242,14 @@ def main():
     p0, kp, cfg = workload(args.ng, args.nd)
     ctx = hsr.Context(local)
 
+    # ---- launch shape: time every shape on this workload, keep the fastest ----
+    tune_rows = None
+    if kernel == hsr.KERNEL_AUTO:
+        ctx.rcb_kick(p0.copy(), kp, kernel=kernel)
+        tune_rows = [{k: (round(v, 4) if k == "ms" else v) for k, v in r.items()}
+                     for r in ctx.autotune(iters=3)]
+    cfg["shape"] = ctx.get_tune()
+
     # ---- end to end through the C ABI (host arrays in, host arrays out) ----
     for _ in range(max(args.warmup, 3)):
         ctx.rcb_kick(p0.copy(), kp, kernel=kernel)
@@ -298,7 +331,9 @@ def main():
             "adjoint": {"vjp_ms": vjp_ms, "vjp_pairs_per_s": pairs / (vjp_ms * 1e-3)},
             "multibox": multibox,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak if peak else None, "traffic": None,
+                         "frac": achieved / peak if peak else None,
+                         "traffic": profiled_traffic(cfg["workload"], cfg["shape"]),
+                         "traffic_source": TRAFFIC_NOTE,
                          "peak_source": "FFMA-chain probe on this device (hsr_probe_fp32_peak)",
                          "flops_per_pair": FLOPS_PER_PAIR,
                          "pairs_basis": "evaluated pairs (after the box test)"},
@@ -306,7 +341,10 @@ def main():
             "e2e": {"value": world * pairs * args.steps / e2e_t, "unit": UNIT,
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "s_per_kick": e2e_t / args.steps,
-                    "host_build_ms": st["t_build_ms"], "host_walk_ms": st["t_walk_ms"]},
+                    "tree_build_ms": st["t_build_ms"], "lists_ms": st["t_walk_ms"],
+                    "h2d_ms": st["t_h2d_ms"], "force_ms": st["t_force_ms"],
+                    "d2h_ms": st["t_d2h_ms"]},
+            "autotune": tune_rows,
             "gpu_launches": args.steps,
             "clocks": cs.summary(),
         }

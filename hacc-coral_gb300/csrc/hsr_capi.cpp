@@ -114,6 +114,8 @@ struct Work {
   int64_t n = 0, nleaves = 0, nitems = 0;
   int law = 0;
   int kernel = HSR_KERNEL_BATCHED;
+  int leaf_threads = 128;  // plain kernel: threads per leaf
+  int group = 32;          // batched kernel: particles per group of the items
   float fcoeff = 0, rsm2 = 0, rc2 = 0, rcull2 = 0;
   bool device_built = false;
 };
@@ -145,6 +147,9 @@ struct hsr_ctx {
   int32_t batch_n = 0;        // boxes of the last multi-box kick (replays)
   int64_t batch_items = 0;
   int batch_law = 0;
+  int batch_group = 32;
+  // launch shapes (hsr_set_tune / hsr_autotune)
+  hsr_tune tune{HSR_KERNEL_BATCHED, 128, 32, 0};
 
   // Launches a pair kernel on the current work (the batched kernel's queue
   // counter and evaluated-pair counter are reset first).
@@ -153,14 +158,14 @@ struct hsr_ctx {
     float *dv = w.vel;
     const int64_t n = w.n;
     if (kernel == HSR_KERNEL_PLAIN)
-      return hsr::launch_leaf_plain(w.law, w.table, w.leaves, w.nleaves, w.idx, dv, dv + n,
+      return hsr::launch_leaf_plain(w.law, w.leaf_threads, w.table, w.leaves, w.nleaves, w.idx, dv, dv + n,
                                     dv + 2 * n, w.fcoeff, w.rsm2, w.rc2, stream);
     if (batched_ctas == 0) batched_ctas = hsr::batched_resident_ctas(device);
     cudaError_t e = d_queue.ensure(64);
     if (e != cudaSuccess) return e;
     e = cudaMemsetAsync(d_queue.p, 0, 2 * sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
-    return hsr::launch_pairs_batched(w.law, w.table, w.items, w.nitems, w.gidx, w.idx, dv, dv + n,
+    return hsr::launch_pairs_batched(w.law, w.group, w.table, w.items, w.nitems, w.gidx, w.idx, dv, dv + n,
                                      dv + 2 * n, w.fcoeff, w.rsm2, w.rc2, w.rcull2,
                                      d_queue.as<unsigned long long>(), batched_ctas, stream);
   }
@@ -169,7 +174,7 @@ struct hsr_ctx {
   cudaError_t launch_batch_pairs() {
     cudaError_t e = cudaMemsetAsync(d_queue.p, 0, 2 * sizeof(unsigned long long), stream);
     if (e != cudaSuccess) return e;
-    return hsr::launch_pairs_batched_multi(batch_law, d_box_desc.as<hsr::BoxDesc>(),
+    return hsr::launch_pairs_batched_multi(batch_law, batch_group, d_box_desc.as<hsr::BoxDesc>(),
                                            d_box_items.as<hsr::PairItem>(), batch_items,
                                            d_queue.as<unsigned long long>(), batched_ctas, stream);
   }
@@ -264,6 +269,8 @@ hsr_status check_params(const hsr_params *p, int64_t n, const void *const *arrs,
   if (p->nd < 1) return err = "nd must be >= 1", HSR_ERR_ARG;
   if (p->law != HSR_LAW_POLY6 && p->law != HSR_LAW_POLY5_STEP16)
     return err = "unknown force law", HSR_ERR_ARG;
+  if (p->kernel != HSR_KERNEL_AUTO && p->kernel != HSR_KERNEL_PLAIN && p->kernel != HSR_KERNEL_BATCHED)
+    return err = "unknown kernel", HSR_ERR_ARG;
   // int32 position-table indices: particles plus pseudo-particles of <= 2n+1 nodes
   if (n > (int64_t(INT32_MAX) - 64) / (1 + 2 * int64_t(p->tdpts)))
     return err = "too many particles for one call", HSR_ERR_ARG;
@@ -433,7 +440,7 @@ void export_lists(const hsr::RcbHost &H, const float *tab, int64_t *leaf_offset,
 // emits one batched-kernel item per group and list chunk of at most `jsplit`
 // entries, sorted by list length, longest first.  gidx has n entries: each
 // leaf's range holds a permutation of its particles, grouped.
-void make_items(hsr::RcbHost &H, const std::vector<int64_t> &list_begin, int64_t jsplit,
+void make_items(hsr::RcbHost &H, const std::vector<int64_t> &list_begin, int64_t jsplit, int G,
                 std::vector<int32_t> &gidx, std::vector<hsr::PairItem> &items) {
   const auto &leaves = H.leaves();
   const auto &el = H.elems();
@@ -441,7 +448,7 @@ void make_items(hsr::RcbHost &H, const std::vector<int64_t> &list_begin, int64_t
   gidx.resize(size_t(H.n()));
   std::vector<int64_t> item_base(size_t(nl) + 1, 0);
   for (int64_t l = 0; l < nl; ++l) {
-    const int64_t ng = std::max<int64_t>(0, (leaves[l].count + 31) / 32);
+    const int64_t ng = std::max<int64_t>(0, (leaves[l].count + G - 1) / G);
     const int64_t nch = std::max<int64_t>(1, (leaves[l].list_len + jsplit - 1) / jsplit);
     item_base[l + 1] = item_base[l] + ng * nch;
   }
@@ -459,7 +466,7 @@ void make_items(hsr::RcbHost &H, const std::vector<int64_t> &list_begin, int64_t
       while (!stack.empty()) {
         auto [a, c] = stack.back();
         stack.pop_back();
-        if (c <= 32) {
+        if (c <= G) {
           if (c > 0) out.push_back({a, c});
           continue;
         }
@@ -475,8 +482,8 @@ void make_items(hsr::RcbHost &H, const std::vector<int64_t> &list_begin, int64_t
         int d = 0;
         for (int k = 1; k < 3; ++k)
           if (hi[k] - lo[k] > hi[d] - lo[d]) d = k;
-        const int32_t ng = (c + 31) / 32;
-        const int32_t left = 32 * ((ng + 1) / 2);
+        const int32_t ng = (c + G - 1) / G;
+        const int32_t left = G * ((ng + 1) / 2);
         auto key = [&](int32_t i) {
           const hsr::Elem &q = el[i];
           return d == 0 ? q.x : d == 1 ? q.y : q.z;
@@ -516,14 +523,16 @@ struct hsr_lists {
 
 namespace {
 
-void set_work_params(Work &w, const hsr_params *p, int64_t n) {
+void set_work_params(Work &w, const hsr_params *p, int64_t n, const hsr_tune &t) {
   w.n = n;
   w.law = p->law;
   w.fcoeff = p->fcoeff;
   w.rsm2 = p->rsm * p->rsm;
   w.rc2 = cut2(p->law, p->fsrrmax);
   w.rcull2 = cull2(w.rc2);
-  w.kernel = p->kernel == HSR_KERNEL_PLAIN ? HSR_KERNEL_PLAIN : HSR_KERNEL_BATCHED;
+  w.kernel = p->kernel == HSR_KERNEL_AUTO ? t.kernel : p->kernel;
+  w.leaf_threads = t.leaf_threads;
+  w.group = t.group;
 }
 
 // Tree and lists on the host (rcb_host.cpp), pair kernel on the device.
@@ -545,13 +554,13 @@ hsr_status kick_host_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *
   std::vector<int64_t> list_begin;
   host_fill(H, n, x, y, z, vx, vy, vz, mass, phi, id, mask, hp, hv, hl, hs, &list_begin);
   Work &w = ctx->work;
-  set_work_params(w, p, n);
+  set_work_params(w, p, n, ctx->tune);
   const bool plain = w.kernel == HSR_KERNEL_PLAIN;
   int64_t nitems = 0;
   if (!plain) {
     std::vector<int32_t> gidx;
     std::vector<hsr::PairItem> items;
-    make_items(H, list_begin, kJSplit, gidx, items);
+    make_items(H, list_begin, kJSplit, w.group, gidx, items);
     nitems = int64_t(items.size());
     CU(ctx->h_items.ensure(std::max<size_t>(items.size(), 1) * sizeof(hsr::PairItem)), "cudaHostAlloc(items)");
     CU(ctx->h_gidx.ensure(std::max<size_t>(gidx.size(), 1) * 4), "cudaHostAlloc(gidx)");
@@ -692,6 +701,7 @@ hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float
   cfg.ppc = p->ppc;
   cfg.nd = int32_t(std::min<int64_t>(p->nd, INT32_MAX));
   cfg.tdpts = p->tdpts;
+  cfg.group = ctx->tune.group;
   {
     const char *f = std::getenv("HSR_FORCE_CM_FALLBACK");  // test hook
     cfg.force_cm_fallback = (f && f[0] == '1') ? 1 : 0;
@@ -711,7 +721,7 @@ hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float
   const int32_t *perm = ctx->tree.perm();
   // outputs in tree order: velocities to the kick buffer, the rest to d_out
   Work &w = ctx->work;
-  set_work_params(w, p, n);
+  set_work_params(w, p, n, ctx->tune);
   float *ovx = reinterpret_cast<float *>(ob + A.f[3]), *ovy = reinterpret_cast<float *>(ob + A.f[4]),
         *ovz = reinterpret_cast<float *>(ob + A.f[5]);
   CU(ctx->d_vel.ensure(size_t(std::max<int64_t>(3 * n, 1)) * 4), "cudaMalloc(vel)");
@@ -983,6 +993,7 @@ hsr_status hsr_force_fwd(hsr_ctx *ctx, const hsr_params *p, int64_t n, const flo
   cfg.ppc = p->ppc;
   cfg.nd = int32_t(std::min<int64_t>(p->nd, INT32_MAX));
   cfg.tdpts = p->tdpts;
+  cfg.group = ctx->tune.group;
   cudaError_t e = ctx->tree.build(cfg, n, pos4, kJSplit, s);
   if (e != cudaSuccess) {
     if (ctx->tree.error()) return ctx->fail(HSR_ERR_UNSUPPORTED, ctx->tree.error());
@@ -990,7 +1001,7 @@ hsr_status hsr_force_fwd(hsr_ctx *ctx, const hsr_params *p, int64_t n, const flo
   }
   const hsr::DeviceTreeInfo &ti = ctx->tree.info();
   Work &w = ctx->work;
-  set_work_params(w, p, n);
+  set_work_params(w, p, n, ctx->tune);
   CU(ctx->d_vel.ensure(size_t(std::max<int64_t>(3 * n, 1)) * 4 + 256), "cudaMalloc(vel)");
   float *dv = ctx->d_vel.as<float>();
   CU(cudaMemsetAsync(dv, 0, size_t(3 * n) * 4, s), "zero dv");
@@ -1258,6 +1269,7 @@ hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *para
     cfg.ppc = p->ppc;
     cfg.nd = int32_t(std::min<int64_t>(p->nd, INT32_MAX));
     cfg.tdpts = p->tdpts;
+    cfg.group = ctx->tune.group;
     cudaError_t e = B.tree.build(cfg, n, B.pos4.as<float4>(), kJSplit, s);
     if (e != cudaSuccess) {
       if (B.tree.error()) return ctx->fail(HSR_ERR_UNSUPPORTED, B.tree.error());
@@ -1317,7 +1329,7 @@ hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *para
   CU(cudaMemsetAsync(ctx->d_queue.p, 0, 2 * sizeof(unsigned long long), s), "reset queue");
   if (ctx->batched_ctas == 0) ctx->batched_ctas = hsr::batched_resident_ctas(ctx->device);
   CU(cudaEventRecord(ctx->ev0, s), "event");
-  CU(hsr::launch_pairs_batched_multi(params[0].law, ctx->d_box_desc.as<hsr::BoxDesc>(), items,
+  CU(hsr::launch_pairs_batched_multi(params[0].law, ctx->tune.group, ctx->d_box_desc.as<hsr::BoxDesc>(), items,
                                      total_items, ctx->d_queue.as<unsigned long long>(),
                                      ctx->batched_ctas, s),
      "multi-box pair kernel");
@@ -1357,6 +1369,7 @@ hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *para
   ctx->batch_n = nbox;
   ctx->batch_items = total_items;
   ctx->batch_law = params[0].law;
+  ctx->batch_group = ctx->tune.group;
   return HSR_OK;
 }
 
@@ -1381,7 +1394,7 @@ hsr_status hsr_build_lists(const hsr_params *p, int64_t n, float *x, float *y, f
             sd.data(), &list_begin);
   std::vector<int32_t> gidx;
   std::vector<hsr::PairItem> items;
-  make_items(*L->host, list_begin, kJSplit, gidx, items);
+  make_items(*L->host, list_begin, kJSplit, 32, gidx, items);
   L->st.work_items = int64_t(items.size());
   *out = L;
   return HSR_OK;
@@ -1504,6 +1517,95 @@ hsr_status hsr_bench_pairs_graph(hsr_ctx *ctx, int32_t iters, int32_t flush_l2,
   cudaGraphExecDestroy(exec);
   CU(e, "graph replay");
   *ms_per_launch = total / iters;
+  return HSR_OK;
+}
+
+hsr_status hsr_set_tune(hsr_ctx *ctx, const hsr_tune *t) {
+  if (!ctx || !t) return HSR_ERR_ARG;
+  if (t->kernel != HSR_KERNEL_PLAIN && t->kernel != HSR_KERNEL_BATCHED)
+    return ctx->fail(HSR_ERR_ARG, "tune.kernel must be HSR_KERNEL_PLAIN or HSR_KERNEL_BATCHED");
+  if (t->leaf_threads != 32 && t->leaf_threads != 64 && t->leaf_threads != 128)
+    return ctx->fail(HSR_ERR_ARG, "tune.leaf_threads must be 32, 64 or 128");
+  if (t->group != 16 && t->group != 32) return ctx->fail(HSR_ERR_ARG, "tune.group must be 16 or 32");
+  ctx->tune = *t;
+  ctx->tune.reserved = 0;
+  return HSR_OK;
+}
+
+hsr_status hsr_get_tune(const hsr_ctx *ctx, hsr_tune *t) {
+  if (!ctx || !t) return HSR_ERR_ARG;
+  *t = ctx->tune;
+  return HSR_OK;
+}
+
+hsr_status hsr_autotune(hsr_ctx *ctx, int32_t iters, int32_t flush_l2, hsr_tune_row *rows,
+                        int32_t cap, int32_t *nrows) {
+  if (!ctx || iters < 1 || cap < 0 || (cap > 0 && !rows)) return HSR_ERR_ARG;
+  if (!ctx->have_lists || !ctx->work.device_built || ctx->last_was_batch)
+    return ctx->fail(HSR_ERR_STATE, "autotune replays the last single-box kick built on the device");
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  Work &w = ctx->work;
+  const int saved_kernel = w.kernel, saved_threads = w.leaf_threads, saved_group = w.group;
+  std::vector<hsr_tune_row> table;
+  auto time_shape = [&](const hsr_tune &t) -> hsr_status {
+    w.kernel = t.kernel;
+    w.leaf_threads = t.leaf_threads;
+    w.group = t.group;
+    double warm = 0, ms = 0;
+    if (hsr_status r = hsr_bench_pairs(ctx, t.kernel, 1, flush_l2, &warm)) return r;
+    if (hsr_status r = hsr_bench_pairs(ctx, t.kernel, iters, flush_l2, &ms)) return r;
+    int64_t ev = ctx->tree.padded_pairs();
+    if (t.kernel == HSR_KERNEL_BATCHED) {
+      unsigned long long c[2] = {0, 0};
+      CU(cudaMemcpy(c, ctx->d_queue.p, sizeof(c), cudaMemcpyDeviceToHost), "D2H counters");
+      ev = int64_t(c[1]);
+    }
+    table.push_back(hsr_tune_row{t, ms, ev});
+    return HSR_OK;
+  };
+  hsr_status r = HSR_OK;
+  for (int nt : {32, 64, 128})
+    if (r == HSR_OK) r = time_shape(hsr_tune{HSR_KERNEL_PLAIN, nt, saved_group, 0});
+  for (int g : {16, 32}) {
+    if (r != HSR_OK) break;
+    if (ctx->tree.regroup(g, kJSplit, ctx->stream) != cudaSuccess) {
+      r = ctx->fail(HSR_ERR_CUDA, "regroup");
+      break;
+    }
+    w.items = ctx->tree.items();
+    w.gidx = ctx->tree.gidx();
+    w.nitems = ctx->tree.info().items;
+    r = time_shape(hsr_tune{HSR_KERNEL_BATCHED, saved_threads, g, 0});
+  }
+  if (r != HSR_OK) {
+    w.kernel = saved_kernel;
+    w.leaf_threads = saved_threads;
+    w.group = saved_group;
+    return r;
+  }
+  // the context takes the fastest shape
+  size_t best = 0;
+  for (size_t i = 1; i < table.size(); ++i)
+    if (table[i].ms < table[best].ms) best = i;
+  hsr_tune t = table[best].tune;
+  // each family keeps its own best shape for explicit kernel requests
+  double bp = 1e300, bb = 1e300;
+  for (const auto &row : table) {
+    if (row.tune.kernel == HSR_KERNEL_PLAIN && row.ms < bp) bp = row.ms, t.leaf_threads = row.tune.leaf_threads;
+    if (row.tune.kernel == HSR_KERNEL_BATCHED && row.ms < bb) bb = row.ms, t.group = row.tune.group;
+  }
+  ctx->tune = t;
+  if (ctx->tree.regroup(t.group, kJSplit, ctx->stream) != cudaSuccess)
+    return ctx->fail(HSR_ERR_CUDA, "regroup");
+  w.items = ctx->tree.items();
+  w.gidx = ctx->tree.gidx();
+  w.nitems = ctx->tree.info().items;
+  w.kernel = t.kernel;
+  w.leaf_threads = t.leaf_threads;
+  w.group = t.group;
+  const int32_t nr = int32_t(table.size());
+  for (int32_t i = 0; i < std::min(nr, cap); ++i) rows[i] = table[size_t(i)];
+  if (nrows) *nrows = nr;
   return HSR_OK;
 }
 

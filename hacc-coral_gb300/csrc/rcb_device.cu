@@ -863,18 +863,18 @@ __device__ __forceinline__ float o2f(uint32_t o) {
   return __uint_as_float((o & 0x80000000u) ? (o & 0x7fffffffu) : ~o);
 }
 
-// Splits each processed leaf into groups of 32 (the last one shorter) by
-// recursive median splits along the longest axis, left parts a multiple of
-// 32: the particles of a group are close, so the batched kernel's box test
+// Splits each processed leaf into groups of G particles (the last one
+// shorter) by recursive median splits along the longest axis, left parts a
+// multiple of G: the particles of a group are close, so the batched kernel's box test
 // keeps few list entries.  Every level sorts all segments of the leaf at once
 // by (segment, coordinate along the segment's longest axis).
 __global__ void __launch_bounds__(kGroupThreads)
     k_groups(const DNode *nodes, const int32_t *leaf_ids, int64_t nleaves,
-             const float4 *__restrict__ pos, int32_t *gidx) {
+             const float4 *__restrict__ pos, int32_t *gidx, int G) {
   __shared__ uint64_t key[kGroupSort];
   __shared__ int32_t val[kGroupSort];
-  __shared__ int32_t seg_a[kGroupSort / 32 + 1], seg_c[kGroupSort / 32 + 1];
-  __shared__ uint32_t seg_lo[3][kGroupSort / 32 + 1], seg_hi[3][kGroupSort / 32 + 1];
+  __shared__ int32_t seg_a[kGroupSort / 16 + 1], seg_c[kGroupSort / 16 + 1];
+  __shared__ uint32_t seg_lo[3][kGroupSort / 16 + 1], seg_hi[3][kGroupSort / 16 + 1];
   __shared__ int nseg_s, more_s;
   const int64_t li = blockIdx.x;
   if (li >= nleaves) return;
@@ -906,7 +906,7 @@ __global__ void __launch_bounds__(kGroupThreads)
     for (int i = threadIdx.x; i < c; i += blockDim.x) {
       int q = 0;
       while (q + 1 < nseg && seg_a[q + 1] <= i) ++q;
-      if (seg_c[q] <= 32) continue;
+      if (seg_c[q] <= G) continue;
       const float4 p = pos[val[i]];
       const uint32_t o[3] = {f2o(p.x), f2o(p.y), f2o(p.z)};
       for (int d = 0; d < 3; ++d) {
@@ -922,7 +922,7 @@ __global__ void __launch_bounds__(kGroupThreads)
         int q = 0;
         while (q + 1 < nseg && seg_a[q + 1] <= i) ++q;
         uint32_t ko = 0;
-        if (seg_c[q] > 32) {
+        if (seg_c[q] > G) {
           float ext[3];
           for (int d = 0; d < 3; ++d) ext[d] = o2f(seg_hi[d][q]) - o2f(seg_lo[d][q]);
           const int ax = (ext[0] >= ext[1] && ext[0] >= ext[2]) ? 0 : (ext[1] >= ext[2] ? 1 : 2);
@@ -954,24 +954,24 @@ __global__ void __launch_bounds__(kGroupThreads)
         }
         __syncthreads();
       }
-    // split every segment above 32 at 32 * ceil(groups / 2)
+    // split every segment above G at G * ceil(groups / 2)
     if (threadIdx.x == 0) {
       int n2 = 0;
-      int32_t na[kGroupSort / 32 + 1], nc[kGroupSort / 32 + 1];
+      int32_t na[kGroupSort / 16 + 1], nc[kGroupSort / 16 + 1];
       int more = 0;
       for (int q = 0; q < nseg; ++q) {
         const int32_t a0 = seg_a[q], c0 = seg_c[q];
-        if (c0 <= 32) {
+        if (c0 <= G) {
           na[n2] = a0;
           nc[n2++] = c0;
           continue;
         }
-        const int32_t ng = (c0 + 31) / 32, left = 32 * ((ng + 1) / 2);
+        const int32_t ng = (c0 + G - 1) / G, left = G * ((ng + 1) / 2);
         na[n2] = a0;
         nc[n2++] = left;
         na[n2] = a0 + left;
         nc[n2++] = c0 - left;
-        more |= left > 32 || c0 - left > 32;
+        more |= left > G || c0 - left > G;
       }
       for (int q = 0; q < n2; ++q) {
         seg_a[q] = na[q];
@@ -992,13 +992,13 @@ __device__ __forceinline__ int len_bucket(int64_t len) {
   return 31 - min(31, b);
 }
 
-__global__ void k_item_hist(const LeafDesc *ld, int64_t nleaves, int64_t jsplit,
+__global__ void k_item_hist(const LeafDesc *ld, int64_t nleaves, int64_t jsplit, int G,
                             int64_t *counters) {
   const int64_t li = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (li >= nleaves) return;
   const LeafDesc &L = ld[li];
   const int64_t nch = max64(1, (L.list_len + jsplit - 1) / jsplit);
-  const int64_t items = int64_t((L.count + 31) / 32) * nch;
+  const int64_t items = int64_t((L.count + G - 1) / G) * nch;
   atomicAdd((unsigned long long *)&counters[C_BUCKET + len_bucket(min64(L.list_len, jsplit))],
             (unsigned long long)items);
 }
@@ -1013,13 +1013,13 @@ __global__ void k_item_bases(int64_t *counters) {
   counters[C_NITEMS] = run;
 }
 
-__global__ void k_item_fill(const LeafDesc *ld, int64_t nleaves, int64_t jsplit, int64_t *counters,
-                            PairItem *items) {
+__global__ void k_item_fill(const LeafDesc *ld, int64_t nleaves, int64_t jsplit, int G,
+                            int64_t *counters, PairItem *items) {
   const int64_t li = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (li >= nleaves) return;
   const LeafDesc &L = ld[li];
   const int64_t nch = max64(1, (L.list_len + jsplit - 1) / jsplit);
-  const int32_t ng = (L.count + 31) / 32;
+  const int32_t ng = (L.count + G - 1) / G;
   const int64_t items_n = int64_t(ng) * nch;
   if (items_n == 0) return;
   const int b = len_bucket(min64(L.list_len, jsplit));
@@ -1030,8 +1030,8 @@ __global__ void k_item_fill(const LeafDesc *ld, int64_t nleaves, int64_t jsplit,
       PairItem it{};
       it.j_begin = L.list_begin + c * jsplit;
       it.j_len = int32_t(min64(jsplit, L.list_len - c * jsplit));
-      it.g_begin = L.offset + 32 * g;
-      it.g_count = min(32, L.count - 32 * g);
+      it.g_begin = L.offset + G * g;
+      it.g_count = min(G, L.count - G * g);
       it.flags = nch > 1 ? 1 : 0;
       items[at++] = it;
     }
@@ -1208,6 +1208,7 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     DT_CHECK(cudaMemcpyToSymbolAsync(c_design, d, sizeof(d), 0, cudaMemcpyHostToDevice, s));
   }
   const size_t nn = size_t(std::max<int64_t>(n, 1));
+  n_ = n;
   DT_CHECK(grow(epos_, cap_e_, nn, s));
   DT_CHECK(grow(tpos_, cap_t_, nn, s));
   DT_CHECK(grow(oid_, cap_o_, nn, s));
@@ -1366,10 +1367,27 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   DT_CHECK(cudaGetLastError());
 
   // ---- groups and work items ----
-  DT_CHECK(grow(gidx_, cap_gidx_, nn, s));
+  group_ = cfg.group == 16 ? 16 : 32;
+  DT_CHECK(make_items(n, jsplit, s));
+  lists_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
+  return cudaSuccess;
+}
+
+cudaError_t DeviceTree::regroup(int group, int64_t jsplit, cudaStream_t s) {
+  if (group != 16 && group != 32) return cudaErrorInvalidValue;
+  group_ = group;
+  return make_items(n_, jsplit, s);
+}
+
+cudaError_t DeviceTree::make_items(int64_t n, int64_t jsplit, cudaStream_t s) {
+  const int64_t nleaves = info_.processed_leaves;
+  const int G = group_;
+  DT_CHECK(grow(gidx_, cap_gidx_, size_t(std::max<int64_t>(n, 1)), s));
+  DT_CHECK(cudaMemsetAsync(counters_ + C_BUCKET, 0, 32 * sizeof(int64_t), s));
   if (nleaves > 0) {
-    k_groups<<<unsigned(nleaves), kGroupThreads, 0, s>>>(nodes_, leaf_ids_, nleaves, epos_, gidx_);
-    k_item_hist<<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(leafdesc_, nleaves, jsplit, counters_);
+    k_groups<<<unsigned(nleaves), kGroupThreads, 0, s>>>(nodes_, leaf_ids_, nleaves, epos_, gidx_, G);
+    k_item_hist<<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(leafdesc_, nleaves, jsplit, G,
+                                                                counters_);
     k_item_bases<<<1, 32, 0, s>>>(counters_);
   }
   DT_CHECK(cudaGetLastError());
@@ -1381,11 +1399,10 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   padded_pairs_ = h_counters_[C_PADDED];
   DT_CHECK(grow(items_, cap_items_, size_t(std::max<int64_t>(nitems, 1)), s));
   if (nitems > 0)
-    k_item_fill<<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(leafdesc_, nleaves, jsplit, counters_,
-                                                               items_);
+    k_item_fill<<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(leafdesc_, nleaves, jsplit, G,
+                                                               counters_, items_);
   DT_CHECK(cudaGetLastError());
   DT_CHECK(cudaStreamSynchronize(s));
-  lists_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
   return cudaSuccess;
 }
 

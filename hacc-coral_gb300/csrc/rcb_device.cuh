@@ -44,6 +44,7 @@ struct TreeConfig {
   float fsrrmax, tan_oa, ppc;
   int32_t nd, tdpts;
   int32_t force_cm_fallback;  // test hook: every node takes the sequential sum
+  int32_t group;              // particles per work-item group: 16 or 32 (0 = 32)
 };
 
 // Result sizes of a device build.
@@ -70,6 +71,11 @@ class DeviceTree {
   cudaError_t build(const TreeConfig &cfg, int64_t n, const float4 *pos_in, int64_t jsplit,
                     cudaStream_t s);
 
+  // Rebuilds the groups and work items of the last build for another group
+  // size (16 or 32); the tree and the lists stay.
+  cudaError_t regroup(int group, int64_t jsplit, cudaStream_t s);
+  int group() const { return group_; }
+
   const DeviceTreeInfo &info() const { return info_; }
   const int32_t *perm() const { return oid_; }
   const float4 *table() const { return table_; }
@@ -93,12 +99,15 @@ class DeviceTree {
  private:
   template <typename T>
   cudaError_t grow(T *&p, size_t &cap, size_t count, cudaStream_t s, bool keep = false);
+  cudaError_t make_items(int64_t n, int64_t jsplit, cudaStream_t s);
 
   DeviceTreeInfo info_{};
   int64_t padded_pairs_ = 0;
   double build_ms_ = 0, lists_ms_ = 0;
   std::vector<int32_t> levels_;
   const char *err_ = nullptr;
+  int group_ = 32;
+  int64_t n_ = 0;
   // elements: current and scratch (x, y, z, m) + input index
   float4 *epos_ = nullptr, *tpos_ = nullptr;
   int32_t *oid_ = nullptr, *toid_ = nullptr, *idx_ = nullptr;

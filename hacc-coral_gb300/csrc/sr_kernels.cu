@@ -107,35 +107,62 @@ __global__ void __launch_bounds__(NT)
   }
 }
 
-cudaError_t launch_leaf_plain(int law, const float4 *pos, const LeafDesc *leaves, int64_t nleaves,
-                              const int32_t *idx, float *vx, float *vy, float *vz, float fcoeff,
-                              float rsm2, float rcut2, cudaStream_t s) {
-  if (nleaves <= 0) return cudaSuccess;
-  constexpr int NT = 128;
+namespace {
+template <int NT>
+void leaf_plain_nt(int law, unsigned nl, cudaStream_t s, const float4 *pos, const LeafDesc *leaves,
+                   const int32_t *idx, float *vx, float *vy, float *vz, float fcoeff, float rsm2,
+                   float rcut2) {
   if (law == LAW_POLY5_STEP16)
-    k_leaf_plain<LAW_POLY5_STEP16, NT><<<unsigned(nleaves), NT, 0, s>>>(pos, leaves, idx, vx, vy, vz,
-                                                                        fcoeff, rsm2, rcut2);
+    k_leaf_plain<LAW_POLY5_STEP16, NT><<<nl, NT, 0, s>>>(pos, leaves, idx, vx, vy, vz, fcoeff,
+                                                         rsm2, rcut2);
   else
-    k_leaf_plain<LAW_POLY6, NT><<<unsigned(nleaves), NT, 0, s>>>(pos, leaves, idx, vx, vy, vz,
-                                                                 fcoeff, rsm2, rcut2);
+    k_leaf_plain<LAW_POLY6, NT><<<nl, NT, 0, s>>>(pos, leaves, idx, vx, vy, vz, fcoeff, rsm2,
+                                                  rcut2);
+}
+}  // namespace
+
+cudaError_t launch_leaf_plain(int law, int threads, const float4 *pos, const LeafDesc *leaves,
+                              int64_t nleaves, const int32_t *idx, float *vx, float *vy, float *vz,
+                              float fcoeff, float rsm2, float rcut2, cudaStream_t s) {
+  if (nleaves <= 0) return cudaSuccess;
+  const unsigned nl = unsigned(nleaves);
+  switch (threads) {
+    case 32:
+      leaf_plain_nt<32>(law, nl, s, pos, leaves, idx, vx, vy, vz, fcoeff, rsm2, rcut2);
+      break;
+    case 64:
+      leaf_plain_nt<64>(law, nl, s, pos, leaves, idx, vx, vy, vz, fcoeff, rsm2, rcut2);
+      break;
+    case 128:
+      leaf_plain_nt<128>(law, nl, s, pos, leaves, idx, vx, vy, vz, fcoeff, rsm2, rcut2);
+      break;
+    default:
+      return cudaErrorInvalidValue;
+  }
   return cudaGetLastError();
 }
 
 // ---------------------------------------------------------------------------
 // Batched persistent kernel.  Every warp works alone: it takes the next item
 // from the queue (items are sorted by cost, largest first), loads its group's
-// particles (one per lane) and the group's bounding box, then streams the
-// item's list range 32 entries at a time.  Each lane gathers one entry and
-// tests it against the box; the warp ballots, and only entries within the
-// cutoff of the box are evaluated, broadcast from the warp's shared-memory
-// slot.  The skipped entries are farther than fsrrmax from every particle of
+// particles and the group's bounding box, then streams the item's list range
+// 32 entries at a time.  Each lane gathers one entry and tests it against the
+// box; the warp ballots, and the kept entries are compacted into the warp's
+// shared-memory buffer and evaluated 32 at a time from there (a broadcast
+// read).  The skipped entries are farther than fsrrmax from every particle of
 // the group (the test uses a bound slightly above fsrrmax^2), so the
 // reference's mask gives them an exactly zero contribution: the result is the
 // full list's, up to FP32 summation order.
+//
+// G is the group size.  G = 32: one particle per lane, every lane on the same
+// entry.  G = 16: the two half-warps hold the same 16 particles and take the
+// even and odd entries of the buffer, and their sums are added at the end, so
+// a group of 16 keeps the whole warp busy: smaller groups keep fewer entries
+// and leave fewer lanes idle in a leaf's last group.
 // ---------------------------------------------------------------------------
 constexpr int kBatchedWarps = 8;
 
-template <int LAW, bool MULTI>
+template <int LAW, bool MULTI, int G>
 __global__ void __launch_bounds__(32 * kBatchedWarps, 5)
     k_pairs_batched(const float4 *__restrict__ pos_, const PairItem *__restrict__ items,
                     int64_t nitems, const int32_t *__restrict__ gidx_,
@@ -143,11 +170,15 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 5)
                     float *__restrict__ vy_, float *__restrict__ vz_, float fcoeff_, LawS law_,
                     float rcull2_, unsigned long long *__restrict__ queue,
                     const BoxDesc *__restrict__ boxes) {
-  // kept entries of the current item, compacted; full batches of 32 are
-  // evaluated in one unrolled loop
-  __shared__ float4 buf[kBatchedWarps][64];
+  static_assert(G == 16 || G == 32, "group size");
+  constexpr bool kDrop = LAW == LAW_POLY5_STEP16;
+  // kept entries of the current item, compacted; one slot past 63 holds the
+  // padding entry of an odd tail (G = 16)
+  __shared__ float4 buf[kBatchedWarps][65];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
+  const int gl = G == 16 ? (lane & 15) : lane;  // particle of the group
+  const int half = G == 16 ? (lane >> 4) : 0;   // even or odd entries
   const unsigned full = 0xffffffffu;
   const unsigned below = (1u << lane) - 1u;
   unsigned long long evaluated = 0;  // (particle, entry) pairs this warp evaluated
@@ -174,13 +205,13 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 5)
       rcull2 = B.rcull2;
       L = B.law;
     }
-    const bool act = lane < W.g_count;
-    const int pi = gidx[W.g_begin + (act ? lane : 0)];
+    const bool act = gl < W.g_count;
+    const int pi = gidx[W.g_begin + (act ? gl : 0)];
     const float4 P = pos[pi];
-    // group bounding box (inactive lanes repeat lane 0's particle)
+    // group bounding box (inactive lanes repeat the first particle)
     float lox = P.x, hix = P.x, loy = P.y, hiy = P.y, loz = P.z, hiz = P.z;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
+    for (int o = G / 2; o > 0; o >>= 1) {
       lox = fminf(lox, __shfl_xor_sync(full, lox, o));
       hix = fmaxf(hix, __shfl_xor_sync(full, hix, o));
       loy = fminf(loy, __shfl_xor_sync(full, loy, o));
@@ -190,12 +221,25 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 5)
     }
     float ax = 0.f, ay = 0.f, az = 0.f;
     const int32_t *lst = idx + W.j_begin;
+    const int len = W.j_len;
     int nbuf = 0;  // warp-uniform
     unsigned kept = 0;
-    for (int j0 = 0; j0 < W.j_len; j0 += 32) {
-      const int j = j0 + lane;
-      const bool ok = j < W.j_len;
-      const float4 J = pos[lst[ok ? j : 0]];
+    // software pipeline: the entry of the next iteration and the index of the
+    // one after it are in flight while this iteration tests and evaluates
+    float4 Jn = make_float4(0.f, 0.f, 0.f, 0.f);
+    int32_t in2 = 0;
+    if (len > 0) {
+      Jn = pos[lst[lane < len ? lane : 0]];
+      in2 = lst[32 + lane < len ? 32 + lane : 0];
+    }
+    for (int j0 = 0; j0 < len; j0 += 32) {
+      const bool ok = j0 + lane < len;
+      const float4 J = Jn;
+      if (j0 + 32 < len) {
+        Jn = pos[in2];
+        const int j2 = j0 + 64 + lane;
+        in2 = lst[j2 < len ? j2 : 0];
+      }
       const float dx = fmaxf(fmaxf(lox - J.x, J.x - hix), 0.f);
       const float dy = fmaxf(fmaxf(loy - J.y, J.y - hiy), 0.f);
       const float dz = fmaxf(fmaxf(loz - J.z, J.z - hiz), 0.f);
@@ -207,19 +251,31 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 5)
       if (nbuf >= 32) {
         __syncwarp();
 #pragma unroll 8
-        for (int q = 0; q < 32; ++q) pair_acc_s<LAW == LAW_POLY5_STEP16>(P.x, P.y, P.z, buf[w][q], L, ax, ay, az);
+        for (int q = 0; q < 32 / (32 / G); ++q)
+          pair_acc_s<kDrop>(P.x, P.y, P.z, buf[w][(32 / G) * q + half], L, ax, ay, az);
         __syncwarp();
         if (lane < nbuf - 32) buf[w][lane] = buf[w][32 + lane];
         nbuf -= 32;
         __syncwarp();
       }
     }
+    if (G == 16 && (nbuf & 1)) {
+      // far-away massless padding: outside the cutoff, so its weight is 0
+      if (lane == 0) buf[w][nbuf] = make_float4(1e18f, 1e18f, 1e18f, 0.f);
+      ++nbuf;
+    }
     __syncwarp();
-    for (int q = 0; q < nbuf; ++q) pair_acc_s<LAW == LAW_POLY5_STEP16>(P.x, P.y, P.z, buf[w][q], L, ax, ay, az);
+    for (int q = 0; q < nbuf / (32 / G); ++q)
+      pair_acc_s<kDrop>(P.x, P.y, P.z, buf[w][(32 / G) * q + half], L, ax, ay, az);
     __syncwarp();
+    if (G == 16) {
+      ax += __shfl_xor_sync(full, ax, 16);
+      ay += __shfl_xor_sync(full, ay, 16);
+      az += __shfl_xor_sync(full, az, 16);
+    }
     evaluated += (unsigned long long)kept * (unsigned long long)W.g_count;
-    if (act) {
-      const float c = (LAW == LAW_POLY5_STEP16) ? fcoeff : fcoeff * P.w;
+    if (act && half == 0) {
+      const float c = kDrop ? fcoeff : fcoeff * P.w;
       if (W.flags & 1) {
         atomicAdd(vx + pi, c * ax);
         atomicAdd(vy + pi, c * ay);
@@ -237,54 +293,67 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 5)
 int batched_resident_ctas(int device) {
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pairs_batched<LAW_POLY6, false>,
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_pairs_batched<LAW_POLY6, false, 32>,
                                                 32 * kBatchedWarps, 0);
   return std::max(1, sms) * std::max(1, per);
 }
 
-cudaError_t launch_pairs_batched(int law, const float4 *pos, const PairItem *items, int64_t nitems,
-                                 const int32_t *gidx, const int32_t *idx, float *vx, float *vy,
-                                 float *vz, float fcoeff, float rsm2, float rcut2, float rcull2,
-                                 unsigned long long *queue, int ctas, cudaStream_t s) {
-  if (nitems <= 0) return cudaSuccess;
-  if (ctas <= 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    ctas = batched_resident_ctas(dev);
-  }
-  const int64_t need = (nitems + kBatchedWarps - 1) / kBatchedWarps;
-  if (ctas > need) ctas = int(need);
-  const LawS L = make_law_s(law, rsm2, rcut2);
-  if (law == LAW_POLY5_STEP16)
-    k_pairs_batched<LAW_POLY5_STEP16, false><<<ctas, 32 * kBatchedWarps, 0, s>>>(
-        pos, items, nitems, gidx, idx, vx, vy, vz, fcoeff, L, rcull2, queue, nullptr);
+namespace {
+template <int LAW, bool MULTI>
+cudaError_t batched_group(int group, int ctas, cudaStream_t s, const float4 *pos,
+                          const PairItem *items, int64_t nitems, const int32_t *gidx,
+                          const int32_t *idx, float *vx, float *vy, float *vz, float fcoeff,
+                          const LawS &L, float rcull2, unsigned long long *queue,
+                          const BoxDesc *boxes) {
+  if (group == 16)
+    k_pairs_batched<LAW, MULTI, 16><<<ctas, 32 * kBatchedWarps, 0, s>>>(
+        pos, items, nitems, gidx, idx, vx, vy, vz, fcoeff, L, rcull2, queue, boxes);
+  else if (group == 32)
+    k_pairs_batched<LAW, MULTI, 32><<<ctas, 32 * kBatchedWarps, 0, s>>>(
+        pos, items, nitems, gidx, idx, vx, vy, vz, fcoeff, L, rcull2, queue, boxes);
   else
-    k_pairs_batched<LAW_POLY6, false><<<ctas, 32 * kBatchedWarps, 0, s>>>(
-        pos, items, nitems, gidx, idx, vx, vy, vz, fcoeff, L, rcull2, queue, nullptr);
+    return cudaErrorInvalidValue;
   return cudaGetLastError();
 }
 
-cudaError_t launch_pairs_batched_multi(int law, const BoxDesc *boxes, const PairItem *items,
-                                       int64_t nitems, unsigned long long *queue, int ctas,
-                                       cudaStream_t s) {
-  if (nitems <= 0) return cudaSuccess;
+int clamp_ctas(int ctas, int64_t nitems) {
   if (ctas <= 0) {
     int dev = 0;
     cudaGetDevice(&dev);
     ctas = batched_resident_ctas(dev);
   }
   const int64_t need = (nitems + kBatchedWarps - 1) / kBatchedWarps;
-  if (ctas > need) ctas = int(need);
+  return ctas > need ? int(need) : ctas;
+}
+}  // namespace
+
+cudaError_t launch_pairs_batched(int law, int group, const float4 *pos, const PairItem *items,
+                                 int64_t nitems, const int32_t *gidx, const int32_t *idx,
+                                 float *vx, float *vy, float *vz, float fcoeff, float rsm2,
+                                 float rcut2, float rcull2, unsigned long long *queue, int ctas,
+                                 cudaStream_t s) {
+  if (nitems <= 0) return cudaSuccess;
+  ctas = clamp_ctas(ctas, nitems);
+  const LawS L = make_law_s(law, rsm2, rcut2);
+  if (law == LAW_POLY5_STEP16)
+    return batched_group<LAW_POLY5_STEP16, false>(group, ctas, s, pos, items, nitems, gidx, idx,
+                                                  vx, vy, vz, fcoeff, L, rcull2, queue, nullptr);
+  return batched_group<LAW_POLY6, false>(group, ctas, s, pos, items, nitems, gidx, idx, vx, vy,
+                                         vz, fcoeff, L, rcull2, queue, nullptr);
+}
+
+cudaError_t launch_pairs_batched_multi(int law, int group, const BoxDesc *boxes,
+                                       const PairItem *items, int64_t nitems,
+                                       unsigned long long *queue, int ctas, cudaStream_t s) {
+  if (nitems <= 0) return cudaSuccess;
+  ctas = clamp_ctas(ctas, nitems);
   const LawS L{};
   if (law == LAW_POLY5_STEP16)
-    k_pairs_batched<LAW_POLY5_STEP16, true><<<ctas, 32 * kBatchedWarps, 0, s>>>(
-        nullptr, items, nitems, nullptr, nullptr, nullptr, nullptr, nullptr, 0.f, L, 0.f, queue,
-        boxes);
-  else
-    k_pairs_batched<LAW_POLY6, true><<<ctas, 32 * kBatchedWarps, 0, s>>>(
-        nullptr, items, nitems, nullptr, nullptr, nullptr, nullptr, nullptr, 0.f, L, 0.f, queue,
-        boxes);
-  return cudaGetLastError();
+    return batched_group<LAW_POLY5_STEP16, true>(group, ctas, s, nullptr, items, nitems, nullptr,
+                                                 nullptr, nullptr, nullptr, nullptr, 0.f, L, 0.f,
+                                                 queue, boxes);
+  return batched_group<LAW_POLY6, true>(group, ctas, s, nullptr, items, nitems, nullptr, nullptr,
+                                        nullptr, nullptr, nullptr, 0.f, L, 0.f, queue, boxes);
 }
 
 __global__ void k_tag_items(const PairItem *in, PairItem *out, int64_t n, int box) {

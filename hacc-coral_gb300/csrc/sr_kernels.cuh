@@ -199,22 +199,25 @@ __device__ __forceinline__ void pair_acc(float xi, float yi, float zi, const flo
 // the launch status.
 cudaError_t launch_expand_segments(const SegDesc *segs, int64_t nsegs, int32_t *idx,
                                    cudaStream_t s);
-cudaError_t launch_leaf_plain(int law, const float4 *pos, const LeafDesc *leaves, int64_t nleaves,
-                              const int32_t *idx, float *vx, float *vy, float *vz, float fcoeff,
-                              float rsm2, float rcut2, cudaStream_t s);
+// threads: CTA size, i.e. threads per leaf (32, 64 or 128).
+cudaError_t launch_leaf_plain(int law, int threads, const float4 *pos, const LeafDesc *leaves,
+                              int64_t nleaves, const int32_t *idx, float *vx, float *vy, float *vz,
+                              float fcoeff, float rsm2, float rcut2, cudaStream_t s);
 cudaError_t launch_ffma_probe(float *out, int blocks, int threads, int iters, cudaStream_t s);
 // Persistent batched kernel: `ctas` CTAs (0 = size from occupancy) pull
 // items through the counter queue[0] (zero at launch); queue[1] receives the
 // number of (particle, entry) pairs actually evaluated after the box test.
-cudaError_t launch_pairs_batched(int law, const float4 *pos, const PairItem *items, int64_t nitems,
-                                 const int32_t *gidx, const int32_t *idx, float *vx, float *vy,
-                                 float *vz, float fcoeff, float rsm2, float rcut2, float rcull2,
-                                 unsigned long long *queue, int ctas, cudaStream_t s);
+// group: particles per group of the items (16 or 32).
+cudaError_t launch_pairs_batched(int law, int group, const float4 *pos, const PairItem *items,
+                                 int64_t nitems, const int32_t *gidx, const int32_t *idx,
+                                 float *vx, float *vy, float *vz, float fcoeff, float rsm2,
+                                 float rcut2, float rcull2, unsigned long long *queue, int ctas,
+                                 cudaStream_t s);
 // The batched kernel over the items of several boxes (items of box b carry
 // b << 8 in flags), one persistent launch; queue as above.
-cudaError_t launch_pairs_batched_multi(int law, const BoxDesc *boxes, const PairItem *items,
-                                       int64_t nitems, unsigned long long *queue, int ctas,
-                                       cudaStream_t s);
+cudaError_t launch_pairs_batched_multi(int law, int group, const BoxDesc *boxes,
+                                       const PairItem *items, int64_t nitems,
+                                       unsigned long long *queue, int ctas, cudaStream_t s);
 // Copies n items, tagging them with box b.
 cudaError_t launch_tag_items(const PairItem *in, PairItem *out, int64_t n, int box,
                              cudaStream_t s);

@@ -35,7 +35,7 @@ EXPORTS = ("hsr_create", "hsr_destroy", "hsr_last_error", "hsr_version", "hsr_rc
            "hsr_force_law", "hsr_bench_pairs", "hsr_probe_fp32_peak", "hsr_kick_lists_noalloc",
            "hsr_force_fwd", "hsr_force_vjp", "hsr_last_perm", "hsr_tree_size", "hsr_tree_export",
            "hsr_lists_export_index", "hsr_rcb_kick_batch", "hsr_bench_pairs_graph",
-           "hsr_subcycle")
+           "hsr_subcycle", "hsr_set_tune", "hsr_get_tune", "hsr_autotune")
 
 
 class HsrError(RuntimeError):
@@ -58,6 +58,19 @@ class HsrSubcycleParams(C.Structure):
     _fields_ = [("kick", HsrParams), ("nsub", C.c_int32), ("ng", C.c_int32 * 3),
                 ("alpha", C.c_float), ("pp", C.c_float), ("tau", C.c_float), ("adot", C.c_float),
                 ("skip_stream", C.c_int32), ("skip_kick", C.c_int32)]
+
+
+class HsrTune(C.Structure):
+    _fields_ = [("kernel", C.c_int32), ("leaf_threads", C.c_int32), ("group", C.c_int32),
+                ("reserved", C.c_int32)]
+
+    def as_dict(self):
+        return {"kernel": {KERNEL_PLAIN: "plain", KERNEL_BATCHED: "batched"}.get(self.kernel, self.kernel),
+                "leaf_threads": self.leaf_threads, "group": self.group}
+
+
+class HsrTuneRow(C.Structure):
+    _fields_ = [("tune", HsrTune), ("ms", C.c_double), ("evaluated_pairs", C.c_int64)]
 
 
 class HsrStats(C.Structure):
@@ -143,6 +156,12 @@ def load(path: str = LIB_PATH):
     lib.hsr_bench_pairs.argtypes = [vp, i32, i32, i32, C.POINTER(C.c_double)]
     lib.hsr_probe_fp32_peak.restype = i32
     lib.hsr_probe_fp32_peak.argtypes = [vp, C.POINTER(C.c_double)]
+    lib.hsr_set_tune.restype = i32
+    lib.hsr_set_tune.argtypes = [vp, C.POINTER(HsrTune)]
+    lib.hsr_get_tune.restype = i32
+    lib.hsr_get_tune.argtypes = [vp, C.POINTER(HsrTune)]
+    lib.hsr_autotune.restype = i32
+    lib.hsr_autotune.argtypes = [vp, i32, i32, C.POINTER(HsrTuneRow), i32, C.POINTER(C.c_int32)]
     _lib = lib
     return lib
 
@@ -330,6 +349,27 @@ class Context:
                                                 *[C.cast(t, C.c_void_p) for t in tables], MEM_HOST),
                     "hsr_rcb_kick_batch")
         return self.stats()
+
+    def set_tune(self, kernel: str = "batched", leaf_threads: int = 128, group: int = 32):
+        """Launch shape for HSR_KERNEL_AUTO kicks (hsr_set_tune)."""
+        k = {"plain": KERNEL_PLAIN, "batched": KERNEL_BATCHED}[kernel]
+        t = HsrTune(k, leaf_threads, group, 0)
+        self._check(self.lib.hsr_set_tune(self.h, C.byref(t)), "hsr_set_tune")
+
+    def get_tune(self) -> dict:
+        t = HsrTune()
+        self._check(self.lib.hsr_get_tune(self.h, C.byref(t)), "hsr_get_tune")
+        return t.as_dict()
+
+    def autotune(self, iters: int = 5, flush_l2: bool = True) -> list:
+        """Times every launch shape on the last device-built kick and keeps the
+        fastest (hsr_autotune); returns one dict per shape."""
+        rows = (HsrTuneRow * 16)()
+        nr = C.c_int32()
+        self._check(self.lib.hsr_autotune(self.h, iters, int(flush_l2), rows, 16, C.byref(nr)),
+                    "hsr_autotune")
+        return [dict(rows[i].tune.as_dict(), ms=rows[i].ms, evaluated_pairs=rows[i].evaluated_pairs)
+                for i in range(nr.value)]
 
     def fp32_peak_tflops(self) -> float:
         t = C.c_double()

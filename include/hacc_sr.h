@@ -63,7 +63,7 @@ enum { HSR_BUILD_DEVICE = 0, HSR_BUILD_HOST = 1 };
 /* Kernel variants for the pair evaluation (same results up to FP32
  * summation order). */
 enum {
-  HSR_KERNEL_AUTO = 0,      /* batched persistent kernel, autotuned shape      */
+  HSR_KERNEL_AUTO = 0,      /* the context's tuned kernel (batched by default) */
   HSR_KERNEL_PLAIN = 1,     /* one CTA per leaf, every list entry evaluated    */
   HSR_KERNEL_BATCHED = 2    /* persistent CTAs over a work queue of tiles       */
 };
@@ -180,6 +180,42 @@ hsr_status hsr_lists_get(const hsr_lists *L, int64_t *leaf_offset, int64_t *leaf
  * index), >= n a pseudo-particle. */
 hsr_status hsr_lists_index(const hsr_lists *L, int64_t *entry_index);
 hsr_status hsr_lists_free(hsr_lists *L);
+
+/* ---- launch shapes ------------------------------------------------------ */
+
+/* Launch shape of the pair kernels, held per context.  Kicks with
+ * HSR_KERNEL_AUTO run `kernel`; the plain kernel runs `leaf_threads` threads
+ * per leaf (32, 64 or 128); the batched kernel takes work items of `group`
+ * particles (16 or 32).  Defaults: HSR_KERNEL_BATCHED, 128, 32.  The shape
+ * changes the FP32 summation order only, never the pair set.  No counterpart in
+ * the reference (nbody1, src/halo_finder/RCBForceTree.cxx:575-620, is a plain
+ * loop with no launch shape). */
+typedef struct hsr_tune {
+  int32_t kernel;        /* HSR_KERNEL_PLAIN or HSR_KERNEL_BATCHED */
+  int32_t leaf_threads;  /* 32, 64, 128 */
+  int32_t group;         /* 16, 32 */
+  int32_t reserved;      /* 0 */
+} hsr_tune;
+
+typedef struct hsr_tune_row {
+  hsr_tune tune;
+  double ms;                /* mean device time of one pair-kernel launch */
+  int64_t evaluated_pairs;  /* pairs the launch evaluated */
+} hsr_tune_row;
+
+hsr_status hsr_set_tune(hsr_ctx *ctx, const hsr_tune *t);
+hsr_status hsr_get_tune(const hsr_ctx *ctx, hsr_tune *t);
+
+/* Times every shape (plain kernel with 32, 64 and 128 threads per leaf,
+ * batched kernel with groups of 16 and 32) on the tree and lists of the last
+ * single-box kick built on the device, `iters` launches each after one
+ * warm-up launch (L2 flushed before each when flush_l2 != 0), and sets the
+ * context's shape to the fastest.  The launches accumulate into the context's
+ * own velocity scratch, never into caller arrays.  Writes min(cap, *nrows)
+ * rows; *nrows receives the number of shapes timed.  HSR_ERR_STATE without
+ * such a kick. */
+hsr_status hsr_autotune(hsr_ctx *ctx, int32_t iters, int32_t flush_l2, hsr_tune_row *rows,
+                        int32_t cap, int32_t *nrows);
 
 /* ---- the sub-cycle around the kick ------------------------------------- */
 
