@@ -63,6 +63,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--multibox", type=int, default=8,
                     help="boxes of 96^3 in the multi-box line (0: skip)")
+    ap.add_argument("--clustered", type=int, default=256,
+                    help="side of the clustered set of the leaf size x shape sweep (0: skip)")
     ap.add_argument("--cpu-slab", type=float, default=0.25,
                     help="fraction of the force box (along x) in the CPU sample")
     return ap.parse_args()
@@ -309,6 +311,30 @@ def main():
                     "pairs_per_s": stb["pairs"] / (ms_b * 1e-3),
                     "e2e_s": wall_b, "e2e_pairs_per_s": stb["pairs"] / wall_b}
 
+    # ---- clustered set: leaf size x launch shape sweep ----
+    clustered = None
+    if args.clustered > 0:
+        import autotune
+        pc = synth.clustered_box(args.clustered)
+        t0 = time.perf_counter()
+        sw = autotune.sweep(ctx, pc, nds=(64, 128, 256), iters=2)
+        clustered = {"n_side": args.clustered, "n_particles": pc.n,
+                     "halos": pc.meta["nhalo"], "sweep_s": time.perf_counter() - t0,
+                     "best": sw["best"],
+                     "rows": [{"nd": r["nd"], "pairs": r["pairs"],
+                               "list_entries": r["list_entries"],
+                               "tree_build_ms": round(r["tree_build_ms"], 3),
+                               "lists_ms": round(r["lists_ms"], 3),
+                               "best_shape": r["best_shape"],
+                               "best_kernel_ms": round(r["best_kernel_ms"], 4),
+                               "pairs_per_s": r["pairs_per_s"],
+                               "shape_ms": {(f"{q['kernel']}-{q['leaf_threads']}"
+                                             if q["kernel"] == "plain"
+                                             else f"batched-g{q['group']}"): round(q["ms"], 4)
+                                            for q in r["shapes"]}}
+                              for r in sw["rows"]]}
+        del pc
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(p0, kp, args.cpu_slab, os.cpu_count() or 1)
@@ -330,6 +356,7 @@ def main():
                                  "speedup": ms_plain / ms},
             "adjoint": {"vjp_ms": vjp_ms, "vjp_pairs_per_s": pairs / (vjp_ms * 1e-3)},
             "multibox": multibox,
+            "clustered": clustered,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak if peak else None,
                          "traffic": profiled_traffic(cfg["workload"], cfg["shape"]),

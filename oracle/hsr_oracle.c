@@ -703,7 +703,17 @@ ora_result *ora_rcb_run(const ora_params *p, int64_t n, float *x, float *y, floa
   if (!R) { *err = ORA_ERR_NOMEM; return NULL; }
 #ifdef _OPENMP
   int nest = omp_get_max_active_levels();
-  omp_set_max_active_levels(64);
+  /* The reference nests a two-thread team per split (omp_set_nested(1),
+   * RCBForceTree.cxx:418-421), so a deep tree asks for ~2^depth threads at
+   * once.  ORA_MAX_ACTIVE_LEVELS caps the nesting for very large inputs
+   * (deeper splits then run in the calling thread); the results do not
+   * depend on it. */
+  int levels = 64;
+  {
+    const char *e = getenv("ORA_MAX_ACTIVE_LEVELS");
+    if (e && atoi(e) > 0) levels = atoi(e);
+  }
+  omp_set_max_active_levels(levels);
   if (p->nthreads > 0) omp_set_num_threads(p->nthreads);
 #endif
   R->tdpts = p->tdpts;
