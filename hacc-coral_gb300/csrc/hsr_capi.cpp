@@ -704,7 +704,7 @@ hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float
   cfg.group = ctx->tune.group;
   {
     const char *f = std::getenv("HSR_FORCE_CM_FALLBACK");  // test hook
-    cfg.force_cm_fallback = (f && f[0] == '1') ? 1 : 0;
+    cfg.force_cm_fallback = (f && (f[0] == '1' || f[0] == '2')) ? f[0] - '0' : 0;
   }
   CU(cudaEventRecord(ctx->ev3, s), "event");
   const auto tb = clk::now();
@@ -743,6 +743,7 @@ hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float
   w.idx = ctx->tree.index();
   w.items = ctx->tree.items();
   w.gidx = ctx->tree.gidx();
+  w.group = ctx->tree.group();
   w.vel = dv;
   w.nleaves = ti.processed_leaves;
   w.nitems = ti.items;
@@ -993,7 +994,7 @@ hsr_status hsr_force_fwd(hsr_ctx *ctx, const hsr_params *p, int64_t n, const flo
   cfg.ppc = p->ppc;
   cfg.nd = int32_t(std::min<int64_t>(p->nd, INT32_MAX));
   cfg.tdpts = p->tdpts;
-  cfg.group = ctx->tune.group;
+  cfg.group = 32;  // the adjoint kernel takes one particle per lane
   cudaError_t e = ctx->tree.build(cfg, n, pos4, kJSplit, s);
   if (e != cudaSuccess) {
     if (ctx->tree.error()) return ctx->fail(HSR_ERR_UNSUPPORTED, ctx->tree.error());
@@ -1010,6 +1011,7 @@ hsr_status hsr_force_fwd(hsr_ctx *ctx, const hsr_params *p, int64_t n, const flo
   w.idx = ctx->tree.index();
   w.items = ctx->tree.items();
   w.gidx = ctx->tree.gidx();
+  w.group = ctx->tree.group();
   w.vel = dv;
   w.nleaves = ti.processed_leaves;
   w.nitems = ti.items;

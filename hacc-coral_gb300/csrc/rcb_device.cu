@@ -47,8 +47,8 @@ constexpr int kPartDoubles = 16;    // per-chunk partial record
 constexpr int kWalkStack = 256;     // DFS stack of the list walk
 
 enum { C_NCHUNK = 0, C_NSPLIT = 1, C_NFALLBACK = 2, C_NLEAF = 3, C_NSEG = 4, C_NENT = 5,
-       C_PAIRS = 6, C_PADDED = 7, C_NITEMS = 8, C_MAXLEN = 9, C_BUCKET = 16, C_FILL = 48,
-       C_COUNT = 80 };
+       C_PAIRS = 6, C_PADDED = 7, C_NITEMS = 8, C_MAXLEN = 9, C_TDONE1 = 10, C_TDONE2 = 11,
+       C_NTIGHT = 12, C_BUCKET = 16, C_FILL = 48, C_COUNT = 80 };
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -330,8 +330,8 @@ __global__ void k_stats_final(DNode *nodes, int32_t nb, int32_t ne, const int64_
     if (emin[q] == INT_MIN || emin[q] < -1000) return false;
     return sabs < ldexp(1.0, 53 + emin[q]);
   };
-  const bool mexact = exact(3, s[7]);
-  bool ok = !force_fallback;
+  const bool mexact = exact(3, s[7]) && force_fallback == 0;
+  bool ok = force_fallback == 0;
   for (int d = 0; d < 3 && ok; ++d) {
     float v;
     if (mexact && exact(d, s[4 + d]) && s[3] != 0.0) N.xc[d] = __double2float_rn(__ddiv_rn(s[d], s[3]));
@@ -344,6 +344,286 @@ __global__ void k_stats_final(DNode *nodes, int32_t nb, int32_t ne, const int64_
   }
 }
 
+// ---------------------------------------------------------------------------
+// Tight certification of the centre of mass for the nodes the loose bound
+// could not decide (k_stats_final's fallback list, at most kTightNodes of
+// them per level).  The reference's sequential sum s_k = fl(s_{k-1} + t_k)
+// differs from the exact sum by sum_k d_k, where the rounding error d_k is
+// zero when s_{k-1} and t_k are both multiples of ulp(s_k) (then the exact
+// sum is representable), and |d_k| <= ulp(s_k) / 2 otherwise.  ulp(s_k) is
+// bounded from the exact prefix sums P_k: |s_k - P_k| is below the loose
+// bound, so the binade of s_k lies within that of [P_k - E, P_k + E].  The
+// resulting bound B counts only the terms that can round, which for
+// coordinates of O(100) is a few thousand times ulp, not n ulp: the quotient
+// is then decided on both sides of the bound far more often.  The exact sum
+// itself is taken in double-double (error far below B).  Nodes the tight
+// bound cannot decide either stay on the list for the sequential sum.
+// ---------------------------------------------------------------------------
+constexpr int kTightChunk = 2048;   // elements per chunk (8 per thread)
+constexpr int kTightThreads = 256;
+constexpr int kTightNodes = 64;     // fallback nodes per level taken by this pass
+constexpr int kTightBlocks = 152 * 2;
+
+struct TightChunk {  // per chunk of a listed node
+  double hi[4], lo[4];  // double-double sum of the chunk's terms (x, y, z, m)
+  double a[4];          // sum of |terms|
+  double pre[4];        // approximate prefix sum of the terms before the chunk
+};
+struct TightNode {
+  double hi[4], lo[4], a[4];
+  double b[4];          // rounding-error bound of the sequential sum
+};
+
+__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e) {
+  s = __dadd_rn(a, b);
+  const double bb = __dsub_rn(s, a);
+  e = __dadd_rn(__dsub_rn(a, __dsub_rn(s, bb)), __dsub_rn(b, bb));
+}
+__device__ __forceinline__ void dd_add(double &hi, double &lo, double bhi, double blo) {
+  double s, e;
+  two_sum(hi, bhi, s, e);
+  e = __dadd_rn(e, __dadd_rn(lo, blo));
+  hi = __dadd_rn(s, e);
+  lo = __dsub_rn(e, __dsub_rn(hi, s));
+}
+
+// Chunks of the listed nodes in one index space: node f owns chunks
+// [cbase[f], cbase[f + 1]).  Computed per block into shared memory.
+__device__ int tight_layout(const DNode *nodes, const int32_t *fallback, const int64_t *counters,
+                            int32_t *cbase, int32_t skip) {
+  const int nt = skip ? 0 : int(min64(counters[C_NFALLBACK], kTightNodes));
+  if (threadIdx.x == 0) {
+    int32_t run = 0;
+    for (int f = 0; f < nt; ++f) {
+      cbase[f] = run;
+      run += (nodes[fallback[f]].count + kTightChunk - 1) / kTightChunk;
+    }
+    cbase[nt] = run;
+  }
+  __syncthreads();
+  return nt;
+}
+
+__device__ __forceinline__ void terms_of(const float4 &p, double t[4], int lsb[4]) {
+  const float fx = fmul_(p.w, p.x), fy = fmul_(p.w, p.y), fz = fmul_(p.w, p.z);
+  t[0] = double(fx);
+  t[1] = double(fy);
+  t[2] = double(fz);
+  t[3] = double(p.w);
+  lsb[0] = lsb_exp(fx);
+  lsb[1] = lsb_exp(fy);
+  lsb[2] = lsb_exp(fz);
+  lsb[3] = lsb_exp(p.w);
+}
+
+// Pass 1: double-double chunk sums; the last block to finish forms each
+// node's chunk prefixes and totals.
+__global__ void __launch_bounds__(kTightThreads)
+    k_cm_tight_sums(const float4 *__restrict__ pos, const DNode *nodes, const int32_t *fallback,
+                    int64_t *counters, TightChunk *chunks, TightNode *tn, int32_t skip) {
+  __shared__ int32_t cbase[kTightNodes + 1];
+  __shared__ double red[kTightThreads / 32][12];
+  __shared__ int last;
+  const int nt = tight_layout(nodes, fallback, counters, cbase, skip);
+  const int total = cbase[nt];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    int f = 0;
+    while (f + 1 < nt && cbase[f + 1] <= g) ++f;
+    const DNode &N = nodes[fallback[f]];
+    const int64_t b0 = int64_t(N.offset) + int64_t(g - cbase[f]) * kTightChunk;
+    const int64_t e0 = min64(int64_t(N.offset) + N.count, b0 + kTightChunk);
+    double hi[4] = {0, 0, 0, 0}, lo[4] = {0, 0, 0, 0}, a[4] = {0, 0, 0, 0};
+    for (int64_t i = b0 + threadIdx.x; i < e0; i += kTightThreads) {
+      double t[4];
+      int lsb[4];
+      terms_of(pos[i], t, lsb);
+      for (int q = 0; q < 4; ++q) {
+        dd_add(hi[q], lo[q], t[q], 0.0);
+        a[q] = __dadd_ru(a[q], fabs(t[q]));
+      }
+    }
+    for (int o = 16; o > 0; o >>= 1)
+      for (int q = 0; q < 4; ++q) {
+        const double oh = __shfl_xor_sync(0xffffffffu, hi[q], o);
+        const double ol = __shfl_xor_sync(0xffffffffu, lo[q], o);
+        dd_add(hi[q], lo[q], oh, ol);
+        a[q] = __dadd_ru(a[q], __shfl_xor_sync(0xffffffffu, a[q], o));
+      }
+    if (lane == 0)
+      for (int q = 0; q < 4; ++q) {
+        red[warp][q] = hi[q];
+        red[warp][4 + q] = lo[q];
+        red[warp][8 + q] = a[q];
+      }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      TightChunk c{};
+      for (int q = 0; q < 4; ++q) {
+        c.hi[q] = red[0][q];
+        c.lo[q] = red[0][4 + q];
+        c.a[q] = red[0][8 + q];
+      }
+      for (int w = 1; w < kTightThreads / 32; ++w)
+        for (int q = 0; q < 4; ++q) {
+          dd_add(c.hi[q], c.lo[q], red[w][q], red[w][4 + q]);
+          c.a[q] = __dadd_ru(c.a[q], red[w][8 + q]);
+        }
+      chunks[g] = c;
+    }
+    __syncthreads();
+  }
+  // the last block to finish forms the prefixes and totals
+  __threadfence();
+  if (threadIdx.x == 0)
+    last = atomicAdd((unsigned long long *)&counters[C_TDONE1], 1ull) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int f = threadIdx.x; f < nt; f += blockDim.x) {
+    double hi[4] = {0, 0, 0, 0}, lo[4] = {0, 0, 0, 0}, a[4] = {0, 0, 0, 0};
+    for (int32_t g = cbase[f]; g < cbase[f + 1]; ++g) {
+      TightChunk &c = chunks[g];
+      for (int q = 0; q < 4; ++q) {
+        c.pre[q] = hi[q] + lo[q];
+        dd_add(hi[q], lo[q], c.hi[q], c.lo[q]);
+        a[q] = __dadd_ru(a[q], c.a[q]);
+      }
+    }
+    for (int q = 0; q < 4; ++q) {
+      tn[f].hi[q] = hi[q];
+      tn[f].lo[q] = lo[q];
+      tn[f].a[q] = a[q];
+      tn[f].b[q] = 0.0;
+    }
+  }
+  if (threadIdx.x == 0) counters[C_TDONE1] = 0;
+}
+
+// Binade exponent range of the values in [v - e, v + e].
+__device__ __forceinline__ void binades(double v, double e, int &emin, int &emax) {
+  const double lo = v - e, hi = v + e;
+  const double amax = fmax(fabs(lo), fabs(hi));
+  emax = amax > 0.0 ? ilogb(amax) : -1074;
+  if (lo <= 0.0 && hi >= 0.0) emin = -1074;
+  else emin = ilogb(fmin(fabs(lo), fabs(hi)));
+}
+
+// Pass 2: the rounding-error bound per listed node; the last block certifies
+// and writes the centres of mass (certified nodes leave the list as -1).
+__global__ void __launch_bounds__(kTightThreads)
+    k_cm_tight_bound(const float4 *__restrict__ pos, DNode *nodes, int32_t *fallback,
+                     int64_t *counters, const TightChunk *chunks, TightNode *tn, int32_t skip) {
+  __shared__ int32_t cbase[kTightNodes + 1];
+  __shared__ float4 el[kTightChunk];
+  __shared__ double wsum[kTightThreads / 32][4];
+  __shared__ double bred[kTightThreads / 32][4];
+  __shared__ int last;
+  const int nt = tight_layout(nodes, fallback, counters, cbase, skip);
+  const int total = cbase[nt];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  constexpr int kPerT = kTightChunk / kTightThreads;
+  for (int g = blockIdx.x; g < total; g += gridDim.x) {
+    int f = 0;
+    while (f + 1 < nt && cbase[f + 1] <= g) ++f;
+    const DNode &N = nodes[fallback[f]];
+    const int64_t b0 = int64_t(N.offset) + int64_t(g - cbase[f]) * kTightChunk;
+    const int len = int(min64(int64_t(N.offset) + N.count - b0, kTightChunk));
+    for (int i = threadIdx.x; i < len; i += kTightThreads) el[i] = pos[b0 + i];
+    __syncthreads();
+    // this thread's elements [8 tid, 8 tid + 8): local sums, then a block scan
+    double loc[4] = {0, 0, 0, 0};
+    for (int k = 0; k < kPerT; ++k) {
+      const int i = threadIdx.x * kPerT + k;
+      if (i < len) {
+        double t[4];
+        int lsb[4];
+        terms_of(el[i], t, lsb);
+        for (int q = 0; q < 4; ++q) loc[q] += t[q];
+      }
+    }
+    double inc[4];
+    for (int q = 0; q < 4; ++q) {
+      inc[q] = loc[q];
+      for (int o = 1; o < 32; o <<= 1) {
+        const double v = __shfl_up_sync(0xffffffffu, inc[q], o);
+        if (lane >= o) inc[q] += v;
+      }
+      if (lane == 31) wsum[warp][q] = inc[q];
+    }
+    __syncthreads();
+    const TightChunk &C = chunks[g];
+    const TightNode &T = tn[f];
+    double P[4], E[4], bsum[4] = {0, 0, 0, 0};
+    for (int q = 0; q < 4; ++q) {
+      double wpre = 0;
+      for (int w = 0; w < warp; ++w) wpre += wsum[w][q];
+      P[q] = C.pre[q] + wpre + (inc[q] - loc[q]);
+      // |s_k - P_k| (sequential error) and the error of this approximate
+      // prefix are each below (n + 64) u sum|t|
+      E[q] = 4.0 * (double(N.count) + 64.0) * 0x1p-53 * T.a[q];
+    }
+    for (int k = 0; k < kPerT; ++k) {
+      const int i = threadIdx.x * kPerT + k;
+      if (i >= len) break;
+      double t[4];
+      int lsb[4];
+      terms_of(el[i], t, lsb);
+      const bool first = b0 + i == N.offset;
+      for (int q = 0; q < 4; ++q) {
+        const double prev = P[q];
+        P[q] += t[q];
+        if (first || t[q] == 0.0) continue;  // 0 + t and s + 0 are exact
+        int pmin, pmax, cmin, cmax;
+        binades(prev, E[q], pmin, pmax);
+        binades(P[q], E[q], cmin, cmax);
+        const int ulp_e = max(cmax, -1022) - 52;  // largest possible ulp(s_k)
+        const bool exact = pmin >= cmax && lsb[q] != INT_MIN && lsb[q] >= ulp_e;
+        if (!exact) bsum[q] = __dadd_ru(bsum[q], ldexp(1.0, ulp_e - 1));
+      }
+    }
+    for (int q = 0; q < 4; ++q) {
+      for (int o = 16; o > 0; o >>= 1) bsum[q] = __dadd_ru(bsum[q], __shfl_xor_sync(0xffffffffu, bsum[q], o));
+      if (lane == 0) bred[warp][q] = bsum[q];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int q = 0; q < 4; ++q) {
+        double b = 0;
+        for (int w = 0; w < kTightThreads / 32; ++w) b = __dadd_ru(b, bred[w][q]);
+        if (b > 0) atomicAdd(&tn[f].b[q], b);
+      }
+    __syncthreads();
+  }
+  __threadfence();
+  if (threadIdx.x == 0)
+    last = atomicAdd((unsigned long long *)&counters[C_TDONE2], 1ull) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  for (int f = threadIdx.x; f < nt; f += blockDim.x) {
+    const TightNode &T = tn[f];
+    DNode &N = nodes[fallback[f]];
+    double sx[4], bx[4];
+    for (int q = 0; q < 4; ++q) {
+      sx[q] = T.hi[q] + T.lo[q];
+      // B (atomics rounded to nearest: slack), the double-double error and
+      // the rounding of hi + lo
+      bx[q] = T.b[q] * (1.0 + 0x1p-30) + (double(N.count) + 64.0) * 0x1p-98 * T.a[q] +
+              fabs(sx[q]) * 0x1p-52;
+    }
+    float v[3];
+    bool ok = true;
+    for (int d = 0; d < 3 && ok; ++d) ok = certify(sx[d], bx[d], sx[3], bx[3], &v[d]);
+    if (ok) {
+      for (int d = 0; d < 3; ++d) N.xc[d] = v[d];
+      fallback[f] = -1;
+      atomicAdd((unsigned long long *)&counters[C_NTIGHT], 1ull);
+    }
+  }
+  if (threadIdx.x == 0) counters[C_TDONE2] = 0;
+}
+
 // The reference's centre of mass for the listed nodes, summed sequentially
 // in array order in double (BGQCM.c:186-211).
 __global__ void k_cm_fallback(const float4 *__restrict__ pos, DNode *nodes, const int32_t *fallback,
@@ -351,6 +631,7 @@ __global__ void k_cm_fallback(const float4 *__restrict__ pos, DNode *nodes, cons
   const int64_t nf = counters[C_NFALLBACK];
   for (int64_t f = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; f < nf;
        f += int64_t(gridDim.x) * blockDim.x) {
+    if (fallback[f] < 0) continue;  // certified by the tight pass
     DNode &N = nodes[fallback[f]];
     double x = 0, y = 0, z = 0, m = 0;
     for (int32_t i = 0; i < N.count; ++i) {
@@ -1159,7 +1440,7 @@ DeviceTree::~DeviceTree() {
   void *ptrs[] = {epos_, tpos_, oid_, toid_, idx_, nodes_, ppm_, chunk_node_, chunk_base_, part_,
                   left_cnt_, left_base_, scan_tmp_, node_tmp_, fallback_, counters_, leaf_ids_,
                   leaf_tmp_, leafdesc_, segs_, idx_list_, table_, items_, items_tmp_, gidx_,
-                  walk_err_};
+                  walk_err_, tight_chunks_, tight_nodes_};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h_counters_) cudaFreeHost(h_counters_);
@@ -1209,6 +1490,9 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   }
   const size_t nn = size_t(std::max<int64_t>(n, 1));
   n_ = n;
+  DT_CHECK(grow(tight_chunks_, cap_tc_,
+                (size_t(n) / kTightChunk + kTightNodes + 1) * (sizeof(TightChunk) / sizeof(double)), s));
+  DT_CHECK(grow(tight_nodes_, cap_tn_, size_t(kTightNodes) * (sizeof(TightNode) / sizeof(double)), s));
   DT_CHECK(grow(epos_, cap_e_, nn, s));
   DT_CHECK(grow(tpos_, cap_t_, nn, s));
   DT_CHECK(grow(oid_, cap_o_, nn, s));
@@ -1247,6 +1531,7 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     DT_CHECK(grow(left_cnt_, cap_lc_, size_t(max_chunks), s));
     DT_CHECK(grow(left_base_, cap_lb_, size_t(max_chunks), s));
     DT_CHECK(cudaMemsetAsync(counters_ + C_NFALLBACK, 0, sizeof(int64_t), s));
+    DT_CHECK(cudaMemsetAsync(counters_ + C_NTIGHT, 0, sizeof(int64_t), s));
 
     const unsigned gL = unsigned((L + 127) / 128);
     k_chunk_counts<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
@@ -1257,6 +1542,12 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
                                                  counters_ + C_NCHUNK, part_);
     k_stats_final<<<unsigned((int64_t(L) * 32 + 255) / 256), 256, 0, s>>>(
         nodes_, nb, ne, chunk_base_, part_, fallback_, counters_, cfg.force_cm_fallback);
+    k_cm_tight_sums<<<kTightBlocks, kTightThreads, 0, s>>>(
+        epos_, nodes_, fallback_, counters_, reinterpret_cast<TightChunk *>(tight_chunks_),
+        reinterpret_cast<TightNode *>(tight_nodes_), cfg.force_cm_fallback == 1);
+    k_cm_tight_bound<<<kTightBlocks, kTightThreads, 0, s>>>(
+        epos_, nodes_, fallback_, counters_, reinterpret_cast<const TightChunk *>(tight_chunks_),
+        reinterpret_cast<TightNode *>(tight_nodes_), cfg.force_cm_fallback == 1);
     k_cm_fallback<<<unsigned(std::min<int64_t>((L + 127) / 128, 1024)), 128, 0, s>>>(
         epos_, nodes_, fallback_, counters_);
     k_split_decide<<<gL, 128, 0, s>>>(nodes_, nb, ne, cfg.nd);
@@ -1273,7 +1564,8 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     DT_CHECK(exclusive_scan_i64(node_tmp_, node_tmp_, L, counters_ + C_NSPLIT, scan_tmp_, s));
     k_children<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
     DT_CHECK(cudaGetLastError());
-    DT_CHECK(cudaMemcpyAsync(h_counters_, counters_, 4 * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    DT_CHECK(cudaMemcpyAsync(h_counters_, counters_, (C_NTIGHT + 1) * sizeof(int64_t),
+                             cudaMemcpyDeviceToHost, s));
     int32_t perr = 0;
     DT_CHECK(cudaMemcpyAsync(&perr, walk_err_, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     DT_CHECK(cudaStreamSynchronize(s));
@@ -1281,7 +1573,7 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
       err_ = "partition chain check failed";
       return cudaErrorUnknown;
     }
-    info_.cm_fallbacks += h_counters_[C_NFALLBACK];
+    info_.cm_fallbacks += h_counters_[C_NFALLBACK] - h_counters_[C_NTIGHT];
     const int64_t nsplit = h_counters_[C_NSPLIT];
     nb = ne;
     ne = int32_t(ne + 2 * nsplit);

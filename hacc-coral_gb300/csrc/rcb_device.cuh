@@ -43,7 +43,8 @@ struct TreeConfig {
   float min[3], max[3], min_force[3], max_force[3];
   float fsrrmax, tan_oa, ppc;
   int32_t nd, tdpts;
-  int32_t force_cm_fallback;  // test hook: every node takes the sequential sum
+  int32_t force_cm_fallback;  // test hook: 1 = every node takes the sequential sum,
+                              // 2 = every node goes through the tight certification
   int32_t group;              // particles per work-item group: 16 or 32 (0 = 32)
 };
 
@@ -131,6 +132,8 @@ class DeviceTree {
   size_t cap_nt_ = 0;
   int32_t *fallback_ = nullptr;
   size_t cap_fb_ = 0;
+  double *tight_chunks_ = nullptr, *tight_nodes_ = nullptr;  // tight c.m. certification
+  size_t cap_tc_ = 0, cap_tn_ = 0;
   int64_t *counters_ = nullptr;  // device scalars
   int64_t *h_counters_ = nullptr;  // pinned mirror
   // lists

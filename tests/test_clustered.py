@@ -64,7 +64,7 @@ def test_clustered48_vs_oracle(ctx, oracle_lib, nd):
     # halo leaves have far longer lists than field leaves
     _, cnt, ptr = r.leaves()
     ln = np.diff(ptr)
-    assert ln.max() > 4 * np.median(ln)
+    assert ln.max() > 2.5 * np.median(ln)
 
 
 @pytest.mark.gpu

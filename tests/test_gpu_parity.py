@@ -250,6 +250,26 @@ def test_cm_sequential_fallback_path(ctx, monkeypatch):
     assert np.array_equal(vel(p), vel(q))
 
 
+@pytest.mark.parametrize("ng,nd", [(20, 32), (48, 64)])
+def test_cm_tight_certification_path(ctx, monkeypatch, ng, nd):
+    """Every node's centre of mass through the tight certification (up to 64
+    nodes per level; the rest sequential) gives the same tree as the loose
+    certification: the tight bound never certifies a wrong float."""
+    p = synth.clustered_box(ng, nhalo=30, seed=5)
+    kp = synth.kick_params(p, nd=nd)
+    q = p.copy()
+    ctx.rcb_kick(p, kp)
+    lp = ctx.lists()
+    monkeypatch.setenv("HSR_FORCE_CM_FALLBACK", "2")
+    st = ctx.rcb_kick(q, kp)
+    monkeypatch.delenv("HSR_FORCE_CM_FALLBACK")
+    assert st["cm_fallbacks"] < st["nodes"]  # the tight pass certified some
+    for k in EXACT:
+        assert np.array_equal(getattr(p, k).view(np.uint8), getattr(q, k).view(np.uint8)), k
+    assert same_lists(*lp, *ctx.lists())
+    assert np.array_equal(vel(p), vel(q))
+
+
 def test_device_memory_arrays(ctx):
     """HSR_MEM_DEVICE: the same kick on arrays already in HBM."""
     torch = pytest.importorskip("torch")

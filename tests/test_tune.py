@@ -133,3 +133,23 @@ def test_autotune_needs_device_kick(hsr_lib):
             c.autotune(iters=1)
     finally:
         c.close()
+
+
+@pytest.mark.gpu
+def test_adjoint_under_group16_context(tctx, hsr_lib):
+    """A context tuned to groups of 16 still runs the forward/VJP pair on its
+    own 32-particle items: same dv and xbar as a default context."""
+    p = synth.zeldovich_box(24, z=10.0, seed=17)
+    kp = synth.kick_params(p, nd=64, fcoeff=1.0)
+    u = np.random.default_rng(3).standard_normal((p.n, 3)).astype(np.float32)
+    tctx.set_tune("batched", 128, 16)
+    dv16 = tctx.force_fwd(p.x, p.y, p.z, p.mass, kp)
+    xb16 = tctx.force_vjp(u)
+    tctx.set_tune("batched", 128, 32)
+    with hsr.Context(0) as c:
+        dv = c.force_fwd(p.x, p.y, p.z, p.mass, kp)
+        xb = c.force_vjp(u)
+    rms, mx = force_errors(dv16.astype(np.float64), dv.astype(np.float64))
+    assert rms <= RMS_TOL and mx <= MAX_TOL, (rms, mx)
+    rms, mx = force_errors(xb16.astype(np.float64), xb.astype(np.float64))
+    assert rms <= RMS_TOL and mx <= MAX_TOL, (rms, mx)
