@@ -63,6 +63,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--multibox", type=int, default=8,
                     help="boxes of 96^3 in the multi-box line (0: skip)")
+    ap.add_argument("--adjoint-boxes", type=int, default=8,
+                    help="boxes of 96^3 in the multi-step adjoint line (0: skip)")
     ap.add_argument("--clustered", type=int, default=256,
                     help="side of the clustered set of the leaf size x shape sweep (0: skip)")
     ap.add_argument("--cpu-slab", type=float, default=0.25,
@@ -311,6 +313,42 @@ def main():
                     "pairs_per_s": stb["pairs"] / (ms_b * 1e-3),
                     "e2e_s": wall_b, "e2e_pairs_per_s": stb["pairs"] / wall_b}
 
+    # ---- multi-step adjoint: boxes of 96^3, 10 PM steps x 5 sub-cycles ----
+    multistep_line = None
+    if args.adjoint_boxes > 0:
+        import torch
+        import multistep
+        nsteps, nsub, every = 10, 5, 2
+        boxes = [synth.zeldovich_box(96, z=50.0, seed=300 + b) for b in range(args.adjoint_boxes)]
+        kps = [synth.kick_params(b, nd=args.nd) for b in boxes]
+        sched = multistep.schedule(50.0, 10.0, nsteps, nsub)
+        msr = multistep.MultiStep(ctx, kps, sched, nsub, checkpoint_every=every)
+        states = [multistep.box_state(b, local) for b in boxes]
+        rng = np.random.default_rng(5)
+        cots = [[torch.from_numpy(rng.standard_normal(b.n).astype(np.float32)).cuda(local)
+                 for _ in range(6)] for b in boxes]
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for b, S in enumerate(states):
+            msr.forward_box(b, S.clone())
+        torch.cuda.synchronize()
+        t_fwd = time.perf_counter() - t0
+        k0 = msr.kicks
+        t0 = time.perf_counter()
+        for b, S in enumerate(states):
+            msr.adjoint_box(b, S, cots[b][:3], cots[b][3:])
+        torch.cuda.synchronize()
+        t_adj = time.perf_counter() - t0
+        nsc = args.adjoint_boxes * nsteps * nsub
+        multistep_line = {
+            "boxes": args.adjoint_boxes, "n_side": 96, "n_particles_per_box": boxes[0].n,
+            "pm_steps": nsteps, "sub_cycles": nsub, "checkpoint_every": every,
+            "forward_s": t_fwd, "adjoint_s": t_adj,
+            "s_per_substep_forward": t_fwd / nsc, "s_per_substep_adjoint": t_adj / nsc,
+            "kicks_in_adjoint": msr.kicks - k0,
+            "note": "short-range sub-cycles only (map1, kick, map1); the PM kick is not in the map"}
+        del states, cots
+
     # ---- clustered set: leaf size x launch shape sweep ----
     clustered = None
     if args.clustered > 0:
@@ -357,6 +395,7 @@ def main():
             "adjoint": {"vjp_ms": vjp_ms, "vjp_pairs_per_s": pairs / (vjp_ms * 1e-3)},
             "multibox": multibox,
             "clustered": clustered,
+            "multistep_adjoint": multistep_line,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak if peak else None,
                          "traffic": profiled_traffic(cfg["workload"], cfg["shape"]),

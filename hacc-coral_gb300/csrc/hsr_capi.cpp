@@ -956,9 +956,15 @@ hsr_status hsr_subcycle(hsr_ctx *ctx, const hsr_subcycle_params *sp, int64_t n, 
   return HSR_OK;
 }
 
-hsr_status hsr_force_fwd(hsr_ctx *ctx, const hsr_params *p, int64_t n, const float *x,
-                         const float *y, const float *z, const float *mass, float *dvx,
-                         float *dvy, float *dvz, int32_t mem) {
+}  // extern "C"
+
+namespace {
+
+// hsr_force_fwd (accumulate = false: dv written) and hsr_force_kick
+// (accumulate = true: dv added into the arrays).
+hsr_status force_fwd_impl(hsr_ctx *ctx, const hsr_params *p, int64_t n, const float *x,
+                          const float *y, const float *z, const float *mass, float *dvx,
+                          float *dvy, float *dvz, int32_t mem, bool accumulate) {
   if (!ctx) return HSR_ERR_ARG;
   const auto t_start = clk::now();
   const void *arrs[10] = {x, y, z, dvx, dvy, dvz, mass, x, x, x};
@@ -1026,7 +1032,13 @@ hsr_status hsr_force_fwd(hsr_ctx *ctx, const hsr_params *p, int64_t n, const flo
   float *outs[3] = {dvx, dvy, dvz};
   for (int d = 0; d < 3; ++d) {
     float *o = mem == HSR_MEM_HOST ? ob + d * stride : outs[d];
-    CU(hsr::launch_scatter_f32(dv + d * n, ctx->tree.perm(), o, n, s), "scatter dv");
+    if (accumulate) {
+      if (mem == HSR_MEM_HOST)
+        CU(cudaMemcpyAsync(o, outs[d], size_t(n) * 4, cudaMemcpyHostToDevice, s), "H2D v");
+      CU(hsr::launch_scatter_add_f32(dv + d * n, ctx->tree.perm(), o, n, s), "scatter-add dv");
+    } else {
+      CU(hsr::launch_scatter_f32(dv + d * n, ctx->tree.perm(), o, n, s), "scatter dv");
+    }
     if (mem == HSR_MEM_HOST)
       CU(cudaMemcpyAsync(outs[d], o, size_t(n) * 4, cudaMemcpyDeviceToHost, s), "D2H dv");
   }
@@ -1049,6 +1061,40 @@ hsr_status hsr_force_fwd(hsr_ctx *ctx, const hsr_params *p, int64_t n, const flo
   ctx->have_lists = true;
   ctx->last_tdpts = p->tdpts;
   ctx->tape = true;
+  return HSR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+hsr_status hsr_force_fwd(hsr_ctx *ctx, const hsr_params *p, int64_t n, const float *x,
+                         const float *y, const float *z, const float *mass, float *dvx,
+                         float *dvy, float *dvz, int32_t mem) {
+  return force_fwd_impl(ctx, p, n, x, y, z, mass, dvx, dvy, dvz, mem, false);
+}
+
+hsr_status hsr_force_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, const float *x,
+                          const float *y, const float *z, const float *mass, float *vx,
+                          float *vy, float *vz, int32_t mem) {
+  return force_fwd_impl(ctx, p, n, x, y, z, mass, vx, vy, vz, mem, true);
+}
+
+hsr_status hsr_stream(hsr_ctx *ctx, int64_t n, float *x, float *y, float *z, const float *vx,
+                      const float *vy, const float *vz, float alpha, float pp, float tau,
+                      float adot, int32_t mem) {
+  if (!ctx || n < 0 || (n > 0 && (!x || !y || !z || !vx || !vy || !vz))) return HSR_ERR_ARG;
+  if (mem != HSR_MEM_DEVICE)
+    return ctx->fail(HSR_ERR_UNSUPPORTED, "hsr_stream takes device arrays (HSR_MEM_DEVICE)");
+  if (!(alpha != 0.0f) || !(adot != 0.0f) || !(pp > 0.0f))
+    return ctx->fail(HSR_ERR_ARG, "alpha, adot must be nonzero and pp positive");
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  // map1's prefactor in float, as the reference computes it
+  const float pf = std::pow(pp, float(1.0 + 1.0 / alpha));
+  const float prefactor = float(1.0 / (alpha * adot * pf));
+  const float pt = prefactor * tau;
+  CU(hsr::launch_stream(x, y, z, vx, vy, vz, n, pt, ctx->stream), "stream kernel");
+  CU(cudaStreamSynchronize(ctx->stream), "stream kernel execution");
   return HSR_OK;
 }
 

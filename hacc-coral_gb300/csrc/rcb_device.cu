@@ -1354,6 +1354,13 @@ __global__ void k_scatter_f32(const float *__restrict__ in, const int32_t *__res
     out[perm[i]] = in[i];
 }
 
+__global__ void k_scatter_add_f32(const float *__restrict__ in, const int32_t *__restrict__ perm,
+                                  float *out, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x)
+    out[perm[i]] += in[i];
+}
+
 // acc holds, per node, sum over it and its ancestors of xbar_P / M_P.
 __global__ void k_adj_root(const float4 *table, int64_t n, const float *xbx, const float *xby,
                            const float *xbz, float *acc) {
@@ -1720,6 +1727,13 @@ cudaError_t launch_scatter_f32(const float *in, const int32_t *perm, float *out,
                                cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   k_scatter_f32<<<grid_for(n, 256), 256, 0, s>>>(in, perm, out, n);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_scatter_add_f32(const float *in, const int32_t *perm, float *out, int64_t n,
+                                   cudaStream_t s) {
+  if (n <= 0) return cudaSuccess;
+  k_scatter_add_f32<<<grid_for(n, 256), 256, 0, s>>>(in, perm, out, n);
   return cudaGetLastError();
 }
 

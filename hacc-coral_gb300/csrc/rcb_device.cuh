@@ -171,6 +171,9 @@ cudaError_t launch_unpack4(const float4 *in, float *x, float *y, float *z, float
 // out[perm[i]] = in[i] (back to the caller's order).
 cudaError_t launch_scatter_f32(const float *in, const int32_t *perm, float *out, int64_t n,
                                cudaStream_t s);
+// out[perm[i]] += in[i].
+cudaError_t launch_scatter_add_f32(const float *in, const int32_t *perm, float *out, int64_t n,
+                                   cudaStream_t s);
 // Monopole pseudo-particle gradients passed to the particles through the
 // nodes' centres of mass: xbar_k += m_k sum_{nodes P containing k} xbar_P / M_P,
 // where xbar_P sits at slot n + P of the 3 arrays and M_P is the pseudo mass.

@@ -35,7 +35,8 @@ EXPORTS = ("hsr_create", "hsr_destroy", "hsr_last_error", "hsr_version", "hsr_rc
            "hsr_force_law", "hsr_bench_pairs", "hsr_probe_fp32_peak", "hsr_kick_lists_noalloc",
            "hsr_force_fwd", "hsr_force_vjp", "hsr_last_perm", "hsr_tree_size", "hsr_tree_export",
            "hsr_lists_export_index", "hsr_rcb_kick_batch", "hsr_bench_pairs_graph",
-           "hsr_subcycle", "hsr_set_tune", "hsr_get_tune", "hsr_autotune")
+           "hsr_subcycle", "hsr_set_tune", "hsr_get_tune", "hsr_autotune",
+           "hsr_force_kick", "hsr_stream")
 
 
 class HsrError(RuntimeError):
@@ -156,6 +157,10 @@ def load(path: str = LIB_PATH):
     lib.hsr_bench_pairs.argtypes = [vp, i32, i32, i32, C.POINTER(C.c_double)]
     lib.hsr_probe_fp32_peak.restype = i32
     lib.hsr_probe_fp32_peak.argtypes = [vp, C.POINTER(C.c_double)]
+    lib.hsr_force_kick.restype = i32
+    lib.hsr_force_kick.argtypes = [vp, C.POINTER(HsrParams), i64, vp, vp, vp, vp, vp, vp, vp, i32]
+    lib.hsr_stream.restype = i32
+    lib.hsr_stream.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, f32, f32, f32, f32, i32]
     lib.hsr_set_tune.restype = i32
     lib.hsr_set_tune.argtypes = [vp, C.POINTER(HsrTune)]
     lib.hsr_get_tune.restype = i32
@@ -282,6 +287,38 @@ class Context:
         self._check(self.lib.hsr_force_fwd(self.h, C.byref(P), n, *[vp(a) for a in arrs],
                                            *[vp(a) for a in dv], MEM_HOST), "hsr_force_fwd")
         return np.stack(dv, 1)
+
+    def force_kick_device(self, x, y, z, mass, vx, vy, vz, kp, kernel: int = KERNEL_AUTO):
+        """hsr_force_kick on device buffers (objects with data_ptr(), e.g. CUDA
+        tensors of float32): v += dv in the caller's order; records the tape."""
+        n = int(x.numel())
+        P = make_params(kp, kernel, BUILD_DEVICE)
+        ptr = lambda t: C.c_void_p(t.data_ptr())
+        self._check(self.lib.hsr_force_kick(self.h, C.byref(P), n, ptr(x), ptr(y), ptr(z),
+                                            ptr(mass), ptr(vx), ptr(vy), ptr(vz), MEM_DEVICE),
+                    "hsr_force_kick")
+
+    def force_fwd_device(self, x, y, z, mass, dvx, dvy, dvz, kp, kernel: int = KERNEL_AUTO):
+        """hsr_force_fwd on device buffers: dv written in the caller's order."""
+        n = int(x.numel())
+        P = make_params(kp, kernel, BUILD_DEVICE)
+        ptr = lambda t: C.c_void_p(t.data_ptr())
+        self._check(self.lib.hsr_force_fwd(self.h, C.byref(P), n, ptr(x), ptr(y), ptr(z),
+                                           ptr(mass), ptr(dvx), ptr(dvy), ptr(dvz), MEM_DEVICE),
+                    "hsr_force_fwd")
+
+    def force_vjp_device(self, ux, uy, uz, xbx, xby, xbz):
+        """hsr_force_vjp on device buffers: xbar = (d dv / d x)^T u, caller order."""
+        ptr = lambda t: C.c_void_p(t.data_ptr())
+        self._check(self.lib.hsr_force_vjp(self.h, ptr(ux), ptr(uy), ptr(uz), ptr(xbx), ptr(xby),
+                                           ptr(xbz), MEM_DEVICE), "hsr_force_vjp")
+
+    def stream_device(self, x, y, z, vx, vy, vz, alpha, pp, tau, adot):
+        """hsr_stream (Particles::map1) on device buffers: x += pt v."""
+        ptr = lambda t: C.c_void_p(t.data_ptr())
+        self._check(self.lib.hsr_stream(self.h, int(x.numel()), ptr(x), ptr(y), ptr(z), ptr(vx),
+                                        ptr(vy), ptr(vz), alpha, pp, tau, adot, MEM_DEVICE),
+                    "hsr_stream")
 
     def force_vjp(self, dvbar):
         """hsr_force_vjp: xbar (n x 3) for the cotangent dvbar (n x 3), caller order."""

@@ -1,0 +1,212 @@
+"""Multi-step adjoint of HACC's short-range sub-cycles, with checkpoints.
+
+The forward map is the sub-cycled short-range part of HACC's time step
+(src/simulation/driver_hires.cxx:320-447 around Particles::subCycle,
+src/cpu/Particles.cxx:1176-1201): for each PM step s, with the time stepper
+advanced half a step (TimeStepper::advanceHalfStep, src/simulation/
+TimeStepper.cxx:60-67), nsub times
+
+    x += pt v              Particles::map1 with tau2 / nsub     (hsr_stream)
+    v += c K(x)            the RCB short-range kick, c = map2's  (hsr_force_kick)
+    x += pt v              map1 again                            (hsr_stream)
+
+on a fixed set of particles kept at fixed indices (the kick does not permute
+them; the tree is rebuilt at every kick).  The long-range PM kick between the
+steps is not part of this library and is left out of the map.
+
+The reverse pass gives the vector-Jacobian product of the whole map: for
+cotangents (xbar_T, vbar_T) of the final state, (xbar_0, vbar_0) of the
+initial one.  Per sub-cycle, in reverse:
+
+    vbar += pt xbar                                   (hsr_stream on (vbar, xbar))
+    xbar += (dK/dx)^T (c vbar) at the kick positions  (hsr_force_fwd + hsr_force_vjp)
+    vbar += pt xbar
+
+The trees and lists are held fixed within each kick (they are piecewise
+constant in the positions).  The kick positions are not stored for the whole
+run: the state is checkpointed every `checkpoint_every` PM steps and each
+segment is recomputed from its checkpoint during the reverse pass.  Boxes
+are independent and run one after the other on the context's stream.
+
+Buffers are CUDA tensors (torch is used for device memory only); every
+arithmetic step on particle data runs in this library's kernels, apart from
+the vector sum xbar += (kick VJP), done with torch's add on the device.  The
+library works on its context's own stream and returns with it synchronized;
+the torch copies and sums run on torch's current stream and are waited for
+before the next library call reads their results.
+"""
+from __future__ import annotations
+
+import dataclasses
+from typing import Callable, List, Optional, Sequence
+
+import numpy as np
+
+import hsr
+import synth
+
+
+@dataclasses.dataclass
+class StepParams:
+    """One PM step's sub-cycle parameters (time stepper at mid-step)."""
+    alpha: float
+    pp: float
+    adot: float
+    tau_sub: float   # map1's tau: stepFraction * tau2 = tau / (2 nsub)
+    fcoeff: float    # map2's kick coefficient with stepFraction 1 / nsub
+
+
+def schedule(z_in: float, z_fin: float, nsteps: int, nsub: int) -> List[StepParams]:
+    """PM steps from z_in to z_fin (the reference's TimeStepper)."""
+    ts0 = synth.stepper(z_in=z_in, z_fin=z_fin, nsteps=nsteps)
+    out = []
+    for s in range(nsteps):
+        ts = synth.Stepper(alpha=ts0.alpha, pp=ts0.pp + s * ts0.tau + ts0.tau2,
+                           omegatot=ts0.omegatot, tau=ts0.tau)
+        out.append(StepParams(alpha=ts.alpha, pp=ts.pp, adot=ts.adot,
+                              tau_sub=float(np.float32(ts.tau2 / nsub)),
+                              fcoeff=float(synth.kick_coefficient(ts, nsub))))
+    return out
+
+
+@dataclasses.dataclass
+class BoxState:
+    """Device state of one box: positions, velocities (3 float32 CUDA tensors
+    each) and masses."""
+    x: list
+    v: list
+    mass: object
+
+    def clone(self) -> "BoxState":
+        return BoxState([t.clone() for t in self.x], [t.clone() for t in self.v], self.mass)
+
+
+def _torch_done():
+    import torch
+    torch.cuda.current_stream().synchronize()
+
+
+def box_state(p: synth.Particles, device: int = 0) -> BoxState:
+    import torch
+    dev = torch.device("cuda", device)
+    f = lambda a: torch.from_numpy(np.ascontiguousarray(a, np.float32)).to(dev)
+    return BoxState([f(p.x), f(p.y), f(p.z)], [f(p.vx), f(p.vy), f(p.vz)], f(p.mass))
+
+
+TapeHook = Callable[[int, int, int, hsr.Context, list], None]
+
+
+class MultiStep:
+    """Forward map and its checkpointed adjoint for a list of boxes.
+
+    kps: one synth.KickParams per box (fcoeff is replaced per PM step).
+    on_tape(box, step, sub, ctx, x), if set, runs in the reverse pass right
+    after each kick's tape is recorded at its positions x: the context then
+    holds that kick's tree and lists (the FP64 checkers in the tests read
+    them there).
+    """
+
+    def __init__(self, ctx: hsr.Context, kps: Sequence[synth.KickParams],
+                 steps: Sequence[StepParams], nsub: int, checkpoint_every: Optional[int] = 2):
+        if checkpoint_every is not None and checkpoint_every < 1:
+            raise ValueError("checkpoint_every must be >= 1 or None")
+        self.ctx = ctx
+        self.kps = list(kps)
+        self.steps = list(steps)
+        self.nsub = nsub
+        self.every = checkpoint_every
+        self.on_tape: Optional[TapeHook] = None
+        self.kicks = 0
+
+    # ---- one box ----------------------------------------------------------
+    def _kp(self, b: int, st: StepParams) -> synth.KickParams:
+        return dataclasses.replace(self.kps[b], fcoeff=st.fcoeff)
+
+    def _stream(self, x, v, st: StepParams):
+        self.ctx.stream_device(x[0], x[1], x[2], v[0], v[1], v[2], st.alpha, st.pp, st.tau_sub,
+                               st.adot)
+
+    def _subcycle(self, b: int, s: int, j: int, S: BoxState, record: Optional[list]):
+        st = self.steps[s]
+        self._stream(S.x, S.v, st)
+        if record is not None:
+            record.append([t.clone() for t in S.x])
+            _torch_done()  # the copy is taken before the next half-stream moves x
+        self.ctx.force_kick_device(S.x[0], S.x[1], S.x[2], S.mass, S.v[0], S.v[1], S.v[2],
+                                   self._kp(b, st))
+        self.kicks += 1
+        self._stream(S.x, S.v, st)
+
+    def _run(self, b: int, S: BoxState, s0: int, s1: int, record: Optional[list] = None):
+        for s in range(s0, s1):
+            for j in range(self.nsub):
+                self._subcycle(b, s, j, S, record)
+
+    def forward_box(self, b: int, S: BoxState) -> BoxState:
+        """The whole map on box b's state (in place); returns it."""
+        _torch_done()
+        self._run(b, S, 0, len(self.steps))
+        return S
+
+    def _reverse_segment(self, b: int, s0: int, s1: int, xk: list, mass, xb, vb, scratch):
+        k = len(xk)
+        for s in reversed(range(s0, s1)):
+            st = self.steps[s]
+            kp = self._kp(b, st)
+            for j in reversed(range(self.nsub)):
+                k -= 1
+                x1 = xk[k]
+                self._stream(vb, xb, st)                      # second half-stream
+                self.ctx.force_fwd_device(x1[0], x1[1], x1[2], mass, *scratch, kp)
+                self.kicks += 1
+                if self.on_tape:
+                    self.on_tape(b, s, j, self.ctx, x1)
+                self.ctx.force_vjp_device(vb[0], vb[1], vb[2], *scratch)
+                for d in range(3):
+                    xb[d].add_(scratch[d])                     # kick
+                _torch_done()
+                self._stream(vb, xb, st)                      # first half-stream
+
+    def adjoint_box(self, b: int, S0: BoxState, xbar, vbar):
+        """(xbar_0, vbar_0) for the final-state cotangents (xbar, vbar) (lists
+        of 3 CUDA tensors); S0, xbar and vbar are not modified.  With
+        checkpoints the forward keeps the state every `checkpoint_every` PM
+        steps and the reverse pass recomputes each segment's kick positions;
+        without (None) the forward keeps every kick position."""
+        import torch
+        nst = len(self.steps)
+        xb = [t.clone() for t in xbar]
+        vb = [t.clone() for t in vbar]
+        scratch = [torch.empty_like(S0.x[0]) for _ in range(3)]
+        S = S0.clone()
+        _torch_done()
+        if self.every is None:
+            xk: list = []
+            self._run(b, S, 0, nst, record=xk)
+            self._reverse_segment(b, 0, nst, xk, S0.mass, xb, vb, scratch)
+            return xb, vb
+        cps = []
+        for s0 in range(0, nst, self.every):
+            cps.append((s0, S.clone()))
+            _torch_done()
+            self._run(b, S, s0, min(nst, s0 + self.every))
+        for s0, C in reversed(cps):
+            s1 = min(nst, s0 + self.every)
+            xk = []
+            self._run(b, C, s0, s1, record=xk)
+            self._reverse_segment(b, s0, s1, xk, S0.mass, xb, vb, scratch)
+        return xb, vb
+
+    def forward(self, states: Sequence[BoxState]) -> List[BoxState]:
+        return [self.forward_box(b, S) for b, S in enumerate(states)]
+
+    def adjoint(self, states: Sequence[BoxState], xbars, vbars):
+        return [self.adjoint_box(b, S, xb, vb)
+                for b, (S, xb, vb) in enumerate(zip(states, xbars, vbars))]
+
+
+def kicks_per_box(nsteps: int, nsub: int, checkpointed: bool = True) -> int:
+    """Kicks one box's adjoint runs: the forward, the recomputation of every
+    segment (checkpointed only) and the tape of every kick in the reverse
+    pass."""
+    return (3 if checkpointed else 2) * nsteps * nsub

@@ -257,6 +257,25 @@ hsr_status hsr_force_fwd(hsr_ctx *ctx, const hsr_params *p, int64_t n, const flo
                          const float *y, const float *z, const float *mass, float *dvx,
                          float *dvy, float *dvz, int32_t mem);
 
+/* hsr_force_fwd that adds dv into (vx, vy, vz), the caller's order, instead
+ * of writing it: the sub-cycle's short-range kick (RCBForceTree's nbody1
+ * update v += fcoeff m_i sum_j m_j g d, src/halo_finder/RCBForceTree.cxx:
+ * 599-619) without permuting the caller's arrays, so a multi-step driver
+ * keeps every particle at a fixed index.  Records the same tape as
+ * hsr_force_fwd. */
+hsr_status hsr_force_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, const float *x,
+                          const float *y, const float *z, const float *mass, float *vx,
+                          float *vy, float *vz, int32_t mem);
+
+/* Particles::map1 (src/cpu/Particles.cxx:732-758) on device arrays:
+ * x += pt * v for the three components, pt = prefactor * tau with prefactor =
+ * 1 / (alpha * adot * pp^(1 + 1/alpha)), all in float as map1 computes them.
+ * Called with (vbar, xbar) in place of (x, v) it is also the half-stream's adjoint
+ * (vbar += pt xbar).  mem must be HSR_MEM_DEVICE. */
+hsr_status hsr_stream(hsr_ctx *ctx, int64_t n, float *x, float *y, float *z, const float *vx,
+                      const float *vy, const float *vz, float alpha, float pp, float tau,
+                      float adot, int32_t mem);
+
 /* Backward half: xbar = (d dv / d x)^T dvbar for the tape of the last
  * hsr_force_fwd, caller's order, with the tree and the lists held fixed (they
  * are piecewise constant in the positions).  A monopole pseudo-particle sits

@@ -1134,6 +1134,115 @@ void ora_vjp_fp64_tab(int64_t n, const float *tab, int64_t ntab, const int64_t *
   free(xt);
 }
 
+/* FP64 positions of the table: particles (tree order) then one pseudo-particle
+ * per node slot at the FP64 centre of mass of the node's particles. */
+static void tab64_fill(int64_t n, const double *pos, const double *m, int64_t nslots,
+                       const int64_t *pnode_off, const int64_t *pnode_cnt, double *tab) {
+  for (int64_t i = 0; i < n; ++i) {
+    tab[4 * i] = pos[3 * i];
+    tab[4 * i + 1] = pos[3 * i + 1];
+    tab[4 * i + 2] = pos[3 * i + 2];
+    tab[4 * i + 3] = m[i];
+  }
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 64)
+#endif
+  for (int64_t t = 0; t < nslots; ++t) {
+    double M = 0, c[3] = {0, 0, 0};
+    for (int64_t k = pnode_off[t]; k < pnode_off[t] + pnode_cnt[t]; ++k) {
+      M += m[k];
+      for (int a = 0; a < 3; ++a) c[a] += m[k] * pos[3 * k + a];
+    }
+    double *o = tab + 4 * (n + t);
+    for (int a = 0; a < 3; ++a) o[a] = M != 0 ? c[a] / M : 0.0;
+    o[3] = M;
+  }
+}
+
+void ora_kick64(int64_t n, const double *pos, const double *m, int64_t nslots,
+                const int64_t *pnode_off, const int64_t *pnode_cnt, int law, double rsm,
+                double fsrrmax, double c, int64_t nleaves, const int64_t *leaf_offset,
+                const int64_t *leaf_count, const int64_t *list_ptr, const int64_t *list_idx,
+                double *dv) {
+  double rmax2 = fsrrmax * fsrrmax;
+  double *tab = (double *)malloc((size_t)(4 * (n + nslots) + 4) * sizeof(double));
+  tab64_fill(n, pos, m, nslots, pnode_off, pnode_cnt, tab);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 4)
+#endif
+  for (int64_t l = 0; l < nleaves; ++l) {
+    for (int64_t i = leaf_offset[l]; i < leaf_offset[l] + leaf_count[l]; ++i) {
+      double a[3] = {0, 0, 0};
+      for (int64_t k = list_ptr[l]; k < list_ptr[l + 1]; ++k) {
+        int64_t e = list_idx[k];
+        if (e == i) continue;
+        double d[3] = {tab[4 * e] - tab[4 * i], tab[4 * e + 1] - tab[4 * i + 1],
+                       tab[4 * e + 2] - tab[4 * i + 2]};
+        double wg, wgp;
+        if (!pair_terms(law, rsm, rmax2, tab[4 * i + 3], tab[4 * e + 3], d, &wg, &wgp)) continue;
+        for (int q = 0; q < 3; ++q) a[q] += wg * d[q];
+      }
+      for (int q = 0; q < 3; ++q) dv[3 * i + q] += c * a[q];
+    }
+  }
+  free(tab);
+}
+
+void ora_kick64_vjp(int64_t n, const double *pos, const double *m, int64_t nslots,
+                    const int64_t *pnode_off, const int64_t *pnode_cnt, int law, double rsm,
+                    double fsrrmax, double c, int64_t nleaves, const int64_t *leaf_offset,
+                    const int64_t *leaf_count, const int64_t *list_ptr, const int64_t *list_idx,
+                    const double *u, double *xbar) {
+  double rmax2 = fsrrmax * fsrrmax;
+  int64_t ntab = n + nslots;
+  double *tab = (double *)malloc((size_t)(4 * ntab + 4) * sizeof(double));
+  double *xt = (double *)calloc((size_t)(3 * ntab + 3), sizeof(double));
+  tab64_fill(n, pos, m, nslots, pnode_off, pnode_cnt, tab);
+#ifdef _OPENMP
+#pragma omp parallel for schedule(dynamic, 4)
+#endif
+  for (int64_t l = 0; l < nleaves; ++l) {
+    for (int64_t i = leaf_offset[l]; i < leaf_offset[l] + leaf_count[l]; ++i) {
+      const double *ui = u + 3 * i;
+      double acc[3] = {0, 0, 0};
+      for (int64_t k = list_ptr[l]; k < list_ptr[l + 1]; ++k) {
+        int64_t e = list_idx[k];
+        if (e == i) continue;
+        double d[3] = {tab[4 * e] - tab[4 * i], tab[4 * e + 1] - tab[4 * i + 1],
+                       tab[4 * e + 2] - tab[4 * i + 2]};
+        double wg, wgp;
+        if (!pair_terms(law, rsm, rmax2, tab[4 * i + 3], tab[4 * e + 3], d, &wg, &wgp)) continue;
+        double du = d[0] * ui[0] + d[1] * ui[1] + d[2] * ui[2];
+        for (int a = 0; a < 3; ++a) {
+          double v = c * (wg * ui[a] + 2.0 * wgp * du * d[a]);
+          acc[a] -= v;
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+          xt[3 * e + a] += v;
+        }
+      }
+      for (int a = 0; a < 3; ++a) {
+#ifdef _OPENMP
+#pragma omp atomic
+#endif
+        xt[3 * i + a] += acc[a];
+      }
+    }
+  }
+  for (int64_t k = 0; k < n; ++k)
+    for (int a = 0; a < 3; ++a) xbar[3 * k + a] += xt[3 * k + a];
+  for (int64_t t = 0; t < nslots; ++t) {
+    const double *g = xt + 3 * (n + t);
+    double M = tab[4 * (n + t) + 3];
+    if (M == 0 || (g[0] == 0 && g[1] == 0 && g[2] == 0)) continue;
+    for (int64_t k = pnode_off[t]; k < pnode_off[t] + pnode_cnt[t]; ++k)
+      for (int a = 0; a < 3; ++a) xbar[3 * k + a] += m[k] / M * g[a];
+  }
+  free(xt);
+  free(tab);
+}
+
 typedef struct occ_t { int64_t leaf, pos; } occ_t;
 
 void ora_fd_fp64_tab(int64_t n, const float *tab, int64_t ntab, const int64_t *pnode_off,

@@ -140,6 +140,24 @@ void ora_fd_fp64_tab(int64_t n, const float *tab, int64_t ntab, const int64_t *p
                      const int64_t *list_ptr, const int64_t *list_idx, const double *u,
                      int64_t nsamples, const int64_t *samples, double h, double *fd, int32_t *near);
 
+/* FP64 kick over lists of table indices with positions in FP64 (pos: n x 3,
+ * tree order; m: masses).  Table entries >= n are monopole pseudo-particles at
+ * the FP64 centre of mass of their node's particles (node slot t = idx - n,
+ * particle range pnode_off/pnode_cnt); self entries skipped.
+ * dv (n x 3) += c m_i sum_j m_j g(r2) d over the cutoff. */
+void ora_kick64(int64_t n, const double *pos, const double *m, int64_t nslots,
+                const int64_t *pnode_off, const int64_t *pnode_cnt, int law, double rsm,
+                double fsrrmax, double c, int64_t nleaves, const int64_t *leaf_offset,
+                const int64_t *leaf_count, const int64_t *list_ptr, const int64_t *list_idx,
+                double *dv);
+/* Its vector-Jacobian product: xbar (n x 3) += (d dv / d pos)^T u, the
+ * centre-of-mass chain rule included. */
+void ora_kick64_vjp(int64_t n, const double *pos, const double *m, int64_t nslots,
+                    const int64_t *pnode_off, const int64_t *pnode_cnt, int law, double rsm,
+                    double fsrrmax, double c, int64_t nleaves, const int64_t *leaf_offset,
+                    const int64_t *leaf_count, const int64_t *list_ptr, const int64_t *list_idx,
+                    const double *u, double *xbar);
+
 /* Particles::map1 (src/cpu/Particles.cxx:732-758): x += prefactor*tau*v. */
 void ora_map1(int64_t n, float *x, float *y, float *z, const float *vx,
               const float *vy, const float *vz, float alpha, float pp,

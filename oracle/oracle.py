@@ -159,6 +159,10 @@ class Oracle:
                                         pi64, pi64, pi64, pd, i64, pi64, f64, pd,
                                         C.POINTER(C.c_int32)]
         lib.ora_map1.argtypes = [i64, pf, pf, pf, pf, pf, pf, f32, f32, f32, f32]
+        kick64 = [i64, pd, pd, i64, pi64, pi64, C.c_int, f64, f64, f64, i64, pi64, pi64, pi64,
+                  pi64]
+        lib.ora_kick64.argtypes = kick64 + [pd]
+        lib.ora_kick64_vjp.argtypes = kick64 + [pd, pd]
         lib.ora_resort.restype = i64
         lib.ora_resort.argtypes = [i64, C.POINTER(C.c_int), pf, pf, pf, pf, pf, pf, pf, pf, pi64, pu16]
 
@@ -236,6 +240,89 @@ class Oracle:
                                  len(smp), _ptr(smp, C.c_int64), h, _ptr(fd, C.c_double),
                                  near.ctypes.data_as(C.POINTER(C.c_int32)))
         return fd, near.astype(bool)
+
+    # -- FP64 multi-step checker --------------------------------------------
+    def kick64(self, pos, m, tape, c, law=LAW_POLY6, rsm=0.1, fsrrmax=3.116326355):
+        """FP64 kick over one tape (tree order): dv (n x 3)."""
+        n = len(m)
+        dv = np.zeros((n, 3))
+        self.lib.ora_kick64(n, *self._k64args(pos, m, tape, law, rsm, fsrrmax, c),
+                            _ptr(dv, C.c_double))
+        return dv
+
+    def kick64_vjp(self, pos, m, tape, c, u, law=LAW_POLY6, rsm=0.1, fsrrmax=3.116326355):
+        """(d dv / d pos)^T u for kick64, n x 3 (tree order)."""
+        n = len(m)
+        u = np.ascontiguousarray(u, np.float64)
+        xb = np.zeros((n, 3))
+        self.lib.ora_kick64_vjp(n, *self._k64args(pos, m, tape, law, rsm, fsrrmax, c),
+                                _ptr(u, C.c_double), _ptr(xb, C.c_double))
+        return xb
+
+    def _k64args(self, pos, m, tape, law, rsm, fsrrmax, c):
+        self._keep = [np.ascontiguousarray(pos, np.float64), np.ascontiguousarray(m, np.float64)]
+        self._keep += [np.ascontiguousarray(tape[k], np.int64)
+                       for k in ("noff", "ncnt", "off", "cnt", "ptr", "idx")]
+        pos, m, noff, ncnt, off, cnt, ptr, idx = self._keep
+        return (_ptr(pos, C.c_double), _ptr(m, C.c_double), len(noff), _ptr(noff, C.c_int64),
+                _ptr(ncnt, C.c_int64), law, float(np.float32(rsm)), float(np.float32(fsrrmax)),
+                float(c), len(off), _ptr(off, C.c_int64), _ptr(cnt, C.c_int64),
+                _ptr(ptr, C.c_int64), _ptr(idx, C.c_int64))
+
+    def stream_factor(self, alpha, pp, tau, adot) -> float:
+        """map1's float factor pt (x += pt v), from the restated map1."""
+        z = np.zeros(1, np.float32)
+        one = np.ones(1, np.float32)
+        x, y, zz = z.copy(), z.copy(), z.copy()
+        self.lib.ora_map1(1, _ptr(x, C.c_float), _ptr(y, C.c_float), _ptr(zz, C.c_float),
+                          _ptr(one, C.c_float), _ptr(one.copy(), C.c_float),
+                          _ptr(one.copy(), C.c_float), alpha, pp, tau, adot)
+        return float(x[0])
+
+    def multistep64(self, x0, v0, m, steps, nsub, tapes, xbar=None, vbar=None, kick_pos=None,
+                    law=LAW_POLY6, rsm=0.1, fsrrmax=3.116326355):
+        """FP64 restatement of the sub-cycled short-range map (map1, kick,
+        map1; nsub per PM step) with every kick's tree and lists frozen to
+        `tapes` (one per kick in forward order: perm, node ranges, leaves and
+        lists in tree order).  Caller-order n x 3 arrays.
+
+        Returns the final (x, v) and, when cotangents (xbar, vbar) are given,
+        also L = sum xbar.x_T + vbar.v_T and its FP64 gradient (x0bar, v0bar).
+        kick_pos: optional positions of every kick (n x 3 each) at which the
+        reverse pass evaluates the kick's VJP (default: this FP64 trajectory).
+        """
+        x = np.array(x0, np.float64)
+        v = np.array(v0, np.float64)
+        m = np.asarray(m, np.float64)
+        pts = [self.stream_factor(st.alpha, st.pp, st.tau_sub, st.adot) for st in steps]
+        traj = []
+        k = 0
+        for s, st in enumerate(steps):
+            for _ in range(nsub):
+                x += pts[s] * v
+                traj.append(x.copy())
+                t = tapes[k]
+                perm = t["perm"]
+                v[perm] += self.kick64(x[perm], m[perm], t, st.fcoeff, law, rsm, fsrrmax)
+                x += pts[s] * v
+                k += 1
+        if xbar is None:
+            return x, v
+        L = float((np.asarray(xbar) * x).sum() + (np.asarray(vbar) * v).sum())
+        xb = np.array(xbar, np.float64)
+        vb = np.array(vbar, np.float64)
+        for s in reversed(range(len(steps))):
+            st = steps[s]
+            for _ in range(nsub):
+                k -= 1
+                vb += pts[s] * xb
+                t = tapes[k]
+                perm = t["perm"]
+                xk = traj[k] if kick_pos is None else np.asarray(kick_pos[k], np.float64)
+                xb[perm] += self.kick64_vjp(xk[perm], m[perm], t, st.fcoeff, vb[perm], law, rsm,
+                                            fsrrmax)
+                vb += pts[s] * xb
+        return x, v, L, xb, vb
 
     def map1(self, p, alpha, pp, tau, adot):
         self.lib.ora_map1(p.n, *[_ptr(getattr(p, k), C.c_float) for k in ("x", "y", "z", "vx", "vy", "vz")],

@@ -1,0 +1,213 @@
+"""Multi-step adjoint of the sub-cycled short-range map (multistep.py).
+
+The benchmark's multi-box adjoint case: boxes of Zel'dovich particles, 10 PM
+steps x 5 sub-cycles (map1, kick, map1), checkpoints every 2 PM steps.  The
+GPU reverse pass is compared with an FP64 restatement of the same map over
+the same frozen trees and lists (oracle.multistep64): its gradient along the
+GPU trajectory (rms 1e-5 / max 1e-3 of the rms) and FP64 central differences
+(h = 1e-4 grid units) of the FP64 map on 64 particles per box (relative 1e-4
+of the larger of the sample's gradient norm and the rms gradient).  Samples
+whose difference quotient changes between h and h/2 saw a list entry cross
+the cutoff (the law steps there) and are set aside; at most a quarter may be.
+Each difference quotient is refined by Richardson extrapolation over h, h/2
+and h/4 (the softened law is stiff at small separations).
+"""
+import dataclasses
+
+import numpy as np
+import pytest
+
+import hsr
+import multistep
+import synth
+from hsr_testutil import force_errors
+
+ADJ_TOL = 1e-4
+
+
+def _host_tape(x, m, kp):
+    """Tree and lists of the host build at positions x (no pseudo-particles:
+    opening angle 0)."""
+    n = len(m)
+    f = lambda a: np.ascontiguousarray(a, np.float32)
+    p = synth.Particles(x=f(x[:, 0]), y=f(x[:, 1]), z=f(x[:, 2]), vx=np.zeros(n, np.float32),
+                        vy=np.zeros(n, np.float32), vz=np.zeros(n, np.float32), mass=f(m),
+                        phi=np.zeros(n, np.float32), id=np.arange(n, dtype=np.int64),
+                        mask=np.zeros(n, np.uint16))
+    L = hsr.HostLists(p, kp)
+    off, cnt, ptr, _ = L.get()
+    none = np.zeros(0, np.int64)
+    return dict(perm=p.id.copy(), noff=none, ncnt=none, off=off, cnt=cnt, ptr=ptr, idx=L.index())
+
+
+def _fd(O, x0, v0, m, steps, nsub, tapes, xbar, vbar, k, d, h):
+    def L(step):
+        x = x0.copy()
+        x[k] += step * d
+        _, _, val, _, _ = O.multistep64(x, v0, m, steps, nsub, tapes, xbar, vbar)
+        return val
+    return (L(h) - L(-h)) / (2 * h)
+
+
+def _check_fd(O, x0, v0, m, steps, nsub, tapes, xbar, vbar, grad, samples, h, rng):
+    """Directional central differences at h, h/2 and h/4, each pair combined
+    by Richardson extrapolation (error O(h^4)); a sample whose two
+    extrapolations disagree saw a discontinuity (an entry crossing the
+    cutoff) and is set aside."""
+    rms = np.sqrt((grad ** 2).sum(1).mean())
+    bad = skipped = 0
+    for k in samples:
+        d = rng.standard_normal(3)
+        d /= np.linalg.norm(d)
+        f = [_fd(O, x0, v0, m, steps, nsub, tapes, xbar, vbar, k, d, h / 2 ** i) for i in range(3)]
+        r1, r2 = (4 * f[1] - f[0]) / 3, (4 * f[2] - f[1]) / 3
+        scale = max(np.linalg.norm(grad[k]), rms)
+        if abs(r1 - r2) > 0.1 * ADJ_TOL * scale:
+            skipped += 1
+            continue
+        bad += abs(grad[k] @ d - r2) > ADJ_TOL * scale
+    return bad, skipped
+
+
+def test_fp64_multistep_gradient_matches_fd(hsr_lib, oracle_lib):
+    """The FP64 checker itself: its reverse pass against its own central
+    differences (host-built trees, opening angle 0)."""
+    O = oracle_lib
+    p = synth.random_box(1000, 10.0, 11)
+    kp = synth.kick_params(p, nd=16, open_angle=0.0)
+    kp.min_force, kp.max_force = (-1.0,) * 3, (10.0,) * 3
+    steps = [multistep.StepParams(alpha=1.0, pp=0.5, adot=1.0, tau_sub=0.02, fcoeff=0.03),
+             multistep.StepParams(alpha=1.0, pp=0.6, adot=1.0, tau_sub=0.02, fcoeff=0.025)]
+    nsub = 2
+    x = np.stack([p.x, p.y, p.z], 1).astype(np.float64)
+    v = 0.1 * np.stack([p.vx, p.vy, p.vz], 1).astype(np.float64)
+    m = p.mass.astype(np.float64)
+    # trees and lists along the FP64 trajectory
+    tapes = []
+    xx, vv = x.copy(), v.copy()
+    for st in steps:
+        pt = O.stream_factor(st.alpha, st.pp, st.tau_sub, st.adot)
+        for _ in range(nsub):
+            xx += pt * vv
+            t = _host_tape(xx, m, dataclasses.replace(kp, fcoeff=st.fcoeff))
+            tapes.append(t)
+            vv[t["perm"]] += O.kick64(xx[t["perm"]], m[t["perm"]], t, st.fcoeff)
+            xx += pt * vv
+    rng = np.random.default_rng(4)
+    xbar, vbar = rng.standard_normal(x.shape), rng.standard_normal(v.shape)
+    xT, vT, L, gx, gv = O.multistep64(x, v, m, steps, nsub, tapes, xbar, vbar)
+    assert np.allclose(xT, xx) and np.allclose(vT, vv)
+    smp = rng.choice(len(m), 24, replace=False)
+    bad, skipped = _check_fd(O, x, v, m, steps, nsub, tapes, xbar, vbar, gx, smp, 1e-4, rng)
+    assert skipped <= len(smp) // 4 and bad == 0, (bad, skipped)
+    # the velocity gradient: directional differences in v0
+    k = int(smp[0])
+    d = np.array([0.3, -0.5, 0.8]) / np.linalg.norm([0.3, -0.5, 0.8])
+    def Lv(step):
+        vv0 = v.copy()
+        vv0[k] += step * d
+        return O.multistep64(x, vv0, m, steps, nsub, tapes, xbar, vbar)[2]
+    fdv = (Lv(1e-4) - Lv(-1e-4)) / 2e-4
+    assert abs(fdv - gv[k] @ d) <= ADJ_TOL * max(np.linalg.norm(gv[k]), 1.0)
+
+
+def _boxes(nbox, ng, seed0):
+    return [synth.zeldovich_box(ng, z=50.0, seed=seed0 + b) for b in range(nbox)]
+
+
+def _tape_of(ctx, n):
+    tree = ctx.tree()
+    off, cnt, ptr, _ = ctx.lists()
+    return dict(perm=ctx.last_perm(n), noff=tree["offset"], ncnt=tree["count"], off=off,
+                cnt=cnt, ptr=ptr, idx=ctx.lists_index())
+
+
+@pytest.mark.gpu
+def test_multistep_adjoint_vs_fp64_and_fd(ctx, oracle_lib):
+    """2 boxes x 12^3 at z = 50, 10 PM steps x 5 sub-cycles, checkpoints
+    every 2 steps, opening angle 0.1 (pseudo-particles on)."""
+    torch = pytest.importorskip("torch")
+    O = oracle_lib
+    nsteps, nsub = 10, 5
+    steps = multistep.schedule(50.0, 10.0, nsteps, nsub)
+    boxes = _boxes(2, 12, 70)
+    kps = [synth.kick_params(b, nd=64) for b in boxes]
+    ms = multistep.MultiStep(ctx, kps, steps, nsub, checkpoint_every=2)
+    tapes, kick_x = {}, {}
+
+    def on_tape(b, s, j, c, x1):
+        n = boxes[b].n
+        tapes[(b, s, j)] = _tape_of(c, n)
+        kick_x[(b, s, j)] = np.stack([t.cpu().numpy() for t in x1], 1).astype(np.float64)
+    ms.on_tape = on_tape
+    rng = np.random.default_rng(8)
+    for b, p in enumerate(boxes):
+        S0 = multistep.box_state(p)
+        n = p.n
+        xbar = rng.standard_normal((n, 3)).astype(np.float32)
+        vbar = rng.standard_normal((n, 3)).astype(np.float32)
+        tx = [torch.from_numpy(np.ascontiguousarray(xbar[:, d])).cuda() for d in range(3)]
+        tv = [torch.from_numpy(np.ascontiguousarray(vbar[:, d])).cuda() for d in range(3)]
+        gx_t, gv_t = ms.adjoint_box(b, S0, tx, tv)
+        gx = np.stack([t.cpu().numpy() for t in gx_t], 1).astype(np.float64)
+        gv = np.stack([t.cpu().numpy() for t in gv_t], 1).astype(np.float64)
+        order = [(b, s, j) for s in range(nsteps) for j in range(nsub)]
+        tl = [tapes[k] for k in order]
+        xl = [kick_x[k] for k in order]
+        x0 = np.stack([p.x, p.y, p.z], 1).astype(np.float64)
+        v0 = np.stack([p.vx, p.vy, p.vz], 1).astype(np.float64)
+        m = p.mass.astype(np.float64)
+        # FP64 gradient along the GPU's own trajectory
+        _, _, _, rx, rv = O.multistep64(x0, v0, m, steps, nsub, tl, xbar, vbar, kick_pos=xl)
+        for g, r in ((gx, rx), (gv, rv)):
+            rms, mx = force_errors(g, r)
+            assert rms <= 1e-5 and mx <= 1e-3, (b, rms, mx)
+        # FP64 differences of the FP64 map (frozen trees) on 64 particles
+        inner = np.flatnonzero(p.mask == 0) if np.any(p.mask == 0) else np.arange(n)
+        smp = rng.choice(inner, 64, replace=False)
+        _, _, _, fx, _ = O.multistep64(x0, v0, m, steps, nsub, tl, xbar, vbar)
+        bad, skipped = _check_fd(O, x0, v0, m, steps, nsub, tl, xbar, vbar, fx, smp, 1e-4, rng)
+        assert skipped <= 16 and bad == 0, (b, bad, skipped)
+        # and the GPU gradient against the same differences' gradient
+        rms, mx = force_errors(gx[smp], fx[smp])
+        assert rms <= ADJ_TOL, (b, rms)
+    assert ms.kicks == multistep.kicks_per_box(nsteps, nsub) * 2
+
+
+@pytest.mark.gpu
+def test_checkpointed_equals_stored_and_is_linear(ctx):
+    """Checkpointed and fully stored reverse passes agree (the recomputed
+    trajectory is the forward one), and the adjoint is linear in the
+    cotangent."""
+    torch = pytest.importorskip("torch")
+    nsteps, nsub = 4, 5
+    steps = multistep.schedule(50.0, 30.0, nsteps, nsub)
+    p = _boxes(1, 24, 90)[0]
+    kp = synth.kick_params(p, nd=128)
+    S0 = multistep.box_state(p)
+    rng = np.random.default_rng(2)
+    cot = lambda: [torch.from_numpy(rng.standard_normal(p.n).astype(np.float32)).cuda()
+                   for _ in range(3)]
+    xa, va, xb_, vb_ = cot(), cot(), cot(), cot()
+    a = multistep.MultiStep(ctx, [kp], steps, nsub, checkpoint_every=1)
+    b = multistep.MultiStep(ctx, [kp], steps, nsub, checkpoint_every=None)
+    ga = a.adjoint_box(0, S0, xa, va)
+    gb = b.adjoint_box(0, S0, xa, va)
+    for u, w in zip(ga[0] + ga[1], gb[0] + gb[1]):
+        rms, mx = force_errors(u.double().cpu().numpy()[:, None], w.double().cpu().numpy()[:, None])
+        assert rms <= 1e-6, rms
+    # linearity: adj(2 u + w) = 2 adj(u) + adj(w)
+    g1 = b.adjoint_box(0, S0, xb_, vb_)
+    comb = b.adjoint_box(0, S0, [2 * s + t for s, t in zip(xa, xb_)],
+                         [2 * s + t for s, t in zip(va, vb_)])
+    for c_, u, w in zip(comb[0] + comb[1], gb[0] + gb[1], g1[0] + g1[1]):
+        ref = (2 * u.double() + w.double()).cpu().numpy()[:, None]
+        rms, _ = force_errors(c_.double().cpu().numpy()[:, None], ref)
+        assert rms <= 1e-5, rms
+    # the forward map alone reproduces the state the reverse pass started from
+    S = S0.clone()
+    a.forward_box(0, S)
+    S2 = S0.clone()
+    a.forward_box(0, S2)
+    for u, w in zip(S.x + S.v, S2.x + S2.v):
+        assert torch.equal(u, w)
