@@ -1163,10 +1163,15 @@ void ora_kick64(int64_t n, const double *pos, const double *m, int64_t nslots,
                 const int64_t *pnode_off, const int64_t *pnode_cnt, int law, double rsm,
                 double fsrrmax, double c, int64_t nleaves, const int64_t *leaf_offset,
                 const int64_t *leaf_count, const int64_t *list_ptr, const int64_t *list_idx,
-                double *dv) {
+                const double *pos_cut, double *dv) {
   double rmax2 = fsrrmax * fsrrmax;
   double *tab = (double *)malloc((size_t)(4 * (n + nslots) + 4) * sizeof(double));
+  double *tcut = NULL;
   tab64_fill(n, pos, m, nslots, pnode_off, pnode_cnt, tab);
+  if (pos_cut) {
+    tcut = (double *)malloc((size_t)(4 * (n + nslots) + 4) * sizeof(double));
+    tab64_fill(n, pos_cut, m, nslots, pnode_off, pnode_cnt, tcut);
+  }
 #ifdef _OPENMP
 #pragma omp parallel for schedule(dynamic, 4)
 #endif
@@ -1179,13 +1184,24 @@ void ora_kick64(int64_t n, const double *pos, const double *m, int64_t nslots,
         double d[3] = {tab[4 * e] - tab[4 * i], tab[4 * e + 1] - tab[4 * i + 1],
                        tab[4 * e + 2] - tab[4 * i + 2]};
         double wg, wgp;
-        if (!pair_terms(law, rsm, rmax2, tab[4 * i + 3], tab[4 * e + 3], d, &wg, &wgp)) continue;
+        if (tcut) {
+          /* the cutoff decided at the reference positions, the law at these */
+          double dc[3] = {tcut[4 * e] - tcut[4 * i], tcut[4 * e + 1] - tcut[4 * i + 1],
+                          tcut[4 * e + 2] - tcut[4 * i + 2]};
+          if (!pair_terms(law, rsm, rmax2, tab[4 * i + 3], tab[4 * e + 3], dc, &wg, &wgp)) continue;
+          double mm = tab[4 * e + 3] * (law == ORA_LAW_POLY5_STEP16 ? 1.0 : tab[4 * i + 3]);
+          double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+          wg = mm * ora_law_f64(law, rsm, r2);
+        } else if (!pair_terms(law, rsm, rmax2, tab[4 * i + 3], tab[4 * e + 3], d, &wg, &wgp)) {
+          continue;
+        }
         for (int q = 0; q < 3; ++q) a[q] += wg * d[q];
       }
       for (int q = 0; q < 3; ++q) dv[3 * i + q] += c * a[q];
     }
   }
   free(tab);
+  free(tcut);
 }
 
 void ora_kick64_vjp(int64_t n, const double *pos, const double *m, int64_t nslots,

@@ -144,12 +144,14 @@ void ora_fd_fp64_tab(int64_t n, const float *tab, int64_t ntab, const int64_t *p
  * tree order; m: masses).  Table entries >= n are monopole pseudo-particles at
  * the FP64 centre of mass of their node's particles (node slot t = idx - n,
  * particle range pnode_off/pnode_cnt); self entries skipped.
- * dv (n x 3) += c m_i sum_j m_j g(r2) d over the cutoff. */
+ * dv (n x 3) += c m_i sum_j m_j g(r2) d over the cutoff.  pos_cut, when not
+ * NULL, holds reference positions (n x 3) on which each pair's cutoff test is
+ * made instead (the map with its cutoff mask frozen, for difference checks). */
 void ora_kick64(int64_t n, const double *pos, const double *m, int64_t nslots,
                 const int64_t *pnode_off, const int64_t *pnode_cnt, int law, double rsm,
                 double fsrrmax, double c, int64_t nleaves, const int64_t *leaf_offset,
                 const int64_t *leaf_count, const int64_t *list_ptr, const int64_t *list_idx,
-                double *dv);
+                const double *pos_cut, double *dv);
 /* Its vector-Jacobian product: xbar (n x 3) += (d dv / d pos)^T u, the
  * centre-of-mass chain rule included. */
 void ora_kick64_vjp(int64_t n, const double *pos, const double *m, int64_t nslots,

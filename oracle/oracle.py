@@ -161,7 +161,7 @@ class Oracle:
         lib.ora_map1.argtypes = [i64, pf, pf, pf, pf, pf, pf, f32, f32, f32, f32]
         kick64 = [i64, pd, pd, i64, pi64, pi64, C.c_int, f64, f64, f64, i64, pi64, pi64, pi64,
                   pi64]
-        lib.ora_kick64.argtypes = kick64 + [pd]
+        lib.ora_kick64.argtypes = kick64 + [pd, pd]
         lib.ora_kick64_vjp.argtypes = kick64 + [pd, pd]
         lib.ora_resort.restype = i64
         lib.ora_resort.argtypes = [i64, C.POINTER(C.c_int), pf, pf, pf, pf, pf, pf, pf, pf, pi64, pu16]
@@ -242,12 +242,15 @@ class Oracle:
         return fd, near.astype(bool)
 
     # -- FP64 multi-step checker --------------------------------------------
-    def kick64(self, pos, m, tape, c, law=LAW_POLY6, rsm=0.1, fsrrmax=3.116326355):
-        """FP64 kick over one tape (tree order): dv (n x 3)."""
+    def kick64(self, pos, m, tape, c, law=LAW_POLY6, rsm=0.1, fsrrmax=3.116326355,
+               pos_cut=None):
+        """FP64 kick over one tape (tree order): dv (n x 3).  pos_cut: the
+        cutoff of every pair decided at these positions instead."""
         n = len(m)
         dv = np.zeros((n, 3))
+        pc = None if pos_cut is None else np.ascontiguousarray(pos_cut, np.float64)
         self.lib.ora_kick64(n, *self._k64args(pos, m, tape, law, rsm, fsrrmax, c),
-                            _ptr(dv, C.c_double))
+                            None if pc is None else _ptr(pc, C.c_double), _ptr(dv, C.c_double))
         return dv
 
     def kick64_vjp(self, pos, m, tape, c, u, law=LAW_POLY6, rsm=0.1, fsrrmax=3.116326355):
@@ -280,7 +283,7 @@ class Oracle:
         return float(x[0])
 
     def multistep64(self, x0, v0, m, steps, nsub, tapes, xbar=None, vbar=None, kick_pos=None,
-                    law=LAW_POLY6, rsm=0.1, fsrrmax=3.116326355):
+                    law=LAW_POLY6, rsm=0.1, fsrrmax=3.116326355, cut_pos=None, traj_out=None):
         """FP64 restatement of the sub-cycled short-range map (map1, kick,
         map1; nsub per PM step) with every kick's tree and lists frozen to
         `tapes` (one per kick in forward order: perm, node ranges, leaves and
@@ -290,6 +293,9 @@ class Oracle:
         also L = sum xbar.x_T + vbar.v_T and its FP64 gradient (x0bar, v0bar).
         kick_pos: optional positions of every kick (n x 3 each) at which the
         reverse pass evaluates the kick's VJP (default: this FP64 trajectory).
+        cut_pos: optional positions of every kick on which the pairs' cutoff is
+        decided (the map with its cutoff mask frozen); traj_out, a list, receives
+        this run's kick positions.
         """
         x = np.array(x0, np.float64)
         v = np.array(v0, np.float64)
@@ -303,9 +309,12 @@ class Oracle:
                 traj.append(x.copy())
                 t = tapes[k]
                 perm = t["perm"]
-                v[perm] += self.kick64(x[perm], m[perm], t, st.fcoeff, law, rsm, fsrrmax)
+                pc = None if cut_pos is None else np.asarray(cut_pos[k], np.float64)[perm]
+                v[perm] += self.kick64(x[perm], m[perm], t, st.fcoeff, law, rsm, fsrrmax, pc)
                 x += pts[s] * v
                 k += 1
+        if traj_out is not None:
+            traj_out.extend(traj)
         if xbar is None:
             return x, v
         L = float((np.asarray(xbar) * x).sum() + (np.asarray(vbar) * v).sum())
