@@ -1,0 +1,54 @@
+"""Runs the short-range kick of one synthetic workload a few times through the
+C ABI and prints each call's phase statistics as JSON: a fixed, short launch
+sequence for profilers (ncu's launch lists and kernel captures).
+
+    python hacc-coral_gb300/profile_kick.py --workload zeldovich --ng 128 --reps 2
+    python hacc-coral_gb300/profile_kick.py --workload clustered --ng 256 --shape batched-32
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+if HERE not in sys.path:
+    sys.path.insert(0, HERE)
+
+import hsr  # noqa: E402
+import synth  # noqa: E402
+
+KEYS = ("t_total_ms", "t_h2d_ms", "t_build_ms", "t_walk_ms", "t_force_ms", "t_d2h_ms",
+        "n", "nodes", "processed_leaves", "list_entries", "pairs", "evaluated_pairs",
+        "work_items", "cm_fallbacks", "kernel_launches")
+
+
+def main(argv=None) -> int:
+    ap = argparse.ArgumentParser(description=__doc__.splitlines()[0])
+    ap.add_argument("--workload", choices=["zeldovich", "clustered"], default="zeldovich")
+    ap.add_argument("--ng", type=int, default=128)
+    ap.add_argument("--z", type=float, default=50.0)
+    ap.add_argument("--nd", type=int, default=128)
+    ap.add_argument("--reps", type=int, default=2)
+    ap.add_argument("--shape", default="batched-32",
+                    help="plain-32|plain-64|plain-128|batched-16|batched-32")
+    ap.add_argument("--device", type=int, default=0)
+    a = ap.parse_args(argv)
+    kind, num = a.shape.split("-")
+    p = synth.clustered_box(a.ng) if a.workload == "clustered" else synth.zeldovich_box(a.ng, z=a.z)
+    kp = synth.kick_params(p, nd=a.nd)
+    with hsr.Context(a.device) as ctx:
+        if kind == "plain":
+            ctx.set_tune("plain", int(num), 32)
+        else:
+            ctx.set_tune("batched", 128, int(num))
+        for r in range(a.reps):
+            st = ctx.rcb_kick(p.copy(), kp, kernel=hsr.KERNEL_AUTO)
+            print(json.dumps({"rep": r, "workload": f"{a.workload}{a.ng}", "shape": a.shape,
+                              **{k: st[k] for k in KEYS}}), flush=True)
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
