@@ -43,7 +43,6 @@ __device__ __forceinline__ int lsb_exp(float t) {
 constexpr int kChunk = 4096;        // elements per statistics / partition chunk
 constexpr int kChunkThreads = 256;  // threads per chunk (16 elements each)
 constexpr int kPer = kChunk / kChunkThreads;
-constexpr int kPartDoubles = 16;    // per-chunk partial record
 constexpr int kWalkStack = 256;     // DFS stack of the list walk
 
 enum { C_NCHUNK = 0, C_NSPLIT = 1, C_NFALLBACK = 2, C_NLEAF = 3, C_NSEG = 4, C_NENT = 5,
@@ -183,8 +182,68 @@ __device__ __forceinline__ ChunkRange chunk_range(const DNode *nodes, const int3
   return r;
 }
 
-// Partial sums of one chunk: sum w*x, sum |w*x| (x, y, z), sum w, sum |w|,
-// and the bounding box.  Fixed thread-to-element map and reduction tree.
+// Exact sums in 128-bit fixed point.  A float term t = M 2^E (M < 2^24) is
+// the integer M 2^(E - kFix) in units of 2^kFix: exact for |t| >= 2^(kFix+23)
+// in lsb terms (lsb exponent >= kFix), truncated toward zero below (|t| <
+// 2^(kFix+24), counted in the error bound).  Terms up to 2^kFixMax keep a sum
+// of 2^31 of them below 2^125; a larger term flags the chunk (its node takes
+// the sequential sum).  Integer adds avoid the FP64 pipe, which runs at a
+// small fraction of the FP32 rate on this part.
+constexpr int kFix = -64;
+constexpr int kFixMaxShift = 70;  // |t| < 2^(70 + 24 + kFix) = 2^30
+
+__device__ __forceinline__ __int128 to_fix(float t, bool &overflow) {
+  const uint32_t b = __float_as_uint(t);
+  const uint32_t a = b & 0x7fffffffu;
+  int e = int(a >> 23);
+  uint32_t m = a & 0x7fffffu;
+  if (e == 0) e = 1;
+  else m |= 0x800000u;
+  if (e == 255) {
+    overflow = true;
+    return 0;
+  }
+  const int sh = e - 150 - kFix;
+  __int128 v;
+  if (sh >= 0) {
+    if (sh > kFixMaxShift) overflow = true;
+    v = __int128(m) << min(sh, kFixMaxShift);
+  } else {
+    v = sh > -32 ? __int128(m >> (-sh)) : __int128(0);
+  }
+  return (b >> 31) ? -v : v;
+}
+
+__device__ __forceinline__ __int128 shfl_xor_i128(__int128 v, int o) {
+  const unsigned long long lo = (unsigned long long)v, hi = (unsigned long long)(v >> 64);
+  const unsigned long long l2 = __shfl_xor_sync(0xffffffffu, lo, o);
+  const unsigned long long h2 = __shfl_xor_sync(0xffffffffu, hi, o);
+  return (__int128(h2) << 64) | __int128(l2);
+}
+
+// Correctly rounded double of v 2^kFix.
+__device__ double fix_to_double(__int128 v) {
+  const bool neg = v < 0;
+  unsigned __int128 u = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
+  int k = 0;
+  while ((u >> 63) != 0) {  // keep 63 bits, the shifted-out ones as a sticky bit
+    const unsigned __int128 sticky = u & 1;
+    u = (u >> 1) | sticky;
+    ++k;
+  }
+  const double d = __ull2double_rn((unsigned long long)u);
+  const double r = ldexp(d, k + kFix);
+  return neg ? -r : r;
+}
+
+// Layout of a chunk's partial record (in 8-byte words): sums of the terms
+// (x, y, z, m) as 4 x int128, upper bounds of the sums of |terms| (4 doubles),
+// the bounding box (6 floats), the least significant exponents (4 ints) and
+// an overflow flag.
+constexpr int kPartWords = 18;
+
+// Partial sums of one chunk and its bounding box.  Fixed thread-to-element
+// map and reduction tree.
 __global__ void __launch_bounds__(kChunkThreads)
     k_stats_partial(const float4 *__restrict__ pos, const DNode *nodes,
                     const int32_t *chunk_node, const int64_t *chunk_base, int32_t nb,
@@ -192,34 +251,31 @@ __global__ void __launch_bounds__(kChunkThreads)
   const int64_t chunk = blockIdx.x;
   if (chunk >= *nchunk) return;
   const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
-  double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  __int128 s[4] = {0, 0, 0, 0};
+  float fa[4] = {0.f, 0.f, 0.f, 0.f};
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   int emin[4] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX};
-  bool any = false;
+  bool ovf = false;
   for (int k = threadIdx.x; k < R.len; k += kChunkThreads) {
     const float4 p = pos[R.begin + k];
     const float w = p.w;
-    const float fx = fmul_(w, p.x), fy = fmul_(w, p.y), fz = fmul_(w, p.z);
-    emin[0] = min(emin[0], lsb_exp(fx));
-    emin[1] = min(emin[1], lsb_exp(fy));
-    emin[2] = min(emin[2], lsb_exp(fz));
-    emin[3] = min(emin[3], lsb_exp(w));
-    const double wx = double(fx), wy = double(fy), wz = double(fz);
-    s[0] += wx; s[1] += wy; s[2] += wz; s[3] += double(w);
-    s[4] += fabs(wx); s[5] += fabs(wy); s[6] += fabs(wz); s[7] += fabs(double(w));
-    if (!any) {
-      lo[0] = hi[0] = p.x; lo[1] = hi[1] = p.y; lo[2] = hi[2] = p.z;
-      any = true;
-    } else {
-      lo[0] = fminf(lo[0], p.x); hi[0] = fmaxf(hi[0], p.x);
-      lo[1] = fminf(lo[1], p.y); hi[1] = fmaxf(hi[1], p.y);
-      lo[2] = fminf(lo[2], p.z); hi[2] = fmaxf(hi[2], p.z);
-    }
-  }
-  // fminf/fmaxf ignore the +-INFINITY identity only if a real value exists;
-  // lanes without elements hold the identities, which min/max absorb.
+    const float t[4] = {fmul_(w, p.x), fmul_(w, p.y), fmul_(w, p.z), w};
 #pragma unroll
-  for (int q = 0; q < 8; ++q) s[q] = warp_sum(s[q]);
+    for (int q = 0; q < 4; ++q) {
+      emin[q] = min(emin[q], lsb_exp(t[q]));
+      s[q] += to_fix(t[q], ovf);
+      fa[q] = __fadd_ru(fa[q], fabsf(t[q]));
+    }
+    lo[0] = fminf(lo[0], p.x); hi[0] = fmaxf(hi[0], p.x);
+    lo[1] = fminf(lo[1], p.y); hi[1] = fmaxf(hi[1], p.y);
+    lo[2] = fminf(lo[2], p.z); hi[2] = fmaxf(hi[2], p.z);
+  }
+  double a[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    for (int o = 16; o > 0; o >>= 1) s[q] += shfl_xor_i128(s[q], o);
+    a[q] = warp_sum(double(fa[q]));
+  }
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     lo[d] = warp_min(lo[d]);
@@ -228,35 +284,57 @@ __global__ void __launch_bounds__(kChunkThreads)
 #pragma unroll
   for (int q = 0; q < 4; ++q)
     for (int o = 16; o > 0; o >>= 1) emin[q] = min(emin[q], __shfl_xor_sync(0xffffffffu, emin[q], o));
-  __shared__ int she[kChunkThreads / 32][4];
-  __shared__ double sh[kChunkThreads / 32][14];
+  const bool wovf = __any_sync(0xffffffffu, ovf);
+  __shared__ __int128 shs[kChunkThreads / 32][4];
+  __shared__ double sha[kChunkThreads / 32][4];
+  __shared__ float shb[kChunkThreads / 32][6];
+  __shared__ int she[kChunkThreads / 32][5];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (lane == 0) {
-    for (int q = 0; q < 8; ++q) sh[warp][q] = s[q];
-    for (int d = 0; d < 3; ++d) {
-      sh[warp][8 + d] = lo[d];
-      sh[warp][11 + d] = hi[d];
+    for (int q = 0; q < 4; ++q) {
+      shs[warp][q] = s[q];
+      sha[warp][q] = a[q];
+      she[warp][q] = emin[q];
     }
-    for (int q = 0; q < 4; ++q) she[warp][q] = emin[q];
+    for (int d = 0; d < 3; ++d) {
+      shb[warp][d] = lo[d];
+      shb[warp][3 + d] = hi[d];
+    }
+    she[warp][4] = wovf ? 1 : 0;
   }
   __syncthreads();
   if (threadIdx.x == 0) {
-    double t[14];
-    int e[4];
-    for (int q = 0; q < 14; ++q) t[q] = sh[0][q];
-    for (int q = 0; q < 4; ++q) e[q] = she[0][q];
-    for (int w = 1; w < kChunkThreads / 32; ++w) {
-      for (int q = 0; q < 8; ++q) t[q] += sh[w][q];
-      for (int d = 0; d < 3; ++d) {
-        t[8 + d] = fmin(t[8 + d], sh[w][8 + d]);
-        t[11 + d] = fmax(t[11 + d], sh[w][11 + d]);
-      }
-      for (int q = 0; q < 4; ++q) e[q] = min(e[q], she[w][q]);
+    __int128 ts[4];
+    double ta[4];
+    float tb[6];
+    int te[5];
+    for (int q = 0; q < 4; ++q) {
+      ts[q] = shs[0][q];
+      ta[q] = sha[0][q];
+      te[q] = she[0][q];
     }
-    double *o = part + chunk * kPartDoubles;
-    for (int q = 0; q < 14; ++q) o[q] = t[q];
-    int *oe = reinterpret_cast<int *>(o + 14);
-    for (int q = 0; q < 4; ++q) oe[q] = e[q];
+    for (int d = 0; d < 6; ++d) tb[d] = shb[0][d];
+    te[4] = she[0][4];
+    for (int w = 1; w < kChunkThreads / 32; ++w) {
+      for (int q = 0; q < 4; ++q) {
+        ts[q] += shs[w][q];
+        ta[q] += sha[w][q];
+        te[q] = min(te[q], she[w][q]);
+      }
+      for (int d = 0; d < 3; ++d) {
+        tb[d] = fminf(tb[d], shb[w][d]);
+        tb[3 + d] = fmaxf(tb[3 + d], shb[w][3 + d]);
+      }
+      te[4] |= she[w][4];
+    }
+    double *o = part + chunk * kPartWords;
+    __int128 *os = reinterpret_cast<__int128 *>(o);
+    for (int q = 0; q < 4; ++q) os[q] = ts[q];
+    for (int q = 0; q < 4; ++q) o[8 + q] = ta[q];
+    float *ob = reinterpret_cast<float *>(o + 12);
+    for (int d = 0; d < 6; ++d) ob[d] = tb[d];
+    int *oe = reinterpret_cast<int *>(o + 15);
+    for (int q = 0; q < 5; ++q) oe[q] = te[q];
   }
 }
 
@@ -279,8 +357,8 @@ __device__ bool certify(double sx, double bx, double sm, double bm, float *out) 
 }
 
 // One warp per node of the level: reduce the node's chunk partials, set the
-// bounding box and, where certified, the centre of mass; list the others for
-// the sequential fallback.
+// bounding box and, where decided, the centre of mass; list the others for
+// the tight certification and the sequential fallback.
 __global__ void k_stats_final(DNode *nodes, int32_t nb, int32_t ne, const int64_t *chunk_base,
                               const double *part, int32_t *fallback, int64_t *counters,
                               int32_t force_fallback) {
@@ -292,50 +370,69 @@ __global__ void k_stats_final(DNode *nodes, int32_t nb, int32_t ne, const int64_
   if (N.count <= 0) return;
   const int64_t cb = chunk_base[wid];
   const int64_t nc = (int64_t(N.count) + kChunk - 1) / kChunk;
-  double s[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  __int128 s[4] = {0, 0, 0, 0};
+  double a[4] = {0, 0, 0, 0};
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   int emin[4] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX};
+  int ovf = 0;
   for (int64_t c = lane; c < nc; c += 32) {
-    const double *p = part + (cb + c) * kPartDoubles;
-    for (int q = 0; q < 8; ++q) s[q] += p[q];
-    for (int d = 0; d < 3; ++d) {
-      lo[d] = fminf(lo[d], float(p[8 + d]));
-      hi[d] = fmaxf(hi[d], float(p[11 + d]));
+    const double *p = part + (cb + c) * kPartWords;
+    const __int128 *ps = reinterpret_cast<const __int128 *>(p);
+    const float *pb = reinterpret_cast<const float *>(p + 12);
+    const int *pe = reinterpret_cast<const int *>(p + 15);
+    for (int q = 0; q < 4; ++q) {
+      s[q] += ps[q];
+      a[q] += p[8 + q];
+      emin[q] = min(emin[q], pe[q]);
     }
-    const int *pe = reinterpret_cast<const int *>(p + 14);
-    for (int q = 0; q < 4; ++q) emin[q] = min(emin[q], pe[q]);
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = fminf(lo[d], pb[d]);
+      hi[d] = fmaxf(hi[d], pb[3 + d]);
+    }
+    ovf |= pe[4];
   }
-  for (int q = 0; q < 8; ++q) s[q] = warp_sum(s[q]);
+  for (int q = 0; q < 4; ++q) {
+    for (int o = 16; o > 0; o >>= 1) s[q] += shfl_xor_i128(s[q], o);
+    a[q] = warp_sum(a[q]);
+  }
   for (int d = 0; d < 3; ++d) {
     lo[d] = warp_min(lo[d]);
     hi[d] = warp_max(hi[d]);
   }
   for (int q = 0; q < 4; ++q)
     for (int o = 16; o > 0; o >>= 1) emin[q] = min(emin[q], __shfl_xor_sync(0xffffffffu, emin[q], o));
+  ovf = __any_sync(0xffffffffu, ovf != 0);
   if (lane != 0) return;
   for (int d = 0; d < 3; ++d) {
     N.xmin[d] = lo[d];
     N.xmax[d] = hi[d];
   }
-  // Both the reference's sequential sum and this tree sum are within
-  // (n - 1 + depth) u sum|terms| of the exact sum (depth < 64 + n); the factor
-  // 2 covers the higher-order terms.
-  const double g = 2.0 * (double(N.count) + 64.0) * 0x1p-53;
-  const double bm = g * s[7];
-  // Exact sums: every term a multiple of 2^emin and the magnitudes summing
-  // below 2^(53 + emin) -- then the reference's sequential sum and this one are
-  // the same exact value, and so is the quotient it rounds.
-  auto exact = [&](int q, double sabs) {
-    if (emin[q] == INT_MAX) return true;  // all terms zero
-    if (emin[q] == INT_MIN || emin[q] < -1000) return false;
-    return sabs < ldexp(1.0, 53 + emin[q]);
-  };
-  const bool mexact = exact(3, s[7]) && force_fallback == 0;
-  bool ok = force_fallback == 0;
+  // Sums of |terms|: float partials of <= 16 terms (rounded up) added in
+  // double; the factor covers the double additions' rounding.
+  for (int q = 0; q < 4; ++q) a[q] *= 1.0 + 0x1p-30;
+  const double n = double(N.count);
+  // The reference's sequential sum lies within (n - 1) u sum|terms| of the
+  // exact sum, to first order; 2 (n + 64) u covers the rest.  This sum is
+  // exact except for terms below 2^(kFix + 24) (truncated: < 2^(kFix+24) each)
+  // and its rounding to double.
+  const double g = 2.0 * (n + 64.0) * 0x1p-53;
+  double sd[4], bd[4];
+  bool exact_ok[4];
+  for (int q = 0; q < 4; ++q) {
+    sd[q] = fix_to_double(s[q]);
+    const bool trunc = emin[q] != INT_MAX && emin[q] < kFix;
+    bd[q] = g * a[q] + fabs(sd[q]) * 0x1p-52 + (trunc ? n * ldexp(1.0, kFix + 24) : 0.0);
+    // Exact: every term a multiple of 2^emin (none truncated) and the
+    // magnitudes summing below 2^(53 + emin) -- then the reference's
+    // sequential sum and this one are the same exact value, a double.
+    if (emin[q] == INT_MAX) exact_ok[q] = true;  // all terms zero
+    else exact_ok[q] = !trunc && emin[q] > -1000 && a[q] < ldexp(1.0, 53 + emin[q]);
+  }
+  bool ok = force_fallback == 0 && !ovf;
   for (int d = 0; d < 3 && ok; ++d) {
     float v;
-    if (mexact && exact(d, s[4 + d]) && s[3] != 0.0) N.xc[d] = __double2float_rn(__ddiv_rn(s[d], s[3]));
-    else if (certify(s[d], g * s[4 + d], s[3], bm, &v)) N.xc[d] = v;
+    if (exact_ok[3] && exact_ok[d] && sd[3] != 0.0) N.xc[d] = __double2float_rn(__ddiv_rn(sd[d], sd[3]));
+    else if (certify(sd[d], bd[d], sd[3], bd[3], &v)) N.xc[d] = v;
     else ok = false;
   }
   if (!ok) {
@@ -1534,7 +1631,7 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     DT_CHECK(grow(fallback_, cap_fb_, size_t(L), s));
     const int64_t max_chunks = n / kChunk + L + 1;
     DT_CHECK(grow(chunk_node_, cap_cn_, size_t(max_chunks), s));
-    DT_CHECK(grow(part_, cap_part_, size_t(max_chunks) * kPartDoubles, s));
+    DT_CHECK(grow(part_, cap_part_, size_t(max_chunks) * kPartWords, s));
     DT_CHECK(grow(left_cnt_, cap_lc_, size_t(max_chunks), s));
     DT_CHECK(grow(left_base_, cap_lb_, size_t(max_chunks), s));
     DT_CHECK(cudaMemsetAsync(counters_ + C_NFALLBACK, 0, sizeof(int64_t), s));
