@@ -1230,6 +1230,8 @@ __global__ void k_leaf_desc(const DNode *nodes, const int32_t *leaf_ids, int64_t
 // inside the leaf's box) and the batched kernel's work items.
 // ---------------------------------------------------------------------------
 constexpr int kGroupSort = 1024;
+constexpr int kGW = 256;     // leaves up to this size are grouped by one warp
+constexpr int kGWarps = 4;   // warps (leaves) per block of k_groups_warp
 constexpr int kGroupThreads = 256;
 
 // Order-preserving map of a float to an unsigned integer.
@@ -1258,6 +1260,7 @@ __global__ void __launch_bounds__(kGroupThreads)
   if (li >= nleaves) return;
   const DNode &T = nodes[leaf_ids[li]];
   const int32_t c = T.count;
+  if (c <= kGW) return;  // k_groups_warp
   if (c > kGroupSort) {
     for (int32_t i = threadIdx.x; i < c; i += blockDim.x) gidx[T.offset + i] = T.offset + i;
     return;
@@ -1362,6 +1365,123 @@ __global__ void __launch_bounds__(kGroupThreads)
     if (!more_s) break;
   }
   for (int i = threadIdx.x; i < c; i += blockDim.x) gidx[T.offset + i] = val[i];
+}
+
+// Warp-per-leaf grouping for leaves of at most kGW particles (the usual
+// case; larger leaves take k_groups).  Same median splits as k_groups: per
+// level, every segment above G particles is sorted along its longest axis by
+// ranking (each element counts the keys below its own, ties by position) and
+// split at G * ceil(groups / 2).
+__global__ void __launch_bounds__(32 * kGWarps)
+    k_groups_warp(const DNode *nodes, const int32_t *leaf_ids, int64_t nleaves,
+                  const float4 *__restrict__ pos, int32_t *gidx, int G) {
+  __shared__ float key[kGWarps][kGW];
+  __shared__ int32_t val[kGWarps][2][kGW];
+  __shared__ uint8_t segid[kGWarps][kGW];
+  __shared__ int16_t seg_a[kGWarps][kGW / 16 + 1], seg_c[kGWarps][kGW / 16 + 1];
+  __shared__ int8_t seg_ax[kGWarps][kGW / 16 + 1];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int64_t li = int64_t(blockIdx.x) * kGWarps + w;
+  if (li >= nleaves) return;
+  const DNode &T = nodes[leaf_ids[li]];
+  const int c = T.count;
+  if (c <= 0 || c > kGW) return;
+  if (c <= G) {
+    for (int i = lane; i < c; i += 32) gidx[T.offset + i] = T.offset + i;
+    return;
+  }
+  for (int i = lane; i < c; i += 32) {
+    val[w][0][i] = T.offset + i;
+    segid[w][i] = 0;
+  }
+  int nseg = 1;
+  if (lane == 0) {
+    seg_a[w][0] = 0;
+    seg_c[w][0] = int16_t(c);
+  }
+  __syncwarp();
+  int cur = 0;
+  for (int level = 0; level < 16; ++level) {
+    // longest axis of every segment above G
+    bool any = false;
+    for (int q = 0; q < nseg; ++q) {
+      const int a0 = seg_a[w][q], c0 = seg_c[w][q];
+      if (c0 <= G) continue;
+      any = true;
+      float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+      for (int i = a0 + lane; i < a0 + c0; i += 32) {
+        const float4 p = pos[val[w][cur][i]];
+        lo[0] = fminf(lo[0], p.x); hi[0] = fmaxf(hi[0], p.x);
+        lo[1] = fminf(lo[1], p.y); hi[1] = fmaxf(hi[1], p.y);
+        lo[2] = fminf(lo[2], p.z); hi[2] = fmaxf(hi[2], p.z);
+      }
+      for (int d = 0; d < 3; ++d) {
+        lo[d] = warp_min(lo[d]);
+        hi[d] = warp_max(hi[d]);
+      }
+      const float e0 = hi[0] - lo[0], e1 = hi[1] - lo[1], e2 = hi[2] - lo[2];
+      if (lane == 0) seg_ax[w][q] = int8_t((e0 >= e1 && e0 >= e2) ? 0 : (e1 >= e2 ? 1 : 2));
+    }
+    if (!any) break;
+    __syncwarp();
+    for (int i = lane; i < c; i += 32) {
+      const int q = segid[w][i];
+      float k = 0.f;
+      if (seg_c[w][q] > G) {
+        const float4 p = pos[val[w][cur][i]];
+        const int ax = seg_ax[w][q];
+        k = ax == 0 ? p.x : (ax == 1 ? p.y : p.z);
+      }
+      key[w][i] = k;
+    }
+    __syncwarp();
+    for (int i = lane; i < c; i += 32) {
+      const int q = segid[w][i];
+      const int a0 = seg_a[w][q], c0 = seg_c[w][q];
+      int np = i;
+      if (c0 > G) {
+        const float ki = key[w][i];
+        int r = 0;
+        for (int j = a0; j < a0 + c0; ++j) {
+          const float kj = key[w][j];
+          r += (kj < ki) || (kj == ki && j < i);
+        }
+        np = a0 + r;
+      }
+      val[w][cur ^ 1][np] = val[w][cur][i];
+    }
+    __syncwarp();
+    cur ^= 1;
+    // split every segment above G at G * ceil(groups / 2)
+    if (lane == 0) {
+      int16_t na[kGW / 16 + 1], nc[kGW / 16 + 1];
+      int n2 = 0;
+      for (int q = 0; q < nseg; ++q) {
+        const int a0 = seg_a[w][q], c0 = seg_c[w][q];
+        if (c0 <= G) {
+          na[n2] = int16_t(a0);
+          nc[n2++] = int16_t(c0);
+          continue;
+        }
+        const int ng = (c0 + G - 1) / G, left = G * ((ng + 1) / 2);
+        na[n2] = int16_t(a0);
+        nc[n2++] = int16_t(left);
+        na[n2] = int16_t(a0 + left);
+        nc[n2++] = int16_t(c0 - left);
+      }
+      for (int q = 0; q < n2; ++q) {
+        seg_a[w][q] = na[q];
+        seg_c[w][q] = nc[q];
+      }
+      seg_ax[w][kGW / 16] = int8_t(n2);  // count, read back below
+    }
+    __syncwarp();
+    nseg = seg_ax[w][kGW / 16];
+    for (int q = 0; q < nseg; ++q)
+      for (int i = seg_a[w][q] + lane; i < seg_a[w][q] + seg_c[w][q]; i += 32) segid[w][i] = uint8_t(q);
+    __syncwarp();
+  }
+  for (int i = lane; i < c; i += 32) gidx[T.offset + i] = val[w][cur][i];
 }
 
 __device__ __forceinline__ int len_bucket(int64_t len) {
@@ -1781,6 +1901,8 @@ cudaError_t DeviceTree::make_items(int64_t n, int64_t jsplit, cudaStream_t s) {
   DT_CHECK(grow(gidx_, cap_gidx_, size_t(std::max<int64_t>(n, 1)), s));
   DT_CHECK(cudaMemsetAsync(counters_ + C_BUCKET, 0, 32 * sizeof(int64_t), s));
   if (nleaves > 0) {
+    k_groups_warp<<<unsigned((nleaves + kGWarps - 1) / kGWarps), 32 * kGWarps, 0, s>>>(
+        nodes_, leaf_ids_, nleaves, epos_, gidx_, G);
     k_groups<<<unsigned(nleaves), kGroupThreads, 0, s>>>(nodes_, leaf_ids_, nleaves, epos_, gidx_, G);
     k_item_hist<<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(leafdesc_, nleaves, jsplit, G,
                                                                 counters_);
