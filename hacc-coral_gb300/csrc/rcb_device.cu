@@ -42,7 +42,6 @@ __device__ __forceinline__ int lsb_exp(float t) {
 
 constexpr int kChunk = 4096;        // elements per statistics / partition chunk
 constexpr int kChunkThreads = 256;  // threads per chunk (16 elements each)
-constexpr int kPer = kChunk / kChunkThreads;
 constexpr int kWalkStack = 256;     // DFS stack of the list walk
 
 enum { C_NCHUNK = 0, C_NSPLIT = 1, C_NFALLBACK = 2, C_NLEAF = 3, C_NSEG = 4, C_NENT = 5,
@@ -221,18 +220,17 @@ __device__ __forceinline__ __int128 shfl_xor_i128(__int128 v, int o) {
   return (__int128(h2) << 64) | __int128(l2);
 }
 
-// Correctly rounded double of v 2^kFix.
+// Correctly rounded double of v 2^kFix: the top 63 bits of |v| with the
+// rest folded into a sticky bit, rounded once by the conversion.
 __device__ double fix_to_double(__int128 v) {
   const bool neg = v < 0;
-  unsigned __int128 u = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
-  int k = 0;
-  while ((u >> 63) != 0) {  // keep 63 bits, the shifted-out ones as a sticky bit
-    const unsigned __int128 sticky = u & 1;
-    u = (u >> 1) | sticky;
-    ++k;
-  }
-  const double d = __ull2double_rn((unsigned long long)u);
-  const double r = ldexp(d, k + kFix);
+  const unsigned __int128 u = neg ? (unsigned __int128)(-v) : (unsigned __int128)v;
+  const unsigned long long hi = (unsigned long long)(u >> 64), lo = (unsigned long long)u;
+  const int bits = hi ? 128 - __clzll((long long)hi) : (lo ? 64 - __clzll((long long)lo) : 0);
+  const int k = bits > 63 ? bits - 63 : 0;
+  unsigned long long m = (unsigned long long)(u >> k);
+  if (k > 0 && (u & ((((unsigned __int128)1) << k) - 1)) != 0) m |= 1ull;
+  const double r = ldexp(__ull2double_rn(m), k + kFix);
   return neg ? -r : r;
 }
 
@@ -832,11 +830,15 @@ __global__ void k_part_node_scan(DNode *nodes, int32_t nb, int32_t ne, const int
 }
 
 // Left particles go to their rank; idx[rank] records where each came from.
+// Warp w takes the chunk's elements [w * kSub, (w + 1) * kSub) 32 at a time
+// (coalesced); ranks follow array order through the warps' totals and a
+// ballot prefix within each step.
 __global__ void __launch_bounds__(kChunkThreads)
     k_part_left(const float4 *__restrict__ pos, const int32_t *__restrict__ oid, const DNode *nodes,
                 const int32_t *chunk_node, const int64_t *chunk_base, int32_t nb,
                 const int64_t *nchunk, const int64_t *left_base, float4 *tpos, int32_t *toid,
                 int32_t *idx) {
+  constexpr int kWarps = kChunkThreads / 32, kSub = kChunk / kWarps;
   const int64_t chunk = blockIdx.x;
   if (chunk >= *nchunk) return;
   const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
@@ -844,28 +846,35 @@ __global__ void __launch_bounds__(kChunkThreads)
   if (N.split_dim < 0) return;
   const int d = N.split_dim;
   const float split = N.xc[d];
-  // thread t owns kPer consecutive elements so ranks follow array order
-  const int k0 = threadIdx.x * kPer;
-  unsigned flags = 0;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned below = (1u << lane) - 1u;
+  __shared__ int wtot[kWarps];
   int c = 0;
-  for (int k = 0; k < kPer; ++k) {
-    const int e = k0 + k;
-    if (e < R.len && key_of(pos[R.begin + e], d) < split) {
-      flags |= 1u << k;
-      ++c;
-    }
+  for (int j = 0; j < kSub; j += 32) {
+    const int e = warp * kSub + j + lane;
+    const bool l = e < R.len && key_of(pos[R.begin + e], d) < split;
+    c += __popc(__ballot_sync(0xffffffffu, l));
   }
-  __shared__ int sw[32];
-  int tot;
-  int r = block_excl_scan(c, sw, &tot) + int(left_base[chunk]);
-  for (int k = 0; k < kPer; ++k) {
-    if (!(flags & (1u << k))) continue;
-    const int e = k0 + k;
-    const int64_t src = R.begin + e;
-    tpos[N.offset + r] = pos[src];
-    toid[N.offset + r] = oid[src];
-    idx[N.offset + r] = R.local + e;
-    ++r;
+  if (lane == 0) wtot[warp] = c;
+  __syncthreads();
+  int r = int(left_base[chunk]);
+  for (int w = 0; w < warp; ++w) r += wtot[w];
+  for (int j = 0; j < kSub; j += 32) {
+    const int e = warp * kSub + j + lane;
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool l = false;
+    if (e < R.len) {
+      p = pos[R.begin + e];
+      l = key_of(p, d) < split;
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, l);
+    if (l) {
+      const int q = r + __popc(bal & below);
+      tpos[N.offset + q] = p;
+      toid[N.offset + q] = oid[R.begin + e];
+      idx[N.offset + q] = R.local + e;
+    }
+    r += __popc(bal);
   }
 }
 
@@ -909,17 +918,21 @@ __global__ void __launch_bounds__(kChunkThreads)
   }
 }
 
+// The element buffers alternate between levels.  Nodes that did not split
+// at this level (leaves) keep their elements: copied once into the next
+// level's buffer, after which both buffers hold them (later levels write only
+// inside splitting nodes).
 __global__ void __launch_bounds__(kChunkThreads)
-    k_part_copyback(float4 *pos, int32_t *oid, const DNode *nodes, const int32_t *chunk_node,
-                    const int64_t *chunk_base, int32_t nb, const int64_t *nchunk,
-                    const float4 *tpos, const int32_t *toid) {
+    k_part_keep(const float4 *pos, const int32_t *oid, const DNode *nodes,
+                const int32_t *chunk_node, const int64_t *chunk_base, int32_t nb,
+                const int64_t *nchunk, float4 *tpos, int32_t *toid) {
   const int64_t chunk = blockIdx.x;
   if (chunk >= *nchunk) return;
   const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
-  if (nodes[R.node].split_dim < 0) return;
+  if (nodes[R.node].split_dim >= 0) return;
   for (int k = threadIdx.x; k < R.len; k += kChunkThreads) {
-    pos[R.begin + k] = tpos[R.begin + k];
-    oid[R.begin + k] = toid[R.begin + k];
+    tpos[R.begin + k] = pos[R.begin + k];
+    toid[R.begin + k] = oid[R.begin + k];
   }
 }
 
@@ -1782,8 +1795,12 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
                                              counters_ + C_NCHUNK, left_base_, tpos_, toid_, idx_);
     k_part_right<<<gC, kChunkThreads, 0, s>>>(epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
                                               counters_ + C_NCHUNK, idx_, tpos_, toid_, walk_err_);
-    k_part_copyback<<<gC, kChunkThreads, 0, s>>>(epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
-                                                 counters_ + C_NCHUNK, tpos_, toid_);
+    k_part_keep<<<gC, kChunkThreads, 0, s>>>(epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
+                                             counters_ + C_NCHUNK, tpos_, toid_);
+    std::swap(epos_, tpos_);
+    std::swap(cap_e_, cap_t_);
+    std::swap(oid_, toid_);
+    std::swap(cap_o_, cap_to_);
     k_split_flags<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
     DT_CHECK(exclusive_scan_i64(node_tmp_, node_tmp_, L, counters_ + C_NSPLIT, scan_tmp_, s));
     k_children<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
