@@ -240,21 +240,34 @@ __device__ double fix_to_double(__int128 v) {
 // an overflow flag.
 constexpr int kPartWords = 18;
 
+// The chunk kernels run a block per chunk, or (WM, on deep levels where
+// nodes are small) a warp per chunk, 8 chunks per block.
+#define CHUNK_PROLOGUE                                                                  \
+  const int lane_ = threadIdx.x & 31;                                                 \
+  const int64_t chunk =                                                               \
+      WM ? int64_t(blockIdx.x) * (kChunkThreads / 32) + (threadIdx.x >> 5) : int64_t(blockIdx.x); \
+  const int tid = WM ? lane_ : int(threadIdx.x);                                      \
+  constexpr int NT = WM ? 32 : kChunkThreads;                                         \
+  (void)lane_;                                                                        \
+  (void)tid;                                                                          \
+  (void)NT;                                                                           \
+  if (chunk >= *nchunk) return;
+
 // Partial sums of one chunk and its bounding box.  Fixed thread-to-element
 // map and reduction tree.
+template <bool WM>
 __global__ void __launch_bounds__(kChunkThreads)
     k_stats_partial(const float4 *__restrict__ pos, const DNode *nodes,
                     const int32_t *chunk_node, const int64_t *chunk_base, int32_t nb,
                     const int64_t *nchunk, double *part) {
-  const int64_t chunk = blockIdx.x;
-  if (chunk >= *nchunk) return;
+  CHUNK_PROLOGUE
   const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
   __int128 s[4] = {0, 0, 0, 0};
   float fa[4] = {0.f, 0.f, 0.f, 0.f};
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   int emin[4] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX};
   bool ovf = false;
-  for (int k = threadIdx.x; k < R.len; k += kChunkThreads) {
+  for (int k = tid; k < R.len; k += NT) {
     const float4 p = pos[R.begin + k];
     const float w = p.w;
     const float t[4] = {fmul_(w, p.x), fmul_(w, p.y), fmul_(w, p.z), w};
@@ -283,6 +296,23 @@ __global__ void __launch_bounds__(kChunkThreads)
   for (int q = 0; q < 4; ++q)
     for (int o = 16; o > 0; o >>= 1) emin[q] = min(emin[q], __shfl_xor_sync(0xffffffffu, emin[q], o));
   const bool wovf = __any_sync(0xffffffffu, ovf);
+  if (WM) {
+    if (lane_ == 0) {
+      double *o = part + chunk * kPartWords;
+      __int128 *os = reinterpret_cast<__int128 *>(o);
+      for (int q = 0; q < 4; ++q) os[q] = s[q];
+      for (int q = 0; q < 4; ++q) o[8 + q] = a[q];
+      float *ob = reinterpret_cast<float *>(o + 12);
+      for (int d = 0; d < 3; ++d) {
+        ob[d] = lo[d];
+        ob[3 + d] = hi[d];
+      }
+      int *oe = reinterpret_cast<int *>(o + 15);
+      for (int q = 0; q < 4; ++q) oe[q] = emin[q];
+      oe[4] = wovf ? 1 : 0;
+    }
+    return;
+  }
   __shared__ __int128 shs[kChunkThreads / 32][4];
   __shared__ double sha[kChunkThreads / 32][4];
   __shared__ float shb[kChunkThreads / 32][6];
@@ -790,21 +820,26 @@ __device__ __forceinline__ int block_excl_scan(int v, int *sh_warp, int *total) 
 }
 
 // Left counts of each chunk of a splitting node.
+template <bool WM>
 __global__ void __launch_bounds__(kChunkThreads)
     k_part_count(const float4 *__restrict__ pos, const DNode *nodes, const int32_t *chunk_node,
                  const int64_t *chunk_base, int32_t nb, const int64_t *nchunk, int32_t *left_cnt) {
-  const int64_t chunk = blockIdx.x;
-  if (chunk >= *nchunk) return;
+  CHUNK_PROLOGUE
   const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
   const DNode &N = nodes[R.node];
   if (N.split_dim < 0) {
-    if (threadIdx.x == 0) left_cnt[chunk] = 0;
+    if (tid == 0) left_cnt[chunk] = 0;
     return;
   }
   const int d = N.split_dim;
   const float split = N.xc[d];
   int c = 0;
-  for (int k = threadIdx.x; k < R.len; k += kChunkThreads) c += key_of(pos[R.begin + k], d) < split;
+  for (int k = tid; k < R.len; k += NT) c += key_of(pos[R.begin + k], d) < split;
+  if (WM) {
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane_ == 0) left_cnt[chunk] = c;
+    return;
+  }
   __shared__ int sw[32];
   int tot;
   block_excl_scan(c, sw, &tot);
@@ -833,33 +868,37 @@ __global__ void k_part_node_scan(DNode *nodes, int32_t nb, int32_t ne, const int
 // Warp w takes the chunk's elements [w * kSub, (w + 1) * kSub) 32 at a time
 // (coalesced); ranks follow array order through the warps' totals and a
 // ballot prefix within each step.
+template <bool WM>
 __global__ void __launch_bounds__(kChunkThreads)
     k_part_left(const float4 *__restrict__ pos, const int32_t *__restrict__ oid, const DNode *nodes,
                 const int32_t *chunk_node, const int64_t *chunk_base, int32_t nb,
                 const int64_t *nchunk, const int64_t *left_base, float4 *tpos, int32_t *toid,
                 int32_t *idx) {
-  constexpr int kWarps = kChunkThreads / 32, kSub = kChunk / kWarps;
-  const int64_t chunk = blockIdx.x;
-  if (chunk >= *nchunk) return;
+  constexpr int kWarps = kChunkThreads / 32;
+  constexpr int kSub = WM ? kChunk : kChunk / kWarps;  // a warp's share of the chunk
+  CHUNK_PROLOGUE
   const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
   const DNode &N = nodes[R.node];
   if (N.split_dim < 0) return;
   const int d = N.split_dim;
   const float split = N.xc[d];
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31, warp = WM ? 0 : int(threadIdx.x >> 5);
   const unsigned below = (1u << lane) - 1u;
-  __shared__ int wtot[kWarps];
-  int c = 0;
-  for (int j = 0; j < kSub; j += 32) {
-    const int e = warp * kSub + j + lane;
-    const bool l = e < R.len && key_of(pos[R.begin + e], d) < split;
-    c += __popc(__ballot_sync(0xffffffffu, l));
-  }
-  if (lane == 0) wtot[warp] = c;
-  __syncthreads();
+  const int sub_end = min(kSub, R.len - warp * kSub);  // elements of this warp's share
   int r = int(left_base[chunk]);
-  for (int w = 0; w < warp; ++w) r += wtot[w];
-  for (int j = 0; j < kSub; j += 32) {
+  if (!WM) {
+    __shared__ int wtot[kWarps];
+    int c = 0;
+    for (int j = 0; j < sub_end; j += 32) {
+      const int e = warp * kSub + j + lane;
+      const bool l = e < R.len && key_of(pos[R.begin + e], d) < split;
+      c += __popc(__ballot_sync(0xffffffffu, l));
+    }
+    if (lane == 0) wtot[warp] = c;
+    __syncthreads();
+    for (int w = 0; w < warp; ++w) r += wtot[w];
+  }
+  for (int j = 0; j < sub_end; j += 32) {
     const int e = warp * kSub + j + lane;
     float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
     bool l = false;
@@ -882,20 +921,20 @@ __global__ void __launch_bounds__(kChunkThreads)
 // nleft moves along p -> idx[p] -> ... until it lands at or after nleft (the
 // reference's swap sequence, RCBForceTree.cxx:647-669).  Positions increase
 // strictly along a chain, so it ends within count steps.
+template <bool WM>
 __global__ void __launch_bounds__(kChunkThreads)
     k_part_right(const float4 *__restrict__ pos, const int32_t *__restrict__ oid, const DNode *nodes,
                  const int32_t *chunk_node, const int64_t *chunk_base, int32_t nb,
                  const int64_t *nchunk, const int32_t *__restrict__ idx, float4 *tpos,
                  int32_t *toid, int32_t *err) {
-  const int64_t chunk = blockIdx.x;
-  if (chunk >= *nchunk) return;
+  CHUNK_PROLOGUE
   const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
   const DNode &N = nodes[R.node];
   if (N.split_dim < 0) return;
   const int d = N.split_dim;
   const float split = N.xc[d];
   const int32_t is = N.nleft;
-  for (int k = threadIdx.x; k < R.len; k += kChunkThreads) {
+  for (int k = tid; k < R.len; k += NT) {
     const int64_t src = R.begin + k;
     const float4 p = pos[src];
     if (key_of(p, d) < split) continue;
@@ -922,15 +961,15 @@ __global__ void __launch_bounds__(kChunkThreads)
 // at this level (leaves) keep their elements: copied once into the next
 // level's buffer, after which both buffers hold them (later levels write only
 // inside splitting nodes).
+template <bool WM>
 __global__ void __launch_bounds__(kChunkThreads)
     k_part_keep(const float4 *pos, const int32_t *oid, const DNode *nodes,
                 const int32_t *chunk_node, const int64_t *chunk_base, int32_t nb,
                 const int64_t *nchunk, float4 *tpos, int32_t *toid) {
-  const int64_t chunk = blockIdx.x;
-  if (chunk >= *nchunk) return;
+  CHUNK_PROLOGUE
   const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
   if (nodes[R.node].split_dim >= 0) return;
-  for (int k = threadIdx.x; k < R.len; k += kChunkThreads) {
+  for (int k = tid; k < R.len; k += NT) {
     tpos[R.begin + k] = pos[R.begin + k];
     toid[R.begin + k] = oid[R.begin + k];
   }
@@ -1774,9 +1813,16 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     k_chunk_counts<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
     DT_CHECK(exclusive_scan_i64(node_tmp_, chunk_base_, L, counters_ + C_NCHUNK, scan_tmp_, s));
     k_chunk_fill<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, chunk_node_);
-    const unsigned gC = unsigned(max_chunks);
-    k_stats_partial<<<gC, kChunkThreads, 0, s>>>(epos_, nodes_, chunk_node_, chunk_base_, nb,
-                                                 counters_ + C_NCHUNK, part_);
+    // deep levels (nodes of ~2048 elements or fewer on average): a warp per chunk
+    const bool wm = int64_t(L) * 2048 >= n;
+    const unsigned gC = wm ? unsigned((max_chunks + 7) / 8) : unsigned(max_chunks);
+#define CHUNK_LAUNCH(kern, ...)                                                  \
+  do {                                                                           \
+    if (wm) kern<true><<<gC, kChunkThreads, 0, s>>>(__VA_ARGS__);                \
+    else kern<false><<<gC, kChunkThreads, 0, s>>>(__VA_ARGS__);                  \
+  } while (0)
+    CHUNK_LAUNCH(k_stats_partial, epos_, nodes_, chunk_node_, chunk_base_, nb, counters_ + C_NCHUNK,
+                 part_);
     k_stats_final<<<unsigned((int64_t(L) * 32 + 255) / 256), 256, 0, s>>>(
         nodes_, nb, ne, chunk_base_, part_, fallback_, counters_, cfg.force_cm_fallback);
     k_cm_tight_sums<<<kTightBlocks, kTightThreads, 0, s>>>(
@@ -1788,15 +1834,16 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     k_cm_fallback<<<unsigned(std::min<int64_t>((L + 127) / 128, 1024)), 128, 0, s>>>(
         epos_, nodes_, fallback_, counters_);
     k_split_decide<<<gL, 128, 0, s>>>(nodes_, nb, ne, cfg.nd);
-    k_part_count<<<gC, kChunkThreads, 0, s>>>(epos_, nodes_, chunk_node_, chunk_base_, nb,
-                                              counters_ + C_NCHUNK, left_cnt_);
+    CHUNK_LAUNCH(k_part_count, epos_, nodes_, chunk_node_, chunk_base_, nb, counters_ + C_NCHUNK,
+                 left_cnt_);
     k_part_node_scan<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, left_cnt_, left_base_);
-    k_part_left<<<gC, kChunkThreads, 0, s>>>(epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
-                                             counters_ + C_NCHUNK, left_base_, tpos_, toid_, idx_);
-    k_part_right<<<gC, kChunkThreads, 0, s>>>(epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
-                                              counters_ + C_NCHUNK, idx_, tpos_, toid_, walk_err_);
-    k_part_keep<<<gC, kChunkThreads, 0, s>>>(epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
-                                             counters_ + C_NCHUNK, tpos_, toid_);
+    CHUNK_LAUNCH(k_part_left, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
+                 counters_ + C_NCHUNK, left_base_, tpos_, toid_, idx_);
+    CHUNK_LAUNCH(k_part_right, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
+                 counters_ + C_NCHUNK, idx_, tpos_, toid_, walk_err_);
+    CHUNK_LAUNCH(k_part_keep, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
+                 counters_ + C_NCHUNK, tpos_, toid_);
+#undef CHUNK_LAUNCH
     std::swap(epos_, tpos_);
     std::swap(cap_e_, cap_t_);
     std::swap(oid_, toid_);
