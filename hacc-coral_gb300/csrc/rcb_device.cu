@@ -181,15 +181,16 @@ __device__ __forceinline__ ChunkRange chunk_range(const DNode *nodes, const int3
   return r;
 }
 
-// Exact sums in 128-bit fixed point.  A float term t = M 2^E (M < 2^24) is
-// the integer M 2^(E - kFix) in units of 2^kFix: exact for |t| >= 2^(kFix+23)
-// in lsb terms (lsb exponent >= kFix), truncated toward zero below (|t| <
-// 2^(kFix+24), counted in the error bound).  Terms up to 2^kFixMax keep a sum
-// of 2^31 of them below 2^125; a larger term flags the chunk (its node takes
-// the sequential sum).  Integer adds avoid the FP64 pipe, which runs at a
-// small fraction of the FP32 rate on this part.
-constexpr int kFix = -64;
-constexpr int kFixMaxShift = 70;  // |t| < 2^(70 + 24 + kFix) = 2^30
+// Exact sums in 128-bit fixed point.  A float term t is the integer
+// t 2^-kFix in units of 2^kFix: exact when t's least significant bit is at
+// least 2^kFix, truncated toward zero otherwise (an error below one unit per
+// term, counted in the bound).  Terms below 2^14 convert in hardware
+// (t 2^48 < 2^62 fits an int64); larger ones take a shift, and terms of
+// 2^46 or more flag the chunk (its node takes the sequential sum), which keeps
+// a sum of 2^31 terms below 2^125.  Integer adds avoid the FP64 pipe, which
+// runs at a small fraction of the FP32 rate on this part.
+constexpr int kFix = -48;
+constexpr int kFixMaxShift = 70;  // |t| < 2^(70 + 24 + kFix) = 2^46
 
 __device__ __forceinline__ __int128 to_fix(float t, bool &overflow) {
   const uint32_t b = __float_as_uint(t);
@@ -211,6 +212,11 @@ __device__ __forceinline__ __int128 to_fix(float t, bool &overflow) {
     v = sh > -32 ? __int128(m >> (-sh)) : __int128(0);
   }
   return (b >> 31) ? -v : v;
+}
+
+__device__ __forceinline__ void fix_add(__int128 &acc, float t, bool &overflow) {
+  if (fabsf(t) < 16384.0f) acc += __int128(__float2ll_rz(t * 0x1p48f));
+  else acc += to_fix(t, overflow);
 }
 
 __device__ __forceinline__ __int128 shfl_xor_i128(__int128 v, int o) {
@@ -274,7 +280,7 @@ __global__ void __launch_bounds__(kChunkThreads)
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
       emin[q] = min(emin[q], lsb_exp(t[q]));
-      s[q] += to_fix(t[q], ovf);
+      fix_add(s[q], t[q], ovf);
       fa[q] = __fadd_ru(fa[q], fabsf(t[q]));
     }
     lo[0] = fminf(lo[0], p.x); hi[0] = fmaxf(hi[0], p.x);
@@ -384,9 +390,76 @@ __device__ bool certify(double sx, double bx, double sm, double bm, float *out) 
   return true;
 }
 
-// One warp per node of the level: reduce the node's chunk partials, set the
-// bounding box and, where decided, the centre of mass; list the others for
-// the tight certification and the sequential fallback.
+// Sets a node's bounding box and, where decided, its centre of mass from the
+// reduced sums; lists it for the tight certification otherwise.
+__device__ void finish_node(DNode &N, int32_t node, const __int128 *s, double *a, const float *lo,
+                            const float *hi, const int *emin, bool ovf, int32_t *fallback,
+                            int64_t *counters, int32_t force_fallback) {
+  for (int d = 0; d < 3; ++d) {
+    N.xmin[d] = lo[d];
+    N.xmax[d] = hi[d];
+  }
+  // Sums of |terms|: float partials rounded up, added in double; the factor
+  // covers the double additions' rounding.
+  for (int q = 0; q < 4; ++q) a[q] *= 1.0 + 0x1p-30;
+  const double n = double(N.count);
+  // The reference's sequential sum lies within (n - 1) u sum|terms| of the
+  // exact sum, to first order; 2 (n + 64) u covers the rest.  This sum is
+  // exact except for the truncation of terms with bits below 2^kFix (under
+  // 2^kFix each) and its rounding to double.
+  const double g = 2.0 * (n + 64.0) * 0x1p-53;
+  double sd[4];
+  bool exact_ok[4];
+  for (int q = 0; q < 4; ++q) {
+    sd[q] = fix_to_double(s[q]);
+    // Exact: every term a multiple of 2^emin (none truncated) and the
+    // magnitudes summing below 2^(53 + emin) -- then the reference's
+    // sequential sum and this one are the same exact value, a double.
+    if (emin[q] == INT_MAX) exact_ok[q] = true;  // all terms zero
+    else exact_ok[q] = emin[q] >= kFix && a[q] < ldexp(1.0, 53 + emin[q]);
+  }
+  bool ok = force_fallback == 0 && !ovf;
+  for (int d = 0; d < 3 && ok; ++d) {
+    float v;
+    if (exact_ok[3] && exact_ok[d] && sd[3] != 0.0) {
+      N.xc[d] = __double2float_rn(__ddiv_rn(sd[d], sd[3]));
+      continue;
+    }
+    double bd[2];
+    const int qs[2] = {d, 3};
+    for (int t = 0; t < 2; ++t) {
+      const int q = qs[t];
+      const bool trunc = emin[q] != INT_MAX && emin[q] < kFix;
+      bd[t] = g * a[q] + fabs(sd[q]) * 0x1p-52 + (trunc ? n * ldexp(1.0, kFix) : 0.0);
+    }
+    if (certify(sd[d], bd[0], sd[3], bd[1], &v)) N.xc[d] = v;
+    else ok = false;
+  }
+  if (!ok) {
+    const unsigned long long k = atomicAdd((unsigned long long *)&counters[C_NFALLBACK], 1ull);
+    fallback[k] = node;
+  }
+}
+
+__device__ __forceinline__ void read_part(const double *p, __int128 *s, double *a, float *lo,
+                                          float *hi, int *emin, int &ovf) {
+  const __int128 *ps = reinterpret_cast<const __int128 *>(p);
+  const float *pb = reinterpret_cast<const float *>(p + 12);
+  const int *pe = reinterpret_cast<const int *>(p + 15);
+  for (int q = 0; q < 4; ++q) {
+    s[q] += ps[q];
+    a[q] += p[8 + q];
+    emin[q] = min(emin[q], pe[q]);
+  }
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = fminf(lo[d], pb[d]);
+    hi[d] = fmaxf(hi[d], pb[3 + d]);
+  }
+  ovf |= pe[4];
+}
+
+// One warp per node of more than one chunk: reduce the chunk partials and
+// finish the node.
 __global__ void k_stats_final(DNode *nodes, int32_t nb, int32_t ne, const int64_t *chunk_base,
                               const double *part, int32_t *fallback, int64_t *counters,
                               int32_t force_fallback) {
@@ -395,30 +468,15 @@ __global__ void k_stats_final(DNode *nodes, int32_t nb, int32_t ne, const int64_
   const int32_t node = nb + wid;
   if (node >= ne) return;
   DNode &N = nodes[node];
-  if (N.count <= 0) return;
-  const int64_t cb = chunk_base[wid];
   const int64_t nc = (int64_t(N.count) + kChunk - 1) / kChunk;
+  if (nc <= 1) return;  // k_stats_final_one
+  const int64_t cb = chunk_base[wid];
   __int128 s[4] = {0, 0, 0, 0};
   double a[4] = {0, 0, 0, 0};
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   int emin[4] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX};
   int ovf = 0;
-  for (int64_t c = lane; c < nc; c += 32) {
-    const double *p = part + (cb + c) * kPartWords;
-    const __int128 *ps = reinterpret_cast<const __int128 *>(p);
-    const float *pb = reinterpret_cast<const float *>(p + 12);
-    const int *pe = reinterpret_cast<const int *>(p + 15);
-    for (int q = 0; q < 4; ++q) {
-      s[q] += ps[q];
-      a[q] += p[8 + q];
-      emin[q] = min(emin[q], pe[q]);
-    }
-    for (int d = 0; d < 3; ++d) {
-      lo[d] = fminf(lo[d], pb[d]);
-      hi[d] = fmaxf(hi[d], pb[3 + d]);
-    }
-    ovf |= pe[4];
-  }
+  for (int64_t c = lane; c < nc; c += 32) read_part(part + (cb + c) * kPartWords, s, a, lo, hi, emin, ovf);
   for (int q = 0; q < 4; ++q) {
     for (int o = 16; o > 0; o >>= 1) s[q] += shfl_xor_i128(s[q], o);
     a[q] = warp_sum(a[q]);
@@ -431,42 +489,26 @@ __global__ void k_stats_final(DNode *nodes, int32_t nb, int32_t ne, const int64_
     for (int o = 16; o > 0; o >>= 1) emin[q] = min(emin[q], __shfl_xor_sync(0xffffffffu, emin[q], o));
   ovf = __any_sync(0xffffffffu, ovf != 0);
   if (lane != 0) return;
-  for (int d = 0; d < 3; ++d) {
-    N.xmin[d] = lo[d];
-    N.xmax[d] = hi[d];
-  }
-  // Sums of |terms|: float partials of <= 16 terms (rounded up) added in
-  // double; the factor covers the double additions' rounding.
-  for (int q = 0; q < 4; ++q) a[q] *= 1.0 + 0x1p-30;
-  const double n = double(N.count);
-  // The reference's sequential sum lies within (n - 1) u sum|terms| of the
-  // exact sum, to first order; 2 (n + 64) u covers the rest.  This sum is
-  // exact except for terms below 2^(kFix + 24) (truncated: < 2^(kFix+24) each)
-  // and its rounding to double.
-  const double g = 2.0 * (n + 64.0) * 0x1p-53;
-  double sd[4], bd[4];
-  bool exact_ok[4];
-  for (int q = 0; q < 4; ++q) {
-    sd[q] = fix_to_double(s[q]);
-    const bool trunc = emin[q] != INT_MAX && emin[q] < kFix;
-    bd[q] = g * a[q] + fabs(sd[q]) * 0x1p-52 + (trunc ? n * ldexp(1.0, kFix + 24) : 0.0);
-    // Exact: every term a multiple of 2^emin (none truncated) and the
-    // magnitudes summing below 2^(53 + emin) -- then the reference's
-    // sequential sum and this one are the same exact value, a double.
-    if (emin[q] == INT_MAX) exact_ok[q] = true;  // all terms zero
-    else exact_ok[q] = !trunc && emin[q] > -1000 && a[q] < ldexp(1.0, 53 + emin[q]);
-  }
-  bool ok = force_fallback == 0 && !ovf;
-  for (int d = 0; d < 3 && ok; ++d) {
-    float v;
-    if (exact_ok[3] && exact_ok[d] && sd[3] != 0.0) N.xc[d] = __double2float_rn(__ddiv_rn(sd[d], sd[3]));
-    else if (certify(sd[d], bd[d], sd[3], bd[3], &v)) N.xc[d] = v;
-    else ok = false;
-  }
-  if (!ok) {
-    const unsigned long long k = atomicAdd((unsigned long long *)&counters[C_NFALLBACK], 1ull);
-    fallback[k] = node;
-  }
+  finish_node(N, node, s, a, lo, hi, emin, ovf != 0, fallback, counters, force_fallback);
+}
+
+// One thread per node of a single chunk (most nodes of the deep levels): the
+// per-node arithmetic, much of it FP64, then fills whole warps.
+__global__ void k_stats_final_one(DNode *nodes, int32_t nb, int32_t ne, const int64_t *chunk_base,
+                                  const double *part, int32_t *fallback, int64_t *counters,
+                                  int32_t force_fallback) {
+  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  const int32_t node = nb + i;
+  if (node >= ne) return;
+  DNode &N = nodes[node];
+  if (N.count <= 0 || N.count > kChunk) return;
+  __int128 s[4] = {0, 0, 0, 0};
+  double a[4] = {0, 0, 0, 0};
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  int emin[4] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX};
+  int ovf = 0;
+  read_part(part + chunk_base[i] * kPartWords, s, a, lo, hi, emin, ovf);
+  finish_node(N, node, s, a, lo, hi, emin, ovf != 0, fallback, counters, force_fallback);
 }
 
 // ---------------------------------------------------------------------------
@@ -934,26 +976,68 @@ __global__ void __launch_bounds__(kChunkThreads)
   const int d = N.split_dim;
   const float split = N.xc[d];
   const int32_t is = N.nleft;
-  for (int k = tid; k < R.len; k += NT) {
-    const int64_t src = R.begin + k;
-    const float4 p = pos[src];
-    if (key_of(p, d) < split) continue;
-    int32_t q = R.local + k;
-    int32_t steps = 0;
-    while (q < is && steps++ <= N.count) {
-      const int32_t nq = idx[N.offset + q];
-      if (nq <= q || nq >= N.count) {  // cannot happen for a valid partition
-        atomicExch(err, 2);
-        break;
+  if (WM) {
+    for (int k = tid; k < R.len; k += NT) {
+      const int64_t src = R.begin + k;
+      const float4 p = pos[src];
+      if (key_of(p, d) < split) continue;
+      int32_t q = R.local + k;
+      int32_t steps = 0;
+      while (q < is && steps++ <= N.count) {
+        const int32_t nq = idx[N.offset + q];
+        if (nq <= q || nq >= N.count) {  // cannot happen for a valid partition
+          atomicExch(err, 2);
+          break;
+        }
+        q = nq;
       }
-      q = nq;
+      if (q < is) {
+        atomicExch(err, 2);
+        continue;
+      }
+      tpos[N.offset + q] = p;
+      toid[N.offset + q] = oid[src];
     }
-    if (q < is) {
-      atomicExch(err, 2);
-      continue;
+    return;
+  }
+  // Block mode: the thread's 16 elements follow their chains in lockstep, so
+  // up to 16 independent loads are in flight per step (chains run ~log n
+  // steps on cell-sorted input).
+  constexpr int kPerT = kChunk / kChunkThreads;
+  int32_t q[kPerT];
+  unsigned right = 0;
+#pragma unroll
+  for (int j = 0; j < kPerT; ++j) {
+    const int k = tid + j * NT;
+    q[j] = R.local + k;
+    if (k < R.len && !(key_of(pos[R.begin + k], d) < split)) right |= 1u << j;
+  }
+  unsigned active = 0;
+#pragma unroll
+  for (int j = 0; j < kPerT; ++j)
+    if ((right >> j & 1u) && q[j] < is) active |= 1u << j;
+  for (int32_t step = 0; active && step <= N.count; ++step) {
+#pragma unroll
+    for (int j = 0; j < kPerT; ++j) {
+      if (!(active >> j & 1u)) continue;
+      const int32_t nq = idx[N.offset + q[j]];
+      if (nq <= q[j] || nq >= N.count) {  // cannot happen for a valid partition
+        atomicExch(err, 2);
+        active &= ~(1u << j);
+        right &= ~(1u << j);
+        continue;
+      }
+      q[j] = nq;
+      if (nq >= is) active &= ~(1u << j);
     }
-    tpos[N.offset + q] = p;
-    toid[N.offset + q] = oid[src];
+  }
+  if (active) atomicExch(err, 2);
+#pragma unroll
+  for (int j = 0; j < kPerT; ++j) {
+    if (!(right >> j & 1u) || (active >> j & 1u)) continue;
+    const int64_t src = R.begin + tid + j * NT;
+    tpos[N.offset + q[j]] = pos[src];
+    toid[N.offset + q[j]] = oid[src];
   }
 }
 
@@ -1823,6 +1907,8 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   } while (0)
     CHUNK_LAUNCH(k_stats_partial, epos_, nodes_, chunk_node_, chunk_base_, nb, counters_ + C_NCHUNK,
                  part_);
+    k_stats_final_one<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, part_, fallback_, counters_,
+                                          cfg.force_cm_fallback);
     k_stats_final<<<unsigned((int64_t(L) * 32 + 255) / 256), 256, 0, s>>>(
         nodes_, nb, ne, chunk_base_, part_, fallback_, counters_, cfg.force_cm_fallback);
     k_cm_tight_sums<<<kTightBlocks, kTightThreads, 0, s>>>(

@@ -94,7 +94,8 @@ double ora_law_f64(int law, double rsm, double r2) {
     const float *a = k_poly6;
     p = (double)a[0] + r2 * ((double)a[1] + r2 * ((double)a[2] + r2 * ((double)a[3] + r2 * ((double)a[4] + r2 * ((double)a[5] + r2 * (double)a[6])))));
   }
-  return pow(r2 + rs2, -1.5) - p;
+  double s = r2 + rs2;
+  return 1.0 / (s * sqrt(s)) - p;  /* s^-1.5 */
 }
 
 double ora_law_dg_f64(int law, double rsm, double r2) {
@@ -105,7 +106,8 @@ double ora_law_dg_f64(int law, double rsm, double r2) {
   } else {
     for (int k = 6; k >= 1; --k) dp = dp * r2 + k * (double)k_poly6[k];
   }
-  return -1.5 * pow(r2 + rs2, -2.5) - dp;
+  double s = r2 + rs2;
+  return -1.5 / (s * s * sqrt(s)) - dp;  /* -1.5 s^-2.5 */
 }
 
 /* ------------------------------------------------------------------------- */
@@ -1183,18 +1185,16 @@ void ora_kick64(int64_t n, const double *pos, const double *m, int64_t nslots,
         if (e == i) continue;
         double d[3] = {tab[4 * e] - tab[4 * i], tab[4 * e + 1] - tab[4 * i + 1],
                        tab[4 * e + 2] - tab[4 * i + 2]};
-        double wg, wgp;
-        if (tcut) {
-          /* the cutoff decided at the reference positions, the law at these */
-          double dc[3] = {tcut[4 * e] - tcut[4 * i], tcut[4 * e + 1] - tcut[4 * i + 1],
-                          tcut[4 * e + 2] - tcut[4 * i + 2]};
-          if (!pair_terms(law, rsm, rmax2, tab[4 * i + 3], tab[4 * e + 3], dc, &wg, &wgp)) continue;
-          double mm = tab[4 * e + 3] * (law == ORA_LAW_POLY5_STEP16 ? 1.0 : tab[4 * i + 3]);
-          double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
-          wg = mm * ora_law_f64(law, rsm, r2);
-        } else if (!pair_terms(law, rsm, rmax2, tab[4 * i + 3], tab[4 * e + 3], d, &wg, &wgp)) {
-          continue;
-        }
+        /* the cutoff decided at the reference positions when given */
+        const double *tc = tcut ? tcut : tab;
+        double dc[3] = {tc[4 * e] - tc[4 * i], tc[4 * e + 1] - tc[4 * i + 1],
+                        tc[4 * e + 2] - tc[4 * i + 2]};
+        double rc2 = dc[0] * dc[0] + dc[1] * dc[1] + dc[2] * dc[2];
+        if (!(rc2 < rmax2)) continue;
+        if (law == ORA_LAW_POLY5_STEP16 && !(rc2 > 0)) continue;
+        double r2 = d[0] * d[0] + d[1] * d[1] + d[2] * d[2];
+        double mm = tab[4 * e + 3] * (law == ORA_LAW_POLY5_STEP16 ? 1.0 : tab[4 * i + 3]);
+        double wg = mm * ora_law_f64(law, rsm, r2);
         for (int q = 0; q < 3; ++q) a[q] += wg * d[q];
       }
       for (int q = 0; q < 3; ++q) dv[3 * i + q] += c * a[q];
