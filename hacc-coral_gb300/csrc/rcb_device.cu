@@ -192,31 +192,41 @@ __device__ __forceinline__ ChunkRange chunk_range(const DNode *nodes, const int3
 constexpr int kFix = -48;
 constexpr int kFixMaxShift = 70;  // |t| < 2^(70 + 24 + kFix) = 2^46
 
-__device__ __forceinline__ __int128 to_fix(float t, bool &overflow) {
+// Adds t 2^-kFix to acc; ors |t 2^-kFix| into bits (its lowest set bit is the
+// least significant bit of all terms, when none is truncated).  |t| < 2^14
+// takes a 64-bit shift on the integer pipe; larger terms the 128-bit one.
+// (Conversions to and from 64-bit types run on the FP64 pipe, slow here.)
+__device__ __forceinline__ void fix_add(__int128 &acc, unsigned __int128 &bits, float t,
+                                        bool &overflow, bool &trunc) {
   const uint32_t b = __float_as_uint(t);
   const uint32_t a = b & 0x7fffffffu;
+  if (a == 0) return;
   int e = int(a >> 23);
   uint32_t m = a & 0x7fffffu;
   if (e == 0) e = 1;
   else m |= 0x800000u;
-  if (e == 255) {
-    overflow = true;
-    return 0;
-  }
   const int sh = e - 150 - kFix;
-  __int128 v;
-  if (sh >= 0) {
-    if (sh > kFixMaxShift) overflow = true;
-    v = __int128(m) << min(sh, kFixMaxShift);
+  unsigned __int128 v;
+  if (sh >= 0 && sh <= 39) {
+    v = (unsigned __int128)((unsigned long long)m << sh);
+  } else if (sh > 39) {
+    if (sh > kFixMaxShift || e == 255) overflow = true;
+    v = (unsigned __int128)m << min(sh, kFixMaxShift);
   } else {
-    v = sh > -32 ? __int128(m >> (-sh)) : __int128(0);
+    const int r = -sh;
+    const uint32_t kept = r < 32 ? m >> r : 0u;
+    if ((r < 32 ? (kept << r) : 0u) != m) trunc = true;
+    v = kept;
   }
-  return (b >> 31) ? -v : v;
+  bits |= v;
+  acc += (b >> 31) ? -__int128(v) : __int128(v);
 }
 
-__device__ __forceinline__ void fix_add(__int128 &acc, float t, bool &overflow) {
-  if (fabsf(t) < 16384.0f) acc += __int128(__float2ll_rz(t * 0x1p48f));
-  else acc += to_fix(t, overflow);
+__device__ __forceinline__ int lsb_of(unsigned __int128 v) {
+  const unsigned long long lo = (unsigned long long)v, hi = (unsigned long long)(v >> 64);
+  if (lo) return __ffsll((long long)lo) - 1;
+  if (hi) return 64 + __ffsll((long long)hi) - 1;
+  return -1;
 }
 
 __device__ __forceinline__ __int128 shfl_xor_i128(__int128 v, int o) {
@@ -269,18 +279,18 @@ __global__ void __launch_bounds__(kChunkThreads)
   CHUNK_PROLOGUE
   const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
   __int128 s[4] = {0, 0, 0, 0};
+  unsigned __int128 bits[4] = {0, 0, 0, 0};
   float fa[4] = {0.f, 0.f, 0.f, 0.f};
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
-  int emin[4] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX};
   bool ovf = false;
+  bool trn[4] = {false, false, false, false};
   for (int k = tid; k < R.len; k += NT) {
     const float4 p = pos[R.begin + k];
     const float w = p.w;
     const float t[4] = {fmul_(w, p.x), fmul_(w, p.y), fmul_(w, p.z), w};
 #pragma unroll
     for (int q = 0; q < 4; ++q) {
-      emin[q] = min(emin[q], lsb_exp(t[q]));
-      fix_add(s[q], t[q], ovf);
+      fix_add(s[q], bits[q], t[q], ovf, trn[q]);
       fa[q] = __fadd_ru(fa[q], fabsf(t[q]));
     }
     lo[0] = fminf(lo[0], p.x); hi[0] = fmaxf(hi[0], p.x);
@@ -288,19 +298,26 @@ __global__ void __launch_bounds__(kChunkThreads)
     lo[2] = fminf(lo[2], p.z); hi[2] = fmaxf(hi[2], p.z);
   }
   double a[4];
+  int emin[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
-    for (int o = 16; o > 0; o >>= 1) s[q] += shfl_xor_i128(s[q], o);
-    a[q] = warp_sum(double(fa[q]));
+    for (int o = 16; o > 0; o >>= 1) {
+      s[q] += shfl_xor_i128(s[q], o);
+      bits[q] |= (unsigned __int128)shfl_xor_i128(__int128(bits[q]), o);
+      fa[q] = __fadd_ru(fa[q], __shfl_xor_sync(0xffffffffu, fa[q], o));
+    }
+    a[q] = double(fa[q]);
+    const bool tq = __any_sync(0xffffffffu, trn[q]);
+    const int l = lsb_of(bits[q]);
+    // least significant exponent of the warp's terms; below kFix if any term
+    // lost bits to the truncation, INT_MAX if all are zero
+    emin[q] = tq ? kFix - 1 : (l < 0 ? INT_MAX : kFix + l);
   }
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
     lo[d] = warp_min(lo[d]);
     hi[d] = warp_max(hi[d]);
   }
-#pragma unroll
-  for (int q = 0; q < 4; ++q)
-    for (int o = 16; o > 0; o >>= 1) emin[q] = min(emin[q], __shfl_xor_sync(0xffffffffu, emin[q], o));
   const bool wovf = __any_sync(0xffffffffu, ovf);
   if (WM) {
     if (lane_ == 0) {
@@ -1016,22 +1033,25 @@ __global__ void __launch_bounds__(kChunkThreads)
 #pragma unroll
   for (int j = 0; j < kPerT; ++j)
     if ((right >> j & 1u) && q[j] < is) active |= 1u << j;
+  bool bad = false;
   for (int32_t step = 0; active && step <= N.count; ++step) {
+    int32_t nq[kPerT];
+#pragma unroll
+    for (int j = 0; j < kPerT; ++j) nq[j] = (active >> j & 1u) ? idx[N.offset + q[j]] : q[j];
 #pragma unroll
     for (int j = 0; j < kPerT; ++j) {
       if (!(active >> j & 1u)) continue;
-      const int32_t nq = idx[N.offset + q[j]];
-      if (nq <= q[j] || nq >= N.count) {  // cannot happen for a valid partition
-        atomicExch(err, 2);
+      if (nq[j] <= q[j] || nq[j] >= N.count) {  // cannot happen for a valid partition
+        bad = true;
         active &= ~(1u << j);
         right &= ~(1u << j);
         continue;
       }
-      q[j] = nq;
-      if (nq >= is) active &= ~(1u << j);
+      q[j] = nq[j];
+      if (nq[j] >= is) active &= ~(1u << j);
     }
   }
-  if (active) atomicExch(err, 2);
+  if (active || bad) atomicExch(err, 2);
 #pragma unroll
   for (int j = 0; j < kPerT; ++j) {
     if (!(right >> j & 1u) || (active >> j & 1u)) continue;
