@@ -67,7 +67,7 @@ def parse_args():
                     help="boxes of 96^3 in the multi-step adjoint line (0: skip)")
     ap.add_argument("--clustered", type=int, default=256,
                     help="side of the clustered set of the leaf size x shape sweep (0: skip)")
-    ap.add_argument("--cpu-slab", type=float, default=0.25,
+    ap.add_argument("--cpu-slab", type=float, default=1.0,
                     help="fraction of the force box (along x) in the CPU sample")
     return ap.parse_args()
 
@@ -191,8 +191,17 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+# The reference nests a two-thread OpenMP team per tree split and keeps
+# nesting on during the list walk; with nesting capped at one level the same
+# code gives the same results 3-4x faster on these hosts.  The CPU timings use
+# the faster setting, so they understate the GPU's advantage rather than
+# overstate it.
+OMP_LEVELS = "1"
+
+
 def cpu_baseline(p, kp, slab: float, threads: int):
     """Reference force tree (CPU restatement) on a slab of the force box."""
+    os.environ["ORA_MAX_ACTIVE_LEVELS"] = OMP_LEVELS
     import oracle
     oracle.build()
     O = oracle.Oracle()
@@ -206,7 +215,8 @@ def cpu_baseline(p, kp, slab: float, threads: int):
     pairs = r.stats["pairs"]
     return {"value": pairs / dt, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": (f"leaves of the force box with x in [{lo:.1f}, {ks.max_force[0]:.1f}] "
-                       f"({pairs:.3e} pairs, full tree built), {dt:.2f} s wall"),
+                       f"({pairs:.3e} pairs, full tree built), {dt:.2f} s wall, "
+                       f"OpenMP nesting capped at {OMP_LEVELS} level"),
             "seconds": dt, "pairs": pairs}
 
 

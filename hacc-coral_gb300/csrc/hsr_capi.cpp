@@ -4,6 +4,10 @@
 
 #include <algorithm>
 #include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <functional>
+#include <mutex>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -95,6 +99,66 @@ constexpr int64_t kJSplit = 8192;
 
 }  // namespace
 
+// One background thread that issues host<->device copies of pageable arrays
+// (a pageable copy holds the calling thread while it is staged), so they run
+// while the calling thread drives the tree build.
+class CopyWorker {
+ public:
+  CopyWorker() : th_([this] { loop(); }) {}
+  ~CopyWorker() {
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      stop_ = true;
+    }
+    cv_.notify_all();
+    th_.join();
+  }
+  void submit(std::function<cudaError_t()> f) {
+    {
+      std::lock_guard<std::mutex> g(mu_);
+      q_.push_back(std::move(f));
+      ++pending_;
+    }
+    cv_.notify_all();
+  }
+  // Waits for every submitted task; returns the first error among them.
+  cudaError_t wait() {
+    std::unique_lock<std::mutex> g(mu_);
+    done_.wait(g, [this] { return pending_ == 0; });
+    const cudaError_t e = err_;
+    err_ = cudaSuccess;
+    return e;
+  }
+
+ private:
+  void loop() {
+    for (;;) {
+      std::function<cudaError_t()> f;
+      {
+        std::unique_lock<std::mutex> g(mu_);
+        cv_.wait(g, [this] { return stop_ || !q_.empty(); });
+        if (q_.empty()) return;
+        f = std::move(q_.front());
+        q_.pop_front();
+      }
+      const cudaError_t e = f();
+      {
+        std::lock_guard<std::mutex> g(mu_);
+        if (e != cudaSuccess && err_ == cudaSuccess) err_ = e;
+        --pending_;
+      }
+      done_.notify_all();
+    }
+  }
+  std::mutex mu_;
+  std::condition_variable cv_, done_;
+  std::deque<std::function<cudaError_t()>> q_;
+  int pending_ = 0;
+  bool stop_ = false;
+  cudaError_t err_ = cudaSuccess;
+  std::thread th_;
+};
+
 // Device state of one box of a multi-box kick.
 struct BoxState {
   hsr::DeviceTree tree;
@@ -124,6 +188,10 @@ struct hsr_ctx {
   int device = 0;
   cudaStream_t stream = nullptr;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+  // overlapped copies of the arrays off the critical path
+  cudaStream_t copy_stream = nullptr;
+  cudaEvent_t ev_in = nullptr, ev_perm = nullptr;
+  std::unique_ptr<CopyWorker> copier;
   std::unique_ptr<hsr::RcbHost> host;
   hsr::DeviceTree tree;
   // host-build path
@@ -218,6 +286,9 @@ hsr_status hsr_create(hsr_ctx **out, int device) {
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev1);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev2);
   if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev3);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->copy_stream, cudaStreamNonBlocking);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_in, cudaEventDisableTiming);
+  if (e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->ev_perm, cudaEventDisableTiming);
   if (e != cudaSuccess) {
     delete ctx;
     return HSR_ERR_CUDA;
@@ -242,9 +313,12 @@ hsr_status hsr_destroy(hsr_ctx *ctx) {
   for (auto &b : ctx->boxes)
     for (DevBuf *d : {&b->in, &b->out, &b->pos4, &b->vel}) d->release();
   ctx->boxes.clear();
-  for (cudaEvent_t ev : {ctx->ev0, ctx->ev1, ctx->ev2, ctx->ev3})
+  ctx->copier.reset();
+  if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
+  for (cudaEvent_t ev : {ctx->ev0, ctx->ev1, ctx->ev2, ctx->ev3, ctx->ev_in, ctx->ev_perm})
     if (ev) cudaEventDestroy(ev);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  if (ctx->copy_stream) cudaStreamDestroy(ctx->copy_stream);
   delete ctx;
   return HSR_OK;
 }
@@ -666,18 +740,49 @@ hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float
   const uint16_t *in_mask;
   char *ob = ctx->d_out.as<char>();
   const auto t_in = clk::now();
+  // Host arrays: x, y, z and mass (the tree build's input) are copied on the
+  // critical path; the other six arrays are copied by the context's copy
+  // thread on its own stream while the tree is built, and the permuted x, y,
+  // z, mass, phi, id and mask go back while the lists and the kick run.
+  const bool overlap = mem == HSR_MEM_HOST && n > 0;
+  // on every return, no copy of the caller's arrays may still be in flight
+  struct CopyGuard {
+    CopyWorker *w = nullptr;
+    ~CopyGuard() {
+      if (w) w->wait();
+    }
+  } guard;
   if (mem == HSR_MEM_HOST) {
     CU(ctx->d_in.ensure(A.bytes), "cudaMalloc(in)");
     char *ib = ctx->d_in.as<char>();
-    for (int i = 0; i < 8; ++i) {
-      CU(cudaMemcpyAsync(ib + A.f[i], arr[i], size_t(n) * 4, cudaMemcpyHostToDevice, s), "H2D arrays");
-      in[i] = reinterpret_cast<const float *>(ib + A.f[i]);
-    }
-    CU(cudaMemcpyAsync(ib + A.id, id, size_t(n) * 8, cudaMemcpyHostToDevice, s), "H2D ids");
-    CU(cudaMemcpyAsync(ib + A.mask, mask, size_t(n) * 2, cudaMemcpyHostToDevice, s), "H2D masks");
+    for (int i = 0; i < 8; ++i) in[i] = reinterpret_cast<const float *>(ib + A.f[i]);
+    for (int i : {0, 1, 2, 6})
+      CU(cudaMemcpyAsync(ib + A.f[i], arr[i], size_t(n) * 4, cudaMemcpyHostToDevice, s), "H2D positions");
     in_id = reinterpret_cast<const int64_t *>(ib + A.id);
     in_mask = reinterpret_cast<const uint16_t *>(ib + A.mask);
     st.h2d_bytes = n * 42;
+    if (overlap) {
+      if (!ctx->copier) ctx->copier.reset(new (std::nothrow) CopyWorker());
+      if (!ctx->copier) return ctx->fail(HSR_ERR_NOMEM, "copy thread");
+      guard.w = ctx->copier.get();
+      const int dev = ctx->device;
+      cudaStream_t s2 = ctx->copy_stream;
+      cudaEvent_t ev = ctx->ev_in;
+      float *src[4] = {arr[3], arr[4], arr[5], arr[7]};
+      char *dst[4] = {ib + A.f[3], ib + A.f[4], ib + A.f[5], ib + A.f[7]};
+      char *did = ib + A.id, *dmask = ib + A.mask;
+      const int64_t *hid = id;
+      const uint16_t *hmask = mask;
+      ctx->copier->submit([=]() -> cudaError_t {
+        cudaError_t e = cudaSetDevice(dev);
+        for (int i = 0; i < 4 && e == cudaSuccess; ++i)
+          e = cudaMemcpyAsync(dst[i], src[i], size_t(n) * 4, cudaMemcpyHostToDevice, s2);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(did, hid, size_t(n) * 8, cudaMemcpyHostToDevice, s2);
+        if (e == cudaSuccess) e = cudaMemcpyAsync(dmask, hmask, size_t(n) * 2, cudaMemcpyHostToDevice, s2);
+        if (e == cudaSuccess) e = cudaEventRecord(ev, s2);
+        return e;
+      });
+    }
   } else {
     for (int i = 0; i < 8; ++i) in[i] = arr[i];
     in_id = id;
@@ -719,6 +824,10 @@ hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float
   const hsr::DeviceTreeInfo &ti = ctx->tree.info();
   launches += ti.levels * 16 + 24;
   const int32_t *perm = ctx->tree.perm();
+  if (overlap) {
+    CU(ctx->copier->wait(), "H2D arrays (copy thread)");
+    CU(cudaStreamWaitEvent(s, ctx->ev_in, 0), "wait for the copies");
+  }
   // outputs in tree order: velocities to the kick buffer, the rest to d_out
   Work &w = ctx->work;
   set_work_params(w, p, n, ctx->tune);
@@ -738,6 +847,28 @@ hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float
                          reinterpret_cast<float *>(ob + A.f[6]), n, s),
      "unpack kernel");
   launches += 7;
+  if (overlap) {
+    // the permuted arrays other than the velocities go back now
+    CU(cudaEventRecord(ctx->ev_perm, s), "event");
+    const int dev = ctx->device;
+    cudaStream_t s2 = ctx->copy_stream;
+    cudaEvent_t ev = ctx->ev_perm;
+    float *dst[5] = {arr[0], arr[1], arr[2], arr[6], arr[7]};
+    const char *src[5] = {ob + A.f[0], ob + A.f[1], ob + A.f[2], ob + A.f[6], ob + A.f[7]};
+    const char *sid = ob + A.id, *smask = ob + A.mask;
+    int64_t *hid = id;
+    uint16_t *hmask = mask;
+    ctx->copier->submit([=]() -> cudaError_t {
+      cudaError_t e = cudaSetDevice(dev);
+      if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, ev, 0);
+      for (int i = 0; i < 5 && e == cudaSuccess; ++i)
+        e = cudaMemcpyAsync(dst[i], src[i], size_t(n) * 4, cudaMemcpyDeviceToHost, s2);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(hid, sid, size_t(n) * 8, cudaMemcpyDeviceToHost, s2);
+      if (e == cudaSuccess) e = cudaMemcpyAsync(hmask, smask, size_t(n) * 2, cudaMemcpyDeviceToHost, s2);
+      if (e == cudaSuccess) e = cudaStreamSynchronize(s2);
+      return e;
+    });
+  }
   w.table = ctx->tree.table();
   w.leaves = ctx->tree.leaves();
   w.idx = ctx->tree.index();
@@ -759,14 +890,18 @@ hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float
   CU(cudaMemcpyAsync(ovz, dv + 2 * n, size_t(n) * 4, cudaMemcpyDeviceToDevice, s), "copy vz");
   const cudaMemcpyKind back = mem == HSR_MEM_HOST ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice;
   for (int i = 0; i < 8; ++i)
-    CU(cudaMemcpyAsync(arr[i], ob + A.f[i], size_t(n) * 4, back, s), "copy arrays back");
-  CU(cudaMemcpyAsync(id, ob + A.id, size_t(n) * 8, back, s), "copy ids back");
-  CU(cudaMemcpyAsync(mask, ob + A.mask, size_t(n) * 2, back, s), "copy masks back");
+    if (!overlap || (i >= 3 && i <= 5))
+      CU(cudaMemcpyAsync(arr[i], ob + A.f[i], size_t(n) * 4, back, s), "copy arrays back");
+  if (!overlap) {
+    CU(cudaMemcpyAsync(id, ob + A.id, size_t(n) * 8, back, s), "copy ids back");
+    CU(cudaMemcpyAsync(mask, ob + A.mask, size_t(n) * 2, back, s), "copy masks back");
+  }
   unsigned long long counters[2] = {0, 0};
   if (!plain) CU(cudaMemcpyAsync(counters, ctx->d_queue.p, sizeof(counters), cudaMemcpyDeviceToHost, s),
                  "D2H counters");
   CU(cudaEventRecord(ctx->ev2, s), "event");
   CU(cudaStreamSynchronize(s), "kernel execution");
+  if (overlap) CU(ctx->copier->wait(), "D2H arrays (copy thread)");
   float fms = 0, oms = 0;
   CU(cudaEventElapsedTime(&fms, ctx->ev0, ctx->ev1), "event time");
   CU(cudaEventElapsedTime(&oms, ctx->ev1, ctx->ev2), "event time");
