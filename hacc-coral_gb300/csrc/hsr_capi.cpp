@@ -345,6 +345,7 @@ hsr_status check_params(const hsr_params *p, int64_t n, const void *const *arrs,
     return err = "unknown force law", HSR_ERR_ARG;
   if (p->kernel != HSR_KERNEL_AUTO && p->kernel != HSR_KERNEL_PLAIN && p->kernel != HSR_KERNEL_BATCHED)
     return err = "unknown kernel", HSR_ERR_ARG;
+  if (p->tree != HSR_TREE_RCB && p->tree != HSR_TREE_RCO) return err = "unknown tree kind", HSR_ERR_ARG;
   // int32 position-table indices: particles plus pseudo-particles of <= 2n+1 nodes
   if (n > (int64_t(INT32_MAX) - 64) / (1 + 2 * int64_t(p->tdpts)))
     return err = "too many particles for one call", HSR_ERR_ARG;
@@ -364,6 +365,7 @@ hsr::TreeParams tree_params(const hsr_params *p) {
   tp.nd = p->nd;
   tp.ppc = p->ppc;
   tp.tdpts = p->tdpts;
+  tp.tree = p->tree;
   return tp;
 }
 
@@ -935,14 +937,16 @@ hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, 
   if (mem != HSR_MEM_HOST && mem != HSR_MEM_DEVICE) return ctx->fail(HSR_ERR_ARG, "bad memory kind");
   if (p->build != HSR_BUILD_DEVICE && p->build != HSR_BUILD_HOST)
     return ctx->fail(HSR_ERR_ARG, "bad build location");
-  if (p->build == HSR_BUILD_HOST && mem != HSR_MEM_HOST)
-    return ctx->fail(HSR_ERR_UNSUPPORTED, "the host build takes host arrays");
+  // the RCO octree is built on the host
+  const bool host_build = p->build == HSR_BUILD_HOST || p->tree == HSR_TREE_RCO;
+  if (host_build && mem != HSR_MEM_HOST)
+    return ctx->fail(HSR_ERR_UNSUPPORTED, "the host build (and the RCO tree) takes host arrays");
   CU(cudaSetDevice(ctx->device), "cudaSetDevice");
   ctx->have_lists = false;
   ctx->tape = false;
   ctx->last_was_batch = false;
   hsr_stats st{};
-  hsr_status r = p->build == HSR_BUILD_HOST
+  hsr_status r = host_build
                      ? kick_host_build(ctx, p, n, x, y, z, vx, vy, vz, mass, phi, id, mask, st)
                      : kick_device_build(ctx, p, n, x, y, z, vx, vy, vz, mass, phi, id, mask, mem, st);
   if (r != HSR_OK) return r;
@@ -1021,6 +1025,8 @@ hsr_status hsr_subcycle(hsr_ctx *ctx, const hsr_subcycle_params *sp, int64_t n, 
   const void *arrs[10] = {x, y, z, vx, vy, vz, mass, phi, id, mask};
   if (hsr_status e = check_params(&sp->kick, n, arrs, ctx->err)) return e;
   if (mem != HSR_MEM_HOST && mem != HSR_MEM_DEVICE) return ctx->fail(HSR_ERR_ARG, "bad memory kind");
+  if (sp->kick.tree != HSR_TREE_RCB)
+    return ctx->fail(HSR_ERR_UNSUPPORTED, "the device sub-cycle builds the RCB tree only");
   if (sp->nsub < 0 || sp->ng[0] < 1 || sp->ng[1] < 1 || sp->ng[2] < 1 ||
       double(sp->ng[0]) * sp->ng[1] * sp->ng[2] >= 4294967295.0)
     return ctx->fail(HSR_ERR_ARG, "bad sub-cycle count or grid");
@@ -1105,6 +1111,8 @@ hsr_status force_fwd_impl(hsr_ctx *ctx, const hsr_params *p, int64_t n, const fl
   const void *arrs[10] = {x, y, z, dvx, dvy, dvz, mass, x, x, x};
   if (hsr_status e = check_params(p, n, arrs, ctx->err)) return e;
   if (mem != HSR_MEM_HOST && mem != HSR_MEM_DEVICE) return ctx->fail(HSR_ERR_ARG, "bad memory kind");
+  if (p->tree != HSR_TREE_RCB)
+    return ctx->fail(HSR_ERR_UNSUPPORTED, "the forward/adjoint pair builds the RCB tree only");
   CU(cudaSetDevice(ctx->device), "cudaSetDevice");
   ctx->have_lists = false;
   ctx->tape = false;
@@ -1330,8 +1338,8 @@ hsr_status hsr_tree_export(const hsr_ctx *ctx_c, int64_t *count, int64_t *offset
       const hsr::Node &N = H.node(t);
       count[t] = N.count;
       offset[t] = N.offset;
-      cl[t] = N.cl;
-      cr[t] = N.cr;
+      cl[t] = N.c[0];
+      cr[t] = N.c[1];
       tdr[t] = N.tdr;
       for (int i = 0; i < 3; ++i) {
         bbox9[9 * t + i] = N.xmin[i];
@@ -1399,6 +1407,8 @@ hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *para
     if (hsr_status e = check_params(&params[b], ns[b], arrs, ctx->err)) return e;
     if (params[b].law != params[0].law)
       return ctx->fail(HSR_ERR_UNSUPPORTED, "all boxes of a batch use one force law");
+    if (params[b].tree != HSR_TREE_RCB)
+      return ctx->fail(HSR_ERR_UNSUPPORTED, "the multi-box kick builds RCB trees only");
   }
   CU(cudaSetDevice(ctx->device), "cudaSetDevice");
   ctx->have_lists = false;

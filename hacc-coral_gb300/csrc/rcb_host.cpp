@@ -155,69 +155,105 @@ void pp_accum(int k, int64_t count, Src src, const float *xc, const float *px,
 
 RcbHost::RcbHost(int nthreads) : pool_(nthreads) {}
 
-int32_t RcbHost::alloc_pair() {
+int32_t RcbHost::alloc_nodes(int k) {
   std::lock_guard<std::mutex> g(alloc_mu_);
   int64_t i = num_alloc_.load();
-  num_alloc_.store(i + 2);
-  for (int64_t k = i; k < i + 2; ++k) {
-    auto &c = chunks_[k >> kChunkBits];
+  num_alloc_.store(i + k);
+  for (int64_t j = i; j < i + k; ++j) {
+    auto &c = chunks_[j >> kChunkBits];
     if (!c) c.reset(new Node[kChunk]);
-    N(k) = Node();
+    N(j) = Node();
   }
   return int32_t(i);
+}
+
+// Bounding box and centre of mass, in array order with double sums
+// (BGQCM.c:181-212; RCOForceTree.cxx's cm is the same).
+void RcbHost::node_stats(Node &T) {
+  const int64_t cnt = T.count;
+  const Elem *e = elems_.data() + T.offset;
+  double sx = 0, sy = 0, sz = 0, sm = 0;
+  for (int64_t i = 0; i < cnt; ++i) {
+    const Elem &q = e[i];
+    if (i == 0) {
+      T.xmin[0] = T.xmax[0] = q.x;
+      T.xmin[1] = T.xmax[1] = q.y;
+      T.xmin[2] = T.xmax[2] = q.z;
+    } else {
+      T.xmin[0] = std::fmin(T.xmin[0], q.x);
+      T.xmax[0] = std::fmax(T.xmax[0], q.x);
+      T.xmin[1] = std::fmin(T.xmin[1], q.y);
+      T.xmax[1] = std::fmax(T.xmax[1], q.y);
+      T.xmin[2] = std::fmin(T.xmin[2], q.z);
+      T.xmax[2] = std::fmax(T.xmax[2], q.z);
+    }
+    const float w = q.m;
+    sx += double(w * q.x);
+    sy += double(w * q.y);
+    sz += double(w * q.z);
+    sm += double(w);
+  }
+  T.xc[0] = float(sx / sm);
+  T.xc[1] = float(sy / sm);
+  T.xc[2] = float(sz / sm);
+}
+
+// Pseudo-particles of a leaf from its own particles (RCBForceTree.cxx:788-800).
+void RcbHost::leaf_pseudo(Node &T) {
+  const int k = p_.tdpts;
+  const Elem *e = elems_.data() + T.offset;
+  T.tdr = p_.ppc * pptdr(T);
+  std::fill(T.ppm, T.ppm + 12, 0.0f);
+  if (T.count > k) {
+    float px[12], py[12], pz[12];
+    pppts(k, T.tdr, T.xc, px, py, pz);
+    auto own = [e](int64_t i, float &x, float &y, float &z, float &m) {
+      x = e[i].x; y = e[i].y; z = e[i].z; m = e[i].m;
+    };
+    pp_accum(k, T.count, own, T.xc, px, py, pz, T.ppm, T.tdr);
+  }
+}
+
+// Pseudo-particles of an inner node from its children, in child order
+// (RCBForceTree.cxx:856-889; RCOForceTree.cxx:716-737).
+void RcbHost::pseudo_from_children(Node &T, const int32_t *kids, int nk) {
+  const int k = p_.tdpts;
+  float px[12], py[12], pz[12];
+  T.tdr = p_.ppc * pptdr(T);
+  pppts(k, T.tdr, T.xc, px, py, pz);
+  std::fill(T.ppm, T.ppm + 12, 0.0f);
+  for (int j = 0; j < nk; ++j) {
+    const Node *C = &N(kids[j]);
+    if (C->count <= 0) continue;
+    if (C->count <= k) {
+      const Elem *ce = elems_.data() + C->offset;
+      auto src = [ce](int64_t i, float &x, float &y, float &z, float &m) {
+        x = ce[i].x; y = ce[i].y; z = ce[i].z; m = ce[i].m;
+      };
+      pp_accum(k, C->count, src, T.xc, px, py, pz, T.ppm, T.tdr);
+    } else {
+      float cx[12], cy[12], cz[12];
+      pppts(k, C->tdr, C->xc, cx, cy, cz);
+      const float *cm = C->ppm;
+      auto src = [&](int64_t i, float &x, float &y, float &z, float &m) {
+        x = cx[i]; y = cy[i]; z = cz[i]; m = cm[i];
+      };
+      pp_accum(k, k, src, T.xc, px, py, pz, T.ppm, T.tdr);
+    }
+  }
 }
 
 void RcbHost::build_node(int32_t tl, int depth) {
   Node &T = N(tl);
   const int64_t cnt = T.count, off = T.offset;
   Elem *e = elems_.data() + off;
-  const int k = p_.tdpts;
-
-  // Bounding box and centre of mass, in array order with double sums
-  // (BGQCM.c:181-212).
-  {
-    double sx = 0, sy = 0, sz = 0, sm = 0;
-    for (int64_t i = 0; i < cnt; ++i) {
-      const Elem &q = e[i];
-      if (i == 0) {
-        T.xmin[0] = T.xmax[0] = q.x;
-        T.xmin[1] = T.xmax[1] = q.y;
-        T.xmin[2] = T.xmax[2] = q.z;
-      } else {
-        T.xmin[0] = std::fmin(T.xmin[0], q.x);
-        T.xmax[0] = std::fmax(T.xmax[0], q.x);
-        T.xmin[1] = std::fmin(T.xmin[1], q.y);
-        T.xmax[1] = std::fmax(T.xmax[1], q.y);
-        T.xmin[2] = std::fmin(T.xmin[2], q.z);
-        T.xmax[2] = std::fmax(T.xmax[2], q.z);
-      }
-      const float w = q.m;
-      sx += double(w * q.x);
-      sy += double(w * q.y);
-      sz += double(w * q.z);
-      sm += double(w);
-    }
-    T.xc[0] = float(sx / sm);
-    T.xc[1] = float(sy / sm);
-    T.xc[2] = float(sz / sm);
-  }
-
-  auto own = [e](int64_t i, float &x, float &y, float &z, float &m) {
-    x = e[i].x; y = e[i].y; z = e[i].z; m = e[i].m;
-  };
-
+  node_stats(T);
   if (cnt <= p_.nd) {  // leaf (RCBForceTree.cxx:788-800)
-    T.tdr = p_.ppc * pptdr(T);
-    std::fill(T.ppm, T.ppm + 12, 0.0f);
-    if (cnt > k) {
-      float px[12], py[12], pz[12];
-      pppts(k, T.tdr, T.xc, px, py, pz);
-      pp_accum(k, cnt, own, T.xc, px, py, pz, T.ppm, T.tdr);
-    }
+    leaf_pseudo(T);
     return;
   }
 
-  const int32_t tlcl = alloc_pair(), tlcr = tlcl + 1;
+  const int32_t tlcl = alloc_nodes(2), tlcr = tlcl + 1;
   Node &L = N(tlcl), &R = N(tlcr);
   for (int i = 0; i < 3; ++i) {
     L.xmin[i] = R.xmin[i] = T.xmin[i];
@@ -249,10 +285,10 @@ void RcbHost::build_node(int32_t tl, int depth) {
   if (is != 0 && is != cnt) {
     L.count = is;
     R.count = cnt - is;
-    T.cl = tlcl;
+    T.c[0] = tlcl;
     L.offset = off;
     L.xmax[d] = split;
-    T.cr = tlcr;
+    T.c[1] = tlcr;
     R.offset = off + is;
     R.xmin[d] = split;
     if (depth < par_depth_) {
@@ -264,30 +300,72 @@ void RcbHost::build_node(int32_t tl, int depth) {
       build_node(tlcr, depth + 1);
     }
   }
+  const int32_t kids[2] = {tlcl, tlcr};
+  pseudo_from_children(T, kids, 2);
+}
 
-  // Pseudo-particles from the children (RCBForceTree.cxx:856-889).
-  float px[12], py[12], pz[12];
-  T.tdr = p_.ppc * pptdr(T);
-  pppts(k, T.tdr, T.xc, px, py, pz);
-  std::fill(T.ppm, T.ppm + 12, 0.0f);
-  for (const Node *C : {&L, &R}) {
-    if (C->count <= 0) continue;
-    if (C->count <= k) {
-      const Elem *ce = elems_.data() + C->offset;
-      auto src = [ce](int64_t i, float &x, float &y, float &z, float &m) {
-        x = ce[i].x; y = ce[i].y; z = ce[i].z; m = ce[i].m;
-      };
-      pp_accum(k, C->count, src, T.xc, px, py, pz, T.ppm, T.tdr);
-    } else {
-      float cx[12], cy[12], cz[12];
-      pppts(k, C->tdr, C->xc, cx, cy, cz);
-      const float *cm = C->ppm;
-      auto src = [&](int64_t i, float &x, float &y, float &z, float &m) {
-        x = cx[i]; y = cy[i]; z = cz[i]; m = cm[i];
-      };
-      pp_accum(k, k, src, T.xc, px, py, pz, T.ppm, T.tdr);
+// The RCO octree (RCOForceTree.cxx:580-738): every inner node splits all three
+// axes at its centre of mass into up to eight children.  Partition, in one
+// pass in array order: a particle of octant p < 7 (coordinates at or above
+// the split add 4, 2, 1 for x, y, z) moves to the end of octant p's run, and
+// the first particle of each later run moves to that run's end in turn; the
+// particles of octant 7 stay behind the runs.  (The reference's swap chain
+// starts from is[7] of a 7-entry array; the end of the processed range, i,
+// is the value the chain needs there.)
+void RcbHost::build_node_oct(int32_t tl, int depth) {
+  Node &T = N(tl);
+  const int64_t cnt = T.count, off = T.offset;
+  Elem *e = elems_.data() + off;
+  node_stats(T);
+  if (cnt <= p_.nd) {
+    leaf_pseudo(T);
+    return;
+  }
+  const int32_t c0 = alloc_nodes(8);
+  for (int j = 0; j < 8; ++j) {
+    Node &C = N(c0 + j);
+    for (int i = 0; i < 3; ++i) {
+      C.xmin[i] = T.xmin[i];
+      C.xmax[i] = T.xmax[i];
     }
   }
+  const float sx = T.xc[0], sy = T.xc[1], sz = T.xc[2];
+  int64_t is[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  for (int64_t i = 0; i < cnt; ++i) {
+    const int p = (e[i].x >= sx ? 4 : 0) + (e[i].y >= sy ? 2 : 0) + (e[i].z >= sz ? 1 : 0);
+    if (p == 7) continue;
+    is[7] = i;
+    std::swap(e[is[7]], e[i]);
+    for (int q = 7; q > p; --q) std::swap(e[is[q - 1]], e[is[q]]);
+    for (int q = p; q < 7; ++q) ++is[q];
+  }
+  bool div = false;
+  for (int q = 0; q < 7; ++q) div |= !(is[q] == 0 || is[q] == cnt);
+  int32_t kids[8];
+  for (int j = 0; j < 8; ++j) kids[j] = c0 + j;
+  if (div) {
+    int64_t counts[8];
+    counts[0] = is[0];
+    for (int q = 1; q < 7; ++q) counts[q] = is[q] - is[q - 1];
+    counts[7] = cnt - is[6];
+    int64_t coff = off;
+    std::vector<std::thread> ths;
+    for (int j = 0; j < 8; ++j) {
+      Node &C = N(c0 + j);
+      C.count = counts[j];
+      if (counts[j] <= 0) continue;
+      T.c[j] = c0 + j;
+      C.offset = coff;
+      coff += counts[j];
+    }
+    for (int j = 0; j < 8; ++j) {
+      if (T.c[j] <= 0) continue;
+      if (depth < par_depth_oct_) ths.emplace_back([this, c0, j, depth] { build_node_oct(c0 + j, depth + 1); });
+      else build_node_oct(c0 + j, depth + 1);
+    }
+    for (auto &th : ths) th.join();
+  }
+  pseudo_from_children(T, kids, 8);
 }
 
 void RcbHost::build(const TreeParams &p, int64_t n, const float *x, const float *y,
@@ -299,7 +377,7 @@ void RcbHost::build(const TreeParams &p, int64_t n, const float *x, const float 
     for (int64_t i = b; i < e; ++i) elems_[i] = Elem{x[i], y[i], z[i], m[i], int32_t(i)};
   });
   chunks_.clear();
-  chunks_.resize(size_t(((2 * n + 3) >> kChunkBits) + 2));
+  chunks_.resize(size_t((((p.tree == 1 ? 8 : 2) * n + 9) >> kChunkBits) + 2));
   num_alloc_.store(1);
   chunks_[0].reset(new Node[kChunk]);
   N(0) = Node();
@@ -312,7 +390,10 @@ void RcbHost::build(const TreeParams &p, int64_t n, const float *x, const float 
   }
   par_depth_ = 0;
   while ((1 << par_depth_) < 2 * pool_.size()) ++par_depth_;
-  build_node(0, 0);
+  par_depth_oct_ = 0;
+  while ((1 << (3 * par_depth_oct_)) < 2 * pool_.size()) ++par_depth_oct_;
+  if (p.tree == 1) build_node_oct(0, 0);
+  else build_node(0, 0);
 
   num_nodes_ = num_alloc_.load();
   flat_.resize(size_t(num_nodes_));
@@ -349,7 +430,7 @@ int64_t RcbHost::padded_pairs() const {
 int64_t RcbHost::nonempty_leaves() const {
   int64_t c = 0;
   for (int64_t t = 1; t < num_nodes_; ++t)
-    if (flat_[t].cl == 0 && flat_[t].cr == 0 && flat_[t].count > 0) ++c;
+    if (flat_[t].leaf() && flat_[t].count > 0) ++c;
   return c;
 }
 
@@ -387,8 +468,10 @@ void RcbHost::leaf_list(int64_t tl, std::vector<Seg> &out, std::vector<int32_t> 
     // Ancestors of the target: descend without interacting.  Tree ranges are
     // nested or disjoint, so containment of the target's range identifies them.
     if (t != tl && Q.offset <= T.offset && T.offset + T.count <= Q.offset + Q.count) {
-      if (Q.cl != tl && Q.cl > 0 && flat_[Q.cl].count > 0) st.push_back(Q.cl);
-      if (Q.cr != tl && Q.cr > 0 && flat_[Q.cr].count > 0) st.push_back(Q.cr);
+      for (int j = 0; j < 8; ++j) {
+        const int32_t c = Q.c[j];
+        if (c != tl && c > 0 && flat_[c].count > 0) st.push_back(c);
+      }
       continue;
     }
 
@@ -421,12 +504,14 @@ void RcbHost::leaf_list(int64_t tl, std::vector<Seg> &out, std::vector<int32_t> 
       else emit(n_ + int64_t(t) * k, k);
       continue;
     }
-    if (Q.cr == 0 && Q.cl == 0) {
+    if (Q.leaf()) {
       emit(Q.offset, Q.count);
       continue;
     }
-    if (Q.cl > 0 && flat_[Q.cl].count > 0 && close(flat_[Q.cl])) st.push_back(Q.cl);
-    if (Q.cr > 0 && flat_[Q.cr].count > 0 && close(flat_[Q.cr])) st.push_back(Q.cr);
+    for (int j = 0; j < 8; ++j) {
+      const int32_t c = Q.c[j];
+      if (c > 0 && flat_[c].count > 0 && close(flat_[c])) st.push_back(c);
+    }
   }
   emit(T.offset, T.count);  // self interactions last
 }
@@ -440,7 +525,7 @@ void RcbHost::walk() {
     while (!q.empty()) {
       const int32_t tl = q.back();
       const Node &T = flat_[tl];
-      if (T.cr == 0 && T.cl == 0) {
+      if (T.leaf()) {
         q.pop_back();
         bool inside = true;
         for (int i = 0; i < 3; ++i)
@@ -451,8 +536,8 @@ void RcbHost::walk() {
         parents.pop_back();
         q.pop_back();
       } else {
-        if (T.cl > 0) q.push_back(T.cl);
-        if (T.cr > 0) q.push_back(T.cr);
+        for (int j = 0; j < 8; ++j)
+          if (T.c[j] > 0) q.push_back(T.c[j]);
         parents.push_back(tl);
       }
     }

@@ -48,9 +48,16 @@ class Pool {
 
 // Tree node (the reference's TreeNode, RCBForceTree.h:131-147), with int32
 // child indices and the pseudo-particles' own slot in the position table.
+// Children: c[0], c[1] (left, right) in the RCB tree, c[0..7] in the RCO
+// octree; 0 = none.
 struct Node {
   int64_t count = 0, offset = 0;
-  int32_t cl = 0, cr = 0;
+  int32_t c[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  bool leaf() const {
+    for (int i = 0; i < 8; ++i)
+      if (c[i] > 0) return false;
+    return true;
+  }
   float tdr = 0;
   float xmin[3] = {0, 0, 0}, xmax[3] = {0, 0, 0}, xc[3] = {0, 0, 0};
   float ppm[12] = {0};
@@ -68,6 +75,7 @@ struct TreeParams {
   int64_t nd;
   float ppc;
   int tdpts;
+  int tree;  // 0: RCB (binary, longest axis); 1: RCO (octree, all three axes)
 };
 
 // Work description of one kick: processed leaves and their list segments.
@@ -116,8 +124,12 @@ class RcbHost {
 
  private:
   Node &N(int64_t i) { return chunks_[i >> kChunkBits][i & (kChunk - 1)]; }
-  int32_t alloc_pair();
+  int32_t alloc_nodes(int k);
+  void node_stats(Node &T);
+  void leaf_pseudo(Node &T);
+  void pseudo_from_children(Node &T, const int32_t *kids, int nk);
   void build_node(int32_t tl, int depth);
+  void build_node_oct(int32_t tl, int depth);
   void leaf_list(int64_t tl, std::vector<Seg> &out, std::vector<int32_t> &stack) const;
 
   static constexpr int kChunkBits = 13;
@@ -131,7 +143,7 @@ class RcbHost {
   std::atomic<int64_t> num_alloc_{0};
   int64_t num_nodes_ = 0;
   std::vector<Node> flat_;
-  int par_depth_ = 0;
+  int par_depth_ = 0, par_depth_oct_ = 0;
   std::vector<LeafWork> leaves_;
   std::vector<Seg> segs_;
   int64_t list_entries_ = 0, pairs_ = 0;

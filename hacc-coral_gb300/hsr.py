@@ -26,6 +26,7 @@ STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory",
 MEM_HOST, MEM_DEVICE = 0, 1
 LAW_POLY6, LAW_POLY5_STEP16 = 0, 1
 KERNEL_AUTO, KERNEL_PLAIN, KERNEL_BATCHED = 0, 1, 2
+TREE_RCB, TREE_RCO = 0, 1
 BUILD_DEVICE, BUILD_HOST = 0, 1
 
 # Symbols the library exports (include/hacc_sr.h).
@@ -52,7 +53,7 @@ class HsrParams(C.Structure):
                 ("open_angle", C.c_float), ("nd", C.c_int64), ("ds", C.c_int64),
                 ("tmin", C.c_int64), ("fcoeff", C.c_float), ("ppc", C.c_float),
                 ("tdpts", C.c_int32), ("law", C.c_int32), ("kernel", C.c_int32),
-                ("build", C.c_int32)]
+                ("build", C.c_int32), ("tree", C.c_int32), ("reserved", C.c_int32)]
 
 
 class HsrSubcycleParams(C.Structure):
@@ -190,6 +191,7 @@ def make_params(kp, kernel: int = KERNEL_AUTO, build: int = BUILD_DEVICE) -> Hsr
     P.fcoeff, P.ppc, P.tdpts, P.law = kp.fcoeff, kp.ppc, kp.tdpts, kp.law
     P.kernel = kernel
     P.build = build
+    P.tree = getattr(kp, "tree", TREE_RCB)
     return P
 
 
@@ -528,6 +530,28 @@ def RCBForceTree(minLoc, maxLoc, minForceLoc, maxForceLoc, count, xLoc, yLoc, zL
     a.min_force, a.max_force = tuple(minForceLoc), tuple(maxForceLoc)
     a.avg_mass, a.fsrrmax, a.rsm, a.open_angle = avgMass, fsm, fl.rsm, oa
     a.nd, a.ds, a.tmin, a.fcoeff, a.ppc, a.tdpts, a.law = nd, ds, tmin, fcoeff, ppc, tdpts, fl.law
+    p = _Args()
+    p.n = int(count)
+    p.x, p.y, p.z, p.vx, p.vy, p.vz = xLoc, yLoc, zLoc, xVel, yVel, zVel
+    p.mass, p.phi, p.id, p.mask = mass, phiLoc, idLoc, maskLoc
+    return (ctx or default_context()).rcb_kick(p, a)
+
+
+def RCOForceTree(minLoc, maxLoc, minForceLoc, maxForceLoc, count, xLoc, yLoc, zLoc, xVel, yVel,
+                 zVel, mass, phiLoc, idLoc, maskLoc, avgMass, fsm, oa, nd=1, ds=1, fl=None,
+                 fcoeff=0.0, ppc=0.9, tdpts=1, ctx: Context | None = None):
+    """The RCOForceTree<TDPTS> constructor (src/halo_finder/RCOForceTree.h:
+    95-121, RCOForceTree.cxx:326-412): the octree variant -- every inner node
+    split along all three axes at its centre of mass.  The softening comes
+    from `fl` (a ForceLawSR), as in the reference."""
+    if fl is None:
+        raise HsrError(5, "fl=None selects ForceLawNewton in the reference; pass a ForceLawSR")
+    a = _Args()
+    a.min, a.max = tuple(minLoc), tuple(maxLoc)
+    a.min_force, a.max_force = tuple(minForceLoc), tuple(maxForceLoc)
+    a.avg_mass, a.fsrrmax, a.rsm, a.open_angle = avgMass, fsm, fl.rsm, oa
+    a.nd, a.ds, a.tmin, a.fcoeff, a.ppc, a.tdpts, a.law = nd, ds, 0, fcoeff, ppc, tdpts, fl.law
+    a.tree = TREE_RCO
     p = _Args()
     p.n = int(count)
     p.x, p.y, p.z, p.vx, p.vy, p.vz = xLoc, yLoc, zLoc, xVel, yVel, zVel

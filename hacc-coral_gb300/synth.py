@@ -308,6 +308,7 @@ class KickParams:
     ppc: float = 0.9
     tdpts: int = 1
     law: int = 0
+    tree: int = 0  # 0: RCBForceTree, 1: RCOForceTree
 
 
 def kick_params(p: Particles, nd: int = 128, rsm: float = 0.1, open_angle: float = 0.1,

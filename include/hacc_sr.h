@@ -86,7 +86,20 @@ typedef struct hsr_params {
   int32_t law;                      /* HSR_LAW_*                                */
   int32_t kernel;                   /* HSR_KERNEL_*                             */
   int32_t build;                    /* HSR_BUILD_*                              */
+  int32_t tree;                     /* HSR_TREE_* (0 = RCB)                     */
+  int32_t reserved;                 /* 0                                        */
 } hsr_params;
+
+/* Tree kinds.  HSR_TREE_RCB is RCBForceTree (binary splits along the longest
+ * axis at the centre of mass, src/halo_finder/RCBForceTree.cxx:778-890).
+ * HSR_TREE_RCO is RCOForceTree (src/halo_finder/RCOForceTree.cxx:580-738: up
+ * to eight children, all three axes split at the centre of mass), selected by
+ * HACC's -O option (src/cpu/Particles.cxx:1259-1310); its tree and lists are
+ * built on the host (hsr_rcb_kick with host arrays, hsr_build_lists), the
+ * pairs on the device.  The reference's RCO partition reads past its 7-entry
+ * split array (RCOForceTree.cxx:607-608); this build uses the end of the
+ * processed range there, the value that makes the partition valid. */
+enum { HSR_TREE_RCB = 0, HSR_TREE_RCO = 1 };
 
 /* Statistics of the last call on a context. */
 typedef struct hsr_stats {

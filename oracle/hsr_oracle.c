@@ -115,8 +115,11 @@ double ora_law_dg_f64(int law, double rsm, double r2) {
 /* allocation never moves a node another thread is using.                    */
 /* ------------------------------------------------------------------------- */
 
+/* Children: c[0], c[1] (left, right) for the RCB tree, c[0..7] for the RCO
+ * octree; 0 = none.  A node without children is a leaf. */
 typedef struct onode {
-  int64_t count, offset, cl, cr;
+  int64_t count, offset;
+  int64_t c[8];
   float ppm[12];
   float tdr;
   float xmin[3], xmax[3], xc[3];
@@ -349,10 +352,10 @@ static void split_node(obuild *B, int d, int64_t tl, int64_t tlcl, int64_t tlcr)
   onode *L = NODE(&B->pool, tlcl), *R = NODE(&B->pool, tlcr);
   L->count = is;
   R->count = T->count - is;
-  T->cl = tlcl;
+  T->c[0] = tlcl;
   L->offset = off;
   L->xmax[d] = split;
-  T->cr = tlcr;
+  T->c[1] = tlcr;
   R->offset = off + is;
   R->xmin[d] = split;
 #ifdef _OPENMP
@@ -431,6 +434,112 @@ static void build_node(obuild *B, int64_t tl) {
   memset(T->ppm, 0, sizeof(T->ppm));
   if (L->count > 0) pp_from_child(B, T, L, ppx, ppy, ppz, T->ppm);
   if (R->count > 0) pp_from_child(B, T, R, ppx, ppy, ppz, T->ppm);
+}
+
+/* ------------------------------------------------------------------------- */
+/* RCO octree build (RCOForceTree.cxx:580-738)                               */
+/* ------------------------------------------------------------------------- */
+
+static int is_leaf(const onode *N) {
+  for (int i = 0; i < 8; ++i)
+    if (N->c[i] > 0) return 0;
+  return 1;
+}
+
+static void swap10(obuild *B, int64_t a, int64_t b) {
+  float t;
+  int64_t ti;
+  uint16_t tm;
+#define SWAPF(arr) t = B->arr[a]; B->arr[a] = B->arr[b]; B->arr[b] = t
+  SWAPF(x); SWAPF(y); SWAPF(z); SWAPF(vx); SWAPF(vy); SWAPF(vz); SWAPF(m); SWAPF(phi);
+#undef SWAPF
+  ti = B->id[a]; B->id[a] = B->id[b]; B->id[b] = ti;
+  tm = B->mask[a]; B->mask[a] = B->mask[b]; B->mask[b] = tm;
+}
+
+/* partition (RCOForceTree.cxx:580-623): one pass in array order; a particle
+ * of octant p < 7 (x, y, z at or above the split add 4, 2, 1) goes to the
+ * end of octant p's run, the first particle of each later run moving up to
+ * the end of the next run in turn; is[q] ends as the end of octant q's run. */
+static void partition_oct(obuild *B, int64_t off, int64_t n, const float *pv, int64_t *is) {
+  for (int q = 0; q < 7; ++q) is[q] = 0;
+  for (int64_t i = 0; i < n; ++i) {
+    int p = 0;
+    if (B->x[off + i] >= pv[0]) p += 4;
+    if (B->y[off + i] >= pv[1]) p += 2;
+    if (B->z[off + i] >= pv[2]) p += 1;
+    if (p >= 7) continue;
+    swap10(B, off + is[6], off + i);
+    for (int q = 6; q > p; --q) swap10(B, off + is[q - 1], off + is[q]);
+    for (int q = p; q < 7; ++q) ++is[q];
+  }
+}
+
+/* createRCOForceTreeInParallel / createRCOForceSubtree
+ * (RCOForceTree.cxx:625-738): split all three axes at the centre of mass
+ * into up to eight children, built depth first in order. */
+static void build_node_oct(obuild *B, int64_t tl) {
+  onode *T = NODE(&B->pool, tl);
+  int64_t cnt = T->count, off = T->offset;
+  int k = B->tdpts;
+
+  cm((int)cnt, B->x + off, B->y + off, B->z + off, B->m + off, T->xmin, T->xmax, T->xc);
+
+  if (cnt <= B->nd) {
+    T->tdr = B->ppc * pptdr(T->xmin, T->xmax, T->xc);
+    memset(T->ppm, 0, sizeof(T->ppm));
+    if (cnt > k) {
+      float ppx[12], ppy[12], ppz[12];
+      pppts(k, T->tdr, T->xc, ppx, ppy, ppz);
+      pp_accum(k, cnt, B->x + off, B->y + off, B->z + off, B->m + off, T->xc, ppx,
+               ppy, ppz, T->ppm, T->tdr);
+    }
+    return;
+  }
+
+  int64_t c0 = pool_alloc(&B->pool, 8);
+  if (c0 < 0) { B->failed = 1; return; }
+  T = NODE(&B->pool, tl);
+  for (int j = 0; j < 8; ++j) {
+    onode *C = NODE(&B->pool, c0 + j);
+    for (int i = 0; i < 3; ++i) {
+      C->xmin[i] = T->xmin[i];
+      C->xmax[i] = T->xmax[i];
+    }
+  }
+  float split[3] = {T->xc[0], T->xc[1], T->xc[2]};
+  int64_t is[7];
+  partition_oct(B, off, cnt, split, is);
+  int div = 0;
+  for (int q = 0; q < 7; ++q)
+    if (!(is[q] == 0 || is[q] == cnt)) div = 1;
+  if (div) {
+    int64_t counts[8];
+    counts[0] = is[0];
+    for (int q = 1; q < 7; ++q) counts[q] = is[q] - is[q - 1];
+    counts[7] = cnt - is[6];
+    int64_t coff = off;
+    for (int j = 0; j < 8; ++j) {
+      onode *C = NODE(&B->pool, c0 + j);
+      C->count = counts[j];
+      if (counts[j] > 0) {
+        T->c[j] = c0 + j;
+        C->offset = coff;
+        coff += counts[j];
+        build_node_oct(B, c0 + j);
+        if (B->failed) return;
+      }
+    }
+  }
+
+  float ppx[12], ppy[12], ppz[12];
+  T->tdr = B->ppc * pptdr(T->xmin, T->xmax, T->xc);
+  pppts(k, T->tdr, T->xc, ppx, ppy, ppz);
+  memset(T->ppm, 0, sizeof(T->ppm));
+  for (int j = 0; j < 8; ++j) {
+    const onode *C = NODE(&B->pool, c0 + j);
+    if (C->count > 0 && T->c[j] > 0) pp_from_child(B, T, C, ppx, ppy, ppz, T->ppm);
+  }
 }
 
 /* ------------------------------------------------------------------------- */
@@ -606,9 +715,10 @@ static int leaf_walk(const owalk *W, int64_t tl, const int64_t *parents, int64_t
     const onode *N = NODE(P, tln);
 
     if (tln < tl && is_ancestor(parents, np, tln)) {
-      int64_t c1 = N->cr, c0 = N->cl;
-      if (c0 != tl && c0 > 0 && NODE(P, c0)->count > 0) QPUSH(c0);
-      if (c1 != tl && c1 > 0 && NODE(P, c1)->count > 0) QPUSH(c1);
+      for (int j = 0; j < 8; ++j) {
+        int64_t c = N->c[j];
+        if (c != tl && c > 0 && NODE(P, c)->count > 0) QPUSH(c);
+      }
       continue;
     }
 
@@ -654,15 +764,16 @@ static int leaf_walk(const owalk *W, int64_t tl, const int64_t *parents, int64_t
       }
       if (W->vmax > 0 && L->size >= W->vmax) return ORA_ERR_VMAX;
       continue;
-    } else if (N->cr == 0 && N->cl == 0) {
+    } else if (is_leaf(N)) {
       if (!append_particles(L, W, N->offset, N->count)) return ORA_ERR_NOMEM;
       if (W->vmax > 0 && L->size >= W->vmax) return ORA_ERR_VMAX;
       continue;
     }
 
-    int64_t c1 = N->cr, c0 = N->cl;
-    if (c0 > 0 && NODE(P, c0)->count > 0 && box_close(T, NODE(P, c0), W->fsrrmax)) QPUSH(c0);
-    if (c1 > 0 && NODE(P, c1)->count > 0 && box_close(T, NODE(P, c1), W->fsrrmax)) QPUSH(c1);
+    for (int j = 0; j < 8; ++j) {
+      int64_t c = N->c[j];
+      if (c > 0 && NODE(P, c)->count > 0 && box_close(T, NODE(P, c), W->fsrrmax)) QPUSH(c);
+    }
   }
 #undef QPUSH
 
@@ -697,7 +808,8 @@ ora_result *ora_rcb_run(const ora_params *p, int64_t n, float *x, float *y, floa
                         int *err) {
   *err = ORA_OK;
   if (!p || n < 0 || (n > 0 && (!x || !y || !z || !vx || !vy || !vz || !mass || !phi || !id || !mask)) ||
-      (p->tdpts != 1 && p->tdpts != 12) || p->nd < 1 || n >= ((int64_t)1 << 31)) {
+      (p->tdpts != 1 && p->tdpts != 12) || p->nd < 1 || n >= ((int64_t)1 << 31) ||
+      (p->tree != ORA_TREE_RCB && p->tree != ORA_TREE_RCO)) {
     *err = ORA_ERR_ARG;
     return NULL;
   }
@@ -727,7 +839,11 @@ ora_result *ora_rcb_run(const ora_params *p, int64_t n, float *x, float *y, floa
   double t0 = now_s();
   obuild B;
   memset(&B, 0, sizeof(B));
-  if (!pool_init(&B.pool, 2 * n + 3)) { free(R); *err = ORA_ERR_NOMEM; return NULL; }
+  if (!pool_init(&B.pool, (p->tree == ORA_TREE_RCO ? 8 : 2) * n + 9)) {
+    free(R);
+    *err = ORA_ERR_NOMEM;
+    return NULL;
+  }
   B.x = x; B.y = y; B.z = z; B.vx = vx; B.vy = vy; B.vz = vz; B.m = mass; B.phi = phi;
   B.id = id; B.mask = mask; B.tdpts = p->tdpts; B.nd = p->nd; B.ppc = p->ppc;
   int64_t root = pool_alloc(&B.pool, 1);
@@ -735,7 +851,8 @@ ora_result *ora_rcb_run(const ora_params *p, int64_t n, float *x, float *y, floa
   T0->count = n;
   T0->offset = 0;
   for (int i = 0; i < 3; ++i) { T0->xmin[i] = p->min[i]; T0->xmax[i] = p->max[i]; }
-  build_node(&B, root);
+  if (p->tree == ORA_TREE_RCO) build_node_oct(&B, root);
+  else build_node(&B, root);
   double t1 = now_s();
   R->pool = B.pool;
   if (B.failed) { *err = ORA_ERR_NOMEM; ora_result_free(R); return NULL; }
@@ -753,7 +870,7 @@ ora_result *ora_rcb_run(const ora_params *p, int64_t n, float *x, float *y, floa
   while (qn > 0) {
     int64_t tl = q[qn - 1];
     const onode *N = NODE(P, tl);
-    if (N->cr == 0 && N->cl == 0) {
+    if (is_leaf(N)) {
       --qn;
       int inside = 1;
       for (int i = 0; i < 3; ++i)
@@ -776,9 +893,9 @@ ora_result *ora_rcb_run(const ora_params *p, int64_t n, float *x, float *y, floa
       --pn;
       --qn;
     } else {
-      if (qn + 2 > qc) { qc *= 2; q = (int64_t *)realloc(q, (size_t)qc * sizeof(int64_t)); }
-      if (N->cl > 0) q[qn++] = N->cl;
-      if (N->cr > 0) q[qn++] = N->cr;
+      if (qn + 8 > qc) { qc *= 2; q = (int64_t *)realloc(q, (size_t)qc * sizeof(int64_t)); }
+      for (int j = 0; j < 8; ++j)
+        if (N->c[j] > 0) q[qn++] = N->c[j];
       if (pn == pc) { pc *= 2; par = (int64_t *)realloc(par, (size_t)pc * sizeof(int64_t)); }
       par[pn++] = tl;
     }
@@ -839,7 +956,7 @@ ora_result *ora_rcb_run(const ora_params *p, int64_t n, float *x, float *y, floa
   R->st.nodes = P->size;
   for (int64_t t = 1; t < P->size; ++t) {
     const onode *N = NODE(P, t);
-    if (N->cl == 0 && N->cr == 0) {
+    if (is_leaf(N)) {
       if (N->count > 0) {
         R->st.leaves++;
         if (N->count > R->st.max_ppn) R->st.max_ppn = N->count;
@@ -908,8 +1025,8 @@ void ora_result_nodes(const ora_result *r, int64_t *count, int64_t *offset, int6
     const onode *N = NODE(&r->pool, t);
     count[t] = N->count;
     offset[t] = N->offset;
-    cl[t] = N->cl;
-    cr[t] = N->cr;
+    cl[t] = N->c[0];
+    cr[t] = N->c[1];
     tdr[t] = N->tdr;
     for (int i = 0; i < 3; ++i) {
       bbox9[9 * t + i] = N->xmin[i];

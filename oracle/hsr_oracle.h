@@ -47,7 +47,13 @@ typedef struct ora_params {
   int32_t vmax;                     /* >0: fail like the reference when a list
                                        reaches this many entries (VMAX = 16384)    */
   int32_t nthreads;                 /* 0 = OpenMP default                          */
+  int32_t tree;                     /* ORA_TREE_RCB or ORA_TREE_RCO                 */
 } ora_params;
+
+/* Tree kinds: RCBForceTree (binary splits along the longest axis) and
+ * RCOForceTree (src/halo_finder/RCOForceTree.cxx: up to eight children split
+ * along all three axes at the centre of mass). */
+enum { ORA_TREE_RCB = 0, ORA_TREE_RCO = 1 };
 
 typedef struct ora_stats {
   int64_t nodes;            /* tree nodes allocated (incl. unused split pairs)   */

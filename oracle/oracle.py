@@ -24,6 +24,9 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "_build", "libhsr_oracle.so")
 REF_EXE = os.path.join(HERE, "_ref", "rcb_ref")
+# the reference's RCOForceTree, built from a copy with its octant array sized
+# 8 (the file as shipped reads past that array; see oracle/Makefile)
+REF_RCO_EXE = os.path.join(HERE, "_ref", "rco_ref")
 
 LAW_POLY6 = 0
 LAW_POLY5_STEP16 = 1
@@ -44,7 +47,7 @@ class OraParams(C.Structure):
                 ("open_angle", C.c_float), ("nd", C.c_int64), ("ds", C.c_int64),
                 ("tmin", C.c_int64), ("fcoeff", C.c_float), ("ppc", C.c_float),
                 ("tdpts", C.c_int32), ("law", C.c_int32), ("vmax", C.c_int32),
-                ("nthreads", C.c_int32)]
+                ("nthreads", C.c_int32), ("tree", C.c_int32)]
 
 
 class OraStats(C.Structure):
@@ -69,6 +72,7 @@ def params_struct(kp, nthreads: int = 0, vmax: int = 0) -> OraParams:
     P.nd, P.ds, P.tmin = kp.nd, kp.ds, kp.tmin
     P.fcoeff, P.ppc, P.tdpts, P.law = kp.fcoeff, kp.ppc, kp.tdpts, kp.law
     P.vmax, P.nthreads = vmax, nthreads
+    P.tree = getattr(kp, "tree", 0)
     return P
 
 
@@ -355,7 +359,7 @@ _PFMT = "<16f3q2f6i"
 def write_case(path: str, p, kp, nthreads: int = 0, reps: int = 1) -> None:
     head = struct.pack(_PFMT, *kp.min, *kp.max, *kp.min_force, *kp.max_force, kp.avg_mass,
                        kp.fsrrmax, kp.rsm, kp.open_angle, kp.nd, kp.ds, kp.tmin, kp.fcoeff,
-                       kp.ppc, kp.tdpts, kp.law, 0, nthreads, reps, 0)
+                       kp.ppc, kp.tdpts, kp.law, 0, nthreads, reps, getattr(kp, "tree", 0))
     with open(path, "wb") as f:
         f.write(CASE_MAGIC)
         f.write(struct.pack("<q", p.n))
@@ -386,22 +390,24 @@ def _unlimited_stack():
     resource.setrlimit(resource.RLIMIT_STACK, (resource.RLIM_INFINITY, resource.RLIM_INFINITY))
 
 
-def reference_available() -> bool:
-    return os.path.exists(REF_EXE)
+def reference_available(tree: int = 0) -> bool:
+    return os.path.exists(REF_RCO_EXE if tree == 1 else REF_EXE)
 
 
 def run_reference(p, kp, nthreads: int = 0, reps: int = 1, timeout: float = 3600.0):
     """Runs the reference force tree on a copy of `p`; returns (arrays after the
     last repetition, list of wall times in seconds)."""
-    if not reference_available():
-        raise FileNotFoundError(REF_EXE)
+    tree = getattr(kp, "tree", 0)
+    exe = REF_RCO_EXE if tree == 1 else REF_EXE
+    if not reference_available(tree):
+        raise FileNotFoundError(exe)
     with tempfile.TemporaryDirectory() as td:
         cin, cout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
         write_case(cin, p, kp, nthreads, reps)
         env = dict(os.environ, OMP_STACKSIZE="256M")
         if nthreads > 0:
             env["OMP_NUM_THREADS"] = str(nthreads)
-        r = subprocess.run([REF_EXE, cin, cout], env=env, capture_output=True, text=True,
+        r = subprocess.run([exe, cin, cout], env=env, capture_output=True, text=True,
                            preexec_fn=_unlimited_stack, timeout=timeout)
         if r.returncode != 0:
             raise RuntimeError(f"reference run failed ({r.returncode}): {r.stderr[-2000:]}")

@@ -15,6 +15,9 @@
 #include "ForceLaw.h"
 #include "Partition.h"
 #include "RCBForceTree.h"
+#ifdef HSR_REF_RCO
+#include "RCOForceTree.h"
+#endif
 
 #include <chrono>
 #include <cstdint>
@@ -33,7 +36,8 @@ struct CaseParams {
   float avg_mass, fsrrmax, rsm, open_angle;
   int64_t nd, ds, tmin;
   float fcoeff, ppc;
-  int32_t tdpts, law, vmax, nthreads, reps, pad;
+  int32_t tdpts, law, vmax, nthreads, reps;
+  int32_t tree;  // 0: RCBForceTree; 1: RCOForceTree (builds with HSR_REF_RCO only)
 };
 
 template <typename T>
@@ -86,6 +90,24 @@ int main(int argc, char **argv) {
     wid = id;
     wmask = mask;
     auto t0 = std::chrono::steady_clock::now();
+#ifdef HSR_REF_RCO
+    if (P.tree == 1 && P.tdpts == 1) {
+      RCOMonopoleForceTree t(P.min, P.max, P.min_force, P.max_force, n, w[0].data(), w[1].data(),
+                             w[2].data(), w[3].data(), w[4].data(), w[5].data(), w[6].data(),
+                             w[7].data(), wid.data(), wmask.data(), P.avg_mass, P.fsrrmax,
+                             P.open_angle, P.nd, P.ds, &fl, P.fcoeff, P.ppc);
+    } else if (P.tree == 1) {
+      RCOQuadrupoleForceTree t(P.min, P.max, P.min_force, P.max_force, n, w[0].data(),
+                               w[1].data(), w[2].data(), w[3].data(), w[4].data(), w[5].data(),
+                               w[6].data(), w[7].data(), wid.data(), wmask.data(), P.avg_mass,
+                               P.fsrrmax, P.open_angle, P.nd, P.ds, &fl, P.fcoeff, P.ppc);
+    } else
+#else
+    if (P.tree != 0) {
+      fprintf(stderr, "this driver runs RCBForceTree only (build rco_ref for RCOForceTree)\n");
+      return 3;
+    }
+#endif
     if (P.tdpts == 1) {
       RCBMonopoleForceTree t(P.min, P.max, P.min_force, P.max_force, n, w[0].data(), w[1].data(),
                              w[2].data(), w[3].data(), w[4].data(), w[5].data(), w[6].data(),

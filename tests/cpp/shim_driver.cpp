@@ -1,5 +1,6 @@
-// Calls the drop-in RCBForceTree (include/RCBForceTree_gb300.h) the way
-// Particles::map2 constructs the reference tree, on one case file written by
+// Calls the drop-in RCBForceTree / RCOForceTree (include/RCBForceTree_gb300.h,
+// include/RCOForceTree_gb300.h) the way Particles::map2 constructs the
+// reference trees, on one case file written by
 // oracle/oracle.py (write_case), and writes the arrays back in the same format.
 // Exit status 3 with a message when the library cannot run (no device).
 #include <cstdio>
@@ -8,13 +9,14 @@
 #include <vector>
 
 #include "RCBForceTree_gb300.h"
+#include "RCOForceTree_gb300.h"
 
 struct CaseParams {
   float min[3], max[3], min_force[3], max_force[3];
   float avg_mass, fsrrmax, rsm, open_angle;
   int64_t nd, ds, tmin;
   float fcoeff, ppc;
-  int32_t tdpts, law, vmax, nthreads, reps, pad;
+  int32_t tdpts, law, vmax, nthreads, reps, tree;
 };
 
 int main(int argc, char **argv) {
@@ -37,7 +39,22 @@ int main(int argc, char **argv) {
   int token = 0;
   ForceLaw *fl = reinterpret_cast<ForceLaw *>(&token);  // stands for HACC's m_fl
   try {
-    if (P.tdpts == 1) {
+    if (P.tree == 1) {
+      hacc_sr_gb300::set_rco_softening(P.rsm);
+      if (P.tdpts == 1) {
+        RCOMonopoleForceTree t(P.min, P.max, P.min_force, P.max_force, n, a[0].data(),
+                               a[1].data(), a[2].data(), a[3].data(), a[4].data(), a[5].data(),
+                               a[6].data(), a[7].data(), id.data(), mask.data(), P.avg_mass,
+                               P.fsrrmax, P.open_angle, P.nd, P.ds, fl, P.fcoeff, P.ppc);
+        printf("pairs %lld\n", (long long)t.stats().pairs);
+      } else {
+        RCOQuadrupoleForceTree t(P.min, P.max, P.min_force, P.max_force, n, a[0].data(),
+                                 a[1].data(), a[2].data(), a[3].data(), a[4].data(), a[5].data(),
+                                 a[6].data(), a[7].data(), id.data(), mask.data(), P.avg_mass,
+                                 P.fsrrmax, P.open_angle, P.nd, P.ds, fl, P.fcoeff, P.ppc);
+        printf("pairs %lld\n", (long long)t.stats().pairs);
+      }
+    } else if (P.tdpts == 1) {
       RCBMonopoleForceTree t(P.min, P.max, P.min_force, P.max_force, n, a[0].data(), a[1].data(),
                              a[2].data(), a[3].data(), a[4].data(), a[5].data(), a[6].data(),
                              a[7].data(), id.data(), mask.data(), P.avg_mass, P.fsrrmax, P.rsm,

@@ -1,10 +1,12 @@
-"""Writes the golden fixtures of the RCB short-range kick.
+"""Writes the golden fixtures of the RCB and RCO short-range kicks.
 
 Each fixture holds a seeded input particle set, the constructor arguments, and
 the ten arrays after the reference's own RCBForceTree constructor ran on it
 (oracle/_ref/rcb_ref: the reference sources compiled unmodified, single
-thread).  Run from the repository root in a checkout that has the reference
-tree and `make -C oracle ref` built:
+thread) -- or, for the *_rco fixtures, its RCOForceTree constructor
+(oracle/_ref/rco_ref: RCOForceTree.cxx with its octant array sized 8, the one
+change it needs to run; see oracle/Makefile).  Run from the repository root in
+a checkout that has the reference tree and `make -C oracle ref` built:
 
     python tests/golden/make_golden.py
 
@@ -73,6 +75,11 @@ def cases():
     kp = synth.kick_params(p, nd=64, fcoeff=1.0)
     kp.min_force, kp.max_force = (-1.0, -1.0, -1.0), (7.0, 7.0, 7.0)
     out.append(("single_leaf40", p, kp))
+    # E-G: the RCO octree (RCOForceTree): uniform random, Zel'dovich with
+    # quadrupole pseudo-particles, and the clumped set with a wide opening angle
+    for name, p, kp in list(out[:3]):
+        kp2 = synth.KickParams(**{**kp.__dict__, "tree": 1})
+        out.append((name + "_rco", p, kp2))
     return out
 
 
@@ -84,7 +91,7 @@ def main():
         arrays.update({f"out_{k}": res[k] for k in synth.FIELDS})
         params = np.array([*kp.min, *kp.max, *kp.min_force, *kp.max_force, kp.avg_mass, kp.fsrrmax,
                            kp.rsm, kp.open_angle, kp.nd, kp.ds, kp.tmin, kp.fcoeff, kp.ppc,
-                           kp.tdpts, kp.law], dtype=np.float64)
+                           kp.tdpts, kp.law, kp.tree], dtype=np.float64)
         path = os.path.join(OUT, f"{name}.npz")
         np.savez_compressed(path, params=params, nglt=np.array(p.nglt), **arrays)
         print(f"{name}: n={p.n} -> {path} ({os.path.getsize(path)} bytes, {times[0]:.3f} s)")

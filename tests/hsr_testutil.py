@@ -30,7 +30,8 @@ def load_golden(name):
                           max_force=tuple(v[9:12]), avg_mass=float(v[12]), fsrrmax=float(v[13]),
                           rsm=float(v[14]), open_angle=float(v[15]), nd=int(v[16]), ds=int(v[17]),
                           tmin=int(v[18]), fcoeff=float(v[19]), ppc=float(v[20]),
-                          tdpts=int(v[21]), law=int(v[22]))
+                          tdpts=int(v[21]), law=int(v[22]),
+                          tree=int(v[23]) if len(v) > 23 else 0)
     out = {k: d["out_" + k] for k in synth.FIELDS}
     return p, kp, out
 

@@ -29,6 +29,22 @@ def test_oracle_matches_reference_live(oracle_lib, nd, tdpts, oa):
         assert np.array_equal(getattr(q, k).view(np.uint8), ref[k].view(np.uint8)), k
 
 
+@pytest.mark.skipif(not oracle.reference_available(1), reason="RCO reference build absent")
+@pytest.mark.parametrize("nd,tdpts,oa", [(64, 1, 0.1), (16, 12, 0.5), (8, 1, 0.1)])
+def test_oracle_rco_matches_reference_live(oracle_lib, nd, tdpts, oa):
+    """The RCO octree restatement against the reference's RCOForceTree
+    (oracle/_ref/rco_ref: its octant array sized 8, otherwise unmodified)."""
+    p = synth.clustered_box(16, nhalo=20, seed=98)
+    kp = synth.kick_params(p, nd=nd, tdpts=tdpts, open_angle=oa)
+    kp.tree = 1
+    q = p.copy()
+    st = oracle_lib.rcb_run(q, kp, nthreads=4).stats
+    ref, _, _ = oracle.run_reference(p, kp, nthreads=4)
+    for k in synth.FIELDS:
+        assert np.array_equal(getattr(q, k).view(np.uint8), ref[k].view(np.uint8)), k
+    assert st["processed_leaves"] > 0
+
+
 def test_oracle_law_matches_fp64(oracle_lib):
     r2 = np.linspace(0.0, 9.7, 977)
     for x in r2:
