@@ -2,7 +2,8 @@
 
 Device code is compiled for sm_103a only.  Host code is compiled with
 -ffp-contract=off so the tree and list decisions round exactly as the
-reference's x86-64 build does.  Translation units compile in parallel.
+reference's x86-64 build does.  Translation units compile in parallel.  The
+PM kick's transforms link cuFFT from the same toolkit.
 """
 from __future__ import annotations
 
@@ -76,7 +77,9 @@ def build(force: bool = False, verbose: bool = False) -> str:
             if verbose and msg:
                 print(msg, file=sys.stderr)
     if force or jobs or _needs(LIB, objs):
-        cmd = [nv, "-shared"] + ARCH + ["-Xcompiler", "-fPIC", "-o", LIB] + objs + ["-lpthread"]
+        cudalib = os.path.join(os.path.dirname(os.path.dirname(os.path.realpath(nv))), "lib64")
+        cmd = ([nv, "-shared"] + ARCH + ["-Xcompiler", "-fPIC", "-o", LIB] + objs
+               + ["-lcufft", "-lpthread", "-Xlinker", "-rpath=" + cudalib])
         run(cmd)
     return LIB
 

@@ -1,6 +1,7 @@
 // hsr_capi.cpp -- the C ABI (include/hacc_sr.h) over the host tree and the
 // sm_103a kernels.
 #include "hacc_sr.h"
+#include "hacc_pm.h"
 
 #include <algorithm>
 #include <chrono>
@@ -24,6 +25,7 @@
 #include "subcycle.cuh"
 #include "rcb_host.hpp"
 #include "sr_kernels.cuh"
+#include "pm.cuh"
 
 namespace {
 
@@ -218,6 +220,10 @@ struct hsr_ctx {
   int batch_group = 32;
   // launch shapes (hsr_set_tune / hsr_autotune)
   hsr_tune tune{HSR_KERNEL_BATCHED, 128, 32, 0};
+  // long-range PM kick (hacc_pm.h)
+  std::unique_ptr<hsr_pm::Solver> pm;
+  DevBuf d_pm;
+  hsr_pm_stats pm_stats{};
 
   // Launches a pair kernel on the current work (the batched kernel's queue
   // counter and evaluated-pair counter are reset first).
@@ -1823,6 +1829,158 @@ hsr_status hsr_probe_fp32_peak(hsr_ctx *ctx, double *tflops) {
     best = std::max(best, flops / (double(ms) * 1e-3) / 1e12);
   }
   *tflops = best;
+  return HSR_OK;
+}
+
+}  // extern "C"
+
+// ---- long-range PM kick (hacc_pm.h) -------------------------------------
+
+namespace {
+
+hsr_status pm_check(hsr_ctx *ctx, const hsr_pm_params *p, int64_t n, const void *const *arrs,
+                    int narr, int32_t mem) {
+  if (!p) return ctx->fail(HSR_ERR_ARG, "null PM params");
+  if (n < 0) return ctx->fail(HSR_ERR_ARG, "negative particle count");
+  if (n > 0)
+    for (int i = 0; i < narr; ++i)
+      if (!arrs[i]) return ctx->fail(HSR_ERR_ARG, "null particle array");
+  if (p->ng < 2 || (p->ng & 1) || p->ng > 4096)
+    return ctx->fail(HSR_ERR_ARG, "ng must be even and in [2, 4096]");
+  // GridExchange fills the ngo + 1 upper dead cells from the alive block
+  if (p->ngo < 0 || p->ngo >= p->ng) return ctx->fail(HSR_ERR_ARG, "ngo must be in [0, ng)");
+  if (p->precision != HSR_PM_F64 && p->precision != HSR_PM_F32)
+    return ctx->fail(HSR_ERR_ARG, "unknown PM precision");
+  if (mem != HSR_MEM_HOST && mem != HSR_MEM_DEVICE) return ctx->fail(HSR_ERR_ARG, "bad memory kind");
+  return HSR_OK;
+}
+
+hsr_pm::Params pm_params(const hsr_pm_params *p) {
+  hsr_pm::Params q;
+  q.ng = p->ng;
+  q.ngo = p->ngo;
+  q.gpscal = p->gpscal;
+  q.fscal = p->fscal;
+  q.tau = p->tau;
+  q.prec = p->precision == HSR_PM_F32 ? hsr_pm::PREC_F32 : hsr_pm::PREC_F64;
+  return q;
+}
+
+hsr_status pm_prepare(hsr_ctx *ctx, const hsr_pm::Params &q) {
+  if (!ctx->pm) ctx->pm.reset(new (std::nothrow) hsr_pm::Solver());
+  if (!ctx->pm) return ctx->fail(HSR_ERR_NOMEM, "PM solver");
+  std::string err;
+  if (!ctx->pm->prepare(q.ng, q.prec, ctx->stream, &err)) return ctx->fail(HSR_ERR_CUDA, err);
+  return HSR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+hsr_status hsr_pm_tables(int32_t ng, double *filter, double *denom, double *gradient) {
+  if (ng < 2 || (ng & 1) || !filter || !denom || !gradient) return HSR_ERR_ARG;
+  hsr_pm::quiet_tables(ng, filter, denom, gradient);
+  return HSR_OK;
+}
+
+hsr_status hsr_pm_kick(hsr_ctx *ctx, const hsr_pm_params *p, int64_t n, const float *x,
+                       const float *y, const float *z, float *vx, float *vy, float *vz,
+                       int32_t mem) {
+  if (!ctx) return HSR_ERR_ARG;
+  const auto t0 = clk::now();
+  const void *arrs[6] = {x, y, z, vx, vy, vz};
+  hsr_status st = pm_check(ctx, p, n, arrs, 6, mem);
+  if (st != HSR_OK) return st;
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  const hsr_pm::Params q = pm_params(p);
+  if ((st = pm_prepare(ctx, q)) != HSR_OK) return st;
+  cudaStream_t s = ctx->stream;
+  hsr_pm_stats ps{};
+  const float *dx = x, *dy = y, *dz = z;
+  float *dvx = vx, *dvy = vy, *dvz = vz;
+  const size_t nb = size_t(n) * sizeof(float);
+  if (mem == HSR_MEM_HOST && n > 0) {
+    CU(ctx->d_pm.ensure(6 * nb), "cudaMalloc(PM particles)");
+    float *b = ctx->d_pm.as<float>();
+    dx = b;
+    dy = b + n;
+    dz = b + 2 * n;
+    dvx = b + 3 * n;
+    dvy = b + 4 * n;
+    dvz = b + 5 * n;
+    CU(cudaEventRecord(ctx->ev0, s), "event");
+    const float *src[6] = {x, y, z, vx, vy, vz};
+    for (int a = 0; a < 6; ++a)
+      CU(cudaMemcpyAsync(b + a * n, src[a], nb, cudaMemcpyHostToDevice, s), "PM copy in");
+    CU(cudaEventRecord(ctx->ev1, s), "event");
+    CU(cudaEventSynchronize(ctx->ev1), "PM copy in");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ps.t_h2d_ms = ms;
+    ps.h2d_bytes = int64_t(6 * nb);
+  }
+  cudaEvent_t ev[4] = {ctx->ev0, ctx->ev1, ctx->ev2, ctx->ev3};
+  hsr_pm::Timing tm;
+  std::string err;
+  if (!ctx->pm->kick(q, n, dx, dy, dz, dvx, dvy, dvz, s, ev, &tm, &err))
+    return ctx->fail(HSR_ERR_CUDA, err);
+  if (mem == HSR_MEM_HOST && n > 0) {
+    CU(cudaEventRecord(ctx->ev0, s), "event");
+    float *dst[3] = {vx, vy, vz};
+    for (int a = 0; a < 3; ++a)
+      CU(cudaMemcpyAsync(dst[a], ctx->d_pm.as<float>() + (3 + a) * n, nb, cudaMemcpyDeviceToHost, s),
+         "PM copy out");
+    CU(cudaEventRecord(ctx->ev1, s), "event");
+    CU(cudaEventSynchronize(ctx->ev1), "PM copy out");
+    float ms = 0;
+    cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+    ps.t_d2h_ms = ms;
+    ps.d2h_bytes = int64_t(3 * nb);
+  }
+  ps.t_deposit_ms = tm.deposit_ms;
+  ps.t_solve_ms = tm.solve_ms;
+  ps.t_interp_ms = tm.interp_ms;
+  ps.kernel_launches = tm.launches;
+  ps.fft_execs = tm.fft_execs;
+  ps.t_total_ms = ms_since(t0);
+  ctx->pm_stats = ps;
+  return HSR_OK;
+}
+
+hsr_status hsr_pm_fields(hsr_ctx *ctx, const hsr_pm_params *p, int64_t n, const float *x,
+                         const float *y, const float *z, float *rho, float *grad, int32_t mem) {
+  if (!ctx) return HSR_ERR_ARG;
+  const void *arrs[3] = {x, y, z};
+  hsr_status st = pm_check(ctx, p, n, arrs, 3, mem);
+  if (st != HSR_OK) return st;
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  const hsr_pm::Params q = pm_params(p);
+  if ((st = pm_prepare(ctx, q)) != HSR_OK) return st;
+  cudaStream_t s = ctx->stream;
+  const float *dx = x, *dy = y, *dz = z;
+  const size_t nb = size_t(n) * sizeof(float);
+  if (mem == HSR_MEM_HOST && n > 0) {
+    CU(ctx->d_pm.ensure(3 * nb), "cudaMalloc(PM particles)");
+    float *b = ctx->d_pm.as<float>();
+    const float *src[3] = {x, y, z};
+    for (int a = 0; a < 3; ++a)
+      CU(cudaMemcpyAsync(b + a * n, src[a], nb, cudaMemcpyHostToDevice, s), "PM copy in");
+    dx = b;
+    dy = b + n;
+    dz = b + 2 * n;
+  }
+  std::string err;
+  if (!ctx->pm->deposit(q, n, dx, dy, dz, s, &err)) return ctx->fail(HSR_ERR_CUDA, err);
+  if (grad && !ctx->pm->solve(s, &err)) return ctx->fail(HSR_ERR_CUDA, err);
+  if (!ctx->pm->export_fields(rho, grad, mem == HSR_MEM_HOST, s, &err))
+    return ctx->fail(HSR_ERR_CUDA, err);
+  return HSR_OK;
+}
+
+hsr_status hsr_pm_get_stats(const hsr_ctx *ctx, hsr_pm_stats *st) {
+  if (!ctx || !st) return HSR_ERR_ARG;
+  *st = ctx->pm_stats;
   return HSR_OK;
 }
 

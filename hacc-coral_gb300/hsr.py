@@ -37,7 +37,11 @@ EXPORTS = ("hsr_create", "hsr_destroy", "hsr_last_error", "hsr_version", "hsr_rc
            "hsr_force_fwd", "hsr_force_vjp", "hsr_last_perm", "hsr_tree_size", "hsr_tree_export",
            "hsr_lists_export_index", "hsr_rcb_kick_batch", "hsr_bench_pairs_graph",
            "hsr_subcycle", "hsr_set_tune", "hsr_get_tune", "hsr_autotune",
-           "hsr_force_kick", "hsr_stream")
+           "hsr_force_kick", "hsr_stream",
+           # include/hacc_pm.h
+           "hsr_pm_kick", "hsr_pm_fields", "hsr_pm_get_stats", "hsr_pm_tables")
+
+PM_F64, PM_F32 = 0, 1
 
 
 class HsrError(RuntimeError):
@@ -54,6 +58,30 @@ class HsrParams(C.Structure):
                 ("tmin", C.c_int64), ("fcoeff", C.c_float), ("ppc", C.c_float),
                 ("tdpts", C.c_int32), ("law", C.c_int32), ("kernel", C.c_int32),
                 ("build", C.c_int32), ("tree", C.c_int32), ("reserved", C.c_int32)]
+
+
+class HsrPmParams(C.Structure):
+    """hsr_pm_params (include/hacc_pm.h)."""
+    _fields_ = [("ng", C.c_int32), ("ngo", C.c_int32), ("gpscal", C.c_float),
+                ("fscal", C.c_float), ("tau", C.c_float), ("precision", C.c_int32)]
+
+
+class HsrPmStats(C.Structure):
+    _fields_ = [("t_total_ms", C.c_double), ("t_h2d_ms", C.c_double),
+                ("t_deposit_ms", C.c_double), ("t_solve_ms", C.c_double),
+                ("t_interp_ms", C.c_double), ("t_d2h_ms", C.c_double),
+                ("h2d_bytes", C.c_int64), ("d2h_bytes", C.c_int64),
+                ("kernel_launches", C.c_int64), ("fft_execs", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def pm_params(ng: int, ngo: int, gpscal: float = 1.0, fscal: float = 1.0, tau: float = 1.0,
+              precision: int = PM_F64) -> HsrPmParams:
+    P = HsrPmParams()
+    P.ng, P.ngo, P.gpscal, P.fscal, P.tau, P.precision = ng, ngo, gpscal, fscal, tau, precision
+    return P
 
 
 class HsrSubcycleParams(C.Structure):
@@ -168,8 +196,28 @@ def load(path: str = LIB_PATH):
     lib.hsr_get_tune.argtypes = [vp, C.POINTER(HsrTune)]
     lib.hsr_autotune.restype = i32
     lib.hsr_autotune.argtypes = [vp, i32, i32, C.POINTER(HsrTuneRow), i32, C.POINTER(C.c_int32)]
+    lib.hsr_pm_kick.argtypes = [vp, C.POINTER(HsrPmParams), i64] + [vp] * 6 + [i32]
+    lib.hsr_pm_kick.restype = i32
+    lib.hsr_pm_fields.argtypes = [vp, C.POINTER(HsrPmParams), i64] + [vp] * 5 + [i32]
+    lib.hsr_pm_fields.restype = i32
+    lib.hsr_pm_get_stats.argtypes = [vp, C.POINTER(HsrPmStats)]
+    lib.hsr_pm_get_stats.restype = i32
+    lib.hsr_pm_tables.argtypes = [i32, C.POINTER(C.c_double), C.POINTER(C.c_double),
+                                  C.POINTER(C.c_double)]
+    lib.hsr_pm_tables.restype = i32
     _lib = lib
     return lib
+
+
+def pm_tables(ng: int):
+    """hsr_pm_tables: the quiet solver's (filter, denominator, gradient)
+    tables as the library computes them (host code, no device)."""
+    lib = load()
+    out = [np.zeros(ng, np.float64) for _ in range(3)]
+    st = lib.hsr_pm_tables(ng, *[_p(a, C.c_double) for a in out])
+    if st != HSR_OK:
+        raise HsrError(st, "hsr_pm_tables")
+    return tuple(out)
 
 
 def _p(a, ct):
@@ -314,6 +362,43 @@ class Context:
         ptr = lambda t: C.c_void_p(t.data_ptr())
         self._check(self.lib.hsr_force_vjp(self.h, ptr(ux), ptr(uy), ptr(uz), ptr(xbx), ptr(xby),
                                            ptr(xbz), MEM_DEVICE), "hsr_force_vjp")
+
+    # ---- long-range PM kick (include/hacc_pm.h) ---------------------------
+    def pm_kick(self, x, y, z, vx, vy, vz, params: HsrPmParams) -> dict:
+        """hsr_pm_kick on host float32 arrays (velocities kicked in place);
+        returns the call's hsr_pm_stats."""
+        n = len(x)
+        for a, nm in ((x, "x"), (y, "y"), (z, "z"), (vx, "vx"), (vy, "vy"), (vz, "vz")):
+            _check_host(a, np.float32, n, nm)
+        vp = lambda a: a.ctypes.data_as(C.c_void_p)
+        self._check(self.lib.hsr_pm_kick(self.h, C.byref(params), n, vp(x), vp(y), vp(z), vp(vx),
+                                         vp(vy), vp(vz), MEM_HOST), "hsr_pm_kick")
+        return self.pm_stats()
+
+    def pm_kick_device(self, x, y, z, vx, vy, vz, params: HsrPmParams) -> dict:
+        """hsr_pm_kick on device buffers (objects with data_ptr())."""
+        ptr = lambda t: C.c_void_p(t.data_ptr())
+        self._check(self.lib.hsr_pm_kick(self.h, C.byref(params), int(x.numel()), ptr(x), ptr(y),
+                                         ptr(z), ptr(vx), ptr(vy), ptr(vz), MEM_DEVICE),
+                    "hsr_pm_kick(device arrays)")
+        return self.pm_stats()
+
+    def pm_fields(self, x, y, z, params: HsrPmParams, grad: bool = True):
+        """hsr_pm_fields on host positions: (rho (ng,ng,ng), grad (3,ng,ng,ng)
+        or None), float32, x the slowest index."""
+        ng = params.ng
+        xs = [np.ascontiguousarray(a, np.float32) for a in (x, y, z)]
+        rho = np.zeros((ng, ng, ng), np.float32)
+        g = np.zeros((3, ng, ng, ng), np.float32) if grad else None
+        vp = lambda a: a.ctypes.data_as(C.c_void_p) if a is not None else None
+        self._check(self.lib.hsr_pm_fields(self.h, C.byref(params), len(xs[0]), *[vp(a) for a in xs],
+                                           vp(rho), vp(g), MEM_HOST), "hsr_pm_fields")
+        return rho, g
+
+    def pm_stats(self) -> dict:
+        s = HsrPmStats()
+        self._check(self.lib.hsr_pm_get_stats(self.h, C.byref(s)), "hsr_pm_get_stats")
+        return s.as_dict()
 
     def stream_device(self, x, y, z, vx, vy, vz, alpha, pp, tau, adot):
         """hsr_stream (Particles::map1) on device buffers: x += pt v."""
