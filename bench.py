@@ -21,6 +21,11 @@ the force box, fused with the velocity kick.
                 pairs than the list holds; `value` counts the list's pairs.
 * cpu_baseline -- the CPU restatement of the reference force tree (oracle),
                 timed on this host's cores on a bounded slab of the workload.
+* treepm     -- the long-range PM kick on the same box (deposit, FFT solve,
+                inverse CIC; double and single precision) and one whole
+                TreePM step (PM half kick, 5 short-range sub-cycles, PM kick)
+                end to end from host arrays, with the PM restatement timed on
+                the host.
 
 `--impl reference` times that CPU path alone as the reference arm.  Under
 torchrun each rank runs an independent replica on its own GPU (the path does
@@ -67,6 +72,8 @@ def parse_args():
                     help="boxes of 96^3 in the multi-step adjoint line (0: skip)")
     ap.add_argument("--clustered", type=int, default=256,
                     help="side of the clustered set of the leaf size x shape sweep (0: skip)")
+    ap.add_argument("--treepm", type=int, default=1,
+                    help="time the PM kick and one full TreePM step on the bench box (0: skip)")
     ap.add_argument("--cpu-slab", type=float, default=1.0,
                     help="fraction of the force box (along x) in the CPU sample")
     return ap.parse_args()
@@ -218,6 +225,78 @@ def cpu_baseline(p, kp, slab: float, threads: int):
                        f"({pairs:.3e} pairs, full tree built), {dt:.2f} s wall, "
                        f"OpenMP nesting capped at {OMP_LEVELS} level"),
             "seconds": dt, "pairs": pairs}
+
+
+def treepm_section(ctx, p0, kp, args, device: int, cpu: bool):
+    """The PM kick (hsr_pm_kick) on device-resident arrays of the bench box,
+    double and single precision, and one TreePM step (hsr_treepm_step: PM
+    half kick, 5 short-range sub-cycles, PM kick) end to end from host
+    arrays; with the numpy restatement of the PM kick timed on the host."""
+    import torch
+    import hsr
+    import treepm
+    ng, ngo = p0.meta["ng"], p0.meta["ngo"]
+    dev = torch.device("cuda", device)
+    t = [torch.from_numpy(np.ascontiguousarray(a)).to(dev) for a in (p0.x, p0.y, p0.z, p0.vx,
+                                                                     p0.vy, p0.vz)]
+    torch.cuda.synchronize()
+    ts = synth.stepper()
+    kick = {}
+    for name, prec in (("f64", hsr.PM_F64), ("f32", hsr.PM_F32)):
+        prm = treepm.pm_params(ts, 0.5, ng, ngo, precision=prec)
+        for _ in range(3):
+            ctx.pm_kick_device(*t, prm)
+        rows = [ctx.pm_kick_device(*t, prm) for _ in range(max(3, args.steps))]
+        med = {k: float(np.median([r[k] for r in rows]))
+               for k in ("t_deposit_ms", "t_solve_ms", "t_interp_ms")}
+        dev_ms = med["t_deposit_ms"] + med["t_solve_ms"] + med["t_interp_ms"]
+        v = [a.copy() for a in (p0.vx, p0.vy, p0.vz)]
+        ctx.pm_kick(p0.x, p0.y, p0.z, *v, prm)
+        e2e = []
+        for _ in range(3):
+            v = [a.copy() for a in (p0.vx, p0.vy, p0.vz)]
+            t0 = time.perf_counter()
+            ctx.pm_kick(p0.x, p0.y, p0.z, *v, prm)
+            e2e.append(time.perf_counter() - t0)
+        hs = ctx.pm_stats()
+        kick[name] = {**{k: round(v, 4) for k, v in med.items()}, "device_ms": round(dev_ms, 4),
+                      "particles_per_s": p0.n / (dev_ms * 1e-3),
+                      "e2e_ms": round(1e3 * min(e2e), 4), "h2d_bytes": hs["h2d_bytes"],
+                      "d2h_bytes": hs["d2h_bytes"], "kernel_launches": rows[-1]["kernel_launches"],
+                      "fft_execs": rows[-1]["fft_execs"]}
+    del t
+    # one step of the loop: the first step of a run has both PM kicks
+    nsub = 5
+    sp = treepm.plan(50.0, 10.0, 10)[0]
+    T = treepm.step_params(sp, kp, nsub, ng, ngo, p0.nglt)
+    treepm.step(ctx, p0.copy(), T)
+    steps = []
+    for _ in range(2):
+        q = p0.copy()
+        t0 = time.perf_counter()
+        r = treepm.step(ctx, q, T)
+        steps.append((time.perf_counter() - t0, r))
+    wall, r = min(steps, key=lambda a: a[0])
+    out = {"n_side": ng, "n_particles": p0.n, "pm_kick": kick,
+           "step": {"s_per_step": wall, "sub_cycles": nsub, "pm_kicks": 2,
+                    "sr_tree_build_ms": r["sr"]["t_build_ms"], "sr_lists_ms": r["sr"]["t_walk_ms"],
+                    "sr_force_ms": r["sr"]["t_force_ms"], "sr_pairs": r["sr"]["pairs"],
+                    "pm_deposit_ms": r["pm"]["t_deposit_ms"], "pm_solve_ms": r["pm"]["t_solve_ms"],
+                    "pm_interp_ms": r["pm"]["t_interp_ms"],
+                    "h2d_bytes": r["sr"]["h2d_bytes"], "d2h_bytes": r["sr"]["d2h_bytes"]},
+           "note": "PM kick: deposit + FFT solve + inverse CIC on the whole box; step: "
+                   "driver_hires.cxx's loop body (PM half kick, subCycle, PM kick)"}
+    if cpu:
+        import pm_oracle
+        t0 = time.perf_counter()
+        pm_oracle.pm_kick(p0.x, p0.y, p0.z, p0.vx, p0.vy, p0.vz, ng, ngo, 1.0, 1.0, 1e-3)
+        sec = time.perf_counter() - t0
+        out["pm_cpu_baseline"] = {"value": p0.n / sec, "unit": "particles/s", "cores": 1,
+                                  "kind": "port", "seconds": sec,
+                                  "sample": f"one PM kick of the {ng}^3 box, numpy restatement "
+                                            "(float64, one thread; the reference's PM needs FFTW "
+                                            "and MPI)"}
+    return out
 
 
 def run_reference_arm(args, world, rank):
@@ -383,6 +462,12 @@ def main():
                               for r in sw["rows"]]}
         del pc
 
+    # ---- long-range PM kick and one whole TreePM step on the bench box ----
+    treepm_line = None
+    if args.treepm:
+        treepm_line = treepm_section(ctx, p0, kp, args, local,
+                                     cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(p0, kp, args.cpu_slab, os.cpu_count() or 1)
@@ -406,6 +491,7 @@ def main():
             "multibox": multibox,
             "clustered": clustered,
             "multistep_adjoint": multistep_line,
+            "treepm": treepm_line,
             "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                          "frac": achieved / peak if peak else None,
                          "traffic": profiled_traffic(cfg["workload"], cfg["shape"]),

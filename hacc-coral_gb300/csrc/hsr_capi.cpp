@@ -931,6 +931,46 @@ hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float
 
 }  // namespace
 
+namespace {
+
+// The sub-cycles of hsr_subcycle on arrays already resident on the device
+// (f: x, y, z, vx, vy, vz, mass, phi): nsub times stream, resort, masses = 1,
+// kick, stream.  Statistics of the kicks are summed into `total`.
+hsr_status subcycle_resident(hsr_ctx *ctx, const hsr_subcycle_params *sp, int64_t n, float **f,
+                             int64_t *ids, uint16_t *msk, int64_t *inbox, hsr_stats &total) {
+  cudaStream_t s = ctx->stream;
+  CU(ctx->d_sort.ensure(hsr::resort_scratch_bytes(n)), "cudaMalloc(sort)");
+  // map1's prefactor in float, as the reference computes it
+  const float pf = std::pow(sp->pp, float(1.0 + 1.0 / sp->alpha));
+  const float prefactor = float(1.0 / (sp->alpha * sp->adot * pf));
+  const float pt = prefactor * sp->tau;
+  for (int32_t step = 0; step < sp->nsub; ++step) {
+    if (!sp->skip_stream) CU(hsr::launch_stream(f[0], f[1], f[2], f[3], f[4], f[5], n, pt, s), "stream");
+    if (!sp->skip_kick) {
+      CU(hsr::resort_by_cell(n, sp->ng, f, ids, msk, ctx->d_sort.p, inbox, s), "resort");
+      CU(hsr::launch_fill(f[6], n, 1.0f, s), "masses");
+      hsr_stats st{};
+      hsr_status r = kick_device_build(ctx, &sp->kick, *inbox, f[0], f[1], f[2], f[3], f[4], f[5],
+                                       f[6], f[7], ids, msk, HSR_MEM_DEVICE, st);
+      if (r != HSR_OK) return r;
+      total.pairs += st.pairs;
+      total.evaluated_pairs += st.evaluated_pairs;
+      total.list_entries += st.list_entries;
+      total.processed_leaves += st.processed_leaves;
+      total.nodes += st.nodes;
+      total.t_build_ms += st.t_build_ms;
+      total.t_walk_ms += st.t_walk_ms;
+      total.t_force_ms += st.t_force_ms;
+      total.cm_fallbacks += st.cm_fallbacks;
+      total.kernel_launches += st.kernel_launches;
+    }
+    if (!sp->skip_stream) CU(hsr::launch_stream(f[0], f[1], f[2], f[3], f[4], f[5], n, pt, s), "stream");
+  }
+  return HSR_OK;
+}
+
+}  // namespace
+
 extern "C" {
 
 hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, float *y, float *z,
@@ -1057,34 +1097,9 @@ hsr_status hsr_subcycle(hsr_ctx *ctx, const hsr_subcycle_params *sp, int64_t n, 
     ids = reinterpret_cast<int64_t *>(rb + A.id);
     msk = reinterpret_cast<uint16_t *>(rb + A.mask);
   }
-  CU(ctx->d_sort.ensure(hsr::resort_scratch_bytes(n)), "cudaMalloc(sort)");
-  // map1's prefactor in float, as the reference computes it
-  const float pf = std::pow(sp->pp, float(1.0 + 1.0 / sp->alpha));
-  const float prefactor = float(1.0 / (sp->alpha * sp->adot * pf));
-  const float pt = prefactor * sp->tau;
   hsr_stats total{};
   int64_t inbox = n;
-  for (int32_t step = 0; step < sp->nsub; ++step) {
-    if (!sp->skip_stream) CU(hsr::launch_stream(f[0], f[1], f[2], f[3], f[4], f[5], n, pt, s), "stream");
-    if (!sp->skip_kick) {
-      CU(hsr::resort_by_cell(n, sp->ng, f, ids, msk, ctx->d_sort.p, &inbox, s), "resort");
-      CU(hsr::launch_fill(f[6], n, 1.0f, s), "masses");
-      hsr_stats st{};
-      hsr_status r = kick_device_build(ctx, &sp->kick, inbox, f[0], f[1], f[2], f[3], f[4], f[5],
-                                       f[6], f[7], ids, msk, HSR_MEM_DEVICE, st);
-      if (r != HSR_OK) return r;
-      total.pairs += st.pairs;
-      total.evaluated_pairs += st.evaluated_pairs;
-      total.list_entries += st.list_entries;
-      total.processed_leaves += st.processed_leaves;
-      total.nodes += st.nodes;
-      total.t_build_ms += st.t_build_ms;
-      total.t_walk_ms += st.t_walk_ms;
-      total.t_force_ms += st.t_force_ms;
-      total.cm_fallbacks += st.cm_fallbacks;
-    }
-    if (!sp->skip_stream) CU(hsr::launch_stream(f[0], f[1], f[2], f[3], f[4], f[5], n, pt, s), "stream");
-  }
+  if (hsr_status r = subcycle_resident(ctx, sp, n, f, ids, msk, &inbox, total)) return r;
   if (mem == HSR_MEM_HOST) {
     float *out[8] = {x, y, z, vx, vy, vz, mass, phi};
     for (int i = 0; i < 8; ++i)
@@ -1975,6 +1990,86 @@ hsr_status hsr_pm_fields(hsr_ctx *ctx, const hsr_pm_params *p, int64_t n, const 
   if (grad && !ctx->pm->solve(s, &err)) return ctx->fail(HSR_ERR_CUDA, err);
   if (!ctx->pm->export_fields(rho, grad, mem == HSR_MEM_HOST, s, &err))
     return ctx->fail(HSR_ERR_CUDA, err);
+  return HSR_OK;
+}
+
+hsr_status hsr_treepm_step(hsr_ctx *ctx, const hsr_treepm_params *tp, int64_t n, float *x,
+                           float *y, float *z, float *vx, float *vy, float *vz, float *mass,
+                           float *phi, int64_t *id, uint16_t *mask, int32_t mem,
+                           int64_t *n_inbox) {
+  if (!ctx) return HSR_ERR_ARG;
+  if (!tp) return ctx->fail(HSR_ERR_ARG, "null parameters");
+  const auto t_start = clk::now();
+  const hsr_subcycle_params *sp = &tp->sub;
+  const void *arrs[10] = {x, y, z, vx, vy, vz, mass, phi, id, mask};
+  if (hsr_status e = check_params(&sp->kick, n, arrs, ctx->err)) return e;
+  if (sp->kick.tree != HSR_TREE_RCB)
+    return ctx->fail(HSR_ERR_UNSUPPORTED, "the device sub-cycle builds the RCB tree only");
+  if (sp->nsub < 0 || sp->ng[0] < 1 || sp->ng[1] < 1 || sp->ng[2] < 1 ||
+      double(sp->ng[0]) * sp->ng[1] * sp->ng[2] >= 4294967295.0)
+    return ctx->fail(HSR_ERR_ARG, "bad sub-cycle count or grid");
+  const bool open = tp->pm_open.tau != 0.0f;
+  if (open && pm_check(ctx, &tp->pm_open, n, arrs, 0, mem) != HSR_OK) return HSR_ERR_ARG;
+  if (pm_check(ctx, &tp->pm_close, n, arrs, 0, mem) != HSR_OK) return HSR_ERR_ARG;
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  ctx->tape = false;
+  ctx->last_was_batch = false;
+  cudaStream_t s = ctx->stream;
+  const ArrayLayout A(n);
+  float *f[8] = {x, y, z, vx, vy, vz, mass, phi};
+  int64_t *ids = id;
+  uint16_t *msk = mask;
+  if (mem == HSR_MEM_HOST) {
+    CU(ctx->d_res.ensure(A.bytes), "cudaMalloc(resident)");
+    char *rb = ctx->d_res.as<char>();
+    for (int i = 0; i < 8; ++i) {
+      CU(cudaMemcpyAsync(rb + A.f[i], f[i], size_t(n) * 4, cudaMemcpyHostToDevice, s), "H2D arrays");
+      f[i] = reinterpret_cast<float *>(rb + A.f[i]);
+    }
+    CU(cudaMemcpyAsync(rb + A.id, id, size_t(n) * 8, cudaMemcpyHostToDevice, s), "H2D ids");
+    CU(cudaMemcpyAsync(rb + A.mask, mask, size_t(n) * 2, cudaMemcpyHostToDevice, s), "H2D masks");
+    ids = reinterpret_cast<int64_t *>(rb + A.id);
+    msk = reinterpret_cast<uint16_t *>(rb + A.mask);
+  }
+  hsr_pm_stats pm{};
+  cudaEvent_t ev[4] = {ctx->ev0, ctx->ev1, ctx->ev2, ctx->ev3};
+  std::string err;
+  auto pm_kick = [&](const hsr_pm_params *pp) -> hsr_status {
+    const hsr_pm::Params q = pm_params(pp);
+    if (hsr_status r = pm_prepare(ctx, q)) return r;
+    hsr_pm::Timing tm;
+    if (!ctx->pm->kick(q, n, f[0], f[1], f[2], f[3], f[4], f[5], s, ev, &tm, &err))
+      return ctx->fail(HSR_ERR_CUDA, err);
+    pm.t_deposit_ms += tm.deposit_ms;
+    pm.t_solve_ms += tm.solve_ms;
+    pm.t_interp_ms += tm.interp_ms;
+    pm.kernel_launches += tm.launches;
+    pm.fft_execs += tm.fft_execs;
+    return HSR_OK;
+  };
+  if (open)
+    if (hsr_status r = pm_kick(&tp->pm_open)) return r;
+  hsr_stats total{};
+  int64_t inbox = n;
+  if (hsr_status r = subcycle_resident(ctx, sp, n, f, ids, msk, &inbox, total)) return r;
+  if (hsr_status r = pm_kick(&tp->pm_close)) return r;
+  if (mem == HSR_MEM_HOST) {
+    float *out[8] = {x, y, z, vx, vy, vz, mass, phi};
+    for (int i = 0; i < 8; ++i)
+      CU(cudaMemcpyAsync(out[i], f[i], size_t(n) * 4, cudaMemcpyDeviceToHost, s), "D2H arrays");
+    CU(cudaMemcpyAsync(id, ids, size_t(n) * 8, cudaMemcpyDeviceToHost, s), "D2H ids");
+    CU(cudaMemcpyAsync(mask, msk, size_t(n) * 2, cudaMemcpyDeviceToHost, s), "D2H masks");
+    total.h2d_bytes = n * 42;
+    total.d2h_bytes = n * 42;
+  }
+  CU(cudaStreamSynchronize(s), "TreePM step");
+  if (n_inbox) *n_inbox = inbox;
+  total.n = n;
+  total.t_total_ms = ms_since(t_start);
+  pm.t_total_ms = total.t_total_ms;
+  ctx->stats = total;
+  ctx->pm_stats = pm;
+  ctx->have_lists = !sp->skip_kick && sp->nsub > 0;
   return HSR_OK;
 }
 

@@ -39,7 +39,8 @@ EXPORTS = ("hsr_create", "hsr_destroy", "hsr_last_error", "hsr_version", "hsr_rc
            "hsr_subcycle", "hsr_set_tune", "hsr_get_tune", "hsr_autotune",
            "hsr_force_kick", "hsr_stream",
            # include/hacc_pm.h
-           "hsr_pm_kick", "hsr_pm_fields", "hsr_pm_get_stats", "hsr_pm_tables")
+           "hsr_pm_kick", "hsr_pm_fields", "hsr_pm_get_stats", "hsr_pm_tables",
+           "hsr_treepm_step")
 
 PM_F64, PM_F32 = 0, 1
 

@@ -17,6 +17,9 @@
  *                     228-245), GridExchange::exchangeGrid and
  *                     Particles::inverse_cic (Particles.cxx:647-714) for the
  *                     three components
+ *   hsr_treepm_step <- one pass of the time-step loop of
+ *                     src/simulation/driver_hires.cxx:320-447: PM half kick,
+ *                     Particles::subCycle, PM kick
  *   hsr_pm_fields  <- the grids those calls leave behind: the alive block of
  *                     the density after cic + fft_copy_arr_forward and of
  *                     each gradient component after backward_solve_gradient +
@@ -42,9 +45,9 @@ extern "C" {
 #endif
 
 /* Arithmetic of the transforms and the spectra.  F64: double, as the
- * reference's FFTW solve (complex_t double); F32: single precision (about
- * 6e-7 relative error on the gradient fields, half the HBM traffic and none
- * of the FP64 pipe). */
+ * reference's FFTW solve (complex_t double); F32: single precision (half the
+ * HBM traffic and none of the FP64 pipe, at single-precision rounding of the
+ * gradient fields). */
 enum { HSR_PM_F64 = 0, HSR_PM_F32 = 1 };
 
 typedef struct hsr_pm_params {
@@ -87,6 +90,32 @@ hsr_status hsr_pm_fields(hsr_ctx *ctx, const hsr_pm_params *p, int64_t n, const 
                          const float *y, const float *z, float *rho, float *grad, int32_t mem);
 
 hsr_status hsr_pm_get_stats(const hsr_ctx *ctx, hsr_pm_stats *st);
+
+/* One time step of HACC's TreePM loop on the device (the body of the step
+ * loop in src/simulation/driver_hires.cxx:320-447 on one rank):
+ *   open   if pm_open.tau != 0: the PM kick with pm_open (the loop's half
+ *          kick, stepFraction 0.5, at the step's start; tau == 0 stands for
+ *          doHalfKick == 0 and skips it),
+ *   sub    hsr_subcycle with `sub` (the stepper at mid-step: map1's and
+ *          map2's arguments),
+ *   close  the PM kick with pm_close (at the step's end; stepFraction 1, or
+ *          0.5 on the last step).
+ * The PM kicks see all n particles (the reference's cic and inverse_cic run
+ * over every local particle, overloaded ones included); the sub-cycle
+ * resorts them and kicks the in-box ones, as hsr_subcycle does.  The arrays
+ * stay on the device for the whole step.  hsr_get_stats reports the
+ * sub-cycle, hsr_pm_get_stats the two PM kicks summed (t_total_ms: the whole
+ * step).  *n_inbox receives the in-box count of the last resort. */
+typedef struct hsr_treepm_params {
+  hsr_subcycle_params sub;
+  hsr_pm_params pm_open;
+  hsr_pm_params pm_close;
+} hsr_treepm_params;
+
+hsr_status hsr_treepm_step(hsr_ctx *ctx, const hsr_treepm_params *tp, int64_t n, float *x,
+                           float *y, float *z, float *vx, float *vy, float *vz, float *mass,
+                           float *phi, int64_t *id, uint16_t *mask, int32_t mem,
+                           int64_t *n_inbox);
 
 /* SolverQuiet's 1-D tables (src/dfft/solver.hpp:726-790) as this library
  * computes them on the host in double: the filter W(k), the denominator term

@@ -267,3 +267,66 @@ def test_bad_arguments(ctx):
         with pytest.raises(hsr.HsrError) as e:
             ctx.pm_kick(x, x.copy(), x.copy(), *v, _params(ng, ngo, prec))
         assert e.value.status == 1
+
+
+# ---------------------------------------------------------------------------
+# the TreePM step
+# ---------------------------------------------------------------------------
+
+def test_step_plan_follows_the_driver_loop():
+    import treepm
+    steps = treepm.plan(50.0, 20.0, 4)
+    assert [s.open_fraction for s in steps] == [0.5, 0.0, 0.0, 0.0]
+    assert [s.close_fraction for s in steps] == [1.0, 1.0, 1.0, 0.5]
+    ts0 = synth.stepper(z_in=50.0, z_fin=20.0, nsteps=4)
+    # the PM kicks add up to one full tau per step
+    total = sum(s.open_fraction + s.close_fraction for s in steps)
+    assert total == 4.0
+    assert abs(steps[-1].end.pp - (ts0.pp + 4 * ts0.tau)) < 1e-12
+    for s in steps:
+        assert abs(s.mid.pp - s.start.pp - ts0.tau2) < 1e-15
+        assert abs(s.end.pp - s.mid.pp - ts0.tau2) < 1e-15
+
+
+@pytest.mark.gpu
+def test_treepm_step_matches_restatement(ctx, oracle_lib):
+    """hsr_treepm_step (first and last step of a run: both half kicks)
+    against the PM restatement + the oracle's sub-cycle, particle by id."""
+    import treepm
+    nsub = 5
+    p0 = synth.zeldovich_box(24, z=50.0, seed=29)
+    p0.id[:] = np.arange(p0.n)
+    ng, ngo = 24, p0.meta["ngo"]
+    kp = synth.kick_params(p0, nd=64, nsub=nsub)
+    sp = treepm.plan(50.0, 40.0, 1)[0]
+    T = treepm.step_params(sp, kp, nsub, ng, ngo, p0.nglt)
+    p = p0.copy()
+    treepm.step(ctx, p, T)
+
+    q = p0.copy()
+    po, pc = T.pm_open, T.pm_close
+    q.vx, q.vy, q.vz = P.pm_kick(q.x, q.y, q.z, q.vx, q.vy, q.vz, ng, ngo, 1.0, po.fscal, po.tau)
+    kps = dataclasses_replace(kp, fcoeff=T.sub.kick.fcoeff)
+    tau = np.float32(T.sub.tau)
+    for _ in range(nsub):
+        oracle_lib.map1(q, 1.0, T.sub.pp, float(tau), T.sub.adot)
+        nin = oracle_lib.resort(q)
+        q.mass[:] = 1.0
+        oracle_lib.rcb_run(synth.Particles(*(getattr(q, k)[:nin] for k in synth.FIELDS),
+                                           nglt=q.nglt), kps, nthreads=0)
+        oracle_lib.map1(q, 1.0, T.sub.pp, float(tau), T.sub.adot)
+    q.vx, q.vy, q.vz = P.pm_kick(q.x, q.y, q.z, q.vx, q.vy, q.vz, ng, ngo, 1.0, pc.fscal, pc.tau)
+
+    a, b = np.argsort(p.id), np.argsort(q.id)
+    dx = np.stack([p.x[a] - q.x[b], p.y[a] - q.y[b], p.z[a] - q.z[b]])
+    assert np.abs(dx).max() < 1e-4
+    v0 = np.stack([p0.vx, p0.vy, p0.vz], 1)[np.argsort(p0.id)].astype(np.float64)
+    dv = np.stack([p.vx, p.vy, p.vz], 1)[a] - v0
+    dv_o = np.stack([q.vx, q.vy, q.vz], 1)[b] - v0
+    rms, mx = _err(dv, dv_o)
+    assert rms < 1e-4 and mx < 1e-2, (rms, mx)
+
+
+def dataclasses_replace(obj, **kw):
+    import dataclasses
+    return dataclasses.replace(obj, **kw)
