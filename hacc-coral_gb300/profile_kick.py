@@ -4,6 +4,7 @@ sequence for profilers (ncu's launch lists and kernel captures).
 
     python hacc-coral_gb300/profile_kick.py --workload zeldovich --ng 128 --reps 2
     python hacc-coral_gb300/profile_kick.py --workload clustered --ng 256 --shape batched-32
+    python hacc-coral_gb300/profile_kick.py --ng 128 --reps 2 --pm f64   # + the PM kick
 """
 from __future__ import annotations
 
@@ -33,6 +34,8 @@ def main(argv=None) -> int:
     ap.add_argument("--reps", type=int, default=2)
     ap.add_argument("--shape", default="batched-32",
                     help="plain-32|plain-64|plain-128|batched-16|batched-32")
+    ap.add_argument("--pm", choices=["none", "f64", "f32"], default="none",
+                    help="also run the long-range PM kick (hsr_pm_kick) after each short-range kick")
     ap.add_argument("--device", type=int, default=0)
     a = ap.parse_args(argv)
     kind, num = a.shape.split("-")
@@ -44,9 +47,15 @@ def main(argv=None) -> int:
         else:
             ctx.set_tune("batched", 128, int(num))
         for r in range(a.reps):
-            st = ctx.rcb_kick(p.copy(), kp, kernel=hsr.KERNEL_AUTO)
+            q = p.copy()
+            st = ctx.rcb_kick(q, kp, kernel=hsr.KERNEL_AUTO)
             print(json.dumps({"rep": r, "workload": f"{a.workload}{a.ng}", "shape": a.shape,
                               **{k: st[k] for k in KEYS}}), flush=True)
+            if a.pm != "none":
+                prm = hsr.pm_params(a.ng, p.meta["ngo"], 1.0, 1.0, 1e-3,
+                                    hsr.PM_F64 if a.pm == "f64" else hsr.PM_F32)
+                ps = ctx.pm_kick(q.x, q.y, q.z, q.vx, q.vy, q.vz, prm)
+                print(json.dumps({"rep": r, "pm": a.pm, **ps}), flush=True)
     return 0
 
 
