@@ -476,6 +476,7 @@ void host_fill(hsr::RcbHost &H, int64_t n, float *x, float *y, float *z, float *
       d.offset = int32_t(L.offset);
       d.count = int32_t(L.count);
       d.list_len = int32_t(L.list_len);
+      d.kept_len = d.list_len;  // host lists are not pruned
       d.list_begin = lb[l];
       ld[l] = d;
       int64_t dst = lb[l];
@@ -810,6 +811,7 @@ hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float
     cfg.max_force[i] = p->max_force[i];
   }
   cfg.fsrrmax = p->fsrrmax;
+  cfg.prune2 = cull2(cut2(p->law, p->fsrrmax));
   cfg.tan_oa = std::tan(p->open_angle);  // host tanf, as the reference computes it
   cfg.ppc = p->ppc;
   cfg.nd = int32_t(std::min<int64_t>(p->nd, INT32_MAX));
@@ -1160,6 +1162,7 @@ hsr_status force_fwd_impl(hsr_ctx *ctx, const hsr_params *p, int64_t n, const fl
     cfg.max_force[i] = p->max_force[i];
   }
   cfg.fsrrmax = p->fsrrmax;
+  cfg.prune2 = cull2(cut2(p->law, p->fsrrmax));
   cfg.tan_oa = std::tan(p->open_angle);
   cfg.ppc = p->ppc;
   cfg.nd = int32_t(std::min<int64_t>(p->nd, INT32_MAX));
@@ -1404,11 +1407,26 @@ hsr_status hsr_lists_export_index(const hsr_ctx *ctx_c, int64_t *entry_index) {
                  nullptr, nullptr, entry_index);
     return HSR_OK;
   }
-  const int64_t ne = ctx->tree.info().list_entries;
-  std::vector<int32_t> ix(static_cast<size_t>(std::max<int64_t>(ne, 1)));
+  // the full lists from the segments (the device index array holds only the
+  // entries the kernels need)
+  const auto &ti = ctx->tree.info();
+  const int64_t nl = ti.processed_leaves, ns = ti.segments;
+  std::vector<hsr::LeafDesc> ld(static_cast<size_t>(std::max<int64_t>(nl, 1)));
+  std::vector<hsr::SegDesc> sd(static_cast<size_t>(std::max<int64_t>(ns, 1)));
   CU(cudaSetDevice(ctx->device), "cudaSetDevice");
-  CU(cudaMemcpy(ix.data(), ctx->tree.index(), size_t(ne) * 4, cudaMemcpyDeviceToHost), "D2H index");
-  for (int64_t i = 0; i < ne; ++i) entry_index[i] = ix[i];
+  CU(cudaMemcpy(ld.data(), ctx->tree.leaves(), size_t(nl) * sizeof(hsr::LeafDesc),
+                cudaMemcpyDeviceToHost), "D2H leaves");
+  CU(cudaMemcpy(sd.data(), ctx->tree.segs(), size_t(ns) * sizeof(hsr::SegDesc),
+                cudaMemcpyDeviceToHost), "D2H segments");
+  int64_t seg = 0;
+  for (int64_t l = 0; l < nl; ++l) {
+    int64_t run = ld[l].list_begin;
+    const int64_t end = ld[l].list_begin + ld[l].list_len;
+    while (run < end && seg < ns) {
+      const hsr::SegDesc &g = sd[seg++];
+      for (int32_t q = 0; q < g.count; ++q) entry_index[run++] = int64_t(g.start) + q;
+    }
+  }
   return HSR_OK;
 }
 
@@ -1479,6 +1497,8 @@ hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *para
       cfg.max_force[i] = p->max_force[i];
     }
     cfg.fsrrmax = p->fsrrmax;
+    cfg.prune2 = cull2(cut2(p->law, p->fsrrmax));
+  cfg.prune2 = cull2(cut2(p->law, p->fsrrmax));
     cfg.tan_oa = std::tan(p->open_angle);
     cfg.ppc = p->ppc;
     cfg.nd = int32_t(std::min<int64_t>(p->nd, INT32_MAX));

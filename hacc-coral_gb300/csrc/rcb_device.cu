@@ -1352,9 +1352,61 @@ __global__ void k_walk(const DNode *__restrict__ nodes, int32_t nnodes, const in
   }
 }
 
+// Expands each leaf's segments into the index array at the leaf's list_base,
+// keeping only the entries within sqrt(cull2) of the leaf's box: the others
+// are farther than the cutoff from every particle of the leaf, so the
+// reference's mask gives them exactly 0.  Warp per leaf: the leaf's box as
+// centre and half-width (widened by 4 ulps of
+// the coordinates, as in the batched kernel), then its segments 32 entries at
+// a time, compacting the kept entries by ballot.
+__global__ void k_expand_pruned(const SegDesc *__restrict__ segs,
+                                const int64_t *__restrict__ seg_base,
+                                const int64_t *__restrict__ seg_cnt,
+                                const int64_t *__restrict__ list_base,
+                                const DNode *__restrict__ nodes,
+                                const int32_t *__restrict__ leaf_ids, int64_t nleaves,
+                                const float4 *__restrict__ table, float cull2,
+                                int32_t *__restrict__ idx, int64_t *__restrict__ kept) {
+  const int lane = threadIdx.x & 31;
+  const unsigned below = (1u << lane) - 1u;
+  const int64_t warps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t li = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; li < nleaves;
+       li += warps) {
+    const DNode &T = nodes[leaf_ids[li]];
+    const float lox = T.xmin[0], loy = T.xmin[1], loz = T.xmin[2];
+    const float hix = T.xmax[0], hiy = T.xmax[1], hiz = T.xmax[2];
+    const float hx = fmaf(fmaxf(fabsf(lox), fabsf(hix)), 4.8e-7f, 0.5f * (hix - lox));
+    const float hy = fmaf(fmaxf(fabsf(loy), fabsf(hiy)), 4.8e-7f, 0.5f * (hiy - loy));
+    const float hz = fmaf(fmaxf(fabsf(loz), fabsf(hiz)), 4.8e-7f, 0.5f * (hiz - loz));
+    const float cx = 0.5f * (lox + hix), cy = 0.5f * (loy + hiy), cz = 0.5f * (loz + hiz);
+    int32_t *out = idx + list_base[li];
+    int64_t nk = 0;
+    const int64_t s0 = seg_base[li], s1 = s0 + seg_cnt[li];
+    for (int64_t q = s0; q < s1; ++q) {
+      const SegDesc S = segs[q];
+      for (int k0 = 0; k0 < S.count; k0 += 32) {
+        const int k = k0 + lane;
+        bool keep = false;
+        if (k < S.count) {
+          const float4 J = table[S.start + k];
+          const float dx = fmaxf(fabsf(J.x - cx) - hx, 0.f);
+          const float dy = fmaxf(fabsf(J.y - cy) - hy, 0.f);
+          const float dz = fmaxf(fabsf(J.z - cz) - hz, 0.f);
+          keep = fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < cull2;
+        }
+        const unsigned m = __ballot_sync(0xffffffffu, keep);
+        if (keep) out[nk + __popc(m & below)] = S.start + k;
+        nk += __popc(m);
+      }
+    }
+    if (lane == 0) kept[li] = nk;
+  }
+}
+
+
 __global__ void k_leaf_desc(const DNode *nodes, const int32_t *leaf_ids, int64_t nleaves,
-                            const int64_t *list_len, const int64_t *list_base, LeafDesc *ld,
-                            int64_t *counters) {
+                            const int64_t *list_len, const int64_t *kept_len,
+                            const int64_t *list_base, LeafDesc *ld, int64_t *counters) {
   const int64_t li = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   long long pairs = 0, padded = 0, mx = 0;
   if (li < nleaves) {
@@ -1363,11 +1415,12 @@ __global__ void k_leaf_desc(const DNode *nodes, const int32_t *leaf_ids, int64_t
     d.offset = T.offset;
     d.count = T.count;
     d.list_len = int32_t(list_len[li]);
+    d.kept_len = int32_t(kept_len ? kept_len[li] : list_len[li]);
     d.list_begin = list_base[li];
     ld[li] = d;
     pairs = (long long)T.count * list_len[li];
-    padded = (long long)((T.count + 31) / 32) * 32 * list_len[li];
-    mx = list_len[li];
+    padded = (long long)((T.count + 31) / 32) * 32 * d.kept_len;
+    mx = d.kept_len;
   }
   for (int o = 16; o > 0; o >>= 1) {
     pairs += __shfl_xor_sync(0xffffffffu, pairs, o);
@@ -1651,9 +1704,9 @@ __global__ void k_item_hist(const LeafDesc *ld, int64_t nleaves, int64_t jsplit,
   const int64_t li = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (li >= nleaves) return;
   const LeafDesc &L = ld[li];
-  const int64_t nch = max64(1, (L.list_len + jsplit - 1) / jsplit);
+  const int64_t nch = max64(1, (L.kept_len + jsplit - 1) / jsplit);
   const int64_t items = int64_t((L.count + G - 1) / G) * nch;
-  atomicAdd((unsigned long long *)&counters[C_BUCKET + len_bucket(min64(L.list_len, jsplit))],
+  atomicAdd((unsigned long long *)&counters[C_BUCKET + len_bucket(min64(L.kept_len, jsplit))],
             (unsigned long long)items);
 }
 
@@ -1672,18 +1725,18 @@ __global__ void k_item_fill(const LeafDesc *ld, int64_t nleaves, int64_t jsplit,
   const int64_t li = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (li >= nleaves) return;
   const LeafDesc &L = ld[li];
-  const int64_t nch = max64(1, (L.list_len + jsplit - 1) / jsplit);
+  const int64_t nch = max64(1, (L.kept_len + jsplit - 1) / jsplit);
   const int32_t ng = (L.count + G - 1) / G;
   const int64_t items_n = int64_t(ng) * nch;
   if (items_n == 0) return;
-  const int b = len_bucket(min64(L.list_len, jsplit));
+  const int b = len_bucket(min64(L.kept_len, jsplit));
   int64_t at = int64_t(atomicAdd((unsigned long long *)&counters[C_FILL + b],
                                  (unsigned long long)items_n));
   for (int32_t g = 0; g < ng; ++g)
     for (int64_t c = 0; c < nch; ++c) {
       PairItem it{};
       it.j_begin = L.list_begin + c * jsplit;
-      it.j_len = int32_t(min64(jsplit, L.list_len - c * jsplit));
+      it.j_len = int32_t(min64(jsplit, L.kept_len - c * jsplit));
       it.g_begin = L.offset + G * g;
       it.g_count = min(G, L.count - G * g);
       it.flags = nch > 1 ? 1 : 0;
@@ -2015,7 +2068,7 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
 
   // ---- lists: count, scan, write ----
   const size_t nlw = size_t(std::max<int64_t>(nleaves, 1));
-  DT_CHECK(grow(node_tmp_, cap_nt_, 4 * nlw + 4, s));
+  DT_CHECK(grow(node_tmp_, cap_nt_, 5 * nlw + 4, s));
   int64_t *seg_cnt = node_tmp_, *list_len = node_tmp_ + nlw, *seg_base = node_tmp_ + 2 * nlw,
           *list_base = node_tmp_ + 3 * nlw;
   DT_CHECK(grow(scan_tmp_, cap_scan_, size_t(scan_tmp_size(int64_t(nlw))), s));
@@ -2046,9 +2099,18 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   if (nleaves > 0) {
     k_walk<true><<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(
         nodes_, nnodes, leaf_ids_, nleaves, cfg, n, nullptr, nullptr, seg_base, list_base, segs_, walk_err_);
-    DT_CHECK(launch_expand_segments(segs_, nseg, idx_list_, s));
-    k_leaf_desc<<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(nodes_, leaf_ids_, nleaves, list_len,
-                                                                list_base, leafdesc_, counters_);
+    int64_t *kept = nullptr;
+    if (cfg.prune2 > 0.0f) {
+      kept = node_tmp_ + 4 * nlw;
+      int64_t blocks = std::min<int64_t>((nleaves + 7) / 8, 152 * 64);
+      k_expand_pruned<<<unsigned(blocks), 256, 0, s>>>(segs_, seg_base, seg_cnt, list_base, nodes_,
+                                                       leaf_ids_, nleaves, table_, cfg.prune2,
+                                                       idx_list_, kept);
+    } else {
+      DT_CHECK(launch_expand_segments(segs_, nseg, idx_list_, s));
+    }
+    k_leaf_desc<<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(
+        nodes_, leaf_ids_, nleaves, list_len, kept, list_base, leafdesc_, counters_);
   }
   DT_CHECK(cudaGetLastError());
 

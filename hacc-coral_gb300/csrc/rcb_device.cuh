@@ -46,6 +46,9 @@ struct TreeConfig {
   int32_t force_cm_fallback;  // test hook: 1 = every node takes the sequential sum,
                               // 2 = every node goes through the tight certification
   int32_t group;              // particles per work-item group: 16 or 32 (0 = 32)
+  float prune2;               // > 0: the index lists keep only entries within
+                              // sqrt(prune2) of their leaf's box (the kernels'
+                              // cull radius); 0: every list entry
 };
 
 // Result sizes of a device build.

@@ -86,13 +86,13 @@ __global__ void __launch_bounds__(NT)
     const float4 pi = act ? pos[L.offset + i] : make_float4(0.f, 0.f, 0.f, 0.f);
     const bool warp_act = i0 + (tid & ~31) < L.count;
     float ax = 0.f, ay = 0.f, az = 0.f;
-    for (int t0 = 0; t0 < L.list_len; t0 += NT) {
-      const int tn = min(NT, L.list_len - t0);
+    for (int t0 = 0; t0 < L.kept_len; t0 += NT) {
+      const int tn = min(NT, L.kept_len - t0);
       __syncthreads();
       if (tid < tn) tile[tid] = pos[lst[t0 + tid]];
       __syncthreads();
       if (warp_act) {
-#pragma unroll 4
+#pragma unroll 8
         for (int j = 0; j < tn; ++j)
           pair_acc<LAW>(pi.x, pi.y, pi.z, tile[j], rsm2, rcut2, ax, ay, az);
       }
@@ -163,7 +163,7 @@ cudaError_t launch_leaf_plain(int law, int threads, const float4 *pos, const Lea
 constexpr int kBatchedWarps = 8;
 
 template <int LAW, bool MULTI, int G>
-__global__ void __launch_bounds__(32 * kBatchedWarps, 5)
+__global__ void __launch_bounds__(32 * kBatchedWarps, 4)
     k_pairs_batched(const float4 *__restrict__ pos_, const PairItem *__restrict__ items,
                     int64_t nitems, const int32_t *__restrict__ gidx_,
                     const int32_t *__restrict__ idx_, float *__restrict__ vx_,
@@ -172,13 +172,13 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 5)
                     const BoxDesc *__restrict__ boxes) {
   static_assert(G == 16 || G == 32, "group size");
   constexpr bool kDrop = LAW == LAW_POLY5_STEP16;
-  // kept entries of the current item, compacted; one slot past 63 holds the
-  // padding entry of an odd tail (G = 16)
-  __shared__ float4 buf[kBatchedWarps][65];
+  // kept entries of the current item, compacted, two entries per slot pair:
+  // entry k lives in bufA[k/2] = (x, x', y, y') and bufB[k/2] = (z, z', m, m')
+  // at component k % 2 (the packed pair evaluation reads a slot pair as
+  // adjacent registers); two slots past 63 entries hold a tail's padding
+  __shared__ float4 bufA[kBatchedWarps][34], bufB[kBatchedWarps][34];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
-  const int gl = G == 16 ? (lane & 15) : lane;  // particle of the group
-  const int half = G == 16 ? (lane >> 4) : 0;   // even or odd entries
   const unsigned full = 0xffffffffu;
   const unsigned below = (1u << lane) - 1u;
   unsigned long long evaluated = 0;  // (particle, entry) pairs this warp evaluated
@@ -205,6 +205,12 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 5)
       rcull2 = B.rcull2;
       L = B.law;
     }
+    // groups of at most 16 particles run on half-warps: both halves hold the
+    // group and take the even and odd buffered entries (warp-uniform)
+    const bool hm = G == 16 || W.g_count <= 16;
+    const int gl = hm ? (lane & 15) : lane;  // particle of the group
+    const int half = hm ? (lane >> 4) : 0;   // even or odd entries
+    const int step = hm ? 2 : 1;
     const bool act = gl < W.g_count;
     const int pi = gidx[W.g_begin + (act ? gl : 0)];
     const float4 P = pos[pi];
@@ -219,7 +225,17 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 5)
       loz = fminf(loz, __shfl_xor_sync(full, loz, o));
       hiz = fmaxf(hiz, __shfl_xor_sync(full, hiz, o));
     }
-    float ax = 0.f, ay = 0.f, az = 0.f;
+    // the box as centre and half-width, the half-width widened by 4 ulps of
+    // the coordinates so rounding never shrinks it
+    const float hx = fmaf(fmaxf(fabsf(lox), fabsf(hix)), 4.8e-7f, 0.5f * (hix - lox));
+    const float hy = fmaf(fmaxf(fabsf(loy), fabsf(hiy)), 4.8e-7f, 0.5f * (hiy - loy));
+    const float hz = fmaf(fmaxf(fabsf(loz), fabsf(hiz)), 4.8e-7f, 0.5f * (hiz - loz));
+    const float cx = 0.5f * (lox + hix), cy = 0.5f * (loy + hiy), cz = 0.5f * (loz + hiz);
+    float2 ax2 = make_float2(0.f, 0.f), ay2 = ax2, az2 = ax2;
+    const float2 nxi = make_float2(-P.x, -P.x), nyi = make_float2(-P.y, -P.y),
+                 nzi = make_float2(-P.z, -P.z);
+    float *const fa = reinterpret_cast<float *>(bufA[w]);
+    float *const fb = reinterpret_cast<float *>(bufB[w]);
     const int32_t *lst = idx + W.j_begin;
     const int len = W.j_len;
     int nbuf = 0;  // warp-uniform
@@ -240,35 +256,60 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 5)
         const int j2 = j0 + 64 + lane;
         in2 = lst[j2 < len ? j2 : 0];
       }
-      const float dx = fmaxf(fmaxf(lox - J.x, J.x - hix), 0.f);
-      const float dy = fmaxf(fmaxf(loy - J.y, J.y - hiy), 0.f);
-      const float dz = fmaxf(fmaxf(loz - J.z, J.z - hiz), 0.f);
+      const float dx = fmaxf(fabsf(J.x - cx) - hx, 0.f);
+      const float dy = fmaxf(fabsf(J.y - cy) - hy, 0.f);
+      const float dz = fmaxf(fabsf(J.z - cz) - hz, 0.f);
       const bool k = ok && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < rcull2;
       const unsigned keep = __ballot_sync(full, k);
-      if (k) buf[w][nbuf + __popc(keep & below)] = J;
+      if (k) {
+        const int e = nbuf + __popc(keep & below);
+        const int o = 4 * (e >> 1) + (e & 1);
+        fa[o] = J.x;
+        fa[o + 2] = J.y;
+        fb[o] = J.z;
+        fb[o + 2] = J.w;
+      }
       nbuf += __popc(keep);
       kept += __popc(keep);
       if (nbuf >= 32) {
         __syncwarp();
+        if (hm) {
 #pragma unroll 8
-        for (int q = 0; q < 32 / (32 / G); ++q)
-          pair_acc_s<kDrop>(P.x, P.y, P.z, buf[w][(32 / G) * q + half], L, ax, ay, az);
+          for (int q = 0; q < 8; ++q)
+            pair2_acc_s<kDrop>(nxi, nyi, nzi, bufA[w][2 * q + half], bufB[w][2 * q + half], L,
+                               ax2, ay2, az2);
+        } else {
+#pragma unroll 8
+          for (int q = 0; q < 16; ++q)
+            pair2_acc_s<kDrop>(nxi, nyi, nzi, bufA[w][q], bufB[w][q], L, ax2, ay2, az2);
+        }
         __syncwarp();
-        if (lane < nbuf - 32) buf[w][lane] = buf[w][32 + lane];
+        if (2 * lane < nbuf - 32) {
+          bufA[w][lane] = bufA[w][16 + lane];
+          bufB[w][lane] = bufB[w][16 + lane];
+        }
         nbuf -= 32;
         __syncwarp();
       }
     }
-    if (G == 16 && (nbuf & 1)) {
-      // far-away massless padding: outside the cutoff, so its weight is 0
-      if (lane == 0) buf[w][nbuf] = make_float4(1e18f, 1e18f, 1e18f, 0.f);
-      ++nbuf;
+    // the tail: pad with far-away massless entries (outside the cutoff, so
+    // their weight is 0) to whole slot pairs, two per step on half-warps
+    const int padded = hm ? (nbuf + 3) & ~3 : (nbuf + 1) & ~1;
+    if (lane < padded - nbuf) {
+      const int e = nbuf + lane;
+      const int o = 4 * (e >> 1) + (e & 1);
+      fa[o] = 1e18f;
+      fa[o + 2] = 1e18f;
+      fb[o] = 1e18f;
+      fb[o + 2] = 0.f;
     }
     __syncwarp();
-    for (int q = 0; q < nbuf / (32 / G); ++q)
-      pair_acc_s<kDrop>(P.x, P.y, P.z, buf[w][(32 / G) * q + half], L, ax, ay, az);
+    for (int q = 0; q < padded / (2 * step); ++q)
+      pair2_acc_s<kDrop>(nxi, nyi, nzi, bufA[w][step * q + half], bufB[w][step * q + half], L,
+                         ax2, ay2, az2);
     __syncwarp();
-    if (G == 16) {
+    float ax = ax2.x + ax2.y, ay = ay2.x + ay2.y, az = az2.x + az2.y;
+    if (hm) {
       ax += __shfl_xor_sync(full, ax, 16);
       ay += __shfl_xor_sync(full, ay, 16);
       az += __shfl_xor_sync(full, az, 16);
@@ -417,6 +458,11 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
       loz = fminf(loz, __shfl_xor_sync(full, loz, o));
       hiz = fmaxf(hiz, __shfl_xor_sync(full, hiz, o));
     }
+    // centre and half-width, widened by 4 ulps of the coordinates
+    const float hx = fmaf(fmaxf(fabsf(lox), fabsf(hix)), 4.8e-7f, 0.5f * (hix - lox));
+    const float hy = fmaf(fmaxf(fabsf(loy), fabsf(hiy)), 4.8e-7f, 0.5f * (hiy - loy));
+    const float hz = fmaf(fmaxf(fabsf(loz), fabsf(hiz)), 4.8e-7f, 0.5f * (hiz - loz));
+    const float cx = 0.5f * (lox + hix), cy = 0.5f * (loy + hiy), cz = 0.5f * (loz + hiz);
     float bx = 0.f, by = 0.f, bz = 0.f;
     const int32_t *lst = idx + W.j_begin;
     for (int j0 = 0; j0 < W.j_len; j0 += 32) {
@@ -424,9 +470,9 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
       const bool ok = j < W.j_len;
       const int32_t jt = lst[ok ? j : 0];
       const float4 J = pos[jt];
-      const float dx = fmaxf(fmaxf(lox - J.x, J.x - hix), 0.f);
-      const float dy = fmaxf(fmaxf(loy - J.y, J.y - hiy), 0.f);
-      const float dz = fmaxf(fmaxf(loz - J.z, J.z - hiz), 0.f);
+      const float dx = fmaxf(fabsf(J.x - cx) - hx, 0.f);
+      const float dy = fmaxf(fabsf(J.y - cy) - hy, 0.f);
+      const float dz = fmaxf(fabsf(J.z - cz) - hz, 0.f);
       unsigned keep = __ballot_sync(full, ok && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < rcull2);
       if (!keep) continue;
       slot[w][lane] = J;
@@ -531,7 +577,7 @@ __global__ void k_ffma_probe(float *out, int iters) {
   const float a = 0.99999f, b = 1.0e-6f;
   float x0 = threadIdx.x * 1e-7f, x1 = x0 + 0.1f, x2 = x0 + 0.2f, x3 = x0 + 0.3f;
   float x4 = x0 + 0.4f, x5 = x0 + 0.5f, x6 = x0 + 0.6f, x7 = x0 + 0.7f;
-#pragma unroll 4
+#pragma unroll 8
   for (int i = 0; i < iters; ++i) {
     x0 = fmaf(x0, a, b); x1 = fmaf(x1, a, b); x2 = fmaf(x2, a, b); x3 = fmaf(x3, a, b);
     x4 = fmaf(x4, a, b); x5 = fmaf(x5, a, b); x6 = fmaf(x6, a, b); x7 = fmaf(x7, a, b);

@@ -22,7 +22,10 @@ struct alignas(16) LeafDesc {
   int32_t offset;      // first particle of the leaf in the position table
   int32_t count;       // particles in the leaf
   int32_t list_len;    // entries in its interaction list (self included)
-  int32_t pad;
+  int32_t kept_len;    // entries in the index array: the list less the entries
+                       // farther than the cutoff from the leaf's box (they add
+                       // exactly 0 to every particle of the leaf), or list_len
+                       // where the list is not pruned
   int64_t list_begin;  // first entry of the list in the index array
   int64_t pad2;
 };
@@ -176,6 +179,40 @@ __device__ __forceinline__ void pair_acc_s(float xi, float yi, float zi, const f
   ax = fmaf(w, dx, ax);
   ay = fmaf(w, dy, ay);
   az = fmaf(w, dz, az);
+}
+
+// Two pairs at once in the s form, on the packed FP32 pipe operations of
+// sm_100+ (__ffma2_rn and friends: each component rounds as the scalar
+// operation does): particle i against list entries a and b, given as
+// A = (x_a, x_b, y_a, y_b) and B = (z_a, z_b, m_a, m_b).  (nxi, nyi, nzi) hold
+// -x_i twice; x_j + (-x_i) is x_j - x_i exactly.  The accumulators keep the a
+// and b sums apart.
+template <bool DROP_SELF>
+__device__ __forceinline__ void pair2_acc_s(float2 nxi, float2 nyi, float2 nzi, const float4 A,
+                                            const float4 B, const LawS &L, float2 &ax,
+                                            float2 &ay, float2 &az) {
+  const float2 dx = __fadd2_rn(make_float2(A.x, A.y), nxi);
+  const float2 dy = __fadd2_rn(make_float2(A.z, A.w), nyi);
+  const float2 dz = __fadd2_rn(make_float2(B.x, B.y), nzi);
+  float2 s = __ffma2_rn(dz, dz, make_float2(L.rsm2, L.rsm2));
+  s = __ffma2_rn(dy, dy, s);
+  s = __ffma2_rn(dx, dx, s);
+  const float2 y = make_float2(rsqrt_ftz(s.x), rsqrt_ftz(s.y));
+  float2 q = make_float2(L.nb[6], L.nb[6]);
+  q = __ffma2_rn(q, s, make_float2(L.nb[5], L.nb[5]));
+  q = __ffma2_rn(q, s, make_float2(L.nb[4], L.nb[4]));
+  q = __ffma2_rn(q, s, make_float2(L.nb[3], L.nb[3]));
+  q = __ffma2_rn(q, s, make_float2(L.nb[2], L.nb[2]));
+  q = __ffma2_rn(q, s, make_float2(L.nb[1], L.nb[1]));
+  q = __ffma2_rn(q, s, make_float2(L.nb[0], L.nb[0]));
+  float2 w = __fmul2_rn(make_float2(B.z, B.w), __ffma2_rn(y, __fmul2_rn(y, y), q));
+  const bool ina = DROP_SELF ? (s.x < L.scut && s.x > L.rsm2) : (s.x < L.scut);
+  const bool inb = DROP_SELF ? (s.y < L.scut && s.y > L.rsm2) : (s.y < L.scut);
+  w.x = ina ? w.x : 0.f;
+  w.y = inb ? w.y : 0.f;
+  ax = __ffma2_rn(w, dx, ax);
+  ay = __ffma2_rn(w, dy, ay);
+  az = __ffma2_rn(w, dz, az);
 }
 
 // One pair: accumulates m_j g(r2) d into (ax, ay, az).

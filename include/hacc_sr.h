@@ -116,10 +116,13 @@ typedef struct hsr_stats {
   double t_total_ms;         /* wall time of the whole call                     */
   int64_t h2d_bytes;         /* bytes copied host -> device by the call         */
   int64_t d2h_bytes;         /* bytes copied device -> host by the call         */
-  int64_t evaluated_pairs;   /* (particle, entry) pairs the kernel evaluated:
-                                every listed pair for each lane of a warp for
-                                the plain kernel; after the box test for the
-                                batched kernel (the others contribute exactly 0) */
+  int64_t evaluated_pairs;   /* (particle, entry) pairs the kernel evaluated.
+                                Device-built lists reach the kernels without
+                                the entries farther than the cutoff from their
+                                leaf's box (they contribute exactly 0): the
+                                plain kernel evaluates every remaining entry
+                                for each lane of a warp, the batched kernel
+                                those that also pass its group's box test */
   int64_t work_items;        /* batched-kernel work items (group x list chunk)  */
   int64_t cm_fallbacks;      /* device build: nodes whose centre of mass needed
                                 the sequential sum (see rcb_device.cuh)         */
