@@ -2093,6 +2093,56 @@ hsr_status hsr_treepm_step(hsr_ctx *ctx, const hsr_treepm_params *tp, int64_t n,
   return HSR_OK;
 }
 
+hsr_status hsr_pm_vjp(hsr_ctx *ctx, const hsr_pm_params *p, int64_t n, const float *x,
+                      const float *y, const float *z, const float *vbx, const float *vby,
+                      const float *vbz, float *xbx, float *xby, float *xbz, int32_t mem) {
+  if (!ctx) return HSR_ERR_ARG;
+  const auto t0 = clk::now();
+  const void *arrs[9] = {x, y, z, vbx, vby, vbz, xbx, xby, xbz};
+  hsr_status st = pm_check(ctx, p, n, arrs, 9, mem);
+  if (st != HSR_OK) return st;
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  const hsr_pm::Params q = pm_params(p);
+  if ((st = pm_prepare(ctx, q)) != HSR_OK) return st;
+  cudaStream_t s = ctx->stream;
+  const float *in[6] = {x, y, z, vbx, vby, vbz};
+  float *out[3] = {xbx, xby, xbz};
+  const size_t nb = size_t(n) * sizeof(float);
+  hsr_pm_stats ps{};
+  if (mem == HSR_MEM_HOST && n > 0) {
+    CU(ctx->d_pm.ensure(9 * nb), "cudaMalloc(PM adjoint)");
+    float *b = ctx->d_pm.as<float>();
+    for (int a = 0; a < 6; ++a) {
+      CU(cudaMemcpyAsync(b + a * n, in[a], nb, cudaMemcpyHostToDevice, s), "PM adjoint copy in");
+      in[a] = b + a * n;
+    }
+    for (int a = 0; a < 3; ++a) out[a] = b + (6 + a) * n;
+    ps.h2d_bytes = int64_t(6 * nb);
+    ps.d2h_bytes = int64_t(3 * nb);
+  }
+  const int64_t l0 = ctx->pm->launches, f0 = ctx->pm->fft_execs;
+  std::string err;
+  CU(cudaEventRecord(ctx->ev0, s), "event");
+  if (!ctx->pm->vjp(q, n, in[0], in[1], in[2], in[3], in[4], in[5], out[0], out[1], out[2], s,
+                    &err))
+    return ctx->fail(HSR_ERR_CUDA, err);
+  CU(cudaEventRecord(ctx->ev1, s), "event");
+  if (mem == HSR_MEM_HOST && n > 0) {
+    float *dst[3] = {xbx, xby, xbz};
+    for (int a = 0; a < 3; ++a)
+      CU(cudaMemcpyAsync(dst[a], out[a], nb, cudaMemcpyDeviceToHost, s), "PM adjoint copy out");
+  }
+  CU(cudaStreamSynchronize(s), "PM adjoint");
+  float ms = 0;
+  cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1);
+  ps.t_solve_ms = ms;  // the whole device part: deposits, four transforms, kernels
+  ps.kernel_launches = ctx->pm->launches - l0;
+  ps.fft_execs = ctx->pm->fft_execs - f0;
+  ps.t_total_ms = ms_since(t0);
+  ctx->pm_stats = ps;
+  return HSR_OK;
+}
+
 hsr_status hsr_pm_get_stats(const hsr_ctx *ctx, hsr_pm_stats *st) {
   if (!ctx || !st) return HSR_ERR_ARG;
   *st = ctx->pm_stats;

@@ -217,6 +217,165 @@ __global__ void __launch_bounds__(kThreads)
   }
 }
 
+// The CIC weights of a particle and their derivatives, the corner cells
+// mapped as `map` says (-1: no cell).  Returns false when every corner lies
+// outside the local grid (and for NaN).
+struct Cic {
+  int cx[2], cy[2], cz[2];
+  float wx[2], wy[2], wz[2];
+};
+
+__device__ __forceinline__ bool cic_of(float xx, float yy, float zz, int nglt, Cic &c, int *ix3) {
+  const float lo = -2.0f, hi = float(nglt) + 1.0f;
+  if (!(xx > lo && xx < hi && yy > lo && yy < hi && zz > lo && zz < hi)) return false;
+  const int ix = int(floorf(xx)), iy = int(floorf(yy)), iz = int(floorf(zz));
+  const float ab = 1.0f + (float(ix) - xx);
+  const float de = 1.0f + (float(iy) - yy);
+  const float gh = 1.0f + (float(iz) - zz);
+  c.wx[0] = ab;
+  c.wx[1] = 1.0f - ab;
+  c.wy[0] = de;
+  c.wy[1] = 1.0f - de;
+  c.wz[0] = gh;
+  c.wz[1] = 1.0f - gh;
+  ix3[0] = ix;
+  ix3[1] = iy;
+  ix3[2] = iz;
+  return true;
+}
+
+// Transpose of the interpolation for the three cotangent components:
+// adj_a[image(c)] += W(x - c) vbar_a.
+__global__ void __launch_bounds__(kThreads)
+    k_adj_deposit(int64_t n, const float *__restrict__ x, const float *__restrict__ y,
+                  const float *__restrict__ z, const float *__restrict__ vbx,
+                  const float *__restrict__ vby, const float *__restrict__ vbz, int ng, int ngo,
+                  int nglt, float *__restrict__ adj) {
+  const int64_t m = int64_t(ng) * ng * ng;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    Cic c;
+    int i3[3];
+    if (!cic_of(x[i], y[i], z[i], nglt, c, i3)) continue;
+    const float u[3] = {vbx[i], vby[i], vbz[i]};
+    int cx[2], cy[2], cz[2];
+    for (int a = 0; a < 2; ++a) {
+      cx[a] = image_cell(i3[0] + a, ngo, ng, nglt);
+      cy[a] = image_cell(i3[1] + a, ngo, ng, nglt);
+      cz[a] = image_cell(i3[2] + a, ngo, ng, nglt);
+    }
+#pragma unroll
+    for (int a = 0; a < 2; ++a) {
+      if (cx[a] < 0) continue;
+#pragma unroll
+      for (int b = 0; b < 2; ++b) {
+        if (cy[b] < 0) continue;
+        const int64_t row = (int64_t(cx[a]) * ng + cy[b]) * ng;
+        const float wab = c.wx[a] * c.wy[b];
+#pragma unroll
+        for (int d = 0; d < 2; ++d) {
+          if (cz[d] < 0) continue;
+          const float w = wab * c.wz[d];
+          const int64_t k = row + cz[d];
+          atomicAdd(adj + k, w * u[0]);
+          atomicAdd(adj + m + k, w * u[1]);
+          atomicAdd(adj + 2 * m + k, w * u[2]);
+        }
+      }
+    }
+  }
+}
+
+template <typename T>
+__global__ void k_to_real3(int64_t m3, const float *__restrict__ a, T *__restrict__ b) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < m3;
+       i += int64_t(gridDim.x) * blockDim.x)
+    b[i] = T(a[i]);
+}
+
+// The transposed solve, summed over the three components:
+// phibar_k = sum_a conj(S_a) adj_a,k with S_a = -I g(k_a) green, i.e.
+// green * sum_a I g(k_a) adj_a,k.
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_adj_spectra(int ng, int nh, const typename Cplx<T>::type *__restrict__ a3,
+                  const T *__restrict__ green, const T *__restrict__ g,
+                  typename Cplx<T>::type *__restrict__ out) {
+  using C = typename Cplx<T>::type;
+  const int64_t m = int64_t(ng) * ng * nh;
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < m;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int kz = int(i % nh);
+    const int64_t t = i / nh;
+    const int ky = int(t % ng), kx = int(t / ng);
+    const int k[3] = {kx, ky, kz};
+    T re = T(0), im = T(0);
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const C v = a3[a * m + i];
+      const T ga = g[k[a]];
+      re -= ga * v.y;
+      im += ga * v.x;
+    }
+    const T G = green[i];
+    C o;
+    o.x = G * re;
+    o.y = G * im;
+    out[i] = o;
+  }
+}
+
+// xbar = fscal tau [sum_c grad W (vbar . G[image(c)])
+//                   + gpscal^3 sum_{c alive} grad W phibar[c]].
+template <typename T>
+__global__ void __launch_bounds__(kThreads)
+    k_vjp_interp(int64_t n, const float *__restrict__ x, const float *__restrict__ y,
+                 const float *__restrict__ z, const float *__restrict__ vbx,
+                 const float *__restrict__ vby, const float *__restrict__ vbz, int ng, int ngo,
+                 int nglt, const float4 *__restrict__ grad, const T *__restrict__ phibar,
+                 float cm, float coef, float *__restrict__ xbx, float *__restrict__ xby,
+                 float *__restrict__ xbz) {
+  for (int64_t i = blockIdx.x * int64_t(blockDim.x) + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    float gx = 0.f, gy = 0.f, gz = 0.f;
+    Cic c;
+    int i3[3];
+    if (cic_of(x[i], y[i], z[i], nglt, c, i3)) {
+      const float u0 = vbx[i], u1 = vby[i], u2 = vbz[i];
+      const float sg[2] = {-1.0f, 1.0f};
+#pragma unroll
+      for (int a = 0; a < 2; ++a)
+#pragma unroll
+        for (int b = 0; b < 2; ++b)
+#pragma unroll
+          for (int d = 0; d < 2; ++d) {
+            const float dwx = sg[a] * c.wy[b] * c.wz[d];
+            const float dwy = c.wx[a] * sg[b] * c.wz[d];
+            const float dwz = c.wx[a] * c.wy[b] * sg[d];
+            float f = 0.f;
+            const int ix = image_cell(i3[0] + a, ngo, ng, nglt);
+            const int iy = image_cell(i3[1] + b, ngo, ng, nglt);
+            const int iz = image_cell(i3[2] + d, ngo, ng, nglt);
+            if (ix >= 0 && iy >= 0 && iz >= 0) {
+              const float4 G = __ldg(grad + (int64_t(ix) * ng + iy) * ng + iz);
+              f = fmaf(u0, G.x, fmaf(u1, G.y, u2 * G.z));
+            }
+            const int ax = alive_cell(i3[0] + a, ngo, ng);
+            const int ay = alive_cell(i3[1] + b, ngo, ng);
+            const int az = alive_cell(i3[2] + d, ngo, ng);
+            if (ax >= 0 && ay >= 0 && az >= 0)
+              f = fmaf(cm, float(phibar[(int64_t(ax) * ng + ay) * ng + az]), f);
+            gx = fmaf(dwx, f, gx);
+            gy = fmaf(dwy, f, gy);
+            gz = fmaf(dwz, f, gz);
+          }
+    }
+    xbx[i] = coef * gx;
+    xby[i] = coef * gy;
+    xbz[i] = coef * gz;
+  }
+}
+
 }  // namespace
 
 void quiet_tables(int ng, double *filter, double *denom, double *gradient) {
@@ -251,10 +410,13 @@ Solver::~Solver() { release(); }
 void Solver::release() {
   if (have_fwd_) cufftDestroy(fwd_);
   if (have_inv_) cufftDestroy(inv_);
-  have_fwd_ = have_inv_ = false;
-  for (void *p : {(void *)rho_, real_, spec_, gspec_, greal_, green_, gtab_, (void *)grad_})
+  if (have_fwd3_) cufftDestroy(fwd3_);
+  if (have_inv1_) cufftDestroy(inv1_);
+  have_fwd_ = have_inv_ = have_fwd3_ = have_inv1_ = false;
+  for (void *p : {(void *)rho_, real_, spec_, gspec_, greal_, green_, gtab_, (void *)grad_,
+                  (void *)adj_})
     if (p) cudaFree(p);
-  rho_ = nullptr;
+  rho_ = adj_ = nullptr;
   real_ = spec_ = gspec_ = greal_ = green_ = gtab_ = nullptr;
   grad_ = nullptr;
   ng_ = 0;
@@ -414,6 +576,86 @@ bool Solver::export_fields(float *rho, float *grad, bool to_host, cudaStream_t s
         return false;
   }
   return cu_ok(cudaStreamSynchronize(s), "pm export", err);
+}
+
+bool Solver::prepare_vjp(std::string *err) {
+  if (have_fwd3_ && have_inv1_ && adj_) return true;
+  const int ng = ng_, nh = ng / 2 + 1;
+  const int64_t m = int64_t(ng) * ng * ng, mh = int64_t(ng) * ng * nh;
+  if (!adj_ && !cu_ok(cudaMalloc(&adj_, 3 * m * sizeof(float)), "pm adjoint fields", err))
+    return false;
+  long long dims[3] = {ng, ng, ng};
+  const bool f64 = prec_ == PREC_F64;
+  size_t ws = 0;
+  if (!have_fwd3_) {
+    if (!fft_ok(cufftCreate(&fwd3_), "pm adjoint forward plan", err)) return false;
+    have_fwd3_ = true;
+    if (!fft_ok(cufftMakePlanMany64(fwd3_, 3, dims, nullptr, 1, m, nullptr, 1, mh,
+                                    f64 ? CUFFT_D2Z : CUFFT_R2C, 3, &ws),
+                "pm adjoint forward plan", err))
+      return false;
+  }
+  if (!have_inv1_) {
+    if (!fft_ok(cufftCreate(&inv1_), "pm adjoint inverse plan", err)) return false;
+    have_inv1_ = true;
+    if (!fft_ok(cufftMakePlanMany64(inv1_, 3, dims, nullptr, 1, mh, nullptr, 1, m,
+                                    f64 ? CUFFT_Z2D : CUFFT_C2R, 1, &ws),
+                "pm adjoint inverse plan", err))
+      return false;
+  }
+  return true;
+}
+
+bool Solver::vjp(const Params &p, int64_t n, const float *x, const float *y, const float *z,
+                 const float *vbx, const float *vby, const float *vbz, float *xbx, float *xby,
+                 float *xbz, cudaStream_t s, std::string *err) {
+  if (!prepare_vjp(err)) return false;
+  if (!deposit(p, n, x, y, z, s, err) || !solve(s, err)) return false;
+  if (n == 0) return true;
+  const int ng = ng_, nh = ng / 2 + 1, nglt = ng + 2 * p.ngo + 1;
+  const int64_t m = int64_t(ng) * ng * ng, mh = int64_t(ng) * ng * nh;
+  if (!cu_ok(cudaMemsetAsync(adj_, 0, 3 * m * sizeof(float), s), "pm adjoint clear", err))
+    return false;
+  k_adj_deposit<<<blocks_for(n), kThreads, 0, s>>>(n, x, y, z, vbx, vby, vbz, ng, p.ngo, nglt,
+                                                   adj_);
+  ++launches;
+  if (!cu_ok(cudaGetLastError(), "pm adjoint deposit", err)) return false;
+  if (!fft_ok(cufftSetStream(fwd3_, s), "pm adjoint stream", err)) return false;
+  if (!fft_ok(cufftSetStream(inv1_, s), "pm adjoint stream", err)) return false;
+  const float cm = p.gpscal * p.gpscal * p.gpscal;
+  const float coef = p.fscal * p.tau;
+  if (prec_ == PREC_F64) {
+    k_to_real3<double><<<blocks_for(3 * m), kThreads, 0, s>>>(3 * m, adj_, (double *)greal_);
+    if (!fft_ok(cufftExecD2Z(fwd3_, (cufftDoubleReal *)greal_, (cufftDoubleComplex *)gspec_),
+                "pm adjoint forward transform", err))
+      return false;
+    k_adj_spectra<double><<<blocks_for(mh), kThreads, 0, s>>>(
+        ng, nh, (const double2 *)gspec_, (const double *)green_, (const double *)gtab_,
+        (double2 *)spec_);
+    if (!fft_ok(cufftExecZ2D(inv1_, (cufftDoubleComplex *)spec_, (cufftDoubleReal *)real_),
+                "pm adjoint inverse transform", err))
+      return false;
+    k_vjp_interp<double><<<blocks_for(n), kThreads, 0, s>>>(
+        n, x, y, z, vbx, vby, vbz, ng, p.ngo, nglt, grad_, (const double *)real_, cm, coef, xbx,
+        xby, xbz);
+  } else {
+    if (!fft_ok(cufftExecR2C(fwd3_, (cufftReal *)adj_, (cufftComplex *)gspec_),
+                "pm adjoint forward transform", err))
+      return false;
+    k_adj_spectra<float><<<blocks_for(mh), kThreads, 0, s>>>(
+        ng, nh, (const float2 *)gspec_, (const float *)green_, (const float *)gtab_,
+        (float2 *)spec_);
+    // the density grid is free once the solve ran: the inverse lands there
+    if (!fft_ok(cufftExecC2R(inv1_, (cufftComplex *)spec_, (cufftReal *)rho_),
+                "pm adjoint inverse transform", err))
+      return false;
+    k_vjp_interp<float><<<blocks_for(n), kThreads, 0, s>>>(n, x, y, z, vbx, vby, vbz, ng, p.ngo,
+                                                          nglt, grad_, rho_, cm, coef, xbx, xby,
+                                                          xbz);
+  }
+  launches += prec_ == PREC_F64 ? 3 : 2;
+  fft_execs += 2;
+  return cu_ok(cudaGetLastError(), "pm adjoint kernels", err);
 }
 
 bool Solver::kick(const Params &p, int64_t n, const float *x, const float *y, const float *z,

@@ -83,6 +83,13 @@ class Solver {
   // Copies rho_ (ng^3) and the three gradient components (3 x ng^3, planar).
   bool export_fields(float *rho, float *grad, bool to_host, cudaStream_t s, std::string *err);
 
+  // The kick's vector-Jacobian product for positions x and the cotangent
+  // vbar of its velocity change: xbar = (d dv / d x)^T vbar, written to xb*
+  // (recomputes the deposit and the solve of these positions first).
+  bool vjp(const Params &p, int64_t n, const float *x, const float *y, const float *z,
+           const float *vbx, const float *vby, const float *vbz, float *xbx, float *xby,
+           float *xbz, cudaStream_t s, std::string *err);
+
   // Deposit, solve and interpolation with event timings (the context's
   // events ev[0..3] on stream s).
   bool kick(const Params &p, int64_t n, const float *x, const float *y, const float *z, float *vx,
@@ -96,6 +103,12 @@ class Solver {
   int ng_ = 0, prec_ = -1;
   cufftHandle fwd_ = 0, inv_ = 0;
   bool have_fwd_ = false, have_inv_ = false;
+  // adjoint: batched forward of the three deposited cotangent fields, single
+  // inverse of the combined spectrum (made on the first vjp)
+  cufftHandle fwd3_ = 0, inv1_ = 0;
+  bool have_fwd3_ = false, have_inv1_ = false;
+  float *adj_ = nullptr;     // 3 x ng^3: deposited cotangents (float atomics)
+  bool prepare_vjp(std::string *err);
   float *rho_ = nullptr;     // ng^3
   void *real_ = nullptr;     // ng^3 real (T): transform input (double only)
   void *spec_ = nullptr;     // ng^2 (ng/2+1) complex (T)

@@ -40,7 +40,7 @@ EXPORTS = ("hsr_create", "hsr_destroy", "hsr_last_error", "hsr_version", "hsr_rc
            "hsr_force_kick", "hsr_stream",
            # include/hacc_pm.h
            "hsr_pm_kick", "hsr_pm_fields", "hsr_pm_get_stats", "hsr_pm_tables",
-           "hsr_treepm_step")
+           "hsr_treepm_step", "hsr_pm_vjp")
 
 PM_F64, PM_F32 = 0, 1
 
@@ -201,6 +201,8 @@ def load(path: str = LIB_PATH):
     lib.hsr_pm_kick.restype = i32
     lib.hsr_pm_fields.argtypes = [vp, C.POINTER(HsrPmParams), i64] + [vp] * 5 + [i32]
     lib.hsr_pm_fields.restype = i32
+    lib.hsr_pm_vjp.argtypes = [vp, C.POINTER(HsrPmParams), i64] + [vp] * 9 + [i32]
+    lib.hsr_pm_vjp.restype = i32
     lib.hsr_pm_get_stats.argtypes = [vp, C.POINTER(HsrPmStats)]
     lib.hsr_pm_get_stats.restype = i32
     lib.hsr_pm_tables.argtypes = [i32, C.POINTER(C.c_double), C.POINTER(C.c_double),
@@ -395,6 +397,26 @@ class Context:
         self._check(self.lib.hsr_pm_fields(self.h, C.byref(params), len(xs[0]), *[vp(a) for a in xs],
                                            vp(rho), vp(g), MEM_HOST), "hsr_pm_fields")
         return rho, g
+
+    def pm_vjp(self, x, y, z, vbar, params: HsrPmParams):
+        """hsr_pm_vjp on host arrays: xbar (n x 3) for the cotangent vbar
+        (n x 3) of the PM kick's velocity change at positions x, y, z."""
+        n = len(x)
+        xs = [np.ascontiguousarray(a, np.float32) for a in (x, y, z)]
+        u = [np.ascontiguousarray(vbar[:, d], np.float32) for d in range(3)]
+        xb = [np.zeros(n, np.float32) for _ in range(3)]
+        vp = lambda a: a.ctypes.data_as(C.c_void_p)
+        self._check(self.lib.hsr_pm_vjp(self.h, C.byref(params), n, *[vp(a) for a in xs],
+                                        *[vp(a) for a in u], *[vp(a) for a in xb], MEM_HOST),
+                    "hsr_pm_vjp")
+        return np.stack(xb, 1)
+
+    def pm_vjp_device(self, x, y, z, ux, uy, uz, xbx, xby, xbz, params: HsrPmParams):
+        """hsr_pm_vjp on device buffers (objects with data_ptr())."""
+        ptr = lambda t: C.c_void_p(t.data_ptr())
+        self._check(self.lib.hsr_pm_vjp(self.h, C.byref(params), int(x.numel()), ptr(x), ptr(y),
+                                        ptr(z), ptr(ux), ptr(uy), ptr(uz), ptr(xbx), ptr(xby),
+                                        ptr(xbz), MEM_DEVICE), "hsr_pm_vjp(device arrays)")
 
     def pm_stats(self) -> dict:
         s = HsrPmStats()

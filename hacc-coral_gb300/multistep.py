@@ -11,8 +11,10 @@ TimeStepper.cxx:60-67), nsub times
     x += pt v              map1 again                            (hsr_stream)
 
 on a fixed set of particles kept at fixed indices (the kick does not permute
-them; the tree is rebuilt at every kick).  The long-range PM kick between the
-steps is not part of this library and is left out of the map.
+them; the tree is rebuilt at every kick).  With `pm` set, each PM step is the
+whole TreePM step of src/simulation/driver_hires.cxx:320-447: the long-range
+PM kick v += dv(x) (hsr_pm_kick) before the sub-cycles where the step opens
+with a half kick, and after them.
 
 The reverse pass gives the vector-Jacobian product of the whole map: for
 cotangents (xbar_T, vbar_T) of the final state, (xbar_0, vbar_0) of the
@@ -21,6 +23,8 @@ initial one.  Per sub-cycle, in reverse:
     vbar += pt xbar                                   (hsr_stream on (vbar, xbar))
     xbar += (dK/dx)^T (c vbar) at the kick positions  (hsr_force_fwd + hsr_force_vjp)
     vbar += pt xbar
+
+and for a PM kick, xbar += (d dv / dx)^T vbar at its positions (hsr_pm_vjp).
 
 The trees and lists are held fixed within each kick (they are piecewise
 constant in the positions).  The kick positions are not stored for the whole
@@ -38,7 +42,7 @@ before the next library call reads their results.
 from __future__ import annotations
 
 import dataclasses
-from typing import Callable, List, Optional, Sequence
+from typing import Callable, List, Optional, Sequence, Tuple
 
 import numpy as np
 
@@ -95,6 +99,24 @@ def box_state(p: synth.Particles, device: int = 0) -> BoxState:
 
 TapeHook = Callable[[int, int, int, hsr.Context, list], None]
 
+# Per PM step: the opening PM kick's parameters (None: no opening kick) and
+# the closing one's (None: none), hsr.HsrPmParams each.
+PMKicks = Sequence[Tuple[Optional[object], Optional[object]]]
+
+
+def pm_schedule(z_in: float, z_fin: float, nsteps: int, ng: int, ngo: int,
+                gpscal: float = 1.0, precision: int = hsr.PM_F64) -> List[tuple]:
+    """The PM kicks of driver_hires' loop for `schedule`'s steps: a half kick
+    opening the first step, a kick closing every step (half on the last)."""
+    import treepm
+    out = []
+    for sp in treepm.plan(z_in, z_fin, nsteps):
+        open_p = (treepm.pm_params(sp.start, sp.open_fraction, ng, ngo, gpscal, precision)
+                  if sp.open_fraction else None)
+        out.append((open_p, treepm.pm_params(sp.end, sp.close_fraction, ng, ngo, gpscal,
+                                             precision)))
+    return out
+
 
 class MultiStep:
     """Forward map and its checkpointed adjoint for a list of boxes.
@@ -107,16 +129,21 @@ class MultiStep:
     """
 
     def __init__(self, ctx: hsr.Context, kps: Sequence[synth.KickParams],
-                 steps: Sequence[StepParams], nsub: int, checkpoint_every: Optional[int] = 2):
+                 steps: Sequence[StepParams], nsub: int, checkpoint_every: Optional[int] = 2,
+                 pm: Optional[PMKicks] = None):
         if checkpoint_every is not None and checkpoint_every < 1:
             raise ValueError("checkpoint_every must be >= 1 or None")
+        if pm is not None and len(pm) != len(steps):
+            raise ValueError("one (open, close) PM pair per step")
         self.ctx = ctx
         self.kps = list(kps)
         self.steps = list(steps)
         self.nsub = nsub
         self.every = checkpoint_every
+        self.pm = list(pm) if pm is not None else None
         self.on_tape: Optional[TapeHook] = None
         self.kicks = 0
+        self.pm_kicks = 0
 
     # ---- one box ----------------------------------------------------------
     def _kp(self, b: int, st: StepParams) -> synth.KickParams:
@@ -130,17 +157,30 @@ class MultiStep:
         st = self.steps[s]
         self._stream(S.x, S.v, st)
         if record is not None:
-            record.append([t.clone() for t in S.x])
+            record.append(("sr", s, [t.clone() for t in S.x]))
             _torch_done()  # the copy is taken before the next half-stream moves x
         self.ctx.force_kick_device(S.x[0], S.x[1], S.x[2], S.mass, S.v[0], S.v[1], S.v[2],
                                    self._kp(b, st))
         self.kicks += 1
         self._stream(S.x, S.v, st)
 
+    def _pm_kick(self, prm, S: BoxState, record: Optional[list]):
+        if prm is None:
+            return
+        if record is not None:
+            record.append(("pm", prm, [t.clone() for t in S.x]))
+            _torch_done()
+        self.ctx.pm_kick_device(S.x[0], S.x[1], S.x[2], S.v[0], S.v[1], S.v[2], prm)
+        self.pm_kicks += 1
+
     def _run(self, b: int, S: BoxState, s0: int, s1: int, record: Optional[list] = None):
         for s in range(s0, s1):
+            if self.pm:
+                self._pm_kick(self.pm[s][0], S, record)
             for j in range(self.nsub):
                 self._subcycle(b, s, j, S, record)
+            if self.pm:
+                self._pm_kick(self.pm[s][1], S, record)
 
     def forward_box(self, b: int, S: BoxState) -> BoxState:
         """The whole map on box b's state (in place); returns it."""
@@ -149,23 +189,32 @@ class MultiStep:
         return S
 
     def _reverse_segment(self, b: int, s0: int, s1: int, xk: list, mass, xb, vb, scratch):
-        k = len(xk)
-        for s in reversed(range(s0, s1)):
-            st = self.steps[s]
-            kp = self._kp(b, st)
-            for j in reversed(range(self.nsub)):
-                k -= 1
-                x1 = xk[k]
-                self._stream(vb, xb, st)                      # second half-stream
-                self.ctx.force_fwd_device(x1[0], x1[1], x1[2], mass, *scratch, kp)
-                self.kicks += 1
-                if self.on_tape:
-                    self.on_tape(b, s, j, self.ctx, x1)
-                self.ctx.force_vjp_device(vb[0], vb[1], vb[2], *scratch)
+        """Adjoint of steps s0..s1-1 from their recorded kick positions xk
+        (("sr", step, x) per sub-cycle kick, ("pm", params, x) per PM kick,
+        in forward order)."""
+        sub = {s: self.nsub for s in range(s0, s1)}
+        for kind, arg, x1 in reversed(xk):
+            if kind == "pm":
+                # v += dv(x): vbar passes through, xbar += (d dv / dx)^T vbar
+                self.ctx.pm_vjp_device(x1[0], x1[1], x1[2], vb[0], vb[1], vb[2], *scratch, arg)
                 for d in range(3):
-                    xb[d].add_(scratch[d])                     # kick
+                    xb[d].add_(scratch[d])
                 _torch_done()
-                self._stream(vb, xb, st)                      # first half-stream
+                continue
+            s = arg
+            st = self.steps[s]
+            sub[s] -= 1
+            j = sub[s]
+            self._stream(vb, xb, st)                      # second half-stream
+            self.ctx.force_fwd_device(x1[0], x1[1], x1[2], mass, *scratch, self._kp(b, st))
+            self.kicks += 1
+            if self.on_tape:
+                self.on_tape(b, s, j, self.ctx, x1)
+            self.ctx.force_vjp_device(vb[0], vb[1], vb[2], *scratch)
+            for d in range(3):
+                xb[d].add_(scratch[d])                     # kick
+            _torch_done()
+            self._stream(vb, xb, st)                      # first half-stream
 
     def adjoint_box(self, b: int, S0: BoxState, xbar, vbar):
         """(xbar_0, vbar_0) for the final-state cotangents (xbar, vbar) (lists

@@ -91,6 +91,20 @@ hsr_status hsr_pm_fields(hsr_ctx *ctx, const hsr_pm_params *p, int64_t n, const 
 
 hsr_status hsr_pm_get_stats(const hsr_ctx *ctx, hsr_pm_stats *st);
 
+/* Vector-Jacobian product of the PM kick with respect to the positions: for
+ * the velocity change dv = fscal tau F(x) that hsr_pm_kick adds and a
+ * cotangent vbar of it, writes xbar = (d dv / d x)^T vbar (n entries each,
+ * caller's order).  The density, the solve and both halves of the chain rule
+ * run on the device: the interpolation's derivative at each particle and,
+ * through the density, the cotangents deposited by CIC, the transposed solve
+ * (the conjugate spectrum) and the CIC derivative at each depositor.  CIC
+ * weights are piecewise linear: the product is the derivative away from cell
+ * faces.  Same `mem` rule as hsr_pm_kick for all nine arrays.  No
+ * counterpart in the reference (differentiation is new in this build). */
+hsr_status hsr_pm_vjp(hsr_ctx *ctx, const hsr_pm_params *p, int64_t n, const float *x,
+                      const float *y, const float *z, const float *vbx, const float *vby,
+                      const float *vbz, float *xbx, float *xby, float *xbz, int32_t mem);
+
 /* One time step of HACC's TreePM loop on the device (the body of the step
  * loop in src/simulation/driver_hires.cxx:320-447 on one rank):
  *   open   if pm_open.tau != 0: the PM kick with pm_open (the loop's half

@@ -287,7 +287,8 @@ class Oracle:
         return float(x[0])
 
     def multistep64(self, x0, v0, m, steps, nsub, tapes, xbar=None, vbar=None, kick_pos=None,
-                    law=LAW_POLY6, rsm=0.1, fsrrmax=3.116326355, cut_pos=None, traj_out=None):
+                    law=LAW_POLY6, rsm=0.1, fsrrmax=3.116326355, cut_pos=None, traj_out=None,
+                    pm=None, pm_pos=None, pm_cut=None, pm_traj_out=None):
         """FP64 restatement of the sub-cycled short-range map (map1, kick,
         map1; nsub per PM step) with every kick's tree and lists frozen to
         `tapes` (one per kick in forward order: perm, node ranges, leaves and
@@ -300,32 +301,65 @@ class Oracle:
         cut_pos: optional positions of every kick on which the pairs' cutoff is
         decided (the map with its cutoff mask frozen); traj_out, a list, receives
         this run's kick positions.
+
+        pm: optional PM kicks, one (open, close) pair per step, each None or a
+        dict(ng, ngo, gpscal, fscal, tau): v += fscal tau F(x) before the step's
+        sub-cycles (open) and after them (close), F from pm_oracle.force64.
+        pm_pos / pm_cut / pm_traj_out play the roles of kick_pos / cut_pos /
+        traj_out for the PM kicks (pm_cut freezes each particle's CIC cell).
         """
+        import pm_oracle
+
+        def pm_kick(q, prm, base):
+            return prm["fscal"] * prm["tau"] * pm_oracle.force64(
+                q[:, 0], q[:, 1], q[:, 2], prm["ng"], prm["ngo"], prm["gpscal"], base=base)
+        pm_traj = []
         x = np.array(x0, np.float64)
         v = np.array(v0, np.float64)
         m = np.asarray(m, np.float64)
         pts = [self.stream_factor(st.alpha, st.pp, st.tau_sub, st.adot) for st in steps]
         traj = []
         k = 0
+        q = 0
         for s, st in enumerate(steps):
-            for _ in range(nsub):
-                x += pts[s] * v
-                traj.append(x.copy())
-                t = tapes[k]
-                perm = t["perm"]
-                pc = None if cut_pos is None else np.asarray(cut_pos[k], np.float64)[perm]
-                v[perm] += self.kick64(x[perm], m[perm], t, st.fcoeff, law, rsm, fsrrmax, pc)
-                x += pts[s] * v
-                k += 1
+            for half in (0, 1):
+                prm = pm[s][half] if pm is not None else None
+                if half == 1:
+                    for _ in range(nsub):
+                        x += pts[s] * v
+                        traj.append(x.copy())
+                        t = tapes[k]
+                        perm = t["perm"]
+                        pc = None if cut_pos is None else np.asarray(cut_pos[k], np.float64)[perm]
+                        v[perm] += self.kick64(x[perm], m[perm], t, st.fcoeff, law, rsm, fsrrmax,
+                                               pc)
+                        x += pts[s] * v
+                        k += 1
+                if prm is not None:
+                    pm_traj.append(x.copy())
+                    base = None if pm_cut is None else np.asarray(pm_cut[q], np.float64)
+                    v += pm_kick(x, prm, base)
+                    q += 1
         if traj_out is not None:
             traj_out.extend(traj)
+        if pm_traj_out is not None:
+            pm_traj_out.extend(pm_traj)
         if xbar is None:
             return x, v
         L = float((np.asarray(xbar) * x).sum() + (np.asarray(vbar) * v).sum())
         xb = np.array(xbar, np.float64)
         vb = np.array(vbar, np.float64)
+
+        def pm_adj(prm):
+            nonlocal q
+            q -= 1
+            xq = pm_traj[q] if pm_pos is None else np.asarray(pm_pos[q], np.float64)
+            return prm["fscal"] * prm["tau"] * pm_oracle.vjp64(
+                xq[:, 0], xq[:, 1], xq[:, 2], vb, prm["ng"], prm["ngo"], prm["gpscal"])
         for s in reversed(range(len(steps))):
             st = steps[s]
+            if pm is not None and pm[s][1] is not None:
+                xb += pm_adj(pm[s][1])
             for _ in range(nsub):
                 k -= 1
                 vb += pts[s] * xb
@@ -335,6 +369,8 @@ class Oracle:
                 xb[perm] += self.kick64_vjp(xk[perm], m[perm], t, st.fcoeff, vb[perm], law, rsm,
                                             fsrrmax)
                 vb += pts[s] * xb
+            if pm is not None and pm[s][0] is not None:
+                xb += pm_adj(pm[s][0])
         return x, v, L, xb, vb
 
     def map1(self, p, alpha, pp, tau, adot):

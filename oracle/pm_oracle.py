@@ -213,3 +213,107 @@ def point_mass_force(ng: int, src, targets) -> np.ndarray:
     dvec -= ng * np.round(dvec / ng)
     r = np.linalg.norm(dvec, axis=1)
     return 4.0 * math.pi * np.sum(acc * dvec, axis=1) / r
+
+
+# ---------------------------------------------------------------------------
+# float64 forward and its vector-Jacobian product (checker of hsr_pm_vjp)
+# ---------------------------------------------------------------------------
+#
+# The kick is dv_i = fscal tau F(x_i) with F_d(x) = sum_c W(x - c) G_d[img(c)],
+# G_d = A_d rho, A_d = Re IFFT(S_d FFT .), S_d = -i g(k_d) green (the solve
+# above), rho[c] = gpscal^3 sum_j W(x_j - c) over the alive block.  For a
+# cotangent vbar of dv:
+#   xbar_i = fscal tau [ sum_c grad W(x_i - c) (vbar_i . G[img(c)])
+#                       + gpscal^3 sum_{c alive} grad W(x_i - c) phibar[c] ],
+#   phibar = sum_d A_d^T a_d,  A_d^T = Re IFFT(conj(S_d) FFT .),
+#   a_d[img(c)] += W(x_i - c) vbar_{i,d}  (the transpose of the interpolation).
+# W is the CIC weight, piecewise linear: the product is the derivative away
+# from cell faces.
+
+def _corners64(x, y, z, base=None):
+    """(cx, cy, cz, w, dw/dx, dw/dy, dw/dz) of the eight corners, float64.
+    base (n, 3), if given, fixes each particle's cell (the weights continue
+    linearly past the cell faces: the map with its CIC cells frozen)."""
+    x, y, z = (np.asarray(a, np.float64) for a in (x, y, z))
+    if base is None:
+        ix, iy, iz = (np.floor(a).astype(np.int64) for a in (x, y, z))
+    else:
+        ix, iy, iz = (np.floor(np.asarray(base, np.float64)[:, d]).astype(np.int64)
+                      for d in range(3))
+    fx, fy, fz = x - ix, y - iy, z - iz
+    wx, wy, wz = (1.0 - fx, fx), (1.0 - fy, fy), (1.0 - fz, fz)
+    sg = (-1.0, 1.0)
+    out = []
+    for a, b, c in ((0, 0, 0), (0, 1, 0), (0, 1, 1), (0, 0, 1),
+                    (1, 0, 1), (1, 1, 1), (1, 1, 0), (1, 0, 0)):
+        out.append((ix + a, iy + b, iz + c, wx[a] * wy[b] * wz[c],
+                    sg[a] * wy[b] * wz[c], wx[a] * sg[b] * wz[c], wx[a] * wy[b] * sg[c]))
+    return out
+
+
+def _alive_index(cx, cy, cz, ng, ngo):
+    u, v, w = cx - ngo, cy - ngo, cz - ngo
+    ok = (u >= 0) & (u < ng) & (v >= 0) & (v < ng) & (w >= 0) & (w < ng)
+    return ok, (np.where(ok, u, 0) * ng + np.where(ok, v, 0)) * ng + np.where(ok, w, 0)
+
+
+def _image_index(cx, cy, cz, ng, ngo):
+    nglt = ng + 2 * ngo + 1
+    ok = ((cx >= 0) & (cx < nglt) & (cy >= 0) & (cy < nglt) & (cz >= 0) & (cz < nglt))
+    u, v, w = ((c - ngo) % ng for c in (cx, cy, cz))
+    return ok, (u * ng + v) * ng + w
+
+
+def _solve_ops(ng):
+    G = green(ng)
+    _, _, g = quiet_tables(ng)
+    shp = [(ng, 1, 1), (1, ng, 1), (1, 1, ng)]
+    return [-1j * g.reshape(shp[a]) * G for a in range(3)]
+
+
+def _deposit64(x, y, z, ng, ngo, c, base=None):
+    rho = np.zeros(ng ** 3)
+    for cx, cy, cz, w, *_ in _corners64(x, y, z, base):
+        ok, k = _alive_index(cx, cy, cz, ng, ngo)
+        np.add.at(rho, k[ok], c * w[ok])
+    return rho.reshape(ng, ng, ng)
+
+
+def force64(x, y, z, ng: int, ngo: int, gpscal: float = 1.0, base=None) -> np.ndarray:
+    """F (n, 3) in float64: the interpolated gradient fields (dv / (fscal tau)).
+    base: see _corners64."""
+    S = _solve_ops(ng)
+    rk = np.fft.fftn(_deposit64(x, y, z, ng, ngo, gpscal ** 3, base))
+    Gd = [(np.fft.ifftn(S[a] * rk) * ng ** 3).real.ravel() for a in range(3)]
+    F = np.zeros((len(np.atleast_1d(x)), 3))
+    for cx, cy, cz, w, *_ in _corners64(x, y, z, base):
+        ok, k = _image_index(cx, cy, cz, ng, ngo)
+        for a in range(3):
+            F[:, a] += np.where(ok, w * Gd[a][k], 0.0)
+    return F
+
+
+def vjp64(x, y, z, vbar, ng: int, ngo: int, gpscal: float = 1.0) -> np.ndarray:
+    """(dF/dx)^T vbar per particle, (n, 3) float64 (multiply by fscal tau for
+    the kick's)."""
+    vbar = np.asarray(vbar, np.float64)
+    c = gpscal ** 3
+    S = _solve_ops(ng)
+    rk = np.fft.fftn(_deposit64(x, y, z, ng, ngo, c))
+    Gd = [(np.fft.ifftn(S[a] * rk) * ng ** 3).real.ravel() for a in range(3)]
+    corners = _corners64(x, y, z)
+    xbar = np.zeros((vbar.shape[0], 3))
+    adj = [np.zeros(ng ** 3) for _ in range(3)]
+    for cx, cy, cz, w, gx, gy, gz in corners:
+        ok, k = _image_index(cx, cy, cz, ng, ngo)
+        dot = sum(vbar[:, a] * np.where(ok, Gd[a][k], 0.0) for a in range(3))
+        xbar += np.stack([gx, gy, gz], 1) * dot[:, None]
+        for a in range(3):
+            np.add.at(adj[a], k[ok], (w * vbar[:, a])[ok])
+    spec = sum(np.conj(S[a]) * np.fft.fftn(adj[a].reshape(ng, ng, ng)) for a in range(3))
+    phibar = (np.fft.ifftn(spec) * ng ** 3).real.ravel()
+    for cx, cy, cz, w, gx, gy, gz in corners:
+        ok, k = _alive_index(cx, cy, cz, ng, ngo)
+        f = np.where(ok, phibar[k], 0.0) * c
+        xbar += np.stack([gx, gy, gz], 1) * f[:, None]
+    return xbar

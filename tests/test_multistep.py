@@ -215,3 +215,138 @@ def test_checkpointed_equals_stored_and_is_linear(ctx):
     a.forward_box(0, S2)
     for u, w in zip(S.x + S.v, S2.x + S2.v):
         assert torch.equal(u, w)
+
+
+# ---------------------------------------------------------------------------
+# the map with PM kicks (the whole TreePM step)
+# ---------------------------------------------------------------------------
+
+def _pm_dicts(pm):
+    return [tuple(None if q is None else dict(ng=q.ng, ngo=q.ngo, gpscal=q.gpscal, fscal=q.fscal,
+                                              tau=q.tau) for q in pair) for pair in pm]
+
+
+def _fd_pm(O, x0, v0, m, steps, nsub, tapes, pm, xbar, vbar, k, d, h, base, pm_base):
+    out = []
+    for step in (h, -h):
+        x = x0.copy()
+        x[k] += step * d
+        out.append(O.multistep64(x, v0, m, steps, nsub, tapes, cut_pos=base, pm=pm,
+                                 pm_cut=pm_base))
+    (xp, vp), (xm, vm) = out
+    return (float((xbar * (xp - xm)).sum() + (vbar * (vp - vm)).sum())) / (2 * h)
+
+
+def _check_fd_pm(O, x0, v0, m, steps, nsub, tapes, pm, xbar, vbar, grad, samples, h, rng):
+    """_check_fd for the map with PM kicks: cutoffs and CIC cells decided on
+    the unperturbed run (the weights are piecewise linear in the positions)."""
+    base, pm_base = [], []
+    O.multistep64(x0, v0, m, steps, nsub, tapes, pm=pm, traj_out=base, pm_traj_out=pm_base)
+    rms = np.sqrt((grad ** 2).sum(1).mean())
+    bad = 0
+    for k in samples:
+        d = rng.standard_normal(3)
+        d /= np.linalg.norm(d)
+        f = _fd_pm(O, x0, v0, m, steps, nsub, tapes, pm, xbar, vbar, k, d, h, base, pm_base)
+        bad += abs(grad[k] @ d - f) > ADJ_TOL * max(np.linalg.norm(grad[k]), rms)
+    return bad
+
+
+def test_fp64_multistep_with_pm_gradient_matches_fd(hsr_lib, oracle_lib):
+    """The FP64 checker with PM kicks opening and closing each step (8^3 PM
+    grid): its reverse pass against its own central differences."""
+    O = oracle_lib
+    p = synth.random_box(600, 8.0, 21)
+    kp = synth.kick_params(p, nd=16, open_angle=0.0)
+    kp.min_force, kp.max_force = (-1.0,) * 3, (9.0,) * 3
+    steps = [multistep.StepParams(alpha=1.0, pp=0.5, adot=1.0, tau_sub=0.02, fcoeff=0.03),
+             multistep.StepParams(alpha=1.0, pp=0.6, adot=1.0, tau_sub=0.02, fcoeff=0.025)]
+    pm = [(dict(ng=8, ngo=0, gpscal=1.0, fscal=2.0, tau=0.05),
+           dict(ng=8, ngo=0, gpscal=1.0, fscal=2.2, tau=0.1)),
+          (None, dict(ng=8, ngo=0, gpscal=1.0, fscal=2.4, tau=0.05))]
+    nsub = 2
+    x = np.stack([p.x, p.y, p.z], 1).astype(np.float64)
+    v = 0.1 * np.stack([p.vx, p.vy, p.vz], 1).astype(np.float64)
+    m = p.mass.astype(np.float64)
+    tapes = []
+    xx, vv = x.copy(), v.copy()
+    import pm_oracle
+    for s, st in enumerate(steps):
+        pt = O.stream_factor(st.alpha, st.pp, st.tau_sub, st.adot)
+        for half in (0, 1):
+            if half == 1:
+                for _ in range(nsub):
+                    xx += pt * vv
+                    t = _host_tape(xx, m, dataclasses.replace(kp, fcoeff=st.fcoeff))
+                    tapes.append(t)
+                    vv[t["perm"]] += O.kick64(xx[t["perm"]], m[t["perm"]], t, st.fcoeff)
+                    xx += pt * vv
+            q = pm[s][half]
+            if q is not None:
+                vv += q["fscal"] * q["tau"] * pm_oracle.force64(xx[:, 0], xx[:, 1], xx[:, 2], 8,
+                                                                 0, 1.0)
+    rng = np.random.default_rng(5)
+    xbar, vbar = rng.standard_normal(x.shape), rng.standard_normal(v.shape)
+    xT, vT, L, gx, gv = O.multistep64(x, v, m, steps, nsub, tapes, xbar, vbar, pm=pm)
+    assert np.allclose(xT, xx) and np.allclose(vT, vv)
+    smp = rng.choice(len(m), 16, replace=False)
+    bad = _check_fd_pm(O, x, v, m, steps, nsub, tapes, pm, xbar, vbar, gx, smp, 1e-5, rng)
+    assert bad == 0, bad
+
+
+@pytest.mark.gpu
+def test_multistep_with_pm_adjoint_vs_fp64_and_fd(ctx, oracle_lib):
+    """One 12^3 box with overload ghosts, 3 PM steps x 2 sub-cycles with the
+    driver's PM kicks (half kick opening the first step, a kick closing every
+    step), checkpoints every 2 steps: the GPU reverse pass against the FP64
+    gradient along the GPU trajectory and FP64 differences of the map."""
+    torch = pytest.importorskip("torch")
+    O = oracle_lib
+    nsteps, nsub = 3, 2
+    steps = multistep.schedule(50.0, 30.0, nsteps, nsub)
+    p = _boxes(1, 12, 130)[0]
+    ng, ngo = p.meta["ng"], p.meta["ngo"]
+    pm = multistep.pm_schedule(50.0, 30.0, nsteps, ng, ngo)
+    kp = synth.kick_params(p, nd=64)
+    ms = multistep.MultiStep(ctx, [kp], steps, nsub, checkpoint_every=2, pm=pm)
+    tapes, kick_x = {}, {}
+
+    def on_tape(b, s, j, c, x1):
+        tapes[(s, j)] = _tape_of(c, p.n)
+        kick_x[(s, j)] = np.stack([t.cpu().numpy() for t in x1], 1).astype(np.float64)
+    ms.on_tape = on_tape
+    rng = np.random.default_rng(9)
+    n = p.n
+    xbar = rng.standard_normal((n, 3)).astype(np.float32)
+    vbar = rng.standard_normal((n, 3)).astype(np.float32)
+    tx = [torch.from_numpy(np.ascontiguousarray(xbar[:, d])).cuda() for d in range(3)]
+    tv = [torch.from_numpy(np.ascontiguousarray(vbar[:, d])).cuda() for d in range(3)]
+    S0 = multistep.box_state(p)
+    # PM kick positions of the GPU trajectory (forward pass, stored)
+    rec = []
+    ms._run(0, S0.clone(), 0, nsteps, record=rec)
+    pm_x = [np.stack([t.cpu().numpy() for t in r[2]], 1).astype(np.float64)
+            for r in rec if r[0] == "pm"]
+    gx_t, gv_t = ms.adjoint_box(0, S0, tx, tv)
+    gx = np.stack([t.cpu().numpy() for t in gx_t], 1).astype(np.float64)
+    gv = np.stack([t.cpu().numpy() for t in gv_t], 1).astype(np.float64)
+    order = [(s, j) for s in range(nsteps) for j in range(nsub)]
+    tl = [tapes[k] for k in order]
+    xl = [kick_x[k] for k in order]
+    pmd = _pm_dicts(pm)
+    x0 = np.stack([p.x, p.y, p.z], 1).astype(np.float64)
+    v0 = np.stack([p.vx, p.vy, p.vz], 1).astype(np.float64)
+    m = p.mass.astype(np.float64)
+    _, _, _, rx, rv = O.multistep64(x0, v0, m, steps, nsub, tl, xbar, vbar, kick_pos=xl, pm=pmd,
+                                    pm_pos=pm_x)
+    for g, r in ((gx, rx), (gv, rv)):
+        rms, mx = force_errors(g, r)
+        assert rms <= 2e-5 and mx <= 2e-3, (rms, mx)
+    inner = np.flatnonzero(p.mask == 0)
+    smp = rng.choice(inner, 24, replace=False)
+    _, _, _, fx, _ = O.multistep64(x0, v0, m, steps, nsub, tl, xbar, vbar, pm=pmd)
+    bad = _check_fd_pm(O, x0, v0, m, steps, nsub, tl, pmd, xbar, vbar, fx, smp, 1e-4, rng)
+    assert bad == 0, bad
+    rms, mx = force_errors(gx[smp], fx[smp])
+    assert rms <= ADJ_TOL, rms
+    assert ms.pm_kicks == 3 * (nsteps + 1)  # forward, recomputation, stored run

@@ -330,3 +330,72 @@ def test_treepm_step_matches_restatement(ctx, oracle_lib):
 def dataclasses_replace(obj, **kw):
     import dataclasses
     return dataclasses.replace(obj, **kw)
+
+
+# ---------------------------------------------------------------------------
+# the PM kick's vector-Jacobian product
+# ---------------------------------------------------------------------------
+
+def test_restatement_vjp_matches_fd():
+    """vjp64 (the float64 checker of hsr_pm_vjp) against central differences
+    of force64, with overload ghosts and a deposit weight gpscal^3 != 1."""
+    p = _box(8, seed=3)
+    ng, ngo = 8, p.meta["ngo"]
+    x, y, z = (a.astype(np.float64) for a in (p.x, p.y, p.z))
+    rng = np.random.default_rng(0)
+    vb = rng.standard_normal((p.n, 3))
+    xb = P.vjp64(x, y, z, vb, ng, ngo, 1.3)
+    h = 1e-6
+    for i in rng.choice(p.n, 8, replace=False):
+        for d in range(3):
+            xs = [x.copy(), y.copy(), z.copy()]
+            xs[d][i] += h
+            fp = (P.force64(*xs, ng, ngo, 1.3) * vb).sum()
+            xs[d][i] -= 2 * h
+            fm = (P.force64(*xs, ng, ngo, 1.3) * vb).sum()
+            fd = (fp - fm) / (2 * h)
+            assert abs(fd - xb[i, d]) <= 1e-6 * max(abs(xb[i, d]), 1e-3), (i, d, fd, xb[i, d])
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("prec", [0, 1], ids=["f64", "f32"])
+def test_vjp_matches_restatement(ctx, prec):
+    p = _box(32, seed=41)
+    ng, ngo = 32, p.meta["ngo"]
+    prm = _params(ng, ngo, prec, gpscal=1.1, fscal=0.8, tau=0.02)
+    rng = np.random.default_rng(3)
+    vb = rng.standard_normal((p.n, 3)).astype(np.float32)
+    got = ctx.pm_vjp(p.x, p.y, p.z, vb, prm)
+    want = 0.8 * 0.02 * P.vjp64(p.x.astype(np.float64), p.y.astype(np.float64),
+                                p.z.astype(np.float64), vb.astype(np.float64), ng, ngo,
+                                float(np.float32(1.1)))
+    rms, mx = _err(got, want)
+    rt, mt = (1e-5, 1e-3) if prec == 0 else (3e-5, 2e-3)
+    assert rms < rt and mx < mt, (rms, mx)
+    st = ctx.pm_stats()
+    assert st["fft_execs"] == 4
+
+
+@pytest.mark.gpu
+def test_vjp_is_linear_and_device_matches_host(ctx):
+    import torch
+    p = _box(16, seed=43)
+    ng, ngo = 16, p.meta["ngo"]
+    prm = _params(ng, ngo, 0, fscal=1.0, tau=1.0)
+    rng = np.random.default_rng(4)
+    u = rng.standard_normal((p.n, 3)).astype(np.float32)
+    w = rng.standard_normal((p.n, 3)).astype(np.float32)
+    a = ctx.pm_vjp(p.x, p.y, p.z, u, prm).astype(np.float64)
+    b = ctx.pm_vjp(p.x, p.y, p.z, w, prm).astype(np.float64)
+    c = ctx.pm_vjp(p.x, p.y, p.z, 2 * u + w, prm).astype(np.float64)
+    rms, _ = _err(c, 2 * a + b)
+    assert rms < 1e-5, rms
+    dev = torch.device("cuda", 0)
+    t = [torch.from_numpy(np.ascontiguousarray(q)).to(dev) for q in (p.x, p.y, p.z)]
+    tu = [torch.from_numpy(np.ascontiguousarray(u[:, d])).to(dev) for d in range(3)]
+    out = [torch.zeros(p.n, device=dev) for _ in range(3)]
+    torch.cuda.synchronize()
+    ctx.pm_vjp_device(*t, *tu, *out, prm)
+    got = np.stack([o.cpu().numpy() for o in out], 1).astype(np.float64)
+    rms, _ = _err(got, a)
+    assert rms < 1e-5, rms
