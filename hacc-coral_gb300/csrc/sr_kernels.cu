@@ -431,11 +431,20 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
                 const float *__restrict__ uz, float *__restrict__ xbx, float *__restrict__ xby,
                 float *__restrict__ xbz, float fcoeff, float rsm2, float rcut2, float rcull2,
                 unsigned long long *__restrict__ queue) {
-  __shared__ float4 slot[kBatchedWarps][32];
-  __shared__ int32_t sidx[kBatchedWarps][32];
+  // kept entries, two per slot pair as in k_pairs_batched: (x, x', y, y'),
+  // (z, z', m, m') and their table indices; the group's particles, two per
+  // slot pair: (x, x', y, y'), (z, z', w, w'), (u0, u0', u1, u1'),
+  // (u2, u2', index bits, index bits')
+  __shared__ float4 bufA[kBatchedWarps][33], bufB[kBatchedWarps][33];
+  __shared__ int32_t bufI[kBatchedWarps][66];
+  __shared__ float4 grp[kBatchedWarps][4][16];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
   const unsigned full = 0xffffffffu;
+  const unsigned below = (1u << lane) - 1u;
+  float *const fa = reinterpret_cast<float *>(bufA[w]);
+  float *const fb = reinterpret_cast<float *>(bufB[w]);
+  float *const fg = reinterpret_cast<float *>(grp[w]);
   for (;;) {
     unsigned long long it = 0;
     if (lane == 0) it = atomicAdd(queue, 1ull);
@@ -445,9 +454,9 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
     const bool act = lane < W.g_count;
     const int pi = gidx[W.g_begin + (act ? lane : 0)];
     const float4 P = pos[pi];
-    // inactive lanes carry a zero cotangent, so they add nothing
+    // inactive lanes carry a zero cotangent and weight, so they add nothing
     const float u0 = act ? ux[pi] : 0.f, u1 = act ? uy[pi] : 0.f, u2 = act ? uz[pi] : 0.f;
-    const float wi = (LAW == LAW_POLY5_STEP16) ? fcoeff : fcoeff * P.w;
+    const float wi = act ? ((LAW == LAW_POLY5_STEP16) ? fcoeff : fcoeff * P.w) : 0.f;
     float lox = P.x, hix = P.x, loy = P.y, hiy = P.y, loz = P.z, hiz = P.z;
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
@@ -463,62 +472,130 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
     const float hy = fmaf(fmaxf(fabsf(loy), fabsf(hiy)), 4.8e-7f, 0.5f * (hiy - loy));
     const float hz = fmaf(fmaxf(fabsf(loz), fabsf(hiz)), 4.8e-7f, 0.5f * (hiz - loz));
     const float cx = 0.5f * (lox + hix), cy = 0.5f * (loy + hiy), cz = 0.5f * (loz + hiz);
-    float bx = 0.f, by = 0.f, bz = 0.f;
+    // the group in shared memory for the entry-side pass
+    {
+      const int o = 4 * (lane >> 1) + (lane & 1);
+      fg[o] = P.x;
+      fg[o + 2] = P.y;
+      fg[64 + o] = P.z;
+      fg[64 + o + 2] = wi;
+      fg[128 + o] = u0;
+      fg[128 + o + 2] = u1;
+      fg[192 + o] = u2;
+      fg[192 + o + 2] = __int_as_float(act ? pi : -1);
+    }
+    const float2 nxi = make_float2(-P.x, -P.x), nyi = make_float2(-P.y, -P.y),
+                 nzi = make_float2(-P.z, -P.z);
+    const float2 wi2 = make_float2(wi, wi), ua = make_float2(u0, u0), ub = make_float2(u1, u1),
+                 uc = make_float2(u2, u2);
+    float2 bx = make_float2(0.f, 0.f), by = bx, bz = bx;  // particle side
     const int32_t *lst = idx + W.j_begin;
-    for (int j0 = 0; j0 < W.j_len; j0 += 32) {
-      const int j = j0 + lane;
-      const bool ok = j < W.j_len;
-      const int32_t jt = lst[ok ? j : 0];
-      const float4 J = pos[jt];
-      const float dx = fmaxf(fabsf(J.x - cx) - hx, 0.f);
-      const float dy = fmaxf(fabsf(J.y - cy) - hy, 0.f);
-      const float dz = fmaxf(fabsf(J.z - cz) - hz, 0.f);
-      unsigned keep = __ballot_sync(full, ok && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < rcull2);
-      if (!keep) continue;
-      slot[w][lane] = J;
-      sidx[w][lane] = jt;
+    const int len = W.j_len;
+    int nbuf = 0;
+    for (int j0 = 0; j0 < len || nbuf > 0; j0 += 32) {
+      if (j0 < len) {
+        const int j = j0 + lane;
+        const bool ok = j < len;
+        const int32_t jt = lst[ok ? j : 0];
+        const float4 J = pos[jt];
+        const float dx = fmaxf(fabsf(J.x - cx) - hx, 0.f);
+        const float dy = fmaxf(fabsf(J.y - cy) - hy, 0.f);
+        const float dz = fmaxf(fabsf(J.z - cz) - hz, 0.f);
+        const bool k = ok && fmaf(dx, dx, fmaf(dy, dy, dz * dz)) < rcull2;
+        const unsigned keep = __ballot_sync(full, k);
+        if (k) {
+          const int e = nbuf + __popc(keep & below);
+          const int o = 4 * (e >> 1) + (e & 1);
+          fa[o] = J.x;
+          fa[o + 2] = J.y;
+          fb[o] = J.z;
+          fb[o + 2] = J.w;
+          bufI[w][e] = jt;
+        }
+        nbuf += __popc(keep);
+        if (nbuf < 32 && j0 + 32 < len) continue;
+      }
+      // evaluate up to 32 buffered entries (all of them at the end of the list)
+      const int ne = nbuf < 32 ? nbuf : 32;
+      if (lane >= ne && lane < ((ne + 1) & ~1)) {
+        // odd tail: a far-away massless entry of no particle
+        const int o = 4 * (lane >> 1) + (lane & 1);
+        fa[o] = 1e18f;
+        fa[o + 2] = 1e18f;
+        fb[o] = 1e18f;
+        fb[o + 2] = 0.f;
+        bufI[w][lane] = -2;
+      }
       __syncwarp();
-      while (keep) {
-        const int b = __ffs(keep) - 1;
-        keep &= keep - 1;
-        const float4 Q = slot[w][b];
-        const int32_t qt = sidx[w][b];
-        const float ex = Q.x - P.x, ey = Q.y - P.y, ez = Q.z - P.z;
-        const float r2 = fmaf(ex, ex, fmaf(ey, ey, ez * ez));
-        float vx = 0.f, vy = 0.f, vz = 0.f;
-        if (qt != pi && in_range<LAW>(r2, rcut2)) {
-          const float y = rsqrtf(r2 + rsm2);
-          const float y2 = y * y;
-          const float g = fmaf(y, y2, neg_poly<LAW>(r2));
-          const float gp = fmaf(-1.5f * y2, y2 * y, neg_dpoly<LAW>(r2));  // dg/dr2
-          const float wij = wi * Q.w;
-          const float du = fmaf(ex, u0, fmaf(ey, u1, ez * u2));
-          const float a = wij * g, bq = 2.f * wij * gp * du;
-          vx = fmaf(a, u0, bq * ex);
-          vy = fmaf(a, u1, bq * ey);
-          vz = fmaf(a, u2, bq * ez);
+      // particle side: lanes are the group's particles, two entries a step
+      for (int q = 0; q < (ne + 1) / 2; ++q) {
+        const float4 A = bufA[w][q], B = bufB[w][q];
+        const int ja = bufI[w][2 * q], jb = bufI[w][2 * q + 1];
+        const float2 ex = __fadd2_rn(make_float2(A.x, A.y), nxi);
+        const float2 ey = __fadd2_rn(make_float2(A.z, A.w), nyi);
+        const float2 ez = __fadd2_rn(make_float2(B.x, B.y), nzi);
+        const float2 r2 = __ffma2_rn(ex, ex, __ffma2_rn(ey, ey, __fmul2_rn(ez, ez)));
+        const bool on_a = act && ja != pi && in_range<LAW>(r2.x, rcut2);
+        const bool on_b = act && jb != pi && in_range<LAW>(r2.y, rcut2);
+        float2 vx, vy, vz;
+        vjp2_term<LAW>(ex, ey, ez, __fmul2_rn(wi2, make_float2(B.z, B.w)), ua, ub, uc, rsm2, on_a,
+                       on_b, vx, vy, vz);
+        bx = __fadd2_rn(bx, vx);
+        by = __fadd2_rn(by, vy);
+        bz = __fadd2_rn(bz, vz);
+      }
+      // entry side: lanes are the buffered entries, two particles a step
+      if (lane < ne) {
+        const int o = 4 * (lane >> 1) + (lane & 1);
+        const float xj = fa[o], yj = fa[o + 2], zj = fb[o], mj = fb[o + 2];
+        const int jt = bufI[w][lane];
+        const float2 xj2 = make_float2(xj, xj), yj2 = make_float2(yj, yj),
+                     zj2 = make_float2(zj, zj), mj2 = make_float2(mj, mj);
+        float2 ex2 = make_float2(0.f, 0.f), ey2 = ex2, ez2 = ex2;
+        const int np2 = (W.g_count + 1) / 2;
+        for (int q = 0; q < np2; ++q) {
+          const float4 G0 = grp[w][0][q], G1 = grp[w][1][q], G2 = grp[w][2][q],
+                       G3 = grp[w][3][q];
+          // e = x_j - x_i
+          const float2 ex = __fadd2_rn(xj2, make_float2(-G0.x, -G0.y));
+          const float2 ey = __fadd2_rn(yj2, make_float2(-G0.z, -G0.w));
+          const float2 ez = __fadd2_rn(zj2, make_float2(-G1.x, -G1.y));
+          const float2 r2 = __ffma2_rn(ex, ex, __ffma2_rn(ey, ey, __fmul2_rn(ez, ez)));
+          const int ia = __float_as_int(G3.z), ib = __float_as_int(G3.w);
+          const bool on_a = ia >= 0 && jt != ia && in_range<LAW>(r2.x, rcut2);
+          const bool on_b = ib >= 0 && jt != ib && in_range<LAW>(r2.y, rcut2);
+          float2 vx, vy, vz;
+          vjp2_term<LAW>(ex, ey, ez, __fmul2_rn(make_float2(G1.z, G1.w), mj2),
+                         make_float2(G2.x, G2.y), make_float2(G2.z, G2.w),
+                         make_float2(G3.x, G3.y), rsm2, on_a, on_b, vx, vy, vz);
+          ex2 = __fadd2_rn(ex2, vx);
+          ey2 = __fadd2_rn(ey2, vy);
+          ez2 = __fadd2_rn(ez2, vz);
         }
-        bx -= vx;
-        by -= vy;
-        bz -= vz;
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-          vx += __shfl_xor_sync(full, vx, o);
-          vy += __shfl_xor_sync(full, vy, o);
-          vz += __shfl_xor_sync(full, vz, o);
-        }
-        if (lane == 0 && (vx != 0.f || vy != 0.f || vz != 0.f)) {
-          atomicAdd(xbx + qt, vx);
-          atomicAdd(xby + qt, vy);
-          atomicAdd(xbz + qt, vz);
+        const float vx = ex2.x + ex2.y, vy = ey2.x + ey2.y, vz = ez2.x + ez2.y;
+        if (vx != 0.f || vy != 0.f || vz != 0.f) {
+          atomicAdd(xbx + jt, vx);
+          atomicAdd(xby + jt, vy);
+          atomicAdd(xbz + jt, vz);
         }
       }
       __syncwarp();
+      // keep what is past the first 32 (slot pairs 16.. move to 0..)
+      if (nbuf > 32) {
+        if (2 * lane < nbuf - 32) {
+          bufA[w][lane] = bufA[w][16 + lane];
+          bufB[w][lane] = bufB[w][16 + lane];
+        }
+        if (lane < nbuf - 32) bufI[w][lane] = bufI[w][32 + lane];
+      }
+      nbuf -= ne;
+      __syncwarp();
+      if (j0 >= len && nbuf == 0) break;
     }
     if (act) {
-      atomicAdd(xbx + pi, bx);
-      atomicAdd(xby + pi, by);
-      atomicAdd(xbz + pi, bz);
+      atomicAdd(xbx + pi, -(bx.x + bx.y));
+      atomicAdd(xby + pi, -(by.x + by.y));
+      atomicAdd(xbz + pi, -(bz.x + bz.y));
     }
   }
 }

@@ -215,6 +215,83 @@ __device__ __forceinline__ void pair2_acc_s(float2 nxi, float2 nyi, float2 nzi, 
   az = __ffma2_rn(w, dz, az);
 }
 
+// -p(r2) and -p'(r2) of the law on two values at once (packed FP32), the
+// same coefficients and Horner order as neg_poly / neg_dpoly.
+template <int LAW>
+__device__ __forceinline__ float2 neg_poly2(float2 r2);
+template <>
+__device__ __forceinline__ float2 neg_poly2<LAW_POLY6>(float2 r2) {
+  const float c[7] = {-static_cast<float>(0.000000147305), -static_cast<float>(-0.00000663394),
+                      -static_cast<float>(0.000132336),    -static_cast<float>(-0.00159485),
+                      -static_cast<float>(0.0133122),      -static_cast<float>(-0.0783394),
+                      -static_cast<float>(0.271431)};
+  float2 q = make_float2(c[0], c[0]);
+#pragma unroll
+  for (int k = 1; k < 7; ++k) q = __ffma2_rn(q, r2, make_float2(c[k], c[k]));
+  return q;
+}
+template <>
+__device__ __forceinline__ float2 neg_poly2<LAW_POLY5_STEP16>(float2 r2) {
+  const float c[6] = {-static_cast<float>(-0.00000147177), -static_cast<float>(0.0000605491),
+                      -static_cast<float>(-0.00109313),    -static_cast<float>(0.0114808),
+                      -static_cast<float>(-0.0750978),     -static_cast<float>(0.269327)};
+  float2 q = make_float2(c[0], c[0]);
+#pragma unroll
+  for (int k = 1; k < 6; ++k) q = __ffma2_rn(q, r2, make_float2(c[k], c[k]));
+  return q;
+}
+template <int LAW>
+__device__ __forceinline__ float2 neg_dpoly2(float2 r2);
+template <>
+__device__ __forceinline__ float2 neg_dpoly2<LAW_POLY6>(float2 r2) {
+  const float c[6] = {-6.0f * static_cast<float>(0.000000147305),
+                      -5.0f * static_cast<float>(-0.00000663394),
+                      -4.0f * static_cast<float>(0.000132336),
+                      -3.0f * static_cast<float>(-0.00159485),
+                      -2.0f * static_cast<float>(0.0133122), -static_cast<float>(-0.0783394)};
+  float2 q = make_float2(c[0], c[0]);
+#pragma unroll
+  for (int k = 1; k < 6; ++k) q = __ffma2_rn(q, r2, make_float2(c[k], c[k]));
+  return q;
+}
+template <>
+__device__ __forceinline__ float2 neg_dpoly2<LAW_POLY5_STEP16>(float2 r2) {
+  const float c[5] = {-5.0f * static_cast<float>(-0.00000147177),
+                      -4.0f * static_cast<float>(0.0000605491),
+                      -3.0f * static_cast<float>(-0.00109313),
+                      -2.0f * static_cast<float>(0.0114808), -static_cast<float>(-0.0750978)};
+  float2 q = make_float2(c[0], c[0]);
+#pragma unroll
+  for (int k = 1; k < 5; ++k) q = __ffma2_rn(q, r2, make_float2(c[k], c[k]));
+  return q;
+}
+
+// The adjoint pair term for two pairs at once: with e = x_j - x_i,
+// M = w (g I + 2 g' e e^T), w = w_i m_j, returns M u (u: particle i's
+// cotangent), zero where `on` is false.  Packed FP32 as pair2_acc_s.
+template <int LAW>
+__device__ __forceinline__ void vjp2_term(float2 ex, float2 ey, float2 ez, float2 w, float2 u0,
+                                          float2 u1, float2 u2, float rsm2, bool on_a, bool on_b,
+                                          float2 &vx, float2 &vy, float2 &vz) {
+  const float2 r2 = __ffma2_rn(ex, ex, __ffma2_rn(ey, ey, __fmul2_rn(ez, ez)));
+  const float2 s = __fadd2_rn(r2, make_float2(rsm2, rsm2));
+  const float2 y = make_float2(rsqrt_ftz(s.x), rsqrt_ftz(s.y));
+  const float2 y2 = __fmul2_rn(y, y);
+  const float2 g = __ffma2_rn(y, y2, neg_poly2<LAW>(r2));
+  const float2 gp = __ffma2_rn(__fmul2_rn(make_float2(-1.5f, -1.5f), y2), __fmul2_rn(y2, y),
+                               neg_dpoly2<LAW>(r2));
+  const float2 du = __ffma2_rn(ex, u0, __ffma2_rn(ey, u1, __fmul2_rn(ez, u2)));
+  float2 a = __fmul2_rn(w, g);
+  float2 bq = __fmul2_rn(__fmul2_rn(__fmul2_rn(make_float2(2.f, 2.f), w), gp), du);
+  a.x = on_a ? a.x : 0.f;
+  a.y = on_b ? a.y : 0.f;
+  bq.x = on_a ? bq.x : 0.f;
+  bq.y = on_b ? bq.y : 0.f;
+  vx = __ffma2_rn(a, u0, __fmul2_rn(bq, ex));
+  vy = __ffma2_rn(a, u1, __fmul2_rn(bq, ey));
+  vz = __ffma2_rn(a, u2, __fmul2_rn(bq, ez));
+}
+
 // One pair: accumulates m_j g(r2) d into (ax, ay, az).
 template <int LAW>
 __device__ __forceinline__ void pair_acc(float xi, float yi, float zi, const float4 pj, float rsm2,
