@@ -971,15 +971,20 @@ __global__ void __launch_bounds__(kChunkThreads)
       tpos[N.offset + q] = p;
       toid[N.offset + q] = oid[R.begin + e];
       idx[N.offset + q] = R.local + e;
+    } else if (e < R.len && R.local + e >= N.nleft) {
+      // a right element at or after nleft: no swap touches it, it stays
+      tpos[R.begin + e] = p;
+      toid[R.begin + e] = oid[R.begin + e];
     }
     r += __popc(bal);
   }
 }
 
-// The other particles: those at or after position nleft stay; one at p <
-// nleft moves along p -> idx[p] -> ... until it lands at or after nleft (the
-// reference's swap sequence, RCBForceTree.cxx:647-669).  Positions increase
-// strictly along a chain, so it ends within count steps.
+// The other particles: those at or after position nleft stay (k_part_left
+// writes them); one at p < nleft moves along p -> idx[p] -> ... until it
+// lands at or after nleft (the reference's swap sequence,
+// RCBForceTree.cxx:647-669).  Positions increase strictly along a chain, so
+// it ends within count steps.
 template <bool WM>
 __global__ void __launch_bounds__(kChunkThreads)
     k_part_right(const float4 *__restrict__ pos, const int32_t *__restrict__ oid, const DNode *nodes,
@@ -993,8 +998,9 @@ __global__ void __launch_bounds__(kChunkThreads)
   const int d = N.split_dim;
   const float split = N.xc[d];
   const int32_t is = N.nleft;
+  if (R.local >= is) return;  // every element here stays (k_part_left)
   if (WM) {
-    for (int k = tid; k < R.len; k += NT) {
+    for (int k = tid; k < R.len && R.local + k < is; k += NT) {
       const int64_t src = R.begin + k;
       const float4 p = pos[src];
       if (key_of(p, d) < split) continue;
@@ -1027,7 +1033,7 @@ __global__ void __launch_bounds__(kChunkThreads)
   for (int j = 0; j < kPerT; ++j) {
     const int k = tid + j * NT;
     q[j] = R.local + k;
-    if (k < R.len && !(key_of(pos[R.begin + k], d) < split)) right |= 1u << j;
+    if (k < R.len && q[j] < is && !(key_of(pos[R.begin + k], d) < split)) right |= 1u << j;
   }
   unsigned active = 0;
 #pragma unroll
