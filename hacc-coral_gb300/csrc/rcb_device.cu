@@ -1186,12 +1186,22 @@ __global__ void k_pseudo(DNode *nodes, int32_t lb, int32_t le, const float4 *__r
     // leaf by size: masses from its particles when it has more than k;
     // a leaf left by a failed split keeps zero masses (its children are empty)
     if (T.count <= nd && T.count > k) {
-      pppts_(k, T.tdr, T.xc, px, py, pz);
       const float4 *p = pos + T.offset;
-      pp_accum_(k, T.count, [&](int32_t i, float &x, float &y, float &z, float &m) {
-        const float4 q = p[i];
-        x = q.x; y = q.y; z = q.z; m = q.w;
-      }, T.xc, px, py, pz, ppm, T.tdr);
+      if (k == 1) {
+        // the monopole's point is the centre of mass: every term's weight is
+        // 1/1 + 0 + 0 (pp_accum_ with rj2 == 0), so the mass is the
+        // sequential float sum of the particle masses
+        float m = 0.f;
+#pragma unroll 8
+        for (int32_t i = 0; i < T.count; ++i) m = fadd_(m, fmul_(p[i].w, 1.0f));
+        ppm[0] = m;
+      } else {
+        pppts_(k, T.tdr, T.xc, px, py, pz);
+        pp_accum_(k, T.count, [&](int32_t i, float &x, float &y, float &z, float &m) {
+          const float4 q = p[i];
+          x = q.x; y = q.y; z = q.z; m = q.w;
+        }, T.xc, px, py, pz, ppm, T.tdr);
+      }
     }
   } else {
     pppts_(k, T.tdr, T.xc, px, py, pz);
