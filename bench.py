@@ -22,7 +22,8 @@ the force box, fused with the velocity kick.
 * cpu_baseline -- the CPU restatement of the reference force tree (oracle),
                 timed on this host's cores on a bounded slab of the workload.
 * treepm     -- the long-range PM kick on the same box (deposit, FFT solve,
-                inverse CIC; double and single precision) and one whole
+                inverse CIC; double and single precision), the short-range
+                sub-cycles alone (hsr_subcycle: s/substep), and one whole
                 TreePM step (PM half kick, 5 short-range sub-cycles, PM kick)
                 end to end from host arrays, with the PM restatement timed on
                 the host.
@@ -34,6 +35,7 @@ not shard across GPUs); rank 0 prints one JSON line.
 from __future__ import annotations
 
 import argparse
+import dataclasses
 import json
 import os
 import statistics
@@ -265,8 +267,27 @@ def treepm_section(ctx, p0, kp, args, device: int, cpu: bool):
                       "d2h_bytes": hs["d2h_bytes"], "kernel_launches": rows[-1]["kernel_launches"],
                       "fft_execs": rows[-1]["fft_execs"]}
     del t
-    # one step of the loop: the first step of a run has both PM kicks
+    # the short-range sub-cycles alone (Particles::subCycle): s/substep
     nsub = 5
+    ts_mid = treepm.plan(50.0, 10.0, 10)[0].mid
+    kp_sub = dataclasses.replace(kp, fcoeff=float(synth.kick_coefficient(ts_mid, nsub)))
+    tau_sub = float(np.float32(ts_mid.tau2 / nsub))
+    ctx.subcycle(p0.copy(), kp_sub, nsub, p0.nglt, ts_mid.alpha, ts_mid.pp, tau_sub, ts_mid.adot)
+    sub_runs = []
+    for _ in range(2):
+        q = p0.copy()
+        t0 = time.perf_counter()
+        sst, _ = ctx.subcycle(q, kp_sub, nsub, p0.nglt, ts_mid.alpha, ts_mid.pp, tau_sub,
+                              ts_mid.adot)
+        sub_runs.append((time.perf_counter() - t0, sst))
+    sub_wall, sst = min(sub_runs, key=lambda a: a[0])
+    subcycle = {"nsub": nsub, "s_per_substep": sub_wall / nsub, "s_total": sub_wall,
+                "pairs_per_substep": sst["pairs"] / nsub,
+                "tree_build_ms": sst["t_build_ms"], "lists_ms": sst["t_walk_ms"],
+                "force_ms": sst["t_force_ms"],
+                "note": "hsr_subcycle from host arrays: 5 x (map1, resort, kick, map1) with the "
+                        "arrays resident, copies in and out once"}
+    # one step of the loop: the first step of a run has both PM kicks
     sp = treepm.plan(50.0, 10.0, 10)[0]
     T = treepm.step_params(sp, kp, nsub, ng, ngo, p0.nglt)
     treepm.step(ctx, p0.copy(), T)
@@ -277,7 +298,7 @@ def treepm_section(ctx, p0, kp, args, device: int, cpu: bool):
         r = treepm.step(ctx, q, T)
         steps.append((time.perf_counter() - t0, r))
     wall, r = min(steps, key=lambda a: a[0])
-    out = {"n_side": ng, "n_particles": p0.n, "pm_kick": kick,
+    out = {"n_side": ng, "n_particles": p0.n, "pm_kick": kick, "subcycle": subcycle,
            "step": {"s_per_step": wall, "sub_cycles": nsub, "pm_kicks": 2,
                     "sr_tree_build_ms": r["sr"]["t_build_ms"], "sr_lists_ms": r["sr"]["t_walk_ms"],
                     "sr_force_ms": r["sr"]["t_force_ms"], "sr_pairs": r["sr"]["pairs"],
