@@ -376,6 +376,7 @@ def main():
         e2e_secs.append(time.perf_counter() - t0)
     e2e_t = max_over_ranks(world, sum(e2e_secs))
     pairs = st["pairs"]
+    in_cutoff = ctx.pairs_in_cutoff()
     h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
 
     evaluated = st["evaluated_pairs"]
@@ -504,6 +505,7 @@ def main():
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Zel'dovich lattice with overload ghosts)",
             "config": {**cfg, "pairs_per_step": pairs, "evaluated_pairs_per_step": evaluated,
+                       "in_cutoff_pairs_per_step": in_cutoff,
                        "processed_leaves": st["processed_leaves"],
                        "list_entries": st["list_entries"], "kernel": args.kernel,
                        "parallelism": f"replicas{world}"},

@@ -1843,6 +1843,24 @@ hsr_status hsr_autotune(hsr_ctx *ctx, int32_t iters, int32_t flush_l2, hsr_tune_
   return HSR_OK;
 }
 
+hsr_status hsr_pairs_in_cutoff(hsr_ctx *ctx, int64_t *count) {
+  if (!ctx || !count) return HSR_ERR_ARG;
+  const Work &w = ctx->work;
+  if (!ctx->have_lists || !w.device_built || ctx->last_was_batch)
+    return ctx->fail(HSR_ERR_STATE, "hsr_pairs_in_cutoff needs a single-box kick built on the device");
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  cudaStream_t s = ctx->stream;
+  CU(ctx->d_queue.ensure(64), "cudaMalloc(counter)");
+  unsigned long long *c = ctx->d_queue.as<unsigned long long>() + 4;
+  CU(cudaMemsetAsync(c, 0, sizeof(unsigned long long), s), "counter clear");
+  CU(hsr::launch_count_in_cutoff(w.table, w.leaves, w.nleaves, w.idx, w.rc2, c, s), "count kernel");
+  unsigned long long h = 0;
+  CU(cudaMemcpyAsync(&h, c, sizeof(h), cudaMemcpyDeviceToHost, s), "count copy");
+  CU(cudaStreamSynchronize(s), "count");
+  *count = int64_t(h);
+  return HSR_OK;
+}
+
 hsr_status hsr_probe_fp32_peak(hsr_ctx *ctx, double *tflops) {
   if (!ctx || !tflops) return HSR_ERR_ARG;
   CU(cudaSetDevice(ctx->device), "cudaSetDevice");

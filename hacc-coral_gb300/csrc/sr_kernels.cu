@@ -30,6 +30,47 @@ cudaError_t launch_expand_segments(const SegDesc *segs, int64_t nsegs, int32_t *
   return cudaGetLastError();
 }
 
+__global__ void __launch_bounds__(128)
+    k_count_in_cutoff(const float4 *__restrict__ pos, const LeafDesc *__restrict__ leaves,
+                      int64_t nleaves, const int32_t *__restrict__ idx, float rcut2,
+                      unsigned long long *__restrict__ count) {
+  __shared__ float4 tile[128];
+  unsigned long long c = 0;
+  for (int64_t l = blockIdx.x; l < nleaves; l += gridDim.x) {
+    const LeafDesc L = leaves[l];
+    for (int i0 = 0; i0 < L.count; i0 += blockDim.x) {
+      const int i = i0 + threadIdx.x;
+      const float4 P = pos[L.offset + (i < L.count ? i : 0)];
+      for (int t0 = 0; t0 < L.kept_len; t0 += 128) {
+        const int tn = min(128, L.kept_len - t0);
+        __syncthreads();
+        if (threadIdx.x < tn) tile[threadIdx.x] = pos[idx[L.list_begin + t0 + threadIdx.x]];
+        __syncthreads();
+        if (i < L.count)
+          for (int t = 0; t < tn; ++t) {
+            const float4 J = tile[t];
+            const float dx = __fsub_rn(J.x, P.x), dy = __fsub_rn(J.y, P.y),
+                        dz = __fsub_rn(J.z, P.z);
+            const float r2 =
+                __fadd_rn(__fadd_rn(__fmul_rn(dx, dx), __fmul_rn(dy, dy)), __fmul_rn(dz, dz));
+            c += r2 < rcut2;
+          }
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+  if ((threadIdx.x & 31) == 0 && c) atomicAdd(count, c);
+}
+
+cudaError_t launch_count_in_cutoff(const float4 *pos, const LeafDesc *leaves, int64_t nleaves,
+                                   const int32_t *idx, float rcut2, unsigned long long *count,
+                                   cudaStream_t s) {
+  if (nleaves <= 0) return cudaSuccess;
+  const int64_t blocks = nleaves < 152 * 16 ? nleaves : 152 * 16;
+  k_count_in_cutoff<<<unsigned(blocks), 128, 0, s>>>(pos, leaves, nleaves, idx, rcut2, count);
+  return cudaGetLastError();
+}
+
 LawS make_law_s(int law, float rsm2, float rcut2) {
   // a_k of the law's polynomial in r2 (float values, as the reference stores them)
   double a[7] = {0, 0, 0, 0, 0, 0, 0};

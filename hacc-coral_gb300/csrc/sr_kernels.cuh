@@ -311,6 +311,13 @@ __device__ __forceinline__ void pair_acc(float xi, float yi, float zi, const flo
 
 // Launchers (sr_kernels.cu).  All take the stream to launch on and return
 // the launch status.
+// Counts the (leaf particle, list entry) pairs with r2 < rcut2 over the
+// index lists (r2 rounded as the reference computes it, no fused
+// multiply-add), added into *count.
+cudaError_t launch_count_in_cutoff(const float4 *pos, const LeafDesc *leaves, int64_t nleaves,
+                                   const int32_t *idx, float rcut2, unsigned long long *count,
+                                   cudaStream_t s);
+
 cudaError_t launch_expand_segments(const SegDesc *segs, int64_t nsegs, int32_t *idx,
                                    cudaStream_t s);
 // threads: CTA size, i.e. threads per leaf (32, 64 or 128).

@@ -40,7 +40,7 @@ EXPORTS = ("hsr_create", "hsr_destroy", "hsr_last_error", "hsr_version", "hsr_rc
            "hsr_force_kick", "hsr_stream",
            # include/hacc_pm.h
            "hsr_pm_kick", "hsr_pm_fields", "hsr_pm_get_stats", "hsr_pm_tables",
-           "hsr_treepm_step", "hsr_pm_vjp")
+           "hsr_treepm_step", "hsr_pm_vjp", "hsr_pairs_in_cutoff")
 
 PM_F64, PM_F32 = 0, 1
 
@@ -201,6 +201,8 @@ def load(path: str = LIB_PATH):
     lib.hsr_pm_kick.restype = i32
     lib.hsr_pm_fields.argtypes = [vp, C.POINTER(HsrPmParams), i64] + [vp] * 5 + [i32]
     lib.hsr_pm_fields.restype = i32
+    lib.hsr_pairs_in_cutoff.argtypes = [vp, pi64]
+    lib.hsr_pairs_in_cutoff.restype = i32
     lib.hsr_pm_vjp.argtypes = [vp, C.POINTER(HsrPmParams), i64] + [vp] * 9 + [i32]
     lib.hsr_pm_vjp.restype = i32
     lib.hsr_pm_get_stats.argtypes = [vp, C.POINTER(HsrPmStats)]
@@ -417,6 +419,12 @@ class Context:
         self._check(self.lib.hsr_pm_vjp(self.h, C.byref(params), int(x.numel()), ptr(x), ptr(y),
                                         ptr(z), ptr(ux), ptr(uy), ptr(uz), ptr(xbx), ptr(xby),
                                         ptr(xbz), MEM_DEVICE), "hsr_pm_vjp(device arrays)")
+
+    def pairs_in_cutoff(self) -> int:
+        """hsr_pairs_in_cutoff: pairs of the last device-built kick within the cutoff."""
+        c = C.c_int64()
+        self._check(self.lib.hsr_pairs_in_cutoff(self.h, C.byref(c)), "hsr_pairs_in_cutoff")
+        return c.value
 
     def pm_stats(self) -> dict:
         s = HsrPmStats()

@@ -368,6 +368,13 @@ hsr_status hsr_bench_pairs(hsr_ctx *ctx, int32_t kernel, int32_t iters, int32_t 
 hsr_status hsr_bench_pairs_graph(hsr_ctx *ctx, int32_t iters, int32_t flush_l2,
                                  double *ms_per_launch);
 
+/* The number of (leaf particle, list entry) pairs of the last single-box kick
+ * built on the device whose distance is within the cutoff (r2 < the law's
+ * cutoff squared, r2 rounded as the reference's nbody1 computes it): the
+ * pairs that contribute, beside hsr_stats.pairs (every listed pair).
+ * HSR_ERR_STATE without such a kick. */
+hsr_status hsr_pairs_in_cutoff(hsr_ctx *ctx, int64_t *count);
+
 /* Measures this device's FP32 FMA throughput with a kernel of independent
  * fused multiply-add chains (2 flops each) on every SM; the roofline
  * denominator of the pair kernels. */

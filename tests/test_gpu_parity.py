@@ -315,3 +315,26 @@ def test_graph_replay_of_single_kick(ctx):
     p = synth.zeldovich_box(24, seed=5)
     ctx.rcb_kick(p, synth.kick_params(p, nd=64))
     assert ctx.bench_pairs_graph(3, flush_l2=True) > 0
+
+
+def test_pairs_in_cutoff_count(ctx):
+    """hsr_pairs_in_cutoff against a count over the exported lists (float32
+    r2 as the reference rounds it)."""
+    p = synth.zeldovich_box(16, z=10.0, seed=31)
+    kp = synth.kick_params(p, nd=32)
+    q = p.copy()
+    st = ctx.rcb_kick(q, kp)
+    got = ctx.pairs_in_cutoff()
+    off, cnt, ptr, e = ctx.lists()
+    fs2 = np.float32(kp.fsrrmax) * np.float32(kp.fsrrmax)
+    r2max = np.float32(3.116326355) * np.float32(3.116326355)
+    rc2 = min(fs2, np.nextafter(r2max, np.float32(np.inf)))
+    want = 0
+    for l in range(len(off)):
+        xi = np.stack([q.x, q.y, q.z], 1)[off[l]:off[l] + cnt[l]].astype(np.float32)
+        ej = e[:3, ptr[l]:ptr[l + 1]].T.astype(np.float32)
+        d = ej[None, :, :] - xi[:, None, :]
+        r2 = (d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2]
+        want += int((r2 < rc2).sum())
+    assert got == want, (got, want)
+    assert 0 < got < st["pairs"]
