@@ -11,8 +11,9 @@ the force box, fused with the velocity kick.
 * value      -- pairs/s of the device step with its inputs resident in HBM
                 (pair kernel relaunched on the resident lists, L2 flushed
                 between launches), max over ranks.
-* e2e        -- pairs/s of hsr_rcb_kick through the C ABI with host arrays:
-                tree build, lists, host<->device copies and the kernels.
+* e2e        -- pairs/s of hsr_rcb_kick through the C ABI with pinned host
+                arrays: tree build, lists, host<->device copies and the
+                kernels.
 * roofline   -- the pair kernel against the FP32 FMA peak measured by the
                 library's FFMA probe on this device: 31 flops per pair the
                 kernel evaluates.  The batched kernel skips list entries
@@ -229,6 +230,28 @@ def cpu_baseline(p, kp, slab: float, threads: int):
             "seconds": dt, "pairs": pairs}
 
 
+def pinned_copy(p):
+    """The particle set in page-locked host memory (torch's pinned allocator,
+    seen as numpy arrays)."""
+    import torch
+    arrs = []
+    for k in synth.FIELDS:
+        a = getattr(p, k)
+        t = torch.empty(a.shape, dtype=getattr(torch, str(a.dtype)) if a.dtype != np.uint16
+                        else torch.int16, pin_memory=True)
+        v = t.numpy().view(a.dtype)
+        v[...] = a
+        arrs.append(v)
+    q = synth.Particles(*arrs, nglt=p.nglt, meta=dict(p.meta))
+    q._pinned = True
+    return q
+
+
+def refill(q, p):
+    for k in synth.FIELDS:
+        np.copyto(getattr(q, k), getattr(p, k))
+
+
 def treepm_section(ctx, p0, kp, args, device: int, cpu: bool):
     """The PM kick (hsr_pm_kick) on device-resident arrays of the bench box,
     double and single precision, and one TreePM step (hsr_treepm_step: PM
@@ -364,13 +387,15 @@ def main():
                      for r in ctx.autotune(iters=3)]
     cfg["shape"] = ctx.get_tune()
 
-    # ---- end to end through the C ABI (host arrays in, host arrays out) ----
+    # ---- end to end through the C ABI (pinned host arrays in, host arrays out) ----
+    q = pinned_copy(p0)
     for _ in range(max(args.warmup, 3)):
-        ctx.rcb_kick(p0.copy(), kp, kernel=kernel)
+        refill(q, p0)
+        ctx.rcb_kick(q, kp, kernel=kernel)
     e2e_secs, st = [], None
     barrier(world)
     for _ in range(args.steps):
-        q = p0.copy()
+        refill(q, p0)  # the step's inputs, outside the timed region
         t0 = time.perf_counter()
         st = ctx.rcb_kick(q, kp, kernel=kernel)
         e2e_secs.append(time.perf_counter() - t0)
