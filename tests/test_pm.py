@@ -399,3 +399,41 @@ def test_vjp_is_linear_and_device_matches_host(ctx):
     got = np.stack([o.cpu().numpy() for o in out], 1).astype(np.float64)
     rms, _ = _err(got, a)
     assert rms < 1e-5, rms
+
+
+@pytest.mark.gpu
+def test_treepm_force_is_newtonian(ctx):
+    """The two force halves on the device compose to Newton's force: for a
+    unit source and test points at r = 0.5-10 cells, the PM field
+    (hsr_pm_fields, CIC-interpolated) plus the short-range law the pair
+    kernels evaluate (hsr_force_law: g(r^2) d, cut at fsrrmax), times 4 pi,
+    is 1 / r^2 softened by rsm, less the neutralising background.  The
+    reference built its short-range polynomial to complement its PM force
+    (force.py's f_grid), so this holds to that fit's accuracy.  (The
+    reference's list walk skips nodes on a centre-of-mass distance test, so
+    its kick can miss a pair near the cutoff; the law itself is checked here.)"""
+    ng = 64
+    rng = np.random.default_rng(12)
+    src = np.array([20.3, 31.7, 40.1])
+    radii = np.linspace(0.5, 10.0, 20)
+    r = np.repeat(radii, 24)
+    u = rng.standard_normal((r.size, 3))
+    u /= np.linalg.norm(u, axis=1)[:, None]
+    t = src + r[:, None] * u
+    prm = _params(ng, 0, 0)
+    _, grad = ctx.pm_fields(np.float32([src[0]]), np.float32([src[1]]), np.float32([src[2]]),
+                            prm)
+    pm = np.stack([P.inverse_cic(t[:, 0], t[:, 1], t[:, 2], P.exchange(grad[a], ng, 0))
+                   for a in range(3)], axis=1)
+    d = (src[None, :] - t).astype(np.float32)
+    r2 = (d[:, 0] * d[:, 0] + d[:, 1] * d[:, 1]) + d[:, 2] * d[:, 2]
+    g = ctx.force_law(r2, rsm=0.1).astype(np.float64)
+    sr = (g / (4.0 * math.pi))[:, None] * d.astype(np.float64)
+    radial = 4.0 * math.pi * np.sum((pm + sr) * d, axis=1) / r
+    expect = r / (r * r + 0.01) ** 1.5 - 4.0 * math.pi * r / (3.0 * ng ** 3)
+    for rv in radii:
+        sel = r == rv
+        rel = radial[sel].mean() / expect[sel].mean() - 1.0
+        # the fit is within 1 % near the cutoff (r ~ 3-3.5) and 0.2 % beyond 5
+        lim = 0.01 if rv < 3.0 else (0.015 if rv < 5.0 else 0.003)
+        assert abs(rel) < lim, (rv, rel)
