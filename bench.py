@@ -73,6 +73,9 @@ def parse_args():
                     help="boxes of 96^3 in the multi-box line (0: skip)")
     ap.add_argument("--adjoint-boxes", type=int, default=8,
                     help="boxes of 96^3 in the multi-step adjoint line (0: skip)")
+    ap.add_argument("--adjoint-workers", type=int, default=3,
+                    help="boxes of the multi-step run processed at once (host threads, one "
+                         "context each)")
     ap.add_argument("--clustered", type=int, default=256,
                     help="side of the clustered set of the leaf size x shape sweep (0: skip)")
     ap.add_argument("--treepm", type=int, default=1,
@@ -464,25 +467,27 @@ def main():
         rng = np.random.default_rng(5)
         cots = [[torch.from_numpy(rng.standard_normal(b.n).astype(np.float32)).cuda(local)
                  for _ in range(6)] for b in boxes]
+        workers = max(1, args.adjoint_workers)
+        msr._workers(workers)  # contexts made before the timed runs
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        for b, S in enumerate(states):
-            msr.forward_box(b, S.clone())
+        msr.forward([S.clone() for S in states], workers=workers)
         torch.cuda.synchronize()
         t_fwd = time.perf_counter() - t0
-        k0, q0 = msr.kicks, msr.pm_kicks
+        k0, q0 = msr.total_kicks()
         t0 = time.perf_counter()
-        for b, S in enumerate(states):
-            msr.adjoint_box(b, S, cots[b][:3], cots[b][3:])
+        msr.adjoint(states, [c[:3] for c in cots], [c[3:] for c in cots], workers=workers)
         torch.cuda.synchronize()
         t_adj = time.perf_counter() - t0
+        k1, q1 = msr.total_kicks()
         nsc = args.adjoint_boxes * nsteps * nsub
         multistep_line = {
             "boxes": args.adjoint_boxes, "n_side": 96, "n_particles_per_box": boxes[0].n,
             "pm_steps": nsteps, "sub_cycles": nsub, "checkpoint_every": every,
             "forward_s": t_fwd, "adjoint_s": t_adj,
             "s_per_substep_forward": t_fwd / nsc, "s_per_substep_adjoint": t_adj / nsc,
-            "kicks_in_adjoint": msr.kicks - k0, "pm_kicks_in_adjoint": msr.pm_kicks - q0,
+            "kicks_in_adjoint": k1 - k0, "pm_kicks_in_adjoint": q1 - q0,
+            "host_threads": workers,
             "note": "the whole TreePM step per PM step: PM kicks (half opening the first "
                     "step, one closing each step) around 5 short-range sub-cycles (map1, "
                     "kick, map1); adjoint through hsr_force_vjp and hsr_pm_vjp"}

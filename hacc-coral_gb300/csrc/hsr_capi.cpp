@@ -4,6 +4,7 @@
 #include "hacc_pm.h"
 
 #include <algorithm>
+#include <atomic>
 #include <chrono>
 #include <condition_variable>
 #include <deque>
@@ -99,6 +100,9 @@ float cull2(float rc2) { return rc2 * 1.0001f + 1e-6f; }
 // several items that add into the velocities with atomics.
 constexpr int64_t kJSplit = 8192;
 
+// Host threads that prepare the boxes of a multi-box kick concurrently.
+constexpr int kBatchThreads = 4;
+
 }  // namespace
 
 // One background thread that issues host<->device copies of pageable arrays
@@ -167,6 +171,15 @@ struct BoxState {
   DevBuf in, out, pos4, vel;
   int64_t n = 0;
   bool plain = false;
+  // the box's own stream: boxes of a batch are prepared concurrently
+  cudaStream_t stream = nullptr;
+  cudaEvent_t done = nullptr;
+  hsr_status status = HSR_OK;
+  std::string err;
+  ~BoxState() {
+    if (done) cudaEventDestroy(done);
+    if (stream) cudaStreamDestroy(stream);
+  }
 };
 
 // Device work of the last kick: what a pair-kernel launch reads.
@@ -1452,7 +1465,6 @@ hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *para
   CU(cudaSetDevice(ctx->device), "cudaSetDevice");
   ctx->have_lists = false;
   ctx->tape = false;
-  cudaStream_t s = ctx->stream;
   while (int32_t(ctx->boxes.size()) < nbox) ctx->boxes.emplace_back(new BoxState());
   hsr_stats st{};
   std::vector<hsr::BoxDesc> desc(static_cast<size_t>(nbox));
@@ -1460,35 +1472,55 @@ hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *para
   double build_ms = 0, lists_ms = 0;
   for (int32_t b = 0; b < nbox; ++b) {
     BoxState &B = *ctx->boxes[b];
+    if (!B.stream) CU(cudaStreamCreateWithFlags(&B.stream, cudaStreamNonBlocking), "box stream");
+    if (!B.done) CU(cudaEventCreateWithFlags(&B.done, cudaEventDisableTiming), "box event");
+    B.status = HSR_OK;
+    B.err.clear();
+  }
+  // One box: copies in, tree, lists, gathers, its descriptor; on the box's
+  // own stream, errors into the box's status (the calls run on worker
+  // threads).
+  auto prepare_box = [&](int32_t b) {
+    BoxState &B = *ctx->boxes[b];
+    cudaStream_t s = B.stream;
+    auto fail = [&](hsr_status code, const std::string &msg) {
+      B.status = code;
+      B.err = msg;
+    };
+#define BCU(call, what)                                                     \
+  do {                                                                      \
+    cudaError_t e_ = (call);                                                \
+    if (e_ != cudaSuccess) return fail(HSR_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+    BCU(cudaSetDevice(ctx->device), "cudaSetDevice");
     const hsr_params *p = &params[b];
     const int64_t n = ns[b];
     B.n = n;
     const ArrayLayout A(n);
     float *arr[8] = {x[b], y[b], z[b], vx[b], vy[b], vz[b], mass[b], phi[b]};
-    CU(B.out.ensure(A.bytes), "cudaMalloc(out)");
-    CU(B.pos4.ensure(size_t(std::max<int64_t>(n, 1)) * 16), "cudaMalloc(pos4)");
-    CU(B.vel.ensure(size_t(std::max<int64_t>(3 * n, 1)) * 4), "cudaMalloc(vel)");
+    BCU(B.out.ensure(A.bytes), "cudaMalloc(out)");
+    BCU(B.pos4.ensure(size_t(std::max<int64_t>(n, 1)) * 16), "cudaMalloc(pos4)");
+    BCU(B.vel.ensure(size_t(std::max<int64_t>(3 * n, 1)) * 4), "cudaMalloc(vel)");
     const float *in[8];
     const int64_t *in_id;
     const uint16_t *in_mask;
     if (mem == HSR_MEM_HOST) {
-      CU(B.in.ensure(A.bytes), "cudaMalloc(in)");
+      BCU(B.in.ensure(A.bytes), "cudaMalloc(in)");
       char *ib = B.in.as<char>();
       for (int i = 0; i < 8; ++i) {
-        CU(cudaMemcpyAsync(ib + A.f[i], arr[i], size_t(n) * 4, cudaMemcpyHostToDevice, s), "H2D arrays");
+        BCU(cudaMemcpyAsync(ib + A.f[i], arr[i], size_t(n) * 4, cudaMemcpyHostToDevice, s), "H2D arrays");
         in[i] = reinterpret_cast<const float *>(ib + A.f[i]);
       }
-      CU(cudaMemcpyAsync(ib + A.id, id[b], size_t(n) * 8, cudaMemcpyHostToDevice, s), "H2D ids");
-      CU(cudaMemcpyAsync(ib + A.mask, mask[b], size_t(n) * 2, cudaMemcpyHostToDevice, s), "H2D masks");
+      BCU(cudaMemcpyAsync(ib + A.id, id[b], size_t(n) * 8, cudaMemcpyHostToDevice, s), "H2D ids");
+      BCU(cudaMemcpyAsync(ib + A.mask, mask[b], size_t(n) * 2, cudaMemcpyHostToDevice, s), "H2D masks");
       in_id = reinterpret_cast<const int64_t *>(ib + A.id);
       in_mask = reinterpret_cast<const uint16_t *>(ib + A.mask);
-      st.h2d_bytes += n * 42;
     } else {
       for (int i = 0; i < 8; ++i) in[i] = arr[i];
       in_id = id[b];
       in_mask = mask[b];
     }
-    CU(hsr::launch_pack4(in[0], in[1], in[2], in[6], B.pos4.as<float4>(), n, s), "pack kernel");
+    BCU(hsr::launch_pack4(in[0], in[1], in[2], in[6], B.pos4.as<float4>(), n, s), "pack kernel");
     hsr::TreeConfig cfg{};
     for (int i = 0; i < 3; ++i) {
       cfg.min[i] = p->min[i];
@@ -1498,7 +1530,6 @@ hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *para
     }
     cfg.fsrrmax = p->fsrrmax;
     cfg.prune2 = cull2(cut2(p->law, p->fsrrmax));
-  cfg.prune2 = cull2(cut2(p->law, p->fsrrmax));
     cfg.tan_oa = std::tan(p->open_angle);
     cfg.ppc = p->ppc;
     cfg.nd = int32_t(std::min<int64_t>(p->nd, INT32_MAX));
@@ -1506,26 +1537,25 @@ hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *para
     cfg.group = ctx->tune.group;
     cudaError_t e = B.tree.build(cfg, n, B.pos4.as<float4>(), kJSplit, s);
     if (e != cudaSuccess) {
-      if (B.tree.error()) return ctx->fail(HSR_ERR_UNSUPPORTED, B.tree.error());
-      return ctx->cuda_fail(e, "device tree build");
+      if (B.tree.error()) return fail(HSR_ERR_UNSUPPORTED, B.tree.error());
+      return fail(HSR_ERR_CUDA, std::string("device tree build: ") + cudaGetErrorString(e));
     }
-    build_ms += B.tree.build_ms();
-    lists_ms += B.tree.lists_ms();
-    const hsr::DeviceTreeInfo &ti = B.tree.info();
     const int32_t *perm = B.tree.perm();
     char *ob = B.out.as<char>();
     float *dv = B.vel.as<float>();
-    CU(hsr::launch_gather_f32(in[3], perm, dv, n, s), "gather vx");
-    CU(hsr::launch_gather_f32(in[4], perm, dv + n, n, s), "gather vy");
-    CU(hsr::launch_gather_f32(in[5], perm, dv + 2 * n, n, s), "gather vz");
-    CU(hsr::launch_gather_f32(in[7], perm, reinterpret_cast<float *>(ob + A.f[7]), n, s), "gather phi");
-    CU(hsr::launch_gather_i64(in_id, perm, reinterpret_cast<int64_t *>(ob + A.id), n, s), "gather id");
-    CU(hsr::launch_gather_u16(in_mask, perm, reinterpret_cast<uint16_t *>(ob + A.mask), n, s),
-       "gather mask");
-    CU(hsr::launch_unpack4(B.tree.table(), reinterpret_cast<float *>(ob + A.f[0]),
-                           reinterpret_cast<float *>(ob + A.f[1]), reinterpret_cast<float *>(ob + A.f[2]),
-                           reinterpret_cast<float *>(ob + A.f[6]), n, s),
-       "unpack kernel");
+    BCU(hsr::launch_gather_f32(in[3], perm, dv, n, s), "gather vx");
+    BCU(hsr::launch_gather_f32(in[4], perm, dv + n, n, s), "gather vy");
+    BCU(hsr::launch_gather_f32(in[5], perm, dv + 2 * n, n, s), "gather vz");
+    BCU(hsr::launch_gather_f32(in[7], perm, reinterpret_cast<float *>(ob + A.f[7]), n, s), "gather phi");
+    BCU(hsr::launch_gather_i64(in_id, perm, reinterpret_cast<int64_t *>(ob + A.id), n, s), "gather id");
+    BCU(hsr::launch_gather_u16(in_mask, perm, reinterpret_cast<uint16_t *>(ob + A.mask), n, s),
+        "gather mask");
+    BCU(hsr::launch_unpack4(B.tree.table(), reinterpret_cast<float *>(ob + A.f[0]),
+                            reinterpret_cast<float *>(ob + A.f[1]), reinterpret_cast<float *>(ob + A.f[2]),
+                            reinterpret_cast<float *>(ob + A.f[6]), n, s),
+        "unpack kernel");
+    BCU(cudaEventRecord(B.done, s), "box event");
+#undef BCU
     hsr::BoxDesc &D = desc[b];
     D.table = B.tree.table();
     D.idx = B.tree.index();
@@ -1538,14 +1568,40 @@ hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *para
     D.rcut2 = cut2(p->law, p->fsrrmax);
     D.rcull2 = cull2(D.rcut2);
     D.law = hsr::make_law_s(p->law, D.rsm2, D.rcut2);
+  };
+  // Concurrent builds share only the pseudo-particle design table (constant
+  // memory, written with each build): boxes of one tdpts may overlap.
+  bool same_tdpts = true;
+  for (int32_t b = 1; b < nbox; ++b) same_tdpts &= params[b].tdpts == params[0].tdpts;
+  const int nthreads = same_tdpts ? int(std::min<int32_t>(nbox, kBatchThreads)) : 1;
+  if (nthreads <= 1) {
+    for (int32_t b = 0; b < nbox; ++b) prepare_box(b);
+  } else {
+    std::atomic<int32_t> next{0};
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthreads; ++t)
+      pool.emplace_back([&] {
+        for (int32_t b; (b = next.fetch_add(1)) < nbox;) prepare_box(b);
+      });
+    for (auto &t : pool) t.join();
+  }
+  for (int32_t b = 0; b < nbox; ++b) {
+    BoxState &B = *ctx->boxes[b];
+    if (B.status != HSR_OK) return ctx->fail(B.status, B.err);
+    const hsr::DeviceTreeInfo &ti = B.tree.info();
+    build_ms += B.tree.build_ms();
+    lists_ms += B.tree.lists_ms();
     total_items += ti.items;
-    st.n += n;
+    st.n += B.n;
     st.nodes += ti.nodes;
     st.processed_leaves += ti.processed_leaves;
     st.list_entries += ti.list_entries;
     st.pairs += ti.pairs;
     st.cm_fallbacks += ti.cm_fallbacks;
+    if (mem == HSR_MEM_HOST) st.h2d_bytes += B.n * 42;
+    CU(cudaStreamWaitEvent(ctx->stream, B.done, 0), "wait for box");
   }
+  cudaStream_t s = ctx->stream;
   // all boxes' items, tagged with their box, in one persistent launch
   CU(ctx->d_box_items.ensure(size_t(std::max<int64_t>(total_items, 1)) * sizeof(hsr::PairItem)),
      "cudaMalloc(items)");

@@ -253,6 +253,7 @@ class Context:
 
     def __init__(self, device: int = 0):
         self.lib = load()
+        self.device = device
         h = C.c_void_p()
         st = self.lib.hsr_create(C.byref(h), device)
         if st != HSR_OK:

@@ -246,12 +246,57 @@ class MultiStep:
             self._reverse_segment(b, s0, s1, xk, S0.mass, xb, vb, scratch)
         return xb, vb
 
-    def forward(self, states: Sequence[BoxState]) -> List[BoxState]:
-        return [self.forward_box(b, S) for b, S in enumerate(states)]
+    # ---- several boxes ---------------------------------------------------
+    def _workers(self, n: int) -> List["MultiStep"]:
+        """This driver and n - 1 peers, each on its own context (CUDA stream
+        and buffers) of the same device."""
+        peers = self.__dict__.setdefault("_peers", [])
+        while len(peers) < n - 1:
+            m = MultiStep(hsr.Context(self.ctx.device), self.kps, self.steps, self.nsub,
+                          self.every, self.pm)
+            m.on_tape = self.on_tape
+            peers.append(m)
+        return [self] + peers[:max(0, n - 1)]
 
-    def adjoint(self, states: Sequence[BoxState], xbars, vbars):
-        return [self.adjoint_box(b, S, xb, vb)
-                for b, (S, xb, vb) in enumerate(zip(states, xbars, vbars))]
+    def _map(self, fn, nbox: int, workers: int):
+        ws = self._workers(workers)
+        if len(ws) == 1:
+            return [fn(self, b) for b in range(nbox)]
+        # one box per host thread at a time: a box's host-side waits (the
+        # tree build's per-level synchronisation) overlap another box's
+        # kernels; the library releases the interpreter lock in its calls
+        import threading
+        from concurrent.futures import ThreadPoolExecutor
+        lock = threading.Lock()
+        free = list(ws)
+
+        def job(b):
+            with lock:
+                w = free.pop()
+            try:
+                return fn(w, b)
+            finally:
+                with lock:
+                    free.append(w)
+        with ThreadPoolExecutor(len(ws)) as ex:
+            return list(ex.map(job, range(nbox)))
+
+    def total_kicks(self) -> Tuple[int, int]:
+        """(short-range kicks, PM kicks) run by this driver and its peers."""
+        ws = [self] + self.__dict__.get("_peers", [])
+        return sum(w.kicks for w in ws), sum(w.pm_kicks for w in ws)
+
+    def forward(self, states: Sequence[BoxState], workers: int = 1) -> List[BoxState]:
+        """forward_box over every box; workers > 1 runs that many boxes at
+        once, each on its own context."""
+        _torch_done()
+        return self._map(lambda w, b: w.forward_box(b, states[b]), len(states), workers)
+
+    def adjoint(self, states: Sequence[BoxState], xbars, vbars, workers: int = 1):
+        """adjoint_box over every box (workers as forward)."""
+        _torch_done()
+        return self._map(lambda w, b: w.adjoint_box(b, states[b], xbars[b], vbars[b]),
+                         len(states), workers)
 
 
 def kicks_per_box(nsteps: int, nsub: int, checkpointed: bool = True) -> int:

@@ -350,3 +350,33 @@ def test_multistep_with_pm_adjoint_vs_fp64_and_fd(ctx, oracle_lib):
     rms, mx = force_errors(gx[smp], fx[smp])
     assert rms <= ADJ_TOL, rms
     assert ms.pm_kicks == 3 * (nsteps + 1)  # forward, recomputation, stored run
+
+
+@pytest.mark.gpu
+def test_boxes_on_two_host_threads_match_one(ctx):
+    """Several boxes processed two at a time (two host threads, a context
+    each) give the adjoint of the one-at-a-time run."""
+    torch = pytest.importorskip("torch")
+    nsteps, nsub = 2, 2
+    steps = multistep.schedule(50.0, 40.0, nsteps, nsub)
+    boxes = _boxes(3, 12, 150)
+    kps = [synth.kick_params(b, nd=64) for b in boxes]
+    pm = multistep.pm_schedule(50.0, 40.0, nsteps, 12, boxes[0].meta["ngo"])
+    ms = multistep.MultiStep(ctx, kps, steps, nsub, checkpoint_every=1, pm=pm)
+    states = [multistep.box_state(b) for b in boxes]
+    rng = np.random.default_rng(6)
+    cot = [[torch.from_numpy(rng.standard_normal(b.n).astype(np.float32)).cuda()
+            for _ in range(6)] for b in boxes]
+    one = ms.adjoint(states, [c[:3] for c in cot], [c[3:] for c in cot], workers=1)
+    two = ms.adjoint(states, [c[:3] for c in cot], [c[3:] for c in cot], workers=2)
+    for (ax, av), (bx, bv) in zip(one, two):
+        for u, w in zip(ax + av, bx + bv):
+            rms, _ = force_errors(u.double().cpu().numpy()[:, None], w.double().cpu().numpy()[:, None])
+            assert rms <= 1e-5, rms
+    fwd1 = ms.forward([S.clone() for S in states], workers=1)
+    fwd2 = ms.forward([S.clone() for S in states], workers=2)
+    for a, b in zip(fwd1, fwd2):
+        for u, w in zip(a.x + a.v, b.x + b.v):
+            assert torch.allclose(u, w, rtol=0, atol=1e-4)
+    k, q = ms.total_kicks()
+    assert k > 0 and q > 0
