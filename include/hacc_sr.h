@@ -153,9 +153,10 @@ hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, 
 
 hsr_status hsr_get_stats(const hsr_ctx *ctx, hsr_stats *st);
 
-/* Several independent boxes in one call (BASELINE's multi-box batching; no
+/* Several independent boxes in one call (multi-box batching; no
  * counterpart in the reference, which kicks one rank's box per constructor):
- * every box's tree and lists are built on the device, then ONE persistent
+ * every box's tree and lists are built on the device (up to four boxes at
+ * once, each on its own stream and host thread), then ONE persistent
  * launch of the batched kernel evaluates the work items of all boxes, each
  * with its own parameters (fcoeff, rsm, cutoff; one force law for all).  The
  * per-box arrays are given as arrays of nbox pointers; each box's arrays are
