@@ -115,6 +115,21 @@ def step(ctx: hsr.Context, p: synth.Particles, T: HsrTreePMParams) -> dict:
     return {"sr": ctx.stats(), "pm": ctx.pm_stats(), "n_inbox": nin.value}
 
 
+def step_device(ctx: hsr.Context, t: dict, n: int, T: HsrTreePMParams) -> dict:
+    """hsr_treepm_step on device arrays: `t` maps the ten field names to CUDA
+    tensors (float32 x..phi, int64 id, int16/uint16 mask), modified in place."""
+    lib = _lib()
+    nin = C.c_int64()
+    fp = lambda k: C.cast(C.c_void_p(t[k].data_ptr()), C.POINTER(C.c_float))
+    st = lib.hsr_treepm_step(ctx.h, C.byref(T), n,
+                             *[fp(k) for k in ("x", "y", "z", "vx", "vy", "vz", "mass", "phi")],
+                             C.cast(C.c_void_p(t["id"].data_ptr()), C.POINTER(C.c_int64)),
+                             C.cast(C.c_void_p(t["mask"].data_ptr()), C.POINTER(C.c_uint16)),
+                             hsr.MEM_DEVICE, C.byref(nin))
+    ctx._check(st, "hsr_treepm_step(device arrays)")
+    return {"sr": ctx.stats(), "pm": ctx.pm_stats(), "n_inbox": nin.value}
+
+
 def run(ctx: hsr.Context, p: synth.Particles, z_in: float, z_fin: float, nsteps: int, nsub: int,
         kp: synth.KickParams, precision: int = hsr.PM_F64) -> List[dict]:
     """The whole loop on `p` (in place); per-step statistics."""

@@ -437,3 +437,56 @@ def test_treepm_force_is_newtonian(ctx):
         # the fit is within 1 % near the cutoff (r ~ 3-3.5) and 0.2 % beyond 5
         lim = 0.01 if rv < 3.0 else (0.015 if rv < 5.0 else 0.003)
         assert abs(rel) < lim, (rv, rel)
+
+
+def test_restatement_float32_and_float64_paths_agree():
+    """pm_kick (the reference's float32 CIC weights and grids) and force64
+    (float64 throughout) describe the same kick."""
+    p = _box(8, seed=7)
+    ng, ngo = 8, p.meta["ngo"]
+    z = [np.zeros(p.n, np.float32)] * 3
+    dv32 = np.stack(P.pm_kick(p.x, p.y, p.z, *z, ng, ngo, 1.2, 1.0, 1.0), 1).astype(np.float64)
+    f64 = P.force64(p.x.astype(np.float64), p.y.astype(np.float64), p.z.astype(np.float64), ng,
+                    ngo, float(np.float32(1.2)))
+    rms, mx = _err(dv32, f64)
+    assert rms < 1e-6 and mx < 1e-5, (rms, mx)
+
+
+@pytest.mark.gpu
+def test_treepm_step_device_arrays_match_host(ctx):
+    import torch
+    import treepm
+    p0 = synth.zeldovich_box(16, z=50.0, seed=37)
+    p0.id[:] = np.arange(p0.n)
+    kp = synth.kick_params(p0, nd=64, nsub=3)
+    T = treepm.step_params(treepm.plan(50.0, 45.0, 1)[0], kp, 3, 16, p0.meta["ngo"], p0.nglt)
+    p = p0.copy()
+    treepm.step(ctx, p, T)
+    dev = torch.device("cuda", 0)
+    t = {k: torch.from_numpy(np.ascontiguousarray(getattr(p0, k) if k != "mask"
+                                                  else p0.mask.view(np.int16))).to(dev)
+         for k in synth.FIELDS}
+    torch.cuda.synchronize()
+    treepm.step_device(ctx, t, p0.n, T)
+    q = {k: t[k].cpu().numpy() for k in synth.FIELDS}
+    a, b = np.argsort(p.id), np.argsort(q["id"])
+    for k in ("x", "y", "z"):
+        assert np.abs(getattr(p, k)[a] - q[k][b]).max() < 1e-5, k
+    for k in ("vx", "vy", "vz"):
+        ref = getattr(p, k)[a].astype(np.float64) - getattr(p0, k)[np.argsort(p0.id)]
+        got = q[k][b].astype(np.float64) - getattr(p0, k)[np.argsort(p0.id)]
+        rms, _ = _err(got, ref)
+        assert rms < 1e-5, (k, rms)
+
+
+@pytest.mark.gpu
+def test_smallest_grid_and_widest_overload(ctx):
+    """ng = 2 with ngo = 1 (the widest overload a grid of two cells allows)
+    against the restatement."""
+    rng = np.random.default_rng(9)
+    x, y, z = (rng.random(200).astype(np.float32) * 5.0 - 0.5 for _ in range(3))
+    prm = _params(2, 1, 0)
+    rho, grad = ctx.pm_fields(x, y, z, prm)
+    rho_o, grad_o = P.fields(x, y, z, 2, 1)
+    np.testing.assert_allclose(rho, rho_o, rtol=1e-5, atol=1e-5)
+    np.testing.assert_allclose(grad, grad_o, rtol=1e-4, atol=1e-6)
