@@ -14,6 +14,9 @@ the force box, fused with the velocity kick.
 * e2e        -- pairs/s of hsr_rcb_kick through the C ABI with pinned host
                 arrays: tree build, lists, host<->device copies and the
                 kernels.
+* roofline_hbm -- the same kernel's profiled DRAM bytes per launch over its
+                time against the measured HBM copy bandwidth (a few percent:
+                the kernel is compute-bound).
 * roofline   -- the pair kernel against the FP32 FMA peak measured by the
                 library's FFMA probe on this device: 31 flops per pair the
                 kernel evaluates.  The batched kernel skips list entries
@@ -231,6 +234,23 @@ def cpu_baseline(p, kp, slab: float, threads: int):
                        f"({pairs:.3e} pairs, full tree built), {dt:.2f} s wall, "
                        f"OpenMP nesting capped at {OMP_LEVELS} level"),
             "seconds": dt, "pairs": pairs}
+
+
+def hbm_roofline(traffic, ms):
+    """The pair kernel against the measured HBM copy bandwidth (the file the
+    pool writes at the repository root), from the profiled DRAM bytes per
+    launch: how far the kernel is from being memory-bound."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            peak = float(json.load(f)["hbm_gbs"])
+        src = "measured (MEASURED_PEAKS.json hbm_gbs)"
+    except (OSError, KeyError, ValueError):
+        peak, src = 6800.0, "fallback (6.8 TB/s)"
+    if not traffic:
+        return None
+    achieved = traffic / (ms * 1e-3) / 1e9
+    return {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "traffic": traffic, "peak_source": src}
 
 
 def pinned_copy(p):
@@ -555,6 +575,7 @@ def main():
                          "peak_source": "FFMA-chain probe on this device (hsr_probe_fp32_peak)",
                          "flops_per_pair": FLOPS_PER_PAIR,
                          "pairs_basis": "evaluated pairs (after the box test)"},
+            "roofline_hbm": hbm_roofline(profiled_traffic(cfg["workload"], cfg["shape"]), ms),
             "cpu_baseline": cpu,
             "e2e": {"value": world * pairs * args.steps / e2e_t, "unit": UNIT,
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
