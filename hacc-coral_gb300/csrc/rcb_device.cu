@@ -46,7 +46,11 @@ constexpr int kWalkStack = 256;     // DFS stack of the list walk
 
 enum { C_NCHUNK = 0, C_NSPLIT = 1, C_NFALLBACK = 2, C_NLEAF = 3, C_NSEG = 4, C_NENT = 5,
        C_PAIRS = 6, C_PADDED = 7, C_NITEMS = 8, C_MAXLEN = 9, C_TDONE1 = 10, C_TDONE2 = 11,
-       C_NTIGHT = 12, C_BUCKET = 16, C_FILL = 48, C_COUNT = 80 };
+       C_NTIGHT = 12, C_SEGOVF = 13, C_BUCKET = 16, C_FILL = 48, C_COUNT = 80 };
+
+// Segments a leaf's walk can leave in its own region of the one-pass walk;
+// a leaf with more sends the build to the counting walk and a second pass.
+constexpr int kLocalSegs = 64;
 
 __device__ __forceinline__ double warp_sum(double v) {
 #pragma unroll
@@ -1272,11 +1276,16 @@ __global__ void k_leaf_compact(const int64_t *leaf_at, const int64_t *pos_of, in
 // Interaction lists (calcInternodeForce, RCBForceTree.cxx:923-1144), one
 // thread per processed leaf; a counting pass and a writing pass.
 // ---------------------------------------------------------------------------
-template <bool WRITE>
+// MODE 0: counts (segments and entries per leaf); 1: writes the segments at
+// seg_base / list_base; 2: counts and writes the first kLocalSegs segments
+// of each leaf into its own region (dst relative to the leaf's list),
+// flagging leaves with more in counters[C_SEGOVF].
+template <int MODE>
 __global__ void k_walk(const DNode *__restrict__ nodes, int32_t nnodes, const int32_t *leaf_ids,
                        int64_t nleaves, TreeConfig cfg, int64_t n, int64_t *seg_cnt, int64_t *list_len,
                        const int64_t *seg_base, const int64_t *list_base, SegDesc *segs,
-                       int32_t *err) {
+                       int32_t *err, int64_t *counters) {
+  constexpr bool WRITE = MODE == 1;
   const int64_t li = int64_t(blockIdx.x) * blockDim.x + threadIdx.x;
   if (li >= nleaves) return;
   const int32_t tl = leaf_ids[li];
@@ -1292,6 +1301,8 @@ __global__ void k_walk(const DNode *__restrict__ nodes, int32_t nnodes, const in
   auto emit = [&](int64_t start, int64_t count) {
     if (count <= 0) return;
     if (WRITE) segs[sb + nseg] = SegDesc{int32_t(start), int32_t(count), lb + len};
+    if (MODE == 2 && nseg < kLocalSegs)
+      segs[li * kLocalSegs + nseg] = SegDesc{int32_t(start), int32_t(count), len};
     ++nseg;
     len += count;
   };
@@ -1365,6 +1376,25 @@ __global__ void k_walk(const DNode *__restrict__ nodes, int32_t nnodes, const in
   if (!WRITE) {
     seg_cnt[li] = nseg;
     list_len[li] = len;
+  }
+  if (MODE == 2 && nseg > kLocalSegs) atomicExch((unsigned long long *)&counters[C_SEGOVF], 1ull);
+}
+
+// The one-pass walk's per-leaf regions packed leaf after leaf, with each
+// segment's destination made absolute.
+__global__ void k_pack_segs(const SegDesc *__restrict__ local, const int64_t *seg_cnt,
+                            const int64_t *seg_base, const int64_t *list_base, int64_t nleaves,
+                            SegDesc *__restrict__ segs) {
+  const int lane = threadIdx.x & 31;
+  const int64_t warps = (int64_t(gridDim.x) * blockDim.x) >> 5;
+  for (int64_t li = (int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5; li < nleaves;
+       li += warps) {
+    const int64_t c = seg_cnt[li], sb = seg_base[li], lb = list_base[li];
+    for (int64_t q = lane; q < c; q += 32) {
+      SegDesc d = local[li * kLocalSegs + q];
+      d.dst += lb;
+      segs[sb + q] = d;
+    }
   }
 }
 
@@ -1889,7 +1919,7 @@ DeviceTree::~DeviceTree() {
   void *ptrs[] = {epos_, tpos_, oid_, toid_, idx_, nodes_, ppm_, chunk_node_, chunk_base_, part_,
                   left_cnt_, left_base_, scan_tmp_, node_tmp_, fallback_, counters_, leaf_ids_,
                   leaf_tmp_, leafdesc_, segs_, idx_list_, table_, items_, items_tmp_, gidx_,
-                  walk_err_, tight_chunks_, tight_nodes_};
+                  walk_err_, tight_chunks_, tight_nodes_, segs_local_};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h_counters_) cudaFreeHost(h_counters_);
@@ -2088,14 +2118,22 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   int64_t *seg_cnt = node_tmp_, *list_len = node_tmp_ + nlw, *seg_base = node_tmp_ + 2 * nlw,
           *list_base = node_tmp_ + 3 * nlw;
   DT_CHECK(grow(scan_tmp_, cap_scan_, size_t(scan_tmp_size(int64_t(nlw))), s));
+  // one pass writing each leaf's segments into its own region; the scans
+  // then place them (a leaf with more than kLocalSegs segments sends the
+  // build to a second, placing walk)
+  DT_CHECK(grow(segs_local_, cap_segl_, nlw * kLocalSegs, s));
+  DT_CHECK(cudaMemsetAsync(counters_ + C_SEGOVF, 0, sizeof(int64_t), s));
   if (nleaves > 0) {
-    k_walk<false><<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(
-        nodes_, nnodes, leaf_ids_, nleaves, cfg, n, seg_cnt, list_len, nullptr, nullptr, nullptr, walk_err_);
+    k_walk<2><<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(
+        nodes_, nnodes, leaf_ids_, nleaves, cfg, n, seg_cnt, list_len, nullptr, nullptr,
+        segs_local_, walk_err_, counters_);
     DT_CHECK(exclusive_scan_i64(seg_cnt, seg_base, nleaves, counters_ + C_NSEG, scan_tmp_, s));
     DT_CHECK(exclusive_scan_i64(list_len, list_base, nleaves, counters_ + C_NENT, scan_tmp_, s));
   }
   DT_CHECK(cudaGetLastError());
   DT_CHECK(cudaMemcpyAsync(h_counters_ + C_NSEG, counters_ + C_NSEG, 2 * sizeof(int64_t),
+                           cudaMemcpyDeviceToHost, s));
+  DT_CHECK(cudaMemcpyAsync(h_counters_ + C_SEGOVF, counters_ + C_SEGOVF, sizeof(int64_t),
                            cudaMemcpyDeviceToHost, s));
   int32_t h_err = 0;
   DT_CHECK(cudaMemcpyAsync(&h_err, walk_err_, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
@@ -2113,8 +2151,13 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   DT_CHECK(grow(idx_list_, cap_idx_, size_t(std::max<int64_t>(nent, 1)), s));
   DT_CHECK(grow(leafdesc_, cap_ld_, nlw, s));
   if (nleaves > 0) {
-    k_walk<true><<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(
-        nodes_, nnodes, leaf_ids_, nleaves, cfg, n, nullptr, nullptr, seg_base, list_base, segs_, walk_err_);
+    if (h_counters_[C_SEGOVF])
+      k_walk<1><<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(
+          nodes_, nnodes, leaf_ids_, nleaves, cfg, n, nullptr, nullptr, seg_base, list_base, segs_,
+          walk_err_, counters_);
+    else
+      k_pack_segs<<<unsigned(std::min<int64_t>((nleaves + 7) / 8, 152 * 64)), 256, 0, s>>>(
+          segs_local_, seg_cnt, seg_base, list_base, nleaves, segs_);
     int64_t *kept = nullptr;
     if (cfg.prune2 > 0.0f) {
       kept = node_tmp_ + 4 * nlw;

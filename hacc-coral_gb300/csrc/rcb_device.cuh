@@ -148,6 +148,8 @@ class DeviceTree {
   size_t cap_ld_ = 0;
   SegDesc *segs_ = nullptr;
   size_t cap_seg_ = 0;
+  SegDesc *segs_local_ = nullptr;  // the one-pass walk's per-leaf regions
+  size_t cap_segl_ = 0;
   int32_t *idx_list_ = nullptr;
   size_t cap_idx_ = 0;
   float4 *table_ = nullptr;
