@@ -76,7 +76,7 @@ constexpr int kScanPer = 4;
 constexpr int64_t kScanBlock = kScanThreads * kScanPer;
 
 __global__ void __launch_bounds__(kScanThreads)
-    k_scan_block(const int64_t *in, int64_t *out, int64_t n, int64_t *bsum) {
+    k_scan_block(const int64_t *in, int64_t *out, int64_t n, int64_t *bsum, int64_t *total) {
   __shared__ int64_t wsum[32];
   const int64_t base = int64_t(blockIdx.x) * kScanBlock + int64_t(threadIdx.x) * kScanPer;
   int64_t v[kScanPer];
@@ -112,7 +112,10 @@ __global__ void __launch_bounds__(kScanThreads)
     if (base + k < n) out[base + k] = run;
     run += v[k];
   }
-  if (threadIdx.x == kScanThreads - 1) bsum[blockIdx.x] = run;
+  if (threadIdx.x == kScanThreads - 1) {
+    bsum[blockIdx.x] = run;
+    if (total) *total = run;  // single-block scans only (the caller passes it then)
+  }
 }
 
 __global__ void k_scan_add(int64_t *out, int64_t n, const int64_t *boff) {
@@ -120,7 +123,6 @@ __global__ void k_scan_add(int64_t *out, int64_t n, const int64_t *boff) {
   if (i < n) out[i] += boff[i / kScanBlock];
 }
 
-__global__ void k_copy_total(const int64_t *src, int64_t *dst) { *dst = *src; }
 
 }  // namespace
 
@@ -136,11 +138,8 @@ cudaError_t exclusive_scan_i64(const int64_t *in, int64_t *out, int64_t n, int64
     return cudaSuccess;
   }
   const int64_t nb = (n + kScanBlock - 1) / kScanBlock;
-  k_scan_block<<<unsigned(nb), kScanThreads, 0, s>>>(in, out, n, tmp);
-  if (nb == 1) {
-    if (total) k_copy_total<<<1, 1, 0, s>>>(tmp, total);
-    return cudaGetLastError();
-  }
+  k_scan_block<<<unsigned(nb), kScanThreads, 0, s>>>(in, out, n, tmp, nb == 1 ? total : nullptr);
+  if (nb == 1) return cudaGetLastError();
   // scan the block sums in place, then add them
   cudaError_t e = exclusive_scan_i64(tmp, tmp, nb, total, tmp + nb + 1, s);
   if (e != cudaSuccess) return e;
@@ -166,6 +165,106 @@ __global__ void k_chunk_fill(const DNode *nodes, int32_t nb, int32_t ne, const i
   if (nb + i >= ne) return;
   const int64_t c = (int64_t(nodes[nb + i].count) + kChunk - 1) / kChunk;
   for (int64_t k = 0; k < c; ++k) chunk_node[base[i] + k] = nb + i;
+}
+
+// Exclusive scan over one block of kScanThreads threads, kScanPer values each
+// (v in, out out); returns the block total to every thread.
+__device__ __forceinline__ int64_t block_exclusive_scan(const int64_t (&v)[kScanPer],
+                                                        int64_t (&out)[kScanPer]) {
+  __shared__ int64_t wsum[32];
+  int64_t t = 0;
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) t += v[k];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int64_t x = t;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) wsum[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int64_t w = wsum[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += y;
+    }
+    wsum[lane] = w;
+  }
+  __syncthreads();
+  int64_t run = x - t + (warp > 0 ? wsum[warp - 1] : 0);
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    out[k] = run;
+    run += v[k];
+  }
+  return wsum[31];
+}
+
+// Levels of at most kScanBlock nodes, in one block: the chunks of every node
+// (k_chunk_counts, the scan and k_chunk_fill), the total into *nchunk.
+__global__ void __launch_bounds__(kScanThreads)
+    k_chunk_setup_small(const DNode *nodes, int32_t nb, int32_t ne, int64_t *base,
+                        int32_t *chunk_node, int64_t *nchunk) {
+  int64_t c[kScanPer], b[kScanPer];
+  const int32_t i0 = int32_t(threadIdx.x) * kScanPer;
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k)
+    c[k] = nb + i0 + k < ne ? (int64_t(nodes[nb + i0 + k].count) + kChunk - 1) / kChunk : 0;
+  const int64_t total = block_exclusive_scan(c, b);
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    if (nb + i0 + k >= ne) break;
+    base[i0 + k] = b[k];
+    for (int64_t q = 0; q < c[k]; ++q) chunk_node[b[k] + q] = nb + i0 + k;
+  }
+  if (threadIdx.x == 0) *nchunk = total;
+}
+
+// Levels of at most kScanBlock nodes, in one block: k_split_flags, the scan
+// and k_children; the number of split nodes into *nsplit.
+__global__ void __launch_bounds__(kScanThreads)
+    k_children_small(DNode *nodes, int32_t nb, int32_t ne, int64_t *nsplit) {
+  int64_t f[kScanPer], r[kScanPer];
+  const int32_t i0 = int32_t(threadIdx.x) * kScanPer;
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    f[k] = 0;
+    if (nb + i0 + k < ne) {
+      const DNode &N = nodes[nb + i0 + k];
+      f[k] = (N.split_dim >= 0 && N.nleft > 0 && N.nleft < N.count) ? 1 : 0;
+    }
+  }
+  const int64_t total = block_exclusive_scan(f, r);
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    if (nb + i0 + k >= ne) break;
+    DNode &N = nodes[nb + i0 + k];
+    if (!f[k]) {
+      N.cl = N.cr = 0;
+      continue;
+    }
+    const int32_t cl = ne + 2 * int32_t(r[k]), cr = cl + 1;
+    N.cl = cl;
+    N.cr = cr;
+    for (int s = 0; s < 2; ++s) {
+      DNode &C = nodes[s == 0 ? cl : cr];
+      C.count = s == 0 ? N.nleft : N.count - N.nleft;
+      C.offset = s == 0 ? N.offset : N.offset + N.nleft;
+      C.cl = C.cr = 0;
+      for (int d = 0; d < 3; ++d) {
+        C.xmin[d] = N.xmin[d];
+        C.xmax[d] = N.xmax[d];
+        C.xc[d] = 0.f;
+      }
+      C.tdr = 0.f;
+      C.split_dim = -1;
+      C.nleft = 0;
+    }
+  }
+  if (threadIdx.x == 0) *nsplit = total;
 }
 
 struct ChunkRange {
@@ -2013,9 +2112,15 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     DT_CHECK(cudaMemsetAsync(counters_ + C_NTIGHT, 0, sizeof(int64_t), s));
 
     const unsigned gL = unsigned((L + 127) / 128);
-    k_chunk_counts<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
-    DT_CHECK(exclusive_scan_i64(node_tmp_, chunk_base_, L, counters_ + C_NCHUNK, scan_tmp_, s));
-    k_chunk_fill<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, chunk_node_);
+    const bool small = int64_t(L) <= kScanBlock;
+    if (small) {
+      k_chunk_setup_small<<<1, kScanThreads, 0, s>>>(nodes_, nb, ne, chunk_base_, chunk_node_,
+                                                     counters_ + C_NCHUNK);
+    } else {
+      k_chunk_counts<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
+      DT_CHECK(exclusive_scan_i64(node_tmp_, chunk_base_, L, counters_ + C_NCHUNK, scan_tmp_, s));
+      k_chunk_fill<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, chunk_node_);
+    }
     // deep levels (nodes of ~2048 elements or fewer on average): a warp per chunk
     const bool wm = int64_t(L) * 2048 >= n;
     const unsigned gC = wm ? unsigned((max_chunks + 7) / 8) : unsigned(max_chunks);
@@ -2053,9 +2158,13 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     std::swap(cap_e_, cap_t_);
     std::swap(oid_, toid_);
     std::swap(cap_o_, cap_to_);
-    k_split_flags<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
-    DT_CHECK(exclusive_scan_i64(node_tmp_, node_tmp_, L, counters_ + C_NSPLIT, scan_tmp_, s));
-    k_children<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
+    if (small) {
+      k_children_small<<<1, kScanThreads, 0, s>>>(nodes_, nb, ne, counters_ + C_NSPLIT);
+    } else {
+      k_split_flags<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
+      DT_CHECK(exclusive_scan_i64(node_tmp_, node_tmp_, L, counters_ + C_NSPLIT, scan_tmp_, s));
+      k_children<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
+    }
     DT_CHECK(cudaGetLastError());
     DT_CHECK(cudaMemcpyAsync(h_counters_, counters_, (C_NTIGHT + 1) * sizeof(int64_t),
                              cudaMemcpyDeviceToHost, s));
