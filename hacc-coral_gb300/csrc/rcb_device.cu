@@ -514,10 +514,20 @@ __device__ bool certify(double sx, double bx, double sm, double bm, float *out) 
 // reduced sums; lists it for the tight certification otherwise.
 __device__ void finish_node(DNode &N, int32_t node, const __int128 *s, double *a, const float *lo,
                             const float *hi, const int *emin, bool ovf, int32_t *fallback,
-                            int64_t *counters, int32_t force_fallback) {
+                            int64_t *counters, int32_t force_fallback, int32_t nd) {
   for (int d = 0; d < 3; ++d) {
     N.xmin[d] = lo[d];
     N.xmax[d] = hi[d];
+  }
+  // leaf by size, or the split axis: the longest box edge, ties to the later
+  // axis (RCBForceTree.cxx:837-852); it needs the box only, not the centre
+  N.nleft = 0;
+  if (N.count <= nd) {
+    N.split_dim = -1;
+  } else {
+    const float l0 = fsub_(N.xmax[0], N.xmin[0]), l1 = fsub_(N.xmax[1], N.xmin[1]),
+                l2 = fsub_(N.xmax[2], N.xmin[2]);
+    N.split_dim = (l0 > l1 && l0 > l2) ? 0 : (l1 > l2 ? 1 : 2);
   }
   // Sums of |terms|: float partials rounded up, added in double; the factor
   // covers the double additions' rounding.
@@ -582,14 +592,14 @@ __device__ __forceinline__ void read_part(const double *p, __int128 *s, double *
 // finish the node.
 __global__ void k_stats_final(DNode *nodes, int32_t nb, int32_t ne, const int64_t *chunk_base,
                               const double *part, int32_t *fallback, int64_t *counters,
-                              int32_t force_fallback) {
+                              int32_t force_fallback, int32_t nd, bool all) {
   const int32_t wid = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   const int lane = threadIdx.x & 31;
   const int32_t node = nb + wid;
   if (node >= ne) return;
   DNode &N = nodes[node];
   const int64_t nc = (int64_t(N.count) + kChunk - 1) / kChunk;
-  if (nc <= 1) return;  // k_stats_final_one
+  if (N.count <= 0 || (nc <= 1 && !all)) return;  // k_stats_final_one (unless `all`)
   const int64_t cb = chunk_base[wid];
   __int128 s[4] = {0, 0, 0, 0};
   double a[4] = {0, 0, 0, 0};
@@ -609,14 +619,14 @@ __global__ void k_stats_final(DNode *nodes, int32_t nb, int32_t ne, const int64_
     for (int o = 16; o > 0; o >>= 1) emin[q] = min(emin[q], __shfl_xor_sync(0xffffffffu, emin[q], o));
   ovf = __any_sync(0xffffffffu, ovf != 0);
   if (lane != 0) return;
-  finish_node(N, node, s, a, lo, hi, emin, ovf != 0, fallback, counters, force_fallback);
+  finish_node(N, node, s, a, lo, hi, emin, ovf != 0, fallback, counters, force_fallback, nd);
 }
 
 // One thread per node of a single chunk (most nodes of the deep levels): the
 // per-node arithmetic, much of it FP64, then fills whole warps.
 __global__ void k_stats_final_one(DNode *nodes, int32_t nb, int32_t ne, const int64_t *chunk_base,
                                   const double *part, int32_t *fallback, int64_t *counters,
-                                  int32_t force_fallback) {
+                                  int32_t force_fallback, int32_t nd) {
   const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   const int32_t node = nb + i;
   if (node >= ne) return;
@@ -628,7 +638,7 @@ __global__ void k_stats_final_one(DNode *nodes, int32_t nb, int32_t ne, const in
   int emin[4] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX};
   int ovf = 0;
   read_part(part + chunk_base[i] * kPartWords, s, a, lo, hi, emin, ovf);
-  finish_node(N, node, s, a, lo, hi, emin, ovf != 0, fallback, counters, force_fallback);
+  finish_node(N, node, s, a, lo, hi, emin, ovf != 0, fallback, counters, force_fallback, nd);
 }
 
 // ---------------------------------------------------------------------------
@@ -934,22 +944,6 @@ __global__ void k_cm_fallback(const float4 *__restrict__ pos, DNode *nodes, cons
   }
 }
 
-// Leaf by size, or the split axis: the longest box edge, ties to the later
-// axis (RCBForceTree.cxx:837-852).
-__global__ void k_split_decide(DNode *nodes, int32_t nb, int32_t ne, int32_t nd) {
-  const int32_t i = nb + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= ne) return;
-  DNode &N = nodes[i];
-  N.nleft = 0;
-  if (N.count <= nd) {
-    N.split_dim = -1;
-    return;
-  }
-  const float l0 = fsub_(N.xmax[0], N.xmin[0]), l1 = fsub_(N.xmax[1], N.xmin[1]),
-              l2 = fsub_(N.xmax[2], N.xmin[2]);
-  N.split_dim = (l0 > l1 && l0 > l2) ? 0 : (l1 > l2 ? 1 : 2);
-}
-
 __device__ __forceinline__ float key_of(const float4 &p, int d) {
   return d == 0 ? p.x : (d == 1 ? p.y : p.z);
 }
@@ -1041,7 +1035,14 @@ __global__ void __launch_bounds__(kChunkThreads)
   CHUNK_PROLOGUE
   const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
   const DNode &N = nodes[R.node];
-  if (N.split_dim < 0) return;
+  if (N.split_dim < 0) {
+    // a leaf keeps its elements: copied once into the next level's buffer
+    for (int k = tid; k < R.len; k += NT) {
+      tpos[R.begin + k] = pos[R.begin + k];
+      toid[R.begin + k] = oid[R.begin + k];
+    }
+    return;
+  }
   const int d = N.split_dim;
   const float split = N.xc[d];
   const int lane = threadIdx.x & 31, warp = WM ? 0 : int(threadIdx.x >> 5);
@@ -1170,25 +1171,10 @@ __global__ void __launch_bounds__(kChunkThreads)
   }
 }
 
-// The element buffers alternate between levels.  Nodes that did not split
-// at this level (leaves) keep their elements: copied once into the next
-// level's buffer, after which both buffers hold them (later levels write only
-// inside splitting nodes).
-template <bool WM>
-__global__ void __launch_bounds__(kChunkThreads)
-    k_part_keep(const float4 *pos, const int32_t *oid, const DNode *nodes,
-                const int32_t *chunk_node, const int64_t *chunk_base, int32_t nb,
-                const int64_t *nchunk, float4 *tpos, int32_t *toid) {
-  CHUNK_PROLOGUE
-  const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
-  if (nodes[R.node].split_dim >= 0) return;
-  for (int k = tid; k < R.len; k += NT) {
-    tpos[R.begin + k] = pos[R.begin + k];
-    toid[R.begin + k] = oid[R.begin + k];
-  }
-}
-
-// 1 for nodes whose split produced two non-empty children.
+// 1 for nodes whose split produced two non-empty children.  (The element
+// buffers alternate between levels; a leaf's elements are copied once into
+// the next level's buffer by k_part_left, after which both buffers hold them
+// and later levels write only inside splitting nodes.)
 __global__ void k_split_flags(const DNode *nodes, int32_t nb, int32_t ne, int64_t *flag) {
   const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
   if (nb + i >= ne) return;
@@ -2131,10 +2117,14 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   } while (0)
     CHUNK_LAUNCH(k_stats_partial, epos_, nodes_, chunk_node_, chunk_base_, nb, counters_ + C_NCHUNK,
                  part_);
-    k_stats_final_one<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, part_, fallback_, counters_,
-                                          cfg.force_cm_fallback);
+    // a warp per node finishes every node of a small level in one launch; on
+    // large levels one thread takes each single-chunk node
+    if (!small)
+      k_stats_final_one<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, part_, fallback_,
+                                            counters_, cfg.force_cm_fallback, cfg.nd);
     k_stats_final<<<unsigned((int64_t(L) * 32 + 255) / 256), 256, 0, s>>>(
-        nodes_, nb, ne, chunk_base_, part_, fallback_, counters_, cfg.force_cm_fallback);
+        nodes_, nb, ne, chunk_base_, part_, fallback_, counters_, cfg.force_cm_fallback, cfg.nd,
+        small);
     k_cm_tight_sums<<<kTightBlocks, kTightThreads, 0, s>>>(
         epos_, nodes_, fallback_, counters_, reinterpret_cast<TightChunk *>(tight_chunks_),
         reinterpret_cast<TightNode *>(tight_nodes_), cfg.force_cm_fallback == 1);
@@ -2143,7 +2133,6 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
         reinterpret_cast<TightNode *>(tight_nodes_), cfg.force_cm_fallback == 1);
     k_cm_fallback<<<unsigned(std::min<int64_t>((L + 127) / 128, 1024)), 128, 0, s>>>(
         epos_, nodes_, fallback_, counters_);
-    k_split_decide<<<gL, 128, 0, s>>>(nodes_, nb, ne, cfg.nd);
     CHUNK_LAUNCH(k_part_count, epos_, nodes_, chunk_node_, chunk_base_, nb, counters_ + C_NCHUNK,
                  left_cnt_);
     k_part_node_scan<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, left_cnt_, left_base_);
@@ -2151,8 +2140,6 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
                  counters_ + C_NCHUNK, left_base_, tpos_, toid_, idx_);
     CHUNK_LAUNCH(k_part_right, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
                  counters_ + C_NCHUNK, idx_, tpos_, toid_, walk_err_);
-    CHUNK_LAUNCH(k_part_keep, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
-                 counters_ + C_NCHUNK, tpos_, toid_);
 #undef CHUNK_LAUNCH
     std::swap(epos_, tpos_);
     std::swap(cap_e_, cap_t_);
