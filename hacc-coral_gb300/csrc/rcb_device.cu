@@ -207,7 +207,7 @@ __device__ __forceinline__ int64_t block_exclusive_scan(const int64_t (&v)[kScan
 // (k_chunk_counts, the scan and k_chunk_fill), the total into *nchunk.
 __global__ void __launch_bounds__(kScanThreads)
     k_chunk_setup_small(const DNode *nodes, int32_t nb, int32_t ne, int64_t *base,
-                        int32_t *chunk_node, int64_t *nchunk) {
+                        int32_t *chunk_node, int64_t *counters) {
   int64_t c[kScanPer], b[kScanPer];
   const int32_t i0 = int32_t(threadIdx.x) * kScanPer;
 #pragma unroll
@@ -220,7 +220,11 @@ __global__ void __launch_bounds__(kScanThreads)
     base[i0 + k] = b[k];
     for (int64_t q = 0; q < c[k]; ++q) chunk_node[b[k] + q] = nb + i0 + k;
   }
-  if (threadIdx.x == 0) *nchunk = total;
+  if (threadIdx.x == 0) {
+    counters[C_NCHUNK] = total;
+    counters[C_NFALLBACK] = 0;  // the level's centre-of-mass lists start empty
+    counters[C_NTIGHT] = 0;
+  }
 }
 
 // Levels of at most kScanBlock nodes, in one block: k_split_flags, the scan
@@ -2094,15 +2098,14 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     DT_CHECK(grow(part_, cap_part_, size_t(max_chunks) * kPartWords, s));
     DT_CHECK(grow(left_cnt_, cap_lc_, size_t(max_chunks), s));
     DT_CHECK(grow(left_base_, cap_lb_, size_t(max_chunks), s));
-    DT_CHECK(cudaMemsetAsync(counters_ + C_NFALLBACK, 0, sizeof(int64_t), s));
-    DT_CHECK(cudaMemsetAsync(counters_ + C_NTIGHT, 0, sizeof(int64_t), s));
-
     const unsigned gL = unsigned((L + 127) / 128);
     const bool small = int64_t(L) <= kScanBlock;
     if (small) {
       k_chunk_setup_small<<<1, kScanThreads, 0, s>>>(nodes_, nb, ne, chunk_base_, chunk_node_,
-                                                     counters_ + C_NCHUNK);
+                                                     counters_);
     } else {
+      DT_CHECK(cudaMemsetAsync(counters_ + C_NFALLBACK, 0, sizeof(int64_t), s));
+      DT_CHECK(cudaMemsetAsync(counters_ + C_NTIGHT, 0, sizeof(int64_t), s));
       k_chunk_counts<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
       DT_CHECK(exclusive_scan_i64(node_tmp_, chunk_base_, L, counters_ + C_NCHUNK, scan_tmp_, s));
       k_chunk_fill<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, chunk_node_);
