@@ -845,7 +845,7 @@ hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float
   st.t_walk_ms = ctx->tree.lists_ms();
   (void)tb;
   const hsr::DeviceTreeInfo &ti = ctx->tree.info();
-  launches += ti.levels * 16 + 24;
+  launches += ti.launches;
   const int32_t *perm = ctx->tree.perm();
   if (overlap) {
     CU(ctx->copier->wait(), "H2D arrays (copy thread)");

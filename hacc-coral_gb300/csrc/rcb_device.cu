@@ -2076,10 +2076,12 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   if (n > 0) {
     DT_CHECK(cudaMemcpyAsync(epos_, pos_in, size_t(n) * sizeof(float4), cudaMemcpyDeviceToDevice, s));
     k_iota<<<grid_for(n, 256), 256, 0, s>>>(oid_, n);
+    ++info_.launches;
   }
   size_t want_nodes = size_t(std::max<int64_t>(64, 4 * n / std::max(1, cfg.nd) + 64));
   DT_CHECK(grow(nodes_, cap_nodes_, want_nodes, s));
   k_root<<<1, 1, 0, s>>>(nodes_, n, cfg);
+  ++info_.launches;
   DT_CHECK(cudaGetLastError());
 
   // ---- levels ----
@@ -2103,12 +2105,15 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     if (small) {
       k_chunk_setup_small<<<1, kScanThreads, 0, s>>>(nodes_, nb, ne, chunk_base_, chunk_node_,
                                                      counters_);
+      ++info_.launches;
     } else {
       DT_CHECK(cudaMemsetAsync(counters_ + C_NFALLBACK, 0, sizeof(int64_t), s));
       DT_CHECK(cudaMemsetAsync(counters_ + C_NTIGHT, 0, sizeof(int64_t), s));
       k_chunk_counts<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
-      DT_CHECK(exclusive_scan_i64(node_tmp_, chunk_base_, L, counters_ + C_NCHUNK, scan_tmp_, s));
+      ++info_.launches;
+      DT_CHECK(scan_counted(node_tmp_, chunk_base_, L, counters_ + C_NCHUNK, scan_tmp_, s));
       k_chunk_fill<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, chunk_node_);
+      ++info_.launches;
     }
     // deep levels (nodes of ~2048 elements or fewer on average): a warp per chunk
     const bool wm = int64_t(L) * 2048 >= n;
@@ -2117,28 +2122,36 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   do {                                                                           \
     if (wm) kern<true><<<gC, kChunkThreads, 0, s>>>(__VA_ARGS__);                \
     else kern<false><<<gC, kChunkThreads, 0, s>>>(__VA_ARGS__);                  \
+    ++info_.launches;                                                            \
   } while (0)
     CHUNK_LAUNCH(k_stats_partial, epos_, nodes_, chunk_node_, chunk_base_, nb, counters_ + C_NCHUNK,
                  part_);
     // a warp per node finishes every node of a small level in one launch; on
     // large levels one thread takes each single-chunk node
-    if (!small)
+    if (!small) {
       k_stats_final_one<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, part_, fallback_,
                                             counters_, cfg.force_cm_fallback, cfg.nd);
+      ++info_.launches;
+    }
     k_stats_final<<<unsigned((int64_t(L) * 32 + 255) / 256), 256, 0, s>>>(
         nodes_, nb, ne, chunk_base_, part_, fallback_, counters_, cfg.force_cm_fallback, cfg.nd,
         small);
+    ++info_.launches;
     k_cm_tight_sums<<<kTightBlocks, kTightThreads, 0, s>>>(
         epos_, nodes_, fallback_, counters_, reinterpret_cast<TightChunk *>(tight_chunks_),
         reinterpret_cast<TightNode *>(tight_nodes_), cfg.force_cm_fallback == 1);
+    ++info_.launches;
     k_cm_tight_bound<<<kTightBlocks, kTightThreads, 0, s>>>(
         epos_, nodes_, fallback_, counters_, reinterpret_cast<const TightChunk *>(tight_chunks_),
         reinterpret_cast<TightNode *>(tight_nodes_), cfg.force_cm_fallback == 1);
+    ++info_.launches;
     k_cm_fallback<<<unsigned(std::min<int64_t>((L + 127) / 128, 1024)), 128, 0, s>>>(
         epos_, nodes_, fallback_, counters_);
+    ++info_.launches;
     CHUNK_LAUNCH(k_part_count, epos_, nodes_, chunk_node_, chunk_base_, nb, counters_ + C_NCHUNK,
                  left_cnt_);
     k_part_node_scan<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, left_cnt_, left_base_);
+    ++info_.launches;
     CHUNK_LAUNCH(k_part_left, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
                  counters_ + C_NCHUNK, left_base_, tpos_, toid_, idx_);
     CHUNK_LAUNCH(k_part_right, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
@@ -2150,10 +2163,13 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     std::swap(cap_o_, cap_to_);
     if (small) {
       k_children_small<<<1, kScanThreads, 0, s>>>(nodes_, nb, ne, counters_ + C_NSPLIT);
+      ++info_.launches;
     } else {
       k_split_flags<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
-      DT_CHECK(exclusive_scan_i64(node_tmp_, node_tmp_, L, counters_ + C_NSPLIT, scan_tmp_, s));
+      ++info_.launches;
+      DT_CHECK(scan_counted(node_tmp_, node_tmp_, L, counters_ + C_NSPLIT, scan_tmp_, s));
       k_children<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
+      ++info_.launches;
     }
     DT_CHECK(cudaGetLastError());
     DT_CHECK(cudaMemcpyAsync(h_counters_, counters_, (C_NTIGHT + 1) * sizeof(int64_t),
@@ -2182,15 +2198,18 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   DT_CHECK(grow(ppm_, cap_ppm_, size_t(nnodes) * k + 1, s));
   for (int64_t l = int64_t(level_begin.size()) - 2; l >= 0; --l) {
     const int32_t lb = level_begin[l], le = level_begin[l + 1];
-    if (le > lb)
+    if (le > lb) {
       k_pseudo<<<unsigned((le - lb + 127) / 128), 128, 0, s>>>(nodes_, lb, le, epos_, ppm_, k,
                                                                cfg.ppc, cfg.nd);
+      ++info_.launches;
+    }
   }
   const int64_t ntab = n + int64_t(nnodes) * k;
   DT_CHECK(grow(table_, cap_tab_, size_t(std::max<int64_t>(ntab, 1)), s));
   if (n > 0)
     DT_CHECK(cudaMemcpyAsync(table_, epos_, size_t(n) * sizeof(float4), cudaMemcpyDeviceToDevice, s));
   k_table_pseudo<<<unsigned((nnodes + 127) / 128), 128, 0, s>>>(nodes_, nnodes, ppm_, k, table_, n);
+  ++info_.launches;
   DT_CHECK(cudaGetLastError());
 
   // ---- processed leaves in DFS order ----
@@ -2200,10 +2219,14 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   DT_CHECK(grow(scan_tmp_, cap_scan_, size_t(scan_tmp_size(nl_cap)), s));
   int64_t *leaf_at = leaf_tmp_, *lflag = leaf_tmp_ + nl_cap;
   k_fill_i64<<<grid_for(nl_cap, 256), 256, 0, s>>>(leaf_at, nl_cap, -1);
+  ++info_.launches;
   k_mark_leaves<<<unsigned((nnodes + 127) / 128), 128, 0, s>>>(nodes_, nnodes, cfg, n, leaf_at);
+  ++info_.launches;
   k_leaf_flags<<<unsigned((nl_cap + 255) / 256), 256, 0, s>>>(leaf_at, nl_cap, lflag);
-  DT_CHECK(exclusive_scan_i64(lflag, lflag, nl_cap, counters_ + C_NLEAF, scan_tmp_, s));
+  ++info_.launches;
+  DT_CHECK(scan_counted(lflag, lflag, nl_cap, counters_ + C_NLEAF, scan_tmp_, s));
   k_leaf_compact<<<unsigned((nl_cap + 255) / 256), 256, 0, s>>>(leaf_at, lflag, nl_cap, leaf_ids_);
+  ++info_.launches;
   DT_CHECK(cudaGetLastError());
   DT_CHECK(cudaMemcpyAsync(h_counters_ + C_NLEAF, counters_ + C_NLEAF, sizeof(int64_t),
                            cudaMemcpyDeviceToHost, s));
@@ -2226,8 +2249,9 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     k_walk<2><<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(
         nodes_, nnodes, leaf_ids_, nleaves, cfg, n, seg_cnt, list_len, nullptr, nullptr,
         segs_local_, walk_err_, counters_);
-    DT_CHECK(exclusive_scan_i64(seg_cnt, seg_base, nleaves, counters_ + C_NSEG, scan_tmp_, s));
-    DT_CHECK(exclusive_scan_i64(list_len, list_base, nleaves, counters_ + C_NENT, scan_tmp_, s));
+    ++info_.launches;
+    DT_CHECK(scan_counted(seg_cnt, seg_base, nleaves, counters_ + C_NSEG, scan_tmp_, s));
+    DT_CHECK(scan_counted(list_len, list_base, nleaves, counters_ + C_NENT, scan_tmp_, s));
   }
   DT_CHECK(cudaGetLastError());
   DT_CHECK(cudaMemcpyAsync(h_counters_ + C_NSEG, counters_ + C_NSEG, 2 * sizeof(int64_t),
@@ -2250,13 +2274,16 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   DT_CHECK(grow(idx_list_, cap_idx_, size_t(std::max<int64_t>(nent, 1)), s));
   DT_CHECK(grow(leafdesc_, cap_ld_, nlw, s));
   if (nleaves > 0) {
-    if (h_counters_[C_SEGOVF])
+    if (h_counters_[C_SEGOVF]) {
       k_walk<1><<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(
           nodes_, nnodes, leaf_ids_, nleaves, cfg, n, nullptr, nullptr, seg_base, list_base, segs_,
           walk_err_, counters_);
-    else
+      ++info_.launches;
+    } else {
       k_pack_segs<<<unsigned(std::min<int64_t>((nleaves + 7) / 8, 152 * 64)), 256, 0, s>>>(
           segs_local_, seg_cnt, seg_base, list_base, nleaves, segs_);
+      ++info_.launches;
+    }
     int64_t *kept = nullptr;
     if (cfg.prune2 > 0.0f) {
       kept = node_tmp_ + 4 * nlw;
@@ -2264,11 +2291,14 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
       k_expand_pruned<<<unsigned(blocks), 256, 0, s>>>(segs_, seg_base, seg_cnt, list_base, nodes_,
                                                        leaf_ids_, nleaves, table_, cfg.prune2,
                                                        idx_list_, kept);
+      ++info_.launches;
     } else {
       DT_CHECK(launch_expand_segments(segs_, nseg, idx_list_, s));
+      info_.launches += nseg > 0;
     }
     k_leaf_desc<<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(
         nodes_, leaf_ids_, nleaves, list_len, kept, list_base, leafdesc_, counters_);
+    ++info_.launches;
   }
   DT_CHECK(cudaGetLastError());
 
@@ -2277,6 +2307,19 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   DT_CHECK(make_items(n, jsplit, s));
   lists_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
   return cudaSuccess;
+}
+
+cudaError_t DeviceTree::scan_counted(const int64_t *in, int64_t *out, int64_t n, int64_t *total,
+                                     int64_t *tmp, cudaStream_t s) {
+  // one block-scan launch per level of the recursion plus one add per level above the last
+  for (int64_t m = n; m > 0;) {
+    ++info_.launches;
+    const int64_t nb = (m + kScanBlock - 1) / kScanBlock;
+    if (nb == 1) break;
+    ++info_.launches;
+    m = nb;
+  }
+  return exclusive_scan_i64(in, out, n, total, tmp, s);
 }
 
 cudaError_t DeviceTree::regroup(int group, int64_t jsplit, cudaStream_t s) {
@@ -2293,10 +2336,14 @@ cudaError_t DeviceTree::make_items(int64_t n, int64_t jsplit, cudaStream_t s) {
   if (nleaves > 0) {
     k_groups_warp<<<unsigned((nleaves + kGWarps - 1) / kGWarps), 32 * kGWarps, 0, s>>>(
         nodes_, leaf_ids_, nleaves, epos_, gidx_, G);
+    ++info_.launches;
     k_groups<<<unsigned(nleaves), kGroupThreads, 0, s>>>(nodes_, leaf_ids_, nleaves, epos_, gidx_, G);
+    ++info_.launches;
     k_item_hist<<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(leafdesc_, nleaves, jsplit, G,
                                                                 counters_);
+    ++info_.launches;
     k_item_bases<<<1, 32, 0, s>>>(counters_);
+    ++info_.launches;
   }
   DT_CHECK(cudaGetLastError());
   DT_CHECK(cudaMemcpyAsync(h_counters_, counters_, C_COUNT * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
@@ -2306,9 +2353,11 @@ cudaError_t DeviceTree::make_items(int64_t n, int64_t jsplit, cudaStream_t s) {
   info_.pairs = h_counters_[C_PAIRS];
   padded_pairs_ = h_counters_[C_PADDED];
   DT_CHECK(grow(items_, cap_items_, size_t(std::max<int64_t>(nitems, 1)), s));
-  if (nitems > 0)
+  if (nitems > 0) {
     k_item_fill<<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(leafdesc_, nleaves, jsplit, G,
                                                                counters_, items_);
+    ++info_.launches;
+  }
   DT_CHECK(cudaGetLastError());
   DT_CHECK(cudaStreamSynchronize(s));
   return cudaSuccess;

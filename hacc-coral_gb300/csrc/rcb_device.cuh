@@ -56,6 +56,7 @@ struct DeviceTreeInfo {
   int64_t nodes = 0, levels = 0, leaves = 0, processed_leaves = 0;
   int64_t segments = 0, list_entries = 0, pairs = 0, items = 0;
   int64_t cm_fallbacks = 0;
+  int64_t launches = 0;  // kernels launched by the last build() and the item setups after it
 };
 
 // Owns the device buffers of one tree; reused across calls (grows only).
@@ -104,6 +105,9 @@ class DeviceTree {
   template <typename T>
   cudaError_t grow(T *&p, size_t &cap, size_t count, cudaStream_t s, bool keep = false);
   cudaError_t make_items(int64_t n, int64_t jsplit, cudaStream_t s);
+  // exclusive_scan_i64, adding its kernels to info_.launches
+  cudaError_t scan_counted(const int64_t *in, int64_t *out, int64_t n, int64_t *total, int64_t *tmp,
+                           cudaStream_t s);
 
   DeviceTreeInfo info_{};
   int64_t padded_pairs_ = 0;

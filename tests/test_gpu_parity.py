@@ -338,3 +338,22 @@ def test_pairs_in_cutoff_count(ctx):
         want += int((r2 < rc2).sum())
     assert got == want, (got, want)
     assert 0 < got < st["pairs"]
+
+
+@pytest.mark.parametrize("ng,nd", [(32, 64), (48, 32)])
+def test_kernel_launches_match_cupti(ctx, ng, nd):
+    """The kick's kernel_launches statistic counts exactly the kernels the
+    CUDA profiling interface sees in the call (copies and memsets aside)."""
+    torch = pytest.importorskip("torch")
+    from torch.profiler import ProfilerActivity, profile
+    p = _zero_v(synth.zeldovich_box(ng, seed=3))
+    kp = synth.kick_params(p, nd=nd, fcoeff=1.0)
+    ctx.rcb_kick(p.copy(), kp)  # first call: buffers and the shape choice
+    with profile(activities=[ProfilerActivity.CUDA]) as prof:
+        st = ctx.rcb_kick(p, kp)
+        torch.cuda.synchronize()
+    dev = [e for e in prof.events() if e.device_type == torch.autograd.DeviceType.CUDA]
+    if not dev:
+        pytest.skip("the profiler recorded no device activity")
+    kernels = [e for e in dev if not e.name.startswith(("Memcpy", "Memset"))]
+    assert len(kernels) == st["kernel_launches"], sorted({e.name for e in kernels})
