@@ -43,10 +43,13 @@ __device__ __forceinline__ int lsb_exp(float t) {
 constexpr int kChunk = 4096;        // elements per statistics / partition chunk
 constexpr int kChunkThreads = 256;  // threads per chunk (16 elements each)
 constexpr int kWalkStack = 256;     // DFS stack of the list walk
+constexpr int kNodeMax = 16384;     // largest node the one-block partition takes
+constexpr int kNodeThreads = 256;   // threads of the one-block partition
+constexpr int kChainSteps = 32;     // chain steps before the one-block partition jumps pointers
 
 enum { C_NCHUNK = 0, C_NSPLIT = 1, C_NFALLBACK = 2, C_NLEAF = 3, C_NSEG = 4, C_NENT = 5,
        C_PAIRS = 6, C_PADDED = 7, C_NITEMS = 8, C_MAXLEN = 9, C_TDONE1 = 10, C_TDONE2 = 11,
-       C_NTIGHT = 12, C_SEGOVF = 13, C_BUCKET = 16, C_FILL = 48, C_COUNT = 80 };
+       C_NTIGHT = 12, C_SEGOVF = 13, C_MAXCNT = 14, C_BUCKET = 16, C_FILL = 48, C_COUNT = 80 };
 
 // Segments a leaf's walk can leave in its own region of the one-pass walk;
 // a leaf with more sends the build to the counting walk and a second pass.
@@ -224,14 +227,16 @@ __global__ void __launch_bounds__(kScanThreads)
     counters[C_NCHUNK] = total;
     counters[C_NFALLBACK] = 0;  // the level's centre-of-mass lists start empty
     counters[C_NTIGHT] = 0;
+    counters[C_MAXCNT] = 0;     // the next level's largest node, from the children
   }
 }
 
 // Levels of at most kScanBlock nodes, in one block: k_split_flags, the scan
 // and k_children; the number of split nodes into *nsplit.
 __global__ void __launch_bounds__(kScanThreads)
-    k_children_small(DNode *nodes, int32_t nb, int32_t ne, int64_t *nsplit) {
+    k_children_small(DNode *nodes, int32_t nb, int32_t ne, int64_t *nsplit, int64_t *maxcnt) {
   int64_t f[kScanPer], r[kScanPer];
+  unsigned m = 0;  // largest child count of this thread's nodes
   const int32_t i0 = int32_t(threadIdx.x) * kScanPer;
 #pragma unroll
   for (int k = 0; k < kScanPer; ++k) {
@@ -253,6 +258,7 @@ __global__ void __launch_bounds__(kScanThreads)
     const int32_t cl = ne + 2 * int32_t(r[k]), cr = cl + 1;
     N.cl = cl;
     N.cr = cr;
+    m = max(m, unsigned(max(N.nleft, N.count - N.nleft)));
     for (int s = 0; s < 2; ++s) {
       DNode &C = nodes[s == 0 ? cl : cr];
       C.count = s == 0 ? N.nleft : N.count - N.nleft;
@@ -269,6 +275,8 @@ __global__ void __launch_bounds__(kScanThreads)
     }
   }
   if (threadIdx.x == 0) *nsplit = total;
+  m = __reduce_max_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0 && m) atomicMax(reinterpret_cast<unsigned long long *>(maxcnt), m);
 }
 
 struct ChunkRange {
@@ -1175,6 +1183,141 @@ __global__ void __launch_bounds__(kChunkThreads)
   }
 }
 
+// The whole partition of one node in one block, for levels whose nodes hold
+// at most kNodeMax elements: the left elements go to their ranks (warp w
+// takes a contiguous share of the node, ranks in array order through the
+// warps' totals and ballot prefixes), their source positions into shared
+// memory, and every right element before nleft follows p -> idx[p] -> ...
+// there (the reference's swap sequence, RCBForceTree.cxx:647-669).  A chain
+// longer than kChainSteps sends the block to pointer jumping in place over
+// idx (each entry moves along its own chain, so every read sees a point of
+// that chain), which ends in log2(count) + 1 rounds.  Also sets N.nleft and
+// copies leaves' elements.
+__global__ void __launch_bounds__(kNodeThreads)
+    k_part_node(const float4 *__restrict__ pos, const int32_t *__restrict__ oid, DNode *nodes,
+                int32_t nb, int32_t ne, int32_t node_max, float4 *tpos, int32_t *toid,
+                int32_t *err) {
+  extern __shared__ int32_t sidx[];
+  constexpr int kW = kNodeThreads / 32;
+  __shared__ int wtot[kW];
+  __shared__ int s_long;
+  const int32_t node = nb + int32_t(blockIdx.x);
+  if (node >= ne) return;
+  DNode &N = nodes[node];
+  const int cnt = N.count;
+  if (cnt > node_max) {  // the launch's shared memory does not hold it
+    if (threadIdx.x == 0) atomicExch(err, 3);
+    return;
+  }
+  const int64_t off = N.offset;
+  if (N.split_dim < 0) {
+    for (int e = threadIdx.x; e < cnt; e += kNodeThreads) {
+      tpos[off + e] = pos[off + e];
+      toid[off + e] = oid[off + e];
+    }
+    return;
+  }
+  const int d = N.split_dim;
+  const float split = N.xc[d];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned below = (1u << lane) - 1u;
+  const int sub = (((cnt + kW - 1) / kW) + 31) & ~31;
+  const int beg = warp * sub, end = min(cnt, beg + sub);
+  if (threadIdx.x == 0) s_long = 0;
+  int c = 0;
+  for (int e0 = beg; e0 < end; e0 += 32) {
+    const int e = e0 + lane;
+    const bool l = e < end && key_of(pos[off + e], d) < split;
+    c += __popc(__ballot_sync(0xffffffffu, l));
+  }
+  if (lane == 0) wtot[warp] = c;
+  __syncthreads();
+  int r = 0, nleft = 0;
+#pragma unroll
+  for (int w = 0; w < kW; ++w) {
+    const int v = wtot[w];
+    r += w < warp ? v : 0;
+    nleft += v;
+  }
+  for (int e0 = beg; e0 < end; e0 += 32) {
+    const int e = e0 + lane;
+    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+    bool l = false;
+    if (e < end) {
+      p = pos[off + e];
+      l = key_of(p, d) < split;
+    }
+    const unsigned bal = __ballot_sync(0xffffffffu, l);
+    if (l) {
+      const int q = r + __popc(bal & below);
+      tpos[off + q] = p;
+      toid[off + q] = oid[off + e];
+      sidx[q] = e;
+    } else if (e < end && e >= nleft) {
+      // a right element at or after nleft: no swap touches it, it stays
+      tpos[off + e] = p;
+      toid[off + e] = oid[off + e];
+    }
+    r += __popc(bal);
+  }
+  if (threadIdx.x == 0) N.nleft = nleft;
+  __syncthreads();
+  for (int e = threadIdx.x; e < nleft; e += kNodeThreads) {
+    const float4 p = pos[off + e];
+    if (key_of(p, d) < split) continue;
+    int q = e, steps = 0;
+    bool bad = false;
+    while (q < nleft && steps < kChainSteps) {
+      const int nq = sidx[q];
+      if (nq <= q || nq >= cnt) {  // cannot happen for a valid partition
+        bad = true;
+        break;
+      }
+      q = nq;
+      ++steps;
+    }
+    if (bad) {
+      atomicExch(err, 2);
+      continue;
+    }
+    if (q < nleft) {
+      s_long = 1;
+      continue;
+    }
+    tpos[off + q] = p;
+    toid[off + q] = oid[off + e];
+  }
+  __syncthreads();
+  if (!s_long) return;
+  // pointer jumping: afterwards idx[q] is the end of the chain through q
+  for (int round = 0;; ++round) {
+    bool ch = false;
+    for (int q = threadIdx.x; q < nleft; q += kNodeThreads) {
+      const int j = sidx[q];
+      if (j != q && j < nleft) {  // j == q: a left element that no swap moves
+        sidx[q] = sidx[j];
+        ch = true;
+      }
+    }
+    if (!__syncthreads_or(ch)) break;
+    if (round > 40) {  // cannot happen for a valid partition
+      if (threadIdx.x == 0) atomicExch(err, 2);
+      return;
+    }
+  }
+  for (int e = threadIdx.x; e < nleft; e += kNodeThreads) {
+    const float4 p = pos[off + e];
+    if (key_of(p, d) < split) continue;
+    const int q = sidx[e];
+    if (q < nleft || q >= cnt) {
+      atomicExch(err, 2);
+      continue;
+    }
+    tpos[off + q] = p;
+    toid[off + q] = oid[off + e];
+  }
+}
+
 // 1 for nodes whose split produced two non-empty children.  (The element
 // buffers alternate between levels; a leaf's elements are copied once into
 // the next level's buffer by k_part_left, after which both buffers hold them
@@ -1186,8 +1329,17 @@ __global__ void k_split_flags(const DNode *nodes, int32_t nb, int32_t ne, int64_
   flag[i] = (N.split_dim >= 0 && N.nleft > 0 && N.nleft < N.count) ? 1 : 0;
 }
 
-__global__ void k_children(DNode *nodes, int32_t nb, int32_t ne, const int64_t *rank) {
+__global__ void k_children(DNode *nodes, int32_t nb, int32_t ne, const int64_t *rank,
+                           int64_t *maxcnt) {
   const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+  unsigned m = 0;
+  if (nb + i < ne) {
+    const DNode &N = nodes[nb + i];
+    if (N.split_dim >= 0 && N.nleft > 0 && N.nleft < N.count)
+      m = unsigned(max(N.nleft, N.count - N.nleft));
+  }
+  m = __reduce_max_sync(0xffffffffu, m);
+  if ((threadIdx.x & 31) == 0 && m) atomicMax(reinterpret_cast<unsigned long long *>(maxcnt), m);
   if (nb + i >= ne) return;
   DNode &N = nodes[nb + i];
   if (!(N.split_dim >= 0 && N.nleft > 0 && N.nleft < N.count)) {
@@ -2087,6 +2239,12 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   // ---- levels ----
   std::vector<int32_t> level_begin{0};
   int32_t nb = 0, ne = 1;
+  int64_t level_max = n;  // the level's largest node
+  if (!node_attr_) {
+    DT_CHECK(cudaFuncSetAttribute(k_part_node, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kNodeMax * int(sizeof(int32_t))));
+    node_attr_ = true;
+  }
   while (ne > nb) {
     const int32_t L = ne - nb;
     if (size_t(ne) + 2 * size_t(L) > cap_nodes_)
@@ -2109,6 +2267,7 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     } else {
       DT_CHECK(cudaMemsetAsync(counters_ + C_NFALLBACK, 0, sizeof(int64_t), s));
       DT_CHECK(cudaMemsetAsync(counters_ + C_NTIGHT, 0, sizeof(int64_t), s));
+      DT_CHECK(cudaMemsetAsync(counters_ + C_MAXCNT, 0, sizeof(int64_t), s));
       k_chunk_counts<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
       ++info_.launches;
       DT_CHECK(scan_counted(node_tmp_, chunk_base_, L, counters_ + C_NCHUNK, scan_tmp_, s));
@@ -2148,31 +2307,40 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     k_cm_fallback<<<unsigned(std::min<int64_t>((L + 127) / 128, 1024)), 128, 0, s>>>(
         epos_, nodes_, fallback_, counters_);
     ++info_.launches;
-    CHUNK_LAUNCH(k_part_count, epos_, nodes_, chunk_node_, chunk_base_, nb, counters_ + C_NCHUNK,
-                 left_cnt_);
-    k_part_node_scan<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, left_cnt_, left_base_);
-    ++info_.launches;
-    CHUNK_LAUNCH(k_part_left, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
-                 counters_ + C_NCHUNK, left_base_, tpos_, toid_, idx_);
-    CHUNK_LAUNCH(k_part_right, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
-                 counters_ + C_NCHUNK, idx_, tpos_, toid_, walk_err_);
+    if (level_max <= kNodeMax) {
+      // every node fits one block's shared memory: the whole partition in one launch
+      const size_t smem = size_t(std::max<int64_t>(level_max, 1)) * sizeof(int32_t);
+      k_part_node<<<unsigned(L), kNodeThreads, smem, s>>>(epos_, oid_, nodes_, nb, ne,
+                                                          int32_t(level_max), tpos_, toid_, walk_err_);
+      ++info_.launches;
+    } else {
+      CHUNK_LAUNCH(k_part_count, epos_, nodes_, chunk_node_, chunk_base_, nb, counters_ + C_NCHUNK,
+                   left_cnt_);
+      k_part_node_scan<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, left_cnt_, left_base_);
+      ++info_.launches;
+      CHUNK_LAUNCH(k_part_left, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
+                   counters_ + C_NCHUNK, left_base_, tpos_, toid_, idx_);
+      CHUNK_LAUNCH(k_part_right, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
+                   counters_ + C_NCHUNK, idx_, tpos_, toid_, walk_err_);
+    }
 #undef CHUNK_LAUNCH
     std::swap(epos_, tpos_);
     std::swap(cap_e_, cap_t_);
     std::swap(oid_, toid_);
     std::swap(cap_o_, cap_to_);
     if (small) {
-      k_children_small<<<1, kScanThreads, 0, s>>>(nodes_, nb, ne, counters_ + C_NSPLIT);
+      k_children_small<<<1, kScanThreads, 0, s>>>(nodes_, nb, ne, counters_ + C_NSPLIT,
+                                                  counters_ + C_MAXCNT);
       ++info_.launches;
     } else {
       k_split_flags<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
       ++info_.launches;
       DT_CHECK(scan_counted(node_tmp_, node_tmp_, L, counters_ + C_NSPLIT, scan_tmp_, s));
-      k_children<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
+      k_children<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_, counters_ + C_MAXCNT);
       ++info_.launches;
     }
     DT_CHECK(cudaGetLastError());
-    DT_CHECK(cudaMemcpyAsync(h_counters_, counters_, (C_NTIGHT + 1) * sizeof(int64_t),
+    DT_CHECK(cudaMemcpyAsync(h_counters_, counters_, (C_MAXCNT + 1) * sizeof(int64_t),
                              cudaMemcpyDeviceToHost, s));
     int32_t perr = 0;
     DT_CHECK(cudaMemcpyAsync(&perr, walk_err_, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
@@ -2183,6 +2351,7 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     }
     info_.cm_fallbacks += h_counters_[C_NFALLBACK] - h_counters_[C_NTIGHT];
     const int64_t nsplit = h_counters_[C_NSPLIT];
+    level_max = h_counters_[C_MAXCNT];
     nb = ne;
     ne = int32_t(ne + 2 * nsplit);
     level_begin.push_back(nb);

@@ -152,6 +152,7 @@ class DeviceTree {
   size_t cap_ld_ = 0;
   SegDesc *segs_ = nullptr;
   size_t cap_seg_ = 0;
+  bool node_attr_ = false;         // k_part_node's shared-memory limit raised
   SegDesc *segs_local_ = nullptr;  // the one-pass walk's per-leaf regions
   size_t cap_segl_ = 0;
   int32_t *idx_list_ = nullptr;
