@@ -44,8 +44,8 @@ constexpr int kChunk = 4096;        // elements per statistics / partition chunk
 constexpr int kChunkThreads = 256;  // threads per chunk (16 elements each)
 constexpr int kWalkStack = 256;     // DFS stack of the list walk
 constexpr int kNodeMax = 16384;     // largest node the one-block partition takes
-constexpr int kNodeThreads = 256;   // threads of the one-block partition
 constexpr int kChainSteps = 32;     // chain steps before the one-block partition jumps pointers
+constexpr int kPlainSteps = 4;      // single chain steps before the chunk partition jumps runs
 
 enum { C_NCHUNK = 0, C_NSPLIT = 1, C_NFALLBACK = 2, C_NLEAF = 3, C_NSEG = 4, C_NENT = 5,
        C_PAIRS = 6, C_PADDED = 7, C_NITEMS = 8, C_MAXLEN = 9, C_TDONE1 = 10, C_TDONE2 = 11,
@@ -231,6 +231,27 @@ __global__ void __launch_bounds__(kScanThreads)
   }
 }
 
+// Child s (0 left, 1 right) of split node N, as four 16-byte stores.
+__device__ __forceinline__ void write_child(DNode &dst, const DNode &N, int s) {
+  DNode C;
+  C.count = s == 0 ? N.nleft : N.count - N.nleft;
+  C.offset = s == 0 ? N.offset : N.offset + N.nleft;
+  C.cl = C.cr = 0;
+  for (int d = 0; d < 3; ++d) {
+    C.xmin[d] = N.xmin[d];
+    C.xmax[d] = N.xmax[d];
+    C.xc[d] = 0.f;
+  }
+  C.tdr = 0.f;
+  C.split_dim = -1;
+  C.nleft = 0;
+  static_assert(sizeof(DNode) == 64, "DNode is four 16-byte words");
+  const int4 *src = reinterpret_cast<const int4 *>(&C);
+  int4 *out = reinterpret_cast<int4 *>(&dst);
+#pragma unroll
+  for (int w = 0; w < 4; ++w) out[w] = src[w];
+}
+
 // Levels of at most kScanBlock nodes, in one block: k_split_flags, the scan
 // and k_children; the number of split nodes into *nsplit.
 __global__ void __launch_bounds__(kScanThreads)
@@ -259,20 +280,8 @@ __global__ void __launch_bounds__(kScanThreads)
     N.cl = cl;
     N.cr = cr;
     m = max(m, unsigned(max(N.nleft, N.count - N.nleft)));
-    for (int s = 0; s < 2; ++s) {
-      DNode &C = nodes[s == 0 ? cl : cr];
-      C.count = s == 0 ? N.nleft : N.count - N.nleft;
-      C.offset = s == 0 ? N.offset : N.offset + N.nleft;
-      C.cl = C.cr = 0;
-      for (int d = 0; d < 3; ++d) {
-        C.xmin[d] = N.xmin[d];
-        C.xmax[d] = N.xmax[d];
-        C.xc[d] = 0.f;
-      }
-      C.tdr = 0.f;
-      C.split_dim = -1;
-      C.nleft = 0;
-    }
+    // one block writes every child: whole 16-byte words, not field by field
+    for (int s = 0; s < 2; ++s) write_child(nodes[s == 0 ? cl : cr], N, s);
   }
   if (threadIdx.x == 0) *nsplit = total;
   m = __reduce_max_sync(0xffffffffu, m);
@@ -399,18 +408,29 @@ __global__ void __launch_bounds__(kChunkThreads)
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   bool ovf = false;
   bool trn[4] = {false, false, false, false};
-  for (int k = tid; k < R.len; k += NT) {
-    const float4 p = pos[R.begin + k];
-    const float w = p.w;
-    const float t[4] = {fmul_(w, p.x), fmul_(w, p.y), fmul_(w, p.z), w};
+  // four loads in flight per thread; the elements are then taken in the same
+  // order as one at a time
+  constexpr int kU = 4;
+  for (int k0 = tid; k0 < R.len; k0 += NT * kU) {
+    float4 pu[kU];
 #pragma unroll
-    for (int q = 0; q < 4; ++q) {
-      fix_add(s[q], bits[q], t[q], ovf, trn[q]);
-      fa[q] = __fadd_ru(fa[q], fabsf(t[q]));
+    for (int u = 0; u < kU; ++u)
+      if (k0 + u * NT < R.len) pu[u] = pos[R.begin + k0 + u * NT];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      if (k0 + u * NT >= R.len) break;
+      const float4 p = pu[u];
+      const float w = p.w;
+      const float t[4] = {fmul_(w, p.x), fmul_(w, p.y), fmul_(w, p.z), w};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        fix_add(s[q], bits[q], t[q], ovf, trn[q]);
+        fa[q] = __fadd_ru(fa[q], fabsf(t[q]));
+      }
+      lo[0] = fminf(lo[0], p.x); hi[0] = fmaxf(hi[0], p.x);
+      lo[1] = fminf(lo[1], p.y); hi[1] = fmaxf(hi[1], p.y);
+      lo[2] = fminf(lo[2], p.z); hi[2] = fmaxf(hi[2], p.z);
     }
-    lo[0] = fminf(lo[0], p.x); hi[0] = fmaxf(hi[0], p.x);
-    lo[1] = fminf(lo[1], p.y); hi[1] = fmaxf(hi[1], p.y);
-    lo[2] = fminf(lo[2], p.z); hi[2] = fmaxf(hi[2], p.z);
   }
   double a[4];
   int emin[4];
@@ -1041,7 +1061,7 @@ __global__ void __launch_bounds__(kChunkThreads)
     k_part_left(const float4 *__restrict__ pos, const int32_t *__restrict__ oid, const DNode *nodes,
                 const int32_t *chunk_node, const int64_t *chunk_base, int32_t nb,
                 const int64_t *nchunk, const int64_t *left_base, float4 *tpos, int32_t *toid,
-                int32_t *idx) {
+                int32_t *idx, int32_t *ridx) {
   constexpr int kWarps = kChunkThreads / 32;
   constexpr int kSub = WM ? kChunk : kChunk / kWarps;  // a warp's share of the chunk
   CHUNK_PROLOGUE
@@ -1082,38 +1102,69 @@ __global__ void __launch_bounds__(kChunkThreads)
       l = key_of(p, d) < split;
     }
     const unsigned bal = __ballot_sync(0xffffffffu, l);
+    const int q = r + __popc(bal & below);  // left elements before this one
     if (l) {
-      const int q = r + __popc(bal & below);
       tpos[N.offset + q] = p;
       toid[N.offset + q] = oid[R.begin + e];
       idx[N.offset + q] = R.local + e;
-    } else if (e < R.len && R.local + e >= N.nleft) {
-      // a right element at or after nleft: no swap touches it, it stays
-      tpos[R.begin + e] = p;
-      toid[R.begin + e] = oid[R.begin + e];
+    } else if (e < R.len) {
+      ridx[N.offset + (R.local + e - q)] = R.local + e;
+      if (R.local + e >= N.nleft) {
+        // a right element at or after nleft: no swap touches it, it stays
+        tpos[R.begin + e] = p;
+        toid[R.begin + e] = oid[R.begin + e];
+      }
     }
     r += __popc(bal);
   }
 }
 
+// One or more steps of the chain q -> idx[q] -> ... (q < nleft): the q-th
+// left element has c = idx[q] - q right elements before it, and so has every
+// left element up to the c-th right element (at ridx[c]), whose ranks run to
+// b = ridx[c] - c.  Within that run each step adds c, so the chain leaves
+// [q, min(b, nleft)) at the first of q + c, q + 2c, ... at or past it.
+// Returns a position > q; *bad on an inconsistent partition.
+__device__ __forceinline__ int32_t chain_jump(int32_t q, int32_t nleft, int32_t nright,
+                                              const int32_t *idx, const int32_t *ridx, bool *bad) {
+  const int32_t c = idx[q] - q;
+  if (c <= 0) {  // cannot happen for a valid partition (a chain never meets a fixed point)
+    *bad = true;
+    return nleft;
+  }
+  int32_t lim = nleft;
+  if (c < nright) {
+    const int32_t b = ridx[c] - c;
+    if (b <= q) {  // cannot happen for a valid partition
+      *bad = true;
+      return nleft;
+    }
+    lim = min(lim, b);
+  }
+  const int32_t k = lim > q + c ? (lim - q + c - 1) / c : 1;
+  return q + k * c;
+}
+
 // The other particles: those at or after position nleft stay (k_part_left
 // writes them); one at p < nleft moves along p -> idx[p] -> ... until it
 // lands at or after nleft (the reference's swap sequence,
-// RCBForceTree.cxx:647-669).  Positions increase strictly along a chain, so
-// it ends within count steps.
+// RCBForceTree.cxx:647-669), taken a run of equal steps at a time
+// (chain_jump).  Positions increase strictly along a chain, so it ends within
+// count jumps.
 template <bool WM>
 __global__ void __launch_bounds__(kChunkThreads)
     k_part_right(const float4 *__restrict__ pos, const int32_t *__restrict__ oid, const DNode *nodes,
                  const int32_t *chunk_node, const int64_t *chunk_base, int32_t nb,
-                 const int64_t *nchunk, const int32_t *__restrict__ idx, float4 *tpos,
-                 int32_t *toid, int32_t *err) {
+                 const int64_t *nchunk, const int32_t *__restrict__ idx,
+                 const int32_t *__restrict__ ridx, float4 *tpos, int32_t *toid, int32_t *err) {
   CHUNK_PROLOGUE
   const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
   const DNode &N = nodes[R.node];
   if (N.split_dim < 0) return;
   const int d = N.split_dim;
   const float split = N.xc[d];
-  const int32_t is = N.nleft;
+  const int32_t is = N.nleft, nright = N.count - N.nleft;
+  const int32_t *nidx = idx + N.offset, *nridx = ridx + N.offset;
   if (R.local >= is) return;  // every element here stays (k_part_left)
   if (WM) {
     for (int k = tid; k < R.len && R.local + k < is; k += NT) {
@@ -1122,15 +1173,17 @@ __global__ void __launch_bounds__(kChunkThreads)
       if (key_of(p, d) < split) continue;
       int32_t q = R.local + k;
       int32_t steps = 0;
-      while (q < is && steps++ <= N.count) {
-        const int32_t nq = idx[N.offset + q];
-        if (nq <= q || nq >= N.count) {  // cannot happen for a valid partition
-          atomicExch(err, 2);
-          break;
+      bool bad = false;
+      while (q < is && steps <= N.count && !bad) {
+        if (steps++ < kPlainSteps) {  // single steps first: most chains end within a few
+          const int32_t nq = nidx[q];
+          if (nq <= q) bad = true;
+          q = nq;
+        } else {
+          q = chain_jump(q, is, nright, nidx, nridx, &bad);
         }
-        q = nq;
       }
-      if (q < is) {
+      if (q < is || bad || q >= N.count) {
         atomicExch(err, 2);
         continue;
       }
@@ -1156,10 +1209,12 @@ __global__ void __launch_bounds__(kChunkThreads)
   for (int j = 0; j < kPerT; ++j)
     if ((right >> j & 1u) && q[j] < is) active |= 1u << j;
   bool bad = false;
-  for (int32_t step = 0; active && step <= N.count; ++step) {
+  // single steps first, all chains' loads in flight at once: most chains end
+  // within a few
+  for (int32_t step = 0; active && step < kPlainSteps; ++step) {
     int32_t nq[kPerT];
 #pragma unroll
-    for (int j = 0; j < kPerT; ++j) nq[j] = (active >> j & 1u) ? idx[N.offset + q[j]] : q[j];
+    for (int j = 0; j < kPerT; ++j) nq[j] = (active >> j & 1u) ? nidx[q[j]] : q[j];
 #pragma unroll
     for (int j = 0; j < kPerT; ++j) {
       if (!(active >> j & 1u)) continue;
@@ -1172,6 +1227,20 @@ __global__ void __launch_bounds__(kChunkThreads)
       q[j] = nq[j];
       if (nq[j] >= is) active &= ~(1u << j);
     }
+  }
+  // the longer ones a run of equal steps at a time (chain_jump)
+#pragma unroll
+  for (int j = 0; j < kPerT; ++j) {
+    if (!(active >> j & 1u)) continue;
+    bool b = false;
+    for (int32_t it = 0; q[j] < is && it <= N.count && !b; ++it)
+      q[j] = chain_jump(q[j], is, nright, nidx, nridx, &b);
+    if (b || q[j] < is || q[j] >= N.count) {  // cannot happen for a valid partition
+      bad = true;
+      right &= ~(1u << j);
+      continue;
+    }
+    active &= ~(1u << j);
   }
   if (active || bad) atomicExch(err, 2);
 #pragma unroll
@@ -1193,12 +1262,13 @@ __global__ void __launch_bounds__(kChunkThreads)
 // idx (each entry moves along its own chain, so every read sees a point of
 // that chain), which ends in log2(count) + 1 rounds.  Also sets N.nleft and
 // copies leaves' elements.
-__global__ void __launch_bounds__(kNodeThreads)
+template <int NT>
+__global__ void __launch_bounds__(NT)
     k_part_node(const float4 *__restrict__ pos, const int32_t *__restrict__ oid, DNode *nodes,
                 int32_t nb, int32_t ne, int32_t node_max, float4 *tpos, int32_t *toid,
                 int32_t *err) {
   extern __shared__ int32_t sidx[];
-  constexpr int kW = kNodeThreads / 32;
+  constexpr int kW = NT / 32;
   __shared__ int wtot[kW];
   __shared__ int s_long;
   const int32_t node = nb + int32_t(blockIdx.x);
@@ -1211,7 +1281,7 @@ __global__ void __launch_bounds__(kNodeThreads)
   }
   const int64_t off = N.offset;
   if (N.split_dim < 0) {
-    for (int e = threadIdx.x; e < cnt; e += kNodeThreads) {
+    for (int e = threadIdx.x; e < cnt; e += NT) {
       tpos[off + e] = pos[off + e];
       toid[off + e] = oid[off + e];
     }
@@ -1224,11 +1294,18 @@ __global__ void __launch_bounds__(kNodeThreads)
   const int sub = (((cnt + kW - 1) / kW) + 31) & ~31;
   const int beg = warp * sub, end = min(cnt, beg + sub);
   if (threadIdx.x == 0) s_long = 0;
+  // four loads in flight per lane in both passes
+  constexpr int kU = 4;
   int c = 0;
-  for (int e0 = beg; e0 < end; e0 += 32) {
-    const int e = e0 + lane;
-    const bool l = e < end && key_of(pos[off + e], d) < split;
-    c += __popc(__ballot_sync(0xffffffffu, l));
+  for (int e0 = beg; e0 < end; e0 += 32 * kU) {
+    float key[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int e = e0 + 32 * u + lane;
+      key[u] = e < end ? key_of(pos[off + e], d) : split;
+    }
+#pragma unroll
+    for (int u = 0; u < kU; ++u) c += __popc(__ballot_sync(0xffffffffu, key[u] < split));
   }
   if (lane == 0) wtot[warp] = c;
   __syncthreads();
@@ -1239,30 +1316,40 @@ __global__ void __launch_bounds__(kNodeThreads)
     r += w < warp ? v : 0;
     nleft += v;
   }
-  for (int e0 = beg; e0 < end; e0 += 32) {
-    const int e = e0 + lane;
-    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-    bool l = false;
-    if (e < end) {
-      p = pos[off + e];
-      l = key_of(p, d) < split;
+  for (int e0 = beg; e0 < end; e0 += 32 * kU) {
+    float4 pu[kU];
+    int ou[kU];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int e = e0 + 32 * u + lane;
+      pu[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+      ou[u] = 0;
+      if (e < end) {
+        pu[u] = pos[off + e];
+        ou[u] = oid[off + e];
+      }
     }
-    const unsigned bal = __ballot_sync(0xffffffffu, l);
-    if (l) {
-      const int q = r + __popc(bal & below);
-      tpos[off + q] = p;
-      toid[off + q] = oid[off + e];
-      sidx[q] = e;
-    } else if (e < end && e >= nleft) {
-      // a right element at or after nleft: no swap touches it, it stays
-      tpos[off + e] = p;
-      toid[off + e] = oid[off + e];
+#pragma unroll
+    for (int u = 0; u < kU; ++u) {
+      const int e = e0 + 32 * u + lane;
+      const bool l = e < end && key_of(pu[u], d) < split;
+      const unsigned bal = __ballot_sync(0xffffffffu, l);
+      if (l) {
+        const int q = r + __popc(bal & below);
+        tpos[off + q] = pu[u];
+        toid[off + q] = ou[u];
+        sidx[q] = e;
+      } else if (e < end && e >= nleft) {
+        // a right element at or after nleft: no swap touches it, it stays
+        tpos[off + e] = pu[u];
+        toid[off + e] = ou[u];
+      }
+      r += __popc(bal);
     }
-    r += __popc(bal);
   }
   if (threadIdx.x == 0) N.nleft = nleft;
   __syncthreads();
-  for (int e = threadIdx.x; e < nleft; e += kNodeThreads) {
+  for (int e = threadIdx.x; e < nleft; e += NT) {
     const float4 p = pos[off + e];
     if (key_of(p, d) < split) continue;
     int q = e, steps = 0;
@@ -1292,7 +1379,7 @@ __global__ void __launch_bounds__(kNodeThreads)
   // pointer jumping: afterwards idx[q] is the end of the chain through q
   for (int round = 0;; ++round) {
     bool ch = false;
-    for (int q = threadIdx.x; q < nleft; q += kNodeThreads) {
+    for (int q = threadIdx.x; q < nleft; q += NT) {
       const int j = sidx[q];
       if (j != q && j < nleft) {  // j == q: a left element that no swap moves
         sidx[q] = sidx[j];
@@ -1305,7 +1392,7 @@ __global__ void __launch_bounds__(kNodeThreads)
       return;
     }
   }
-  for (int e = threadIdx.x; e < nleft; e += kNodeThreads) {
+  for (int e = threadIdx.x; e < nleft; e += NT) {
     const float4 p = pos[off + e];
     if (key_of(p, d) < split) continue;
     const int q = sidx[e];
@@ -2160,7 +2247,7 @@ DeviceTree::~DeviceTree() {
   void *ptrs[] = {epos_, tpos_, oid_, toid_, idx_, nodes_, ppm_, chunk_node_, chunk_base_, part_,
                   left_cnt_, left_base_, scan_tmp_, node_tmp_, fallback_, counters_, leaf_ids_,
                   leaf_tmp_, leafdesc_, segs_, idx_list_, table_, items_, items_tmp_, gidx_,
-                  walk_err_, tight_chunks_, tight_nodes_, segs_local_};
+                  walk_err_, tight_chunks_, tight_nodes_, segs_local_, ridx_};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h_counters_) cudaFreeHost(h_counters_);
@@ -2218,6 +2305,7 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   DT_CHECK(grow(oid_, cap_o_, nn, s));
   DT_CHECK(grow(toid_, cap_to_, nn, s));
   DT_CHECK(grow(idx_, cap_i_, nn, s));
+  DT_CHECK(grow(ridx_, cap_ri_, nn, s));
   if (!counters_) {
     DT_CHECK(cudaMalloc(&counters_, C_COUNT * sizeof(int64_t)));
     DT_CHECK(cudaHostAlloc(&h_counters_, C_COUNT * sizeof(int64_t), cudaHostAllocDefault));
@@ -2241,7 +2329,9 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   int32_t nb = 0, ne = 1;
   int64_t level_max = n;  // the level's largest node
   if (!node_attr_) {
-    DT_CHECK(cudaFuncSetAttribute(k_part_node, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    DT_CHECK(cudaFuncSetAttribute(k_part_node<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  kNodeMax * int(sizeof(int32_t))));
+    DT_CHECK(cudaFuncSetAttribute(k_part_node<1024>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                   kNodeMax * int(sizeof(int32_t))));
     node_attr_ = true;
   }
@@ -2285,17 +2375,20 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   } while (0)
     CHUNK_LAUNCH(k_stats_partial, epos_, nodes_, chunk_node_, chunk_base_, nb, counters_ + C_NCHUNK,
                  part_);
-    // a warp per node finishes every node of a small level in one launch; on
-    // large levels one thread takes each single-chunk node
-    if (!small) {
+    // one thread finishes each single-chunk node, a warp each larger one; a
+    // small level with larger nodes has a warp finish every node in one launch
+    const bool one_chunk = level_max <= kChunk;
+    if (!small || one_chunk) {
       k_stats_final_one<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, part_, fallback_,
                                             counters_, cfg.force_cm_fallback, cfg.nd);
       ++info_.launches;
     }
-    k_stats_final<<<unsigned((int64_t(L) * 32 + 255) / 256), 256, 0, s>>>(
-        nodes_, nb, ne, chunk_base_, part_, fallback_, counters_, cfg.force_cm_fallback, cfg.nd,
-        small);
-    ++info_.launches;
+    if (!one_chunk) {
+      k_stats_final<<<unsigned((int64_t(L) * 32 + 255) / 256), 256, 0, s>>>(
+          nodes_, nb, ne, chunk_base_, part_, fallback_, counters_, cfg.force_cm_fallback, cfg.nd,
+          small);
+      ++info_.launches;
+    }
     k_cm_tight_sums<<<kTightBlocks, kTightThreads, 0, s>>>(
         epos_, nodes_, fallback_, counters_, reinterpret_cast<TightChunk *>(tight_chunks_),
         reinterpret_cast<TightNode *>(tight_nodes_), cfg.force_cm_fallback == 1);
@@ -2310,8 +2403,14 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     if (level_max <= kNodeMax) {
       // every node fits one block's shared memory: the whole partition in one launch
       const size_t smem = size_t(std::max<int64_t>(level_max, 1)) * sizeof(int32_t);
-      k_part_node<<<unsigned(L), kNodeThreads, smem, s>>>(epos_, oid_, nodes_, nb, ne,
+      // few large nodes: 1024 threads a node; many (most of them small, as in
+      // clustered sets): 256
+      if (level_max > 2048 && L <= 1024)
+        k_part_node<1024><<<unsigned(L), 1024, smem, s>>>(epos_, oid_, nodes_, nb, ne,
                                                           int32_t(level_max), tpos_, toid_, walk_err_);
+      else
+        k_part_node<256><<<unsigned(L), 256, smem, s>>>(epos_, oid_, nodes_, nb, ne,
+                                                        int32_t(level_max), tpos_, toid_, walk_err_);
       ++info_.launches;
     } else {
       CHUNK_LAUNCH(k_part_count, epos_, nodes_, chunk_node_, chunk_base_, nb, counters_ + C_NCHUNK,
@@ -2319,16 +2418,18 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
       k_part_node_scan<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, left_cnt_, left_base_);
       ++info_.launches;
       CHUNK_LAUNCH(k_part_left, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
-                   counters_ + C_NCHUNK, left_base_, tpos_, toid_, idx_);
+                   counters_ + C_NCHUNK, left_base_, tpos_, toid_, idx_, ridx_);
       CHUNK_LAUNCH(k_part_right, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
-                   counters_ + C_NCHUNK, idx_, tpos_, toid_, walk_err_);
+                   counters_ + C_NCHUNK, idx_, ridx_, tpos_, toid_, walk_err_);
     }
 #undef CHUNK_LAUNCH
     std::swap(epos_, tpos_);
     std::swap(cap_e_, cap_t_);
     std::swap(oid_, toid_);
     std::swap(cap_o_, cap_to_);
-    if (small) {
+    // one block sets up the children of a level of up to 1024 nodes; above
+    // that its stores alone take longer than the three-kernel path
+    if (L <= 1024) {
       k_children_small<<<1, kScanThreads, 0, s>>>(nodes_, nb, ne, counters_ + C_NSPLIT,
                                                   counters_ + C_MAXCNT);
       ++info_.launches;

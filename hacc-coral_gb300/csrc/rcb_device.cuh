@@ -119,7 +119,8 @@ class DeviceTree {
   // elements: current and scratch (x, y, z, m) + input index
   float4 *epos_ = nullptr, *tpos_ = nullptr;
   int32_t *oid_ = nullptr, *toid_ = nullptr, *idx_ = nullptr;
-  size_t cap_e_ = 0, cap_t_ = 0, cap_o_ = 0, cap_to_ = 0, cap_i_ = 0;
+  int32_t *ridx_ = nullptr;  // partition: positions of the right elements by their rank
+  size_t cap_e_ = 0, cap_t_ = 0, cap_o_ = 0, cap_to_ = 0, cap_i_ = 0, cap_ri_ = 0;
   DNode *nodes_ = nullptr;
   size_t cap_nodes_ = 0;
   float *ppm_ = nullptr;
