@@ -654,6 +654,69 @@ __global__ void k_stats_final(DNode *nodes, int32_t nb, int32_t ne, const int64_
   finish_node(N, node, s, a, lo, hi, emin, ovf != 0, fallback, counters, force_fallback, nd);
 }
 
+// One block per node, for the top levels (nodes of many chunks): the warps
+// reduce strided chunk subsets, thread 0 the warps' results, then finishes.
+__global__ void __launch_bounds__(256)
+    k_stats_final_block(DNode *nodes, int32_t nb, int32_t ne, const int64_t *chunk_base,
+                        const double *part, int32_t *fallback, int64_t *counters,
+                        int32_t force_fallback, int32_t nd) {
+  const int32_t node = nb + int32_t(blockIdx.x);
+  if (node >= ne) return;
+  DNode &N = nodes[node];
+  if (N.count <= 0) return;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int64_t nc = (int64_t(N.count) + kChunk - 1) / kChunk;
+  const int64_t cb = chunk_base[blockIdx.x];
+  __int128 s[4] = {0, 0, 0, 0};
+  double a[4] = {0, 0, 0, 0};
+  float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+  int emin[4] = {INT_MAX, INT_MAX, INT_MAX, INT_MAX};
+  int ovf = 0;
+  for (int64_t c = threadIdx.x; c < nc; c += 256)
+    read_part(part + (cb + c) * kPartWords, s, a, lo, hi, emin, ovf);
+  for (int q = 0; q < 4; ++q) {
+    for (int o = 16; o > 0; o >>= 1) s[q] += shfl_xor_i128(s[q], o);
+    a[q] = warp_sum(a[q]);
+    for (int o = 16; o > 0; o >>= 1) emin[q] = min(emin[q], __shfl_xor_sync(0xffffffffu, emin[q], o));
+  }
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = warp_min(lo[d]);
+    hi[d] = warp_max(hi[d]);
+  }
+  ovf = __any_sync(0xffffffffu, ovf != 0);
+  __shared__ __int128 ws[8][4];
+  __shared__ double wa[8][4];
+  __shared__ float wb[8][6];
+  __shared__ int we[8][5];
+  if (lane == 0) {
+    for (int q = 0; q < 4; ++q) {
+      ws[warp][q] = s[q];
+      wa[warp][q] = a[q];
+      we[warp][q] = emin[q];
+    }
+    for (int d = 0; d < 3; ++d) {
+      wb[warp][d] = lo[d];
+      wb[warp][3 + d] = hi[d];
+    }
+    we[warp][4] = ovf;
+  }
+  __syncthreads();
+  if (threadIdx.x != 0) return;
+  for (int w = 1; w < 8; ++w) {
+    for (int q = 0; q < 4; ++q) {
+      s[q] += ws[w][q];
+      a[q] += wa[w][q];
+      emin[q] = min(emin[q], we[w][q]);
+    }
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = fminf(lo[d], wb[w][d]);
+      hi[d] = fmaxf(hi[d], wb[w][3 + d]);
+    }
+    ovf |= we[w][4];
+  }
+  finish_node(N, node, s, a, lo, hi, emin, ovf != 0, fallback, counters, force_fallback, nd);
+}
+
 // One thread per node of a single chunk (most nodes of the deep levels): the
 // per-node arithmetic, much of it FP64, then fills whole warps.
 __global__ void k_stats_final_one(DNode *nodes, int32_t nb, int32_t ne, const int64_t *chunk_base,
@@ -1034,22 +1097,31 @@ __global__ void __launch_bounds__(kChunkThreads)
   if (threadIdx.x == 0) left_cnt[chunk] = tot;
 }
 
-// Per splitting node: exclusive scan of its chunks' left counts (in chunk
-// order) and the node's total.
+// Per splitting node, a warp each: exclusive scan of its chunks' left counts
+// (in chunk order) and the node's total.
 __global__ void k_part_node_scan(DNode *nodes, int32_t nb, int32_t ne, const int64_t *chunk_base,
                                  const int32_t *left_cnt, int64_t *left_base) {
-  const int32_t i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (nb + i >= ne) return;
-  DNode &N = nodes[nb + i];
+  const int32_t w = int32_t((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (nb + w >= ne) return;  // whole warps
+  DNode &N = nodes[nb + w];
   if (N.split_dim < 0) return;
-  const int64_t cb = chunk_base[i];
+  const int64_t cb = chunk_base[w];
   const int64_t nc = (int64_t(N.count) + kChunk - 1) / kChunk;
   int64_t run = 0;
-  for (int64_t c = 0; c < nc; ++c) {
-    left_base[cb + c] = run;
-    run += left_cnt[cb + c];
+  for (int64_t c0 = 0; c0 < nc; c0 += 32) {
+    const int64_t c = c0 + lane;
+    const int64_t v = c < nc ? left_cnt[cb + c] : 0;
+    int64_t x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int64_t y = __shfl_up_sync(0xffffffffu, x, o);
+      if (lane >= o) x += y;
+    }
+    if (c < nc) left_base[cb + c] = run + x - v;
+    run += __shfl_sync(0xffffffffu, x, 31);
   }
-  N.nleft = int32_t(run);
+  if (lane == 0) N.nleft = int32_t(run);
 }
 
 // Left particles go to their rank; idx[rank] records where each came from.
@@ -2378,12 +2450,18 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     // one thread finishes each single-chunk node, a warp each larger one; a
     // small level with larger nodes has a warp finish every node in one launch
     const bool one_chunk = level_max <= kChunk;
-    if (!small || one_chunk) {
+    const bool big_nodes = L <= 16 && level_max > 32 * int64_t(kChunk);
+    if (big_nodes) {
+      // the top levels: a block per node (every node of the level)
+      k_stats_final_block<<<unsigned(L), 256, 0, s>>>(nodes_, nb, ne, chunk_base_, part_, fallback_,
+                                                      counters_, cfg.force_cm_fallback, cfg.nd);
+      ++info_.launches;
+    } else if (!small || one_chunk) {
       k_stats_final_one<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, part_, fallback_,
                                             counters_, cfg.force_cm_fallback, cfg.nd);
       ++info_.launches;
     }
-    if (!one_chunk) {
+    if (!one_chunk && !big_nodes) {
       k_stats_final<<<unsigned((int64_t(L) * 32 + 255) / 256), 256, 0, s>>>(
           nodes_, nb, ne, chunk_base_, part_, fallback_, counters_, cfg.force_cm_fallback, cfg.nd,
           small);
@@ -2415,7 +2493,8 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     } else {
       CHUNK_LAUNCH(k_part_count, epos_, nodes_, chunk_node_, chunk_base_, nb, counters_ + C_NCHUNK,
                    left_cnt_);
-      k_part_node_scan<<<gL, 128, 0, s>>>(nodes_, nb, ne, chunk_base_, left_cnt_, left_base_);
+      k_part_node_scan<<<unsigned((int64_t(L) * 32 + 127) / 128), 128, 0, s>>>(
+          nodes_, nb, ne, chunk_base_, left_cnt_, left_base_);
       ++info_.launches;
       CHUNK_LAUNCH(k_part_left, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
                    counters_ + C_NCHUNK, left_base_, tpos_, toid_, idx_, ridx_);
