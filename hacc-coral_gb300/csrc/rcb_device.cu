@@ -2526,7 +2526,8 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     DT_CHECK(cudaMemcpyAsync(&perr, walk_err_, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     DT_CHECK(cudaStreamSynchronize(s));
     if (perr) {
-      err_ = "partition chain check failed";
+      err_ = perr == 3 ? "partition: a node outgrew the one-block partition's shared memory"
+                       : "partition chain check failed";
       return cudaErrorUnknown;
     }
     info_.cm_fallbacks += h_counters_[C_NFALLBACK] - h_counters_[C_NTIGHT];

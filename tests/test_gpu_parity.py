@@ -340,10 +340,11 @@ def test_pairs_in_cutoff_count(ctx):
     assert 0 < got < st["pairs"]
 
 
-@pytest.mark.parametrize("ng,nd", [(32, 64), (48, 32)])
-def test_kernel_launches_match_cupti(ctx, ng, nd):
+def test_kernel_launches_match_cupti(ctx, ng=32, nd=64):
     """The kick's kernel_launches statistic counts exactly the kernels the
-    CUDA profiling interface sees in the call (copies and memsets aside)."""
+    CUDA profiling interface sees in the call (copies and memsets aside).  One
+    profiler session per process: a second one on the same process recorded
+    no device activity on the GB300 image."""
     torch = pytest.importorskip("torch")
     from torch.profiler import ProfilerActivity, profile
     p = _zero_v(synth.zeldovich_box(ng, seed=3))
