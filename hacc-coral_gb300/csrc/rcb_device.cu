@@ -49,7 +49,8 @@ constexpr int kPlainSteps = 4;      // single chain steps before the chunk parti
 
 enum { C_NCHUNK = 0, C_NSPLIT = 1, C_NFALLBACK = 2, C_NLEAF = 3, C_NSEG = 4, C_NENT = 5,
        C_PAIRS = 6, C_PADDED = 7, C_NITEMS = 8, C_MAXLEN = 9, C_TDONE1 = 10, C_TDONE2 = 11,
-       C_NTIGHT = 12, C_SEGOVF = 13, C_MAXCNT = 14, C_BUCKET = 16, C_FILL = 48, C_COUNT = 80 };
+       C_NTIGHT = 12, C_SEGOVF = 13, C_MAXCNT = 14, C_ERR = 15, C_BUCKET = 16, C_FILL = 48,
+       C_COUNT = 80 };
 
 // Segments a leaf's walk can leave in its own region of the one-pass walk;
 // a leaf with more sends the build to the counting walk and a second pass.
@@ -2319,7 +2320,7 @@ DeviceTree::~DeviceTree() {
   void *ptrs[] = {epos_, tpos_, oid_, toid_, idx_, nodes_, ppm_, chunk_node_, chunk_base_, part_,
                   left_cnt_, left_base_, scan_tmp_, node_tmp_, fallback_, counters_, leaf_ids_,
                   leaf_tmp_, leafdesc_, segs_, idx_list_, table_, items_, items_tmp_, gidx_,
-                  walk_err_, tight_chunks_, tight_nodes_, segs_local_, ridx_};
+                  tight_chunks_, tight_nodes_, segs_local_, ridx_};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h_counters_) cudaFreeHost(h_counters_);
@@ -2381,10 +2382,10 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   if (!counters_) {
     DT_CHECK(cudaMalloc(&counters_, C_COUNT * sizeof(int64_t)));
     DT_CHECK(cudaHostAlloc(&h_counters_, C_COUNT * sizeof(int64_t), cudaHostAllocDefault));
-    DT_CHECK(cudaMalloc(&walk_err_, sizeof(int32_t)));
+    // the kernels' error flag lives in a counter slot: read back with the counters
+    walk_err_ = reinterpret_cast<int32_t *>(counters_ + C_ERR);
   }
   DT_CHECK(cudaMemsetAsync(counters_, 0, C_COUNT * sizeof(int64_t), s));
-  DT_CHECK(cudaMemsetAsync(walk_err_, 0, sizeof(int32_t), s));
   if (n > 0) {
     DT_CHECK(cudaMemcpyAsync(epos_, pos_in, size_t(n) * sizeof(float4), cudaMemcpyDeviceToDevice, s));
     k_iota<<<grid_for(n, 256), 256, 0, s>>>(oid_, n);
@@ -2520,11 +2521,10 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
       ++info_.launches;
     }
     DT_CHECK(cudaGetLastError());
-    DT_CHECK(cudaMemcpyAsync(h_counters_, counters_, (C_MAXCNT + 1) * sizeof(int64_t),
+    DT_CHECK(cudaMemcpyAsync(h_counters_, counters_, (C_ERR + 1) * sizeof(int64_t),
                              cudaMemcpyDeviceToHost, s));
-    int32_t perr = 0;
-    DT_CHECK(cudaMemcpyAsync(&perr, walk_err_, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
     DT_CHECK(cudaStreamSynchronize(s));
+    const int32_t perr = *reinterpret_cast<const int32_t *>(h_counters_ + C_ERR);
     if (perr) {
       err_ = perr == 3 ? "partition: a node outgrew the one-block partition's shared memory"
                        : "partition chain check failed";
@@ -2604,13 +2604,11 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     DT_CHECK(scan_counted(list_len, list_base, nleaves, counters_ + C_NENT, scan_tmp_, s));
   }
   DT_CHECK(cudaGetLastError());
-  DT_CHECK(cudaMemcpyAsync(h_counters_ + C_NSEG, counters_ + C_NSEG, 2 * sizeof(int64_t),
-                           cudaMemcpyDeviceToHost, s));
-  DT_CHECK(cudaMemcpyAsync(h_counters_ + C_SEGOVF, counters_ + C_SEGOVF, sizeof(int64_t),
-                           cudaMemcpyDeviceToHost, s));
-  int32_t h_err = 0;
-  DT_CHECK(cudaMemcpyAsync(&h_err, walk_err_, sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  // segments, entries, the overflow flag and the error flag in one copy
+  DT_CHECK(cudaMemcpyAsync(h_counters_ + C_NSEG, counters_ + C_NSEG,
+                           (C_ERR + 1 - C_NSEG) * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
   DT_CHECK(cudaStreamSynchronize(s));
+  const int32_t h_err = *reinterpret_cast<const int32_t *>(h_counters_ + C_ERR);
   if (h_err) {
     err_ = h_err == 1 ? "interaction-list walk exceeded its stack"
                       : "interaction-list walk visited more nodes than the tree has";
