@@ -54,6 +54,8 @@ def sweep(ctx: hsr.Context, p: synth.Particles, nds=DEFAULT_NDS, iters: int = 3,
     rows = []
     for nd in nds:
         kp = synth.kick_params(p, nd=nd, **kick_kw)
+        # the first kick sizes the buffers for this leaf size; the second is timed
+        ctx.rcb_kick(p.copy(), kp, kernel=hsr.KERNEL_AUTO)
         st = ctx.rcb_kick(p.copy(), kp, kernel=hsr.KERNEL_AUTO)
         shapes = ctx.autotune(iters=iters, flush_l2=flush_l2)
         best = min(shapes, key=lambda r: r["ms"])
