@@ -547,6 +547,9 @@ def main():
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(p0, kp, args.cpu_slab, os.cpu_count() or 1)
         cpu = {k: v for k, v in cpu.items() if k not in ("seconds", "pairs")}
+        # per-core figure: one thread on a twentieth of the slab
+        one = cpu_baseline(p0, kp, args.cpu_slab / 20, 1)
+        cpu["per_core"] = {k: one[k] for k in ("value", "unit", "cores", "sample")}
 
     if rank == 0:
         line = {
