@@ -289,6 +289,22 @@ def random_box(n: int, side: float, seed: int) -> Particles:
         nglt=(int(math.ceil(side)),) * 3, meta=dict(kind="random", seed=seed))
 
 
+def sorted_line(n: int, length: float = 40.0, width: float = 0.5, seed: int = 24) -> Particles:
+    """n particles along a thin box [0, length) x [0, width)^2, sorted by x
+    with the largest x moved to the front: the partitions split along x, and
+    every level's last node has one swap chain through all of its left
+    elements (an adversarial case for the tree build's partition)."""
+    rng = np.random.default_rng(seed)
+    x = np.roll(np.sort(rng.random(n).astype(np.float32) * np.float32(length)), 1)
+    y = rng.random(n).astype(np.float32) * np.float32(width)
+    z = rng.random(n).astype(np.float32) * np.float32(width)
+    zero = np.zeros(n, np.float32)
+    return Particles(x=x, y=y, z=z, vx=zero.copy(), vy=zero.copy(), vz=zero.copy(),
+                     mass=np.ones(n, np.float32), phi=zero.copy(),
+                     id=np.arange(n, dtype=np.int64), mask=np.zeros(n, np.uint16),
+                     nglt=(int(math.ceil(length)), 1, 1), meta=dict(kind="sorted_line", seed=seed))
+
+
 @dataclass
 class KickParams:
     """RCBForceTree constructor arguments (src/halo_finder/RCBForceTree.h:96-124)."""

@@ -217,20 +217,9 @@ def test_device_build_equals_host_build(ctx, case):
     elif case == "blob_oa05":
         p, kp, _ = load_golden("blob3000_nd8_oa05_mono")
     elif case == "long_chains":
-        # sorted along the long x axis with the largest x moved to the front:
-        # every level's last node has one swap chain through all its left
-        # elements (the chunk partition's run jumps at the top levels, the
-        # one-block partition's pointer jumping below 16384 elements)
-        rng = np.random.default_rng(24)
-        n = 40000
-        x = np.roll(np.sort(rng.random(n).astype(np.float32) * np.float32(40.0)), 1)
-        y = rng.random(n).astype(np.float32) * np.float32(0.5)
-        z = rng.random(n).astype(np.float32) * np.float32(0.5)
-        zero = np.zeros(n, np.float32)
-        p = synth.Particles(x=x, y=y, z=z, vx=zero.copy(), vy=zero.copy(), vz=zero.copy(),
-                            mass=np.ones(n, np.float32), phi=zero.copy(),
-                            id=np.arange(n, dtype=np.int64), mask=np.zeros(n, np.uint16),
-                            nglt=(40, 1, 1), meta=dict(kind="chains", seed=24))
+        # the chunk partition's run jumps at the top levels, the one-block
+        # partition's pointer jumping below 16384 elements
+        p = synth.sorted_line(40000)
         kp = synth.kick_params(p, nd=64, fcoeff=1.0)
         kp.min_force, kp.max_force = (1.0, 0.0, 0.0), (39.0, 0.5, 0.5)
     else:

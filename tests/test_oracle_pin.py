@@ -29,6 +29,22 @@ def test_oracle_matches_reference_live(oracle_lib, nd, tdpts, oa):
         assert np.array_equal(getattr(q, k).view(np.uint8), ref[k].view(np.uint8)), k
 
 
+@pytest.mark.skipif(not oracle.reference_available(), reason="reference build (oracle/_ref) absent")
+def test_oracle_matches_reference_on_long_chains(oracle_lib):
+    """A node order whose partitions each carry one swap chain through all of
+    their left elements: the oracle's tree, permutation and kick against the
+    reference's."""
+    p = synth.sorted_line(20000)
+    kp = synth.kick_params(p, nd=32, fcoeff=1.0)
+    kp.min_force, kp.max_force = (1.0, 0.0, 0.0), (39.0, 0.5, 0.5)
+    q = p.copy()
+    st = oracle_lib.rcb_run(q, kp, nthreads=4).stats
+    ref, _, _ = oracle.run_reference(p, kp, nthreads=4)
+    for k in synth.FIELDS:
+        assert np.array_equal(getattr(q, k).view(np.uint8), ref[k].view(np.uint8)), k
+    assert st["processed_leaves"] > 0
+
+
 @pytest.mark.skipif(not oracle.reference_available(1), reason="RCO reference build absent")
 @pytest.mark.parametrize("nd,tdpts,oa", [(64, 1, 0.1), (16, 12, 0.5), (8, 1, 0.1)])
 def test_oracle_rco_matches_reference_live(oracle_lib, nd, tdpts, oa):
