@@ -68,9 +68,14 @@ def test_host_tree_permutation_matches_golden(hsr_lib, name):
     assert L.nleaves >= 1 or p.n == 0
 
 
-@pytest.mark.parametrize("case", ["zel16_nd32", "zel16_nd16_quad", "zel16_oa05_nd8", "random_nd1"])
+@pytest.mark.parametrize("case", ["zel16_nd32", "zel16_nd16_quad", "zel16_oa05_nd8", "random_nd1",
+                                  "long_chains"])
 def test_host_lists_equal_oracle_lists(hsr_lib, oracle_lib, case):
-    if case.startswith("zel16"):
+    if case == "long_chains":
+        p = synth.sorted_line(20000)
+        kp = synth.kick_params(p, nd=32)
+        kp.min_force, kp.max_force = (1.0, 0.0, 0.0), (39.0, 0.5, 0.5)
+    elif case.startswith("zel16"):
         p = synth.zeldovich_box(16, z=10.0, seed=4)
         nd = int(case.split("nd")[-1].split("_")[0])
         kp = synth.kick_params(p, nd=nd, tdpts=12 if "quad" in case else 1,
