@@ -48,7 +48,8 @@ import sys
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
-for _p in (os.path.join(ROOT, "hacc-coral_gb300"), os.path.join(ROOT, "oracle")):
+for _p in (os.path.join(ROOT, "hacc-coral_gb300"), os.path.join(ROOT, "oracle"),
+           os.path.join(ROOT, "tests")):
     if _p not in sys.path:
         sys.path.insert(0, _p)
 
@@ -85,15 +86,19 @@ def parse_args():
                     help="time the PM kick and one full TreePM step on the bench box (0: skip)")
     ap.add_argument("--cpu-slab", type=float, default=1.0,
                     help="fraction of the force box (along x) in the CPU sample")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the oracle / FP64 error fields of the results")
     return ap.parse_args()
 
 
-def workload(ng: int, nd: int):
+def workload(ng: int, nd: int, world: int = 1):
+    """The bench box and its `config` (the same in both arms)."""
     p = synth.zeldovich_box(ng, z=50.0)
     kp = synth.kick_params(p, nd=nd)
     cfg = {"workload": f"zeldovich{ng}_z50_nd{nd}_monopole", "n_side": ng, "n_particles": p.n,
            "nd": nd, "open_angle": kp.open_angle, "rsm": kp.rsm, "fsrrmax": kp.fsrrmax,
-           "tdpts": kp.tdpts, "law": "poly6", "fcoeff": kp.fcoeff, "l2": L2_NOTE}
+           "tdpts": kp.tdpts, "law": "poly6", "fcoeff": kp.fcoeff, "l2": L2_NOTE,
+           "parallelism": f"replicas{world}"}
     return p, kp, cfg
 
 
@@ -215,12 +220,17 @@ class ClockSampler:
 OMP_LEVELS = "1"
 
 
-def cpu_baseline(p, kp, slab: float, threads: int):
-    """Reference force tree (CPU restatement) on a slab of the force box."""
+def _oracle():
     os.environ["ORA_MAX_ACTIVE_LEVELS"] = OMP_LEVELS
     import oracle
     oracle.build()
-    O = oracle.Oracle()
+    return oracle.Oracle()
+
+
+def cpu_baseline(p, kp, slab: float, threads: int):
+    """Reference force tree (CPU restatement) on a slab of the force box.
+    `_out` holds the particles after the run (tree order, kicked)."""
+    O = _oracle()
     q = p.copy()
     ks = synth.KickParams(**{**kp.__dict__})
     lo, hi = kp.min_force[0], kp.max_force[0]
@@ -233,7 +243,132 @@ def cpu_baseline(p, kp, slab: float, threads: int):
             "sample": (f"leaves of the force box with x in [{lo:.1f}, {ks.max_force[0]:.1f}] "
                        f"({pairs:.3e} pairs, full tree built), {dt:.2f} s wall, "
                        f"OpenMP nesting capped at {OMP_LEVELS} level"),
-            "seconds": dt, "pairs": pairs}
+            "seconds": dt, "pairs": pairs, "_out": q}
+
+
+# ---- accuracy of every result: the oracle and FP64 as checkers ----------
+
+EXACT = ("x", "y", "z", "mass", "phi", "id", "mask")
+ACC_NOTE = ("rms = sqrt(sum |a - ref|^2 / sum |ref|^2), max = max_i |a_i - ref_i| / rms |ref| "
+            "over the particles of the processed leaves; targets rms <= 1e-5, max <= 1e-3")
+
+
+def _zero_v(p):
+    p.vx[:] = 0
+    p.vy[:] = 0
+    p.vz[:] = 0
+    return p
+
+
+def _vel(p):
+    return np.stack([p.vx, p.vy, p.vz], axis=1).astype(np.float64)
+
+
+def _err(a, ref):
+    from hsr_testutil import force_errors
+    rms, mx = force_errors(a, ref)
+    return {"rms": rms, "max": mx}
+
+
+def _same_arrays(a, b):
+    return all(np.array_equal(getattr(a, k).view(np.uint8), getattr(b, k).view(np.uint8))
+               for k in EXACT)
+
+
+def _oracle_check(O, z, p, kp, threads, oracle_max_x=None):
+    """Oracle run on `p` with zero velocities (tree, lists, kick) against the
+    GPU's kick `z` of the same input: the permutation bit for bit, the kick
+    against the oracle's and against FP64 over the oracle's lists (fcoeff
+    times the FP64 acceleration).  With oracle_max_x the oracle processes only
+    the leaves of the force box with x below it (the tree is still whole)."""
+    zo = _zero_v(p.copy())
+    ko = synth.KickParams(**{**kp.__dict__})
+    if oracle_max_x is not None:
+        ko.max_force = (float(oracle_max_x), kp.max_force[1], kp.max_force[2])
+    r = O.rcb_run(zo, ko, keep_lists=True, nthreads=threads)
+    off, cnt, _ = r.leaves()
+    sel = (np.concatenate([np.arange(o, o + c) for o, c in zip(off, cnt)])
+           if len(off) else np.zeros(0, np.int64))
+    a64 = r.acc_fp64()[sel] * float(np.float32(kp.fcoeff))
+    out = {"permutation_exact": _same_arrays(z, zo), "particles_checked": int(len(sel)),
+           "vs_oracle": _err(_vel(z)[sel], _vel(zo)[sel]), "vs_fp64": _err(_vel(z)[sel], a64),
+           "oracle_vs_fp64": _err(_vel(zo)[sel], a64)}
+    return out, r
+
+
+def kick_accuracy(ctx, p, kp, threads, oracle_max_x=None, kernel=None):
+    """hsr_rcb_kick of `p` with its velocities zeroed -- the output is then
+    the kick itself -- checked by _oracle_check."""
+    import hsr
+    O = _oracle()
+    z = _zero_v(p.copy())
+    st = ctx.rcb_kick(z, kp, kernel=hsr.KERNEL_AUTO if kernel is None else kernel)
+    out, r = _oracle_check(O, z, p, kp, threads, oracle_max_x)
+    if oracle_max_x is None:
+        out["pairs_equal"] = st["pairs"] == r.stats["pairs"]
+    else:
+        out["oracle_leaves"] = f"force box leaves with x < {oracle_max_x:g} (tree whole)"
+    return out
+
+
+def timed_output_check(p0, q_gpu, perm, q_ora):
+    """The last timed hsr_rcb_kick (velocities as the workload has them)
+    against the oracle's run on the same input (cpu_baseline over the whole
+    force box): the ten arrays' permutation bit for bit and the velocity
+    change v_out - v_in of every particle (input velocities taken in tree
+    order through the kick's permutation)."""
+    vin = _vel(p0)[perm]
+    return {"permutation_exact": _same_arrays(q_gpu, q_ora),
+            "dv_vs_oracle": _err(_vel(q_gpu) - vin, _vel(q_ora) - vin),
+            "note": "both add the kick into nonzero float velocities, so each carries the "
+                    "rounding of v (ulp(|v|)) besides the force error"}
+
+
+def batch_accuracy(ctx, boxes, kps, threads):
+    """The multi-box path (hsr_rcb_kick_batch, one persistent launch) on the
+    boxes with zeroed velocities, every box checked by _oracle_check; the
+    worst box's errors are reported."""
+    O = _oracle()
+    zs = [_zero_v(b.copy()) for b in boxes]
+    ctx.rcb_kick_batch(zs, kps)
+    rows = [_oracle_check(O, z, b, k, threads)[0] for z, b, k in zip(zs, boxes, kps)]
+    worst = lambda key, f: max(r[key][f] for r in rows)
+    return {"boxes_checked": len(rows),
+            "permutation_exact": all(r["permutation_exact"] for r in rows),
+            "vs_oracle": {"rms": worst("vs_oracle", "rms"), "max": worst("vs_oracle", "max")},
+            "vs_fp64": {"rms": worst("vs_fp64", "rms"), "max": worst("vs_fp64", "max")},
+            "worst_of": "max over boxes"}
+
+
+def vjp_accuracy(ctx, p, kp, u, xbar, threads, samples=64):
+    """The VJP of the last hsr_force_fwd (tape of `p`) against the FP64 VJP
+    over the same lists and FP64 central differences (h = 1e-4) at sampled
+    leaf particles (samples with a pair within 2h of the cutoff skipped)."""
+    O = _oracle()
+    n = p.n
+    perm = ctx.last_perm(n)
+    idx = ctx.lists_index()
+    off, cnt, ptr, e = ctx.lists()
+    tree = ctx.tree()
+    table = np.zeros((n + len(tree["count"]), 4), np.float32)
+    table[:n] = np.stack([p.x, p.y, p.z, p.mass], 1)[perm]
+    table[idx] = e.T
+    del e
+    xt = xbar[perm].astype(np.float64)
+    ut = u[perm].astype(np.float64)
+    c = float(np.float32(kp.fcoeff))
+    ref = O.vjp_tab(n, table, tree["offset"], tree["count"], c, off, cnt, ptr, idx, ut)
+    inleaf = np.concatenate([np.arange(o, o + k) for o, k in zip(off, cnt)])
+    smp = np.random.default_rng(10).choice(inleaf, samples, replace=False)
+    fd, near = O.fd_tab(n, table, tree["offset"], tree["count"], c, off, cnt, ptr, idx, ut, smp,
+                        h=1e-4)
+    ok = ~near.astype(bool)
+    rms_g = np.sqrt((fd[ok] ** 2).sum(1).mean())
+    scale = np.maximum(np.linalg.norm(fd[ok], axis=1), rms_g)
+    fd_err = np.linalg.norm(xt[smp][ok] - fd[ok], axis=1) / scale
+    return {"vs_fp64_vjp": _err(xt, ref), "fd_max_rel": float(fd_err.max()),
+            "fd_samples": int(ok.sum()), "fd_h": 1e-4,
+            "fd_note": "max over samples of |xbar - fd| / max(|fd|, rms fd); target <= 1e-4"}
 
 
 def hbm_roofline(traffic, ms):
@@ -369,7 +504,7 @@ def treepm_section(ctx, p0, kp, args, device: int, cpu: bool):
 def run_reference_arm(args, world, rank):
     if rank != 0:
         return 0
-    p, kp, cfg = workload(args.ng, args.nd)
+    p, kp, cfg = workload(args.ng, args.nd, world)
     threads = os.cpu_count() or 1
     for _ in range(args.warmup):
         cpu_baseline(p, kp, args.cpu_slab / 4, threads)
@@ -399,8 +534,10 @@ def main():
     import hsr
 
     kernel = {"auto": hsr.KERNEL_AUTO, "plain": hsr.KERNEL_PLAIN, "batched": hsr.KERNEL_BATCHED}[args.kernel]
-    p0, kp, cfg = workload(args.ng, args.nd)
+    p0, kp, cfg = workload(args.ng, args.nd, world)
     ctx = hsr.Context(local)
+    check = rank == 0 and not args.no_accuracy
+    threads = os.cpu_count() or 1
 
     # ---- launch shape: time every shape on this workload, keep the fastest ----
     tune_rows = None
@@ -408,7 +545,7 @@ def main():
         ctx.rcb_kick(p0.copy(), kp, kernel=kernel)
         tune_rows = [{k: (round(v, 4) if k == "ms" else v) for k, v in r.items()}
                      for r in ctx.autotune(iters=3)]
-    cfg["shape"] = ctx.get_tune()
+    shape = ctx.get_tune()
 
     # ---- end to end through the C ABI (pinned host arrays in, host arrays out) ----
     q = pinned_copy(p0)
@@ -423,6 +560,7 @@ def main():
         st = ctx.rcb_kick(q, kp, kernel=kernel)
         e2e_secs.append(time.perf_counter() - t0)
     e2e_t = max_over_ranks(world, sum(e2e_secs))
+    perm_timed = ctx.last_perm(p0.n)  # tree order of the last timed kick
     pairs = st["pairs"]
     in_cutoff = ctx.pairs_in_cutoff()
     h2d, d2h = st["h2d_bytes"], st["d2h_bytes"]
@@ -449,9 +587,11 @@ def main():
     ctx.force_vjp(u)
     vjp_ms = []
     for _ in range(3):
-        ctx.force_vjp(u)
+        xbar = ctx.force_vjp(u)
         vjp_ms.append(ctx.stats()["t_force_ms"])
     vjp_ms = min(vjp_ms)
+    vjp_acc = vjp_accuracy(ctx, p0, kp, u, xbar, threads) if check else None
+    del xbar
 
     peak = ctx.fp32_peak_tflops()
     achieved = evaluated * FLOPS_PER_PAIR / (ms * 1e-3) / 1e12
@@ -471,6 +611,8 @@ def main():
                     "one_launch_ms": ms_b, "one_launch_graph_ms": ms_bg,
                     "pairs_per_s": stb["pairs"] / (ms_b * 1e-3),
                     "e2e_s": wall_b, "e2e_pairs_per_s": stb["pairs"] / wall_b}
+        if check:
+            multibox["accuracy"] = batch_accuracy(ctx, boxes, kpb, threads)
 
     # ---- multi-step adjoint: boxes of 96^3, 10 PM steps x 5 sub-cycles ----
     multistep_line = None
@@ -520,9 +662,15 @@ def main():
         pc = synth.clustered_box(args.clustered)
         t0 = time.perf_counter()
         sw = autotune.sweep(ctx, pc, nds=(64, 128, 256), iters=2)
+        acc_c = None
+        if check:
+            # the best leaf size and shape (set on the context by the sweep)
+            kpc = synth.kick_params(pc, nd=sw["best"]["nd"])
+            acc_c = kick_accuracy(ctx, pc, kpc, threads,
+                                  oracle_max_x=kpc.min_force[0] + 6.0)
         clustered = {"n_side": args.clustered, "n_particles": pc.n,
                      "halos": pc.meta["nhalo"], "sweep_s": time.perf_counter() - t0,
-                     "best": sw["best"],
+                     "best": sw["best"], "accuracy": acc_c,
                      "rows": [{"nd": r["nd"], "pairs": r["pairs"],
                                "list_entries": r["list_entries"],
                                "tree_build_ms": round(r["tree_build_ms"], 3),
@@ -543,52 +691,87 @@ def main():
         treepm_line = treepm_section(ctx, p0, kp, args, local,
                                      cpu=(rank == 0 and world == 1 and not args.no_cpu_baseline))
 
-    cpu = None
+    cpu, ora_out = None, None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cpu = cpu_baseline(p0, kp, args.cpu_slab, os.cpu_count() or 1)
-        cpu = {k: v for k, v in cpu.items() if k not in ("seconds", "pairs")}
+        ora_out = cpu["_out"] if args.cpu_slab >= 1.0 else None
+        cpu = {k: v for k, v in cpu.items() if k not in ("seconds", "pairs", "_out")}
         # per-core figure: one thread on a twentieth of the slab
         one = cpu_baseline(p0, kp, args.cpu_slab / 20, 1)
         cpu["per_core"] = {k: one[k] for k in ("value", "unit", "cores", "sample")}
 
+    accuracy = None
+    if check:
+        accuracy = kick_accuracy(ctx, p0, kp, threads)
+        accuracy["note"] = ("the kick of the bench box with its velocities zeroed (the output is "
+                            "then the kick itself) through hsr_rcb_kick, against the oracle "
+                            "on the same input and FP64 over the oracle's lists; " + ACC_NOTE)
+        if ora_out is not None:
+            accuracy["timed_output"] = timed_output_check(p0, q, perm_timed, ora_out)
+    del ora_out
+
     if rank == 0:
+        clocks = cs.summary()
+        sms = fp32_theoretical = None
+        try:
+            import torch
+            sms = torch.cuda.get_device_properties(local).multi_processor_count
+            if clocks.get("sm_mhz"):
+                # 128 FP32 lanes per SM, one FMA (2 flops) per lane per clock
+                fp32_theoretical = sms * 128 * 2 * clocks["sm_mhz"] * 1e6 / 1e12
+        except Exception:
+            pass
+        peak_used = min(v for v in (peak, fp32_theoretical) if v) if (peak or fp32_theoretical) \
+            else None
         line = {
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
             "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Zel'dovich lattice with overload ghosts)",
-            "config": {**cfg, "pairs_per_step": pairs, "evaluated_pairs_per_step": evaluated,
+            "config": cfg,
+            "counts": {"pairs_per_step": pairs, "evaluated_pairs_per_step": evaluated,
                        "in_cutoff_pairs_per_step": in_cutoff,
+                       "in_cutoff_over_evaluated": in_cutoff / evaluated if evaluated else None,
+                       "evaluated_pairs_per_s": world * evaluated / (ms * 1e-3),
                        "processed_leaves": st["processed_leaves"],
                        "list_entries": st["list_entries"], "kernel": args.kernel,
-                       "parallelism": f"replicas{world}"},
+                       "launch_shape": shape,
+                       "value_basis": "value counts the listed pairs (what nbody1 iterates); the "
+                                      "kernel evaluates evaluated_pairs_per_step of them, the "
+                                      "rest are exactly zero by the cutoff"},
+            "accuracy": accuracy,
             "plain_vs_batched": {"plain_pairs_per_s": world * pairs / (ms_plain * 1e-3),
                                  "plain_ms": ms_plain, "selected_ms": ms,
                                  "selected_graph_ms": ms_graph,
                                  "speedup": ms_plain / ms},
-            "adjoint": {"vjp_ms": vjp_ms, "vjp_pairs_per_s": pairs / (vjp_ms * 1e-3)},
+            "adjoint": {"vjp_ms": vjp_ms, "vjp_pairs_per_s": pairs / (vjp_ms * 1e-3),
+                        "vjp_over_forward": vjp_ms / ms, "accuracy": vjp_acc},
             "multibox": multibox,
             "clustered": clustered,
             "multistep_adjoint": multistep_line,
             "treepm": treepm_line,
-            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                         "frac": achieved / peak if peak else None,
-                         "traffic": profiled_traffic(cfg["workload"], cfg["shape"]),
+            "roofline": {"bound": "fp32", "achieved": achieved, "peak": peak_used,
+                         "unit": "TFLOP/s",
+                         "frac": achieved / peak_used if peak_used else None,
+                         "traffic": profiled_traffic(cfg["workload"], shape),
                          "traffic_source": TRAFFIC_NOTE,
-                         "peak_source": "FFMA-chain probe on this device (hsr_probe_fp32_peak)",
+                         "peak_probe": peak, "peak_sm_clock_bound": fp32_theoretical, "sms": sms,
+                         "peak_source": "the lower of the FFMA-chain probe on this device "
+                                        "(hsr_probe_fp32_peak) and SMs x 128 lanes x 2 flops x "
+                                        "median SM clock of the timed region",
                          "flops_per_pair": FLOPS_PER_PAIR,
                          "pairs_basis": "evaluated pairs (after the box test)"},
-            "roofline_hbm": hbm_roofline(profiled_traffic(cfg["workload"], cfg["shape"]), ms),
+            "roofline_hbm": hbm_roofline(profiled_traffic(cfg["workload"], shape), ms),
             "cpu_baseline": cpu,
             "e2e": {"value": world * pairs * args.steps / e2e_t, "unit": UNIT,
                     "h2d_bytes_per_step": int(h2d), "d2h_bytes_per_step": int(d2h),
                     "s_per_kick": e2e_t / args.steps,
                     "tree_build_ms": st["t_build_ms"], "lists_ms": st["t_walk_ms"],
                     "h2d_ms": st["t_h2d_ms"], "force_ms": st["t_force_ms"],
-                    "d2h_ms": st["t_d2h_ms"]},
+                    "d2h_ms": st["t_d2h_ms"], "kernel_launches": st["kernel_launches"]},
             "autotune": tune_rows,
             "gpu_launches": args.steps,
-            "clocks": cs.summary(),
+            "clocks": clocks,
         }
         print(json.dumps(line), flush=True)
     ctx.close()

@@ -87,6 +87,9 @@ __global__ void __launch_bounds__(32 * kWarps)
   __shared__ float4 slot[kWarps][32];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const unsigned full = 0xffffffffu;
+  // items that did not fit: no pair is evaluated, the velocities stay as
+  // they are and the host reports the overflow
+  if (head(scr)->overflow) return;
   const unsigned long long nitems = head(scr)->reserved;
   unsigned long long evaluated = 0;
   for (;;) {
@@ -149,16 +152,19 @@ __global__ void __launch_bounds__(32 * kWarps)
 // host-side stand-in, not a device address: handing it to a kernel would
 // fault (or, where the GPU can reach host memory, silently use the wrong
 // memory).  So the first call on each device, with that device current, asks
-// the runtime for the real address once and every call passes that to the
-// kernels.
+// the runtime for the real address (set-up) and every call passes that to the
+// kernels.  Later calls ask again unless their stream is capturing, so the
+// address follows the module if the device's context was reset between calls.
 constexpr int kMaxDevices = 64;
 std::mutex g_mu;
 void *g_addr[kMaxDevices] = {};
 
-hsr_status scratch_address(int dev, void **out) {
+hsr_status scratch_address(int dev, cudaStream_t s, void **out) {
   if (dev < 0 || dev >= kMaxDevices) return HSR_ERR_UNSUPPORTED;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(s, &cap) != cudaSuccess) return HSR_ERR_CUDA;
   std::lock_guard<std::mutex> lock(g_mu);
-  if (!g_addr[dev]) {
+  if (!g_addr[dev] || cap == cudaStreamCaptureStatusNone) {
     void *p = nullptr;
     if (cudaGetSymbolAddress(&p, g_scratch) != cudaSuccess || !p) return HSR_ERR_CUDA;
     g_addr[dev] = p;
@@ -185,27 +191,29 @@ extern "C" hsr_status hsr_kick_lists_noalloc(const float *table, int64_t ntab, i
   if (nleaves > kMaxItems) return HSR_ERR_ARG;  // at least one item per leaf
   int dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess) return HSR_ERR_NO_DEVICE;
-  void *base = nullptr;
-  if (hsr_status st = scratch_address(dev, &base)) return st;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  // counters start at zero on every call (the array keeps the last call's)
+  // the scratch address and the launches are the current device's: a stream
+  // of another device is refused
+  int sdev = -1;
+  if (cudaStreamGetDevice(s, &sdev) != cudaSuccess || sdev != dev) return HSR_ERR_ARG;
+  void *base = nullptr;
+  if (hsr_status st = scratch_address(dev, s, &base)) return st;
+  // counters and the overflow flag start at zero on every call (the array
+  // keeps the last call's)
   if (cudaMemsetAsync(base, 0, sizeof(ScratchHead), s) != cudaSuccess) return HSR_ERR_CUDA;
   unsigned char *scr = static_cast<unsigned char *>(base);
   k_noalloc_items<<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(scr, leaf_offset, leaf_count,
                                                                    list_begin, list_len, nleaves);
   if (cudaGetLastError() != cudaSuccess) return HSR_ERR_CUDA;
-  ScratchHead h{};
-  if (cudaMemcpyAsync(&h, base, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
-      cudaStreamSynchronize(s) != cudaSuccess)
-    return HSR_ERR_CUDA;
-  if (h.overflow) return HSR_ERR_ARG;  // more work items than the fixed array holds
-  if (h.reserved == 0) return HSR_OK;
   const float fs2 = fsrrmax * fsrrmax;
   const float rmax = 3.116326355f, r2max = rmax * rmax;
   const float rc2 = law == HSR_LAW_POLY5_STEP16
                         ? fs2
                         : (fs2 < nextafterf(r2max, INFINITY) ? fs2 : nextafterf(r2max, INFINITY));
   const float rcull2 = rc2 * 1.0001f + 1e-6f;
+  // persistent grid from the SM count and occupancy alone: the pair kernel
+  // reads the item count (and the overflow flag) on the device, and CTAs
+  // beyond the work exit at their first queue read
   int sms = 0, per = 0;
   cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
   if (law == HSR_LAW_POLY5_STEP16)
@@ -214,9 +222,7 @@ extern "C" hsr_status hsr_kick_lists_noalloc(const float *table, int64_t ntab, i
   else
     cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, k_noalloc_pairs<hsr::LAW_POLY6>,
                                                   32 * kWarps, 0);
-  int64_t ctas = int64_t(sms > 0 ? sms : 1) * (per > 0 ? per : 1);
-  const int64_t need = (int64_t(h.reserved) + kWarps - 1) / kWarps;
-  if (ctas > need) ctas = need;
+  const int64_t ctas = int64_t(sms > 0 ? sms : 1) * (per > 0 ? per : 1);
   const float4 *tab = reinterpret_cast<const float4 *>(table);
   if (law == HSR_LAW_POLY5_STEP16)
     k_noalloc_pairs<hsr::LAW_POLY5_STEP16><<<unsigned(ctas), 32 * kWarps, 0, s>>>(
@@ -225,6 +231,12 @@ extern "C" hsr_status hsr_kick_lists_noalloc(const float *table, int64_t ntab, i
     k_noalloc_pairs<hsr::LAW_POLY6><<<unsigned(ctas), 32 * kWarps, 0, s>>>(
         scr, tab, list_index, vx, vy, vz, fcoeff, rsm * rsm, rc2, rcull2);
   if (cudaGetLastError() != cudaSuccess) return HSR_ERR_CUDA;
-  if (cudaStreamSynchronize(s) != cudaSuccess) return HSR_ERR_CUDA;
+  // the overflow flag comes back once the kernels are done (a copy into host
+  // stack memory, which waits for the stream)
+  ScratchHead h{};
+  if (cudaMemcpyAsync(&h, base, sizeof(h), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+      cudaStreamSynchronize(s) != cudaSuccess)
+    return HSR_ERR_CUDA;
+  if (h.overflow) return HSR_ERR_ARG;  // more work items than the fixed array holds
   return HSR_OK;
 }

@@ -5,6 +5,8 @@
 #include <cmath>
 #include <vector>
 
+#include "device_info.cuh"
+
 namespace hsr_pm {
 
 namespace {
@@ -39,7 +41,8 @@ bool fft_ok(cufftResult r, const char *what, std::string *err) {
 
 int blocks_for(int64_t n) {
   int64_t b = (n + kThreads - 1) / kThreads;
-  return int(b < 152 * 64 ? (b > 0 ? b : 1) : 152 * 64);
+  const int64_t cap = int64_t(hsr::sm_count()) * 64;
+  return int(b < cap ? (b > 0 ? b : 1) : cap);
 }
 
 template <typename T> struct Cplx;

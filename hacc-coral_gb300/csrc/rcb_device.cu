@@ -1,6 +1,7 @@
 // rcb_device.cu -- RCB tree, interaction lists and batched work items built on
 // the GPU (see rcb_device.cuh for the method).
 #include "rcb_device.cuh"
+#include "device_info.cuh"
 
 #include <algorithm>
 #include <chrono>
@@ -755,7 +756,8 @@ __global__ void k_stats_final_one(DNode *nodes, int32_t nb, int32_t ne, const in
 constexpr int kTightChunk = 2048;   // elements per chunk (8 per thread)
 constexpr int kTightThreads = 256;
 constexpr int kTightNodes = 64;     // fallback nodes per level taken by this pass
-constexpr int kTightBlocks = 152 * 2;
+// blocks of the tight-certification passes: two per SM (grid-stride over chunks)
+inline unsigned tight_blocks() { return unsigned(2 * sm_count()); }
 
 struct TightChunk {  // per chunk of a listed node
   double hi[4], lo[4];  // double-double sum of the chunk's terms (x, y, z, m)
@@ -2305,7 +2307,8 @@ __global__ void k_root(DNode *nodes, int64_t n, TreeConfig cfg) {
   R.nleft = 0;
 }
 
-inline unsigned grid_for(int64_t n, int threads, int64_t cap = 152 * 32) {
+inline unsigned grid_for(int64_t n, int threads, int64_t cap = 0) {
+  if (cap <= 0) cap = int64_t(sm_count()) * 32;
   int64_t b = (n + threads - 1) / threads;
   return unsigned(std::max<int64_t>(1, std::min(b, cap)));
 }
@@ -2468,11 +2471,11 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
           small);
       ++info_.launches;
     }
-    k_cm_tight_sums<<<kTightBlocks, kTightThreads, 0, s>>>(
+    k_cm_tight_sums<<<tight_blocks(), kTightThreads, 0, s>>>(
         epos_, nodes_, fallback_, counters_, reinterpret_cast<TightChunk *>(tight_chunks_),
         reinterpret_cast<TightNode *>(tight_nodes_), cfg.force_cm_fallback == 1);
     ++info_.launches;
-    k_cm_tight_bound<<<kTightBlocks, kTightThreads, 0, s>>>(
+    k_cm_tight_bound<<<tight_blocks(), kTightThreads, 0, s>>>(
         epos_, nodes_, fallback_, counters_, reinterpret_cast<const TightChunk *>(tight_chunks_),
         reinterpret_cast<TightNode *>(tight_nodes_), cfg.force_cm_fallback == 1);
     ++info_.launches;
@@ -2628,14 +2631,14 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
           walk_err_, counters_);
       ++info_.launches;
     } else {
-      k_pack_segs<<<unsigned(std::min<int64_t>((nleaves + 7) / 8, 152 * 64)), 256, 0, s>>>(
+      k_pack_segs<<<unsigned(std::min<int64_t>((nleaves + 7) / 8, int64_t(sm_count()) * 64)), 256, 0, s>>>(
           segs_local_, seg_cnt, seg_base, list_base, nleaves, segs_);
       ++info_.launches;
     }
     int64_t *kept = nullptr;
     if (cfg.prune2 > 0.0f) {
       kept = node_tmp_ + 4 * nlw;
-      int64_t blocks = std::min<int64_t>((nleaves + 7) / 8, 152 * 64);
+      int64_t blocks = std::min<int64_t>((nleaves + 7) / 8, int64_t(sm_count()) * 64);
       k_expand_pruned<<<unsigned(blocks), 256, 0, s>>>(segs_, seg_base, seg_cnt, list_base, nodes_,
                                                        leaf_ids_, nleaves, table_, cfg.prune2,
                                                        idx_list_, kept);

@@ -1,5 +1,6 @@
 // sr_kernels.cu -- sm_103a kernels of the short-range pair interaction.
 #include "sr_kernels.cuh"
+#include "device_info.cuh"
 
 #include <algorithm>
 #include <cmath>
@@ -25,7 +26,7 @@ cudaError_t launch_expand_segments(const SegDesc *segs, int64_t nsegs, int32_t *
                                    cudaStream_t s) {
   if (nsegs <= 0) return cudaSuccess;
   int64_t blocks = (nsegs + 7) / 8;
-  if (blocks > 152 * 64) blocks = 152 * 64;
+  if (blocks > int64_t(sm_count()) * 64) blocks = int64_t(sm_count()) * 64;
   k_expand_segments<<<unsigned(blocks), 256, 0, s>>>(segs, nsegs, idx);
   return cudaGetLastError();
 }
@@ -66,7 +67,8 @@ cudaError_t launch_count_in_cutoff(const float4 *pos, const LeafDesc *leaves, in
                                    const int32_t *idx, float rcut2, unsigned long long *count,
                                    cudaStream_t s) {
   if (nleaves <= 0) return cudaSuccess;
-  const int64_t blocks = nleaves < 152 * 16 ? nleaves : 152 * 16;
+  const int64_t cap = int64_t(sm_count()) * 16;
+  const int64_t blocks = nleaves < cap ? nleaves : cap;
   k_count_in_cutoff<<<unsigned(blocks), 128, 0, s>>>(pos, leaves, nleaves, idx, rcut2, count);
   return cudaGetLastError();
 }
@@ -451,7 +453,7 @@ cudaError_t launch_tag_items(const PairItem *in, PairItem *out, int64_t n, int b
                              cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   int64_t blocks = (n + 255) / 256;
-  if (blocks > 152 * 8) blocks = 152 * 8;
+  if (blocks > int64_t(sm_count()) * 8) blocks = int64_t(sm_count()) * 8;
   k_tag_items<<<unsigned(blocks), 256, 0, s>>>(in, out, n, box);
   return cudaGetLastError();
 }
@@ -680,7 +682,7 @@ cudaError_t launch_force_law(int law, const float *r2, float *g, int64_t n, floa
                              cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
   int64_t blocks = (n + 255) / 256;
-  if (blocks > 152 * 16) blocks = 152 * 16;
+  if (blocks > int64_t(sm_count()) * 16) blocks = int64_t(sm_count()) * 16;
   if (law == LAW_POLY5_STEP16)
     k_force_law<LAW_POLY5_STEP16><<<unsigned(blocks), 256, 0, s>>>(r2, g, n, rsm2, rcut2);
   else

@@ -7,6 +7,7 @@
 #include <algorithm>
 
 #include "rcb_device.cuh"
+#include "device_info.cuh"
 
 namespace hsr {
 
@@ -137,7 +138,7 @@ __global__ void k_fill_f32(float *p, int64_t n, float v) {
 
 inline unsigned grid_of(int64_t n, int threads = 256) {
   int64_t b = (n + threads - 1) / threads;
-  return unsigned(std::max<int64_t>(1, std::min<int64_t>(b, 152 * 32)));
+  return unsigned(std::max<int64_t>(1, std::min<int64_t>(b, int64_t(sm_count()) * 32)));
 }
 
 }  // namespace

@@ -21,6 +21,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB_PATH = os.path.join(HERE, "lib", "libhacc_sr.so")
 
 HSR_OK = 0
+(HSR_ERR_ARG, HSR_ERR_CUDA, HSR_ERR_NOMEM, HSR_ERR_TIMEOUT, HSR_ERR_UNSUPPORTED,
+ HSR_ERR_NO_DEVICE, HSR_ERR_STATE) = range(1, 8)
 STATUS = {0: "ok", 1: "invalid argument", 2: "CUDA error", 3: "out of memory",
           4: "device wait timed out", 5: "unsupported", 6: "no CUDA device", 7: "bad call order"}
 MEM_HOST, MEM_DEVICE = 0, 1

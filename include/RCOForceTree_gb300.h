@@ -9,25 +9,15 @@
  * the host (every inner node split along all three axes at its centre of
  * mass, the ten particle arrays permuted), the lists of the leaves inside the
  * force box are built there, and the pairs run on the GPU.  The reference
- * takes the softening from its ForceLaw object; this header cannot look
- * inside one, so the caller states it once per thread with
- * hacc_sr_gb300::set_rco_softening (Particles.cxx's m_rsm; 0.1 if unset).
+ * takes the softening from its ForceLaw object (the constructor has no rsm
+ * argument); this header reads it off the law, f_over_r(0) = rsm^-3 - a_0,
+ * and then checks the law as RCBForceTree_gb300.h does: anything but the
+ * polynomial short-range law (HACC option -P) throws.
  */
 #ifndef RCOFORCETREE_GB300_H
 #define RCOFORCETREE_GB300_H
 
 #include "RCBForceTree_gb300.h"
-
-namespace hacc_sr_gb300 {
-
-inline float &rco_softening_slot() {
-  static thread_local float rsm = 0.1f;
-  return rsm;
-}
-// Softening (rsm) of the ForceLawSR the RCOForceTree calls of this thread pass.
-inline void set_rco_softening(float rsm) { rco_softening_slot() = rsm; }
-
-}  // namespace hacc_sr_gb300
 
 template <int TDPTS>
 class RCOForceTree {
@@ -41,6 +31,12 @@ class RCOForceTree {
       throw std::runtime_error(
           "RCOForceTree (GB300): fl == 0 selects the Newtonian law, which is not the "
           "short-range path this build implements");
+    const float rsm = hacc_sr_gb300::law_softening(fl);
+    if (!(rsm > 0.f))
+      throw std::runtime_error(
+          "RCOForceTree (GB300): the ForceLaw has no finite softening at r2 = 0; this library "
+          "implements the polynomial short-range law (ForceLawSR over FGridEvalPoly) only");
+    hacc_sr_gb300::require_poly6_law(fl, rsm, "RCOForceTree (GB300)");
     hsr_params p{};
     for (int i = 0; i < 3; ++i) {
       p.min[i] = minLoc[i];
@@ -50,7 +46,7 @@ class RCOForceTree {
     }
     p.avg_mass = avgMass;
     p.fsrrmax = fsm;
-    p.rsm = hacc_sr_gb300::rco_softening_slot();
+    p.rsm = rsm;
     p.open_angle = oa;
     p.nd = nd;
     p.ds = ds;

@@ -342,11 +342,16 @@ hsr_status hsr_force_law(hsr_ctx *ctx, int32_t law, float rsm, float fsrrmax, in
  * scratch (work items and counters) lives in a fixed 4 MiB device array that
  * every device loading the library holds until the process exits; lists that
  * need more than 131064 work items (one per group of up to 32 leaf particles
- * per 8192 list entries) are rejected with HSR_ERR_ARG before any pair is
- * evaluated.  The first call on a device looks up that array's device address
- * (set-up); make that first call before any stream capture.  Calls share the
- * array: calls that overlap on the GPU race and must not be issued
- * concurrently.  The call waits for its stream (NULL: the default stream). */
+ * per 8192 list entries) are rejected with HSR_ERR_ARG and no pair is
+ * evaluated (the velocities are left as they were).  The first call on a
+ * device looks up that array's device address (set-up); make that first call
+ * before any stream capture.  Later calls look the address up again unless
+ * their stream is capturing.  Calls share the array, which keeps the last
+ * call's contents (each call clears its counters first): calls that overlap
+ * on the GPU race and must not be issued concurrently.  `stream` (NULL: the
+ * default stream) must belong to the current device, else HSR_ERR_ARG.  The
+ * call returns after its work on the stream has finished: it synchronizes
+ * the stream to read the overflow flag back. */
 hsr_status hsr_kick_lists_noalloc(const float *table, int64_t ntab, int64_t n,
                                   const int32_t *leaf_offset, const int32_t *leaf_count,
                                   const int64_t *list_begin, const int32_t *list_len,

@@ -33,11 +33,27 @@ LAW_POLY5_STEP16 = 1
 ERRORS = {1: "bad argument", 2: "interaction list reached VMAX", 3: "out of memory"}
 
 
-def build(ref: bool = False) -> None:
-    """Compiles the restatement (and the reference build when asked and the
-    reference sources are present)."""
-    targets = ["all"] + (["ref"] if ref else [])
-    subprocess.run(["make", "-s", "-C", HERE] + targets, check=True)
+# Where the reference tree is looked for when HSR_REFERENCE_ROOT is unset.
+_REFERENCE_CHECKOUT = "/root/reference"
+
+
+def reference_root() -> str:
+    """Root of the reference tree (the directory holding src/halo_finder):
+    $HSR_REFERENCE_ROOT, else the checkout beside this repository when it
+    exists, else "" (machines that only receive this repository)."""
+    root = os.environ.get("HSR_REFERENCE_ROOT", "")
+    if not root and os.path.isfile(os.path.join(_REFERENCE_CHECKOUT, "src", "halo_finder",
+                                                "RCBForceTree.cxx")):
+        root = _REFERENCE_CHECKOUT
+    return root
+
+
+def build(ref: bool = False, ref_if_present: bool = False) -> None:
+    """Compiles the restatement; with `ref` also the reference build (the
+    reference tree must exist), with `ref_if_present` the reference build
+    where the tree exists."""
+    targets = ["all"] + (["ref"] if ref else ["ref-if-present"] if ref_if_present else [])
+    subprocess.run(["make", "-s", "-C", HERE, f"REF={reference_root()}"] + targets, check=True)
 
 
 class OraParams(C.Structure):

@@ -2,9 +2,9 @@
 C ABI and prints each call's phase statistics as JSON: a fixed, short launch
 sequence for profilers (ncu's launch lists and kernel captures).
 
-    python hacc-coral_gb300/profile_kick.py --workload zeldovich --ng 128 --reps 2
-    python hacc-coral_gb300/profile_kick.py --workload clustered --ng 256 --shape batched-32
-    python hacc-coral_gb300/profile_kick.py --ng 128 --reps 2 --pm f64   # + the PM kick
+    python profile_kick.py --workload zeldovich --ng 128 --reps 2
+    python profile_kick.py --workload clustered --ng 256 --shape batched-32
+    python profile_kick.py --ng 128 --reps 2 --pm f64   # + the PM kick
 """
 from __future__ import annotations
 
@@ -13,7 +13,7 @@ import json
 import os
 import sys
 
-HERE = os.path.dirname(os.path.abspath(__file__))
+HERE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "hacc-coral_gb300")
 if HERE not in sys.path:
     sys.path.insert(0, HERE)
 

@@ -73,3 +73,43 @@ def same_lists(a_off, a_cnt, a_ptr, a_e, b_off, b_cnt, b_ptr, b_e):
         if ea.shape != eb.shape or not np.array_equal(sorted_rows(ea), sorted_rows(eb)):
             return False
     return True
+
+
+def _leaf_major(off, ptr, e):
+    """Entries (4 x m) regrouped leaf by leaf in order of leaf offset, with
+    the leaf rank of every entry."""
+    k = np.argsort(off, kind="stable")
+    lens = np.diff(ptr)[k]
+    starts = ptr[:-1][k]
+    total = int(lens.sum())
+    first = np.cumsum(lens) - lens
+    idx = np.repeat(starts - first, lens) + np.arange(total, dtype=np.int64)
+    return k, e[:, idx], np.repeat(np.arange(len(k), dtype=np.int64), lens)
+
+
+def same_lists_exact(a_off, a_cnt, a_ptr, a_e, b_off, b_cnt, b_ptr, b_e):
+    """same_lists for lists of any size (vectorised): True when both sets name
+    the same leaves (offset and count) with the same multiset of entries per
+    leaf, bit for bit.  Entries in the same order compare directly; otherwise
+    each leaf's entries are sorted by their bits first."""
+    if len(a_off) != len(b_off) or a_e.shape != b_e.shape:
+        return False
+    ka, ea, la = _leaf_major(a_off, a_ptr, a_e)
+    kb, eb, lb = _leaf_major(b_off, b_ptr, b_e)
+    if not (np.array_equal(a_off[ka], b_off[kb]) and np.array_equal(a_cnt[ka], b_cnt[kb])
+            and np.array_equal(np.diff(a_ptr)[ka], np.diff(b_ptr)[kb])):
+        return False
+    ua, ub = ea.view(np.uint32), eb.view(np.uint32)
+    if np.array_equal(ua, ub):
+        return True
+
+    def by_bits(u, leaf):
+        w = u.astype(np.uint64)
+        k1 = (w[0] << np.uint64(32)) | w[1]
+        k2 = (w[2] << np.uint64(32)) | w[3]
+        o = np.lexsort((k2, k1, leaf))
+        return k1[o], k2[o]
+
+    a1, a2 = by_bits(ua, la)
+    b1, b2 = by_bits(ub, lb)
+    return bool(np.array_equal(a1, b1) and np.array_equal(a2, b2))

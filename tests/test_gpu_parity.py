@@ -10,7 +10,7 @@ import pytest
 import hsr
 import synth
 from hsr_testutil import (MAX_TOL, RMS_TOL, force_errors, golden_names, load_golden,
-                          same_lists, vel)
+                          same_lists, same_lists_exact, vel)
 
 pytestmark = pytest.mark.gpu
 
@@ -191,6 +191,36 @@ def test_full_size_128_sampled_leaves_vs_fp64(ctx):
     rms, mx = force_errors(np.concatenate(a_gpu), np.concatenate(a64))
     assert rms <= RMS_TOL and mx <= MAX_TOL, (rms, mx)
     assert st["pairs"] > 1e9
+
+
+def test_full_size_128_vs_oracle(ctx, oracle_lib, monkeypatch):
+    """The bench workload itself -- 128^3 Zel'dovich at z = 50 with overload
+    ghosts (2.57 M particles), nd = 128, opening angle 0.1, rsm = 0.1, poly6,
+    monopole -- through hsr_rcb_kick against the oracle run on the same input:
+    the permutation of x, y, z, mass, phi, id and mask bit for bit, every
+    processed leaf's list the same multiset of entries bit for bit, the same
+    pair count, and the kick within RMS_TOL / MAX_TOL of the oracle's and of
+    FP64 over the same lists."""
+    monkeypatch.setenv("ORA_MAX_ACTIVE_LEVELS", "1")  # the oracle's nesting; same results
+    p = _zero_v(synth.zeldovich_box(128))
+    kp = synth.kick_params(p, nd=128, fcoeff=1.0)
+    q = p.copy()
+    st = ctx.rcb_kick(p, kp)
+    r = oracle_lib.rcb_run(q, kp, keep_lists=True, nthreads=0)
+    for k in EXACT:
+        assert np.array_equal(getattr(p, k).view(np.uint8), getattr(q, k).view(np.uint8)), k
+    assert st["pairs"] == r.stats["pairs"] and st["pairs"] > 5e9
+    assert st["list_entries"] == r.stats["list_entries"]
+    assert st["processed_leaves"] == r.stats["processed_leaves"]
+    off, cnt, ptr = r.leaves()
+    goff, gcnt, gptr, ge = ctx.lists()
+    assert same_lists_exact(goff, gcnt, gptr, ge, off, cnt, ptr, r.entries())
+    del ge
+    sel = np.concatenate([np.arange(o, o + c) for o, c in zip(off, cnt)])
+    rms, mx = force_errors(vel(p)[sel], vel(q)[sel])
+    assert rms <= RMS_TOL and mx <= MAX_TOL, (rms, mx)
+    rms64, mx64 = force_errors(vel(p)[sel], r.acc_fp64()[sel])
+    assert rms64 <= RMS_TOL and mx64 <= MAX_TOL, (rms64, mx64)
 
 
 def _g64(r2, rsm=float(np.float32(0.1))):

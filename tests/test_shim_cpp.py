@@ -22,7 +22,8 @@ SRC = os.path.join(ROOT, "tests", "cpp", "shim_driver.cpp")
 def shim_exe(hsr_lib, tmp_path_factory):
     exe = str(tmp_path_factory.mktemp("shim") / "shim_driver")
     libdir = os.path.dirname(hsr.LIB_PATH)
-    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"), SRC, "-o", exe,
+    subprocess.run(["g++", "-O2", "-std=c++17", "-I", os.path.join(ROOT, "include"),
+                    "-I", os.path.dirname(SRC), SRC, "-o", exe,
                     "-L", libdir, "-lhacc_sr", f"-Wl,-rpath,{libdir}"], check=True)
     return exe
 
@@ -42,6 +43,25 @@ def test_shim_reports_missing_device(shim_exe, tmp_path):
     oracle.write_case(cin, p, kp)
     r = subprocess.run([shim_exe, cin, cout], capture_output=True, text=True)
     assert r.returncode == 3 and "hsr_create" in r.stderr
+
+
+@pytest.mark.parametrize("tree,law", [(0, "fit"), (0, "rsm"), (0, "newton"), (1, "fit"),
+                                      (1, "newton")])
+def test_shim_refuses_other_force_laws(shim_exe, tmp_path, law, tree):
+    """HACC without -P passes ForceLawSR over FGridEvalFit (Particles.cxx:
+    173-183): the drop-in trees throw before any device work instead of
+    running the polynomial law in its place; so does a Newtonian law, and
+    RCBForceTree given a polynomial law at another softening than its `r`.
+    (RCOForceTree has no softening argument: it takes the law's own.)"""
+    p, kp, _ = load_golden(golden_names()[0])
+    kp.tree = tree
+    cin, cout = str(tmp_path / "in.bin"), str(tmp_path / "out.bin")
+    oracle.write_case(cin, p, kp)
+    r = subprocess.run([shim_exe, cin, cout, law], capture_output=True, text=True)
+    assert r.returncode == 3, (r.returncode, r.stderr)
+    assert ("not the polynomial short-range law" in r.stderr
+            or "no finite softening" in r.stderr), r.stderr
+    assert not os.path.exists(cout)
 
 
 @pytest.mark.gpu
