@@ -293,7 +293,7 @@ def _oracle_check(O, z, p, kp, threads, oracle_max_x=None):
     out = {"permutation_exact": _same_arrays(z, zo), "particles_checked": int(len(sel)),
            "vs_oracle": _err(_vel(z)[sel], _vel(zo)[sel]), "vs_fp64": _err(_vel(z)[sel], a64),
            "oracle_vs_fp64": _err(_vel(zo)[sel], a64)}
-    return out, r
+    return out, r, sel, a64
 
 
 def kick_accuracy(ctx, p, kp, threads, oracle_max_x=None, kernel=None):
@@ -303,25 +303,28 @@ def kick_accuracy(ctx, p, kp, threads, oracle_max_x=None, kernel=None):
     O = _oracle()
     z = _zero_v(p.copy())
     st = ctx.rcb_kick(z, kp, kernel=hsr.KERNEL_AUTO if kernel is None else kernel)
-    out, r = _oracle_check(O, z, p, kp, threads, oracle_max_x)
+    out, r, sel, a64 = _oracle_check(O, z, p, kp, threads, oracle_max_x)
     if oracle_max_x is None:
         out["pairs_equal"] = st["pairs"] == r.stats["pairs"]
     else:
         out["oracle_leaves"] = f"force box leaves with x < {oracle_max_x:g} (tree whole)"
-    return out
+    return out, sel, a64
 
 
-def timed_output_check(p0, q_gpu, perm, q_ora):
+def timed_output_check(p0, q_gpu, perm, q_ora, sel, a64):
     """The last timed hsr_rcb_kick (velocities as the workload has them)
     against the oracle's run on the same input (cpu_baseline over the whole
-    force box): the ten arrays' permutation bit for bit and the velocity
-    change v_out - v_in of every particle (input velocities taken in tree
-    order through the kick's permutation)."""
+    force box) and against FP64: the ten arrays' permutation bit for bit and
+    the velocity change v_out - v_in of the processed leaves' particles
+    (input velocities taken in tree order through the kick's permutation)."""
     vin = _vel(p0)[perm]
+    dv = _vel(q_gpu) - vin
     return {"permutation_exact": _same_arrays(q_gpu, q_ora),
-            "dv_vs_oracle": _err(_vel(q_gpu) - vin, _vel(q_ora) - vin),
-            "note": "both add the kick into nonzero float velocities, so each carries the "
-                    "rounding of v (ulp(|v|)) besides the force error"}
+            "dv_vs_fp64": _err(dv[sel], a64), "dv_vs_oracle": _err(dv[sel], (_vel(q_ora) - vin)[sel]),
+            "oracle_dv_vs_fp64": _err((_vel(q_ora) - vin)[sel], a64),
+            "note": "v_out = v_in + kick in float: the library rounds once per particle, the "
+                    "reference (oracle) once per pair term, so the oracle's dv carries ~sqrt(list "
+                    "length) roundings of ulp(|v|) besides the force error"}
 
 
 def batch_accuracy(ctx, boxes, kps, threads):
@@ -667,7 +670,7 @@ def main():
             # the best leaf size and shape (set on the context by the sweep)
             kpc = synth.kick_params(pc, nd=sw["best"]["nd"])
             acc_c = kick_accuracy(ctx, pc, kpc, threads,
-                                  oracle_max_x=kpc.min_force[0] + 6.0)
+                                  oracle_max_x=kpc.min_force[0] + 6.0)[0]
         clustered = {"n_side": args.clustered, "n_particles": pc.n,
                      "halos": pc.meta["nhalo"], "sweep_s": time.perf_counter() - t0,
                      "best": sw["best"], "accuracy": acc_c,
@@ -702,12 +705,13 @@ def main():
 
     accuracy = None
     if check:
-        accuracy = kick_accuracy(ctx, p0, kp, threads)
+        accuracy, sel0, a64_0 = kick_accuracy(ctx, p0, kp, threads)
         accuracy["note"] = ("the kick of the bench box with its velocities zeroed (the output is "
                             "then the kick itself) through hsr_rcb_kick, against the oracle "
                             "on the same input and FP64 over the oracle's lists; " + ACC_NOTE)
         if ora_out is not None:
-            accuracy["timed_output"] = timed_output_check(p0, q, perm_timed, ora_out)
+            accuracy["timed_output"] = timed_output_check(p0, q, perm_timed, ora_out, sel0, a64_0)
+        del sel0, a64_0
     del ora_out
 
     if rank == 0:

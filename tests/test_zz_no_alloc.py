@@ -31,6 +31,9 @@ def _case():
 def _dense_case():
     """40 000 particles in an 8^3 box: every list holds 9 000 to 37 000 entries."""
     p = synth.random_box(40000, 8.0, 5)
+    p.vx[:] = 0
+    p.vy[:] = 0
+    p.vz[:] = 0
     kp = synth.kick_params(p, nd=64, fcoeff=0.5)
     kp.min_force, kp.max_force = (-1.0,) * 3, (9.0,) * 3
     return p, kp
