@@ -455,7 +455,7 @@ def treepm_section(ctx, p0, kp, args, device: int, cpu: bool):
     nsub = 5
     ts_mid = treepm.plan(50.0, 10.0, 10)[0].mid
     kp_sub = dataclasses.replace(kp, fcoeff=float(synth.kick_coefficient(ts_mid, nsub)))
-    tau_sub = float(np.float32(ts_mid.tau2 / nsub))
+    tau_sub = float(synth.stream_tau(ts_mid, nsub))
     ctx.subcycle(p0.copy(), kp_sub, nsub, p0.nglt, ts_mid.alpha, ts_mid.pp, tau_sub, ts_mid.adot)
     sub_runs = []
     for _ in range(2):

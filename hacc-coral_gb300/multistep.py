@@ -62,14 +62,14 @@ class StepParams:
 
 def schedule(z_in: float, z_fin: float, nsteps: int, nsub: int) -> List[StepParams]:
     """PM steps from z_in to z_fin (the reference's TimeStepper)."""
-    ts0 = synth.stepper(z_in=z_in, z_fin=z_fin, nsteps=nsteps)
+    ts = synth.stepper(z_in=z_in, z_fin=z_fin, nsteps=nsteps)
     out = []
     for s in range(nsteps):
-        ts = synth.Stepper(alpha=ts0.alpha, pp=ts0.pp + s * ts0.tau + ts0.tau2,
-                           omegatot=ts0.omegatot, tau=ts0.tau)
-        out.append(StepParams(alpha=ts.alpha, pp=ts.pp, adot=ts.adot,
-                              tau_sub=float(np.float32(ts.tau2 / nsub)),
-                              fcoeff=float(synth.kick_coefficient(ts, nsub))))
+        mid = ts.advanced(1)  # the sub-cycles run at mid-step (pp += tau2)
+        out.append(StepParams(alpha=mid.alpha, pp=mid.pp, adot=mid.adot,
+                              tau_sub=float(synth.stream_tau(mid, nsub)),
+                              fcoeff=float(synth.kick_coefficient(mid, nsub))))
+        ts = mid.advanced(1)
     return out
 
 

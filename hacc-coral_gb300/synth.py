@@ -30,7 +30,9 @@ import numpy as np
 RMAX = np.float32(3.116326355)
 # indat values used by every reference example (indat:24-25, 36-41).
 OMEGA_DM = 0.23387755
-OMEGA_B = 0.0226 / 0.7 ** 2
+DEUT = 0.0226
+HUBBLE = 0.7
+OMEGA_B = DEUT / HUBBLE ** 2
 OVERLOAD_MPC = 8.0
 EDGE = 3.2
 
@@ -76,7 +78,9 @@ FIELDS = ("x", "y", "z", "vx", "vy", "vz", "mass", "phi", "id", "mask")
 
 
 # ---------------------------------------------------------------------------
-# TimeStepper scalars (src/simulation/TimeStepper.cxx:1-65), alpha = 1.
+# TimeStepper scalars (src/simulation/TimeStepper.cxx:1-88): double members;
+# the run's stepper is built from Basedata's float members
+# (src/initializer/Basedata.h:133-140, driver_hires.cxx:269-270).
 # ---------------------------------------------------------------------------
 
 @dataclass
@@ -85,6 +89,14 @@ class Stepper:
     pp: float
     omegatot: float
     tau: float
+
+    def advanced(self, halves: int = 1) -> "Stepper":
+        """The stepper after `halves` calls of advanceHalfStep: pp += tau2
+        each time, accumulated in double as the reference does."""
+        pp = self.pp
+        for _ in range(halves):
+            pp += self.tau2
+        return Stepper(alpha=self.alpha, pp=pp, omegatot=self.omegatot, tau=self.tau)
 
     @property
     def aa(self) -> float:
@@ -106,21 +118,39 @@ class Stepper:
         return 0.5 * self.tau
 
 
-def stepper(z_in: float = 50.0, z_fin: float = 20.0, nsteps: int = 3) -> Stepper:
-    """TimeStepper at the start of the run, as the reference constructs it."""
-    a_in, a_fin = 1.0 / (1.0 + z_in), 1.0 / (1.0 + z_fin)
-    return Stepper(alpha=1.0, pp=a_in, omegatot=OMEGA_DM + OMEGA_B,
-                   tau=(a_fin - a_in) / nsteps)
+def stepper(z_in: float = 50.0, z_fin: float = 20.0, nsteps: int = 3, alpha: float = 1.0,
+            omegadm: float = OMEGA_DM, deut: float = DEUT, hubble: float = HUBBLE) -> Stepper:
+    """TimeStepper at the start of the run, as driver_hires.cxx:269-270 builds
+    it from Basedata: the indat values are floats, ain = 1.0 / (1 + zin) and
+    omegatot = omegadm + deut / hubble / hubble are rounded to float
+    (Basedata.h:133-137); the stepper itself computes in double
+    (TimeStepper.cxx:3-38)."""
+    f = np.float32
+    ain = float(f(1.0 / float(f(1.0) + f(z_in))))
+    afin = float(f(1.0 / float(f(1.0) + f(z_fin))))
+    omegatot = float(f(f(omegadm) + f(f(deut) / f(hubble)) / f(hubble)))
+    a = float(f(alpha))
+    pin, pfin = ain ** a, afin ** a
+    return Stepper(alpha=a, pp=pin, omegatot=omegatot, tau=(pfin - pin) / (1.0 * nsteps))
 
 
 def kick_coefficient(ts: Stepper, nsub: int, gpscal: float = 1.0) -> np.float32:
-    """c = gpscal^3/(4 pi) * fscal * tau * stepFraction (Particles.cxx:1230-1233),
-    evaluated in float like the reference."""
-    divscal = np.float32(gpscal) ** 3
-    pi = np.float32(4.0 * math.atan(1.0))
-    c = (np.float32(divscal) / np.float32(4.0) / pi * np.float32(ts.fscal)
-         * np.float32(ts.tau) * np.float32(1.0 / nsub))
-    return np.float32(c)
+    """map2's c = divscal / 4.0 / pi * fscal * tau * stepFraction
+    (Particles.cxx:1229-1233): divscal = gpscal^3 and pi = 4.0 * atanf(1.0)
+    are floats, the product runs in double from `/ 4.0` on (stepFraction =
+    1.0 / nsub from subCycle, :1179), and c is stored as a float."""
+    f = np.float32
+    g = f(gpscal)
+    divscal = g * g * g
+    pi = f(4.0 * float(f(math.atan(1.0))))
+    c = float(divscal) / 4.0 / float(pi) * ts.fscal * ts.tau * (1.0 / nsub)
+    return f(c)
+
+
+def stream_tau(ts: Stepper, nsub: int) -> np.float32:
+    """map1's tau argument in subCycle: stepFraction * tau2 in double, passed
+    as a float (Particles.cxx:1179-1185)."""
+    return np.float32((1.0 / nsub) * ts.tau2)
 
 
 # ---------------------------------------------------------------------------

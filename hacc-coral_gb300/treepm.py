@@ -58,25 +58,30 @@ class StepPlan:
 
 
 def plan(z_in: float, z_fin: float, nsteps: int) -> List[StepPlan]:
-    ts0 = synth.stepper(z_in=z_in, z_fin=z_fin, nsteps=nsteps)
+    """The stepper points of driver_hires.cxx's loop (:320-447): each step
+    advances half a step before the sub-cycles and half a step after them
+    (pp += tau2 each time)."""
+    ts = synth.stepper(z_in=z_in, z_fin=z_fin, nsteps=nsteps)
     out = []
     half_kick = True
     for s in range(nsteps):
-        at = lambda k: synth.Stepper(alpha=ts0.alpha, pp=ts0.pp + s * ts0.tau + k * ts0.tau2,
-                                     omegatot=ts0.omegatot, tau=ts0.tau)
+        mid = ts.advanced(1)
+        end = mid.advanced(1)
         last = s == nsteps - 1
-        out.append(StepPlan(start=at(0), mid=at(1), end=at(2),
+        out.append(StepPlan(start=ts, mid=mid, end=end,
                             open_fraction=0.5 if half_kick else 0.0,
                             close_fraction=0.5 if last else 1.0))
         half_kick = last
+        ts = end
     return out
 
 
 def pm_params(ts: synth.Stepper, fraction: float, ng: int, ngo: int, gpscal: float = 1.0,
               precision: int = hsr.PM_F64) -> hsr.HsrPmParams:
-    """map2_poisson_backward_gradient's arguments: inverse_cic(tau *
-    stepFraction, fscal) in float."""
-    tau = float(np.float32(np.float32(ts.tau) * np.float32(fraction)))
+    """map2_poisson_backward_gradient's arguments (mc3.cxx:336-374):
+    inverse_cic(ts.tau() * stepFraction, ts.fscal(), d), the product taken
+    in double and both passed as floats."""
+    tau = float(np.float32(ts.tau * fraction))
     return hsr.pm_params(ng, ngo, gpscal, float(np.float32(ts.fscal)), tau, precision)
 
 
@@ -90,7 +95,7 @@ def step_params(sp: StepPlan, kp: synth.KickParams, nsub: int, ng: int, ngo: int
     S.nsub = nsub
     S.ng[:] = [int(v) for v in nglt]
     S.alpha, S.pp, S.adot = sp.mid.alpha, sp.mid.pp, sp.mid.adot
-    S.tau = float(np.float32(sp.mid.tau2 / nsub))
+    S.tau = float(synth.stream_tau(sp.mid, nsub))
     S.skip_stream = S.skip_kick = 0
     if sp.open_fraction:
         T.pm_open = pm_params(sp.start, sp.open_fraction, ng, ngo, gpscal, precision)

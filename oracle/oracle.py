@@ -27,6 +27,8 @@ REF_EXE = os.path.join(HERE, "_ref", "rcb_ref")
 # the reference's RCOForceTree, built from a copy with its octant array sized
 # 8 (the file as shipped reads past that array; see oracle/Makefile)
 REF_RCO_EXE = os.path.join(HERE, "_ref", "rco_ref")
+# the reference's Particles::subCycle and TimeStepper (oracle/sub_driver.cpp)
+REF_SUB_EXE = os.path.join(HERE, "_ref", "sub_ref")
 
 LAW_POLY6 = 0
 LAW_POLY5_STEP16 = 1
@@ -393,6 +395,31 @@ class Oracle:
         self.lib.ora_map1(p.n, *[_ptr(getattr(p, k), C.c_float) for k in ("x", "y", "z", "vx", "vy", "vz")],
                           alpha, pp, tau, adot)
 
+    def subcycle(self, p, ts, nsub, kp, gpscal=1.0, stream=True, kick=True, nthreads=0):
+        """Particles::subCycle (Particles.cxx:1176-1201) restated on `p` in
+        place: nsub times map1 (tau = stepFraction * tau2 as a float), map2
+        (resortParticles, masses = 1, the RCB kick of the in-box particles
+        with c from the stepper), map1.  `ts` is the stepper at which the
+        sub-cycles run (synth.Stepper), `kp` the tree parameters (its fcoeff
+        is replaced by map2's c).  Returns the last in-box count."""
+        import synth
+        tau = float(synth.stream_tau(ts, nsub))
+        kc = synth.KickParams(**{**kp.__dict__})
+        kc.fcoeff = float(synth.kick_coefficient(ts, nsub, gpscal))
+        nin = p.n
+        for _ in range(nsub):
+            if stream:
+                self.map1(p, ts.alpha, ts.pp, tau, ts.adot)
+            if kick:
+                nin = self.resort(p)
+                p.mass[:] = 1.0
+                view = synth.Particles(*(getattr(p, k)[:nin] for k in synth.FIELDS),
+                                       nglt=p.nglt)
+                self.rcb_run(view, kc, nthreads=nthreads)
+            if stream:
+                self.map1(p, ts.alpha, ts.pp, tau, ts.adot)
+        return nin
+
     def resort(self, p) -> int:
         ng = (C.c_int * 3)(*p.nglt)
         return self.lib.ora_resort(p.n, ng, *[_ptr(getattr(p, k), C.c_float) for k in
@@ -465,3 +492,68 @@ def run_reference(p, kp, nthreads: int = 0, reps: int = 1, timeout: float = 3600
             raise RuntimeError(f"reference run failed ({r.returncode}): {r.stderr[-2000:]}")
         info = json.loads(r.stdout.strip().splitlines()[-1])
         return read_case_arrays(cout), info["times"], info["threads"]
+
+
+# ---------------------------------------------------------------------------
+# Reference sub-cycle runs (oracle/_ref/sub_ref)
+# ---------------------------------------------------------------------------
+
+SUB_MAGIC = b"HSRSUBC1"
+_SFMT = "<4d3q10i4f"
+# Particles::m_useRCBTree values (Particles.cxx:1259-1363)
+USE_RCB_MONO, USE_RCB_QUAD, USE_RCO_MONO, USE_RCO_QUAD = 2, 1, 5, 4
+
+
+def subcycle_reference_available() -> bool:
+    return os.path.exists(REF_SUB_EXE)
+
+
+def run_reference_subcycle(p, *, ng, nsub, z_in, z_fin, nsteps, half_steps, nd=128, ds=1,
+                           tmin=128, use_rcb_tree=USE_RCB_MONO, edge=3.2, gpscal=1.0, rsm=0.1,
+                           open_angle=0.1, alpha=1.0, omegatot=None, skip_stream=False,
+                           skip_kick=False, nthreads=0, timeout=3600.0):
+    """Runs the reference's Particles::subCycle on a copy of `p` with a
+    TimeStepper(alpha, 1/(1+z_in), 1/(1+z_fin), nsteps, omegatot) advanced
+    `half_steps` half steps (ain, afin and omegatot rounded to float as
+    Basedata holds them).  Returns (arrays after the sub-cycles, the
+    stepper's values and the last in-box count as a dict)."""
+    import numpy as np
+    f = np.float32
+    if omegatot is None:
+        omegatot = float(f(f(0.23387755) + f(f(0.0226) / f(0.7)) / f(0.7)))
+    ain = float(f(1.0 / float(f(1.0) + f(z_in))))
+    afin = float(f(1.0 / float(f(1.0) + f(z_fin))))
+    head = struct.pack(_SFMT, float(f(alpha)), ain, afin, float(f(omegatot)), nd, ds, tmin,
+                       *[int(v) for v in ng], nsub, nsteps, half_steps, use_rcb_tree,
+                       int(skip_stream), int(skip_kick), nthreads, edge, gpscal, rsm, open_angle)
+    if not subcycle_reference_available():
+        raise FileNotFoundError(REF_SUB_EXE)
+    with tempfile.TemporaryDirectory() as td:
+        cin, cout = os.path.join(td, "in.bin"), os.path.join(td, "out.bin")
+        with open(cin, "wb") as fh:
+            fh.write(SUB_MAGIC)
+            fh.write(struct.pack("<q", p.n))
+            fh.write(head)
+            for k in ("x", "y", "z", "vx", "vy", "vz", "mass", "phi"):
+                fh.write(np.ascontiguousarray(getattr(p, k), np.float32).tobytes())
+            fh.write(np.ascontiguousarray(p.id, np.int64).tobytes())
+            fh.write(np.ascontiguousarray(p.mask, np.uint16).tobytes())
+        env = dict(os.environ, OMP_STACKSIZE="256M")
+        if nthreads > 0:
+            env["OMP_NUM_THREADS"] = str(nthreads)
+        r = subprocess.run([REF_SUB_EXE, cin, cout], env=env, capture_output=True, text=True,
+                           preexec_fn=_unlimited_stack, timeout=timeout)
+        if r.returncode != 0:
+            raise RuntimeError(f"reference sub-cycle failed ({r.returncode}): {r.stderr[-2000:]}")
+        info = json.loads(r.stdout.strip().splitlines()[-1])
+        with open(cout, "rb") as fh:
+            if fh.read(8) != SUB_MAGIC:
+                raise RuntimeError("bad sub-cycle output")
+            n = struct.unpack("<q", fh.read(8))[0]
+            fh.read(struct.calcsize(_SFMT))
+            out = {}
+            for k in ("x", "y", "z", "vx", "vy", "vz", "mass", "phi"):
+                out[k] = np.frombuffer(fh.read(4 * n), np.float32).copy()
+            out["id"] = np.frombuffer(fh.read(8 * n), np.int64).copy()
+            out["mask"] = np.frombuffer(fh.read(2 * n), np.uint16).copy()
+        return out, info

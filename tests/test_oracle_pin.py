@@ -78,3 +78,52 @@ def test_oracle_list_overflow_reported(oracle_lib):
     kp.min_force, kp.max_force = (0.1,) * 3, (3.9,) * 3
     with pytest.raises(RuntimeError, match="VMAX"):
         oracle_lib.rcb_run(p, kp, vmax=1000)
+
+
+# ---- the sub-cycle around the kick and its time stepper -------------------
+
+SUBREF = pytest.mark.skipif(not oracle.subcycle_reference_available(),
+                            reason="reference sub-cycle build (oracle/_ref/sub_ref) absent")
+
+
+@SUBREF
+@pytest.mark.parametrize("z_in,z_fin,nsteps", [(50.0, 10.0, 10), (200.0, 0.0, 500), (30.0, 20.0, 3)])
+def test_stepper_matches_reference(z_in, z_fin, nsteps):
+    """synth.stepper / Stepper.advanced against the reference's TimeStepper
+    (built from Basedata's float values and advanced half a step at a time):
+    pp, aa, adot, fscal, tau and tau2 equal to the last bit."""
+    empty = synth.random_box(0, 4.0, 1)
+    base = synth.stepper(z_in=z_in, z_fin=z_fin, nsteps=nsteps)
+    for half in sorted({0, 1, 2, 3, nsteps, 2 * nsteps - 1, 2 * nsteps}):
+        _, info = oracle.run_reference_subcycle(empty, ng=(4, 4, 4), nsub=0, z_in=z_in,
+                                                z_fin=z_fin, nsteps=nsteps, half_steps=half)
+        ts = base.advanced(half)
+        got = {"pp": ts.pp, "aa": ts.aa, "adot": ts.adot, "fscal": ts.fscal, "tau": ts.tau,
+               "tau2": ts.tau2}
+        for k, v in got.items():
+            assert v == info[k], (half, k, v, info[k])
+
+
+@SUBREF
+@pytest.mark.parametrize("ng,nsub,tdpts,half", [(16, 1, 1, 1), (20, 5, 1, 3), (16, 5, 12, 1),
+                                                (32, 5, 1, 1)])
+def test_subcycle_restatement_matches_reference(oracle_lib, ng, nsub, tdpts, half):
+    """Oracle.subcycle (map1, resortParticles, the kick with map2's
+    coefficient, map1) against the reference's own Particles::subCycle on a
+    Zel'dovich box with ghosts: all ten arrays bit for bit after nsub
+    sub-cycles.  The last case is the one-PM-step workload's 32^3 box."""
+    p = synth.zeldovich_box(ng, z=50.0, seed=40 + ng)
+    q = p.copy()
+    z_in, z_fin, nsteps = 50.0, 10.0, 10
+    ts = synth.stepper(z_in=z_in, z_fin=z_fin, nsteps=nsteps).advanced(half)
+    kp = synth.kick_params(q, nd=64, tdpts=tdpts)
+    nin = oracle_lib.subcycle(q, ts, nsub, kp, nthreads=4)
+    ref, info = oracle.run_reference_subcycle(
+        p, ng=p.nglt, nsub=nsub, z_in=z_in, z_fin=z_fin, nsteps=nsteps, half_steps=half, nd=64,
+        ds=kp.ds, tmin=kp.tmin,
+        use_rcb_tree=oracle.USE_RCB_MONO if tdpts == 1 else oracle.USE_RCB_QUAD, nthreads=4)
+    assert info["np_last"] == nin and info["pp"] == ts.pp
+    for k in synth.FIELDS:
+        assert np.array_equal(getattr(q, k).view(np.uint8), ref[k].view(np.uint8)), k
+    # the kicks did move the velocities
+    assert not np.array_equal(q.vx, p.vx)

@@ -15,32 +15,22 @@ NSUB = 5
 def _state(ng=24, z=50.0, seed=17):
     p = synth.zeldovich_box(ng, z=z, seed=seed)
     p.id[:] = np.arange(p.n)  # unique ids to match particles across orders
-    ts = synth.stepper(z_in=z)
+    # the sub-cycles of the first PM step run at its mid point
+    ts = synth.stepper(z_in=z, z_fin=10.0, nsteps=10).advanced(1)
     return p, ts
 
 
-def _view(p, m):
-    return synth.Particles(*(getattr(p, k)[:m] for k in synth.FIELDS), nglt=p.nglt)
-
-
 def _oracle_subcycle(O, p, kp, ts, nsub, stream=True, kick=True):
-    """Particles::subCycle with the oracle (the reference's arithmetic)."""
-    tau = np.float32(ts.tau2 / nsub)
-    for _ in range(nsub):
-        if stream:
-            O.map1(p, 1.0, ts.pp, float(tau), ts.adot)
-        if kick:
-            nin = O.resort(p)
-            p.mass[:] = 1.0
-            O.rcb_run(_view(p, nin), kp, nthreads=0)
-        if stream:
-            O.map1(p, 1.0, ts.pp, float(tau), ts.adot)
+    """Particles::subCycle restated by the oracle (pinned bit for bit to the
+    reference's own subCycle in the CPU suite)."""
+    return O.subcycle(p, ts, nsub, kp, stream=stream, kick=kick)
 
 
 def _gpu_subcycle(ctx, p, kp, ts, nsub, stream=True, kick=True):
-    tau = np.float32(ts.tau2 / nsub)
-    return ctx.subcycle(p, kp, nsub, p.nglt, 1.0, ts.pp, float(tau), ts.adot,
-                        skip_stream=not stream, skip_kick=not kick)
+    kc = synth.KickParams(**{**kp.__dict__})
+    kc.fcoeff = float(synth.kick_coefficient(ts, nsub))
+    return ctx.subcycle(p, kc, nsub, p.nglt, ts.alpha, ts.pp, float(synth.stream_tau(ts, nsub)),
+                        ts.adot, skip_stream=not stream, skip_kick=not kick)
 
 
 def test_resort_and_tree_permutation_bit_exact(ctx, oracle_lib):
@@ -71,7 +61,17 @@ def test_one_subcycle_matches_oracle(ctx, oracle_lib):
 
 
 def test_five_subcycles_match_oracle_by_particle(ctx, oracle_lib):
-    p0, ts = _state(seed=23)
+    """The one-PM-step workload: 32^3 at z = 50 with ghosts, 5 sub-cycles,
+    starting from rest.  The GPU's kicks differ from the reference's by FP32
+    summation order only, and positions by the resulting map1 differences:
+    the velocity changes stay within the single-kick tolerance.  (From rest
+    because the reference adds every pair term into v: with the box's own
+    velocities its kicks carry ~sqrt(list length) roundings of ulp(|v|) each,
+    which is not force error.)"""
+    p0, ts = _state(ng=32, seed=23)
+    p0.vx[:] = 0
+    p0.vy[:] = 0
+    p0.vz[:] = 0
     kp = synth.kick_params(p0, nd=64, nsub=NSUB)
     p, q = p0.copy(), p0.copy()
     st, _ = _gpu_subcycle(ctx, p, kp, ts, NSUB)
@@ -82,4 +82,4 @@ def test_five_subcycles_match_oracle_by_particle(ctx, oracle_lib):
     assert np.abs(dx).max() < 1e-4
     v0 = vel(p0)[np.argsort(p0.id)]
     rms, mx = force_errors(vel(p)[a] - v0, vel(q)[b] - v0)
-    assert rms <= 10 * RMS_TOL and mx <= MAX_TOL, (rms, mx)
+    assert rms <= RMS_TOL and mx <= MAX_TOL, (rms, mx)
