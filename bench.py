@@ -77,9 +77,6 @@ def parse_args():
                     help="boxes of 96^3 in the multi-box line (0: skip)")
     ap.add_argument("--adjoint-boxes", type=int, default=8,
                     help="boxes of 96^3 in the multi-step adjoint line (0: skip)")
-    ap.add_argument("--adjoint-workers", type=int, default=3,
-                    help="boxes of the multi-step run processed at once (host threads, one "
-                         "context each)")
     ap.add_argument("--clustered", type=int, default=256,
                     help="side of the clustered set of the leaf size x shape sweep (0: skip)")
     ap.add_argument("--treepm", type=int, default=1,
@@ -629,22 +626,22 @@ def main():
         pm = multistep.pm_schedule(50.0, 10.0, nsteps, 96, boxes[0].meta["ngo"])
         msr = multistep.MultiStep(ctx, kps, sched, nsub, checkpoint_every=every, pm=pm)
         states = [multistep.box_state(b, local) for b in boxes]
-        rng = np.random.default_rng(5)
-        cots = [[torch.from_numpy(rng.standard_normal(b.n).astype(np.float32)).cuda(local)
-                 for _ in range(6)] for b in boxes]
-        workers = max(1, args.adjoint_workers)
-        msr._workers(workers)  # contexts made before the timed runs
+        targets = [[t.clone() for t in S.x] for S in states]  # L = sum |x_final - x_initial|^2
         torch.cuda.synchronize()
         t0 = time.perf_counter()
-        msr.forward([S.clone() for S in states], workers=workers)
+        final = msr.forward([S.clone() for S in states])
         torch.cuda.synchronize()
         t_fwd = time.perf_counter() - t0
+        xbars, vbars, loss = multistep.position_loss_cotangent(final, targets)
+        del final
         k0, q0 = msr.total_kicks()
+        c0 = msr.batch_calls
         t0 = time.perf_counter()
-        msr.adjoint(states, [c[:3] for c in cots], [c[3:] for c in cots], workers=workers)
+        grads = msr.adjoint(states, xbars, vbars)
         torch.cuda.synchronize()
         t_adj = time.perf_counter() - t0
         k1, q1 = msr.total_kicks()
+        gnorm = float(sum(float((g.double() ** 2).sum()) for gx, _ in grads for g in gx)) ** 0.5
         nsc = args.adjoint_boxes * nsteps * nsub
         multistep_line = {
             "boxes": args.adjoint_boxes, "n_side": 96, "n_particles_per_box": boxes[0].n,
@@ -652,11 +649,16 @@ def main():
             "forward_s": t_fwd, "adjoint_s": t_adj,
             "s_per_substep_forward": t_fwd / nsc, "s_per_substep_adjoint": t_adj / nsc,
             "kicks_in_adjoint": k1 - k0, "pm_kicks_in_adjoint": q1 - q0,
-            "host_threads": workers,
-            "note": "the whole TreePM step per PM step: PM kicks (half opening the first "
-                    "step, one closing each step) around 5 short-range sub-cycles (map1, "
-                    "kick, map1); adjoint through hsr_force_vjp and hsr_pm_vjp"}
-        del states, cots
+            "multi_box_calls_in_adjoint": msr.batch_calls - c0,
+            "loss": loss, "grad_norm": gnorm,
+            "note": "all boxes in lockstep: every sub-cycle's kicks of the 8 boxes in one "
+                    "persistent launch (hsr_force_kick_batch, replayed as a CUDA graph), the "
+                    "reverse pass's tapes and VJPs of the 8 boxes one multi-box call each "
+                    "(hsr_force_fwd_batch + hsr_force_vjp_batch); PM kicks (half opening the "
+                    "first step, one closing each step) around 5 short-range sub-cycles (map1, "
+                    "kick, map1); L = sum |x_final - x_initial|^2, gradient w.r.t. the initial "
+                    "positions"}
+        del states, grads, xbars, vbars, targets
 
     # ---- clustered set: leaf size x launch shape sweep ----
     clustered = None

@@ -168,9 +168,12 @@ class CopyWorker {
 // Device state of one box of a multi-box kick.
 struct BoxState {
   hsr::DeviceTree tree;
-  DevBuf in, out, pos4, vel;
+  DevBuf in, out, pos4, vel, adj;
   int64_t n = 0;
   bool plain = false;
+  // the box's kick parameters (a multi-box forward's tape, for its adjoint)
+  int law = 0, tdpts = 1;
+  float fcoeff = 0, rsm2 = 0, rc2 = 0, rcull2 = 0;
   // the box's own stream: boxes of a batch are prepared concurrently
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
@@ -227,6 +230,9 @@ struct hsr_ctx {
   std::vector<std::unique_ptr<BoxState>> boxes;
   DevBuf d_box_desc, d_box_items;
   bool last_was_batch = false;
+  int32_t tape_boxes = 0;     // boxes whose trees are the last multi-box forward's tape
+  cudaGraphExec_t batch_exec = nullptr;  // the multi-box forward's launch, replayed per call
+  DevBuf d_vjp_desc;
   int32_t batch_n = 0;        // boxes of the last multi-box kick (replays)
   int64_t batch_items = 0;
   int batch_law = 0;
@@ -330,8 +336,10 @@ hsr_status hsr_destroy(hsr_ctx *ctx) {
   for (PinBuf *b : {&ctx->h_pos, &ctx->h_vel, &ctx->h_leaves, &ctx->h_segs, &ctx->h_items, &ctx->h_gidx})
     b->release();
   for (auto &b : ctx->boxes)
-    for (DevBuf *d : {&b->in, &b->out, &b->pos4, &b->vel}) d->release();
+    for (DevBuf *d : {&b->in, &b->out, &b->pos4, &b->vel, &b->adj}) d->release();
   ctx->boxes.clear();
+  ctx->d_vjp_desc.release();
+  if (ctx->batch_exec) cudaGraphExecDestroy(ctx->batch_exec);
   ctx->copier.reset();
   if (ctx->copy_stream) cudaStreamSynchronize(ctx->copy_stream);
   for (cudaEvent_t ev : {ctx->ev0, ctx->ev1, ctx->ev2, ctx->ev3, ctx->ev_in, ctx->ev_perm})
@@ -1006,6 +1014,7 @@ hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, 
   ctx->have_lists = false;
   ctx->tape = false;
   ctx->last_was_batch = false;
+  ctx->tape_boxes = 0;
   hsr_stats st{};
   hsr_status r = host_build
                      ? kick_host_build(ctx, p, n, x, y, z, vx, vy, vz, mass, phi, id, mask, st)
@@ -1094,6 +1103,7 @@ hsr_status hsr_subcycle(hsr_ctx *ctx, const hsr_subcycle_params *sp, int64_t n, 
   CU(cudaSetDevice(ctx->device), "cudaSetDevice");
   ctx->tape = false;
   ctx->last_was_batch = false;
+  ctx->tape_boxes = 0;
   cudaStream_t s = ctx->stream;
   // resident arrays
   const ArrayLayout A(n);
@@ -1153,6 +1163,7 @@ hsr_status force_fwd_impl(hsr_ctx *ctx, const hsr_params *p, int64_t n, const fl
   ctx->have_lists = false;
   ctx->tape = false;
   ctx->last_was_batch = false;
+  ctx->tape_boxes = 0;
   cudaStream_t s = ctx->stream;
   const size_t nb = size_t(std::max<int64_t>(n, 1)) * 4;
   CU(ctx->d_pos4.ensure(size_t(std::max<int64_t>(n, 1)) * 16), "cudaMalloc(pos4)");
@@ -1465,6 +1476,7 @@ hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *para
   CU(cudaSetDevice(ctx->device), "cudaSetDevice");
   ctx->have_lists = false;
   ctx->tape = false;
+  ctx->tape_boxes = 0;
   while (int32_t(ctx->boxes.size()) < nbox) ctx->boxes.emplace_back(new BoxState());
   hsr_stats st{};
   std::vector<hsr::BoxDesc> desc(static_cast<size_t>(nbox));
@@ -1660,6 +1672,365 @@ hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *para
   ctx->batch_items = total_items;
   ctx->batch_law = params[0].law;
   ctx->batch_group = ctx->tune.group;
+  return HSR_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+// Runs the multi-box pair launch (queue reset + the persistent kernel over
+// every box's items) as a CUDA graph: captured on each call and applied to
+// the context's executable graph (cudaGraphExecUpdate), which is
+// instantiated once and replayed.
+cudaError_t launch_batch_graph(hsr_ctx *ctx, int law, int group, int64_t items) {
+  cudaStream_t s = ctx->stream;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return e;
+  cudaError_t le = cudaMemsetAsync(ctx->d_queue.p, 0, 2 * sizeof(unsigned long long), s);
+  if (le == cudaSuccess)
+    le = hsr::launch_pairs_batched_multi(law, group, ctx->d_box_desc.as<hsr::BoxDesc>(),
+                                         ctx->d_box_items.as<hsr::PairItem>(), items,
+                                         ctx->d_queue.as<unsigned long long>(), ctx->batched_ctas, s);
+  e = cudaStreamEndCapture(s, &g);
+  if (le != cudaSuccess || e != cudaSuccess) {
+    if (g) cudaGraphDestroy(g);
+    return le != cudaSuccess ? le : e;
+  }
+  if (ctx->batch_exec) {
+    cudaGraphExecUpdateResultInfo info{};
+    if (cudaGraphExecUpdate(ctx->batch_exec, g, &info) != cudaSuccess) {
+      cudaGetLastError();  // the topology changed: instantiate afresh
+      cudaGraphExecDestroy(ctx->batch_exec);
+      ctx->batch_exec = nullptr;
+    }
+  }
+  if (!ctx->batch_exec) e = cudaGraphInstantiate(&ctx->batch_exec, g, 0);
+  cudaGraphDestroy(g);
+  if (e != cudaSuccess) return e;
+  return cudaGraphLaunch(ctx->batch_exec, s);
+}
+
+// hsr_force_fwd_batch (accumulate = false) and hsr_force_kick_batch
+// (accumulate = true): every box's tree and lists built on the device (boxes
+// prepared concurrently, each on its own stream), one persistent launch of the
+// pair kernel over all boxes' items, dv back in each caller's order.  The
+// boxes' trees stay as the tape of hsr_force_vjp_batch.
+hsr_status force_batch_impl(hsr_ctx *ctx, int32_t nbox, const hsr_params *params,
+                            const int64_t *ns, const float *const *x, const float *const *y,
+                            const float *const *z, const float *const *mass, float *const *dvx,
+                            float *const *dvy, float *const *dvz, int32_t mem, bool accumulate) {
+  if (!ctx) return HSR_ERR_ARG;
+  const auto t_start = clk::now();
+  if (nbox < 1 || nbox > (1 << 20) || !params || !ns || !x || !y || !z || !mass || !dvx || !dvy ||
+      !dvz)
+    return ctx->fail(HSR_ERR_ARG, "bad batch arguments");
+  if (mem != HSR_MEM_HOST && mem != HSR_MEM_DEVICE) return ctx->fail(HSR_ERR_ARG, "bad memory kind");
+  for (int32_t b = 0; b < nbox; ++b) {
+    const void *arrs[10] = {x[b], y[b], z[b], dvx[b], dvy[b], dvz[b], mass[b], x[b], x[b], x[b]};
+    if (hsr_status e = check_params(&params[b], ns[b], arrs, ctx->err)) return e;
+    if (params[b].law != params[0].law)
+      return ctx->fail(HSR_ERR_UNSUPPORTED, "all boxes of a batch use one force law");
+    if (params[b].tree != HSR_TREE_RCB)
+      return ctx->fail(HSR_ERR_UNSUPPORTED, "the multi-box forward builds RCB trees only");
+  }
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  ctx->have_lists = false;
+  ctx->tape = false;
+  ctx->tape_boxes = 0;
+  ctx->last_was_batch = false;
+  while (int32_t(ctx->boxes.size()) < nbox) ctx->boxes.emplace_back(new BoxState());
+  for (int32_t b = 0; b < nbox; ++b) {
+    BoxState &B = *ctx->boxes[b];
+    if (!B.stream) CU(cudaStreamCreateWithFlags(&B.stream, cudaStreamNonBlocking), "box stream");
+    if (!B.done) CU(cudaEventCreateWithFlags(&B.done, cudaEventDisableTiming), "box event");
+    B.status = HSR_OK;
+    B.err.clear();
+  }
+  std::vector<hsr::BoxDesc> desc(static_cast<size_t>(nbox));
+  auto prepare_box = [&](int32_t b) {
+    BoxState &B = *ctx->boxes[b];
+    cudaStream_t s = B.stream;
+    auto fail = [&](hsr_status code, const std::string &msg) {
+      B.status = code;
+      B.err = msg;
+    };
+#define BCU(call, what)                                                     \
+  do {                                                                      \
+    cudaError_t e_ = (call);                                                \
+    if (e_ != cudaSuccess) return fail(HSR_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e_)); \
+  } while (0)
+    BCU(cudaSetDevice(ctx->device), "cudaSetDevice");
+    const hsr_params *p = &params[b];
+    const int64_t n = ns[b];
+    B.n = n;
+    const size_t nb = (size_t(std::max<int64_t>(n, 1)) * 4 + 255) & ~size_t(255);
+    BCU(B.pos4.ensure(size_t(std::max<int64_t>(n, 1)) * 16), "cudaMalloc(pos4)");
+    BCU(B.vel.ensure(size_t(std::max<int64_t>(3 * n, 1)) * 4), "cudaMalloc(vel)");
+    const float *in[4] = {x[b], y[b], z[b], mass[b]};
+    if (mem == HSR_MEM_HOST) {
+      BCU(B.in.ensure(4 * nb), "cudaMalloc(in)");
+      for (int i = 0; i < 4; ++i) {
+        float *d = reinterpret_cast<float *>(B.in.as<char>() + i * nb);
+        BCU(cudaMemcpyAsync(d, in[i], size_t(n) * 4, cudaMemcpyHostToDevice, s), "H2D positions");
+        in[i] = d;
+      }
+    }
+    BCU(hsr::launch_pack4(in[0], in[1], in[2], in[3], B.pos4.as<float4>(), n, s), "pack kernel");
+    hsr::TreeConfig cfg{};
+    for (int i = 0; i < 3; ++i) {
+      cfg.min[i] = p->min[i];
+      cfg.max[i] = p->max[i];
+      cfg.min_force[i] = p->min_force[i];
+      cfg.max_force[i] = p->max_force[i];
+    }
+    cfg.fsrrmax = p->fsrrmax;
+    cfg.prune2 = cull2(cut2(p->law, p->fsrrmax));
+    cfg.tan_oa = std::tan(p->open_angle);
+    cfg.ppc = p->ppc;
+    cfg.nd = int32_t(std::min<int64_t>(p->nd, INT32_MAX));
+    cfg.tdpts = p->tdpts;
+    cfg.group = 32;  // the adjoint kernel takes one particle per lane
+    cudaError_t e = B.tree.build(cfg, n, B.pos4.as<float4>(), kJSplit, s);
+    if (e != cudaSuccess) {
+      if (B.tree.error()) return fail(HSR_ERR_UNSUPPORTED, B.tree.error());
+      return fail(HSR_ERR_CUDA, std::string("device tree build: ") + cudaGetErrorString(e));
+    }
+    float *dv = B.vel.as<float>();
+    BCU(cudaMemsetAsync(dv, 0, size_t(3 * n) * 4, s), "zero dv");
+    BCU(cudaEventRecord(B.done, s), "box event");
+#undef BCU
+    B.law = p->law;
+    B.tdpts = p->tdpts;
+    B.fcoeff = p->fcoeff;
+    B.rsm2 = p->rsm * p->rsm;
+    B.rc2 = cut2(p->law, p->fsrrmax);
+    B.rcull2 = cull2(B.rc2);
+    hsr::BoxDesc &D = desc[b];
+    D.table = B.tree.table();
+    D.idx = B.tree.index();
+    D.gidx = B.tree.gidx();
+    D.vx = dv;
+    D.vy = dv + n;
+    D.vz = dv + 2 * n;
+    D.fcoeff = B.fcoeff;
+    D.rsm2 = B.rsm2;
+    D.rcut2 = B.rc2;
+    D.rcull2 = B.rcull2;
+    D.law = hsr::make_law_s(p->law, D.rsm2, D.rcut2);
+  };
+  bool same_tdpts = true;
+  for (int32_t b = 1; b < nbox; ++b) same_tdpts &= params[b].tdpts == params[0].tdpts;
+  const int nthreads = same_tdpts ? int(std::min<int32_t>(nbox, kBatchThreads)) : 1;
+  if (nthreads <= 1) {
+    for (int32_t b = 0; b < nbox; ++b) prepare_box(b);
+  } else {
+    std::atomic<int32_t> next{0};
+    std::vector<std::thread> pool;
+    for (int t = 0; t < nthreads; ++t)
+      pool.emplace_back([&] {
+        for (int32_t b; (b = next.fetch_add(1)) < nbox;) prepare_box(b);
+      });
+    for (auto &t : pool) t.join();
+  }
+  hsr_stats st{};
+  int64_t total_items = 0;
+  double build_ms = 0, lists_ms = 0;
+  for (int32_t b = 0; b < nbox; ++b) {
+    BoxState &B = *ctx->boxes[b];
+    if (B.status != HSR_OK) return ctx->fail(B.status, B.err);
+    const hsr::DeviceTreeInfo &ti = B.tree.info();
+    build_ms += B.tree.build_ms();
+    lists_ms += B.tree.lists_ms();
+    total_items += ti.items;
+    st.n += B.n;
+    st.nodes += ti.nodes;
+    st.processed_leaves += ti.processed_leaves;
+    st.list_entries += ti.list_entries;
+    st.pairs += ti.pairs;
+    st.cm_fallbacks += ti.cm_fallbacks;
+    if (mem == HSR_MEM_HOST) st.h2d_bytes += B.n * 16 + (accumulate ? B.n * 12 : 0);
+    CU(cudaStreamWaitEvent(ctx->stream, B.done, 0), "wait for box");
+  }
+  cudaStream_t s = ctx->stream;
+  CU(ctx->d_box_items.ensure(size_t(std::max<int64_t>(total_items, 1)) * sizeof(hsr::PairItem)),
+     "cudaMalloc(items)");
+  CU(ctx->d_box_desc.ensure(size_t(nbox) * sizeof(hsr::BoxDesc)), "cudaMalloc(boxes)");
+  auto *items = ctx->d_box_items.as<hsr::PairItem>();
+  int64_t at = 0;
+  for (int32_t b = 0; b < nbox; ++b) {
+    const int64_t ni = ctx->boxes[b]->tree.info().items;
+    CU(hsr::launch_tag_items(ctx->boxes[b]->tree.items(), items + at, ni, b, s), "tag items");
+    at += ni;
+  }
+  CU(cudaMemcpyAsync(ctx->d_box_desc.p, desc.data(), size_t(nbox) * sizeof(hsr::BoxDesc),
+                     cudaMemcpyHostToDevice, s), "H2D box descriptors");
+  CU(ctx->d_queue.ensure(64), "cudaMalloc(queue)");
+  if (ctx->batched_ctas == 0) ctx->batched_ctas = hsr::batched_resident_ctas(ctx->device);
+  CU(cudaEventRecord(ctx->ev0, s), "event");
+  if (total_items > 0) CU(launch_batch_graph(ctx, params[0].law, 32, total_items), "multi-box pair launch");
+  CU(cudaEventRecord(ctx->ev1, s), "event");
+  for (int32_t b = 0; b < nbox; ++b) {
+    BoxState &B = *ctx->boxes[b];
+    const int64_t n = B.n;
+    const size_t nb = (size_t(std::max<int64_t>(n, 1)) * 4 + 255) & ~size_t(255);
+    float *dv = B.vel.as<float>();
+    float *outs[3] = {dvx[b], dvy[b], dvz[b]};
+    if (mem == HSR_MEM_HOST) CU(B.out.ensure(3 * nb), "cudaMalloc(out)");
+    for (int d = 0; d < 3; ++d) {
+      float *o = mem == HSR_MEM_HOST ? reinterpret_cast<float *>(B.out.as<char>() + d * nb) : outs[d];
+      if (accumulate) {
+        if (mem == HSR_MEM_HOST)
+          CU(cudaMemcpyAsync(o, outs[d], size_t(n) * 4, cudaMemcpyHostToDevice, s), "H2D v");
+        CU(hsr::launch_scatter_add_f32(dv + d * n, B.tree.perm(), o, n, s), "scatter-add dv");
+      } else {
+        CU(hsr::launch_scatter_f32(dv + d * n, B.tree.perm(), o, n, s), "scatter dv");
+      }
+      if (mem == HSR_MEM_HOST)
+        CU(cudaMemcpyAsync(outs[d], o, size_t(n) * 4, cudaMemcpyDeviceToHost, s), "D2H dv");
+    }
+    if (mem == HSR_MEM_HOST) st.d2h_bytes += n * 12;
+  }
+  unsigned long long counters[2] = {0, 0};
+  CU(cudaMemcpyAsync(counters, ctx->d_queue.p, sizeof(counters), cudaMemcpyDeviceToHost, s),
+     "D2H counters");
+  CU(cudaStreamSynchronize(s), "multi-box forward");
+  float fms = 0;
+  CU(cudaEventElapsedTime(&fms, ctx->ev0, ctx->ev1), "event time");
+  st.t_force_ms = fms;
+  st.t_build_ms = build_ms;
+  st.t_walk_ms = lists_ms;
+  st.evaluated_pairs = int64_t(counters[1]);
+  st.work_items = total_items;
+  st.kernel_launches = total_items > 0 ? 1 : 0;
+  st.t_total_ms = ms_since(t_start);
+  ctx->stats = st;
+  ctx->tape_boxes = nbox;
+  // the launch replays through hsr_bench_pairs as a multi-box kick's does
+  ctx->last_was_batch = true;
+  ctx->batch_n = nbox;
+  ctx->batch_items = total_items;
+  ctx->batch_law = params[0].law;
+  ctx->batch_group = 32;
+  return HSR_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+hsr_status hsr_force_fwd_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *params,
+                               const int64_t *n, const float *const *x, const float *const *y,
+                               const float *const *z, const float *const *mass, float *const *dvx,
+                               float *const *dvy, float *const *dvz, int32_t mem) {
+  return force_batch_impl(ctx, nbox, params, n, x, y, z, mass, dvx, dvy, dvz, mem, false);
+}
+
+hsr_status hsr_force_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *params,
+                                const int64_t *n, const float *const *x, const float *const *y,
+                                const float *const *z, const float *const *mass, float *const *vx,
+                                float *const *vy, float *const *vz, int32_t mem) {
+  return force_batch_impl(ctx, nbox, params, n, x, y, z, mass, vx, vy, vz, mem, true);
+}
+
+hsr_status hsr_force_vjp_batch(hsr_ctx *ctx, int32_t nbox, const float *const *dvbx,
+                               const float *const *dvby, const float *const *dvbz,
+                               float *const *xbx, float *const *xby, float *const *xbz,
+                               int32_t mem) {
+  if (!ctx) return HSR_ERR_ARG;
+  if (ctx->tape_boxes < 1)
+    return ctx->fail(HSR_ERR_STATE, "hsr_force_vjp_batch needs a preceding multi-box forward");
+  if (nbox != ctx->tape_boxes)
+    return ctx->fail(HSR_ERR_ARG, "the box count differs from the multi-box forward's");
+  if (!dvbx || !dvby || !dvbz || !xbx || !xby || !xbz) return ctx->fail(HSR_ERR_ARG, "null array");
+  if (mem != HSR_MEM_HOST && mem != HSR_MEM_DEVICE) return ctx->fail(HSR_ERR_ARG, "bad memory kind");
+  for (int32_t b = 0; b < nbox; ++b) {
+    const BoxState &B = *ctx->boxes[b];
+    if (B.tdpts != 1)
+      return ctx->fail(HSR_ERR_UNSUPPORTED, "the adjoint takes monopole pseudo-particles (tdpts = 1)");
+    if (B.n > 0 && (!dvbx[b] || !dvby[b] || !dvbz[b] || !xbx[b] || !xby[b] || !xbz[b]))
+      return ctx->fail(HSR_ERR_ARG, "null array");
+  }
+  CU(cudaSetDevice(ctx->device), "cudaSetDevice");
+  cudaStream_t s = ctx->stream;
+  std::vector<hsr::VjpBoxDesc> desc(static_cast<size_t>(nbox));
+  for (int32_t b = 0; b < nbox; ++b) {
+    BoxState &B = *ctx->boxes[b];
+    const int64_t n = B.n;
+    const hsr::DeviceTreeInfo &ti = B.tree.info();
+    const int64_t ntab = n + ti.nodes;
+    const size_t sn = size_t((std::max<int64_t>(n, 1) + 63) & ~int64_t(63));
+    const size_t st_ = size_t((std::max<int64_t>(ntab, 1) + 63) & ~int64_t(63));
+    const size_t sa = size_t(std::max<int64_t>(ti.nodes, 1)) * 3;
+    // cotangent (caller order, host input) | cotangent (tree order) | xbar table | node acc
+    CU(B.adj.ensure((6 * sn + 3 * st_ + sa + 64) * 4), "cudaMalloc(adjoint)");
+    float *ub = B.adj.as<float>();
+    float *ut = ub + 3 * sn;
+    float *xb = ut + 3 * sn;
+    const float *uin[3] = {dvbx[b], dvby[b], dvbz[b]};
+    for (int d = 0; d < 3; ++d) {
+      const float *src = uin[d];
+      if (mem == HSR_MEM_HOST) {
+        CU(cudaMemcpyAsync(ub + d * sn, uin[d], size_t(n) * 4, cudaMemcpyHostToDevice, s),
+           "H2D cotangent");
+        src = ub + d * sn;
+      }
+      CU(hsr::launch_gather_f32(src, B.tree.perm(), ut + d * sn, n, s), "gather cotangent");
+    }
+    CU(cudaMemsetAsync(xb, 0, 3 * st_ * 4, s), "zero xbar");
+    hsr::VjpBoxDesc &D = desc[b];
+    D.table = B.tree.table();
+    D.idx = B.tree.index();
+    D.gidx = B.tree.gidx();
+    D.ux = ut;
+    D.uy = ut + sn;
+    D.uz = ut + 2 * sn;
+    D.xbx = xb;
+    D.xby = xb + st_;
+    D.xbz = xb + 2 * st_;
+    D.fcoeff = B.fcoeff;
+    D.rsm2 = B.rsm2;
+    D.rcut2 = B.rc2;
+    D.rcull2 = B.rcull2;
+  }
+  CU(ctx->d_vjp_desc.ensure(size_t(nbox) * sizeof(hsr::VjpBoxDesc)), "cudaMalloc(vjp boxes)");
+  CU(cudaMemcpyAsync(ctx->d_vjp_desc.p, desc.data(), size_t(nbox) * sizeof(hsr::VjpBoxDesc),
+                     cudaMemcpyHostToDevice, s), "H2D vjp box descriptors");
+  CU(ctx->d_queue.ensure(64), "cudaMalloc(queue)");
+  CU(cudaMemsetAsync(ctx->d_queue.p, 0, 2 * sizeof(unsigned long long), s), "reset queue");
+  if (ctx->batched_ctas == 0) ctx->batched_ctas = hsr::batched_resident_ctas(ctx->device);
+  CU(cudaEventRecord(ctx->ev0, s), "event");
+  CU(hsr::launch_pairs_vjp_multi(ctx->boxes[0]->law, ctx->d_vjp_desc.as<hsr::VjpBoxDesc>(),
+                                 ctx->d_box_items.as<hsr::PairItem>(), ctx->batch_items,
+                                 ctx->d_queue.as<unsigned long long>(), ctx->batched_ctas, s),
+     "multi-box adjoint kernel");
+  CU(cudaEventRecord(ctx->ev1, s), "event");
+  for (int32_t b = 0; b < nbox; ++b) {
+    BoxState &B = *ctx->boxes[b];
+    const int64_t n = B.n;
+    const hsr::DeviceTreeInfo &ti = B.tree.info();
+    const int64_t ntab = n + ti.nodes;
+    const size_t sn = size_t((std::max<int64_t>(n, 1) + 63) & ~int64_t(63));
+    const size_t st_ = size_t((std::max<int64_t>(ntab, 1) + 63) & ~int64_t(63));
+    float *ub = B.adj.as<float>();
+    float *xb = ub + 6 * sn;
+    float *acc = xb + 3 * st_;
+    CU(hsr::launch_pseudo_adjoint(B.tree.nodes(), B.tree.levels(), B.tree.table(), n, xb, xb + st_,
+                                  xb + 2 * st_, acc, s),
+       "pseudo-particle adjoint");
+    float *outs[3] = {xbx[b], xby[b], xbz[b]};
+    for (int d = 0; d < 3; ++d) {
+      float *o = mem == HSR_MEM_HOST ? ub + d * sn : outs[d];
+      CU(hsr::launch_scatter_f32(xb + d * st_, B.tree.perm(), o, n, s), "scatter xbar");
+      if (mem == HSR_MEM_HOST)
+        CU(cudaMemcpyAsync(outs[d], o, size_t(n) * 4, cudaMemcpyDeviceToHost, s), "D2H xbar");
+    }
+  }
+  CU(cudaStreamSynchronize(s), "multi-box adjoint");
+  float ms = 0;
+  CU(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "event time");
+  ctx->stats.t_force_ms = ms;
   return HSR_OK;
 }
 
@@ -2108,6 +2479,7 @@ hsr_status hsr_treepm_step(hsr_ctx *ctx, const hsr_treepm_params *tp, int64_t n,
   CU(cudaSetDevice(ctx->device), "cudaSetDevice");
   ctx->tape = false;
   ctx->last_was_batch = false;
+  ctx->tape_boxes = 0;
   cudaStream_t s = ctx->stream;
   const ArrayLayout A(n);
   float *f[8] = {x, y, z, vx, vy, vz, mass, phi};

@@ -466,14 +466,14 @@ cudaError_t launch_tag_items(const PairItem *in, PairItem *out, int64_t n, int b
 // accumulates in registers; the j side is summed over the warp's lanes and
 // added with one atomic per kept entry.
 // ---------------------------------------------------------------------------
-template <int LAW>
+template <int LAW, bool MULTI>
 __global__ void __launch_bounds__(32 * kBatchedWarps)
-    k_pairs_vjp(const float4 *__restrict__ pos, const PairItem *__restrict__ items, int64_t nitems,
-                const int32_t *__restrict__ gidx, const int32_t *__restrict__ idx,
-                const float *__restrict__ ux, const float *__restrict__ uy,
-                const float *__restrict__ uz, float *__restrict__ xbx, float *__restrict__ xby,
-                float *__restrict__ xbz, float fcoeff, float rsm2, float rcut2, float rcull2,
-                unsigned long long *__restrict__ queue) {
+    k_pairs_vjp(const float4 *__restrict__ pos_, const PairItem *__restrict__ items, int64_t nitems,
+                const int32_t *__restrict__ gidx_, const int32_t *__restrict__ idx_,
+                const float *__restrict__ ux_, const float *__restrict__ uy_,
+                const float *__restrict__ uz_, float *__restrict__ xbx_, float *__restrict__ xby_,
+                float *__restrict__ xbz_, float fcoeff_, float rsm2_, float rcut2_, float rcull2_,
+                unsigned long long *__restrict__ queue, const VjpBoxDesc *__restrict__ boxes) {
   // kept entries, two per slot pair as in k_pairs_batched: (x, x', y, y'),
   // (z, z', m, m') and their table indices; the group's particles, two per
   // slot pair: (x, x', y, y'), (z, z', w, w'), (u0, u0', u1, u1'),
@@ -494,6 +494,27 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
     it = __shfl_sync(full, it, 0);
     if (it >= (unsigned long long)nitems) break;
     const PairItem W = items[it];
+    const float4 *pos = pos_;
+    const int32_t *gidx = gidx_, *idx = idx_;
+    const float *ux = ux_, *uy = uy_, *uz = uz_;
+    float *xbx = xbx_, *xby = xby_, *xbz = xbz_;
+    float fcoeff = fcoeff_, rsm2 = rsm2_, rcut2 = rcut2_, rcull2 = rcull2_;
+    if (MULTI) {
+      const VjpBoxDesc &B = boxes[W.flags >> 8];
+      pos = B.table;
+      gidx = B.gidx;
+      idx = B.idx;
+      ux = B.ux;
+      uy = B.uy;
+      uz = B.uz;
+      xbx = B.xbx;
+      xby = B.xby;
+      xbz = B.xbz;
+      fcoeff = B.fcoeff;
+      rsm2 = B.rsm2;
+      rcut2 = B.rcut2;
+      rcull2 = B.rcull2;
+    }
     const bool act = lane < W.g_count;
     const int pi = gidx[W.g_begin + (act ? lane : 0)];
     const float4 P = pos[pi];
@@ -657,11 +678,29 @@ cudaError_t launch_pairs_vjp(int law, const float4 *pos, const PairItem *items, 
   const int64_t need = (nitems + kBatchedWarps - 1) / kBatchedWarps;
   if (ctas > need) ctas = int(need);
   if (law == LAW_POLY5_STEP16)
-    k_pairs_vjp<LAW_POLY5_STEP16><<<ctas, 32 * kBatchedWarps, 0, s>>>(
-        pos, items, nitems, gidx, idx, ux, uy, uz, xbx, xby, xbz, fcoeff, rsm2, rcut2, rcull2, queue);
+    k_pairs_vjp<LAW_POLY5_STEP16, false><<<ctas, 32 * kBatchedWarps, 0, s>>>(
+        pos, items, nitems, gidx, idx, ux, uy, uz, xbx, xby, xbz, fcoeff, rsm2, rcut2, rcull2, queue,
+        nullptr);
   else
-    k_pairs_vjp<LAW_POLY6><<<ctas, 32 * kBatchedWarps, 0, s>>>(
-        pos, items, nitems, gidx, idx, ux, uy, uz, xbx, xby, xbz, fcoeff, rsm2, rcut2, rcull2, queue);
+    k_pairs_vjp<LAW_POLY6, false><<<ctas, 32 * kBatchedWarps, 0, s>>>(
+        pos, items, nitems, gidx, idx, ux, uy, uz, xbx, xby, xbz, fcoeff, rsm2, rcut2, rcull2, queue,
+        nullptr);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pairs_vjp_multi(int law, const VjpBoxDesc *boxes, const PairItem *items,
+                                   int64_t nitems, unsigned long long *queue, int ctas,
+                                   cudaStream_t s) {
+  if (nitems <= 0) return cudaSuccess;
+  ctas = clamp_ctas(ctas, nitems);
+  if (law == LAW_POLY5_STEP16)
+    k_pairs_vjp<LAW_POLY5_STEP16, true><<<ctas, 32 * kBatchedWarps, 0, s>>>(
+        nullptr, items, nitems, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+        nullptr, 0.f, 0.f, 0.f, 0.f, queue, boxes);
+  else
+    k_pairs_vjp<LAW_POLY6, true><<<ctas, 32 * kBatchedWarps, 0, s>>>(
+        nullptr, items, nitems, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+        nullptr, 0.f, 0.f, 0.f, 0.f, queue, boxes);
   return cudaGetLastError();
 }
 

@@ -72,6 +72,18 @@ struct alignas(16) BoxDesc {
   LawS law;
 };
 
+// One box of a multi-box adjoint launch: its tape (table, lists, groups),
+// the cotangent in tree order and the gradient table it adds into (particles,
+// then pseudo-particle slots).  Items carry their box in flags >> 8.
+struct alignas(16) VjpBoxDesc {
+  const float4 *table;
+  const int32_t *idx;
+  const int32_t *gidx;
+  const float *ux, *uy, *uz;
+  float *xbx, *xby, *xbz;
+  float fcoeff, rsm2, rcut2, rcull2;
+};
+
 // LawS of a law with softening rsm and strict cutoff rcut2 on r2.
 LawS make_law_s(int law, float rsm2, float rcut2);
 
@@ -354,6 +366,11 @@ cudaError_t launch_pairs_vjp(int law, const float4 *pos, const PairItem *items, 
                              const float *uy, const float *uz, float *xbx, float *xby, float *xbz,
                              float fcoeff, float rsm2, float rcut2, float rcull2,
                              unsigned long long *queue, int ctas, cudaStream_t s);
+// launch_pairs_vjp over the items of several boxes (items of box b carry
+// b << 8 in flags), one persistent launch; queue as above.
+cudaError_t launch_pairs_vjp_multi(int law, const VjpBoxDesc *boxes, const PairItem *items,
+                                   int64_t nitems, unsigned long long *queue, int ctas,
+                                   cudaStream_t s);
 cudaError_t launch_force_law(int law, const float *r2, float *g, int64_t n, float rsm2, float rcut2,
                              cudaStream_t s);
 

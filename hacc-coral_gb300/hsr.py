@@ -39,7 +39,8 @@ EXPORTS = ("hsr_create", "hsr_destroy", "hsr_last_error", "hsr_version", "hsr_rc
            "hsr_force_fwd", "hsr_force_vjp", "hsr_last_perm", "hsr_tree_size", "hsr_tree_export",
            "hsr_lists_export_index", "hsr_rcb_kick_batch", "hsr_bench_pairs_graph",
            "hsr_subcycle", "hsr_set_tune", "hsr_get_tune", "hsr_autotune",
-           "hsr_force_kick", "hsr_stream",
+           "hsr_force_kick", "hsr_stream", "hsr_force_fwd_batch", "hsr_force_kick_batch",
+           "hsr_force_vjp_batch",
            # include/hacc_pm.h
            "hsr_pm_kick", "hsr_pm_fields", "hsr_pm_get_stats", "hsr_pm_tables",
            "hsr_treepm_step", "hsr_pm_vjp", "hsr_pairs_in_cutoff")
@@ -191,6 +192,11 @@ def load(path: str = LIB_PATH):
     lib.hsr_probe_fp32_peak.argtypes = [vp, C.POINTER(C.c_double)]
     lib.hsr_force_kick.restype = i32
     lib.hsr_force_kick.argtypes = [vp, C.POINTER(HsrParams), i64, vp, vp, vp, vp, vp, vp, vp, i32]
+    for nm in ("hsr_force_fwd_batch", "hsr_force_kick_batch"):
+        getattr(lib, nm).restype = i32
+        getattr(lib, nm).argtypes = [vp, i32, C.POINTER(HsrParams), pi64] + [vp] * 7 + [i32]
+    lib.hsr_force_vjp_batch.restype = i32
+    lib.hsr_force_vjp_batch.argtypes = [vp, i32] + [vp] * 6 + [i32]
     lib.hsr_stream.restype = i32
     lib.hsr_stream.argtypes = [vp, i64, vp, vp, vp, vp, vp, vp, f32, f32, f32, f32, i32]
     lib.hsr_set_tune.restype = i32
@@ -370,6 +376,49 @@ class Context:
         ptr = lambda t: C.c_void_p(t.data_ptr())
         self._check(self.lib.hsr_force_vjp(self.h, ptr(ux), ptr(uy), ptr(uz), ptr(xbx), ptr(xby),
                                            ptr(xbz), MEM_DEVICE), "hsr_force_vjp")
+
+    # ---- several boxes at once, device buffers ---------------------------
+    @staticmethod
+    def _ptr_tables(groups):
+        """One C array of device pointers per group of tensors (kept alive by
+        the returned list) and their addresses."""
+        arrs = [(C.c_void_p * len(ts))(*[t.data_ptr() for t in ts]) for ts in groups]
+        return arrs, [C.cast(a, C.c_void_p) for a in arrs]
+
+    def _batch(self, fn, name, xs, masses, outs, kps, kernel):
+        nb = len(kps)
+        P = (HsrParams * nb)(*[make_params(k, kernel, BUILD_DEVICE) for k in kps])
+        ns = np.array([int(x[0].numel()) for x in xs], np.int64)
+        groups = ([[x[d] for x in xs] for d in range(3)] + [list(masses)]
+                  + [[o[d] for o in outs] for d in range(3)])
+        keep, tabs = self._ptr_tables(groups)
+        self._check(fn(self.h, nb, P, _p(ns, C.c_int64), *tabs, MEM_DEVICE), name)
+        del keep
+        return self.stats()
+
+    def force_kick_batch_device(self, xs, masses, vs, kps, kernel: int = KERNEL_AUTO) -> dict:
+        """hsr_force_kick_batch on device buffers: for every box b, v_b +=
+        dv_b in its caller's order, all boxes' pairs in one persistent launch;
+        xs[b] and vs[b] are (x, y, z) triples of float32 CUDA tensors, masses[b]
+        one tensor, kps[b] its KickParams.  Records the multi-box tape."""
+        return self._batch(self.lib.hsr_force_kick_batch, "hsr_force_kick_batch", xs, masses, vs,
+                           kps, kernel)
+
+    def force_fwd_batch_device(self, xs, masses, dvs, kps, kernel: int = KERNEL_AUTO) -> dict:
+        """hsr_force_fwd_batch on device buffers: every box's dv written in
+        its caller's order (dvs[b] a triple); records the multi-box tape."""
+        return self._batch(self.lib.hsr_force_fwd_batch, "hsr_force_fwd_batch", xs, masses, dvs,
+                           kps, kernel)
+
+    def force_vjp_batch_device(self, us, xbars):
+        """hsr_force_vjp_batch on device buffers: xbars[b] = (d dv_b / d x_b)^T
+        us[b] for the tape of the last multi-box forward (triples per box)."""
+        nb = len(us)
+        keep, tabs = self._ptr_tables([[u[d] for u in us] for d in range(3)]
+                                      + [[o[d] for o in xbars] for d in range(3)])
+        self._check(self.lib.hsr_force_vjp_batch(self.h, nb, *tabs, MEM_DEVICE),
+                    "hsr_force_vjp_batch")
+        del keep
 
     # ---- long-range PM kick (include/hacc_pm.h) ---------------------------
     def pm_kick(self, x, y, z, vx, vy, vz, params: HsrPmParams) -> dict:

@@ -29,8 +29,15 @@ and for a PM kick, xbar += (d dv / dx)^T vbar at its positions (hsr_pm_vjp).
 The trees and lists are held fixed within each kick (they are piecewise
 constant in the positions).  The kick positions are not stored for the whole
 run: the state is checkpointed every `checkpoint_every` PM steps and each
-segment is recomputed from its checkpoint during the reverse pass.  Boxes
-are independent and run one after the other on the context's stream.
+segment is recomputed from its checkpoint during the reverse pass.
+
+Boxes are independent.  By default (`batched`) they advance in lockstep:
+every sub-cycle's kicks of all boxes run as one call (hsr_force_kick_batch:
+each box's tree and lists on the device, one persistent pair launch over
+all boxes, replayed as a CUDA graph), and in the reverse pass every kick's
+tapes of all boxes are rebuilt by one hsr_force_fwd_batch and differentiated
+by one hsr_force_vjp_batch launch.  Otherwise boxes run one after another (or
+`workers` at a time on separate contexts), one kick per call.
 
 Buffers are CUDA tensors (torch is used for device memory only); every
 arithmetic step on particle data runs in this library's kernels, apart from
@@ -123,14 +130,16 @@ class MultiStep:
 
     kps: one synth.KickParams per box (fcoeff is replaced per PM step).
     on_tape(box, step, sub, ctx, x), if set, runs in the reverse pass right
-    after each kick's tape is recorded at its positions x: the context then
-    holds that kick's tree and lists (the FP64 checkers in the tests read
-    them there).
+    after each kick's tape is recorded at its positions x.  One box at a time,
+    `ctx` then holds that kick's tree and lists (the FP64 checkers in the
+    tests read them there); in lockstep `ctx` is None (the tape is the
+    multi-box one) and a hook that needs a box's tree builds it on a context
+    of its own from x (the tree and lists are a function of the positions).
     """
 
     def __init__(self, ctx: hsr.Context, kps: Sequence[synth.KickParams],
                  steps: Sequence[StepParams], nsub: int, checkpoint_every: Optional[int] = 2,
-                 pm: Optional[PMKicks] = None):
+                 pm: Optional[PMKicks] = None, batched: bool = True):
         if checkpoint_every is not None and checkpoint_every < 1:
             raise ValueError("checkpoint_every must be >= 1 or None")
         if pm is not None and len(pm) != len(steps):
@@ -142,8 +151,10 @@ class MultiStep:
         self.every = checkpoint_every
         self.pm = list(pm) if pm is not None else None
         self.on_tape: Optional[TapeHook] = None
+        self.batched = batched
         self.kicks = 0
         self.pm_kicks = 0
+        self.batch_calls = 0  # multi-box forward calls (one persistent launch each)
 
     # ---- one box ----------------------------------------------------------
     def _kp(self, b: int, st: StepParams) -> synth.KickParams:
@@ -246,6 +257,106 @@ class MultiStep:
             self._reverse_segment(b, s0, s1, xk, S0.mass, xb, vb, scratch)
         return xb, vb
 
+    # ---- all boxes in lockstep: one persistent launch per kick ----------
+    def _kps_at(self, st: StepParams, nbox: int) -> List[synth.KickParams]:
+        return [dataclasses.replace(self.kps[b], fcoeff=st.fcoeff) for b in range(nbox)]
+
+    def _run_all(self, Ss: Sequence[BoxState], s0: int, s1: int,
+                 record: Optional[List[list]] = None):
+        """Steps s0..s1-1 of every box, in lockstep (states in place); with
+        `record`, each box's kick positions are appended to record[b]."""
+        nb = len(Ss)
+        for s in range(s0, s1):
+            st = self.steps[s]
+            if self.pm:
+                for b, S in enumerate(Ss):
+                    self._pm_kick(self.pm[s][0], S, record[b] if record is not None else None)
+            for _ in range(self.nsub):
+                for S in Ss:
+                    self._stream(S.x, S.v, st)
+                if record is not None:
+                    for b, S in enumerate(Ss):
+                        record[b].append(("sr", s, [t.clone() for t in S.x]))
+                    _torch_done()
+                self.ctx.force_kick_batch_device([S.x for S in Ss], [S.mass for S in Ss],
+                                                 [S.v for S in Ss], self._kps_at(st, nb))
+                self.kicks += nb
+                self.batch_calls += 1
+                for S in Ss:
+                    self._stream(S.x, S.v, st)
+            if self.pm:
+                for b, S in enumerate(Ss):
+                    self._pm_kick(self.pm[s][1], S, record[b] if record is not None else None)
+
+    def _reverse_all(self, s0: int, s1: int, xks: List[list], masses, xbs, vbs, scratch):
+        """Adjoint of steps s0..s1-1 of every box from their recorded kick
+        positions (xks[b] as _reverse_segment's list, the same sequence for
+        every box), each kick's tapes rebuilt and differentiated for all boxes
+        at once."""
+        nb = len(xks)
+        sub = {s: self.nsub for s in range(s0, s1)}
+        for k in reversed(range(len(xks[0]))):
+            kind, arg, _ = xks[0][k]
+            if kind == "pm":
+                for b in range(nb):
+                    _, prm, x1 = xks[b][k]
+                    self.ctx.pm_vjp_device(x1[0], x1[1], x1[2], vbs[b][0], vbs[b][1], vbs[b][2],
+                                           *scratch[b], prm)
+                    for d in range(3):
+                        xbs[b][d].add_(scratch[b][d])
+                _torch_done()
+                continue
+            s = arg
+            st = self.steps[s]
+            sub[s] -= 1
+            j = sub[s]
+            for b in range(nb):
+                self._stream(vbs[b], xbs[b], st)             # second half-stream
+            xs = [xks[b][k][2] for b in range(nb)]
+            self.ctx.force_fwd_batch_device(xs, masses, scratch, self._kps_at(st, nb))
+            self.kicks += nb
+            self.batch_calls += 1
+            if self.on_tape:
+                for b in range(nb):
+                    self.on_tape(b, s, j, None, xs[b])
+            self.ctx.force_vjp_batch_device(vbs, scratch)
+            for b in range(nb):
+                for d in range(3):
+                    xbs[b][d].add_(scratch[b][d])            # kick
+            _torch_done()
+            for b in range(nb):
+                self._stream(vbs[b], xbs[b], st)             # first half-stream
+
+    def forward_all(self, states: Sequence[BoxState]) -> List[BoxState]:
+        """The whole map on every box's state (in place), in lockstep."""
+        _torch_done()
+        self._run_all(list(states), 0, len(self.steps))
+        return list(states)
+
+    def adjoint_all(self, states: Sequence[BoxState], xbars, vbars):
+        """adjoint_box of every box, in lockstep: [(xbar_0, vbar_0)] per box."""
+        import torch
+        nst, nb = len(self.steps), len(states)
+        xbs = [[t.clone() for t in xb] for xb in xbars]
+        vbs = [[t.clone() for t in vb] for vb in vbars]
+        scratch = [[torch.empty_like(S.x[0]) for _ in range(3)] for S in states]
+        masses = [S.mass for S in states]
+        Ss = [S.clone() for S in states]
+        _torch_done()
+        every = self.every if self.every is not None else nst
+        cps = []
+        for s0 in range(0, nst, every):
+            cps.append((s0, [S.clone() for S in Ss]))
+            _torch_done()
+            if self.every is not None:
+                self._run_all(Ss, s0, min(nst, s0 + every))
+        for s0, C in reversed(cps):
+            s1 = min(nst, s0 + every)
+            xks = [[] for _ in range(nb)]
+            self._run_all(C, s0, s1, record=xks)
+            self._reverse_all(s0, s1, xks, masses, xbs, vbs, scratch)
+        return [(xbs[b], vbs[b]) for b in range(nb)]
+
     # ---- several boxes ---------------------------------------------------
     def _workers(self, n: int) -> List["MultiStep"]:
         """This driver and n - 1 peers, each on its own context (CUDA stream
@@ -253,7 +364,7 @@ class MultiStep:
         peers = self.__dict__.setdefault("_peers", [])
         while len(peers) < n - 1:
             m = MultiStep(hsr.Context(self.ctx.device), self.kps, self.steps, self.nsub,
-                          self.every, self.pm)
+                          self.every, self.pm, batched=False)
             m.on_tape = self.on_tape
             peers.append(m)
         return [self] + peers[:max(0, n - 1)]
@@ -287,13 +398,19 @@ class MultiStep:
         return sum(w.kicks for w in ws), sum(w.pm_kicks for w in ws)
 
     def forward(self, states: Sequence[BoxState], workers: int = 1) -> List[BoxState]:
-        """forward_box over every box; workers > 1 runs that many boxes at
-        once, each on its own context."""
+        """The map on every box: in lockstep when batched, else forward_box
+        per box (workers > 1: that many boxes at once, each on its own
+        context)."""
+        if self.batched:
+            return self.forward_all(states)
         _torch_done()
         return self._map(lambda w, b: w.forward_box(b, states[b]), len(states), workers)
 
     def adjoint(self, states: Sequence[BoxState], xbars, vbars, workers: int = 1):
-        """adjoint_box over every box (workers as forward)."""
+        """The adjoint on every box: in lockstep when batched, else
+        adjoint_box per box (workers as forward)."""
+        if self.batched:
+            return self.adjoint_all(states, xbars, vbars)
         _torch_done()
         return self._map(lambda w, b: w.adjoint_box(b, states[b], xbars[b], vbars[b]),
                          len(states), workers)
@@ -304,3 +421,17 @@ def kicks_per_box(nsteps: int, nsub: int, checkpointed: bool = True) -> int:
     segment (checkpointed only) and the tape of every kick in the reverse
     pass."""
     return (3 if checkpointed else 2) * nsteps * nsub
+
+
+def position_loss_cotangent(states: Sequence[BoxState], targets):
+    """Cotangents of L = sum_b sum_i |x_b,i - t_b,i|^2 at the final states:
+    xbar = 2 (x - t), vbar = 0 (targets[b]: 3 CUDA tensors per box); and L
+    itself (float64)."""
+    import torch
+    xbars, vbars, L = [], [], 0.0
+    for S, T in zip(states, targets):
+        d = [x.double() - t.double() for x, t in zip(S.x, T)]
+        L += float(sum((u * u).sum() for u in d))
+        xbars.append([(2.0 * u).float() for u in d])
+        vbars.append([torch.zeros_like(v) for v in S.v])
+    return xbars, vbars, L

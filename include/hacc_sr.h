@@ -284,6 +284,42 @@ hsr_status hsr_force_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, const fl
                           const float *y, const float *z, const float *mass, float *vx,
                           float *vy, float *vz, int32_t mem);
 
+/* Several independent boxes of the forward half at once (multi-box batching;
+ * no counterpart in the reference, which kicks one rank's box per
+ * RCBForceTree constructor): every box's tree and lists are built on the
+ * device (boxes prepared concurrently, each on its own stream), then ONE
+ * persistent launch of the pair kernel evaluates the work items of all boxes
+ * (a CUDA graph, captured on each call and replayed through the context's
+ * executable graph), each box with its own parameters (one force law for
+ * all).  Per box as hsr_force_fwd: positions and masses are read only, dv is
+ * written in the caller's order; arrays are given as arrays of nbox
+ * pointers.  The boxes' trees and lists stay on the context as the tape of
+ * hsr_force_vjp_batch (any other kick or forward call replaces it).
+ * Statistics sum over the boxes. */
+hsr_status hsr_force_fwd_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *params,
+                               const int64_t *n, const float *const *x, const float *const *y,
+                               const float *const *z, const float *const *mass, float *const *dvx,
+                               float *const *dvy, float *const *dvz, int32_t mem);
+
+/* hsr_force_fwd_batch that adds every box's dv into its (vx, vy, vz) (the
+ * caller's order) instead of writing it: one sub-cycle kick of several boxes
+ * in one persistent launch, as hsr_force_kick is for one box. */
+hsr_status hsr_force_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *params,
+                                const int64_t *n, const float *const *x, const float *const *y,
+                                const float *const *z, const float *const *mass, float *const *vx,
+                                float *const *vy, float *const *vz, int32_t mem);
+
+/* Backward half of hsr_force_fwd_batch / hsr_force_kick_batch: for every box,
+ * xbar_b = (d dv_b / d x_b)^T dvbar_b over the tape of the last multi-box
+ * forward (nbox must equal its box count), caller's order, the VJP of all
+ * boxes in one persistent launch.  As hsr_force_vjp: trees, lists and the
+ * cutoff held fixed; HSR_ERR_STATE without a multi-box forward;
+ * HSR_ERR_UNSUPPORTED for 12-point pseudo-particles. */
+hsr_status hsr_force_vjp_batch(hsr_ctx *ctx, int32_t nbox, const float *const *dvbx,
+                               const float *const *dvby, const float *const *dvbz,
+                               float *const *xbx, float *const *xby, float *const *xbz,
+                               int32_t mem);
+
 /* Particles::map1 (src/cpu/Particles.cxx:732-758) on device arrays:
  * x += pt * v for the three components, pt = prefactor * tau with prefactor =
  * 1 / (alpha * adot * pp^(1 + 1/alpha)), all in float as map1 computes them.

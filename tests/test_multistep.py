@@ -126,33 +126,54 @@ def _tape_of(ctx, n):
                 cnt=cnt, ptr=ptr, idx=ctx.lists_index())
 
 
+def _tape_hook(torch, boxes, kps, tapes, kick_x):
+    """on_tape hook recording each kick's tree and lists and its positions;
+    in lockstep (ctx None) the box's tape is rebuilt on a context of its own
+    from the kick positions."""
+    aux = {}
+
+    def on_tape(b, s, j, c, x1):
+        n = boxes[b].n
+        if c is None:
+            if "ctx" not in aux:
+                aux["ctx"] = hsr.Context(0)
+            m = torch.ones(n, dtype=torch.float32, device=x1[0].device)
+            dv = [torch.empty_like(m) for _ in range(3)]
+            aux["ctx"].force_fwd_device(x1[0], x1[1], x1[2], m, *dv, kps[b])
+            c = aux["ctx"]
+        tapes[(b, s, j)] = _tape_of(c, n)
+        kick_x[(b, s, j)] = np.stack([t.cpu().numpy() for t in x1], 1).astype(np.float64)
+    return on_tape
+
+
 @pytest.mark.gpu
-def test_multistep_adjoint_vs_fp64_and_fd(ctx, oracle_lib):
+@pytest.mark.parametrize("batched", [True, False])
+def test_multistep_adjoint_vs_fp64_and_fd(ctx, oracle_lib, batched):
     """2 boxes x 12^3 at z = 50, 10 PM steps x 5 sub-cycles, checkpoints
-    every 2 steps, opening angle 0.1 (pseudo-particles on)."""
+    every 2 steps, opening angle 0.1 (pseudo-particles on); the boxes in
+    lockstep (one multi-box launch per kick) or one after the other."""
     torch = pytest.importorskip("torch")
     O = oracle_lib
     nsteps, nsub = 10, 5
     steps = multistep.schedule(50.0, 10.0, nsteps, nsub)
     boxes = _boxes(2, 12, 70)
     kps = [synth.kick_params(b, nd=64) for b in boxes]
-    ms = multistep.MultiStep(ctx, kps, steps, nsub, checkpoint_every=2)
+    ms = multistep.MultiStep(ctx, kps, steps, nsub, checkpoint_every=2, batched=batched)
     tapes, kick_x = {}, {}
-
-    def on_tape(b, s, j, c, x1):
-        n = boxes[b].n
-        tapes[(b, s, j)] = _tape_of(c, n)
-        kick_x[(b, s, j)] = np.stack([t.cpu().numpy() for t in x1], 1).astype(np.float64)
-    ms.on_tape = on_tape
+    ms.on_tape = _tape_hook(torch, boxes, kps, tapes, kick_x)
     rng = np.random.default_rng(8)
+    cots = []
+    for p in boxes:
+        xbar = rng.standard_normal((p.n, 3)).astype(np.float32)
+        vbar = rng.standard_normal((p.n, 3)).astype(np.float32)
+        cots.append((xbar, vbar))
+    dev = lambda a: [torch.from_numpy(np.ascontiguousarray(a[:, d])).cuda() for d in range(3)]
+    states = [multistep.box_state(p) for p in boxes]
+    grads = ms.adjoint(states, [dev(c[0]) for c in cots], [dev(c[1]) for c in cots])
     for b, p in enumerate(boxes):
-        S0 = multistep.box_state(p)
         n = p.n
-        xbar = rng.standard_normal((n, 3)).astype(np.float32)
-        vbar = rng.standard_normal((n, 3)).astype(np.float32)
-        tx = [torch.from_numpy(np.ascontiguousarray(xbar[:, d])).cuda() for d in range(3)]
-        tv = [torch.from_numpy(np.ascontiguousarray(vbar[:, d])).cuda() for d in range(3)]
-        gx_t, gv_t = ms.adjoint_box(b, S0, tx, tv)
+        xbar, vbar = cots[b]
+        gx_t, gv_t = grads[b]
         gx = np.stack([t.cpu().numpy() for t in gx_t], 1).astype(np.float64)
         gv = np.stack([t.cpu().numpy() for t in gv_t], 1).astype(np.float64)
         order = [(b, s, j) for s in range(nsteps) for j in range(nsub)]
@@ -176,6 +197,68 @@ def test_multistep_adjoint_vs_fp64_and_fd(ctx, oracle_lib):
         rms, mx = force_errors(gx[smp], fx[smp])
         assert rms <= ADJ_TOL, (b, rms)
     assert ms.kicks == multistep.kicks_per_box(nsteps, nsub) * 2
+    if batched:  # one multi-box call per kick of the forward, the recomputation and the tapes
+        assert ms.batch_calls == multistep.kicks_per_box(nsteps, nsub)
+
+
+@pytest.mark.gpu
+def test_kick_and_vjp_batch_equal_single_box_calls(ctx):
+    """hsr_force_kick_batch / hsr_force_vjp_batch on three boxes of different
+    sizes against hsr_force_kick / hsr_force_vjp box by box (the same pairs;
+    FP32 summation order only)."""
+    torch = pytest.importorskip("torch")
+    boxes = [synth.zeldovich_box(ng, z=20.0, seed=5 + ng) for ng in (12, 20, 16)]
+    kps = [synth.kick_params(b, nd=64, fcoeff=0.5 + 0.1 * i) for i, b in enumerate(boxes)]
+    Ss = [multistep.box_state(b) for b in boxes]
+    rng = np.random.default_rng(3)
+    us = [[torch.from_numpy(rng.standard_normal(b.n).astype(np.float32)).cuda() for _ in range(3)]
+          for b in boxes]
+    vb = [[v.clone() for v in S.v] for S in Ss]
+    st = ctx.force_kick_batch_device([S.x for S in Ss], [S.mass for S in Ss], vb, kps)
+    assert st["kernel_launches"] == 1 and st["pairs"] > 0
+    xb = [[torch.empty_like(S.x[0]) for _ in range(3)] for S in Ss]
+    ctx.force_vjp_batch_device(us, xb)
+    for b, S in enumerate(Ss):
+        v1 = [v.clone() for v in S.v]
+        ctx.force_kick_device(*S.x, S.mass, *v1, kps[b])
+        x1 = [torch.empty_like(S.x[0]) for _ in range(3)]
+        ctx.force_vjp_device(*us[b], *x1)
+        dv_b = np.stack([(a - v).double().cpu().numpy() for a, v in zip(vb[b], S.v)], 1)
+        dv_1 = np.stack([(a - v).double().cpu().numpy() for a, v in zip(v1, S.v)], 1)
+        rms, mx = force_errors(dv_b, dv_1)
+        assert rms <= 1e-5 and mx <= 1e-3, (b, rms, mx)
+        g_b = np.stack([t.double().cpu().numpy() for t in xb[b]], 1)
+        g_1 = np.stack([t.double().cpu().numpy() for t in x1], 1)
+        rms, mx = force_errors(g_b, g_1)
+        assert rms <= 1e-5 and mx <= 1e-3, (b, rms, mx)
+    # the multi-box tape is replaced by any single-box call
+    with pytest.raises(hsr.HsrError) as e:
+        ctx.force_vjp_batch_device(us, xb)
+    assert e.value.status == hsr.HSR_ERR_STATE
+
+
+@pytest.mark.gpu
+def test_lockstep_forward_equals_box_by_box(ctx):
+    """The whole multi-step map in lockstep (one multi-box launch per kick)
+    and box by box agree to FP32 summation order."""
+    torch = pytest.importorskip("torch")
+    nsteps, nsub = 3, 5
+    steps = multistep.schedule(50.0, 30.0, nsteps, nsub)
+    boxes = _boxes(3, 14, 120)
+    kps = [synth.kick_params(b, nd=64) for b in boxes]
+    a = multistep.MultiStep(ctx, kps, steps, nsub, batched=True)
+    b_ = multistep.MultiStep(ctx, kps, steps, nsub, batched=False)
+    Sa = a.forward([multistep.box_state(p) for p in boxes])
+    Sb = b_.forward([multistep.box_state(p) for p in boxes])
+    assert a.batch_calls == nsteps * nsub
+    for u, w, p in zip(Sa, Sb, boxes):
+        dx = max(float((x - y).abs().max()) for x, y in zip(u.x, w.x))
+        assert dx < 1e-4, dx
+        v0 = np.stack([p.vx, p.vy, p.vz], 1).astype(np.float64)
+        da = np.stack([t.double().cpu().numpy() for t in u.v], 1) - v0
+        db = np.stack([t.double().cpu().numpy() for t in w.v], 1) - v0
+        rms, mx = force_errors(da, db)
+        assert rms <= 1e-5 and mx <= 1e-3, (rms, mx)
 
 
 @pytest.mark.gpu
@@ -362,7 +445,7 @@ def test_boxes_on_two_host_threads_match_one(ctx):
     boxes = _boxes(3, 12, 150)
     kps = [synth.kick_params(b, nd=64) for b in boxes]
     pm = multistep.pm_schedule(50.0, 40.0, nsteps, 12, boxes[0].meta["ngo"])
-    ms = multistep.MultiStep(ctx, kps, steps, nsub, checkpoint_every=1, pm=pm)
+    ms = multistep.MultiStep(ctx, kps, steps, nsub, checkpoint_every=1, pm=pm, batched=False)
     states = [multistep.box_state(b) for b in boxes]
     rng = np.random.default_rng(6)
     cot = [[torch.from_numpy(rng.standard_normal(b.n).astype(np.float32)).cuda()
