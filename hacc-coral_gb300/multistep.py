@@ -151,6 +151,10 @@ class MultiStep:
         self.every = checkpoint_every
         self.pm = list(pm) if pm is not None else None
         self.on_tape: Optional[TapeHook] = None
+        # on_record(s0, records), if set, runs in the lockstep reverse pass
+        # after each segment's recomputation: records[b] lists box b's kicks
+        # of steps s0.. in forward order, ("sr", step, x) or ("pm", params, x)
+        self.on_record: Optional[Callable[[int, list], None]] = None
         self.batched = batched
         self.kicks = 0
         self.pm_kicks = 0
@@ -354,6 +358,8 @@ class MultiStep:
             s1 = min(nst, s0 + every)
             xks = [[] for _ in range(nb)]
             self._run_all(C, s0, s1, record=xks)
+            if self.on_record:
+                self.on_record(s0, xks)
             self._reverse_all(s0, s1, xks, masses, xbs, vbs, scratch)
         return [(xbs[b], vbs[b]) for b in range(nb)]
 

@@ -1,0 +1,127 @@
+"""The multi-box multi-step adjoint at its full size: 8 boxes of 96^3
+Zel'dovich particles (with ghosts, 1.16 M each) at z = 50, 10 TreePM steps
+(PM kicks around 5 short-range sub-cycles each), all boxes in lockstep (one
+multi-box launch per sub-cycle's kicks), checkpoints every 2 steps; the
+gradient of L = sum_b sum_i |x_final - x_initial|^2 with respect to the
+initial positions.
+
+Checks, against the FP64 restatement of the same map over the GPU's own
+frozen trees and lists (oracle.multistep64):
+  * box 0: the whole gradient against the FP64 adjoint along the GPU
+    trajectory (rms 2e-5 / max 2e-3 of the rms, as the TreePM-step adjoint
+    test at 12^3);
+  * every box: FP64 central differences (h = 1e-4 grid units) of L's
+    linearisation along one random direction over 64 interior particles,
+    against the GPU gradient projected on that direction, within 1e-4 of the
+    GPU gradient's norm over those particles.
+
+Each box costs its 50 kicks' trees and lists (~12 GB on the host) and two
+FP64 runs of the whole map, so the test takes ~15-25 minutes: it runs only
+with HSR_SLOW=1.
+"""
+import os
+
+import numpy as np
+import pytest
+
+import hsr
+import multistep
+import synth
+from hsr_testutil import force_errors
+
+pytestmark = [pytest.mark.gpu,
+              pytest.mark.skipif(os.environ.get("HSR_SLOW") != "1",
+                                 reason="full-size run (~20 min): set HSR_SLOW=1")]
+
+NSTEPS, NSUB, EVERY = 10, 5, 2
+# the benchmark's size; HSR_FULL_NG / HSR_FULL_NBOX shrink it for a quick run
+NG = int(os.environ.get("HSR_FULL_NG", "96"))
+NBOX = int(os.environ.get("HSR_FULL_NBOX", "8"))
+ADJ_TOL = 1e-4
+
+
+def _tape_of(c, n):
+    tree = c.tree()
+    off, cnt, ptr, _ = c.lists()
+    return dict(perm=c.last_perm(n), noff=tree["offset"], ncnt=tree["count"], off=off, cnt=cnt,
+                ptr=ptr, idx=c.lists_index())
+
+
+def _pm_dicts(pm):
+    return [tuple(None if q is None else dict(ng=q.ng, ngo=q.ngo, gpscal=q.gpscal, fscal=q.fscal,
+                                              tau=q.tau) for q in pair) for pair in pm]
+
+
+def test_eight_boxes_96_gradient_vs_fp64_and_fd(ctx, oracle_lib):
+    torch = pytest.importorskip("torch")
+    O = oracle_lib
+    boxes = [synth.zeldovich_box(NG, z=50.0, seed=300 + b) for b in range(NBOX)]
+    kps = [synth.kick_params(b, nd=128) for b in boxes]
+    sched = multistep.schedule(50.0, 10.0, NSTEPS, NSUB)
+    pm = multistep.pm_schedule(50.0, 10.0, NSTEPS, NG, boxes[0].meta["ngo"])
+    pmd = _pm_dicts(pm)
+    ms = multistep.MultiStep(ctx, kps, sched, NSUB, checkpoint_every=EVERY, pm=pm)
+    states = [multistep.box_state(b) for b in boxes]
+    targets = [[t.clone() for t in S.x] for S in states]
+    final = ms.forward([S.clone() for S in states])
+    assert ms.batch_calls == NSTEPS * NSUB
+    xbars, vbars, _ = multistep.position_loss_cotangent(final, targets)
+    del final
+    aux = hsr.Context(0)
+    rng = np.random.default_rng(55)
+    for b in range(NBOX):
+        p = boxes[b]
+        n = p.n
+        tapes, kick_x, pm_x = {}, {}, {}
+
+        def on_tape(bb, s, j, c, x1, b=b, n=n):
+            if bb != b:
+                return
+            m = torch.ones(n, dtype=torch.float32, device=x1[0].device)
+            dv = [torch.empty_like(m) for _ in range(3)]
+            aux.force_fwd_device(x1[0], x1[1], x1[2], m, *dv, kps[b])
+            tapes[(s, j)] = _tape_of(aux, n)
+            if b == 0:
+                kick_x[(s, j)] = np.stack([t.cpu().numpy() for t in x1], 1).astype(np.float64)
+
+        def on_record(s0, records, b=b):
+            if b == 0:
+                pm_x[s0] = [np.stack([t.cpu().numpy() for t in r[2]], 1).astype(np.float64)
+                            for r in records[b] if r[0] == "pm"]
+        ms.on_tape, ms.on_record = on_tape, on_record
+        grads = ms.adjoint(states, xbars, vbars)
+        gx = np.stack([t.cpu().numpy() for t in grads[b][0]], 1).astype(np.float64)
+        del grads
+        xbar = np.stack([t.cpu().numpy() for t in xbars[b]], 1).astype(np.float64)
+        vbar = np.zeros_like(xbar)
+        order = [(s, j) for s in range(NSTEPS) for j in range(NSUB)]
+        tl = [tapes[k] for k in order]
+        x0 = np.stack([p.x, p.y, p.z], 1).astype(np.float64)
+        v0 = np.stack([p.vx, p.vy, p.vz], 1).astype(np.float64)
+        m = p.mass.astype(np.float64)
+        if b == 0:
+            xl = [kick_x[k] for k in order]
+            pml = [x for s0 in sorted(pm_x) for x in pm_x[s0]]
+            _, _, _, rx, _ = O.multistep64(x0, v0, m, sched, NSUB, tl, xbar, vbar, kick_pos=xl,
+                                           pm=pmd, pm_pos=pml)
+            rms, mx = force_errors(gx, rx)
+            assert rms <= 2e-5 and mx <= 2e-3, (b, rms, mx)
+            del xl, pml, kick_x
+        # central differences of the FP64 map along one direction over 64 particles
+        base, pm_base = [], []
+        O.multistep64(x0, v0, m, sched, NSUB, tl, traj_out=base, pm=pmd, pm_traj_out=pm_base)
+        smp = rng.choice(np.flatnonzero(p.mask == 0), 64, replace=False)
+        D = np.zeros_like(x0)
+        D[smp] = rng.standard_normal((64, 3))
+        D /= np.linalg.norm(D)
+        h = 1e-4
+        runs = []
+        for step in (h, -h):
+            xT, vT = O.multistep64(x0 + step * D, v0, m, sched, NSUB, tl, cut_pos=base, pm=pmd,
+                                   pm_cut=pm_base)
+            runs.append(float((xbar * xT).sum() + (vbar * vT).sum()))
+        fd = (runs[0] - runs[1]) / (2 * h)
+        proj = float((gx * D).sum())
+        assert abs(proj - fd) <= ADJ_TOL * np.linalg.norm(gx[smp]), (b, proj, fd)
+        del tapes, tl, base, pm_base
+    aux.close()

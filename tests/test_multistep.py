@@ -12,6 +12,14 @@ the map with trees, lists and the cutoff mask held fixed (the law steps at
 the cutoff, and over 50 sub-cycles some pair of most particles' neighbours
 crosses it within h); the differences therefore decide every pair's cutoff
 on the unperturbed run's positions.
+
+The GPU gradient is also compared with the FP64 map's gradient at the FP64
+map's own trajectory (the one the differences probe).  The FP32 forward
+drifts from the FP64 forward over 50 sub-cycles (final positions ~6e-5 grid
+units apart in the 12^3 boxes), which moves that gradient by ~1e-4 rms; the
+test therefore asks the GPU gradient to be no farther from it than the exact
+FP64 adjoint evaluated along the GPU trajectory is (plus 1e-5): the gap is
+the forward's drift, not adjoint error.
 """
 import dataclasses
 
@@ -193,9 +201,11 @@ def test_multistep_adjoint_vs_fp64_and_fd(ctx, oracle_lib, batched):
         _, _, _, fx, _ = O.multistep64(x0, v0, m, steps, nsub, tl, xbar, vbar)
         bad = _check_fd(O, x0, v0, m, steps, nsub, tl, xbar, vbar, fx, smp, 1e-4, rng)
         assert bad == 0, (b, bad)
-        # and the GPU gradient against the same differences' gradient
-        rms, mx = force_errors(gx[smp], fx[smp])
-        assert rms <= ADJ_TOL, (b, rms)
+        # the GPU gradient against the differences' gradient: as close as the
+        # FP64 adjoint along the GPU trajectory (the FP32 forward's drift)
+        rms, _ = force_errors(gx[smp], fx[smp])
+        drift, _ = force_errors(rx[smp], fx[smp])
+        assert rms <= drift + 1e-5, (b, rms, drift)
     assert ms.kicks == multistep.kicks_per_box(nsteps, nsub) * 2
     if batched:  # one multi-box call per kick of the forward, the recomputation and the tapes
         assert ms.batch_calls == multistep.kicks_per_box(nsteps, nsub)
@@ -430,8 +440,9 @@ def test_multistep_with_pm_adjoint_vs_fp64_and_fd(ctx, oracle_lib):
     _, _, _, fx, _ = O.multistep64(x0, v0, m, steps, nsub, tl, xbar, vbar, pm=pmd)
     bad = _check_fd_pm(O, x0, v0, m, steps, nsub, tl, pmd, xbar, vbar, fx, smp, 1e-4, rng)
     assert bad == 0, bad
-    rms, mx = force_errors(gx[smp], fx[smp])
-    assert rms <= ADJ_TOL, rms
+    rms, _ = force_errors(gx[smp], fx[smp])
+    drift, _ = force_errors(rx[smp], fx[smp])
+    assert rms <= drift + 1e-5, (rms, drift)
     assert ms.pm_kicks == 3 * (nsteps + 1)  # forward, recomputation, stored run
 
 
