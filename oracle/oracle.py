@@ -395,17 +395,20 @@ class Oracle:
         self.lib.ora_map1(p.n, *[_ptr(getattr(p, k), C.c_float) for k in ("x", "y", "z", "vx", "vy", "vz")],
                           alpha, pp, tau, adot)
 
-    def subcycle(self, p, ts, nsub, kp, gpscal=1.0, stream=True, kick=True, nthreads=0):
+    def subcycle(self, p, ts, nsub, kp, gpscal=1.0, stream=True, kick=True, nthreads=0,
+                 fcoeff=None):
         """Particles::subCycle (Particles.cxx:1176-1201) restated on `p` in
         place: nsub times map1 (tau = stepFraction * tau2 as a float), map2
         (resortParticles, masses = 1, the RCB kick of the in-box particles
         with c from the stepper), map1.  `ts` is the stepper at which the
         sub-cycles run (synth.Stepper), `kp` the tree parameters (its fcoeff
-        is replaced by map2's c).  Returns the last in-box count."""
+        is replaced by map2's c, or by `fcoeff` when given).  Returns the
+        last in-box count."""
         import synth
         tau = float(synth.stream_tau(ts, nsub))
         kc = synth.KickParams(**{**kp.__dict__})
-        kc.fcoeff = float(synth.kick_coefficient(ts, nsub, gpscal))
+        kc.fcoeff = (float(synth.kick_coefficient(ts, nsub, gpscal)) if fcoeff is None
+                     else float(fcoeff))
         nin = p.n
         for _ in range(nsub):
             if stream:

@@ -20,15 +20,15 @@ def _state(ng=24, z=50.0, seed=17):
     return p, ts
 
 
-def _oracle_subcycle(O, p, kp, ts, nsub, stream=True, kick=True):
+def _oracle_subcycle(O, p, kp, ts, nsub, stream=True, kick=True, fcoeff=None):
     """Particles::subCycle restated by the oracle (pinned bit for bit to the
-    reference's own subCycle in the CPU suite)."""
-    return O.subcycle(p, ts, nsub, kp, stream=stream, kick=kick)
+    reference's own subCycle in the CPU suite); fcoeff overrides map2's c."""
+    return O.subcycle(p, ts, nsub, kp, stream=stream, kick=kick, fcoeff=fcoeff)
 
 
-def _gpu_subcycle(ctx, p, kp, ts, nsub, stream=True, kick=True):
+def _gpu_subcycle(ctx, p, kp, ts, nsub, stream=True, kick=True, fcoeff=None):
     kc = synth.KickParams(**{**kp.__dict__})
-    kc.fcoeff = float(synth.kick_coefficient(ts, nsub))
+    kc.fcoeff = float(synth.kick_coefficient(ts, nsub)) if fcoeff is None else float(fcoeff)
     return ctx.subcycle(p, kc, nsub, p.nglt, ts.alpha, ts.pp, float(synth.stream_tau(ts, nsub)),
                         ts.adot, skip_stream=not stream, skip_kick=not kick)
 
@@ -41,8 +41,9 @@ def test_resort_and_tree_permutation_bit_exact(ctx, oracle_lib):
     p.x[:50] += 200.0
     kp = synth.kick_params(p, nd=64, fcoeff=0.0)
     q = p.copy()
-    _, nin = _gpu_subcycle(ctx, p, kp, ts, 1, stream=False)
-    _oracle_subcycle(oracle_lib, q, kp, ts, 1, stream=False)
+    # a zero kick coefficient: the velocities are only permuted
+    _, nin = _gpu_subcycle(ctx, p, kp, ts, 1, stream=False, fcoeff=0.0)
+    _oracle_subcycle(oracle_lib, q, kp, ts, 1, stream=False, fcoeff=0.0)
     assert nin == p.n - 50
     for k in synth.FIELDS:
         assert np.array_equal(getattr(p, k).view(np.uint8), getattr(q, k).view(np.uint8)), k
