@@ -105,6 +105,7 @@ def test_eight_boxes_96_gradient_vs_fp64_and_fd(ctx, oracle_lib):
             _, _, _, rx, _ = O.multistep64(x0, v0, m, sched, NSUB, tl, xbar, vbar, kick_pos=xl,
                                            pm=pmd, pm_pos=pml)
             rms, mx = force_errors(gx, rx)
+            print(f"box 0 gradient vs FP64 along the GPU trajectory: rms {rms:.3e} max {mx:.3e}")
             assert rms <= 2e-5 and mx <= 2e-3, (b, rms, mx)
             del xl, pml, kick_x
         # central differences of the FP64 map along one direction over 64 particles
@@ -122,6 +123,8 @@ def test_eight_boxes_96_gradient_vs_fp64_and_fd(ctx, oracle_lib):
             runs.append(float((xbar * xT).sum() + (vbar * vT).sum()))
         fd = (runs[0] - runs[1]) / (2 * h)
         proj = float((gx * D).sum())
+        print(f"box {b}: directional derivative {proj:.6e}, differences {fd:.6e}, "
+              f"error {abs(proj - fd) / np.linalg.norm(gx[smp]):.3e} of the samples' gradient norm")
         assert abs(proj - fd) <= ADJ_TOL * np.linalg.norm(gx[smp]), (b, proj, fd)
         del tapes, tl, base, pm_base
     aux.close()
