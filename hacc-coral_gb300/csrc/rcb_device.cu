@@ -51,7 +51,7 @@ constexpr int kPlainSteps = 4;      // single chain steps before the chunk parti
 enum { C_NCHUNK = 0, C_NSPLIT = 1, C_NFALLBACK = 2, C_NLEAF = 3, C_NSEG = 4, C_NENT = 5,
        C_PAIRS = 6, C_PADDED = 7, C_NITEMS = 8, C_MAXLEN = 9, C_TDONE1 = 10, C_TDONE2 = 11,
        C_NTIGHT = 12, C_SEGOVF = 13, C_MAXCNT = 14, C_ERR = 15, C_BUCKET = 16, C_FILL = 48,
-       C_COUNT = 80 };
+       C_SUBFB = 80, C_COUNT = 81 };
 
 // Segments a leaf's walk can leave in its own region of the one-pass walk;
 // a leaf with more sends the build to the counting walk and a second pass.
@@ -546,9 +546,11 @@ __device__ bool certify(double sx, double bx, double sm, double bm, float *out) 
 
 // Sets a node's bounding box and, where decided, its centre of mass from the
 // reduced sums; lists it for the tight certification otherwise.
-__device__ void finish_node(DNode &N, int32_t node, const __int128 *s, double *a, const float *lo,
-                            const float *hi, const int *emin, bool ovf, int32_t *fallback,
-                            int64_t *counters, int32_t force_fallback, int32_t nd) {
+// The node's box, split axis and (where the bounds decide it) centre of mass
+// from the reduced sums; false when the centre of mass is left undecided.
+__device__ bool decide_node(DNode &N, const __int128 *s, double *a, const float *lo,
+                            const float *hi, const int *emin, bool ovf, int32_t force_fallback,
+                            int32_t nd) {
   for (int d = 0; d < 3; ++d) {
     N.xmin[d] = lo[d];
     N.xmax[d] = hi[d];
@@ -599,7 +601,13 @@ __device__ void finish_node(DNode &N, int32_t node, const __int128 *s, double *a
     if (certify(sd[d], bd[0], sd[3], bd[1], &v)) N.xc[d] = v;
     else ok = false;
   }
-  if (!ok) {
+  return ok;
+}
+
+__device__ void finish_node(DNode &N, int32_t node, const __int128 *s, double *a, const float *lo,
+                            const float *hi, const int *emin, bool ovf, int32_t *fallback,
+                            int64_t *counters, int32_t force_fallback, int32_t nd) {
+  if (!decide_node(N, s, a, lo, hi, emin, ovf, force_fallback, nd)) {
     const unsigned long long k = atomicAdd((unsigned long long *)&counters[C_NFALLBACK], 1ull);
     fallback[k] = node;
   }
@@ -1480,6 +1488,448 @@ __global__ void __launch_bounds__(NT)
   }
 }
 
+// ---------------------------------------------------------------------------
+// Whole subtrees in one block.  Once every node of a level holds at most
+// kSubMax elements, one block per node builds that node's entire subtree:
+// level by level inside the block, each node's statistics (box, exact
+// fixed-point centre-of-mass sums and their certification, the reference's
+// sequential sum where the bounds leave it open), the split decision, the
+// partition at the centre of mass (left elements to their ranks, right
+// elements along the swap chains kept in shared memory, pointer jumping for
+// long chains -- the reference's swap sequence, RCBForceTree.cxx:623-672) and
+// the children.  The level's nodes are shared out to teams of warps: a whole
+// block for one node, down to a warp per node on deep levels.  Elements
+// alternate between the two element buffers as in the level loop (a leaf's
+// elements are copied into the other buffer once, so both end up holding
+// every leaf).  The subtree's nodes go to a scratch region (2 x count
+// records per root, at twice the root's element offset) in per-root
+// breadth-first order; k_subtree_place later numbers all of them by level
+// and offset, as the level loop would have.  One launch and no host
+// synchronisation replace the deep levels' kernels.
+// ---------------------------------------------------------------------------
+constexpr int kSubMax = 16384;       // largest subtree root (elements)
+constexpr int kSubThreads = 512;   // two blocks per SM
+constexpr int kSubWarps = kSubThreads / 32;
+constexpr int kSubDepth = 48;        // deepest level below a root; deeper: the level loop
+
+struct SubWarpStats {
+  __int128 s[4];
+  double a[4];
+  float lo[3], hi[3];
+  int emin[4];
+  int ovf;
+};
+
+// Barrier over the warps [w0, w0 + nw) of the block: named barrier 1 + team
+// for teams of several warps (at most 8 teams), __syncwarp for one warp.
+__device__ __forceinline__ void team_sync(int team, int nw) {
+  if (nw == 1) {
+    __syncwarp();
+  } else {
+    asm volatile("bar.sync %0, %1;" ::"r"(team + 1), "r"(nw * 32) : "memory");
+  }
+}
+
+__global__ void __launch_bounds__(kSubThreads, 2)
+    k_subtree(const DNode *__restrict__ nodes, int32_t nb, int32_t ne, float4 *epos, int32_t *eoid,
+              float4 *tpos, int32_t *toid, DNode *sub, SubWarpStats *sub_stats, int32_t *sub_first,
+              int64_t *hist, int32_t force_fallback, int32_t nd, int64_t *counters) {
+  extern __shared__ int32_t sidx[];  // chain table by element position in the subtree
+  __shared__ SubWarpStats wst[kSubWarps];
+  __shared__ int wtot[kSubWarps];
+  __shared__ int tflag[kSubWarps];      // per team: a chain too long / pointer jumping changed
+  __shared__ int first[kSubDepth + 2];  // first local node of each depth
+  __shared__ int sh_warp[32];
+  __shared__ int s_nsplit;
+  const int32_t r = int32_t(blockIdx.x);
+  const int32_t nroots = ne - nb;
+  const DNode R = nodes[nb + r];
+  const int rcnt = R.count;
+  const int32_t roff = R.offset;
+  DNode *loc = sub + 2 * int64_t(roff);  // this root's 2 x count records
+  // the reduced statistics of the current level's nodes, by position in the
+  // level (a level holds at most count nodes)
+  SubWarpStats *lst = sub_stats + roff;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned below = (1u << lane) - 1u;
+  if (rcnt > kSubMax) {  // the launch's shared memory does not hold it
+    if (threadIdx.x == 0) atomicExch(reinterpret_cast<int32_t *>(counters + C_ERR), 3);
+    return;
+  }
+  if (threadIdx.x == 0) {
+    loc[0] = R;
+    loc[0].cl = loc[0].cr = 0;
+    first[0] = 0;
+    first[1] = 1;
+  }
+  __syncthreads();
+  const float4 *src = epos;
+  const int32_t *soid = eoid;
+  float4 *dst = tpos;
+  int32_t *doid = toid;
+  int f0 = 0, f1 = 1, depth = 0;
+  int nfb = 0;  // sequential centre-of-mass sums (thread 0 of a team counts)
+  while (f1 > f0) {
+    const int F = f1 - f0;
+    // teams: the whole block for one node, halving per doubling of the level
+    // to a warp per node from 9 nodes on (at most 8 teams of several warps,
+    // named barriers 1-8)
+    int nw = 1;
+    if (F <= 8) {
+      int p2 = 1;
+      while (p2 < F) p2 <<= 1;
+      nw = kSubWarps / p2;
+    }
+    const int nteams = kSubWarps / nw;
+    const int team = warp / nw, w0 = team * nw, wi = warp - w0;
+    const int tl = wi * 32 + lane, TN = nw * 32;
+    // ---- statistics: a team per node, reduced into the level's scratch ----
+    for (int f = f0 + team; f < f1; f += nteams) {
+      const DNode N = loc[f];
+      const int c = N.count;
+      const int64_t o = N.offset;
+      __int128 sq[4] = {0, 0, 0, 0};
+      unsigned __int128 bits[4] = {0, 0, 0, 0};
+      float fa[4] = {0.f, 0.f, 0.f, 0.f};
+      float bl[3] = {INFINITY, INFINITY, INFINITY}, bh[3] = {-INFINITY, -INFINITY, -INFINITY};
+      bool ovf = false;
+      bool trn[4] = {false, false, false, false};
+      for (int e = tl; e < c; e += TN) {
+        const float4 p = src[o + e];
+        const float w = p.w;
+        const float t[4] = {fmul_(w, p.x), fmul_(w, p.y), fmul_(w, p.z), w};
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          fix_add(sq[q], bits[q], t[q], ovf, trn[q]);
+          fa[q] = __fadd_ru(fa[q], fabsf(t[q]));
+        }
+        bl[0] = fminf(bl[0], p.x); bh[0] = fmaxf(bh[0], p.x);
+        bl[1] = fminf(bl[1], p.y); bh[1] = fmaxf(bh[1], p.y);
+        bl[2] = fminf(bl[2], p.z); bh[2] = fmaxf(bh[2], p.z);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        for (int sft = 16; sft > 0; sft >>= 1) {
+          sq[q] += shfl_xor_i128(sq[q], sft);
+          bits[q] |= (unsigned __int128)shfl_xor_i128(__int128(bits[q]), sft);
+          fa[q] = __fadd_ru(fa[q], __shfl_xor_sync(0xffffffffu, fa[q], sft));
+        }
+      }
+      int em[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const bool tq = __any_sync(0xffffffffu, trn[q]);
+        const int l = lsb_of(bits[q]);
+        em[q] = tq ? kFix - 1 : (l < 0 ? INT_MAX : kFix + l);
+      }
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        bl[d] = warp_min(bl[d]);
+        bh[d] = warp_max(bh[d]);
+      }
+      const bool wovf = __any_sync(0xffffffffu, ovf);
+      SubWarpStats &W = nw == 1 ? lst[f - f0] : wst[warp];
+      if (lane == 0) {
+        for (int q = 0; q < 4; ++q) {
+          W.s[q] = sq[q];
+          W.a[q] = double(fa[q]);
+          W.emin[q] = em[q];
+        }
+        for (int d = 0; d < 3; ++d) {
+          W.lo[d] = bl[d];
+          W.hi[d] = bh[d];
+        }
+        W.ovf = wovf ? 1 : 0;
+      }
+      if (nw > 1) {
+        team_sync(team, nw);
+        if (tl == 0) {
+          SubWarpStats T = wst[w0];
+          for (int w = 1; w < nw; ++w) {
+            const SubWarpStats &V = wst[w0 + w];
+            for (int q = 0; q < 4; ++q) {
+              T.s[q] += V.s[q];
+              T.a[q] += V.a[q];
+              T.emin[q] = min(T.emin[q], V.emin[q]);
+            }
+            for (int d = 0; d < 3; ++d) {
+              T.lo[d] = fminf(T.lo[d], V.lo[d]);
+              T.hi[d] = fmaxf(T.hi[d], V.hi[d]);
+            }
+            T.ovf |= V.ovf;
+          }
+          lst[f - f0] = T;
+        }
+        team_sync(team, nw);
+      }
+    }
+    __syncthreads();
+    // ---- the level's decisions, a thread per node (the FP64 certification
+    // runs on whole warps) ----
+    for (int f = f0 + int(threadIdx.x); f < f1; f += kSubThreads) {
+      DNode N = loc[f];
+      const int c = N.count;
+      if (c == 0) continue;  // an empty root (no particles) stays as it is
+      SubWarpStats T = lst[f - f0];
+      if (!decide_node(N, T.s, T.a, T.lo, T.hi, T.emin, T.ovf != 0, force_fallback, nd)) {
+        // the reference's own sum: double, in array order (BGQCM.c:181-212)
+        const int64_t o = N.offset;
+        double x = 0, y = 0, z = 0, m = 0;
+        for (int i = 0; i < c; ++i) {
+          const float4 p = src[o + i];
+          x = __dadd_rn(x, double(fmul_(p.w, p.x)));
+          y = __dadd_rn(y, double(fmul_(p.w, p.y)));
+          z = __dadd_rn(z, double(fmul_(p.w, p.z)));
+          m = __dadd_rn(m, double(p.w));
+        }
+        N.xc[0] = __double2float_rn(__ddiv_rn(x, m));
+        N.xc[1] = __double2float_rn(__ddiv_rn(y, m));
+        N.xc[2] = __double2float_rn(__ddiv_rn(z, m));
+        ++nfb;
+      }
+      loc[f] = N;
+    }
+    __syncthreads();
+    // ---- partition at the centre of mass: a team per node ----
+    for (int f = f0 + team; f < f1; f += nteams) {
+      DNode N = loc[f];
+      const int c = N.count;
+      if (c == 0) continue;
+      const int64_t o = N.offset;
+      const int lo_off = int(o - roff);  // the node's first element in the subtree
+      const int d = N.split_dim;
+      if (d < 0) {
+        // a leaf: its elements into the other buffer as well
+        for (int e = tl; e < c; e += TN) {
+          dst[o + e] = src[o + e];
+          doid[o + e] = soid[o + e];
+        }
+        continue;
+      }
+      if (tl == 0) tflag[team] = 0;
+      const float split = N.xc[d];
+      const int share = (((c + nw - 1) / nw) + 31) & ~31;
+      const int beg = wi * share, end = min(c, beg + share);
+      int cl = 0;
+      for (int e0 = beg; e0 < end; e0 += 32) {
+        const int e = e0 + lane;
+        const bool l = e < end && key_of(src[o + e], d) < split;
+        cl += __popc(__ballot_sync(0xffffffffu, l));
+      }
+      if (lane == 0) wtot[warp] = cl;
+      team_sync(team, nw);
+      int rank = 0, nleft = 0;
+      for (int w = 0; w < nw; ++w) {
+        const int v = wtot[w0 + w];
+        rank += w < wi ? v : 0;
+        nleft += v;
+      }
+      for (int e0 = beg; e0 < end; e0 += 32) {
+        const int e = e0 + lane;
+        float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
+        int32_t id = 0;
+        if (e < end) {
+          p = src[o + e];
+          id = soid[o + e];
+        }
+        const bool l = e < end && key_of(p, d) < split;
+        const unsigned bal = __ballot_sync(0xffffffffu, l);
+        if (l) {
+          const int q = rank + __popc(bal & below);
+          dst[o + q] = p;
+          doid[o + q] = id;
+          sidx[lo_off + q] = e;
+        } else if (e < end && e >= nleft) {
+          // a right element at or after nleft: no swap touches it
+          dst[o + e] = p;
+          doid[o + e] = id;
+        }
+        rank += __popc(bal);
+      }
+      team_sync(team, nw);
+      for (int e = tl; e < nleft; e += TN) {
+        const float4 p = src[o + e];
+        if (key_of(p, d) < split) continue;
+        int q = e, steps = 0;
+        bool bad = false;
+        while (q < nleft && steps < kChainSteps) {
+          const int nq = sidx[lo_off + q];
+          if (nq <= q || nq >= c) {  // cannot happen for a valid partition
+            bad = true;
+            break;
+          }
+          q = nq;
+          ++steps;
+        }
+        if (bad) {
+          atomicExch(reinterpret_cast<int32_t *>(counters + C_ERR), 2);
+          continue;
+        }
+        if (q < nleft) {
+          tflag[team] = 1;
+          continue;
+        }
+        dst[o + q] = p;
+        doid[o + q] = soid[o + e];
+      }
+      team_sync(team, nw);
+      if (tflag[team]) {
+        // pointer jumping: afterwards sidx[q] is the end of the chain through q
+        for (int round = 0;; ++round) {
+          team_sync(team, nw);
+          if (tl == 0) tflag[team] = 0;
+          team_sync(team, nw);
+          bool ch = false;
+          for (int q = tl; q < nleft; q += TN) {
+            const int j = sidx[lo_off + q];
+            if (j != q && j < nleft) {  // j == q: a left element no swap moves
+              sidx[lo_off + q] = sidx[lo_off + j];
+              ch = true;
+            }
+          }
+          if (__any_sync(0xffffffffu, ch) && lane == 0) tflag[team] = 1;
+          team_sync(team, nw);
+          if (!tflag[team]) break;
+          if (round > 40) {  // cannot happen for a valid partition
+            if (tl == 0) atomicExch(reinterpret_cast<int32_t *>(counters + C_ERR), 2);
+            break;
+          }
+        }
+        for (int e = tl; e < nleft; e += TN) {
+          const float4 p = src[o + e];
+          if (key_of(p, d) < split) continue;
+          const int q = sidx[lo_off + e];
+          if (q < nleft || q >= c) {
+            atomicExch(reinterpret_cast<int32_t *>(counters + C_ERR), 2);
+            continue;
+          }
+          dst[o + q] = p;
+          doid[o + q] = soid[o + e];
+        }
+      }
+      if (tl == 0) {
+        N.nleft = nleft;
+        loc[f] = N;
+      }
+      team_sync(team, nw);
+    }
+    __syncthreads();
+    // ---- children: two per node split into two non-empty parts ----
+    int base = f1;
+    for (int c0 = f0; c0 < f1; c0 += kSubThreads) {
+      const int f = c0 + int(threadIdx.x);
+      int flag = 0;
+      DNode N;
+      if (f < f1) {
+        N = loc[f];
+        flag = (N.split_dim >= 0 && N.nleft > 0 && N.nleft < N.count) ? 1 : 0;
+      }
+      int tot = 0;
+      const int rk = block_excl_scan(flag, sh_warp, &tot);
+      if (f < f1) {
+        if (flag) {
+          const int cl = base + 2 * rk;
+          N.cl = cl;
+          N.cr = cl + 1;
+          write_child(loc[cl], N, 0);
+          write_child(loc[cl + 1], N, 1);
+        } else {
+          N.cl = N.cr = 0;
+        }
+        loc[f].cl = N.cl;
+        loc[f].cr = N.cr;
+      }
+      base += 2 * tot;
+    }
+    if (threadIdx.x == 0) s_nsplit = (base - f1) / 2;
+    __syncthreads();
+    const int nsplit = s_nsplit;
+    f0 = f1;
+    f1 += 2 * nsplit;
+    ++depth;
+    if (threadIdx.x == 0) first[depth + 1] = f1;
+    if (f1 > f0 && depth >= kSubDepth) {  // deeper than the bookkeeping holds
+      if (threadIdx.x == 0) atomicExch(reinterpret_cast<int32_t *>(counters + C_ERR), 4);
+      return;
+    }
+    {
+      const float4 *t = src;
+      src = dst;
+      dst = const_cast<float4 *>(t);
+      const int32_t *u = soid;
+      soid = doid;
+      doid = const_cast<int32_t *>(u);
+    }
+    __syncthreads();
+  }
+  if (nfb) atomicAdd((unsigned long long *)&counters[C_SUBFB], (unsigned long long)nfb);
+  // per depth: first local node and count (depth 0 is the root)
+  for (int dd = int(threadIdx.x); dd <= kSubDepth + 1; dd += kSubThreads)
+    sub_first[int64_t(r) * (kSubDepth + 2) + dd] = dd <= depth + 1 ? first[min(dd, depth + 1)] : f1;
+  for (int dd = 1 + int(threadIdx.x); dd <= kSubDepth; dd += kSubThreads)
+    hist[int64_t(dd - 1) * nroots + r] = dd <= depth ? first[dd + 1] - first[dd] : 0;
+}
+
+// Node totals of every depth below the subtree roots, into tot[0..kSubDepth).
+__global__ void k_subtree_totals(const int64_t *hist, int32_t nroots, int64_t *tot) {
+  const int dd = blockIdx.x;
+  int64_t v = 0;
+  for (int32_t r = threadIdx.x; r < nroots; r += blockDim.x) v += hist[int64_t(dd) * nroots + r];
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __shared__ int64_t part[32];
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = v;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int64_t t = 0;
+    for (int w = 0; w < int(blockDim.x >> 5); ++w) t += part[w];
+    tot[dd] = t;
+  }
+}
+
+// Copies every subtree node to its place among the levels: depth d below the
+// roots is level nb-level + d, ordered by root (i.e. by offset) and, within a
+// root, by the block's breadth-first order (also by offset).  pos holds the
+// exclusive scan of hist (depth-major), ne the first index after the roots'
+// level.
+__global__ void k_subtree_place(DNode *nodes, int32_t nb, int32_t ne, const DNode *sub,
+                                const int32_t *sub_first, const int64_t *pos) {
+  __shared__ int fs[kSubDepth + 2];
+  const int32_t r = int32_t(blockIdx.x);
+  const int32_t nroots = ne - nb;
+  for (int dd = threadIdx.x; dd <= kSubDepth + 1; dd += blockDim.x)
+    fs[dd] = sub_first[int64_t(r) * (kSubDepth + 2) + dd];
+  __syncthreads();
+  const int32_t roff = nodes[nb + r].offset;
+  const DNode *loc = sub + 2 * int64_t(roff);
+  const int total = fs[kSubDepth + 1];
+  auto depth_of = [&](int j) {
+    int dd = 1;
+    while (dd <= kSubDepth && fs[dd + 1] <= j) ++dd;
+    return dd;
+  };
+  auto global = [&](int j, int dd) {
+    return int32_t(ne + pos[int64_t(dd - 1) * nroots + r] + (j - fs[dd]));
+  };
+  for (int j = 1 + int(threadIdx.x); j < total; j += blockDim.x) {
+    const int dd = depth_of(j);
+    DNode N = loc[j];
+    if (N.cl) {
+      N.cl = global(N.cl, dd + 1);
+      N.cr = global(N.cr, dd + 1);
+    }
+    nodes[global(j, dd)] = N;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    DNode N = loc[0];
+    if (N.cl) {
+      N.cl = global(N.cl, 1);
+      N.cr = global(N.cr, 1);
+    }
+    nodes[nb + r] = N;
+  }
+}
+
 // 1 for nodes whose split produced two non-empty children.  (The element
 // buffers alternate between levels; a leaf's elements are copied once into
 // the next level's buffer by k_part_left, after which both buffers hold them
@@ -2323,10 +2773,12 @@ DeviceTree::~DeviceTree() {
   void *ptrs[] = {epos_, tpos_, oid_, toid_, idx_, nodes_, ppm_, chunk_node_, chunk_base_, part_,
                   left_cnt_, left_base_, scan_tmp_, node_tmp_, fallback_, counters_, leaf_ids_,
                   leaf_tmp_, leafdesc_, segs_, idx_list_, table_, items_, items_tmp_, gidx_,
-                  tight_chunks_, tight_nodes_, segs_local_, ridx_};
+                  tight_chunks_, tight_nodes_, segs_local_, ridx_, sub_nodes_, sub_first_,
+                  sub_hist_, sub_pos_, sub_tot_, sub_stats_};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h_counters_) cudaFreeHost(h_counters_);
+  if (h_sub_) cudaFreeHost(h_sub_);
 }
 
 template <typename T>
@@ -2413,6 +2865,66 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   }
   while (ne > nb) {
     const int32_t L = ne - nb;
+    if (!sub_off_ && cfg.force_cm_fallback != 2 && level_max <= kSubMax) {
+      // every node of this level fits one block: each builds its whole subtree
+      DT_CHECK(grow(sub_nodes_, cap_sub_, size_t(2 * std::max<int64_t>(n, 1)), s));
+      DT_CHECK(grow(sub_stats_, cap_ss_, size_t(std::max<int64_t>(n, 1)) * sizeof(SubWarpStats), s));
+      DT_CHECK(grow(sub_first_, cap_sf_, size_t(L) * (kSubDepth + 2), s));
+      DT_CHECK(grow(sub_hist_, cap_sh_, size_t(L) * kSubDepth + 1, s));
+      DT_CHECK(grow(sub_pos_, cap_sp_, size_t(L) * kSubDepth + 1, s));
+      DT_CHECK(grow(sub_tot_, cap_st_, size_t(kSubDepth), s));
+      DT_CHECK(grow(scan_tmp_, cap_scan_, size_t(scan_tmp_size(int64_t(L) * kSubDepth)), s));
+      if (!h_sub_) DT_CHECK(cudaHostAlloc(&h_sub_, kSubDepth * sizeof(int64_t), cudaHostAllocDefault));
+      if (!sub_attr_) {
+        DT_CHECK(cudaFuncSetAttribute(k_subtree, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      kSubMax * int(sizeof(int32_t))));
+        sub_attr_ = true;
+      }
+      const size_t smem = size_t(std::max<int64_t>(level_max, 1)) * sizeof(int32_t);
+      k_subtree<<<unsigned(L), kSubThreads, smem, s>>>(
+          nodes_, nb, ne, epos_, oid_, tpos_, toid_, sub_nodes_,
+          reinterpret_cast<SubWarpStats *>(sub_stats_), sub_first_, sub_hist_,
+          cfg.force_cm_fallback, cfg.nd, counters_);
+      ++info_.launches;
+      DT_CHECK(cudaGetLastError());
+      DT_CHECK(scan_counted(sub_hist_, sub_pos_, int64_t(L) * kSubDepth, nullptr, scan_tmp_, s));
+      k_subtree_totals<<<kSubDepth, 256, 0, s>>>(sub_hist_, L, sub_tot_);
+      ++info_.launches;
+      DT_CHECK(cudaGetLastError());
+      DT_CHECK(cudaMemcpyAsync(h_sub_, sub_tot_, kSubDepth * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+      DT_CHECK(cudaMemcpyAsync(h_counters_, counters_, C_COUNT * sizeof(int64_t),
+                               cudaMemcpyDeviceToHost, s));
+      DT_CHECK(cudaStreamSynchronize(s));
+      const int32_t serr = *reinterpret_cast<const int32_t *>(h_counters_ + C_ERR);
+      if (serr == 4) {
+        // a subtree deeper than kSubDepth levels: build again level by level
+        sub_off_ = true;
+        const cudaError_t e = build(cfg, n, pos_in, jsplit, s);
+        sub_off_ = false;
+        return e;
+      }
+      if (serr) {
+        err_ = serr == 3 ? "subtree: a node outgrew the block's shared memory"
+                         : "partition chain check failed";
+        return cudaErrorUnknown;
+      }
+      info_.cm_fallbacks += h_counters_[C_SUBFB];
+      int64_t total = ne;
+      for (int d = 0; d < kSubDepth; ++d) total += h_sub_[d];
+      if (total > INT32_MAX) return cudaErrorInvalidValue;
+      DT_CHECK(grow(nodes_, cap_nodes_, size_t(total), s, true));
+      k_subtree_place<<<unsigned(L), 256, 0, s>>>(nodes_, nb, ne, sub_nodes_, sub_first_, sub_pos_);
+      ++info_.launches;
+      DT_CHECK(cudaGetLastError());
+      int64_t at = ne;
+      level_begin.push_back(ne);
+      for (int d = 0; d < kSubDepth && h_sub_[d] > 0; ++d) {
+        at += h_sub_[d];
+        level_begin.push_back(int32_t(at));
+      }
+      nb = ne = int32_t(total);
+      break;
+    }
     if (size_t(ne) + 2 * size_t(L) > cap_nodes_)
       DT_CHECK(grow(nodes_, cap_nodes_, size_t(ne) + 2 * size_t(L), s, true));
     DT_CHECK(grow(node_tmp_, cap_nt_, size_t(L) + 1, s));

@@ -72,7 +72,9 @@ class DeviceTree {
   // input index, `table()` holds the position table (particles in tree order,
   // then tdpts pseudo-particles per node), and the processed leaves' lists,
   // work items and group index are built.  `jsplit` bounds the list range of
-  // one work item.  Synchronizes `s` a few times per tree level.
+  // one work item.  Synchronizes `s` once per tree level down to the first
+  // level whose nodes all fit one block; that level's subtrees are built
+  // whole, one block each, with one synchronisation.
   cudaError_t build(const TreeConfig &cfg, int64_t n, const float4 *pos_in, int64_t jsplit,
                     cudaStream_t s);
 
@@ -165,6 +167,17 @@ class DeviceTree {
   int32_t *gidx_ = nullptr;
   size_t cap_gidx_ = 0;
   int32_t *walk_err_ = nullptr;
+  // whole subtrees in one block (k_subtree): node scratch, per-root depth
+  // bookkeeping, placement offsets, per-depth totals (and their pinned copy)
+  DNode *sub_nodes_ = nullptr;
+  unsigned char *sub_stats_ = nullptr;  // reduced statistics of a level's nodes
+  size_t cap_ss_ = 0;
+  int32_t *sub_first_ = nullptr;
+  int64_t *sub_hist_ = nullptr, *sub_pos_ = nullptr, *sub_tot_ = nullptr;
+  size_t cap_sub_ = 0, cap_sf_ = 0, cap_sh_ = 0, cap_sp_ = 0, cap_st_ = 0;
+  int64_t *h_sub_ = nullptr;
+  bool sub_attr_ = false;
+  bool sub_off_ = false;  // this build runs every level in the level loop
 };
 
 // Gathers the caller's arrays into tree order: out[i] = in[perm[i]].

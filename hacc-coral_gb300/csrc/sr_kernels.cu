@@ -462,12 +462,20 @@ cudaError_t launch_tag_items(const PairItem *in, PairItem *out, int64_t n, int b
 // Adjoint of the batched kernel.  For a pair (i, j) with d = x_j - x_i,
 // r2 = |d|^2 and w = fcoeff m_i m_j:
 //   d dv_i / d x_j = w (g(r2) I + 2 g'(r2) d d^T) =: M,  d dv_i / d x_i = -M,
-// so the pair adds M u_i to xbar_j and subtracts it from xbar_i.  The i side
-// accumulates in registers; the j side is summed over the warp's lanes and
-// added with one atomic per kept entry.
+// so the pair adds v = M u_i to xbar_j and subtracts it from xbar_i.  Each
+// pair's v is computed once, lanes = the group's particles and two buffered
+// entries per step on packed FP32: the particle side accumulates in
+// registers, and the entry side goes through shared memory -- for 16 buffered
+// entries at a time every lane writes its v into one row per entry, and then
+// 16 lanes each sum one entry's row (16-byte loads) and add it with one
+// atomic triple.  Self entries (j = i) are skipped: their two terms cancel.
 // ---------------------------------------------------------------------------
+constexpr int kVjpRow = 36;   // floats per transpose row: 32 particles, 16-byte rows
+constexpr int kVjpRows = 16;  // entries per transpose
+constexpr size_t kVjpSmem = size_t(kBatchedWarps) * 3 * kVjpRows * kVjpRow * sizeof(float);
+
 template <int LAW, bool MULTI>
-__global__ void __launch_bounds__(32 * kBatchedWarps)
+__global__ void __launch_bounds__(32 * kBatchedWarps, 2)
     k_pairs_vjp(const float4 *__restrict__ pos_, const PairItem *__restrict__ items, int64_t nitems,
                 const int32_t *__restrict__ gidx_, const int32_t *__restrict__ idx_,
                 const float *__restrict__ ux_, const float *__restrict__ uy_,
@@ -475,19 +483,19 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
                 float *__restrict__ xbz_, float fcoeff_, float rsm2_, float rcut2_, float rcull2_,
                 unsigned long long *__restrict__ queue, const VjpBoxDesc *__restrict__ boxes) {
   // kept entries, two per slot pair as in k_pairs_batched: (x, x', y, y'),
-  // (z, z', m, m') and their table indices; the group's particles, two per
-  // slot pair: (x, x', y, y'), (z, z', w, w'), (u0, u0', u1, u1'),
-  // (u2, u2', index bits, index bits')
+  // (z, z', m, m') and their table indices
   __shared__ float4 bufA[kBatchedWarps][33], bufB[kBatchedWarps][33];
   __shared__ int32_t bufI[kBatchedWarps][66];
-  __shared__ float4 grp[kBatchedWarps][4][16];
+  // per warp, the entry side's transpose: rows (component, entry) of the 32
+  // particles' v
+  extern __shared__ float4 vjp_rows[];
   const int lane = threadIdx.x & 31;
   const int w = threadIdx.x >> 5;
   const unsigned full = 0xffffffffu;
   const unsigned below = (1u << lane) - 1u;
   float *const fa = reinterpret_cast<float *>(bufA[w]);
   float *const fb = reinterpret_cast<float *>(bufB[w]);
-  float *const fg = reinterpret_cast<float *>(grp[w]);
+  float *const tv = reinterpret_cast<float *>(vjp_rows) + size_t(w) * 3 * kVjpRows * kVjpRow;
   for (;;) {
     unsigned long long it = 0;
     if (lane == 0) it = atomicAdd(queue, 1ull);
@@ -536,18 +544,6 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
     const float hy = fmaf(fmaxf(fabsf(loy), fabsf(hiy)), 4.8e-7f, 0.5f * (hiy - loy));
     const float hz = fmaf(fmaxf(fabsf(loz), fabsf(hiz)), 4.8e-7f, 0.5f * (hiz - loz));
     const float cx = 0.5f * (lox + hix), cy = 0.5f * (loy + hiy), cz = 0.5f * (loz + hiz);
-    // the group in shared memory for the entry-side pass
-    {
-      const int o = 4 * (lane >> 1) + (lane & 1);
-      fg[o] = P.x;
-      fg[o + 2] = P.y;
-      fg[64 + o] = P.z;
-      fg[64 + o + 2] = wi;
-      fg[128 + o] = u0;
-      fg[128 + o + 2] = u1;
-      fg[192 + o] = u2;
-      fg[192 + o + 2] = __int_as_float(act ? pi : -1);
-    }
     const float2 nxi = make_float2(-P.x, -P.x), nyi = make_float2(-P.y, -P.y),
                  nzi = make_float2(-P.z, -P.z);
     const float2 wi2 = make_float2(wi, wi), ua = make_float2(u0, u0), ub = make_float2(u1, u1),
@@ -591,59 +587,58 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
         bufI[w][lane] = -2;
       }
       __syncwarp();
-      // particle side: lanes are the group's particles, two entries a step
-      for (int q = 0; q < (ne + 1) / 2; ++q) {
-        const float4 A = bufA[w][q], B = bufB[w][q];
-        const int ja = bufI[w][2 * q], jb = bufI[w][2 * q + 1];
-        const float2 ex = __fadd2_rn(make_float2(A.x, A.y), nxi);
-        const float2 ey = __fadd2_rn(make_float2(A.z, A.w), nyi);
-        const float2 ez = __fadd2_rn(make_float2(B.x, B.y), nzi);
-        const float2 r2 = __ffma2_rn(ex, ex, __ffma2_rn(ey, ey, __fmul2_rn(ez, ez)));
-        const bool on_a = act && ja != pi && in_range<LAW>(r2.x, rcut2);
-        const bool on_b = act && jb != pi && in_range<LAW>(r2.y, rcut2);
-        float2 vx, vy, vz;
-        vjp2_term<LAW>(ex, ey, ez, __fmul2_rn(wi2, make_float2(B.z, B.w)), ua, ub, uc, rsm2, on_a,
-                       on_b, vx, vy, vz);
-        bx = __fadd2_rn(bx, vx);
-        by = __fadd2_rn(by, vy);
-        bz = __fadd2_rn(bz, vz);
-      }
-      // entry side: lanes are the buffered entries, two particles a step
-      if (lane < ne) {
-        const int o = 4 * (lane >> 1) + (lane & 1);
-        const float xj = fa[o], yj = fa[o + 2], zj = fb[o], mj = fb[o + 2];
-        const int jt = bufI[w][lane];
-        const float2 xj2 = make_float2(xj, xj), yj2 = make_float2(yj, yj),
-                     zj2 = make_float2(zj, zj), mj2 = make_float2(mj, mj);
-        float2 ex2 = make_float2(0.f, 0.f), ey2 = ex2, ez2 = ex2;
-        const int np2 = (W.g_count + 1) / 2;
-        for (int q = 0; q < np2; ++q) {
-          const float4 G0 = grp[w][0][q], G1 = grp[w][1][q], G2 = grp[w][2][q],
-                       G3 = grp[w][3][q];
-          // e = x_j - x_i
-          const float2 ex = __fadd2_rn(xj2, make_float2(-G0.x, -G0.y));
-          const float2 ey = __fadd2_rn(yj2, make_float2(-G0.z, -G0.w));
-          const float2 ez = __fadd2_rn(zj2, make_float2(-G1.x, -G1.y));
+      for (int h = 0; 16 * h < ne; ++h) {
+        // entries 16h .. 16h + 15 of the buffer
+        const int q1 = min(8 * h + 8, (ne + 1) / 2);
+        for (int q = 8 * h; q < q1; ++q) {
+          const float4 A = bufA[w][q], B = bufB[w][q];
+          const int ja = bufI[w][2 * q], jb = bufI[w][2 * q + 1];
+          const float2 ex = __fadd2_rn(make_float2(A.x, A.y), nxi);
+          const float2 ey = __fadd2_rn(make_float2(A.z, A.w), nyi);
+          const float2 ez = __fadd2_rn(make_float2(B.x, B.y), nzi);
           const float2 r2 = __ffma2_rn(ex, ex, __ffma2_rn(ey, ey, __fmul2_rn(ez, ez)));
-          const int ia = __float_as_int(G3.z), ib = __float_as_int(G3.w);
-          const bool on_a = ia >= 0 && jt != ia && in_range<LAW>(r2.x, rcut2);
-          const bool on_b = ib >= 0 && jt != ib && in_range<LAW>(r2.y, rcut2);
+          const bool on_a = act && ja != pi && in_range<LAW>(r2.x, rcut2);
+          const bool on_b = act && jb != pi && in_range<LAW>(r2.y, rcut2);
           float2 vx, vy, vz;
-          vjp2_term<LAW>(ex, ey, ez, __fmul2_rn(make_float2(G1.z, G1.w), mj2),
-                         make_float2(G2.x, G2.y), make_float2(G2.z, G2.w),
-                         make_float2(G3.x, G3.y), rsm2, on_a, on_b, vx, vy, vz);
-          ex2 = __fadd2_rn(ex2, vx);
-          ey2 = __fadd2_rn(ey2, vy);
-          ez2 = __fadd2_rn(ez2, vz);
+          vjp2_term<LAW>(ex, ey, ez, __fmul2_rn(wi2, make_float2(B.z, B.w)), ua, ub, uc, rsm2,
+                         on_a, on_b, vx, vy, vz);
+          bx = __fadd2_rn(bx, vx);
+          by = __fadd2_rn(by, vy);
+          bz = __fadd2_rn(bz, vz);
+          float *row = tv + (2 * q - 16 * h) * kVjpRow + lane;
+          row[0] = vx.x;
+          row[kVjpRow] = vx.y;
+          row[kVjpRows * kVjpRow] = vy.x;
+          row[(kVjpRows + 1) * kVjpRow] = vy.y;
+          row[2 * kVjpRows * kVjpRow] = vz.x;
+          row[(2 * kVjpRows + 1) * kVjpRow] = vz.y;
         }
-        const float vx = ex2.x + ex2.y, vy = ey2.x + ey2.y, vz = ez2.x + ez2.y;
-        if (vx != 0.f || vy != 0.f || vz != 0.f) {
-          atomicAdd(xbx + jt, vx);
-          atomicAdd(xby + jt, vy);
-          atomicAdd(xbz + jt, vz);
+        __syncwarp();
+        // entry side: lane e sums entry 16h + e's row of each component
+        const int e = 16 * h + lane;
+        if (lane < 16 && e < ne) {
+          float sum[3];
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const float4 *row =
+                reinterpret_cast<const float4 *>(tv + (c * kVjpRows + lane) * kVjpRow);
+            float2 s2 = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int k = 0; k < 8; ++k) {
+              const float4 t = row[k];
+              s2 = __fadd2_rn(s2, __fadd2_rn(make_float2(t.x, t.y), make_float2(t.z, t.w)));
+            }
+            sum[c] = s2.x + s2.y;
+          }
+          const int jt = bufI[w][e];
+          if (sum[0] != 0.f || sum[1] != 0.f || sum[2] != 0.f) {
+            atomicAdd(xbx + jt, sum[0]);
+            atomicAdd(xby + jt, sum[1]);
+            atomicAdd(xbz + jt, sum[2]);
+          }
         }
+        __syncwarp();
       }
-      __syncwarp();
       // keep what is past the first 32 (slot pairs 16.. move to 0..)
       if (nbuf > 32) {
         if (2 * lane < nbuf - 32) {
@@ -664,43 +659,65 @@ __global__ void __launch_bounds__(32 * kBatchedWarps)
   }
 }
 
+namespace {
+// Shared memory opt-in and resident CTAs of one VJP instantiation (cached
+// per device).
+template <int LAW, bool MULTI>
+int vjp_ctas(int64_t nitems) {
+  constexpr int kDev = 64;
+  static int per[kDev] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int pc = dev >= 0 && dev < kDev ? per[dev] : 0;
+  if (pc == 0) {
+    cudaFuncSetAttribute(k_pairs_vjp<LAW, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(kVjpSmem));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pc, k_pairs_vjp<LAW, MULTI>, 32 * kBatchedWarps,
+                                                  kVjpSmem);
+    if (pc < 1) pc = 1;
+    if (dev >= 0 && dev < kDev) per[dev] = pc;
+  }
+  const int64_t ctas = int64_t(sm_count()) * pc;
+  const int64_t need = (nitems + kBatchedWarps - 1) / kBatchedWarps;
+  return int(ctas < need ? ctas : need);
+}
+}  // namespace
+
 cudaError_t launch_pairs_vjp(int law, const float4 *pos, const PairItem *items, int64_t nitems,
                              const int32_t *gidx, const int32_t *idx, const float *ux,
                              const float *uy, const float *uz, float *xbx, float *xby, float *xbz,
                              float fcoeff, float rsm2, float rcut2, float rcull2,
                              unsigned long long *queue, int ctas, cudaStream_t s) {
+  (void)ctas;  // the VJP kernel's own occupancy sets its grid
   if (nitems <= 0) return cudaSuccess;
-  if (ctas <= 0) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    ctas = batched_resident_ctas(dev);
-  }
-  const int64_t need = (nitems + kBatchedWarps - 1) / kBatchedWarps;
-  if (ctas > need) ctas = int(need);
   if (law == LAW_POLY5_STEP16)
-    k_pairs_vjp<LAW_POLY5_STEP16, false><<<ctas, 32 * kBatchedWarps, 0, s>>>(
-        pos, items, nitems, gidx, idx, ux, uy, uz, xbx, xby, xbz, fcoeff, rsm2, rcut2, rcull2, queue,
-        nullptr);
+    k_pairs_vjp<LAW_POLY5_STEP16, false>
+        <<<vjp_ctas<LAW_POLY5_STEP16, false>(nitems), 32 * kBatchedWarps, kVjpSmem, s>>>(
+            pos, items, nitems, gidx, idx, ux, uy, uz, xbx, xby, xbz, fcoeff, rsm2, rcut2, rcull2,
+            queue, nullptr);
   else
-    k_pairs_vjp<LAW_POLY6, false><<<ctas, 32 * kBatchedWarps, 0, s>>>(
-        pos, items, nitems, gidx, idx, ux, uy, uz, xbx, xby, xbz, fcoeff, rsm2, rcut2, rcull2, queue,
-        nullptr);
+    k_pairs_vjp<LAW_POLY6, false>
+        <<<vjp_ctas<LAW_POLY6, false>(nitems), 32 * kBatchedWarps, kVjpSmem, s>>>(
+            pos, items, nitems, gidx, idx, ux, uy, uz, xbx, xby, xbz, fcoeff, rsm2, rcut2, rcull2,
+            queue, nullptr);
   return cudaGetLastError();
 }
 
 cudaError_t launch_pairs_vjp_multi(int law, const VjpBoxDesc *boxes, const PairItem *items,
                                    int64_t nitems, unsigned long long *queue, int ctas,
                                    cudaStream_t s) {
+  (void)ctas;
   if (nitems <= 0) return cudaSuccess;
-  ctas = clamp_ctas(ctas, nitems);
   if (law == LAW_POLY5_STEP16)
-    k_pairs_vjp<LAW_POLY5_STEP16, true><<<ctas, 32 * kBatchedWarps, 0, s>>>(
-        nullptr, items, nitems, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
-        nullptr, 0.f, 0.f, 0.f, 0.f, queue, boxes);
+    k_pairs_vjp<LAW_POLY5_STEP16, true>
+        <<<vjp_ctas<LAW_POLY5_STEP16, true>(nitems), 32 * kBatchedWarps, kVjpSmem, s>>>(
+            nullptr, items, nitems, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+            nullptr, 0.f, 0.f, 0.f, 0.f, queue, boxes);
   else
-    k_pairs_vjp<LAW_POLY6, true><<<ctas, 32 * kBatchedWarps, 0, s>>>(
-        nullptr, items, nitems, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
-        nullptr, 0.f, 0.f, 0.f, 0.f, queue, boxes);
+    k_pairs_vjp<LAW_POLY6, true>
+        <<<vjp_ctas<LAW_POLY6, true>(nitems), 32 * kBatchedWarps, kVjpSmem, s>>>(
+            nullptr, items, nitems, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+            nullptr, 0.f, 0.f, 0.f, 0.f, queue, boxes);
   return cudaGetLastError();
 }
 

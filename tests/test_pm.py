@@ -470,8 +470,11 @@ def test_treepm_step_device_arrays_match_host(ctx):
     treepm.step_device(ctx, t, p0.n, T)
     q = {k: t[k].cpu().numpy() for k in synth.FIELDS}
     a, b = np.argsort(p.id), np.argsort(q["id"])
+    # the PM deposit adds with float atomics, so two runs differ in the last
+    # bits of the density; positions agree to a few ulps of their magnitude
     for k in ("x", "y", "z"):
-        assert np.abs(getattr(p, k)[a] - q[k][b]).max() < 1e-5, k
+        ref = getattr(p, k)[a]
+        assert np.abs(ref - q[k][b]).max() < 1e-6 * max(1.0, float(np.abs(ref).max())), k
     for k in ("vx", "vy", "vz"):
         ref = getattr(p, k)[a].astype(np.float64) - getattr(p0, k)[np.argsort(p0.id)]
         got = q[k][b].astype(np.float64) - getattr(p0, k)[np.argsort(p0.id)]
