@@ -348,6 +348,77 @@ __device__ __forceinline__ void fix_add(__int128 &acc, unsigned __int128 &bits, 
   acc += (b >> 31) ? -__int128(v) : __int128(v);
 }
 
+// The same sum on four 32-bit limbs (two's complement, least significant
+// first): a term t 2^-kFix with 0 <= shift <= 39 (2^-24 <= |t| < 2^14, the
+// common case) is m << shift on two limbs, added (or subtracted) with one
+// carry chain on the integer pipe; other terms take fix_add's wide path.
+struct FixAcc {
+  uint32_t l[4];  // the sum
+  uint32_t b[4];  // OR of the terms' magnitudes
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int k = 0; k < 4; ++k) l[k] = b[k] = 0u;
+  }
+  __device__ __forceinline__ void add_limbs(uint32_t v0, uint32_t v1, uint32_t v2, uint32_t v3,
+                                            bool neg) {
+    b[0] |= v0;
+    b[1] |= v1;
+    b[2] |= v2;
+    b[3] |= v3;
+    if (neg) {
+      asm("sub.cc.u32 %0, %0, %4;\n\tsubc.cc.u32 %1, %1, %5;\n\tsubc.cc.u32 %2, %2, %6;\n\t"
+          "subc.u32 %3, %3, %7;"
+          : "+r"(l[0]), "+r"(l[1]), "+r"(l[2]), "+r"(l[3])
+          : "r"(v0), "r"(v1), "r"(v2), "r"(v3));
+    } else {
+      asm("add.cc.u32 %0, %0, %4;\n\taddc.cc.u32 %1, %1, %5;\n\taddc.cc.u32 %2, %2, %6;\n\t"
+          "addc.u32 %3, %3, %7;"
+          : "+r"(l[0]), "+r"(l[1]), "+r"(l[2]), "+r"(l[3])
+          : "r"(v0), "r"(v1), "r"(v2), "r"(v3));
+    }
+  }
+  __device__ __forceinline__ void add(float t, bool &overflow, bool &trunc) {
+    const uint32_t bb = __float_as_uint(t);
+    const uint32_t a = bb & 0x7fffffffu;
+    if (a == 0) return;
+    int e = int(a >> 23);
+    uint32_t m = a & 0x7fffffu;
+    if (e == 0) e = 1;
+    else m |= 0x800000u;
+    const int sh = e - 150 - kFix;
+    const bool neg = (bb >> 31) != 0u;
+    if (sh >= 0 && sh < 32) {
+      add_limbs(m << sh, sh ? m >> (32 - sh) : 0u, 0u, 0u, neg);
+    } else if (sh >= 32 && sh <= 39) {
+      add_limbs(0u, m << (sh - 32), 0u, 0u, neg);  // m < 2^24: no bits past limb 1
+    } else {
+      __int128 w = 0;
+      unsigned __int128 wb = 0;
+      fix_add(w, wb, t, overflow, trunc);
+      const unsigned __int128 u = (unsigned __int128)w;  // +/- v in two's complement
+      const unsigned __int128 mag = neg ? (unsigned __int128)(-w) : u;
+      b[0] |= uint32_t(mag);
+      b[1] |= uint32_t(mag >> 32);
+      b[2] |= uint32_t(mag >> 64);
+      b[3] |= uint32_t(mag >> 96);
+      asm("add.cc.u32 %0, %0, %4;\n\taddc.cc.u32 %1, %1, %5;\n\taddc.cc.u32 %2, %2, %6;\n\t"
+          "addc.u32 %3, %3, %7;"
+          : "+r"(l[0]), "+r"(l[1]), "+r"(l[2]), "+r"(l[3])
+          : "r"(uint32_t(u)), "r"(uint32_t(u >> 32)), "r"(uint32_t(u >> 64)),
+            "r"(uint32_t(u >> 96)));
+    }
+  }
+  __device__ __forceinline__ __int128 sum() const {
+    const unsigned __int128 u = ((unsigned __int128)l[3] << 96) | ((unsigned __int128)l[2] << 64) |
+                                ((unsigned __int128)l[1] << 32) | (unsigned __int128)l[0];
+    return __int128(u);
+  }
+  __device__ __forceinline__ unsigned __int128 bits() const {
+    return ((unsigned __int128)b[3] << 96) | ((unsigned __int128)b[2] << 64) |
+           ((unsigned __int128)b[1] << 32) | (unsigned __int128)b[0];
+  }
+};
+
 __device__ __forceinline__ int lsb_of(unsigned __int128 v) {
   const unsigned long long lo = (unsigned long long)v, hi = (unsigned long long)(v >> 64);
   if (lo) return __ffsll((long long)lo) - 1;
@@ -413,6 +484,9 @@ __global__ void __launch_bounds__(kChunkThreads)
   // four loads in flight per thread; the elements are then taken in the same
   // order as one at a time
   constexpr int kU = 4;
+  FixAcc fx[4];
+#pragma unroll
+  for (int q = 0; q < 4; ++q) fx[q].zero();
   for (int k0 = tid; k0 < R.len; k0 += NT * kU) {
     float4 pu[kU];
 #pragma unroll
@@ -426,13 +500,18 @@ __global__ void __launch_bounds__(kChunkThreads)
       const float t[4] = {fmul_(w, p.x), fmul_(w, p.y), fmul_(w, p.z), w};
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
-        fix_add(s[q], bits[q], t[q], ovf, trn[q]);
+        fx[q].add(t[q], ovf, trn[q]);
         fa[q] = __fadd_ru(fa[q], fabsf(t[q]));
       }
       lo[0] = fminf(lo[0], p.x); hi[0] = fmaxf(hi[0], p.x);
       lo[1] = fminf(lo[1], p.y); hi[1] = fmaxf(hi[1], p.y);
       lo[2] = fminf(lo[2], p.z); hi[2] = fmaxf(hi[2], p.z);
     }
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    s[q] = fx[q].sum();
+    bits[q] = fx[q].bits();
   }
   double a[4];
   int emin[4];
@@ -1588,8 +1667,9 @@ __global__ void __launch_bounds__(kSubThreads, 2)
       const DNode N = loc[f];
       const int c = N.count;
       const int64_t o = N.offset;
-      __int128 sq[4] = {0, 0, 0, 0};
-      unsigned __int128 bits[4] = {0, 0, 0, 0};
+      FixAcc fx[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) fx[q].zero();
       float fa[4] = {0.f, 0.f, 0.f, 0.f};
       float bl[3] = {INFINITY, INFINITY, INFINITY}, bh[3] = {-INFINITY, -INFINITY, -INFINITY};
       bool ovf = false;
@@ -1600,12 +1680,19 @@ __global__ void __launch_bounds__(kSubThreads, 2)
         const float t[4] = {fmul_(w, p.x), fmul_(w, p.y), fmul_(w, p.z), w};
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          fix_add(sq[q], bits[q], t[q], ovf, trn[q]);
+          fx[q].add(t[q], ovf, trn[q]);
           fa[q] = __fadd_ru(fa[q], fabsf(t[q]));
         }
         bl[0] = fminf(bl[0], p.x); bh[0] = fmaxf(bh[0], p.x);
         bl[1] = fminf(bl[1], p.y); bh[1] = fmaxf(bh[1], p.y);
         bl[2] = fminf(bl[2], p.z); bh[2] = fmaxf(bh[2], p.z);
+      }
+      __int128 sq[4];
+      unsigned __int128 bits[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        sq[q] = fx[q].sum();
+        bits[q] = fx[q].bits();
       }
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
