@@ -1160,11 +1160,15 @@ __device__ __forceinline__ int block_excl_scan(int v, int *sh_warp, int *total) 
   return excl;
 }
 
-// Left counts of each chunk of a splitting node.
+// Left counts of each chunk of a splitting node; in block mode also each
+// warp's left elements before its share of the chunk (the shares of
+// k_part_left: warp w takes [w * kChunk / 8, (w + 1) * kChunk / 8)).  Only
+// the split coordinate is loaded, every lane's loads in flight at once.
 template <bool WM>
 __global__ void __launch_bounds__(kChunkThreads)
     k_part_count(const float4 *__restrict__ pos, const DNode *nodes, const int32_t *chunk_node,
-                 const int64_t *chunk_base, int32_t nb, const int64_t *nchunk, int32_t *left_cnt) {
+                 const int64_t *chunk_base, int32_t nb, const int64_t *nchunk, int32_t *left_cnt,
+                 int32_t *wpre) {
   CHUNK_PROLOGUE
   const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
   const DNode &N = nodes[R.node];
@@ -1174,17 +1178,38 @@ __global__ void __launch_bounds__(kChunkThreads)
   }
   const int d = N.split_dim;
   const float split = N.xc[d];
-  int c = 0;
-  for (int k = tid; k < R.len; k += NT) c += key_of(pos[R.begin + k], d) < split;
+  const float *key = reinterpret_cast<const float *>(pos + R.begin) + d;
   if (WM) {
-    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    int c = 0;
+    for (int k = tid; k < R.len; k += NT) c += key[4 * k] < split;
+    c = __reduce_add_sync(0xffffffffu, c);
     if (lane_ == 0) left_cnt[chunk] = c;
     return;
   }
-  __shared__ int sw[32];
-  int tot;
-  block_excl_scan(c, sw, &tot);
-  if (threadIdx.x == 0) left_cnt[chunk] = tot;
+  constexpr int kWarps = kChunkThreads / 32, kSub = kChunk / kWarps, kPer = kSub / 32;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  float kv[kPer];
+#pragma unroll
+  for (int u = 0; u < kPer; ++u) {
+    const int e = warp * kSub + 32 * u + lane;
+    kv[u] = e < R.len ? key[4 * e] : INFINITY;
+  }
+  int c = 0;
+#pragma unroll
+  for (int u = 0; u < kPer; ++u) c += kv[u] < split;
+  c = __reduce_add_sync(0xffffffffu, c);
+  __shared__ int wt[kWarps];
+  if (lane == 0) wt[warp] = c;
+  __syncthreads();
+  if (threadIdx.x < kWarps) {
+    int pre = 0, tot = 0;
+    for (int w = 0; w < kWarps; ++w) {
+      pre += w < int(threadIdx.x) ? wt[w] : 0;
+      tot += wt[w];
+    }
+    wpre[chunk * kWarps + threadIdx.x] = pre;
+    if (threadIdx.x == 0) left_cnt[chunk] = tot;
+  }
 }
 
 // Per splitting node, a warp each: exclusive scan of its chunks' left counts
@@ -1216,16 +1241,18 @@ __global__ void k_part_node_scan(DNode *nodes, int32_t nb, int32_t ne, const int
 
 // Left particles go to their rank; idx[rank] records where each came from.
 // Warp w takes the chunk's elements [w * kSub, (w + 1) * kSub) 32 at a time
-// (coalesced); ranks follow array order through the warps' totals and a
-// ballot prefix within each step.
+// (coalesced), kB steps' loads in flight; ranks follow array order through
+// the warps' left counts before them (k_part_count) and a ballot prefix
+// within each step.
 template <bool WM>
 __global__ void __launch_bounds__(kChunkThreads)
     k_part_left(const float4 *__restrict__ pos, const int32_t *__restrict__ oid, const DNode *nodes,
                 const int32_t *chunk_node, const int64_t *chunk_base, int32_t nb,
-                const int64_t *nchunk, const int64_t *left_base, float4 *tpos, int32_t *toid,
-                int32_t *idx, int32_t *ridx) {
+                const int64_t *nchunk, const int64_t *left_base, const int32_t *wpre, float4 *tpos,
+                int32_t *toid, int32_t *idx, int32_t *ridx) {
   constexpr int kWarps = kChunkThreads / 32;
   constexpr int kSub = WM ? kChunk : kChunk / kWarps;  // a warp's share of the chunk
+  constexpr int kB = 4;
   CHUNK_PROLOGUE
   const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
   const DNode &N = nodes[R.node];
@@ -1239,45 +1266,47 @@ __global__ void __launch_bounds__(kChunkThreads)
   }
   const int d = N.split_dim;
   const float split = N.xc[d];
+  const int32_t off = N.offset, nleft = N.nleft;
   const int lane = threadIdx.x & 31, warp = WM ? 0 : int(threadIdx.x >> 5);
   const unsigned below = (1u << lane) - 1u;
   const int sub_end = min(kSub, R.len - warp * kSub);  // elements of this warp's share
-  int r = int(left_base[chunk]);
-  if (!WM) {
-    __shared__ int wtot[kWarps];
-    int c = 0;
-    for (int j = 0; j < sub_end; j += 32) {
-      const int e = warp * kSub + j + lane;
-      const bool l = e < R.len && key_of(pos[R.begin + e], d) < split;
-      c += __popc(__ballot_sync(0xffffffffu, l));
-    }
-    if (lane == 0) wtot[warp] = c;
-    __syncthreads();
-    for (int w = 0; w < warp; ++w) r += wtot[w];
-  }
-  for (int j = 0; j < sub_end; j += 32) {
-    const int e = warp * kSub + j + lane;
-    float4 p = make_float4(0.f, 0.f, 0.f, 0.f);
-    bool l = false;
-    if (e < R.len) {
-      p = pos[R.begin + e];
-      l = key_of(p, d) < split;
-    }
-    const unsigned bal = __ballot_sync(0xffffffffu, l);
-    const int q = r + __popc(bal & below);  // left elements before this one
-    if (l) {
-      tpos[N.offset + q] = p;
-      toid[N.offset + q] = oid[R.begin + e];
-      idx[N.offset + q] = R.local + e;
-    } else if (e < R.len) {
-      ridx[N.offset + (R.local + e - q)] = R.local + e;
-      if (R.local + e >= N.nleft) {
-        // a right element at or after nleft: no swap touches it, it stays
-        tpos[R.begin + e] = p;
-        toid[R.begin + e] = oid[R.begin + e];
+  int r = int(left_base[chunk]) + (WM ? 0 : wpre[chunk * kWarps + warp]);
+  for (int j0 = 0; j0 < sub_end; j0 += 32 * kB) {
+    float4 p[kB];
+    int32_t o[kB];
+#pragma unroll
+    for (int u = 0; u < kB; ++u) {
+      const int e = warp * kSub + j0 + 32 * u + lane;
+      if (j0 + 32 * u < sub_end && e < R.len) {
+        p[u] = pos[R.begin + e];
+        o[u] = oid[R.begin + e];
+      } else {
+        p[u] = make_float4(0.f, 0.f, 0.f, 0.f);
+        o[u] = 0;
       }
     }
-    r += __popc(bal);
+#pragma unroll
+    for (int u = 0; u < kB; ++u) {
+      if (j0 + 32 * u >= sub_end) break;  // the same for the whole warp
+      const int e = warp * kSub + j0 + 32 * u + lane;
+      const bool in = e < R.len;
+      const bool l = in && key_of(p[u], d) < split;
+      const unsigned bal = __ballot_sync(0xffffffffu, l);
+      const int q = r + __popc(bal & below);  // left elements before this one
+      if (l) {
+        tpos[off + q] = p[u];
+        toid[off + q] = o[u];
+        idx[off + q] = R.local + e;
+      } else if (in) {
+        ridx[off + (R.local + e - q)] = R.local + e;
+        if (R.local + e >= nleft) {
+          // a right element at or after nleft: no swap touches it, it stays
+          tpos[R.begin + e] = p[u];
+          toid[R.begin + e] = o[u];
+        }
+      }
+      r += __popc(bal);
+    }
   }
 }
 
@@ -1354,25 +1383,28 @@ __global__ void __launch_bounds__(kChunkThreads)
     }
     return;
   }
-  // Block mode: the thread's 16 elements follow their chains in lockstep, so
-  // up to 16 independent loads are in flight per step (chains run ~log n
-  // steps on cell-sorted input).
+  // Block mode: the thread's 16 elements take their first kPlainSteps steps
+  // in lockstep, so up to 16 independent loads are in flight per step (most
+  // chains end within a few).  The chains still running then go to a block
+  // queue and are followed a chain per thread, a run of equal steps at a time
+  // (chain_jump): a block's time is its longest chain, not the sum of one
+  // thread's long chains.
   constexpr int kPerT = kChunk / kChunkThreads;
+  __shared__ int32_t chain_q[kChunk];
+  __shared__ int16_t chain_k[kChunk];
+  __shared__ int chain_n;
+  if (threadIdx.x == 0) chain_n = 0;
+  const float *key = reinterpret_cast<const float *>(pos + R.begin) + d;
   int32_t q[kPerT];
   unsigned right = 0;
 #pragma unroll
   for (int j = 0; j < kPerT; ++j) {
     const int k = tid + j * NT;
     q[j] = R.local + k;
-    if (k < R.len && q[j] < is && !(key_of(pos[R.begin + k], d) < split)) right |= 1u << j;
+    if (k < R.len && q[j] < is && !(key[4 * k] < split)) right |= 1u << j;
   }
-  unsigned active = 0;
-#pragma unroll
-  for (int j = 0; j < kPerT; ++j)
-    if ((right >> j & 1u) && q[j] < is) active |= 1u << j;
+  unsigned active = right;
   bool bad = false;
-  // single steps first, all chains' loads in flight at once: most chains end
-  // within a few
   for (int32_t step = 0; active && step < kPlainSteps; ++step) {
     int32_t nq[kPerT];
 #pragma unroll
@@ -1390,21 +1422,14 @@ __global__ void __launch_bounds__(kChunkThreads)
       if (nq[j] >= is) active &= ~(1u << j);
     }
   }
-  // the longer ones a run of equal steps at a time (chain_jump)
+  __syncthreads();  // chain_n set
 #pragma unroll
   for (int j = 0; j < kPerT; ++j) {
     if (!(active >> j & 1u)) continue;
-    bool b = false;
-    for (int32_t it = 0; q[j] < is && it <= N.count && !b; ++it)
-      q[j] = chain_jump(q[j], is, nright, nidx, nridx, &b);
-    if (b || q[j] < is || q[j] >= N.count) {  // cannot happen for a valid partition
-      bad = true;
-      right &= ~(1u << j);
-      continue;
-    }
-    active &= ~(1u << j);
+    const int slot = atomicAdd(&chain_n, 1);  // at most one per element of the chunk
+    chain_q[slot] = q[j];
+    chain_k[slot] = int16_t(tid + j * NT);
   }
-  if (active || bad) atomicExch(err, 2);
 #pragma unroll
   for (int j = 0; j < kPerT; ++j) {
     if (!(right >> j & 1u) || (active >> j & 1u)) continue;
@@ -1412,6 +1437,22 @@ __global__ void __launch_bounds__(kChunkThreads)
     tpos[N.offset + q[j]] = pos[src];
     toid[N.offset + q[j]] = oid[src];
   }
+  __syncthreads();
+  const int nchain = chain_n;
+  for (int c = threadIdx.x; c < nchain; c += NT) {
+    int32_t qq = chain_q[c];
+    bool b = false;
+    for (int32_t it = 0; qq < is && it <= N.count && !b; ++it)
+      qq = chain_jump(qq, is, nright, nidx, nridx, &b);
+    if (b || qq < is || qq >= N.count) {  // cannot happen for a valid partition
+      bad = true;
+      continue;
+    }
+    const int64_t src = R.begin + chain_k[c];
+    tpos[N.offset + qq] = pos[src];
+    toid[N.offset + qq] = oid[src];
+  }
+  if (bad) atomicExch(err, 2);
 }
 
 // The whole partition of one node in one block, for levels whose nodes hold
@@ -2861,7 +2902,7 @@ DeviceTree::~DeviceTree() {
                   left_cnt_, left_base_, scan_tmp_, node_tmp_, fallback_, counters_, leaf_ids_,
                   leaf_tmp_, leafdesc_, segs_, idx_list_, table_, items_, items_tmp_, gidx_,
                   tight_chunks_, tight_nodes_, segs_local_, ridx_, sub_nodes_, sub_first_,
-                  sub_hist_, sub_pos_, sub_tot_, sub_stats_};
+                  sub_hist_, sub_pos_, sub_tot_, sub_stats_, wpre_};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h_counters_) cudaFreeHost(h_counters_);
@@ -3023,6 +3064,7 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     DT_CHECK(grow(part_, cap_part_, size_t(max_chunks) * kPartWords, s));
     DT_CHECK(grow(left_cnt_, cap_lc_, size_t(max_chunks), s));
     DT_CHECK(grow(left_base_, cap_lb_, size_t(max_chunks), s));
+    DT_CHECK(grow(wpre_, cap_wp_, size_t(max_chunks) * (kChunkThreads / 32), s));
     const unsigned gL = unsigned((L + 127) / 128);
     const bool small = int64_t(L) <= kScanBlock;
     if (small) {
@@ -3095,12 +3137,12 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
       ++info_.launches;
     } else {
       CHUNK_LAUNCH(k_part_count, epos_, nodes_, chunk_node_, chunk_base_, nb, counters_ + C_NCHUNK,
-                   left_cnt_);
+                   left_cnt_, wpre_);
       k_part_node_scan<<<unsigned((int64_t(L) * 32 + 127) / 128), 128, 0, s>>>(
           nodes_, nb, ne, chunk_base_, left_cnt_, left_base_);
       ++info_.launches;
       CHUNK_LAUNCH(k_part_left, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
-                   counters_ + C_NCHUNK, left_base_, tpos_, toid_, idx_, ridx_);
+                   counters_ + C_NCHUNK, left_base_, wpre_, tpos_, toid_, idx_, ridx_);
       CHUNK_LAUNCH(k_part_right, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
                    counters_ + C_NCHUNK, idx_, ridx_, tpos_, toid_, walk_err_);
     }
