@@ -866,24 +866,22 @@ hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float
         *ovz = reinterpret_cast<float *>(ob + A.f[5]);
   CU(ctx->d_vel.ensure(size_t(std::max<int64_t>(3 * n, 1)) * 4), "cudaMalloc(vel)");
   float *dv = ctx->d_vel.as<float>();
-  CU(hsr::launch_gather_f32(in[3], perm, dv, n, s), "gather vx");
-  CU(hsr::launch_gather_f32(in[4], perm, dv + n, n, s), "gather vy");
-  CU(hsr::launch_gather_f32(in[5], perm, dv + 2 * n, n, s), "gather vz");
-  CU(hsr::launch_gather_f32(in[7], perm, reinterpret_cast<float *>(ob + A.f[7]), n, s), "gather phi");
-  CU(hsr::launch_gather_i64(in_id, perm, reinterpret_cast<int64_t *>(ob + A.id), n, s), "gather id");
-  CU(hsr::launch_gather_u16(in_mask, perm, reinterpret_cast<uint16_t *>(ob + A.mask), n, s),
-     "gather mask");
-  CU(hsr::launch_unpack4(ctx->tree.table(), reinterpret_cast<float *>(ob + A.f[0]),
-                         reinterpret_cast<float *>(ob + A.f[1]), reinterpret_cast<float *>(ob + A.f[2]),
-                         reinterpret_cast<float *>(ob + A.f[6]), n, s),
-     "unpack kernel");
-  launches += 7;
+  CU(hsr::launch_gather3_f32(in[3], in[4], in[5], perm, dv, n, s), "gather velocities");
+  // the other permuted outputs ahead of the pair kernel (which takes every
+  // SM), so that their copies back overlap it
+  CU(hsr::launch_outputs(ctx->tree.table(), in[7], in_id, in_mask, perm,
+                         reinterpret_cast<float *>(ob + A.f[0]), reinterpret_cast<float *>(ob + A.f[1]),
+                         reinterpret_cast<float *>(ob + A.f[2]), reinterpret_cast<float *>(ob + A.f[6]),
+                         reinterpret_cast<float *>(ob + A.f[7]), reinterpret_cast<int64_t *>(ob + A.id),
+                         reinterpret_cast<uint16_t *>(ob + A.mask), n, s),
+     "gather outputs");
+  launches += 2;
   if (overlap) {
     // the permuted arrays other than the velocities go back now
     CU(cudaEventRecord(ctx->ev_perm, s), "event");
+    CU(cudaStreamWaitEvent(ctx->copy_stream, ctx->ev_perm, 0), "wait for the outputs");
     const int dev = ctx->device;
     cudaStream_t s2 = ctx->copy_stream;
-    cudaEvent_t ev = ctx->ev_perm;
     float *dst[5] = {arr[0], arr[1], arr[2], arr[6], arr[7]};
     const char *src[5] = {ob + A.f[0], ob + A.f[1], ob + A.f[2], ob + A.f[6], ob + A.f[7]};
     const char *sid = ob + A.id, *smask = ob + A.mask;
@@ -891,7 +889,6 @@ hsr_status kick_device_build(hsr_ctx *ctx, const hsr_params *p, int64_t n, float
     uint16_t *hmask = mask;
     ctx->copier->submit([=]() -> cudaError_t {
       cudaError_t e = cudaSetDevice(dev);
-      if (e == cudaSuccess) e = cudaStreamWaitEvent(s2, ev, 0);
       for (int i = 0; i < 5 && e == cudaSuccess; ++i)
         e = cudaMemcpyAsync(dst[i], src[i], size_t(n) * 4, cudaMemcpyDeviceToHost, s2);
       if (e == cudaSuccess) e = cudaMemcpyAsync(hid, sid, size_t(n) * 8, cudaMemcpyDeviceToHost, s2);
@@ -1555,17 +1552,13 @@ hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *para
     const int32_t *perm = B.tree.perm();
     char *ob = B.out.as<char>();
     float *dv = B.vel.as<float>();
-    BCU(hsr::launch_gather_f32(in[3], perm, dv, n, s), "gather vx");
-    BCU(hsr::launch_gather_f32(in[4], perm, dv + n, n, s), "gather vy");
-    BCU(hsr::launch_gather_f32(in[5], perm, dv + 2 * n, n, s), "gather vz");
-    BCU(hsr::launch_gather_f32(in[7], perm, reinterpret_cast<float *>(ob + A.f[7]), n, s), "gather phi");
-    BCU(hsr::launch_gather_i64(in_id, perm, reinterpret_cast<int64_t *>(ob + A.id), n, s), "gather id");
-    BCU(hsr::launch_gather_u16(in_mask, perm, reinterpret_cast<uint16_t *>(ob + A.mask), n, s),
-        "gather mask");
-    BCU(hsr::launch_unpack4(B.tree.table(), reinterpret_cast<float *>(ob + A.f[0]),
-                            reinterpret_cast<float *>(ob + A.f[1]), reinterpret_cast<float *>(ob + A.f[2]),
-                            reinterpret_cast<float *>(ob + A.f[6]), n, s),
-        "unpack kernel");
+    BCU(hsr::launch_gather3_f32(in[3], in[4], in[5], perm, dv, n, s), "gather velocities");
+    BCU(hsr::launch_outputs(B.tree.table(), in[7], in_id, in_mask, perm,
+                            reinterpret_cast<float *>(ob + A.f[0]), reinterpret_cast<float *>(ob + A.f[1]),
+                            reinterpret_cast<float *>(ob + A.f[2]), reinterpret_cast<float *>(ob + A.f[6]),
+                            reinterpret_cast<float *>(ob + A.f[7]), reinterpret_cast<int64_t *>(ob + A.id),
+                            reinterpret_cast<uint16_t *>(ob + A.mask), n, s),
+        "gather outputs");
     BCU(cudaEventRecord(B.done, s), "box event");
 #undef BCU
     hsr::BoxDesc &D = desc[b];

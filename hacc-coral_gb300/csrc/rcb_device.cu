@@ -348,23 +348,29 @@ __device__ __forceinline__ void fix_add(__int128 &acc, unsigned __int128 &bits, 
   acc += (b >> 31) ? -__int128(v) : __int128(v);
 }
 
+__device__ __forceinline__ int lsb_of(unsigned __int128 v) {
+  const unsigned long long lo = (unsigned long long)v, hi = (unsigned long long)(v >> 64);
+  if (lo) return __ffsll((long long)lo) - 1;
+  if (hi) return 64 + __ffsll((long long)hi) - 1;
+  return -1;
+}
+
 // The same sum on four 32-bit limbs (two's complement, least significant
 // first): a term t 2^-kFix with 0 <= shift <= 39 (2^-24 <= |t| < 2^14, the
 // common case) is m << shift on two limbs, added (or subtracted) with one
 // carry chain on the integer pipe; other terms take fix_add's wide path.
+// lsb: the least significant set bit over the terms' magnitudes (in units of
+// 2^kFix), INT_MAX while no term has one.
 struct FixAcc {
   uint32_t l[4];  // the sum
-  uint32_t b[4];  // OR of the terms' magnitudes
+  int lsb;
   __device__ __forceinline__ void zero() {
 #pragma unroll
-    for (int k = 0; k < 4; ++k) l[k] = b[k] = 0u;
+    for (int k = 0; k < 4; ++k) l[k] = 0u;
+    lsb = INT_MAX;
   }
   __device__ __forceinline__ void add_limbs(uint32_t v0, uint32_t v1, uint32_t v2, uint32_t v3,
                                             bool neg) {
-    b[0] |= v0;
-    b[1] |= v1;
-    b[2] |= v2;
-    b[3] |= v3;
     if (neg) {
       asm("sub.cc.u32 %0, %0, %4;\n\tsubc.cc.u32 %1, %1, %5;\n\tsubc.cc.u32 %2, %2, %6;\n\t"
           "subc.u32 %3, %3, %7;"
@@ -387,20 +393,16 @@ struct FixAcc {
     else m |= 0x800000u;
     const int sh = e - 150 - kFix;
     const bool neg = (bb >> 31) != 0u;
-    if (sh >= 0 && sh < 32) {
-      add_limbs(m << sh, sh ? m >> (32 - sh) : 0u, 0u, 0u, neg);
-    } else if (sh >= 32 && sh <= 39) {
-      add_limbs(0u, m << (sh - 32), 0u, 0u, neg);  // m < 2^24: no bits past limb 1
+    if (sh >= 0 && sh <= 39) {
+      lsb = min(lsb, sh + __ffs(int(m)) - 1);  // m != 0 here
+      if (sh < 32) add_limbs(m << sh, sh ? m >> (32 - sh) : 0u, 0u, 0u, neg);
+      else add_limbs(0u, m << (sh - 32), 0u, 0u, neg);  // m < 2^24: no bits past limb 1
     } else {
       __int128 w = 0;
       unsigned __int128 wb = 0;
       fix_add(w, wb, t, overflow, trunc);
+      if (wb) lsb = min(lsb, lsb_of(wb));
       const unsigned __int128 u = (unsigned __int128)w;  // +/- v in two's complement
-      const unsigned __int128 mag = neg ? (unsigned __int128)(-w) : u;
-      b[0] |= uint32_t(mag);
-      b[1] |= uint32_t(mag >> 32);
-      b[2] |= uint32_t(mag >> 64);
-      b[3] |= uint32_t(mag >> 96);
       asm("add.cc.u32 %0, %0, %4;\n\taddc.cc.u32 %1, %1, %5;\n\taddc.cc.u32 %2, %2, %6;\n\t"
           "addc.u32 %3, %3, %7;"
           : "+r"(l[0]), "+r"(l[1]), "+r"(l[2]), "+r"(l[3])
@@ -413,18 +415,7 @@ struct FixAcc {
                                 ((unsigned __int128)l[1] << 32) | (unsigned __int128)l[0];
     return __int128(u);
   }
-  __device__ __forceinline__ unsigned __int128 bits() const {
-    return ((unsigned __int128)b[3] << 96) | ((unsigned __int128)b[2] << 64) |
-           ((unsigned __int128)b[1] << 32) | (unsigned __int128)b[0];
-  }
 };
-
-__device__ __forceinline__ int lsb_of(unsigned __int128 v) {
-  const unsigned long long lo = (unsigned long long)v, hi = (unsigned long long)(v >> 64);
-  if (lo) return __ffsll((long long)lo) - 1;
-  if (hi) return 64 + __ffsll((long long)hi) - 1;
-  return -1;
-}
 
 __device__ __forceinline__ __int128 shfl_xor_i128(__int128 v, int o) {
   const unsigned long long lo = (unsigned long long)v, hi = (unsigned long long)(v >> 64);
@@ -469,21 +460,20 @@ constexpr int kPartWords = 18;
 // Partial sums of one chunk and its bounding box.  Fixed thread-to-element
 // map and reduction tree.
 template <bool WM>
-__global__ void __launch_bounds__(kChunkThreads)
+__global__ void __launch_bounds__(kChunkThreads, 4)
     k_stats_partial(const float4 *__restrict__ pos, const DNode *nodes,
                     const int32_t *chunk_node, const int64_t *chunk_base, int32_t nb,
                     const int64_t *nchunk, double *part) {
   CHUNK_PROLOGUE
   const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
   __int128 s[4] = {0, 0, 0, 0};
-  unsigned __int128 bits[4] = {0, 0, 0, 0};
   float fa[4] = {0.f, 0.f, 0.f, 0.f};
   float lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
   bool ovf = false;
   bool trn[4] = {false, false, false, false};
   // four loads in flight per thread; the elements are then taken in the same
   // order as one at a time
-  constexpr int kU = 4;
+  constexpr int kU = 2;
   FixAcc fx[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) fx[q].zero();
@@ -508,10 +498,11 @@ __global__ void __launch_bounds__(kChunkThreads)
       lo[2] = fminf(lo[2], p.z); hi[2] = fmaxf(hi[2], p.z);
     }
   }
+  int lsb[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     s[q] = fx[q].sum();
-    bits[q] = fx[q].bits();
+    lsb[q] = __reduce_min_sync(0xffffffffu, fx[q].lsb);
   }
   double a[4];
   int emin[4];
@@ -519,15 +510,13 @@ __global__ void __launch_bounds__(kChunkThreads)
   for (int q = 0; q < 4; ++q) {
     for (int o = 16; o > 0; o >>= 1) {
       s[q] += shfl_xor_i128(s[q], o);
-      bits[q] |= (unsigned __int128)shfl_xor_i128(__int128(bits[q]), o);
       fa[q] = __fadd_ru(fa[q], __shfl_xor_sync(0xffffffffu, fa[q], o));
     }
     a[q] = double(fa[q]);
     const bool tq = __any_sync(0xffffffffu, trn[q]);
-    const int l = lsb_of(bits[q]);
     // least significant exponent of the warp's terms; below kFix if any term
     // lost bits to the truncation, INT_MAX if all are zero
-    emin[q] = tq ? kFix - 1 : (l < 0 ? INT_MAX : kFix + l);
+    emin[q] = tq ? kFix - 1 : (lsb[q] == INT_MAX ? INT_MAX : kFix + lsb[q]);
   }
 #pragma unroll
   for (int d = 0; d < 3; ++d) {
@@ -1729,17 +1718,16 @@ __global__ void __launch_bounds__(kSubThreads, 2)
         bl[2] = fminf(bl[2], p.z); bh[2] = fmaxf(bh[2], p.z);
       }
       __int128 sq[4];
-      unsigned __int128 bits[4];
+      int lsb[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         sq[q] = fx[q].sum();
-        bits[q] = fx[q].bits();
+        lsb[q] = __reduce_min_sync(0xffffffffu, fx[q].lsb);
       }
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         for (int sft = 16; sft > 0; sft >>= 1) {
           sq[q] += shfl_xor_i128(sq[q], sft);
-          bits[q] |= (unsigned __int128)shfl_xor_i128(__int128(bits[q]), sft);
           fa[q] = __fadd_ru(fa[q], __shfl_xor_sync(0xffffffffu, fa[q], sft));
         }
       }
@@ -1747,8 +1735,7 @@ __global__ void __launch_bounds__(kSubThreads, 2)
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
         const bool tq = __any_sync(0xffffffffu, trn[q]);
-        const int l = lsb_of(bits[q]);
-        em[q] = tq ? kFix - 1 : (l < 0 ? INT_MAX : kFix + l);
+        em[q] = tq ? kFix - 1 : (lsb[q] == INT_MAX ? INT_MAX : kFix + lsb[q]);
       }
 #pragma unroll
       for (int d = 0; d < 3; ++d) {
@@ -2157,11 +2144,16 @@ __device__ void pp_accum_(int k, int32_t count, Src src, const float *xc, const 
   }
 }
 
-// Pseudo-particles of the nodes [lb, le), children done first.
-__global__ void k_pseudo(DNode *nodes, int32_t lb, int32_t le, const float4 *__restrict__ pos,
-                         float *ppm_all, int k, float ppc, int32_t nd) {
-  const int32_t t = lb + blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= le) return;
+// Node ranges of up to kTopLevels levels: level l is [b[l], b[l + 1]).
+constexpr int kTopLevels = 48;
+struct LevelSpan {
+  int32_t b[kTopLevels + 1];
+  int32_t n;
+};
+
+// Pseudo-particles of node t, its children done first.
+__device__ void pseudo_node(DNode *nodes, int32_t t, const float4 *__restrict__ pos, float *ppm_all,
+                            int k, float ppc, int32_t nd) {
   DNode &T = nodes[t];
   T.tdr = fmul_(ppc, pptdr_(T));
   float ppm[12];
@@ -2210,6 +2202,46 @@ __global__ void k_pseudo(DNode *nodes, int32_t lb, int32_t le, const float4 *__r
     }
   }
   for (int j = 0; j < k; ++j) ppm_all[int64_t(t) * k + j] = ppm[j];
+}
+
+// Pseudo-particles of the nodes [lb, le), a warp per node.  A monopole leaf's
+// mass is the sequential float sum of its particles' masses: the warp loads
+// 32 at a time (coalesced) and every lane adds them in order from shuffles.
+// Other nodes: lane 0.
+__global__ void k_pseudo(DNode *nodes, int32_t lb, int32_t le, const float4 *__restrict__ pos,
+                         float *ppm_all, int k, float ppc, int32_t nd) {
+  const int32_t t = lb + int32_t((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (t >= le) return;  // whole warps
+  DNode &T = nodes[t];
+  if (k == 1 && T.cl == 0 && T.cr == 0 && T.count <= nd && T.count > 1) {
+    const float *w = reinterpret_cast<const float *>(pos + T.offset) + 3;
+    const int32_t c = T.count;
+    float m = 0.f;
+    for (int32_t i0 = 0; i0 < c; i0 += 32) {
+      const float v = i0 + lane < c ? w[4 * (i0 + lane)] : 0.f;
+      const int nv = min(32, c - i0);
+      for (int j = 0; j < nv; ++j) m = fadd_(m, fmul_(__shfl_sync(0xffffffffu, v, j), 1.0f));
+    }
+    if (lane == 0) {
+      T.tdr = fmul_(ppc, pptdr_(T));
+      ppm_all[t] = m;
+    }
+    return;
+  }
+  if (lane == 0) pseudo_node(nodes, t, pos, ppm_all, k, ppc, nd);
+}
+
+// The top levels' pseudo-particles in one block, deepest level first, a
+// thread per node (every level here has at most blockDim.x nodes).
+__global__ void __launch_bounds__(1024)
+    k_pseudo_top(DNode *nodes, LevelSpan lv, const float4 *__restrict__ pos, float *ppm_all, int k,
+                 float ppc, int32_t nd) {
+  for (int l = lv.n - 1; l >= 0; --l) {
+    for (int32_t t = lv.b[l] + int32_t(threadIdx.x); t < lv.b[l + 1]; t += int32_t(blockDim.x))
+      pseudo_node(nodes, t, pos, ppm_all, k, ppc, nd);
+    __syncthreads();  // the next level up reads these nodes
+  }
 }
 
 // Position table: particles, then every node's pseudo-particles.
@@ -2782,22 +2814,48 @@ __global__ void k_gather(const T *__restrict__ in, const int32_t *__restrict__ p
     out[i] = in[perm[i]];
 }
 
+// The three velocity components into tree order, perm read once:
+// out[d n + i] = in_d[perm[i]].
+__global__ void k_gather3_f32(const float *__restrict__ a, const float *__restrict__ b,
+                              const float *__restrict__ c, const int32_t *__restrict__ perm,
+                              float *out, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int32_t j = perm[i];
+    out[i] = a[j];
+    out[n + i] = b[j];
+    out[2 * n + i] = c[j];
+  }
+}
+
+// Every permuted output but the velocities in one pass: positions and masses
+// from the tree-ordered table, phi, id and mask through perm.
+__global__ void k_outputs(const float4 *__restrict__ table, const float *__restrict__ phi,
+                          const int64_t *__restrict__ id, const uint16_t *__restrict__ mask,
+                          const int32_t *__restrict__ perm, float *x, float *y, float *z, float *m,
+                          float *ophi, int64_t *oid, uint16_t *omask, int64_t n) {
+  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
+       i += int64_t(gridDim.x) * blockDim.x) {
+    const int32_t j = perm[i];
+    const float4 p = table[i];
+    const float f = phi[j];
+    const int64_t d = id[j];
+    const uint16_t k = mask[j];
+    x[i] = p.x;
+    y[i] = p.y;
+    z[i] = p.z;
+    m[i] = p.w;
+    ophi[i] = f;
+    oid[i] = d;
+    omask[i] = k;
+  }
+}
+
 __global__ void k_pack4(const float *x, const float *y, const float *z, const float *m, float4 *out,
                         int64_t n) {
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * blockDim.x)
     out[i] = make_float4(x[i], y[i], z[i], m[i]);
-}
-
-__global__ void k_unpack4(const float4 *in, float *x, float *y, float *z, float *m, int64_t n) {
-  for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
-       i += int64_t(gridDim.x) * blockDim.x) {
-    const float4 p = in[i];
-    x[i] = p.x;
-    y[i] = p.y;
-    z[i] = p.z;
-    m[i] = p.w;
-  }
 }
 
 __global__ void k_scatter_f32(const float *__restrict__ in, const int32_t *__restrict__ perm,
@@ -3190,11 +3248,25 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
 
   // ---- pseudo-particles, deepest level first ----
   DT_CHECK(grow(ppm_, cap_ppm_, size_t(nnodes) * k + 1, s));
-  for (int64_t l = int64_t(level_begin.size()) - 2; l >= 0; --l) {
-    const int32_t lb = level_begin[l], le = level_begin[l + 1];
-    if (le > lb) {
-      k_pseudo<<<unsigned((le - lb + 127) / 128), 128, 0, s>>>(nodes_, lb, le, epos_, ppm_, k,
-                                                               cfg.ppc, cfg.nd);
+  {
+    // the top levels of at most 1024 nodes each in one launch, the rest a
+    // launch per level
+    const int64_t nlev = int64_t(level_begin.size()) - 1;
+    int64_t lt = 0;
+    while (lt < nlev && lt < kTopLevels && level_begin[lt + 1] - level_begin[lt] <= 1024) ++lt;
+    for (int64_t l = nlev - 1; l >= lt; --l) {
+      const int32_t lb = level_begin[l], le = level_begin[l + 1];
+      if (le > lb) {
+        k_pseudo<<<unsigned((int64_t(le - lb) * 32 + 255) / 256), 256, 0, s>>>(
+            nodes_, lb, le, epos_, ppm_, k, cfg.ppc, cfg.nd);
+        ++info_.launches;
+      }
+    }
+    if (lt > 0) {
+      LevelSpan lv{};
+      lv.n = int32_t(lt);
+      for (int64_t l = 0; l <= lt; ++l) lv.b[l] = level_begin[l];
+      k_pseudo_top<<<1, 1024, 0, s>>>(nodes_, lv, epos_, ppm_, k, cfg.ppc, cfg.nd);
       ++info_.launches;
     }
   }
@@ -3361,16 +3433,19 @@ cudaError_t launch_gather_f32(const float *in, const int32_t *perm, float *out, 
   k_gather<float><<<grid_for(n, 256), 256, 0, s>>>(in, perm, out, n);
   return cudaGetLastError();
 }
-cudaError_t launch_gather_i64(const int64_t *in, const int32_t *perm, int64_t *out, int64_t n,
-                              cudaStream_t s) {
+cudaError_t launch_gather3_f32(const float *a, const float *b, const float *c, const int32_t *perm,
+                               float *out, int64_t n, cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  k_gather<int64_t><<<grid_for(n, 256), 256, 0, s>>>(in, perm, out, n);
+  k_gather3_f32<<<grid_for(n, 256), 256, 0, s>>>(a, b, c, perm, out, n);
   return cudaGetLastError();
 }
-cudaError_t launch_gather_u16(const uint16_t *in, const int32_t *perm, uint16_t *out, int64_t n,
-                              cudaStream_t s) {
+cudaError_t launch_outputs(const float4 *table, const float *phi, const int64_t *id,
+                           const uint16_t *mask, const int32_t *perm, float *x, float *y, float *z,
+                           float *m, float *ophi, int64_t *oid, uint16_t *omask, int64_t n,
+                           cudaStream_t s) {
   if (n <= 0) return cudaSuccess;
-  k_gather<uint16_t><<<grid_for(n, 256), 256, 0, s>>>(in, perm, out, n);
+  k_outputs<<<grid_for(n, 256), 256, 0, s>>>(table, phi, id, mask, perm, x, y, z, m, ophi, oid,
+                                             omask, n);
   return cudaGetLastError();
 }
 cudaError_t launch_scatter_f32(const float *in, const int32_t *perm, float *out, int64_t n,
@@ -3410,11 +3485,4 @@ cudaError_t launch_pack4(const float *x, const float *y, const float *z, const f
   k_pack4<<<grid_for(n, 256), 256, 0, s>>>(x, y, z, m, out, n);
   return cudaGetLastError();
 }
-cudaError_t launch_unpack4(const float4 *in, float *x, float *y, float *z, float *m, int64_t n,
-                           cudaStream_t s) {
-  if (n <= 0) return cudaSuccess;
-  k_unpack4<<<grid_for(n, 256), 256, 0, s>>>(in, x, y, z, m, n);
-  return cudaGetLastError();
-}
-
 }  // namespace hsr

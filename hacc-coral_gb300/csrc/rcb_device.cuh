@@ -181,18 +181,21 @@ class DeviceTree {
   bool sub_off_ = false;  // this build runs every level in the level loop
 };
 
-// Gathers the caller's arrays into tree order: out[i] = in[perm[i]].
+// The three velocity components into tree order (out: 3 n floats).
+cudaError_t launch_gather3_f32(const float *a, const float *b, const float *c, const int32_t *perm,
+                               float *out, int64_t n, cudaStream_t s);
+// The permuted outputs besides the velocities: x, y, z and mass from the
+// tree-ordered table, phi, id and mask through perm.
+cudaError_t launch_outputs(const float4 *table, const float *phi, const int64_t *id,
+                           const uint16_t *mask, const int32_t *perm, float *x, float *y, float *z,
+                           float *m, float *ophi, int64_t *oid, uint16_t *omask, int64_t n,
+                           cudaStream_t s);
+// out[i] = in[perm[i]] (into tree order).
 cudaError_t launch_gather_f32(const float *in, const int32_t *perm, float *out, int64_t n,
                               cudaStream_t s);
-cudaError_t launch_gather_i64(const int64_t *in, const int32_t *perm, int64_t *out, int64_t n,
-                              cudaStream_t s);
-cudaError_t launch_gather_u16(const uint16_t *in, const int32_t *perm, uint16_t *out, int64_t n,
-                              cudaStream_t s);
-// pos4[i] = (x[i], y[i], z[i], m[i]); and its inverse split.
+// pos4[i] = (x[i], y[i], z[i], m[i]).
 cudaError_t launch_pack4(const float *x, const float *y, const float *z, const float *m,
                          float4 *out, int64_t n, cudaStream_t s);
-cudaError_t launch_unpack4(const float4 *in, float *x, float *y, float *z, float *m, int64_t n,
-                           cudaStream_t s);
 // out[perm[i]] = in[i] (back to the caller's order).
 cudaError_t launch_scatter_f32(const float *in, const int32_t *perm, float *out, int64_t n,
                                cudaStream_t s);
