@@ -51,7 +51,7 @@ constexpr int kPlainSteps = 4;      // single chain steps before the chunk parti
 enum { C_NCHUNK = 0, C_NSPLIT = 1, C_NFALLBACK = 2, C_NLEAF = 3, C_NSEG = 4, C_NENT = 5,
        C_PAIRS = 6, C_PADDED = 7, C_NITEMS = 8, C_MAXLEN = 9, C_TDONE1 = 10, C_TDONE2 = 11,
        C_NTIGHT = 12, C_SEGOVF = 13, C_MAXCNT = 14, C_ERR = 15, C_BUCKET = 16, C_FILL = 48,
-       C_SUBFB = 80, C_COUNT = 81 };
+       C_SUBFB = 80, C_CHAINS = 81, C_COUNT = 82 };
 
 // Segments a leaf's walk can leave in its own region of the one-pass walk;
 // a leaf with more sends the build to the counting walk and a second pass.
@@ -230,6 +230,7 @@ __global__ void __launch_bounds__(kScanThreads)
     counters[C_NFALLBACK] = 0;  // the level's centre-of-mass lists start empty
     counters[C_NTIGHT] = 0;
     counters[C_MAXCNT] = 0;     // the next level's largest node, from the children
+    counters[C_CHAINS] = 0;     // the level's queue of long swap chains
   }
 }
 
@@ -355,33 +356,35 @@ __device__ __forceinline__ int lsb_of(unsigned __int128 v) {
   return -1;
 }
 
-// The same sum on four 32-bit limbs (two's complement, least significant
-// first): a term t 2^-kFix with 0 <= shift <= 39 (2^-24 <= |t| < 2^14, the
-// common case) is m << shift on two limbs, added (or subtracted) with one
-// carry chain on the integer pipe; other terms take fix_add's wide path.
+// The same sum on the integer pipe.  A term t 2^-kFix with 0 <= shift <= 34
+// (2^-24 <= |t| < 2^10, the common case) is m << shift < 2^58, added to a
+// signed 64-bit partial sum; fold() moves the partial sum into the 128-bit
+// sum (four 32-bit limbs, two's complement, least significant first) and is
+// called at least every kFoldTerms adds, so the partial sum stays below 2^62.
+// Other terms take fix_add's wide path straight into the limbs.
 // lsb: the least significant set bit over the terms' magnitudes (in units of
 // 2^kFix), INT_MAX while no term has one.
+constexpr int kFoldTerms = 16;
 struct FixAcc {
   uint32_t l[4];  // the sum
+  long long acc;  // fast-path terms since the last fold
   int lsb;
   __device__ __forceinline__ void zero() {
 #pragma unroll
     for (int k = 0; k < 4; ++k) l[k] = 0u;
+    acc = 0;
     lsb = INT_MAX;
   }
-  __device__ __forceinline__ void add_limbs(uint32_t v0, uint32_t v1, uint32_t v2, uint32_t v3,
-                                            bool neg) {
-    if (neg) {
-      asm("sub.cc.u32 %0, %0, %4;\n\tsubc.cc.u32 %1, %1, %5;\n\tsubc.cc.u32 %2, %2, %6;\n\t"
-          "subc.u32 %3, %3, %7;"
-          : "+r"(l[0]), "+r"(l[1]), "+r"(l[2]), "+r"(l[3])
-          : "r"(v0), "r"(v1), "r"(v2), "r"(v3));
-    } else {
-      asm("add.cc.u32 %0, %0, %4;\n\taddc.cc.u32 %1, %1, %5;\n\taddc.cc.u32 %2, %2, %6;\n\t"
-          "addc.u32 %3, %3, %7;"
-          : "+r"(l[0]), "+r"(l[1]), "+r"(l[2]), "+r"(l[3])
-          : "r"(v0), "r"(v1), "r"(v2), "r"(v3));
-    }
+  __device__ __forceinline__ void add_limbs(uint32_t v0, uint32_t v1, uint32_t v2, uint32_t v3) {
+    asm("add.cc.u32 %0, %0, %4;\n\taddc.cc.u32 %1, %1, %5;\n\taddc.cc.u32 %2, %2, %6;\n\t"
+        "addc.u32 %3, %3, %7;"
+        : "+r"(l[0]), "+r"(l[1]), "+r"(l[2]), "+r"(l[3])
+        : "r"(v0), "r"(v1), "r"(v2), "r"(v3));
+  }
+  __device__ __forceinline__ void fold() {
+    const uint32_t sx = uint32_t(acc >> 63);  // sign extension: 0 or all ones
+    add_limbs(uint32_t(acc), uint32_t((unsigned long long)acc >> 32), sx, sx);
+    acc = 0;
   }
   __device__ __forceinline__ void add(float t, bool &overflow, bool &trunc) {
     const uint32_t bb = __float_as_uint(t);
@@ -392,24 +395,20 @@ struct FixAcc {
     if (e == 0) e = 1;
     else m |= 0x800000u;
     const int sh = e - 150 - kFix;
-    const bool neg = (bb >> 31) != 0u;
-    if (sh >= 0 && sh <= 39) {
+    if (unsigned(sh) <= 34u) {
       lsb = min(lsb, sh + __ffs(int(m)) - 1);  // m != 0 here
-      if (sh < 32) add_limbs(m << sh, sh ? m >> (32 - sh) : 0u, 0u, 0u, neg);
-      else add_limbs(0u, m << (sh - 32), 0u, 0u, neg);  // m < 2^24: no bits past limb 1
+      const long long v = (long long)((unsigned long long)m << sh);
+      acc += (bb >> 31) ? -v : v;
     } else {
       __int128 w = 0;
       unsigned __int128 wb = 0;
       fix_add(w, wb, t, overflow, trunc);
       if (wb) lsb = min(lsb, lsb_of(wb));
       const unsigned __int128 u = (unsigned __int128)w;  // +/- v in two's complement
-      asm("add.cc.u32 %0, %0, %4;\n\taddc.cc.u32 %1, %1, %5;\n\taddc.cc.u32 %2, %2, %6;\n\t"
-          "addc.u32 %3, %3, %7;"
-          : "+r"(l[0]), "+r"(l[1]), "+r"(l[2]), "+r"(l[3])
-          : "r"(uint32_t(u)), "r"(uint32_t(u >> 32)), "r"(uint32_t(u >> 64)),
-            "r"(uint32_t(u >> 96)));
+      add_limbs(uint32_t(u), uint32_t(u >> 32), uint32_t(u >> 64), uint32_t(u >> 96));
     }
   }
+  // the 128-bit sum (after a fold)
   __device__ __forceinline__ __int128 sum() const {
     const unsigned __int128 u = ((unsigned __int128)l[3] << 96) | ((unsigned __int128)l[2] << 64) |
                                 ((unsigned __int128)l[1] << 32) | (unsigned __int128)l[0];
@@ -477,7 +476,8 @@ __global__ void __launch_bounds__(kChunkThreads, 4)
   FixAcc fx[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) fx[q].zero();
-  for (int k0 = tid; k0 < R.len; k0 += NT * kU) {
+  int it = 0;
+  for (int k0 = tid; k0 < R.len; k0 += NT * kU, ++it) {
     float4 pu[kU];
 #pragma unroll
     for (int u = 0; u < kU; ++u)
@@ -497,10 +497,15 @@ __global__ void __launch_bounds__(kChunkThreads, 4)
       lo[1] = fminf(lo[1], p.y); hi[1] = fmaxf(hi[1], p.y);
       lo[2] = fminf(lo[2], p.z); hi[2] = fmaxf(hi[2], p.z);
     }
+    if ((it + 1) % (kFoldTerms / kU) == 0) {
+#pragma unroll
+      for (int q = 0; q < 4; ++q) fx[q].fold();
+    }
   }
   int lsb[4];
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
+    fx[q].fold();
     s[q] = fx[q].sum();
     lsb[q] = __reduce_min_sync(0xffffffffu, fx[q].lsb);
   }
@@ -1299,6 +1304,15 @@ __global__ void __launch_bounds__(kChunkThreads)
   }
 }
 
+// A swap chain still running after the partition's single steps: its
+// position in the node, the node and the element's position in the level's
+// array.
+struct ChainItem {
+  int32_t q, node;
+  int64_t src;
+};
+static_assert(sizeof(ChainItem) == sizeof(int4), "a chain item fills one int4 of the queue");
+
 // One or more steps of the chain q -> idx[q] -> ... (q < nleft): the q-th
 // left element has c = idx[q] - q right elements before it, and so has every
 // left element up to the c-th right element (at ridx[c]), whose ranks run to
@@ -1336,7 +1350,8 @@ __global__ void __launch_bounds__(kChunkThreads)
     k_part_right(const float4 *__restrict__ pos, const int32_t *__restrict__ oid, const DNode *nodes,
                  const int32_t *chunk_node, const int64_t *chunk_base, int32_t nb,
                  const int64_t *nchunk, const int32_t *__restrict__ idx,
-                 const int32_t *__restrict__ ridx, float4 *tpos, int32_t *toid, int32_t *err) {
+                 const int32_t *__restrict__ ridx, float4 *tpos, int32_t *toid, int32_t *err,
+                 int64_t *counters, ChainItem *chains, int64_t chain_cap) {
   CHUNK_PROLOGUE
   const ChunkRange R = chunk_range(nodes, chunk_node, chunk_base, nb, chunk);
   const DNode &N = nodes[R.node];
@@ -1374,15 +1389,10 @@ __global__ void __launch_bounds__(kChunkThreads)
   }
   // Block mode: the thread's 16 elements take their first kPlainSteps steps
   // in lockstep, so up to 16 independent loads are in flight per step (most
-  // chains end within a few).  The chains still running then go to a block
-  // queue and are followed a chain per thread, a run of equal steps at a time
-  // (chain_jump): a block's time is its longest chain, not the sum of one
-  // thread's long chains.
+  // chains end within a few).  The chains still running go to the level's
+  // chain queue (k_part_chains follows them a chain per thread): long chains
+  // gather in a few regions of a level, thousands in one chunk.
   constexpr int kPerT = kChunk / kChunkThreads;
-  __shared__ int32_t chain_q[kChunk];
-  __shared__ int16_t chain_k[kChunk];
-  __shared__ int chain_n;
-  if (threadIdx.x == 0) chain_n = 0;
   const float *key = reinterpret_cast<const float *>(pos + R.begin) + d;
   int32_t q[kPerT];
   unsigned right = 0;
@@ -1411,37 +1421,61 @@ __global__ void __launch_bounds__(kChunkThreads)
       if (nq[j] >= is) active &= ~(1u << j);
     }
   }
-  __syncthreads();  // chain_n set
+  // one queue reservation per warp
+  const int lane = threadIdx.x & 31;
+  const int na = __popc(active);
+  int incl = na;
 #pragma unroll
-  for (int j = 0; j < kPerT; ++j) {
-    if (!(active >> j & 1u)) continue;
-    const int slot = atomicAdd(&chain_n, 1);  // at most one per element of the chunk
-    chain_q[slot] = q[j];
-    chain_k[slot] = int16_t(tid + j * NT);
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
   }
+  unsigned long long base = 0;
+  if (lane == 31 && incl > 0)
+    base = atomicAdd((unsigned long long *)&counters[C_CHAINS], (unsigned long long)incl);
+  base = __shfl_sync(0xffffffffu, base, 31);
+  int64_t slot = int64_t(base) + incl - na;
 #pragma unroll
   for (int j = 0; j < kPerT; ++j) {
-    if (!(right >> j & 1u) || (active >> j & 1u)) continue;
+    if (!(right >> j & 1u)) continue;
     const int64_t src = R.begin + tid + j * NT;
+    if (active >> j & 1u) {
+      if (slot < chain_cap) chains[slot] = ChainItem{q[j], R.node, src};
+      else bad = true;  // cannot happen: a chain per element at most
+      ++slot;
+      continue;
+    }
     tpos[N.offset + q[j]] = pos[src];
     toid[N.offset + q[j]] = oid[src];
   }
-  __syncthreads();
-  const int nchain = chain_n;
-  for (int c = threadIdx.x; c < nchain; c += NT) {
-    int32_t qq = chain_q[c];
+  if (bad) atomicExch(err, 2);
+}
+
+// The level's long swap chains, a thread each, a run of equal steps at a
+// time (chain_jump); each lands its element.
+__global__ void __launch_bounds__(256)
+    k_part_chains(const float4 *__restrict__ pos, const int32_t *__restrict__ oid,
+                  const DNode *nodes, const ChainItem *__restrict__ chains, int64_t chain_cap,
+                  const int64_t *counters, const int32_t *__restrict__ idx,
+                  const int32_t *__restrict__ ridx, float4 *tpos, int32_t *toid, int32_t *err) {
+  const int64_t nq = min64(counters[C_CHAINS], chain_cap);
+  for (int64_t c = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; c < nq;
+       c += int64_t(gridDim.x) * blockDim.x) {
+    const ChainItem it = chains[c];
+    const DNode &N = nodes[it.node];
+    const int32_t is = N.nleft, nright = N.count - N.nleft;
+    const int32_t *nidx = idx + N.offset, *nridx = ridx + N.offset;
+    int32_t qq = it.q;
     bool b = false;
-    for (int32_t it = 0; qq < is && it <= N.count && !b; ++it)
+    for (int32_t k = 0; qq < is && k <= N.count && !b; ++k)
       qq = chain_jump(qq, is, nright, nidx, nridx, &b);
     if (b || qq < is || qq >= N.count) {  // cannot happen for a valid partition
-      bad = true;
+      atomicExch(err, 2);
       continue;
     }
-    const int64_t src = R.begin + chain_k[c];
-    tpos[N.offset + qq] = pos[src];
-    toid[N.offset + qq] = oid[src];
+    tpos[N.offset + qq] = pos[it.src];
+    toid[N.offset + qq] = oid[it.src];
   }
-  if (bad) atomicExch(err, 2);
 }
 
 // The whole partition of one node in one block, for levels whose nodes hold
@@ -1704,7 +1738,8 @@ __global__ void __launch_bounds__(kSubThreads, 2)
       float bl[3] = {INFINITY, INFINITY, INFINITY}, bh[3] = {-INFINITY, -INFINITY, -INFINITY};
       bool ovf = false;
       bool trn[4] = {false, false, false, false};
-      for (int e = tl; e < c; e += TN) {
+      int it = 0;
+      for (int e = tl; e < c; e += TN, ++it) {
         const float4 p = src[o + e];
         const float w = p.w;
         const float t[4] = {fmul_(w, p.x), fmul_(w, p.y), fmul_(w, p.z), w};
@@ -1716,11 +1751,16 @@ __global__ void __launch_bounds__(kSubThreads, 2)
         bl[0] = fminf(bl[0], p.x); bh[0] = fmaxf(bh[0], p.x);
         bl[1] = fminf(bl[1], p.y); bh[1] = fmaxf(bh[1], p.y);
         bl[2] = fminf(bl[2], p.z); bh[2] = fmaxf(bh[2], p.z);
+        if ((it + 1) % kFoldTerms == 0) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q) fx[q].fold();
+        }
       }
       __int128 sq[4];
       int lsb[4];
 #pragma unroll
       for (int q = 0; q < 4; ++q) {
+        fx[q].fold();
         sq[q] = fx[q].sum();
         lsb[q] = __reduce_min_sync(0xffffffffu, fx[q].lsb);
       }
@@ -2955,12 +2995,16 @@ inline unsigned grid_for(int64_t n, int threads, int64_t cap = 0) {
 // Host orchestration
 // ---------------------------------------------------------------------------
 
+// Deep levels (nodes of ~2048 elements or fewer on average): the chunk
+// kernels run a warp per chunk.
+inline bool wm_level(int64_t L, int64_t n) { return L * 2048 >= n; }
+
 DeviceTree::~DeviceTree() {
   void *ptrs[] = {epos_, tpos_, oid_, toid_, idx_, nodes_, ppm_, chunk_node_, chunk_base_, part_,
                   left_cnt_, left_base_, scan_tmp_, node_tmp_, fallback_, counters_, leaf_ids_,
                   leaf_tmp_, leafdesc_, segs_, idx_list_, table_, items_, items_tmp_, gidx_,
                   tight_chunks_, tight_nodes_, segs_local_, ridx_, sub_nodes_, sub_first_,
-                  sub_hist_, sub_pos_, sub_tot_, sub_stats_, wpre_};
+                  sub_hist_, sub_pos_, sub_tot_, sub_stats_, wpre_, chains_};
   for (void *p : ptrs)
     if (p) cudaFree(p);
   if (h_counters_) cudaFreeHost(h_counters_);
@@ -3123,6 +3167,8 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
     DT_CHECK(grow(left_cnt_, cap_lc_, size_t(max_chunks), s));
     DT_CHECK(grow(left_base_, cap_lb_, size_t(max_chunks), s));
     DT_CHECK(grow(wpre_, cap_wp_, size_t(max_chunks) * (kChunkThreads / 32), s));
+    if (level_max > kNodeMax && !wm_level(L, n))
+      DT_CHECK(grow(chains_, cap_ch_, size_t(std::max<int64_t>(n, 1)), s));
     const unsigned gL = unsigned((L + 127) / 128);
     const bool small = int64_t(L) <= kScanBlock;
     if (small) {
@@ -3133,6 +3179,7 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
       DT_CHECK(cudaMemsetAsync(counters_ + C_NFALLBACK, 0, sizeof(int64_t), s));
       DT_CHECK(cudaMemsetAsync(counters_ + C_NTIGHT, 0, sizeof(int64_t), s));
       DT_CHECK(cudaMemsetAsync(counters_ + C_MAXCNT, 0, sizeof(int64_t), s));
+      DT_CHECK(cudaMemsetAsync(counters_ + C_CHAINS, 0, sizeof(int64_t), s));
       k_chunk_counts<<<gL, 128, 0, s>>>(nodes_, nb, ne, node_tmp_);
       ++info_.launches;
       DT_CHECK(scan_counted(node_tmp_, chunk_base_, L, counters_ + C_NCHUNK, scan_tmp_, s));
@@ -3140,7 +3187,7 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
       ++info_.launches;
     }
     // deep levels (nodes of ~2048 elements or fewer on average): a warp per chunk
-    const bool wm = int64_t(L) * 2048 >= n;
+    const bool wm = wm_level(L, n);
     const unsigned gC = wm ? unsigned((max_chunks + 7) / 8) : unsigned(max_chunks);
 #define CHUNK_LAUNCH(kern, ...)                                                  \
   do {                                                                           \
@@ -3202,7 +3249,14 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
       CHUNK_LAUNCH(k_part_left, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
                    counters_ + C_NCHUNK, left_base_, wpre_, tpos_, toid_, idx_, ridx_);
       CHUNK_LAUNCH(k_part_right, epos_, oid_, nodes_, chunk_node_, chunk_base_, nb,
-                   counters_ + C_NCHUNK, idx_, ridx_, tpos_, toid_, walk_err_);
+                   counters_ + C_NCHUNK, idx_, ridx_, tpos_, toid_, walk_err_, counters_,
+                   reinterpret_cast<ChainItem *>(chains_), int64_t(cap_ch_));
+      if (!wm) {
+        k_part_chains<<<unsigned(4 * sm_count()), 256, 0, s>>>(
+            epos_, oid_, nodes_, reinterpret_cast<const ChainItem *>(chains_), int64_t(cap_ch_),
+            counters_, idx_, ridx_, tpos_, toid_, walk_err_);
+        ++info_.launches;
+      }
     }
 #undef CHUNK_LAUNCH
     std::swap(epos_, tpos_);

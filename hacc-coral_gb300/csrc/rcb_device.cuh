@@ -136,7 +136,8 @@ class DeviceTree {
   int32_t *left_cnt_ = nullptr;
   int64_t *left_base_ = nullptr;
   int32_t *wpre_ = nullptr;  // per chunk: each warp's left elements before its share
-  size_t cap_lc_ = 0, cap_lb_ = 0, cap_wp_ = 0;
+  int4 *chains_ = nullptr;    // the level's long swap chains (16 bytes each)
+  size_t cap_lc_ = 0, cap_lb_ = 0, cap_wp_ = 0, cap_ch_ = 0;
   int64_t *scan_tmp_ = nullptr;
   size_t cap_scan_ = 0;
   int64_t *node_tmp_ = nullptr;
