@@ -3009,6 +3009,12 @@ DeviceTree::~DeviceTree() {
     if (p) cudaFree(p);
   if (h_counters_) cudaFreeHost(h_counters_);
   if (h_sub_) cudaFreeHost(h_sub_);
+  if (aux_) {
+    cudaStreamSynchronize(aux_);
+    cudaStreamDestroy(aux_);
+  }
+  if (ev_fork_) cudaEventDestroy(ev_fork_);
+  if (ev_groups_) cudaEventDestroy(ev_groups_);
 }
 
 template <typename T>
@@ -3041,6 +3047,10 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   info_ = DeviceTreeInfo{};
   err_ = nullptr;
   padded_pairs_ = 0;
+  if (aux_) {  // a previous build that stopped early may have left its groups running
+    DT_CHECK(cudaStreamSynchronize(aux_));
+    groups_ready_ = 0;
+  }
   const auto t0 = std::chrono::steady_clock::now();
   const int k = cfg.tdpts;
   {
@@ -3353,6 +3363,19 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   DT_CHECK(cudaStreamSynchronize(s));
   const int64_t nleaves = h_counters_[C_NLEAF];
   info_.processed_leaves = nleaves;
+  // the groups need only the leaves: on the second stream, beside the walk
+  // (forked here, launched after the walk)
+  group_ = cfg.group == 16 ? 16 : 32;
+  DT_CHECK(grow(gidx_, cap_gidx_, size_t(std::max<int64_t>(n, 1)), s));
+  if (nleaves > 0) {
+    if (!aux_) {
+      DT_CHECK(cudaStreamCreateWithFlags(&aux_, cudaStreamNonBlocking));
+      DT_CHECK(cudaEventCreateWithFlags(&ev_fork_, cudaEventDisableTiming));
+      DT_CHECK(cudaEventCreateWithFlags(&ev_groups_, cudaEventDisableTiming));
+    }
+    DT_CHECK(cudaEventRecord(ev_fork_, s));
+    DT_CHECK(cudaStreamWaitEvent(aux_, ev_fork_, 0));
+  }
 
   // ---- lists: count, scan, write ----
   const size_t nlw = size_t(std::max<int64_t>(nleaves, 1));
@@ -3370,6 +3393,10 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
         nodes_, nnodes, leaf_ids_, nleaves, cfg, n, seg_cnt, list_len, nullptr, nullptr,
         segs_local_, walk_err_, counters_);
     ++info_.launches;
+    // the groups after the walk's blocks, which then have their SMs first
+    DT_CHECK(launch_groups(nleaves, group_, aux_));
+    DT_CHECK(cudaEventRecord(ev_groups_, aux_));
+    groups_ready_ = group_;
     DT_CHECK(scan_counted(seg_cnt, seg_base, nleaves, counters_ + C_NSEG, scan_tmp_, s));
     DT_CHECK(scan_counted(list_len, list_base, nleaves, counters_ + C_NENT, scan_tmp_, s));
   }
@@ -3420,8 +3447,7 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   }
   DT_CHECK(cudaGetLastError());
 
-  // ---- groups and work items ----
-  group_ = cfg.group == 16 ? 16 : 32;
+  // ---- work items ----
   DT_CHECK(make_items(n, jsplit, s));
   lists_ms_ = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t1).count();
   return cudaSuccess;
@@ -3446,17 +3472,27 @@ cudaError_t DeviceTree::regroup(int group, int64_t jsplit, cudaStream_t s) {
   return make_items(n_, jsplit, s);
 }
 
+cudaError_t DeviceTree::launch_groups(int64_t nleaves, int G, cudaStream_t s) {
+  k_groups_warp<<<unsigned((nleaves + kGWarps - 1) / kGWarps), 32 * kGWarps, 0, s>>>(
+      nodes_, leaf_ids_, nleaves, epos_, gidx_, G);
+  k_groups<<<unsigned(nleaves), kGroupThreads, 0, s>>>(nodes_, leaf_ids_, nleaves, epos_, gidx_, G);
+  info_.launches += 2;
+  return cudaGetLastError();
+}
+
 cudaError_t DeviceTree::make_items(int64_t n, int64_t jsplit, cudaStream_t s) {
   const int64_t nleaves = info_.processed_leaves;
   const int G = group_;
   DT_CHECK(grow(gidx_, cap_gidx_, size_t(std::max<int64_t>(n, 1)), s));
   DT_CHECK(cudaMemsetAsync(counters_ + C_BUCKET, 0, 32 * sizeof(int64_t), s));
   if (nleaves > 0) {
-    k_groups_warp<<<unsigned((nleaves + kGWarps - 1) / kGWarps), 32 * kGWarps, 0, s>>>(
-        nodes_, leaf_ids_, nleaves, epos_, gidx_, G);
-    ++info_.launches;
-    k_groups<<<unsigned(nleaves), kGroupThreads, 0, s>>>(nodes_, leaf_ids_, nleaves, epos_, gidx_, G);
-    ++info_.launches;
+    if (groups_ready_ == G) {
+      DT_CHECK(cudaStreamWaitEvent(s, ev_groups_, 0));  // launched by build()
+    } else {
+      if (groups_ready_) DT_CHECK(cudaStreamWaitEvent(s, ev_groups_, 0));
+      DT_CHECK(launch_groups(nleaves, G, s));
+    }
+    groups_ready_ = 0;
     k_item_hist<<<unsigned((nleaves + 127) / 128), 128, 0, s>>>(leafdesc_, nleaves, jsplit, G,
                                                                 counters_);
     ++info_.launches;

@@ -117,6 +117,11 @@ class DeviceTree {
   std::vector<int32_t> levels_;
   const char *err_ = nullptr;
   int group_ = 32;
+  // the build's groups run on their own stream beside the list walk
+  cudaStream_t aux_ = nullptr;
+  cudaEvent_t ev_fork_ = nullptr, ev_groups_ = nullptr;
+  int groups_ready_ = 0;  // G of groups launched on aux_ and not yet joined
+  cudaError_t launch_groups(int64_t nleaves, int G, cudaStream_t s);
   int64_t n_ = 0;
   // elements: current and scratch (x, y, z, m) + input index
   float4 *epos_ = nullptr, *tpos_ = nullptr;
