@@ -1188,7 +1188,7 @@ hsr_status force_fwd_impl(hsr_ctx *ctx, const hsr_params *p, int64_t n, const fl
   cfg.ppc = p->ppc;
   cfg.nd = int32_t(std::min<int64_t>(p->nd, INT32_MAX));
   cfg.tdpts = p->tdpts;
-  cfg.group = 32;  // the adjoint kernel takes one particle per lane
+  cfg.group = ctx->tune.group;  // the adjoint kernel takes groups of 16 or 32
   cudaError_t e = ctx->tree.build(cfg, n, pos4, kJSplit, s);
   if (e != cudaSuccess) {
     if (ctx->tree.error()) return ctx->fail(HSR_ERR_UNSUPPORTED, ctx->tree.error());
@@ -1784,7 +1784,7 @@ hsr_status force_batch_impl(hsr_ctx *ctx, int32_t nbox, const hsr_params *params
     cfg.ppc = p->ppc;
     cfg.nd = int32_t(std::min<int64_t>(p->nd, INT32_MAX));
     cfg.tdpts = p->tdpts;
-    cfg.group = 32;  // the adjoint kernel takes one particle per lane
+    cfg.group = ctx->tune.group;  // the adjoint kernel takes groups of 16 or 32
     cudaError_t e = B.tree.build(cfg, n, B.pos4.as<float4>(), kJSplit, s);
     if (e != cudaSuccess) {
       if (B.tree.error()) return fail(HSR_ERR_UNSUPPORTED, B.tree.error());
@@ -1862,7 +1862,8 @@ hsr_status force_batch_impl(hsr_ctx *ctx, int32_t nbox, const hsr_params *params
   CU(ctx->d_queue.ensure(64), "cudaMalloc(queue)");
   if (ctx->batched_ctas == 0) ctx->batched_ctas = hsr::batched_resident_ctas(ctx->device);
   CU(cudaEventRecord(ctx->ev0, s), "event");
-  if (total_items > 0) CU(launch_batch_graph(ctx, params[0].law, 32, total_items), "multi-box pair launch");
+  if (total_items > 0)
+    CU(launch_batch_graph(ctx, params[0].law, ctx->tune.group, total_items), "multi-box pair launch");
   CU(cudaEventRecord(ctx->ev1, s), "event");
   for (int32_t b = 0; b < nbox; ++b) {
     BoxState &B = *ctx->boxes[b];
@@ -1905,7 +1906,7 @@ hsr_status force_batch_impl(hsr_ctx *ctx, int32_t nbox, const hsr_params *params
   ctx->batch_n = nbox;
   ctx->batch_items = total_items;
   ctx->batch_law = params[0].law;
-  ctx->batch_group = 32;
+  ctx->batch_group = ctx->tune.group;
   return HSR_OK;
 }
 

@@ -465,14 +465,25 @@ cudaError_t launch_tag_items(const PairItem *in, PairItem *out, int64_t n, int b
 // so the pair adds v = M u_i to xbar_j and subtracts it from xbar_i.  Each
 // pair's v is computed once, lanes = the group's particles and two buffered
 // entries per step on packed FP32: the particle side accumulates in
-// registers, and the entry side goes through shared memory -- for 16 buffered
-// entries at a time every lane writes its v into one row per entry, and then
-// 16 lanes each sum one entry's row (16-byte loads) and add it with one
-// atomic triple.  Self entries (j = i) are skipped: their two terms cancel.
+// registers, and the entry side goes through shared memory -- every lane
+// writes its v into one row per entry, and then one lane per entry sums the
+// entry's row (16-byte loads) and adds it with one atomic triple.  Groups of
+// more than 16 particles take a lane each, 16 buffered entries per transpose;
+// groups of at most 16 run on both half-warps as in k_pairs_batched (half 0
+// the even slot pairs, half 1 the odd ones), 32 entries of 16-column rows per
+// transpose, and their particle sums are added across the halves at the end.
+// Self entries (j = i) are skipped: their two terms cancel.
 // ---------------------------------------------------------------------------
 constexpr int kVjpRow = 36;   // floats per transpose row: 32 particles, 16-byte rows
 constexpr int kVjpRows = 16;  // entries per transpose
-constexpr size_t kVjpSmem = size_t(kBatchedWarps) * 3 * kVjpRows * kVjpRow * sizeof(float);
+// half-warp groups: 16 particles per row; a stride of 24 floats puts the two
+// halves' rows (two apart) on disjoint banks
+constexpr int kVjpRowH = 24;
+constexpr int kVjpRowsH = 32;
+constexpr int kVjpWarpFloats = 3 * kVjpRowsH * kVjpRowH > 3 * kVjpRows * kVjpRow
+                                   ? 3 * kVjpRowsH * kVjpRowH
+                                   : 3 * kVjpRows * kVjpRow;
+constexpr size_t kVjpSmem = size_t(kBatchedWarps) * kVjpWarpFloats * sizeof(float);
 
 template <int LAW, bool MULTI>
 __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
@@ -495,7 +506,7 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
   const unsigned below = (1u << lane) - 1u;
   float *const fa = reinterpret_cast<float *>(bufA[w]);
   float *const fb = reinterpret_cast<float *>(bufB[w]);
-  float *const tv = reinterpret_cast<float *>(vjp_rows) + size_t(w) * 3 * kVjpRows * kVjpRow;
+  float *const tv = reinterpret_cast<float *>(vjp_rows) + size_t(w) * kVjpWarpFloats;
   for (;;) {
     unsigned long long it = 0;
     if (lane == 0) it = atomicAdd(queue, 1ull);
@@ -523,8 +534,12 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
       rcut2 = B.rcut2;
       rcull2 = B.rcull2;
     }
-    const bool act = lane < W.g_count;
-    const int pi = gidx[W.g_begin + (act ? lane : 0)];
+    // groups of at most 16 particles on half-warps (warp-uniform)
+    const bool hm = W.g_count <= 16;
+    const int gl = hm ? (lane & 15) : lane;  // particle of the group
+    const int half = hm ? (lane >> 4) : 0;
+    const bool act = gl < W.g_count;
+    const int pi = gidx[W.g_begin + (act ? gl : 0)];
     const float4 P = pos[pi];
     // inactive lanes carry a zero cotangent and weight, so they add nothing
     const float u0 = act ? ux[pi] : 0.f, u1 = act ? uy[pi] : 0.f, u2 = act ? uz[pi] : 0.f;
@@ -552,12 +567,27 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
     const int32_t *lst = idx + W.j_begin;
     const int len = W.j_len;
     int nbuf = 0;
+    // software pipeline as in k_pairs_batched: the next step's entry and the
+    // index of the one after it are in flight while this step runs
+    int32_t jtn = 0, in2 = 0;
+    float4 Jn = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (len > 0) {
+      jtn = lst[lane < len ? lane : 0];
+      Jn = pos[jtn];
+      in2 = lst[32 + lane < len ? 32 + lane : 0];
+    }
     for (int j0 = 0; j0 < len || nbuf > 0; j0 += 32) {
       if (j0 < len) {
         const int j = j0 + lane;
         const bool ok = j < len;
-        const int32_t jt = lst[ok ? j : 0];
-        const float4 J = pos[jt];
+        const int32_t jt = jtn;
+        const float4 J = Jn;
+        if (j0 + 32 < len) {
+          jtn = in2;
+          Jn = pos[in2];
+          const int j2 = j0 + 64 + lane;
+          in2 = lst[j2 < len ? j2 : 0];
+        }
         const float dx = fmaxf(fabsf(J.x - cx) - hx, 0.f);
         const float dy = fmaxf(fabsf(J.y - cy) - hy, 0.f);
         const float dz = fmaxf(fabsf(J.z - cz) - hz, 0.f);
@@ -587,24 +617,72 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
         bufI[w][lane] = -2;
       }
       __syncwarp();
-      for (int h = 0; 16 * h < ne; ++h) {
+      // v of slot pair q's two entries against this lane's particle
+      auto eval_pair = [&](int q, float2 &vx, float2 &vy, float2 &vz) {
+        const float4 A = bufA[w][q], B = bufB[w][q];
+        const int ja = bufI[w][2 * q], jb = bufI[w][2 * q + 1];
+        const float2 ex = __fadd2_rn(make_float2(A.x, A.y), nxi);
+        const float2 ey = __fadd2_rn(make_float2(A.z, A.w), nyi);
+        const float2 ez = __fadd2_rn(make_float2(B.x, B.y), nzi);
+        const float2 r2 = __ffma2_rn(ex, ex, __ffma2_rn(ey, ey, __fmul2_rn(ez, ez)));
+        const bool on_a = act && ja != pi && in_range<LAW>(r2.x, rcut2);
+        const bool on_b = act && jb != pi && in_range<LAW>(r2.y, rcut2);
+        vjp2_term<LAW>(ex, ey, ez, __fmul2_rn(wi2, make_float2(B.z, B.w)), ua, ub, uc, rsm2,
+                       on_a, on_b, vx, vy, vz);
+        bx = __fadd2_rn(bx, vx);
+        by = __fadd2_rn(by, vy);
+        bz = __fadd2_rn(bz, vz);
+      };
+      if (hm) {
+        // all (up to 32) entries in one transpose: half 0 the even slot
+        // pairs, half 1 the odd ones
+        const int nq = (ne + 1) / 2;
+        for (int q = half; q < nq; q += 2) {
+          float2 vx, vy, vz;
+          eval_pair(q, vx, vy, vz);
+          float *row = tv + (2 * q) * kVjpRowH + gl;
+          row[0] = vx.x;
+          row[kVjpRowH] = vx.y;
+          row[kVjpRowsH * kVjpRowH] = vy.x;
+          row[(kVjpRowsH + 1) * kVjpRowH] = vy.y;
+          row[2 * kVjpRowsH * kVjpRowH] = vz.x;
+          row[(2 * kVjpRowsH + 1) * kVjpRowH] = vz.y;
+        }
+        __syncwarp();
+        // entry side: lane e sums entry e's row of each component; rows start
+        // on 4 bank groups only (stride 24), so lanes 4-7 of each quarter-warp
+        // take the row's 16-byte pieces rotated by one, which puts a quarter-
+        // warp's 8 loads on 32 distinct banks
+        if (lane < ne) {
+          float sum[3];
+          const int rot = (lane >> 2) & 1;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const float4 *row =
+                reinterpret_cast<const float4 *>(tv + (c * kVjpRowsH + lane) * kVjpRowH);
+            float2 s2 = make_float2(0.f, 0.f);
+#pragma unroll
+            for (int k = 0; k < 4; ++k) {
+              const float4 t = row[(k + rot) & 3];
+              s2 = __fadd2_rn(s2, __fadd2_rn(make_float2(t.x, t.y), make_float2(t.z, t.w)));
+            }
+            sum[c] = s2.x + s2.y;
+          }
+          const int jt = bufI[w][lane];
+          if (sum[0] != 0.f || sum[1] != 0.f || sum[2] != 0.f) {
+            atomicAdd(xbx + jt, sum[0]);
+            atomicAdd(xby + jt, sum[1]);
+            atomicAdd(xbz + jt, sum[2]);
+          }
+        }
+        __syncwarp();
+      }
+      for (int h = 0; !hm && 16 * h < ne; ++h) {
         // entries 16h .. 16h + 15 of the buffer
         const int q1 = min(8 * h + 8, (ne + 1) / 2);
         for (int q = 8 * h; q < q1; ++q) {
-          const float4 A = bufA[w][q], B = bufB[w][q];
-          const int ja = bufI[w][2 * q], jb = bufI[w][2 * q + 1];
-          const float2 ex = __fadd2_rn(make_float2(A.x, A.y), nxi);
-          const float2 ey = __fadd2_rn(make_float2(A.z, A.w), nyi);
-          const float2 ez = __fadd2_rn(make_float2(B.x, B.y), nzi);
-          const float2 r2 = __ffma2_rn(ex, ex, __ffma2_rn(ey, ey, __fmul2_rn(ez, ez)));
-          const bool on_a = act && ja != pi && in_range<LAW>(r2.x, rcut2);
-          const bool on_b = act && jb != pi && in_range<LAW>(r2.y, rcut2);
           float2 vx, vy, vz;
-          vjp2_term<LAW>(ex, ey, ez, __fmul2_rn(wi2, make_float2(B.z, B.w)), ua, ub, uc, rsm2,
-                         on_a, on_b, vx, vy, vz);
-          bx = __fadd2_rn(bx, vx);
-          by = __fadd2_rn(by, vy);
-          bz = __fadd2_rn(bz, vz);
+          eval_pair(q, vx, vy, vz);
           float *row = tv + (2 * q - 16 * h) * kVjpRow + lane;
           row[0] = vx.x;
           row[kVjpRow] = vx.y;
@@ -614,22 +692,24 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
           row[(2 * kVjpRows + 1) * kVjpRow] = vz.y;
         }
         __syncwarp();
-        // entry side: lane e sums entry 16h + e's row of each component
-        const int e = 16 * h + lane;
-        if (lane < 16 && e < ne) {
-          float sum[3];
+        // entry side: lanes r and r + 16 sum the two halves of entry 16h + r's
+        // row of each component
+        const int er = lane & 15, e = 16 * h + er, part = lane >> 4;
+        float sum[3];
 #pragma unroll
-          for (int c = 0; c < 3; ++c) {
-            const float4 *row =
-                reinterpret_cast<const float4 *>(tv + (c * kVjpRows + lane) * kVjpRow);
-            float2 s2 = make_float2(0.f, 0.f);
+        for (int c = 0; c < 3; ++c) {
+          const float4 *row =
+              reinterpret_cast<const float4 *>(tv + (c * kVjpRows + er) * kVjpRow) + 4 * part;
+          float2 s2 = make_float2(0.f, 0.f);
 #pragma unroll
-            for (int k = 0; k < 8; ++k) {
-              const float4 t = row[k];
-              s2 = __fadd2_rn(s2, __fadd2_rn(make_float2(t.x, t.y), make_float2(t.z, t.w)));
-            }
-            sum[c] = s2.x + s2.y;
+          for (int k = 0; k < 4; ++k) {
+            const float4 t = row[k];
+            s2 = __fadd2_rn(s2, __fadd2_rn(make_float2(t.x, t.y), make_float2(t.z, t.w)));
           }
+          sum[c] = s2.x + s2.y;
+          sum[c] += __shfl_xor_sync(full, sum[c], 16);
+        }
+        if (part == 0 && e < ne) {
           const int jt = bufI[w][e];
           if (sum[0] != 0.f || sum[1] != 0.f || sum[2] != 0.f) {
             atomicAdd(xbx + jt, sum[0]);
@@ -651,10 +731,16 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
       __syncwarp();
       if (j0 >= len && nbuf == 0) break;
     }
-    if (act) {
-      atomicAdd(xbx + pi, -(bx.x + bx.y));
-      atomicAdd(xby + pi, -(by.x + by.y));
-      atomicAdd(xbz + pi, -(bz.x + bz.y));
+    float sx = bx.x + bx.y, sy = by.x + by.y, sz = bz.x + bz.y;
+    if (hm) {
+      sx += __shfl_xor_sync(full, sx, 16);
+      sy += __shfl_xor_sync(full, sy, 16);
+      sz += __shfl_xor_sync(full, sz, 16);
+    }
+    if (act && half == 0) {
+      atomicAdd(xbx + pi, -sx);
+      atomicAdd(xby + pi, -sy);
+      atomicAdd(xbz + pi, -sz);
     }
   }
 }

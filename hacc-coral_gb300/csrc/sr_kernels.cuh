@@ -252,26 +252,29 @@ __device__ __forceinline__ float2 neg_poly2<LAW_POLY5_STEP16>(float2 r2) {
   for (int k = 1; k < 6; ++k) q = __ffma2_rn(q, r2, make_float2(c[k], c[k]));
   return q;
 }
+// -2 p'(r2) of the law on two values at once (packed FP32): neg_dpoly's
+// coefficients doubled (exactly) and its Horner order, so the result is
+// exactly twice neg_dpoly's.
 template <int LAW>
-__device__ __forceinline__ float2 neg_dpoly2(float2 r2);
+__device__ __forceinline__ float2 neg_dpoly2_x2(float2 r2);
 template <>
-__device__ __forceinline__ float2 neg_dpoly2<LAW_POLY6>(float2 r2) {
-  const float c[6] = {-6.0f * static_cast<float>(0.000000147305),
-                      -5.0f * static_cast<float>(-0.00000663394),
-                      -4.0f * static_cast<float>(0.000132336),
-                      -3.0f * static_cast<float>(-0.00159485),
-                      -2.0f * static_cast<float>(0.0133122), -static_cast<float>(-0.0783394)};
+__device__ __forceinline__ float2 neg_dpoly2_x2<LAW_POLY6>(float2 r2) {
+  const float c[6] = {-12.0f * static_cast<float>(0.000000147305),
+                      -10.0f * static_cast<float>(-0.00000663394),
+                      -8.0f * static_cast<float>(0.000132336),
+                      -6.0f * static_cast<float>(-0.00159485),
+                      -4.0f * static_cast<float>(0.0133122), -2.0f * static_cast<float>(-0.0783394)};
   float2 q = make_float2(c[0], c[0]);
 #pragma unroll
   for (int k = 1; k < 6; ++k) q = __ffma2_rn(q, r2, make_float2(c[k], c[k]));
   return q;
 }
 template <>
-__device__ __forceinline__ float2 neg_dpoly2<LAW_POLY5_STEP16>(float2 r2) {
-  const float c[5] = {-5.0f * static_cast<float>(-0.00000147177),
-                      -4.0f * static_cast<float>(0.0000605491),
-                      -3.0f * static_cast<float>(-0.00109313),
-                      -2.0f * static_cast<float>(0.0114808), -static_cast<float>(-0.0750978)};
+__device__ __forceinline__ float2 neg_dpoly2_x2<LAW_POLY5_STEP16>(float2 r2) {
+  const float c[5] = {-10.0f * static_cast<float>(-0.00000147177),
+                      -8.0f * static_cast<float>(0.0000605491),
+                      -6.0f * static_cast<float>(-0.00109313),
+                      -4.0f * static_cast<float>(0.0114808), -2.0f * static_cast<float>(-0.0750978)};
   float2 q = make_float2(c[0], c[0]);
 #pragma unroll
   for (int k = 1; k < 5; ++k) q = __ffma2_rn(q, r2, make_float2(c[k], c[k]));
@@ -290,11 +293,12 @@ __device__ __forceinline__ void vjp2_term(float2 ex, float2 ey, float2 ez, float
   const float2 y = make_float2(rsqrt_ftz(s.x), rsqrt_ftz(s.y));
   const float2 y2 = __fmul2_rn(y, y);
   const float2 g = __ffma2_rn(y, y2, neg_poly2<LAW>(r2));
-  const float2 gp = __ffma2_rn(__fmul2_rn(make_float2(-1.5f, -1.5f), y2), __fmul2_rn(y2, y),
-                               neg_dpoly2<LAW>(r2));
+  // 2 g': the factors 2 folded into the constants (exact)
+  const float2 gp2 = __ffma2_rn(__fmul2_rn(make_float2(-3.f, -3.f), y2), __fmul2_rn(y2, y),
+                                neg_dpoly2_x2<LAW>(r2));
   const float2 du = __ffma2_rn(ex, u0, __ffma2_rn(ey, u1, __fmul2_rn(ez, u2)));
   float2 a = __fmul2_rn(w, g);
-  float2 bq = __fmul2_rn(__fmul2_rn(__fmul2_rn(make_float2(2.f, 2.f), w), gp), du);
+  float2 bq = __fmul2_rn(w, __fmul2_rn(gp2, du));
   a.x = on_a ? a.x : 0.f;
   a.y = on_b ? a.y : 0.f;
   bq.x = on_a ? bq.x : 0.f;

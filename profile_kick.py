@@ -5,6 +5,7 @@ sequence for profilers (ncu's launch lists and kernel captures).
     python profile_kick.py --workload zeldovich --ng 128 --reps 2
     python profile_kick.py --workload clustered --ng 256 --shape batched-32
     python profile_kick.py --ng 128 --reps 2 --pm f64   # + the PM kick
+    python profile_kick.py --ng 128 --reps 3 --vjp      # + force forward and its VJP
 """
 from __future__ import annotations
 
@@ -36,6 +37,9 @@ def main(argv=None) -> int:
                     help="plain-32|plain-64|plain-128|batched-16|batched-32")
     ap.add_argument("--pm", choices=["none", "f64", "f32"], default="none",
                     help="also run the long-range PM kick (hsr_pm_kick) after each short-range kick")
+    ap.add_argument("--vjp", action="store_true",
+                    help="also run the force forward map on the kick's input and its VJP "
+                         "(hsr_force_fwd, hsr_force_vjp) with a fixed random cotangent")
     ap.add_argument("--device", type=int, default=0)
     a = ap.parse_args(argv)
     kind, num = a.shape.split("-")
@@ -51,6 +55,15 @@ def main(argv=None) -> int:
             st = ctx.rcb_kick(q, kp, kernel=hsr.KERNEL_AUTO)
             print(json.dumps({"rep": r, "workload": f"{a.workload}{a.ng}", "shape": a.shape,
                               **{k: st[k] for k in KEYS}}), flush=True)
+            if a.vjp:
+                import numpy as np
+                ctx.force_fwd(p.x, p.y, p.z, p.mass, kp)
+                fwd = ctx.stats()["t_force_ms"]
+                u = np.random.default_rng(1).standard_normal((p.n, 3)).astype(np.float32)
+                ctx.force_vjp(u)
+                vjp = ctx.stats()["t_force_ms"]
+                print(json.dumps({"rep": r, "forward_ms": fwd, "vjp_ms": vjp,
+                                  "vjp_over_forward": vjp / fwd}), flush=True)
             if a.pm != "none":
                 prm = hsr.pm_params(a.ng, p.meta["ngo"], 1.0, 1.0, 1e-3,
                                     hsr.PM_F64 if a.pm == "f64" else hsr.PM_F32)

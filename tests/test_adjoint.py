@@ -53,8 +53,19 @@ def test_vjp_and_fd_oracles_agree_on_cpu(hsr_lib, oracle_lib):
     assert ok.sum() > 40 and np.all(err <= 1e-6 * scale)
 
 
+@pytest.fixture
+def group_tune(ctx, request):
+    """The context's batched shape with groups of request.param particles
+    (16: the adjoint kernel's half-warp groups), restored afterwards."""
+    saved = ctx.get_tune()
+    ctx.set_tune("batched", 128, request.param)
+    yield request.param
+    ctx.set_tune(saved["kernel"], saved["leaf_threads"], saved["group"])
+
+
 @pytest.mark.gpu
-def test_vjp_matches_fp64_gradient_and_finite_differences(ctx, oracle_lib):
+@pytest.mark.parametrize("group_tune", [32, 16], indirect=True)
+def test_vjp_matches_fp64_gradient_and_finite_differences(ctx, oracle_lib, group_tune):
     p = synth.zeldovich_box(64, z=10.0, seed=3)
     kp = synth.kick_params(p, nd=64, fcoeff=1.0)
     n = p.n
