@@ -1329,8 +1329,10 @@ hsr_status hsr_force_vjp(hsr_ctx *ctx, const float *dvbx, const float *dvby, con
                            xb, xb + st_, xb + 2 * st_, w.fcoeff, w.rsm2, w.rc2, w.rcull2,
                            ctx->d_queue.as<unsigned long long>(), ctx->batched_ctas, s),
      "adjoint kernel");
+  int32_t *aerr = reinterpret_cast<int32_t *>(acc);
+  CU(cudaMemsetAsync(aerr, 0, sizeof(int32_t), s), "reset flag");
   CU(hsr::launch_pseudo_adjoint(ctx->tree.nodes(), ctx->tree.levels(), w.table, n, xb, xb + st_,
-                                xb + 2 * st_, acc, s),
+                                xb + 2 * st_, aerr, s),
      "pseudo-particle adjoint");
   CU(cudaEventRecord(ctx->ev1, s), "event");
   float *outs[3] = {xbx, xby, xbz};
@@ -1340,7 +1342,10 @@ hsr_status hsr_force_vjp(hsr_ctx *ctx, const float *dvbx, const float *dvby, con
     if (mem == HSR_MEM_HOST)
       CU(cudaMemcpyAsync(outs[d], o, size_t(n) * 4, cudaMemcpyDeviceToHost, s), "D2H xbar");
   }
+  int32_t h_aerr = 0;
+  CU(cudaMemcpyAsync(&h_aerr, aerr, sizeof(int32_t), cudaMemcpyDeviceToHost, s), "D2H flag");
   CU(cudaStreamSynchronize(s), "adjoint");
+  if (h_aerr) return ctx->fail(HSR_ERR_STATE, "pseudo-particle adjoint: inconsistent tree");
   float ms = 0;
   CU(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "event time");
   ctx->stats.t_force_ms = ms;
@@ -2000,6 +2005,7 @@ hsr_status hsr_force_vjp_batch(hsr_ctx *ctx, int32_t nbox, const float *const *d
                                  ctx->d_queue.as<unsigned long long>(), ctx->batched_ctas, s),
      "multi-box adjoint kernel");
   CU(cudaEventRecord(ctx->ev1, s), "event");
+  std::vector<int32_t *> aerrs;
   for (int32_t b = 0; b < nbox; ++b) {
     BoxState &B = *ctx->boxes[b];
     const int64_t n = B.n;
@@ -2009,10 +2015,12 @@ hsr_status hsr_force_vjp_batch(hsr_ctx *ctx, int32_t nbox, const float *const *d
     const size_t st_ = size_t((std::max<int64_t>(ntab, 1) + 63) & ~int64_t(63));
     float *ub = B.adj.as<float>();
     float *xb = ub + 6 * sn;
-    float *acc = xb + 3 * st_;
+    int32_t *aerr = reinterpret_cast<int32_t *>(xb + 3 * st_);
+    CU(cudaMemsetAsync(aerr, 0, sizeof(int32_t), s), "reset flag");
     CU(hsr::launch_pseudo_adjoint(B.tree.nodes(), B.tree.levels(), B.tree.table(), n, xb, xb + st_,
-                                  xb + 2 * st_, acc, s),
+                                  xb + 2 * st_, aerr, s),
        "pseudo-particle adjoint");
+    aerrs.push_back(aerr);
     float *outs[3] = {xbx[b], xby[b], xbz[b]};
     for (int d = 0; d < 3; ++d) {
       float *o = mem == HSR_MEM_HOST ? ub + d * sn : outs[d];
@@ -2021,7 +2029,12 @@ hsr_status hsr_force_vjp_batch(hsr_ctx *ctx, int32_t nbox, const float *const *d
         CU(cudaMemcpyAsync(outs[d], o, size_t(n) * 4, cudaMemcpyDeviceToHost, s), "D2H xbar");
     }
   }
+  std::vector<int32_t> h_aerrs(aerrs.size(), 0);
+  for (size_t b = 0; b < aerrs.size(); ++b)
+    CU(cudaMemcpyAsync(&h_aerrs[b], aerrs[b], sizeof(int32_t), cudaMemcpyDeviceToHost, s), "D2H flag");
   CU(cudaStreamSynchronize(s), "multi-box adjoint");
+  for (int32_t e : h_aerrs)
+    if (e) return ctx->fail(HSR_ERR_STATE, "pseudo-particle adjoint: inconsistent tree");
   float ms = 0;
   CU(cudaEventElapsedTime(&ms, ctx->ev0, ctx->ev1), "event time");
   ctx->stats.t_force_ms = ms;

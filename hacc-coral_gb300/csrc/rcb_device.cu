@@ -2913,42 +2913,40 @@ __global__ void k_scatter_add_f32(const float *__restrict__ in, const int32_t *_
 }
 
 // acc holds, per node, sum over it and its ancestors of xbar_P / M_P.
-__global__ void k_adj_root(const float4 *table, int64_t n, const float *xbx, const float *xby,
-                           const float *xbz, float *acc) {
-  const float m = table[n].w;
-  const float s = m != 0.f ? 1.f / m : 0.f;
-  acc[0] = xbx[n] * s;
-  acc[1] = xby[n] * s;
-  acc[2] = xbz[n] * s;
-}
-
-__global__ void k_adj_down(const DNode *nodes, int32_t lb, int32_t le, const float4 *table,
-                           int64_t n, const float *xbx, const float *xby, const float *xbz,
-                           float *acc) {
-  const int32_t t = lb + blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= le) return;
-  const DNode &T = nodes[t];
-  for (int s = 0; s < 2; ++s) {
-    const int32_t c = s == 0 ? T.cl : T.cr;
-    if (c <= 0) continue;
-    const float m = table[n + c].w;
+// Monopole pseudo-particle gradients passed to the particles: a warp per
+// leaf sums xbar / m of the nodes on its root-to-leaf path (root first, the
+// same float additions as a level-by-level top-down pass) and adds m_k times
+// the sum to each of its particles.  The path follows the child holding the
+// leaf's offset (left when below offset + nleft).
+__global__ void k_adj_paths(const DNode *__restrict__ nodes, int32_t nnodes,
+                            const float4 *__restrict__ table, int64_t n, float *xbx, float *xby,
+                            float *xbz, int32_t *err) {
+  const int32_t leaf = int32_t((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (leaf >= nnodes) return;  // whole warps
+  const DNode &L = nodes[leaf];
+  if (L.cl != 0 || L.cr != 0 || L.count <= 0) return;
+  const int32_t lo = L.offset;
+  float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+  int32_t t = 0;
+  for (int depth = 0;; ++depth) {
+    const float m = table[n + t].w;
     const float inv = m != 0.f ? 1.f / m : 0.f;
-    acc[3 * int64_t(c) + 0] = acc[3 * int64_t(t) + 0] + xbx[n + c] * inv;
-    acc[3 * int64_t(c) + 1] = acc[3 * int64_t(t) + 1] + xby[n + c] * inv;
-    acc[3 * int64_t(c) + 2] = acc[3 * int64_t(t) + 2] + xbz[n + c] * inv;
+    a0 = a0 + xbx[n + t] * inv;
+    a1 = a1 + xby[n + t] * inv;
+    a2 = a2 + xbz[n + t] * inv;
+    if (t == leaf) break;
+    const DNode &T = nodes[t];
+    const int32_t c = lo < T.offset + T.nleft ? T.cl : T.cr;
+    if (c <= 0 || c >= nnodes || depth > 256) {  // cannot happen in a valid tree
+      if (lane == 0) atomicExch(err, 5);
+      return;
+    }
+    t = c;
   }
-}
-
-__global__ void k_adj_leaves(const DNode *nodes, int32_t nnodes, const float4 *table, float *xbx,
-                             float *xby, float *xbz, const float *acc) {
-  const int32_t t = blockIdx.x;
-  if (t >= nnodes) return;
-  const DNode &T = nodes[t];
-  if (T.cl != 0 || T.cr != 0) return;
-  const float a0 = acc[3 * int64_t(t)], a1 = acc[3 * int64_t(t) + 1], a2 = acc[3 * int64_t(t) + 2];
   if (a0 == 0.f && a1 == 0.f && a2 == 0.f) return;
-  for (int32_t i = threadIdx.x; i < T.count; i += blockDim.x) {
-    const int32_t k = T.offset + i;
+  for (int32_t i = lane; i < L.count; i += 32) {
+    const int32_t k = L.offset + i;
     const float m = table[k].w;
     xbx[k] += m * a0;
     xby[k] += m * a1;
@@ -3554,18 +3552,12 @@ cudaError_t launch_scatter_add_f32(const float *in, const int32_t *perm, float *
 
 cudaError_t launch_pseudo_adjoint(const DNode *nodes, const std::vector<int32_t> &levels,
                                   const float4 *table, int64_t n, float *xbx, float *xby,
-                                  float *xbz, float *acc, cudaStream_t s) {
+                                  float *xbz, int32_t *err, cudaStream_t s) {
   if (levels.size() < 2) return cudaSuccess;
   const int32_t nnodes = levels.back();
   if (nnodes <= 0) return cudaSuccess;
-  k_adj_root<<<1, 1, 0, s>>>(table, n, xbx, xby, xbz, acc);
-  for (size_t l = 0; l + 1 < levels.size(); ++l) {
-    const int32_t lb = levels[l], le = levels[l + 1];
-    if (le > lb)
-      k_adj_down<<<unsigned((le - lb + 127) / 128), 128, 0, s>>>(nodes, lb, le, table, n, xbx, xby,
-                                                                 xbz, acc);
-  }
-  k_adj_leaves<<<unsigned(nnodes), 128, 0, s>>>(nodes, nnodes, table, xbx, xby, xbz, acc);
+  k_adj_paths<<<unsigned((int64_t(nnodes) * 32 + 255) / 256), 256, 0, s>>>(nodes, nnodes, table, n,
+                                                                           xbx, xby, xbz, err);
   return cudaGetLastError();
 }
 

@@ -211,9 +211,10 @@ cudaError_t launch_scatter_add_f32(const float *in, const int32_t *perm, float *
 // Monopole pseudo-particle gradients passed to the particles through the
 // nodes' centres of mass: xbar_k += m_k sum_{nodes P containing k} xbar_P / M_P,
 // where xbar_P sits at slot n + P of the 3 arrays and M_P is the pseudo mass.
+// *err (zeroed by the caller) is set on an inconsistent tree.
 cudaError_t launch_pseudo_adjoint(const DNode *nodes, const std::vector<int32_t> &levels,
                                   const float4 *table, int64_t n, float *xbx, float *xby,
-                                  float *xbz, float *acc, cudaStream_t s);
+                                  float *xbz, int32_t *err, cudaStream_t s);
 
 // Exclusive prefix sum of n int64 values (in may equal out); *total (device,
 // may be null) receives the sum.  tmp needs scan_tmp_size(n) elements.
