@@ -224,6 +224,8 @@ struct hsr_ctx {
   std::string err = "no error";
   bool have_lists = false;
   int last_tdpts = 1;
+  int32_t tape_nd = 0;   // the taped forward's leaf size and pseudo-particle contraction
+  float tape_ppc = 0.f;
   Work work;
   int batched_ctas = 0;
   // multi-box kicks
@@ -1248,6 +1250,8 @@ hsr_status force_fwd_impl(hsr_ctx *ctx, const hsr_params *p, int64_t n, const fl
   ctx->stats = st;
   ctx->have_lists = true;
   ctx->last_tdpts = p->tdpts;
+  ctx->tape_nd = int32_t(std::min<int64_t>(p->nd, INT32_MAX));
+  ctx->tape_ppc = p->ppc;
   ctx->tape = true;
   return HSR_OK;
 }
@@ -1290,8 +1294,7 @@ hsr_status hsr_force_vjp(hsr_ctx *ctx, const float *dvbx, const float *dvby, con
                          float *xbx, float *xby, float *xbz, int32_t mem) {
   if (!ctx) return HSR_ERR_ARG;
   if (!ctx->tape) return ctx->fail(HSR_ERR_STATE, "hsr_force_vjp needs a preceding hsr_force_fwd");
-  if (ctx->last_tdpts != 1)
-    return ctx->fail(HSR_ERR_UNSUPPORTED, "the adjoint takes monopole pseudo-particles (tdpts = 1)");
+  const bool quad = ctx->last_tdpts == 12;
   if (mem != HSR_MEM_HOST && mem != HSR_MEM_DEVICE) return ctx->fail(HSR_ERR_ARG, "bad memory kind");
   const Work &w = ctx->work;
   const int64_t n = w.n;
@@ -1300,16 +1303,21 @@ hsr_status hsr_force_vjp(hsr_ctx *ctx, const float *dvbx, const float *dvby, con
   CU(cudaSetDevice(ctx->device), "cudaSetDevice");
   cudaStream_t s = ctx->stream;
   const hsr::DeviceTreeInfo &ti = ctx->tree.info();
-  const int64_t ntab = n + ti.nodes;
+  const int64_t ntab = n + ti.nodes * ctx->last_tdpts;
   const size_t sn = size_t((std::max<int64_t>(n, 1) + 63) & ~int64_t(63));
   const size_t st_ = size_t((std::max<int64_t>(ntab, 1) + 63) & ~int64_t(63));
-  const size_t sa = size_t(std::max<int64_t>(ti.nodes, 1)) * 3;
-  // cotangent (caller order) | cotangent (tree order) | xbar table (3 x ntab) | node acc
-  CU(ctx->d_adj.ensure((6 * sn + 3 * st_ + sa + 64) * 4), "cudaMalloc(adjoint)");
+  const size_t sa = (size_t(std::max<int64_t>(ti.nodes, 1)) * 4 + 63) & ~size_t(63);
+  // cotangent (caller order) | cotangent (tree order) | xbar table (3 x ntab) |
+  // mass cotangents (ntab, 12-point pseudo-particles) | per node: xc and tdr
+  // cotangents | error flag
+  CU(ctx->d_adj.ensure((6 * sn + 4 * st_ + sa + 64) * 4), "cudaMalloc(adjoint)");
   float *ub = ctx->d_adj.as<float>();
   float *ut = ub + 3 * sn;
   float *xb = ut + 3 * sn;
-  float *acc = xb + 3 * st_;
+  float *mbar = xb + 3 * st_;
+  float *xcbar = mbar + st_;
+  float *tdrbar = xcbar + 3 * std::max<int64_t>(ti.nodes, 1);
+  float *acc = xcbar + sa;
   const float *uin[3] = {dvbx, dvby, dvbz};
   const int32_t *perm = ctx->tree.perm();
   for (int d = 0; d < 3; ++d) {
@@ -1320,20 +1328,27 @@ hsr_status hsr_force_vjp(hsr_ctx *ctx, const float *dvbx, const float *dvby, con
     }
     CU(hsr::launch_gather_f32(src, perm, ut + d * sn, n, s), "gather cotangent");
   }
-  CU(cudaMemsetAsync(xb, 0, 3 * st_ * 4, s), "zero xbar");
+  CU(cudaMemsetAsync(xb, 0, (quad ? 4 : 3) * st_ * 4, s), "zero xbar");
   CU(ctx->d_queue.ensure(64), "cudaMalloc(queue)");
   CU(cudaMemsetAsync(ctx->d_queue.p, 0, 2 * sizeof(unsigned long long), s), "reset queue");
   if (ctx->batched_ctas == 0) ctx->batched_ctas = hsr::batched_resident_ctas(ctx->device);
   CU(cudaEventRecord(ctx->ev0, s), "event");
   CU(hsr::launch_pairs_vjp(w.law, w.table, w.items, w.nitems, w.gidx, w.idx, ut, ut + sn, ut + 2 * sn,
                            xb, xb + st_, xb + 2 * st_, w.fcoeff, w.rsm2, w.rc2, w.rcull2,
-                           ctx->d_queue.as<unsigned long long>(), ctx->batched_ctas, s),
+                           ctx->d_queue.as<unsigned long long>(), ctx->batched_ctas, s,
+                           quad ? mbar : nullptr, n),
      "adjoint kernel");
   int32_t *aerr = reinterpret_cast<int32_t *>(acc);
   CU(cudaMemsetAsync(aerr, 0, sizeof(int32_t), s), "reset flag");
-  CU(hsr::launch_pseudo_adjoint(ctx->tree.nodes(), ctx->tree.levels(), w.table, n, xb, xb + st_,
-                                xb + 2 * st_, aerr, s),
-     "pseudo-particle adjoint");
+  if (quad)
+    CU(hsr::launch_pseudo_adjoint_quad(ctx->tree.nodes(), ctx->tree.levels(), w.table, n,
+                                       ctx->tape_nd, ctx->tape_ppc, xb, xb + st_, xb + 2 * st_,
+                                       mbar, xcbar, tdrbar, aerr, s),
+       "pseudo-particle adjoint");
+  else
+    CU(hsr::launch_pseudo_adjoint(ctx->tree.nodes(), ctx->tree.levels(), w.table, n, xb, xb + st_,
+                                  xb + 2 * st_, aerr, s),
+       "pseudo-particle adjoint");
   CU(cudaEventRecord(ctx->ev1, s), "event");
   float *outs[3] = {xbx, xby, xbz};
   for (int d = 0; d < 3; ++d) {

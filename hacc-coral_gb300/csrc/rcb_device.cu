@@ -2954,6 +2954,208 @@ __global__ void k_adj_paths(const DNode *__restrict__ nodes, int32_t nnodes,
   }
 }
 
+// ---------------------------------------------------------------------------
+// Adjoint of the 12-point pseudo-particles (RCBForceTree.cxx:519-568,
+// :786-799, :855-889).  A node's point a sits at p_a = xc + tdr e_a and has
+// the mass ppm_a = sum_s m_s f_a(y_s - xc, tdr) over its sources s (its
+// particles, or each child's particles or points), in exact arithmetic
+//   f_a(d, tdr) = 1/K + (3/K) (d.e_a)/tdr + (5/(2K)) (3 (d.e_a)^2 - |d|^2)/tdr^2
+// (1/K alone for tdr = 0); tdr = ppc x (the least distance from xc to a face
+// of the node's box) and xc the node's centre of mass.  Given the cotangents
+// of every point's position (xbar) and mass (mbar), the nodes are taken top
+// down: each passes its points' cotangents to its sources (a child's points
+// before that child is taken), to its xc and to its tdr; the tdr cotangent
+// then goes to the particle on the face pptdr took, and every xc cotangent to
+// the node's particles (m_i / M).
+// ---------------------------------------------------------------------------
+constexpr int kQuad = 12;
+
+// A warp per node of level [lb, le).
+__global__ void k_quad_adj_level(const DNode *__restrict__ nodes, int32_t lb, int32_t le,
+                                 const float4 *__restrict__ table, int64_t n, int32_t nd,
+                                 float *xbx, float *xby, float *xbz, float *mb, float *xcbar,
+                                 float *tdrbar) {
+  __shared__ float sx[8][kQuad][4];  // per warp: the node's points' cotangents (x, y, z, m)
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int32_t t = lb + int32_t((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  if (t >= le) return;  // whole warps
+  const DNode &T = nodes[t];
+  const int32_t c = T.count;
+  const bool leaf = T.cl == 0 && T.cr == 0;
+  // no points used (a node of at most 12 particles is listed by its
+  // particles), or a leaf left by a failed split (massless points, no sources)
+  if (c <= kQuad || (leaf && c > nd)) return;
+  const int64_t pb = n + int64_t(kQuad) * t;
+  if (lane < kQuad) {
+    sx[w][lane][0] = xbx[pb + lane];
+    sx[w][lane][1] = xby[pb + lane];
+    sx[w][lane][2] = xbz[pb + lane];
+    sx[w][lane][3] = mb[pb + lane];
+  }
+  __syncwarp();
+  const float xc0 = T.xc[0], xc1 = T.xc[1], xc2 = T.xc[2], tdr = T.tdr;
+  const float K = float(kQuad);
+  float gx = 0.f, gy = 0.f, gz = 0.f, gt = 0.f;  // xc and tdr cotangents
+  // p_a = xc + tdr e_a
+  if (lane < kQuad) {
+    const float ax = sx[w][lane][0], ay = sx[w][lane][1], az = sx[w][lane][2];
+    gx += ax;
+    gy += ay;
+    gz += az;
+    gt += ax * c_design[lane][0] + ay * c_design[lane][1] + az * c_design[lane][2];
+  }
+  // one source at table index j: its cotangents, and its share of xc's and tdr's
+  auto source = [&](int64_t j, bool point) {
+    const float4 y = table[j];
+    const float dx = y.x - xc0, dy = y.y - xc1, dz = y.z - xc2;
+    float fx = 0.f, fy = 0.f, fz = 0.f, ft = 0.f, fm = 0.f;
+    if (tdr == 0.f) {
+      for (int a = 0; a < kQuad; ++a) fm += sx[w][a][3];
+      fm *= 1.f / K;
+    } else {
+      const float it = 1.f / tdr, it2 = it * it;
+      const float d2 = dx * dx + dy * dy + dz * dz;
+      for (int a = 0; a < kQuad; ++a) {
+        const float ex = c_design[a][0], ey = c_design[a][1], ez = c_design[a][2];
+        const float M = sx[w][a][3];
+        const float q = dx * ex + dy * ey + dz * ez;
+        const float p2 = 3.f * q * q - d2;
+        fm += M * (1.f / K + (3.f / K) * q * it + (2.5f / K) * p2 * it2);
+        // d f / d d = (3/K) e / tdr + (5/(2K)) (6 q e - 2 d) / tdr^2
+        const float ce = M * ((3.f / K) * it + (15.f / K) * q * it2);
+        const float cd = -M * (5.f / K) * it2;
+        fx += ce * ex + cd * dx;
+        fy += ce * ey + cd * dy;
+        fz += ce * ez + cd * dz;
+        // d f / d tdr = -(3/K) q / tdr^2 - (5/K) (3 q^2 - |d|^2) / tdr^3
+        ft -= M * ((3.f / K) * q * it2 + (5.f / K) * p2 * it2 * it);
+      }
+    }
+    const float m = y.w;
+    xbx[j] += m * fx;
+    xby[j] += m * fy;
+    xbz[j] += m * fz;
+    gx -= m * fx;
+    gy -= m * fy;
+    gz -= m * fz;
+    gt += m * ft;
+    if (point) mb[j] += fm;
+  };
+  if (leaf) {
+    for (int32_t s = lane; s < c; s += 32) source(T.offset + s, false);
+  } else {
+    for (int side = 0; side < 2; ++side) {
+      const int32_t ch = side == 0 ? T.cl : T.cr;
+      if (ch <= 0) continue;
+      const DNode &C = nodes[ch];
+      if (C.count <= 0) continue;
+      if (C.count <= kQuad) {
+        for (int32_t s = lane; s < C.count; s += 32) source(C.offset + s, false);
+      } else if (lane < kQuad) {
+        source(n + int64_t(kQuad) * ch + lane, true);
+      }
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) {
+    gx += __shfl_xor_sync(0xffffffffu, gx, o);
+    gy += __shfl_xor_sync(0xffffffffu, gy, o);
+    gz += __shfl_xor_sync(0xffffffffu, gz, o);
+    gt += __shfl_xor_sync(0xffffffffu, gt, o);
+  }
+  if (lane == 0) {
+    xcbar[3 * int64_t(t) + 0] = gx;
+    xcbar[3 * int64_t(t) + 1] = gy;
+    xcbar[3 * int64_t(t) + 2] = gz;
+    tdrbar[t] = gt;
+  }
+}
+
+// A block per node: tdr = ppc (x_max,d - xc_d) or ppc (xc_d - x_min,d), the
+// face pptdr takes (its float expression, ties to the earlier face); the
+// cotangent goes to the first particle of the node on that face and to xc.
+__global__ void k_quad_adj_tdr(const DNode *__restrict__ nodes, int32_t nnodes,
+                               const float4 *__restrict__ table, float ppc, float *xbx, float *xby,
+                               float *xbz, float *xcbar, const float *tdrbar) {
+  __shared__ int32_t best;
+  const int32_t t = blockIdx.x;
+  if (t >= nnodes) return;
+  const float tb = tdrbar[t];
+  const DNode &T = nodes[t];
+  if (tb == 0.f || T.count <= 0) return;
+  float cand[6];
+  for (int d = 0; d < 3; ++d) {
+    cand[d] = fsub_(T.xmax[d], T.xc[d]);
+    cand[3 + d] = fsub_(T.xc[d], T.xmin[d]);
+  }
+  const float v = smin_(cand[0], smin_(cand[1], smin_(cand[2], smin_(cand[3],
+                                                                   smin_(cand[4], cand[5])))));
+  int face = 5;
+  for (int j = 5; j >= 0; --j)
+    if (cand[j] == v) face = j;
+  const int d = face % 3;
+  const float target = face < 3 ? T.xmax[d] : T.xmin[d];
+  if (threadIdx.x == 0) best = INT32_MAX;
+  __syncthreads();
+  for (int32_t i = threadIdx.x; i < T.count; i += blockDim.x) {
+    const float4 p = table[T.offset + i];
+    const float x = d == 0 ? p.x : (d == 1 ? p.y : p.z);
+    if (x == target) atomicMin(&best, i);
+  }
+  __syncthreads();
+  if (threadIdx.x != 0 || best == INT32_MAX) return;
+  const float g = ppc * tb;
+  const int64_t k = T.offset + best;
+  float *xb = d == 0 ? xbx : (d == 1 ? xby : xbz);
+  atomicAdd(xb + k, face < 3 ? g : -g);
+  xcbar[3 * int64_t(t) + d] += face < 3 ? -g : g;
+}
+
+// A warp per leaf: xbar_k += m_k sum over the nodes P on the leaf's
+// root-to-leaf path of xcbar_P / M_P, M_P the node's mass (the sum of its
+// points' masses, which is the sum of its particles' masses).
+__global__ void k_quad_adj_paths(const DNode *__restrict__ nodes, int32_t nnodes,
+                                 const float4 *__restrict__ table, int64_t n, float *xbx,
+                                 float *xby, float *xbz, const float *xcbar, int32_t *err) {
+  const int32_t leaf = int32_t((int64_t(blockIdx.x) * blockDim.x + threadIdx.x) >> 5);
+  const int lane = threadIdx.x & 31;
+  if (leaf >= nnodes) return;  // whole warps
+  const DNode &L = nodes[leaf];
+  if (L.cl != 0 || L.cr != 0 || L.count <= 0) return;
+  const int32_t lo = L.offset;
+  float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+  int32_t t = 0;
+  for (int depth = 0;; ++depth) {
+    const float b0 = xcbar[3 * int64_t(t)], b1 = xcbar[3 * int64_t(t) + 1],
+                b2 = xcbar[3 * int64_t(t) + 2];
+    if (b0 != 0.f || b1 != 0.f || b2 != 0.f) {
+      // the node's mass: lane a < 12 reads point a, summed over the warp
+      float m = lane < kQuad ? table[n + int64_t(kQuad) * t + lane].w : 0.f;
+      for (int o = 16; o > 0; o >>= 1) m += __shfl_xor_sync(0xffffffffu, m, o);
+      if (m != 0.f) {
+        a0 += b0 / m;
+        a1 += b1 / m;
+        a2 += b2 / m;
+      }
+    }
+    if (t == leaf) break;
+    const DNode &T = nodes[t];
+    const int32_t c = lo < T.offset + T.nleft ? T.cl : T.cr;
+    if (c <= 0 || c >= nnodes || depth > 256) {  // cannot happen in a valid tree
+      if (lane == 0) atomicExch(err, 5);
+      return;
+    }
+    t = c;
+  }
+  if (a0 == 0.f && a1 == 0.f && a2 == 0.f) return;
+  for (int32_t i = lane; i < L.count; i += 32) {
+    const int32_t k = L.offset + i;
+    const float m = table[k].w;
+    xbx[k] += m * a0;
+    xby[k] += m * a1;
+    xbz[k] += m * a2;
+  }
+}
+
 __global__ void k_iota(int32_t *p, int64_t n) {
   for (int64_t i = int64_t(blockIdx.x) * blockDim.x + threadIdx.x; i < n;
        i += int64_t(gridDim.x) * blockDim.x)
@@ -3558,6 +3760,29 @@ cudaError_t launch_pseudo_adjoint(const DNode *nodes, const std::vector<int32_t>
   if (nnodes <= 0) return cudaSuccess;
   k_adj_paths<<<unsigned((int64_t(nnodes) * 32 + 255) / 256), 256, 0, s>>>(nodes, nnodes, table, n,
                                                                            xbx, xby, xbz, err);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_pseudo_adjoint_quad(const DNode *nodes, const std::vector<int32_t> &levels,
+                                       const float4 *table, int64_t n, int32_t nd, float ppc,
+                                       float *xbx, float *xby, float *xbz, float *mb, float *xcbar,
+                                       float *tdrbar, int32_t *err, cudaStream_t s) {
+  if (levels.size() < 2) return cudaSuccess;
+  const int32_t nnodes = levels.back();
+  if (nnodes <= 0) return cudaSuccess;
+  cudaError_t e = cudaMemsetAsync(xcbar, 0, size_t(nnodes) * 3 * sizeof(float), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(tdrbar, 0, size_t(nnodes) * sizeof(float), s);
+  if (e != cudaSuccess) return e;
+  for (size_t l = 0; l + 1 < levels.size(); ++l) {
+    const int32_t lb = levels[l], le = levels[l + 1];
+    if (le > lb)
+      k_quad_adj_level<<<unsigned((int64_t(le - lb) * 32 + 255) / 256), 256, 0, s>>>(
+          nodes, lb, le, table, n, nd, xbx, xby, xbz, mb, xcbar, tdrbar);
+  }
+  k_quad_adj_tdr<<<unsigned(nnodes), 256, 0, s>>>(nodes, nnodes, table, ppc, xbx, xby, xbz, xcbar,
+                                                  tdrbar);
+  k_quad_adj_paths<<<unsigned((int64_t(nnodes) * 32 + 255) / 256), 256, 0, s>>>(
+      nodes, nnodes, table, n, xbx, xby, xbz, xcbar, err);
   return cudaGetLastError();
 }
 

@@ -215,6 +215,15 @@ cudaError_t launch_scatter_add_f32(const float *in, const int32_t *perm, float *
 cudaError_t launch_pseudo_adjoint(const DNode *nodes, const std::vector<int32_t> &levels,
                                   const float4 *table, int64_t n, float *xbx, float *xby,
                                   float *xbz, int32_t *err, cudaStream_t s);
+// The same for 12-point pseudo-particles: the points' position cotangents
+// (slots n + 12 P + a of xbx/xby/xbz) and mass cotangents (mb, same slots)
+// passed to the particles through every node's sources, centre of mass and
+// tdr, top down.  xcbar (3 per node) and tdrbar (1 per node) are scratch;
+// nd and ppc as the tree was built with.
+cudaError_t launch_pseudo_adjoint_quad(const DNode *nodes, const std::vector<int32_t> &levels,
+                                       const float4 *table, int64_t n, int32_t nd, float ppc,
+                                       float *xbx, float *xby, float *xbz, float *mb, float *xcbar,
+                                       float *tdrbar, int32_t *err, cudaStream_t s);
 
 // Exclusive prefix sum of n int64 values (in may equal out); *total (device,
 // may be null) receives the sum.  tmp needs scan_tmp_size(n) elements.

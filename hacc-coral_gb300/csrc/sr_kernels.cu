@@ -484,15 +484,23 @@ constexpr int kVjpWarpFloats = 3 * kVjpRowsH * kVjpRowH > 3 * kVjpRows * kVjpRow
                                    ? 3 * kVjpRowsH * kVjpRowH
                                    : 3 * kVjpRows * kVjpRow;
 constexpr size_t kVjpSmem = size_t(kBatchedWarps) * kVjpWarpFloats * sizeof(float);
+// with mass cotangents (12-point pseudo-particles): a fourth component row
+constexpr int kVjpComp = kVjpRowsH * kVjpRowH > kVjpRows * kVjpRow ? kVjpRowsH * kVjpRowH
+                                                                    : kVjpRows * kVjpRow;
+constexpr int kVjpWarpFloatsMB = 4 * kVjpComp;
+constexpr size_t kVjpSmemMB = size_t(kBatchedWarps) * kVjpWarpFloatsMB * sizeof(float);
 
-template <int LAW, bool MULTI>
+// MB: also the mass cotangent of every pseudo-particle entry (table index >=
+// npart) into mb_ (the 12-point pseudo-particles' masses depend on positions).
+template <int LAW, bool MULTI, bool MB = false>
 __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
     k_pairs_vjp(const float4 *__restrict__ pos_, const PairItem *__restrict__ items, int64_t nitems,
                 const int32_t *__restrict__ gidx_, const int32_t *__restrict__ idx_,
                 const float *__restrict__ ux_, const float *__restrict__ uy_,
                 const float *__restrict__ uz_, float *__restrict__ xbx_, float *__restrict__ xby_,
                 float *__restrict__ xbz_, float fcoeff_, float rsm2_, float rcut2_, float rcull2_,
-                unsigned long long *__restrict__ queue, const VjpBoxDesc *__restrict__ boxes) {
+                unsigned long long *__restrict__ queue, const VjpBoxDesc *__restrict__ boxes,
+                float *__restrict__ mb_ = nullptr, int64_t npart = 0) {
   // kept entries, two per slot pair as in k_pairs_batched: (x, x', y, y'),
   // (z, z', m, m') and their table indices
   __shared__ float4 bufA[kBatchedWarps][33], bufB[kBatchedWarps][33];
@@ -506,7 +514,9 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
   const unsigned below = (1u << lane) - 1u;
   float *const fa = reinterpret_cast<float *>(bufA[w]);
   float *const fb = reinterpret_cast<float *>(bufB[w]);
-  float *const tv = reinterpret_cast<float *>(vjp_rows) + size_t(w) * kVjpWarpFloats;
+  float *const tv =
+      reinterpret_cast<float *>(vjp_rows) + size_t(w) * (MB ? kVjpWarpFloatsMB : kVjpWarpFloats);
+  constexpr int NC = MB ? 4 : 3;  // components summed per entry
   for (;;) {
     unsigned long long it = 0;
     if (lane == 0) it = atomicAdd(queue, 1ull);
@@ -618,7 +628,7 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
       }
       __syncwarp();
       // v of slot pair q's two entries against this lane's particle
-      auto eval_pair = [&](int q, float2 &vx, float2 &vy, float2 &vz) {
+      auto eval_pair = [&](int q, float2 &vx, float2 &vy, float2 &vz, float2 &mb2) {
         const float4 A = bufA[w][q], B = bufB[w][q];
         const int ja = bufI[w][2 * q], jb = bufI[w][2 * q + 1];
         const float2 ex = __fadd2_rn(make_float2(A.x, A.y), nxi);
@@ -627,8 +637,8 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
         const float2 r2 = __ffma2_rn(ex, ex, __ffma2_rn(ey, ey, __fmul2_rn(ez, ez)));
         const bool on_a = act && ja != pi && in_range<LAW>(r2.x, rcut2);
         const bool on_b = act && jb != pi && in_range<LAW>(r2.y, rcut2);
-        vjp2_term<LAW>(ex, ey, ez, __fmul2_rn(wi2, make_float2(B.z, B.w)), ua, ub, uc, rsm2,
-                       on_a, on_b, vx, vy, vz);
+        vjp2_term<LAW, MB>(ex, ey, ez, __fmul2_rn(wi2, make_float2(B.z, B.w)), ua, ub, uc, rsm2,
+                           on_a, on_b, vx, vy, vz, wi2, &mb2);
         bx = __fadd2_rn(bx, vx);
         by = __fadd2_rn(by, vy);
         bz = __fadd2_rn(bz, vz);
@@ -638,8 +648,8 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
         // pairs, half 1 the odd ones
         const int nq = (ne + 1) / 2;
         for (int q = half; q < nq; q += 2) {
-          float2 vx, vy, vz;
-          eval_pair(q, vx, vy, vz);
+          float2 vx, vy, vz, mb2;
+          eval_pair(q, vx, vy, vz, mb2);
           float *row = tv + (2 * q) * kVjpRowH + gl;
           row[0] = vx.x;
           row[kVjpRowH] = vx.y;
@@ -647,6 +657,10 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
           row[(kVjpRowsH + 1) * kVjpRowH] = vy.y;
           row[2 * kVjpRowsH * kVjpRowH] = vz.x;
           row[(2 * kVjpRowsH + 1) * kVjpRowH] = vz.y;
+          if (MB) {
+            row[3 * kVjpRowsH * kVjpRowH] = mb2.x;
+            row[(3 * kVjpRowsH + 1) * kVjpRowH] = mb2.y;
+          }
         }
         __syncwarp();
         // entry side: lane e sums entry e's row of each component; rows start
@@ -654,10 +668,10 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
         // take the row's 16-byte pieces rotated by one, which puts a quarter-
         // warp's 8 loads on 32 distinct banks
         if (lane < ne) {
-          float sum[3];
+          float sum[NC];
           const int rot = (lane >> 2) & 1;
 #pragma unroll
-          for (int c = 0; c < 3; ++c) {
+          for (int c = 0; c < NC; ++c) {
             const float4 *row =
                 reinterpret_cast<const float4 *>(tv + (c * kVjpRowsH + lane) * kVjpRowH);
             float2 s2 = make_float2(0.f, 0.f);
@@ -674,6 +688,7 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
             atomicAdd(xby + jt, sum[1]);
             atomicAdd(xbz + jt, sum[2]);
           }
+          if (MB && jt >= npart && sum[NC - 1] != 0.f) atomicAdd(mb_ + jt, sum[NC - 1]);
         }
         __syncwarp();
       }
@@ -681,8 +696,8 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
         // entries 16h .. 16h + 15 of the buffer
         const int q1 = min(8 * h + 8, (ne + 1) / 2);
         for (int q = 8 * h; q < q1; ++q) {
-          float2 vx, vy, vz;
-          eval_pair(q, vx, vy, vz);
+          float2 vx, vy, vz, mb2;
+          eval_pair(q, vx, vy, vz, mb2);
           float *row = tv + (2 * q - 16 * h) * kVjpRow + lane;
           row[0] = vx.x;
           row[kVjpRow] = vx.y;
@@ -690,14 +705,18 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
           row[(kVjpRows + 1) * kVjpRow] = vy.y;
           row[2 * kVjpRows * kVjpRow] = vz.x;
           row[(2 * kVjpRows + 1) * kVjpRow] = vz.y;
+          if (MB) {
+            row[3 * kVjpRows * kVjpRow] = mb2.x;
+            row[(3 * kVjpRows + 1) * kVjpRow] = mb2.y;
+          }
         }
         __syncwarp();
         // entry side: lanes r and r + 16 sum the two halves of entry 16h + r's
         // row of each component
         const int er = lane & 15, e = 16 * h + er, part = lane >> 4;
-        float sum[3];
+        float sum[NC];
 #pragma unroll
-        for (int c = 0; c < 3; ++c) {
+        for (int c = 0; c < NC; ++c) {
           const float4 *row =
               reinterpret_cast<const float4 *>(tv + (c * kVjpRows + er) * kVjpRow) + 4 * part;
           float2 s2 = make_float2(0.f, 0.f);
@@ -716,6 +735,7 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
             atomicAdd(xby + jt, sum[1]);
             atomicAdd(xbz + jt, sum[2]);
           }
+          if (MB && jt >= npart && sum[NC - 1] != 0.f) atomicAdd(mb_ + jt, sum[NC - 1]);
         }
         __syncwarp();
       }
@@ -748,18 +768,19 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
 namespace {
 // Shared memory opt-in and resident CTAs of one VJP instantiation (cached
 // per device).
-template <int LAW, bool MULTI>
+template <int LAW, bool MULTI, bool MB = false>
 int vjp_ctas(int64_t nitems) {
   constexpr int kDev = 64;
+  constexpr size_t smem = MB ? kVjpSmemMB : kVjpSmem;
   static int per[kDev] = {};
   int dev = 0;
   cudaGetDevice(&dev);
   int pc = dev >= 0 && dev < kDev ? per[dev] : 0;
   if (pc == 0) {
-    cudaFuncSetAttribute(k_pairs_vjp<LAW, MULTI>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         int(kVjpSmem));
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pc, k_pairs_vjp<LAW, MULTI>, 32 * kBatchedWarps,
-                                                  kVjpSmem);
+    cudaFuncSetAttribute(k_pairs_vjp<LAW, MULTI, MB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         int(smem));
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&pc, k_pairs_vjp<LAW, MULTI, MB>,
+                                                  32 * kBatchedWarps, smem);
     if (pc < 1) pc = 1;
     if (dev >= 0 && dev < kDev) per[dev] = pc;
   }
@@ -767,25 +788,39 @@ int vjp_ctas(int64_t nitems) {
   const int64_t need = (nitems + kBatchedWarps - 1) / kBatchedWarps;
   return int(ctas < need ? ctas : need);
 }
+
+template <int LAW>
+void vjp_single(const float4 *pos, const PairItem *items, int64_t nitems, const int32_t *gidx,
+                const int32_t *idx, const float *ux, const float *uy, const float *uz, float *xbx,
+                float *xby, float *xbz, float fcoeff, float rsm2, float rcut2, float rcull2,
+                unsigned long long *queue, float *mb, int64_t npart, cudaStream_t s) {
+  if (mb)
+    k_pairs_vjp<LAW, false, true>
+        <<<vjp_ctas<LAW, false, true>(nitems), 32 * kBatchedWarps, kVjpSmemMB, s>>>(
+            pos, items, nitems, gidx, idx, ux, uy, uz, xbx, xby, xbz, fcoeff, rsm2, rcut2, rcull2,
+            queue, nullptr, mb, npart);
+  else
+    k_pairs_vjp<LAW, false>
+        <<<vjp_ctas<LAW, false>(nitems), 32 * kBatchedWarps, kVjpSmem, s>>>(
+            pos, items, nitems, gidx, idx, ux, uy, uz, xbx, xby, xbz, fcoeff, rsm2, rcut2, rcull2,
+            queue, nullptr);
+}
 }  // namespace
 
 cudaError_t launch_pairs_vjp(int law, const float4 *pos, const PairItem *items, int64_t nitems,
                              const int32_t *gidx, const int32_t *idx, const float *ux,
                              const float *uy, const float *uz, float *xbx, float *xby, float *xbz,
                              float fcoeff, float rsm2, float rcut2, float rcull2,
-                             unsigned long long *queue, int ctas, cudaStream_t s) {
+                             unsigned long long *queue, int ctas, cudaStream_t s, float *mb,
+                             int64_t npart) {
   (void)ctas;  // the VJP kernel's own occupancy sets its grid
   if (nitems <= 0) return cudaSuccess;
   if (law == LAW_POLY5_STEP16)
-    k_pairs_vjp<LAW_POLY5_STEP16, false>
-        <<<vjp_ctas<LAW_POLY5_STEP16, false>(nitems), 32 * kBatchedWarps, kVjpSmem, s>>>(
-            pos, items, nitems, gidx, idx, ux, uy, uz, xbx, xby, xbz, fcoeff, rsm2, rcut2, rcull2,
-            queue, nullptr);
+    vjp_single<LAW_POLY5_STEP16>(pos, items, nitems, gidx, idx, ux, uy, uz, xbx, xby, xbz, fcoeff,
+                                 rsm2, rcut2, rcull2, queue, mb, npart, s);
   else
-    k_pairs_vjp<LAW_POLY6, false>
-        <<<vjp_ctas<LAW_POLY6, false>(nitems), 32 * kBatchedWarps, kVjpSmem, s>>>(
-            pos, items, nitems, gidx, idx, ux, uy, uz, xbx, xby, xbz, fcoeff, rsm2, rcut2, rcull2,
-            queue, nullptr);
+    vjp_single<LAW_POLY6>(pos, items, nitems, gidx, idx, ux, uy, uz, xbx, xby, xbz, fcoeff, rsm2,
+                          rcut2, rcull2, queue, mb, npart, s);
   return cudaGetLastError();
 }
 

@@ -284,10 +284,14 @@ __device__ __forceinline__ float2 neg_dpoly2_x2<LAW_POLY5_STEP16>(float2 r2) {
 // The adjoint pair term for two pairs at once: with e = x_j - x_i,
 // M = w (g I + 2 g' e e^T), w = w_i m_j, returns M u (u: particle i's
 // cotangent), zero where `on` is false.  Packed FP32 as pair2_acc_s.
-template <int LAW>
+// With MB, *mb also receives the mass cotangent of the two entries,
+// d (u . dv_i) / d m_j = w_i g (d . u) (wi: fcoeff m_i, or fcoeff for Step16).
+template <int LAW, bool MB = false>
 __device__ __forceinline__ void vjp2_term(float2 ex, float2 ey, float2 ez, float2 w, float2 u0,
                                           float2 u1, float2 u2, float rsm2, bool on_a, bool on_b,
-                                          float2 &vx, float2 &vy, float2 &vz) {
+                                          float2 &vx, float2 &vy, float2 &vz,
+                                          float2 wi = make_float2(0.f, 0.f),
+                                          float2 *mb = nullptr) {
   const float2 r2 = __ffma2_rn(ex, ex, __ffma2_rn(ey, ey, __fmul2_rn(ez, ez)));
   const float2 s = __fadd2_rn(r2, make_float2(rsm2, rsm2));
   const float2 y = make_float2(rsqrt_ftz(s.x), rsqrt_ftz(s.y));
@@ -306,6 +310,12 @@ __device__ __forceinline__ void vjp2_term(float2 ex, float2 ey, float2 ez, float
   vx = __ffma2_rn(a, u0, __fmul2_rn(bq, ex));
   vy = __ffma2_rn(a, u1, __fmul2_rn(bq, ey));
   vz = __ffma2_rn(a, u2, __fmul2_rn(bq, ez));
+  if (MB) {
+    float2 t = __fmul2_rn(__fmul2_rn(wi, g), du);
+    t.x = on_a ? t.x : 0.f;
+    t.y = on_b ? t.y : 0.f;
+    *mb = t;
+  }
 }
 
 // One pair: accumulates m_j g(r2) d into (ax, ay, az).
@@ -364,12 +374,15 @@ int batched_resident_ctas(int device);
 // Vector-Jacobian product of the kick dv_i = fcoeff m_i sum_j m_j g(r2) d_ij
 // with respect to positions, over the same work items: for cotangent u (tree
 // order, 3 x n), adds (d dv / d x)^T u into xbar (3 arrays of ntab entries:
-// particles, then pseudo-particle slots).  Self entries are skipped.
+// particles, then pseudo-particle slots).  Self entries are skipped.  With mb
+// (ntab floats), also adds d (u . dv) / d m_j for every table entry j >= npart
+// (the 12-point pseudo-particles' masses).
 cudaError_t launch_pairs_vjp(int law, const float4 *pos, const PairItem *items, int64_t nitems,
                              const int32_t *gidx, const int32_t *idx, const float *ux,
                              const float *uy, const float *uz, float *xbx, float *xby, float *xbz,
                              float fcoeff, float rsm2, float rcut2, float rcull2,
-                             unsigned long long *queue, int ctas, cudaStream_t s);
+                             unsigned long long *queue, int ctas, cudaStream_t s,
+                             float *mb = nullptr, int64_t npart = 0);
 // launch_pairs_vjp over the items of several boxes (items of box b carry
 // b << 8 in flags), one persistent launch; queue as above.
 cudaError_t launch_pairs_vjp_multi(int law, const VjpBoxDesc *boxes, const PairItem *items,

@@ -333,9 +333,12 @@ hsr_status hsr_stream(hsr_ctx *ctx, int64_t n, float *x, float *y, float *z, con
  * hsr_force_fwd, caller's order, with the tree and the lists held fixed (they
  * are piecewise constant in the positions).  A monopole pseudo-particle sits
  * at its node's centre of mass, so its gradient passes on to the node's
- * particles with weights m_k / M_node.  The cutoff is a step: its delta
- * contribution is not included.  HSR_ERR_STATE without a forward;
- * HSR_ERR_UNSUPPORTED for 12-point pseudo-particles (tdpts = 12). */
+ * particles with weights m_k / M_node.  12-point pseudo-particles
+ * (RCBForceTree.cxx:519-568): their positions and masses depend on the
+ * node's sources, centre of mass and tdr; the gradient passes through all of
+ * them, top down (tdr's to the particle on the box face it is measured to).
+ * The cutoff is a step: its delta contribution is not included.
+ * HSR_ERR_STATE without a forward. */
 hsr_status hsr_force_vjp(hsr_ctx *ctx, const float *dvbx, const float *dvby, const float *dvbz,
                          float *xbx, float *xby, float *xbz, int32_t mem);
 

@@ -115,7 +115,10 @@ def test_vjp_is_linear_in_the_cotangent(ctx):
 
 
 @pytest.mark.gpu
-def test_vjp_call_order_and_quadrupole_are_reported():
+def test_vjp_call_order_is_reported():
+    """hsr_force_vjp without a forward: HSR_ERR_STATE; after a 12-point
+    forward it runs (its accuracy: tests/test_quad_adjoint.py), linear in the
+    cotangent (zero for zero)."""
     with hsr.Context(0) as c:
         with pytest.raises(hsr.HsrError) as e:
             c.force_vjp(np.zeros((4, 3), np.float32))
@@ -123,6 +126,5 @@ def test_vjp_call_order_and_quadrupole_are_reported():
         p = synth.zeldovich_box(12, seed=1)
         kp = synth.kick_params(p, nd=32, tdpts=12)
         c.force_fwd(p.x, p.y, p.z, p.mass, kp)
-        with pytest.raises(hsr.HsrError) as e:
-            c.force_vjp(np.zeros((p.n, 3), np.float32))
-        assert e.value.status == 5
+        xb = c.force_vjp(np.zeros((p.n, 3), np.float32))
+        assert np.all(xb == 0)

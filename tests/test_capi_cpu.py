@@ -30,6 +30,14 @@ def test_header_declares_functions():
     assert len(header_functions()) >= 10
 
 
+def test_library_binds_every_symbol_at_load(hsr_lib):
+    """The library loads with every symbol bound at once (no symbol of its
+    own left undefined by a definition in the wrong namespace)."""
+    import ctypes
+    import os
+    ctypes.CDLL(hsr.LIB_PATH, mode=os.RTLD_NOW | os.RTLD_LOCAL)
+
+
 @pytest.mark.parametrize("name", header_functions())
 def test_library_exports(hsr_lib, name):
     assert hasattr(hsr_lib, name), f"{name} declared in include/ but not exported"
