@@ -1,7 +1,9 @@
 """The adjoint with 12-point (quadrupole) pseudo-particles against FP64.
 
 A 16^3 Zel'dovich lattice at z = 10 with overload ghosts, nd = 32, opening
-angle 0.5 (many pseudo-particle entries), fcoeff = 1.  The checker
+angle 1.0, fcoeff = 1: 15 % of the 50 600 list entries are 12-point
+pseudo-particles (at opening angle 0.5 a node opened within the cutoff holds
+fewer than 12 particles at this density, so the lists hold particles only).  The checker
 (oracle/quad64.py) restates the kick with its pseudo-particles in float64 as a
 function of the particle positions, the tree, the lists and the cutoff mask
 frozen (and the particles that attain each node's box extremes): it must
@@ -26,7 +28,7 @@ ADJ_TOL = 1e-4
 
 def _box():
     p = synth.zeldovich_box(16, z=10.0, seed=4)
-    kp = synth.kick_params(p, nd=32, tdpts=12, open_angle=0.5, fcoeff=1.0)
+    kp = synth.kick_params(p, nd=32, tdpts=12, open_angle=1.0, fcoeff=1.0)
     return p, kp
 
 
@@ -78,18 +80,19 @@ def test_quad_vjp_matches_fp64_differences(ctx):
     h = 1e-4
     gnorm = np.linalg.norm(xt)
     # directional derivatives over all particles; with the pseudo-particles
-    # held constant the differences miss by far more than the tolerance, so
-    # the check covers their chain rule
+    # held constant the differences move by several times the VJP's error, so
+    # the check resolves their chain rule
     tab0 = M.table(x0)
-    miss = 0.0
+    miss, errs = 0.0, []
     for _ in range(4):
         D = rng.standard_normal((n, 3))
         D /= np.linalg.norm(D)
         fd = (M.loss(x0 + h * D, ut) - M.loss(x0 - h * D, ut)) / (2 * h)
-        assert abs((xt * D).sum() - fd) <= ADJ_TOL * gnorm, ((xt * D).sum(), fd, gnorm)
+        errs.append(abs((xt * D).sum() - fd))
+        assert errs[-1] <= ADJ_TOL * gnorm, ((xt * D).sum(), fd, gnorm)
         fd0 = (M.loss(x0 + h * D, ut, tab0) - M.loss(x0 - h * D, ut, tab0)) / (2 * h)
         miss = max(miss, abs(fd0 - fd))
-    assert miss >= 10 * ADJ_TOL * gnorm, (miss, gnorm)
+    assert miss >= 5 * max(errs), (miss, errs, gnorm)
     # particles, axis by axis
     inleaf = np.concatenate([np.arange(o, o + c) for o, c in zip(off, cnt)])
     smp = rng.choice(inleaf, 8, replace=False)
