@@ -173,7 +173,8 @@ struct BoxState {
   bool plain = false;
   // the box's kick parameters (a multi-box forward's tape, for its adjoint)
   int law = 0, tdpts = 1;
-  float fcoeff = 0, rsm2 = 0, rc2 = 0, rcull2 = 0;
+  int32_t nd = 0;
+  float fcoeff = 0, rsm2 = 0, rc2 = 0, rcull2 = 0, ppc = 0;
   // the box's own stream: boxes of a batch are prepared concurrently
   cudaStream_t stream = nullptr;
   cudaEvent_t done = nullptr;
@@ -1816,6 +1817,8 @@ hsr_status force_batch_impl(hsr_ctx *ctx, int32_t nbox, const hsr_params *params
 #undef BCU
     B.law = p->law;
     B.tdpts = p->tdpts;
+    B.nd = int32_t(std::min<int64_t>(p->nd, INT32_MAX));
+    B.ppc = p->ppc;
     B.fcoeff = p->fcoeff;
     B.rsm2 = p->rsm * p->rsm;
     B.rc2 = cut2(p->law, p->fsrrmax);
@@ -1961,24 +1964,36 @@ hsr_status hsr_force_vjp_batch(hsr_ctx *ctx, int32_t nbox, const float *const *d
   if (mem != HSR_MEM_HOST && mem != HSR_MEM_DEVICE) return ctx->fail(HSR_ERR_ARG, "bad memory kind");
   for (int32_t b = 0; b < nbox; ++b) {
     const BoxState &B = *ctx->boxes[b];
-    if (B.tdpts != 1)
-      return ctx->fail(HSR_ERR_UNSUPPORTED, "the adjoint takes monopole pseudo-particles (tdpts = 1)");
     if (B.n > 0 && (!dvbx[b] || !dvby[b] || !dvbz[b] || !xbx[b] || !xby[b] || !xbz[b]))
       return ctx->fail(HSR_ERR_ARG, "null array");
   }
   CU(cudaSetDevice(ctx->device), "cudaSetDevice");
   cudaStream_t s = ctx->stream;
   std::vector<hsr::VjpBoxDesc> desc(static_cast<size_t>(nbox));
+  bool any_quad = false;
+  // per box: cotangent (caller order, host input) | cotangent (tree order) |
+  // xbar table | mass cotangents (12-point boxes) | per node: xc and tdr
+  // cotangents | error flag
+  struct AdjLayout {
+    size_t sn, st, sa;
+  };
+  auto layout = [](const BoxState &B) {
+    const hsr::DeviceTreeInfo &ti = B.tree.info();
+    const int64_t ntab = B.n + ti.nodes * B.tdpts;
+    AdjLayout L;
+    L.sn = size_t((std::max<int64_t>(B.n, 1) + 63) & ~int64_t(63));
+    L.st = size_t((std::max<int64_t>(ntab, 1) + 63) & ~int64_t(63));
+    L.sa = (size_t(std::max<int64_t>(ti.nodes, 1)) * 4 + 63) & ~size_t(63);
+    return L;
+  };
   for (int32_t b = 0; b < nbox; ++b) {
     BoxState &B = *ctx->boxes[b];
     const int64_t n = B.n;
-    const hsr::DeviceTreeInfo &ti = B.tree.info();
-    const int64_t ntab = n + ti.nodes;
-    const size_t sn = size_t((std::max<int64_t>(n, 1) + 63) & ~int64_t(63));
-    const size_t st_ = size_t((std::max<int64_t>(ntab, 1) + 63) & ~int64_t(63));
-    const size_t sa = size_t(std::max<int64_t>(ti.nodes, 1)) * 3;
-    // cotangent (caller order, host input) | cotangent (tree order) | xbar table | node acc
-    CU(B.adj.ensure((6 * sn + 3 * st_ + sa + 64) * 4), "cudaMalloc(adjoint)");
+    const bool quad = B.tdpts == 12;
+    any_quad = any_quad || quad;
+    const AdjLayout AL = layout(B);
+    const size_t sn = AL.sn, st_ = AL.st;
+    CU(B.adj.ensure((6 * sn + 4 * st_ + AL.sa + 64) * 4), "cudaMalloc(adjoint)");
     float *ub = B.adj.as<float>();
     float *ut = ub + 3 * sn;
     float *xb = ut + 3 * sn;
@@ -1992,8 +2007,10 @@ hsr_status hsr_force_vjp_batch(hsr_ctx *ctx, int32_t nbox, const float *const *d
       }
       CU(hsr::launch_gather_f32(src, B.tree.perm(), ut + d * sn, n, s), "gather cotangent");
     }
-    CU(cudaMemsetAsync(xb, 0, 3 * st_ * 4, s), "zero xbar");
+    CU(cudaMemsetAsync(xb, 0, (quad ? 4 : 3) * st_ * 4, s), "zero xbar");
     hsr::VjpBoxDesc &D = desc[b];
+    D.mb = quad ? xb + 3 * st_ : nullptr;
+    D.npart = n;
     D.table = B.tree.table();
     D.idx = B.tree.index();
     D.gidx = B.tree.gidx();
@@ -2017,24 +2034,31 @@ hsr_status hsr_force_vjp_batch(hsr_ctx *ctx, int32_t nbox, const float *const *d
   CU(cudaEventRecord(ctx->ev0, s), "event");
   CU(hsr::launch_pairs_vjp_multi(ctx->boxes[0]->law, ctx->d_vjp_desc.as<hsr::VjpBoxDesc>(),
                                  ctx->d_box_items.as<hsr::PairItem>(), ctx->batch_items,
-                                 ctx->d_queue.as<unsigned long long>(), ctx->batched_ctas, s),
+                                 ctx->d_queue.as<unsigned long long>(), ctx->batched_ctas, s,
+                                 any_quad),
      "multi-box adjoint kernel");
   CU(cudaEventRecord(ctx->ev1, s), "event");
   std::vector<int32_t *> aerrs;
   for (int32_t b = 0; b < nbox; ++b) {
     BoxState &B = *ctx->boxes[b];
     const int64_t n = B.n;
-    const hsr::DeviceTreeInfo &ti = B.tree.info();
-    const int64_t ntab = n + ti.nodes;
-    const size_t sn = size_t((std::max<int64_t>(n, 1) + 63) & ~int64_t(63));
-    const size_t st_ = size_t((std::max<int64_t>(ntab, 1) + 63) & ~int64_t(63));
+    const AdjLayout AL = layout(B);
+    const size_t sn = AL.sn, st_ = AL.st;
     float *ub = B.adj.as<float>();
     float *xb = ub + 6 * sn;
-    int32_t *aerr = reinterpret_cast<int32_t *>(xb + 3 * st_);
+    float *mbar = xb + 3 * st_, *xcbar = mbar + st_;
+    float *tdrbar = xcbar + 3 * std::max<int64_t>(B.tree.info().nodes, 1);
+    int32_t *aerr = reinterpret_cast<int32_t *>(xcbar + AL.sa);
     CU(cudaMemsetAsync(aerr, 0, sizeof(int32_t), s), "reset flag");
-    CU(hsr::launch_pseudo_adjoint(B.tree.nodes(), B.tree.levels(), B.tree.table(), n, xb, xb + st_,
-                                  xb + 2 * st_, aerr, s),
-       "pseudo-particle adjoint");
+    if (B.tdpts == 12)
+      CU(hsr::launch_pseudo_adjoint_quad(B.tree.nodes(), B.tree.levels(), B.tree.table(), n, B.nd,
+                                         B.ppc, xb, xb + st_, xb + 2 * st_, mbar, xcbar, tdrbar,
+                                         aerr, s),
+         "pseudo-particle adjoint");
+    else
+      CU(hsr::launch_pseudo_adjoint(B.tree.nodes(), B.tree.levels(), B.tree.table(), n, xb,
+                                    xb + st_, xb + 2 * st_, aerr, s),
+         "pseudo-particle adjoint");
     aerrs.push_back(aerr);
     float *outs[3] = {xbx[b], xby[b], xbz[b]};
     for (int d = 0; d < 3; ++d) {

@@ -2135,7 +2135,18 @@ __global__ void k_children(DNode *nodes, int32_t nb, int32_t ne, const int64_t *
 // ---------------------------------------------------------------------------
 // Pseudo-particles (RCBForceTree.cxx:519-569, 788-800, 856-889)
 // ---------------------------------------------------------------------------
-__constant__ float c_design[12][3];
+// The 12-point design (RCBForceTree.cxx:227-272): the icosahedron's vertices
+// (0, +-b, +-a) and their cyclic permutations, a = 0.525731112119134,
+// b = 0.85065080835204, in the reference's order.  Fixed: every tree reads
+// it, whatever its point count (a monopole's one point sits at xc, offset 0).
+#define HSR_IA 0.525731112119134f
+#define HSR_IB 0.85065080835204f
+__constant__ float c_design[12][3] = {
+    {0, HSR_IB, HSR_IA},   {0, HSR_IB, -HSR_IA},  {HSR_IA, 0, HSR_IB},   {-HSR_IA, 0, HSR_IB},
+    {HSR_IB, HSR_IA, 0},   {-HSR_IB, HSR_IA, 0},  {0, -HSR_IB, -HSR_IA}, {0, -HSR_IB, HSR_IA},
+    {-HSR_IA, 0, -HSR_IB}, {HSR_IA, 0, -HSR_IB},  {-HSR_IB, -HSR_IA, 0}, {HSR_IB, -HSR_IA, 0}};
+#undef HSR_IA
+#undef HSR_IB
 
 __device__ __forceinline__ float pptdr_(const DNode &t) {
   return smin_(fsub_(t.xmax[0], t.xc[0]),
@@ -2148,9 +2159,11 @@ __device__ __forceinline__ float pptdr_(const DNode &t) {
 __device__ __forceinline__ void pppts_(int k, float tdr, const float *xc, float *px, float *py,
                                        float *pz) {
   for (int i = 0; i < k; ++i) {
-    px[i] = fadd_(fmul_(tdr, c_design[i][0]), xc[0]);
-    py[i] = fadd_(fmul_(tdr, c_design[i][1]), xc[1]);
-    pz[i] = fadd_(fmul_(tdr, c_design[i][2]), xc[2]);
+    const float ex = k == 12 ? c_design[i][0] : 0.f, ey = k == 12 ? c_design[i][1] : 0.f,
+                ez = k == 12 ? c_design[i][2] : 0.f;
+    px[i] = fadd_(fmul_(tdr, ex), xc[0]);
+    py[i] = fadd_(fmul_(tdr, ey), xc[1]);
+    pz[i] = fadd_(fmul_(tdr, ez), xc[2]);
   }
 }
 
@@ -3253,16 +3266,6 @@ cudaError_t DeviceTree::build(const TreeConfig &cfg, int64_t n, const float4 *po
   }
   const auto t0 = std::chrono::steady_clock::now();
   const int k = cfg.tdpts;
-  {
-    float d[12][3];
-    static const float ia = 0.525731112119134f, ib = 0.85065080835204f;
-    const float ico[12][3] = {{0, ib, ia},   {0, ib, -ia},  {ia, 0, ib},   {-ia, 0, ib},
-                              {ib, ia, 0},   {-ib, ia, 0},  {0, -ib, -ia}, {0, -ib, ia},
-                              {-ia, 0, -ib}, {ia, 0, -ib},  {-ib, -ia, 0}, {ib, -ia, 0}};
-    std::memset(d, 0, sizeof(d));
-    if (k == 12) std::memcpy(d, ico, sizeof(d));
-    DT_CHECK(cudaMemcpyToSymbolAsync(c_design, d, sizeof(d), 0, cudaMemcpyHostToDevice, s));
-  }
   const size_t nn = size_t(std::max<int64_t>(n, 1));
   n_ = n;
   DT_CHECK(grow(tight_chunks_, cap_tc_,

@@ -528,8 +528,12 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
     const float *ux = ux_, *uy = uy_, *uz = uz_;
     float *xbx = xbx_, *xby = xby_, *xbz = xbz_;
     float fcoeff = fcoeff_, rsm2 = rsm2_, rcut2 = rcut2_, rcull2 = rcull2_;
+    float *mbp = mb_;
+    int64_t np = npart;
     if (MULTI) {
       const VjpBoxDesc &B = boxes[W.flags >> 8];
+      mbp = B.mb;
+      np = B.npart;
       pos = B.table;
       gidx = B.gidx;
       idx = B.idx;
@@ -688,7 +692,7 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
             atomicAdd(xby + jt, sum[1]);
             atomicAdd(xbz + jt, sum[2]);
           }
-          if (MB && jt >= npart && sum[NC - 1] != 0.f) atomicAdd(mb_ + jt, sum[NC - 1]);
+          if (MB && mbp && jt >= np && sum[NC - 1] != 0.f) atomicAdd(mbp + jt, sum[NC - 1]);
         }
         __syncwarp();
       }
@@ -735,7 +739,7 @@ __global__ void __launch_bounds__(32 * kBatchedWarps, 2)
             atomicAdd(xby + jt, sum[1]);
             atomicAdd(xbz + jt, sum[2]);
           }
-          if (MB && jt >= npart && sum[NC - 1] != 0.f) atomicAdd(mb_ + jt, sum[NC - 1]);
+          if (MB && mbp && jt >= np && sum[NC - 1] != 0.f) atomicAdd(mbp + jt, sum[NC - 1]);
         }
         __syncwarp();
       }
@@ -826,19 +830,21 @@ cudaError_t launch_pairs_vjp(int law, const float4 *pos, const PairItem *items, 
 
 cudaError_t launch_pairs_vjp_multi(int law, const VjpBoxDesc *boxes, const PairItem *items,
                                    int64_t nitems, unsigned long long *queue, int ctas,
-                                   cudaStream_t s) {
+                                   cudaStream_t s, bool mass_cotangents) {
   (void)ctas;
   if (nitems <= 0) return cudaSuccess;
-  if (law == LAW_POLY5_STEP16)
-    k_pairs_vjp<LAW_POLY5_STEP16, true>
-        <<<vjp_ctas<LAW_POLY5_STEP16, true>(nitems), 32 * kBatchedWarps, kVjpSmem, s>>>(
-            nullptr, items, nitems, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
-            nullptr, 0.f, 0.f, 0.f, 0.f, queue, boxes);
-  else
-    k_pairs_vjp<LAW_POLY6, true>
-        <<<vjp_ctas<LAW_POLY6, true>(nitems), 32 * kBatchedWarps, kVjpSmem, s>>>(
-            nullptr, items, nitems, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
-            nullptr, 0.f, 0.f, 0.f, 0.f, queue, boxes);
+#define VJP_MULTI(L, MBV, SMEM)                                                                 \
+  k_pairs_vjp<L, true, MBV><<<vjp_ctas<L, true, MBV>(nitems), 32 * kBatchedWarps, SMEM, s>>>(  \
+      nullptr, items, nitems, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,   \
+      nullptr, 0.f, 0.f, 0.f, 0.f, queue, boxes)
+  if (law == LAW_POLY5_STEP16) {
+    if (mass_cotangents) VJP_MULTI(LAW_POLY5_STEP16, true, kVjpSmemMB);
+    else VJP_MULTI(LAW_POLY5_STEP16, false, kVjpSmem);
+  } else {
+    if (mass_cotangents) VJP_MULTI(LAW_POLY6, true, kVjpSmemMB);
+    else VJP_MULTI(LAW_POLY6, false, kVjpSmem);
+  }
+#undef VJP_MULTI
   return cudaGetLastError();
 }
 

@@ -82,6 +82,8 @@ struct alignas(16) VjpBoxDesc {
   const float *ux, *uy, *uz;
   float *xbx, *xby, *xbz;
   float fcoeff, rsm2, rcut2, rcull2;
+  float *mb;      // 12-point boxes: the pseudo-particles' mass cotangents, else null
+  int64_t npart;  // the box's particles (table entries below are not pseudo-particles)
 };
 
 // LawS of a law with softening rsm and strict cutoff rcut2 on r2.
@@ -387,7 +389,7 @@ cudaError_t launch_pairs_vjp(int law, const float4 *pos, const PairItem *items, 
 // b << 8 in flags), one persistent launch; queue as above.
 cudaError_t launch_pairs_vjp_multi(int law, const VjpBoxDesc *boxes, const PairItem *items,
                                    int64_t nitems, unsigned long long *queue, int ctas,
-                                   cudaStream_t s);
+                                   cudaStream_t s, bool mass_cotangents = false);
 cudaError_t launch_force_law(int law, const float *r2, float *g, int64_t n, float rsm2, float rcut2,
                              cudaStream_t s);
 

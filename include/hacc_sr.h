@@ -313,8 +313,8 @@ hsr_status hsr_force_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *pa
  * xbar_b = (d dv_b / d x_b)^T dvbar_b over the tape of the last multi-box
  * forward (nbox must equal its box count), caller's order, the VJP of all
  * boxes in one persistent launch.  As hsr_force_vjp: trees, lists and the
- * cutoff held fixed; HSR_ERR_STATE without a multi-box forward;
- * HSR_ERR_UNSUPPORTED for 12-point pseudo-particles. */
+ * cutoff held fixed, monopole or 12-point pseudo-particles per box;
+ * HSR_ERR_STATE without a multi-box forward. */
 hsr_status hsr_force_vjp_batch(hsr_ctx *ctx, int32_t nbox, const float *const *dvbx,
                                const float *const *dvby, const float *const *dvbz,
                                float *const *xbx, float *const *xby, float *const *xbz,

@@ -106,3 +106,33 @@ def test_quad_vjp_matches_fp64_differences(ctx):
     scale = np.maximum(np.linalg.norm(fd, axis=1), rms_g)
     err = np.linalg.norm(xt[smp] - fd, axis=1) / scale
     assert err.max() <= ADJ_TOL, (err, scale)
+
+
+@pytest.mark.gpu
+def test_multibox_vjp_with_a_12_point_box_equals_single_box_vjps(ctx):
+    """One multi-box forward and VJP over a 12-point box and a monopole box
+    gives each box's single-box VJP (FP32 summation order aside)."""
+    torch = pytest.importorskip("torch")
+    from hsr_testutil import force_errors
+    boxes = [synth.zeldovich_box(16, z=10.0, seed=4), synth.zeldovich_box(12, z=10.0, seed=6)]
+    kps = [synth.kick_params(boxes[0], nd=32, tdpts=12, open_angle=1.0, fcoeff=1.0),
+           synth.kick_params(boxes[1], nd=32, open_angle=1.5, fcoeff=1.0)]
+    rng = np.random.default_rng(21)
+    us = [rng.standard_normal((b.n, 3)).astype(np.float32) for b in boxes]
+    single = []
+    for b, kp, u in zip(boxes, kps, us):
+        ctx.force_fwd(b.x, b.y, b.z, b.mass, kp)
+        single.append(ctx.force_vjp(u))
+    dev = lambda a: torch.tensor(np.ascontiguousarray(a), device="cuda")
+    xs = [tuple(dev(getattr(b, k)) for k in ("x", "y", "z")) for b in boxes]
+    ms = [dev(b.mass) for b in boxes]
+    dvs = [tuple(torch.zeros(b.n, device="cuda") for _ in range(3)) for b in boxes]
+    ctx.force_fwd_batch_device(xs, ms, dvs, kps)
+    ud = [tuple(dev(u[:, d]) for d in range(3)) for u in us]
+    xb = [tuple(torch.zeros(b.n, device="cuda") for _ in range(3)) for b in boxes]
+    ctx.force_vjp_batch_device(ud, xb)
+    torch.cuda.synchronize()
+    for k in range(2):
+        got = np.stack([t.cpu().numpy() for t in xb[k]], 1).astype(np.float64)
+        rms, mx = force_errors(got, single[k].astype(np.float64))
+        assert rms <= 1e-5 and mx <= 1e-3, (k, rms, mx)
