@@ -601,10 +601,19 @@ def main():
     if args.multibox > 0:
         boxes = [synth.zeldovich_box(96, z=50.0, seed=100 + b) for b in range(args.multibox)]
         kpb = [synth.kick_params(b, nd=args.nd) for b in boxes]
-        ctx.rcb_kick_batch([b.copy() for b in boxes], kpb)
-        t0 = time.perf_counter()
-        stb = ctx.rcb_kick_batch([b.copy() for b in boxes], kpb)
-        wall_b = time.perf_counter() - t0
+        # pinned host arrays, refilled outside the timed calls (as the
+        # single-box end-to-end kick)
+        qb = [pinned_copy(b) for b in boxes]
+        walls = []
+        for r in range(3 + max(3, args.steps // 2)):
+            for q, b in zip(qb, boxes):
+                refill(q, b)
+            t0 = time.perf_counter()
+            stb = ctx.rcb_kick_batch(qb, kpb)
+            if r >= 3:
+                walls.append(time.perf_counter() - t0)
+        wall_b = float(np.median(walls))
+        del qb
         ms_b = ctx.bench_pairs(max(3, args.steps // 2))
         ms_bg = ctx.bench_pairs_graph(max(3, args.steps // 2))
         multibox = {"boxes": args.multibox, "n_side": 96, "pairs": stb["pairs"],

@@ -1595,11 +1595,9 @@ hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *para
     D.rcull2 = cull2(D.rcut2);
     D.law = hsr::make_law_s(p->law, D.rsm2, D.rcut2);
   };
-  // Concurrent builds share only the pseudo-particle design table (constant
-  // memory, written with each build): boxes of one tdpts may overlap.
-  bool same_tdpts = true;
-  for (int32_t b = 1; b < nbox; ++b) same_tdpts &= params[b].tdpts == params[0].tdpts;
-  const int nthreads = same_tdpts ? int(std::min<int32_t>(nbox, kBatchThreads)) : 1;
+  // Concurrent builds share no device state (the pseudo-particle design is a
+  // read-only constant table), so boxes of any tdpts overlap.
+  const int nthreads = int(std::min<int32_t>(nbox, kBatchThreads));
   if (nthreads <= 1) {
     for (int32_t b = 0; b < nbox; ++b) prepare_box(b);
   } else {
@@ -1836,9 +1834,7 @@ hsr_status force_batch_impl(hsr_ctx *ctx, int32_t nbox, const hsr_params *params
     D.rcull2 = B.rcull2;
     D.law = hsr::make_law_s(p->law, D.rsm2, D.rcut2);
   };
-  bool same_tdpts = true;
-  for (int32_t b = 1; b < nbox; ++b) same_tdpts &= params[b].tdpts == params[0].tdpts;
-  const int nthreads = same_tdpts ? int(std::min<int32_t>(nbox, kBatchThreads)) : 1;
+  const int nthreads = int(std::min<int32_t>(nbox, kBatchThreads));
   if (nthreads <= 1) {
     for (int32_t b = 0; b < nbox; ++b) prepare_box(b);
   } else {

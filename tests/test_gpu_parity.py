@@ -350,6 +350,24 @@ def test_batch_of_boxes_equals_separate_kicks(ctx):
     assert ctx.bench_pairs_graph(2, flush_l2=False) > 0
 
 
+def test_batch_of_monopole_and_12_point_boxes_equals_separate_kicks(ctx):
+    """Boxes of 12-point and monopole pseudo-particles in one batch (their
+    trees built concurrently on their own streams) give each box's separate
+    kick bit for bit."""
+    boxes = [synth.zeldovich_box(ng, z=10.0, seed=s) for ng, s in ((16, 4), (20, 7), (16, 8),
+                                                                   (12, 9))]
+    kps = [synth.kick_params(b, nd=32, tdpts=t, open_angle=1.0, fcoeff=1.0)
+           for b, t in zip(boxes, (12, 1, 12, 1))]
+    sep = [b.copy() for b in boxes]
+    for b, kp in zip(sep, kps):
+        ctx.rcb_kick(b, kp)
+    ctx.rcb_kick_batch(boxes, kps)
+    for b, q in zip(boxes, sep):
+        for k in EXACT:
+            assert np.array_equal(getattr(b, k).view(np.uint8), getattr(q, k).view(np.uint8)), k
+        assert np.array_equal(vel(b), vel(q))
+
+
 def test_graph_replay_of_single_kick(ctx):
     p = synth.zeldovich_box(24, seed=5)
     ctx.rcb_kick(p, synth.kick_params(p, nd=64))
