@@ -2,6 +2,7 @@
 include/*.h declares, refuses to run without a device, and its host-side tree
 and interaction lists equal the oracle's exactly."""
 import ctypes as C
+import dataclasses
 import glob
 import os
 import re
@@ -77,14 +78,18 @@ def test_host_tree_permutation_matches_golden(hsr_lib, name):
 
 
 @pytest.mark.parametrize("case", ["zel16_nd32", "zel16_nd16_quad", "zel16_oa05_nd8", "random_nd1",
-                                  "long_chains"])
+                                  "long_chains", "zel16_nd32_rco", "zel16_nd16_quad_rco",
+                                  "clustered16_oa05_nd8_rco"])
 def test_host_lists_equal_oracle_lists(hsr_lib, oracle_lib, case):
+    """The host build (RCB, and the RCO octree where the case says so)
+    against the oracle: permutation, list entries and pair counts exact."""
     if case == "long_chains":
         p = synth.sorted_line(20000)
         kp = synth.kick_params(p, nd=32)
         kp.min_force, kp.max_force = (1.0, 0.0, 0.0), (39.0, 0.5, 0.5)
-    elif case.startswith("zel16"):
-        p = synth.zeldovich_box(16, z=10.0, seed=4)
+    elif case.startswith("zel16") or case.startswith("clustered16"):
+        p = (synth.zeldovich_box(16, z=10.0, seed=4) if case.startswith("zel16")
+             else synth.clustered_box(16, nhalo=20, seed=15))
         nd = int(case.split("nd")[-1].split("_")[0])
         kp = synth.kick_params(p, nd=nd, tdpts=12 if "quad" in case else 1,
                                open_angle=0.5 if "oa05" in case else 0.1)
@@ -92,6 +97,8 @@ def test_host_lists_equal_oracle_lists(hsr_lib, oracle_lib, case):
         p = synth.random_box(600, 8.0, 3)
         kp = synth.kick_params(p, nd=1)
         kp.min_force, kp.max_force = (0.5,) * 3, (7.5,) * 3
+    if case.endswith("_rco"):
+        kp = dataclasses.replace(kp, tree=hsr.TREE_RCO)
     q = p.copy()
     L = hsr.HostLists(p, kp)
     r = oracle_lib.rcb_run(q, kp, keep_lists=True, do_kick=False, nthreads=2)
@@ -102,6 +109,7 @@ def test_host_lists_equal_oracle_lists(hsr_lib, oracle_lib, case):
     assert L.stats["pairs"] == r.stats["pairs"]
     assert L.stats["list_entries"] == r.stats["list_entries"]
     assert same_lists(off, cnt, ptr, e, ooff, ocnt, optr, r.entries())
+    assert L.stats["nodes"] == r.stats["nodes"]
 
 
 def test_host_lists_index_points_at_entries(hsr_lib):
