@@ -600,7 +600,7 @@ __global__ void __launch_bounds__(kChunkThreads, 4)
 }
 
 // Float that the reference's (float)(sx / sm) gives, if the bounds decide it.
-// sx, sm: this build's sums; bx, bm: bounds on |reference sum - this sum|.
+// sx, sm: the sums computed here; bx, bm: bounds on |reference sum - sum here|.
 __device__ bool certify(double sx, double bx, double sm, double bm, float *out) {
   const double xl = sx - bx, xh = sx + bx, ml = sm - bm, mh = sm + bm;
   if (!(ml > 0.0) || !isfinite(xl) || !isfinite(xh) || !isfinite(mh)) return false;

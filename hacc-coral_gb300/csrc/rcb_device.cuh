@@ -184,7 +184,7 @@ class DeviceTree {
   size_t cap_sub_ = 0, cap_sf_ = 0, cap_sh_ = 0, cap_sp_ = 0, cap_st_ = 0;
   int64_t *h_sub_ = nullptr;
   bool sub_attr_ = false;
-  bool sub_off_ = false;  // this build runs every level in the level loop
+  bool sub_off_ = false;  // when set, every level runs in the level loop
 };
 
 // The three velocity components into tree order (out: 3 n floats).

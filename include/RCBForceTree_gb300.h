@@ -117,7 +117,7 @@ class RCBForceTree {
     if (!fl)
       throw std::runtime_error(
           "RCBForceTree (GB300): fl == 0 selects the Newtonian law, which is not the "
-          "short-range path this build implements");
+          "short-range path this library implements");
     hacc_sr_gb300::require_poly6_law(fl, r, "RCBForceTree (GB300)");
     hsr_params p{};
     for (int i = 0; i < 3; ++i) {

@@ -30,7 +30,7 @@ class RCOForceTree {
     if (!fl)
       throw std::runtime_error(
           "RCOForceTree (GB300): fl == 0 selects the Newtonian law, which is not the "
-          "short-range path this build implements");
+          "short-range path this library implements");
     const float rsm = hacc_sr_gb300::law_softening(fl);
     if (!(rsm > 0.f))
       throw std::runtime_error(

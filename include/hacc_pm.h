@@ -100,7 +100,7 @@ hsr_status hsr_pm_get_stats(const hsr_ctx *ctx, hsr_pm_stats *st);
  * (the conjugate spectrum) and the CIC derivative at each depositor.  CIC
  * weights are piecewise linear: the product is the derivative away from cell
  * faces.  Same `mem` rule as hsr_pm_kick for all nine arrays.  No
- * counterpart in the reference (differentiation is new in this build). */
+ * counterpart in the reference (differentiation is new in this library). */
 hsr_status hsr_pm_vjp(hsr_ctx *ctx, const hsr_pm_params *p, int64_t n, const float *x,
                       const float *y, const float *z, const float *vbx, const float *vby,
                       const float *vbz, float *xbx, float *xby, float *xbz, int32_t mem);

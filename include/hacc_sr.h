@@ -97,7 +97,7 @@ typedef struct hsr_params {
  * HACC's -O option (src/cpu/Particles.cxx:1259-1310); its tree and lists are
  * built on the host (hsr_rcb_kick with host arrays, hsr_build_lists), the
  * pairs on the device.  The reference's RCO partition reads past its 7-entry
- * split array (RCOForceTree.cxx:607-608); this build uses the end of the
+ * split array (RCOForceTree.cxx:607-608); this library uses the end of the
  * processed range there, the value that makes the partition valid. */
 enum { HSR_TREE_RCB = 0, HSR_TREE_RCO = 1 };
 
@@ -269,7 +269,7 @@ hsr_status hsr_subcycle(hsr_ctx *ctx, const hsr_subcycle_params *sp, int64_t n, 
  * caller's order.  Keeps the tree, lists and positions on the context as the
  * tape for hsr_force_vjp (any other kick or forward call replaces it).
  * mem: HSR_MEM_HOST or HSR_MEM_DEVICE; the tree is built on the device.
- * No counterpart in the reference (differentiation is new in this build). */
+ * No counterpart in the reference (differentiation is new in this library). */
 hsr_status hsr_force_fwd(hsr_ctx *ctx, const hsr_params *p, int64_t n, const float *x,
                          const float *y, const float *z, const float *mass, float *dvx,
                          float *dvy, float *dvz, int32_t mem);

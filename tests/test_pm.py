@@ -189,7 +189,7 @@ def test_kick_matches_restatement(ctx, prec):
         dv = v[a].astype(np.float64) - (p.vx, p.vy, p.vz)[a]
         dv_o = want[a].astype(np.float64) - (p.vx, p.vy, p.vz)[a]
         rms, mx = _err(dv, dv_o)
-        # velocities carry float32 rounding of v + dv: judge dv against
+        # velocities carry float32 rounding of v + dv: compare dv against
         # that rounding too
         ulp = np.spacing(np.abs((p.vx, p.vy, p.vz)[a])).max()
         assert rms < rt + ulp / np.sqrt(np.mean(dv_o ** 2)), (a, rms)
