@@ -243,7 +243,7 @@ def cpu_baseline(p, kp, slab: float, threads: int):
             "seconds": dt, "pairs": pairs, "_out": q}
 
 
-# ---- accuracy of every result: the oracle and FP64 as checkers ----------
+# ---- accuracy of every result: against the oracle and FP64 --------------
 
 EXACT = ("x", "y", "z", "mass", "phi", "id", "mask")
 ACC_NOTE = ("rms = sqrt(sum |a - ref|^2 / sum |ref|^2), max = max_i |a_i - ref_i| / rms |ref| "

@@ -131,7 +131,7 @@ class MultiStep:
     kps: one synth.KickParams per box (fcoeff is replaced per PM step).
     on_tape(box, step, sub, ctx, x), if set, runs in the reverse pass right
     after each kick's tape is recorded at its positions x.  One box at a time,
-    `ctx` then holds that kick's tree and lists (the FP64 checkers in the
+    `ctx` then holds that kick's tree and lists (the FP64 references in the
     tests read them there); in lockstep `ctx` is None (the tape is the
     multi-box one) and a hook that needs a box's tree builds it on a context
     of its own from x (the tree and lists are a function of the positions).

@@ -1,7 +1,7 @@
 /*
  * hsr_oracle.c -- CPU restatement of HACC's RCBForceTree short-range hot path.
  *
- * TEST INFRASTRUCTURE ONLY: the checker for the GPU build and the CPU baseline
+ * TEST INFRASTRUCTURE ONLY: the oracle of the GPU library and the CPU baseline
  * it is timed beside.  Never linked into or called by the product library.
  *
  * Floating point: every expression keeps the reference's operation order and

@@ -1,7 +1,7 @@
 /*
  * hsr_oracle.h -- CPU restatement of HACC's RCBForceTree short-range hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker the GPU build is
+ * TEST INFRASTRUCTURE ONLY.  This library is the oracle the GPU library is
  * compared against and the CPU baseline it is timed beside.  It is never
  * linked into, loaded by or called from the product library; only tests/,
  * __graft_entry__.smoke() and bench.py's CPU-baseline leg use it.

@@ -1,4 +1,4 @@
-"""Python access to the CPU checker.
+"""Python access to the CPU oracle.
 
 TEST INFRASTRUCTURE ONLY.  Imported by tests/, __graft_entry__.smoke() and
 bench.py's CPU-baseline leg; never by the product package.
@@ -263,7 +263,7 @@ class Oracle:
                                  near.ctypes.data_as(C.POINTER(C.c_int32)))
         return fd, near.astype(bool)
 
-    # -- FP64 multi-step checker --------------------------------------------
+    # -- FP64 multi-step reference ------------------------------------------
     def kick64(self, pos, m, tape, c, law=LAW_POLY6, rsm=0.1, fsrrmax=3.116326355,
                pos_cut=None):
         """FP64 kick over one tape (tree order): dv (n x 3).  pos_cut: the

@@ -216,7 +216,7 @@ def point_mass_force(ng: int, src, targets) -> np.ndarray:
 
 
 # ---------------------------------------------------------------------------
-# float64 forward and its vector-Jacobian product (checker of hsr_pm_vjp)
+# float64 forward and its vector-Jacobian product (FP64 reference of hsr_pm_vjp)
 # ---------------------------------------------------------------------------
 #
 # The kick is dv_i = fscal tau F(x_i) with F_d(x) = sum_c W(x - c) G_d[img(c)],

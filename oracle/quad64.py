@@ -1,6 +1,6 @@
 """FP64 restatement of the short-range kick with 12-point (quadrupole)
 pseudo-particles as a function of the particle positions, the tree and lists
-frozen: the checker of the quadrupole adjoint.
+frozen: the FP64 reference of the quadrupole adjoint.
 
 TEST INFRASTRUCTURE ONLY (the tests import it; the product never does).
 

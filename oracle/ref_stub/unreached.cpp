@@ -1,10 +1,10 @@
 // unreached.cpp -- link-time stand-ins for the reference functions that
-// Particles.cxx and Domain.cxx reference but the sub-cycle checker
+// Particles.cxx and Domain.cxx reference but the sub-cycle oracle
 // (sub_driver.cpp) never calls: the Barnes-Hut tree (HACC without -R/-O), the
 // restart I/O (MPI-IO) and the MPI Cartesian decomposition queries
 // (Domain::initialize).  Each aborts if it is ever reached.
 //
-// TEST INFRASTRUCTURE ONLY (the checker's recipe in oracle/Makefile).
+// TEST INFRASTRUCTURE ONLY (the oracle's recipe in oracle/Makefile).
 #include <cstddef>
 #include <cstdint>
 #include <cstdio>
@@ -16,7 +16,7 @@
 
 namespace {
 [[noreturn]] void unreached(const char *what) {
-  fprintf(stderr, "sub_driver: %s is outside the sub-cycle checker\n", what);
+  fprintf(stderr, "sub_driver: %s is outside the sub-cycle oracle\n", what);
   abort();
 }
 }  // namespace

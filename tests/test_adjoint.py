@@ -32,7 +32,7 @@ def _tape_arrays(ctx, p_caller, n):
 
 
 def test_vjp_and_fd_oracles_agree_on_cpu(hsr_lib, oracle_lib):
-    """The two FP64 checkers agree with each other (opening angle 0: every
+    """The two FP64 references agree with each other (opening angle 0: every
     entry a particle)."""
     p = synth.random_box(3000, 10.0, 5)
     kp = synth.kick_params(p, nd=16, open_angle=0.0, fcoeff=0.7)

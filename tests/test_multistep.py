@@ -79,7 +79,7 @@ def _check_fd(O, x0, v0, m, steps, nsub, tapes, xbar, vbar, grad, samples, h, rn
 
 
 def test_fp64_multistep_gradient_matches_fd(hsr_lib, oracle_lib):
-    """The FP64 checker itself: its reverse pass against its own central
+    """The FP64 reference itself: its reverse pass against its own central
     differences (host-built trees, opening angle 0)."""
     O = oracle_lib
     p = synth.random_box(1000, 10.0, 11)
@@ -346,7 +346,7 @@ def _check_fd_pm(O, x0, v0, m, steps, nsub, tapes, pm, xbar, vbar, grad, samples
 
 
 def test_fp64_multistep_with_pm_gradient_matches_fd(hsr_lib, oracle_lib):
-    """The FP64 checker with PM kicks opening and closing each step (8^3 PM
+    """The FP64 reference with PM kicks opening and closing each step (8^3 PM
     grid): its reverse pass against its own central differences."""
     O = oracle_lib
     p = synth.random_box(600, 8.0, 21)

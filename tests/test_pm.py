@@ -337,7 +337,7 @@ def dataclasses_replace(obj, **kw):
 # ---------------------------------------------------------------------------
 
 def test_restatement_vjp_matches_fd():
-    """vjp64 (the float64 checker of hsr_pm_vjp) against central differences
+    """vjp64 (the float64 reference of hsr_pm_vjp) against central differences
     of force64, with overload ghosts and a deposit weight gpscal^3 != 1."""
     p = _box(8, seed=3)
     ng, ngo = 8, p.meta["ngo"]

@@ -3,9 +3,10 @@
 A 16^3 Zel'dovich lattice at z = 10 with overload ghosts, nd = 32, opening
 angle 1.0, fcoeff = 1: 15 % of the 50 600 list entries are 12-point
 pseudo-particles (at opening angle 0.5 a node opened within the cutoff holds
-fewer than 12 particles at this density, so the lists hold particles only).  The checker
-(oracle/quad64.py) restates the kick with its pseudo-particles in float64 as a
-function of the particle positions, the tree, the lists and the cutoff mask
+fewer than 12 particles at this density, so the lists hold particles only).
+The FP64 reference (oracle/quad64.py) restates the kick with its
+pseudo-particles in float64 as a function of the particle positions, the tree,
+the lists and the cutoff mask
 frozen (and the particles that attain each node's box extremes): it must
 reproduce the GPU's FP32 forward on the same tape, and its central
 differences (h = 1e-4 grid units) check the GPU's VJP along random
