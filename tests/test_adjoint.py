@@ -1,11 +1,11 @@
 """The adjoint pair hsr_force_fwd / hsr_force_vjp against FP64.
 
-Config 3 of the benchmark set: a 64^3 Zel'dovich lattice at z = 10 with
+The adjoint workload: a 64^3 Zel'dovich lattice at z = 10 with
 overload ghosts, opening angle 0.1, monopole pseudo-particles; a seeded N(0,1)
 cotangent.  The VJP (FP32 on the GPU) is compared with an FP64 analytic VJP
 over the same lists and with FP64 central differences (h = 1e-4 grid units) on
 256 sampled particles.  Tolerance: 1e-4 relative to the larger of the sample's
-gradient norm and the rms gradient, as the benchmark's target states; samples
+gradient norm and the rms gradient (the adjoint's stated target); samples
 with a pair within 2h of the cutoff are skipped (the law steps there).
 """
 import numpy as np
