@@ -147,6 +147,14 @@ void pp_accum(int k, int64_t count, Src src, const float *xc, const float *px,
   }
 }
 
+// fminf / fmaxf of the reference's cm (BGQCM.c:193-198) without the libm
+// call: the non-NaN operand where one is NaN, else the smaller (larger).
+// Where both operands are zeros of either sign the result may carry the other
+// sign than libm's; no split, opening test or sum depends on the sign of a
+// zero bound (they take differences and comparisons of the bounds only).
+inline float bound_min(float a, float b) { return (b < a || a != a) ? b : a; }
+inline float bound_max(float a, float b) { return (b > a || a != a) ? b : a; }
+
 }  // namespace
 
 // ---------------------------------------------------------------------------
@@ -173,25 +181,30 @@ void RcbHost::node_stats(Node &T) {
   const int64_t cnt = T.count;
   const Elem *e = elems_.data() + T.offset;
   double sx = 0, sy = 0, sz = 0, sm = 0;
-  for (int64_t i = 0; i < cnt; ++i) {
-    const Elem &q = e[i];
-    if (i == 0) {
-      T.xmin[0] = T.xmax[0] = q.x;
-      T.xmin[1] = T.xmax[1] = q.y;
-      T.xmin[2] = T.xmax[2] = q.z;
-    } else {
-      T.xmin[0] = std::fmin(T.xmin[0], q.x);
-      T.xmax[0] = std::fmax(T.xmax[0], q.x);
-      T.xmin[1] = std::fmin(T.xmin[1], q.y);
-      T.xmax[1] = std::fmax(T.xmax[1], q.y);
-      T.xmin[2] = std::fmin(T.xmin[2], q.z);
-      T.xmax[2] = std::fmax(T.xmax[2], q.z);
+  if (cnt > 0) {
+    // the bounds stay in registers (as far as the compiler knows, the node
+    // could alias the elements)
+    float x0 = e[0].x, x1 = e[0].x, y0 = e[0].y, y1 = e[0].y, z0 = e[0].z, z1 = e[0].z;
+    for (int64_t i = 0; i < cnt; ++i) {
+      const Elem &q = e[i];
+      x0 = bound_min(x0, q.x);
+      x1 = bound_max(x1, q.x);
+      y0 = bound_min(y0, q.y);
+      y1 = bound_max(y1, q.y);
+      z0 = bound_min(z0, q.z);
+      z1 = bound_max(z1, q.z);
+      const float w = q.m;
+      sx += double(w * q.x);
+      sy += double(w * q.y);
+      sz += double(w * q.z);
+      sm += double(w);
     }
-    const float w = q.m;
-    sx += double(w * q.x);
-    sy += double(w * q.y);
-    sz += double(w * q.z);
-    sm += double(w);
+    T.xmin[0] = x0;
+    T.xmax[0] = x1;
+    T.xmin[1] = y0;
+    T.xmax[1] = y1;
+    T.xmin[2] = z0;
+    T.xmax[2] = z1;
   }
   T.xc[0] = float(sx / sm);
   T.xc[1] = float(sy / sm);

@@ -112,6 +112,30 @@ def test_host_lists_equal_oracle_lists(hsr_lib, oracle_lib, case):
     assert L.stats["nodes"] == r.stats["nodes"]
 
 
+@pytest.mark.parametrize("tdpts,tree", [(1, 0), (12, 0), (1, 1), (12, 1)])
+def test_host_lists_with_signed_zero_coordinates(hsr_lib, oracle_lib, tdpts, tree):
+    """A third of the coordinates on the planes x, y, z = 0 with both signs
+    of zero (the node bounds tie at zeros of either sign): the host build's
+    permutation and lists equal the oracle's bit for bit."""
+    p = synth.random_box(3000, 8.0, 2)
+    rng = np.random.default_rng(102)
+    for a in (p.x, p.y, p.z):
+        sel = rng.random(p.n) < 0.3
+        a[sel] = np.where(rng.random(int(sel.sum())) < 0.5, np.float32(0.0), np.float32(-0.0))
+    kp = synth.kick_params(p, nd=8, tdpts=tdpts, open_angle=0.5)
+    kp.min_force, kp.max_force = (-1.0,) * 3, (7.0,) * 3
+    kp = dataclasses.replace(kp, tree=tree)
+    q = p.copy()
+    L = hsr.HostLists(p, kp)
+    r = oracle_lib.rcb_run(q, kp, keep_lists=True, do_kick=False, nthreads=2)
+    for k in ("x", "y", "z", "mass", "phi", "id", "mask"):
+        assert np.array_equal(getattr(p, k).view(np.uint8), getattr(q, k).view(np.uint8)), k
+    off, cnt, ptr, e = L.get()
+    ooff, ocnt, optr = r.leaves()
+    assert L.stats["pairs"] == r.stats["pairs"]
+    assert same_lists(off, cnt, ptr, e, ooff, ocnt, optr, r.entries())
+
+
 def test_host_lists_index_points_at_entries(hsr_lib):
     p = synth.zeldovich_box(8, seed=2)
     kp = synth.kick_params(p, nd=16)
