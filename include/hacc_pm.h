@@ -76,7 +76,9 @@ typedef struct hsr_pm_stats {
  * component of the solved potential), d = x, y, z, for the n particles.
  * Positions are read only.  mem: HSR_MEM_HOST or HSR_MEM_DEVICE (device
  * pointers on the context's device).  Synchronous.  The plans and the Green's
- * function are made on the first call for an (ng, precision) and kept. */
+ * function are made on the first call for an (ng, precision) and kept.
+ * Replaces map2_poisson_forward + map2_poisson_backward_gradient and the
+ * inverse CIC kick (src/simulation/mc3.cxx:304-374). */
 hsr_status hsr_pm_kick(hsr_ctx *ctx, const hsr_pm_params *p, int64_t n, const float *x,
                        const float *y, const float *z, float *vx, float *vy, float *vz,
                        int32_t mem);
@@ -85,7 +87,9 @@ hsr_status hsr_pm_kick(hsr_ctx *ctx, const hsr_pm_params *p, int64_t n, const fl
  * floats, component-major) of the alive block for these positions, each
  * grid with x the slowest and z the fastest index, like the reference's
  * (i*ng + j)*ng + k.  Either output may be NULL.  Same `mem` rule as
- * hsr_pm_kick, for all five pointers. */
+ * hsr_pm_kick, for all five pointers.  The grids the reference's
+ * map2_poisson_forward and map2_poisson_backward_gradient leave in the
+ * solver (src/simulation/mc3.cxx:304-374). */
 hsr_status hsr_pm_fields(hsr_ctx *ctx, const hsr_pm_params *p, int64_t n, const float *x,
                          const float *y, const float *z, float *rho, float *grad, int32_t mem);
 

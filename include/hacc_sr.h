@@ -132,7 +132,9 @@ typedef struct hsr_stats {
 
 typedef struct hsr_ctx hsr_ctx;
 
-/* Creates a context on CUDA device `device` (its own stream and buffers). */
+/* Creates a context on CUDA device `device` (its own stream and buffers).
+ * No counterpart in the reference (its tree is built per call with no
+ * device state). */
 hsr_status hsr_create(hsr_ctx **ctx, int device);
 hsr_status hsr_destroy(hsr_ctx *ctx);
 /* Message of the last error on this context (static storage, never NULL). */
@@ -146,7 +148,9 @@ const char *hsr_version(void);
  * fcoeff * sum_j m_i m_j g(r2_ij) (x_j - x_i) to v_i for r2_ij < fsrrmax^2.
  * mem: HSR_MEM_HOST (any host memory) or HSR_MEM_DEVICE (device pointers on
  * the context's device; HSR_BUILD_DEVICE only).  Synchronous: the arrays
- * hold the result when the call returns. */
+ * hold the result when the call returns.  Replaces the constructor
+ * RCBForceTree<TDPTS>::RCBForceTree (src/halo_finder/RCBForceTree.h:96-124,
+ * src/halo_finder/RCBForceTree.cxx:336-450). */
 hsr_status hsr_rcb_kick(hsr_ctx *ctx, const hsr_params *p, int64_t n, float *x, float *y,
                         float *z, float *vx, float *vy, float *vz, float *mass, float *phi,
                         int64_t *id, uint16_t *mask, int32_t mem);
@@ -172,7 +176,10 @@ hsr_status hsr_rcb_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *para
  * checks.  hsr_lists_size gives the number of processed leaves and of list
  * entries; hsr_lists_export fills leaf_offset/leaf_count (per leaf, into the
  * permuted arrays), list_ptr (nleaves+1) and the entries as the reference's
- * nx/ny/nz/nm arrays would hold them (any order within a leaf). */
+ * nx/ny/nz/nm arrays would hold them (any order within a leaf).  No call
+ * of the reference returns them: they are the lists calcInternodeForce
+ * builds on its stack (src/halo_finder/RCBForceTree.cxx:923-1144, arrays
+ * declared at :940). */
 hsr_status hsr_lists_size(const hsr_ctx *ctx, int64_t *nleaves, int64_t *nentries);
 hsr_status hsr_lists_export(const hsr_ctx *ctx, int64_t *leaf_offset, int64_t *leaf_count,
                             int64_t *list_ptr, float *ex, float *ey, float *ez, float *em);
@@ -189,12 +196,15 @@ hsr_status hsr_build_lists(const hsr_params *p, int64_t n, float *x, float *y, f
                            float *vx, float *vy, float *vz, float *mass, float *phi, int64_t *id,
                            uint16_t *mask, hsr_lists **out);
 /* nleaves/nentries as hsr_lists_size; stats as hsr_get_stats (no timings of
- * device work). */
+ * device work).  Accessors of hsr_build_lists' result: the lists of
+ * src/halo_finder/RCBForceTree.cxx:923-1144. */
 hsr_status hsr_lists_info(const hsr_lists *L, int64_t *nleaves, int64_t *nentries, hsr_stats *st);
 hsr_status hsr_lists_get(const hsr_lists *L, int64_t *leaf_offset, int64_t *leaf_count,
                          int64_t *list_ptr, float *ex, float *ey, float *ez, float *em);
 /* Position-table index of every entry: < n is a particle (post-permutation
- * index), >= n a pseudo-particle. */
+ * index), >= n a pseudo-particle.  (The list entries of
+ * src/halo_finder/RCBForceTree.cxx:1129-1139 and :1085-1123, named by
+ * where they come from.) */
 hsr_status hsr_lists_index(const hsr_lists *L, int64_t *entry_index);
 hsr_status hsr_lists_free(hsr_lists *L);
 
@@ -230,7 +240,8 @@ hsr_status hsr_get_tune(const hsr_ctx *ctx, hsr_tune *t);
  * context's shape to the fastest.  The launches accumulate into the context's
  * own velocity scratch, never into caller arrays.  Writes min(cap, *nrows)
  * rows; *nrows receives the number of shapes timed.  HSR_ERR_STATE without
- * such a kick. */
+ * such a kick.  No counterpart in the reference (its nbody1 has one fixed
+ * loop shape). */
 hsr_status hsr_autotune(hsr_ctx *ctx, int32_t iters, int32_t flush_l2, hsr_tune_row *rows,
                         int32_t cap, int32_t *nrows);
 
@@ -303,7 +314,8 @@ hsr_status hsr_force_fwd_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *par
 
 /* hsr_force_fwd_batch that adds every box's dv into its (vx, vy, vz) (the
  * caller's order) instead of writing it: one sub-cycle kick of several boxes
- * in one persistent launch, as hsr_force_kick is for one box. */
+ * in one persistent launch, as hsr_force_kick is for one box (one
+ * RCBForceTree kick, src/halo_finder/RCBForceTree.cxx:599-619, per box). */
 hsr_status hsr_force_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *params,
                                 const int64_t *n, const float *const *x, const float *const *y,
                                 const float *const *z, const float *const *mass, float *const *vx,
@@ -314,7 +326,8 @@ hsr_status hsr_force_kick_batch(hsr_ctx *ctx, int32_t nbox, const hsr_params *pa
  * forward (nbox must equal its box count), caller's order, the VJP of all
  * boxes in one persistent launch.  As hsr_force_vjp: trees, lists and the
  * cutoff held fixed, monopole or 12-point pseudo-particles per box;
- * HSR_ERR_STATE without a multi-box forward. */
+ * HSR_ERR_STATE without a multi-box forward.  No counterpart in the
+ * reference (differentiation is new in this library). */
 hsr_status hsr_force_vjp_batch(hsr_ctx *ctx, int32_t nbox, const float *const *dvbx,
                                const float *const *dvby, const float *const *dvbz,
                                float *const *xbx, float *const *xby, float *const *xbz,
@@ -343,25 +356,32 @@ hsr_status hsr_force_vjp(hsr_ctx *ctx, const float *dvbx, const float *dvby, con
                          float *xbx, float *xby, float *xbz, int32_t mem);
 
 /* The tree order of the last kick or forward: position k holds input
- * particle perm[k] (n entries). */
+ * particle perm[k] (n entries): the permutation the reference's partition
+ * applies to the ten arrays in place (src/halo_finder/RCBForceTree.cxx:
+ * 623-672), for callers that keep particles at fixed indices. */
 hsr_status hsr_last_perm(const hsr_ctx *ctx, int64_t *perm);
 
 /* The last tree's nodes (any numbering; children have larger indices than
  * their parents): particle range, children (0 = none), pseudo-particle
  * radius, box and centre of mass (xmin[3], xmax[3], xc[3] per node) and the
  * tdpts pseudo-particle masses per node.  A node's pseudo-particles sit at
- * position-table index n + node * tdpts. */
+ * position-table index n + node * tdpts.  The reference keeps these as its
+ * TreeNode vector (src/halo_finder/RCBForceTree.h:131-147) without an
+ * accessor. */
 hsr_status hsr_tree_size(const hsr_ctx *ctx, int64_t *nnodes);
 hsr_status hsr_tree_export(const hsr_ctx *ctx, int64_t *count, int64_t *offset, int64_t *cl,
                            int64_t *cr, float *tdr, float *bbox9, float *ppm);
 
 /* Position-table index of every list entry of the last kick or forward, in
  * the order of hsr_lists_export (< n: particle in tree order, >= n:
- * pseudo-particle). */
+ * pseudo-particle); the entries of src/halo_finder/RCBForceTree.cxx:
+ * 1085-1139 named by where they come from. */
 hsr_status hsr_lists_export_index(const hsr_ctx *ctx, int64_t *entry_index);
 
 /* ForceLawSR::f_over_r on the device for a batch of r2 values (host arrays),
- * with the kernel's own FP32 arithmetic; for law tests. */
+ * with the kernel's own FP32 arithmetic; for law tests.  Replaces
+ * ForceLawSR::f_over_r over FGridEvalPoly::eval
+ * (src/halo_finder/ForceLaw.cxx:137-141, 187-192). */
 hsr_status hsr_force_law(hsr_ctx *ctx, int32_t law, float rsm, float fsrrmax, int64_t n,
                          const float *r2, float *g);
 
@@ -407,7 +427,8 @@ hsr_status hsr_kick_lists_noalloc(const float *table, int64_t ntab, int64_t n,
  * with the previous one's data in L2.  *ms_per_launch is the mean time.
  * kernel: HSR_KERNEL_PLAIN or the kick's own; HSR_KERNEL_BATCHED after
  * hsr_rcb_kick_batch replays its one multi-box launch.  use_graph != 0 replays
- * the launch sequence (queue reset + kernel) as a captured CUDA graph. */
+ * the launch sequence (queue reset + kernel) as a captured CUDA graph.
+ * Measurement only: no counterpart in the reference. */
 hsr_status hsr_bench_pairs(hsr_ctx *ctx, int32_t kernel, int32_t iters, int32_t flush_l2,
                            double *ms_per_launch);
 hsr_status hsr_bench_pairs_graph(hsr_ctx *ctx, int32_t iters, int32_t flush_l2,
@@ -417,12 +438,15 @@ hsr_status hsr_bench_pairs_graph(hsr_ctx *ctx, int32_t iters, int32_t flush_l2,
  * built on the device whose distance is within the cutoff (r2 < the law's
  * cutoff squared, r2 rounded as the reference's nbody1 computes it): the
  * pairs that contribute, beside hsr_stats.pairs (every listed pair).
- * HSR_ERR_STATE without such a kick. */
+ * HSR_ERR_STATE without such a kick.  Measurement only: the reference's
+ * nbody1 masks these pairs per term (src/halo_finder/RCBForceTree.cxx:
+ * 612-617) without counting them. */
 hsr_status hsr_pairs_in_cutoff(hsr_ctx *ctx, int64_t *count);
 
 /* Measures this device's FP32 FMA throughput with a kernel of independent
  * fused multiply-add chains (2 flops each) on every SM; the roofline
- * denominator of the pair kernels. */
+ * denominator of the pair kernels.  Measurement only: no counterpart in the
+ * reference. */
 hsr_status hsr_probe_fp32_peak(hsr_ctx *ctx, double *tflops);
 
 #ifdef __cplusplus

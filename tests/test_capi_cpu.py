@@ -31,6 +31,20 @@ def test_header_declares_functions():
     assert len(header_functions()) >= 10
 
 
+def test_every_entry_point_names_what_it_replaces():
+    """Each declaration's comment cites the reference (file:line) or says it
+    has no counterpart there."""
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    missing = []
+    for h in sorted(glob.glob(os.path.join(root, "include", "hacc_*.h"))):
+        src = open(h).read()
+        for m in re.finditer(r"/\*((?:(?!\*/).)*)\*/\s*hsr_status\s+(hsr_\w+)\s*\(", src, re.S):
+            doc = re.sub(r"\s*\n\s*\*?\s*", "", m.group(1))
+            if not re.search(r"\.(cxx|c|h|cpp|hpp):\d", doc) and "counterpart" not in doc:
+                missing.append(m.group(2))
+    assert not missing, missing
+
+
 def test_library_binds_every_symbol_at_load(hsr_lib):
     """The library loads with every symbol bound at once (no symbol of its
     own left undefined by a definition in the wrong namespace)."""
